@@ -1,0 +1,193 @@
+/*
+ * gate_gpu.h - C ABI of the GB300 photon-transport path (libgategpu.so).
+ *
+ * One context drives one CUDA device.  Every function returns a status code
+ * (GG_OK on success); on failure gg_last_error() gives the message.  Callers
+ * own every host buffer they pass in; nothing is retained past a call (the
+ * context keeps device copies).  Calls on one context are not re-entrant.
+ *
+ * The functions replace the following reference interfaces (paths relative
+ * to the opengate project):
+ *   gg_create / gg_destroy      SimulationEngine.initialize / close
+ *                               (opengate/engines.py:1721, 1414)
+ *   gg_upload_tables            physics-table build inside G4RunManager::Initialize
+ *                               for physics_list_name="G4EmStandardPhysics"
+ *                               (opengate/physics.py:341-347); the per-material
+ *                               cross sections Geant4 computes internally
+ *   gg_upload_volume            ImageVolume.construct + create_label_image +
+ *                               GateImageNestedParameterisation::ComputeMaterial
+ *                               (opengate/geometry/volumes.py:1050, 1200-1243;
+ *                               core/opengate_core/opengate_lib/GateImageNestedParameterisation.cpp:47-75)
+ *   gg_set_world                world volume (opengate/managers.py:1435 VolumeManager)
+ *   gg_set_source               GateGenericSource::InitializePosition/Direction/Energy
+ *                               (core/opengate_core/opengate_lib/GateGenericSource.cpp:312-664)
+ *   gg_set_voxel_source         GateVoxelSource / GateSPSVoxelsPosDistribution
+ *                               (core/opengate_core/opengate_lib/GateSPSVoxelsPosDistribution.cpp:29-74)
+ *   gg_add_dose_tally           GateDoseActor::InitializeCpp / BeginOfRunAction
+ *                               (core/opengate_core/opengate_lib/GateDoseActor.cpp:100-137)
+ *   gg_run                      GateSourceManager::StartMasterThread -> /run/beamOn
+ *                               (core/opengate_core/opengate_lib/GateSourceManager.cpp:198-244)
+ *                               with GateDoseActor::SteppingAction / ScoreSquaredValue /
+ *                               FlushSquaredValues (GateDoseActor.cpp:180-243, 359-397)
+ *   gg_get_image                DoseActor.EndOfRunActionMasterThread -> fetch_from_cpp_image
+ *                               (opengate/actors/doseactors.py:662-715)
+ *   gg_get_counters             SimulationStatisticsActor counts
+ *                               (core/opengate_core/opengate_lib/GateSimulationStatisticsActor.cpp:53-201)
+ */
+#ifndef GATE_GPU_H
+#define GATE_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define GG_OK 0
+#define GG_ERR_ARG 1
+#define GG_ERR_CUDA 2
+#define GG_ERR_QUEUE_OVERFLOW 3
+#define GG_ERR_TIMEOUT 4
+#define GG_ERR_DOMAIN 5
+#define GG_ERR_STATE 6
+
+/* precision of a context's transport arithmetic */
+#define GG_PREC_F32 32
+#define GG_PREC_F64 64
+
+/* source position types (GenericSource position.type) */
+#define GG_POS_POINT 0
+#define GG_POS_BOX 1
+#define GG_POS_SPHERE 2
+#define GG_POS_DISC 3
+
+/* direction types (GenericSource direction.type) */
+#define GG_DIR_ISO 0
+#define GG_DIR_MOMENTUM 1
+#define GG_DIR_FOCUSED 2
+
+/* energy types (GenericSource energy.type) */
+#define GG_ENE_MONO 0
+#define GG_ENE_LINES 1     /* "spectrum_discrete" */
+#define GG_ENE_HISTOGRAM 2 /* "spectrum_histogram", no interpolation */
+#define GG_ENE_RANGE 3
+
+/* images returned by gg_get_image */
+#define GG_IMG_EDEP 0
+#define GG_IMG_EDEP_SQUARED 1
+
+/* counters returned by gg_get_counters (uint64 slots) */
+#define GG_CNT_HISTORIES 0
+#define GG_CNT_WOODCOCK_STEPS 1 /* tentative collision points inside the image */
+#define GG_CNT_REAL_INTERACTIONS 2
+#define GG_CNT_DEPOSITS 3       /* energy deposits (> 0) inside the image */
+#define GG_CNT_TALLY_ENTRIES 4  /* per-history voxel entries flushed to the tally */
+#define GG_CNT_LIST_OVERFLOWS 5 /* per-history list flushed before the history ended */
+#define GG_CNT_WORLD_STEPS 6
+#define GG_CNT_ESCAPED 7
+#define GG_CNT_SKIPPED 8        /* directions rejected by angular acceptance */
+#define GG_CNT_LOOP_CAPPED 9    /* sampling loops stopped at their iteration cap */
+#define GG_CNT_STACK_OVERFLOW 10
+#define GG_CNT_SECONDARIES 11   /* annihilation photons created */
+#define GG_N_COUNTERS 16
+
+/* Physics tables: see opengate_gb300/tables.py for the contract. */
+typedef struct {
+  int32_t n_e;          /* energy grid points */
+  float ln_emin;        /* ln(E_min / MeV) */
+  float inv_dln;        /* (n_e - 1) / ln(E_max / E_min) */
+  float e_min;          /* MeV, photons below are absorbed locally */
+  float e_max;          /* MeV */
+  int32_t n_comp;
+  const float *sig;      /* [n_comp][n_e] mm^-1 per g/cm3 */
+  const float *cum;      /* [n_comp][3][n_e] Compton, +photo, +Rayleigh */
+  const float *ray_amax; /* [n_comp][n_e] */
+  int32_t n_rinv;
+  const float *ray_inv; /* [n_comp][n_rinv] x^2 in 1/Angstrom^2 */
+  int32_t n_mat;
+  const int32_t *mat_comp; /* [n_mat] */
+  const float *mat_rho;    /* [n_mat] g/cm3 */
+} gg_tables_desc;
+
+/* Voxelised image volume, axis aligned, labels index the material table. */
+typedef struct {
+  int32_t dims[3];          /* nx, ny, nz (x fastest in memory) */
+  double spacing[3];        /* mm */
+  double corner[3];         /* mm, world position of the outer corner of voxel (0,0,0) */
+  const uint16_t *labels;   /* [nz][ny][nx] material index per voxel */
+  const float *majorant;    /* [n_e] mm^-1, >= every label's attenuation */
+} gg_volume_desc;
+
+/* World box (centred at the origin) and its material. */
+typedef struct {
+  double half_size[3]; /* mm */
+  int32_t material;    /* index into the material table */
+} gg_world_desc;
+
+typedef struct {
+  /* position */
+  int32_t pos_type;
+  double translation[3]; /* mm */
+  double rotation[9];    /* row-major, local -> world */
+  double half_size[3];   /* box half sizes, mm */
+  double radius;         /* sphere / disc, mm */
+  /* direction */
+  int32_t dir_type;
+  double theta[2]; /* rad, iso */
+  double phi[2];   /* rad, iso */
+  double momentum[3];
+  double focus[3];
+  /* angular acceptance ("Rejection" policy, "SkipEvents"): the direction is
+     re-sampled until the ray from the vertex crosses one of the boxes */
+  int32_t n_accept;
+  const double *accept_boxes; /* [n_accept][6]: min xyz, max xyz (world, mm) */
+  int32_t max_rejection;
+  /* energy */
+  int32_t ene_type;
+  double mono;          /* MeV */
+  int32_t n_spec;       /* lines: n energies; histogram: n bins */
+  const double *spec_e; /* lines: [n]; histogram: [n+1] edges; MeV */
+  const double *spec_cdf; /* [n], normalised cumulative weights */
+  double e_lo, e_hi;    /* range */
+} gg_source_desc;
+
+typedef struct gg_ctx gg_ctx;
+
+typedef struct {
+  int32_t device;     /* CUDA device ordinal */
+  int32_t precision;  /* GG_PREC_F32 or GG_PREC_F64 */
+  int32_t block_size; /* 0 = default */
+  int32_t blocks_per_sm; /* 0 = default */
+  int32_t chunk;      /* histories a warp claims per queue fetch, 0 = default */
+  int64_t batch;      /* histories per tally batch, 0 = default */
+} gg_device_opts;
+
+int gg_create(const gg_device_opts *opts, gg_ctx **out);
+int gg_destroy(gg_ctx *ctx);
+/* Copies the last error message of ctx (or of the last failed gg_create if
+   ctx is NULL) into buf, always NUL-terminated. */
+int gg_last_error(const gg_ctx *ctx, char *buf, size_t len);
+
+int gg_upload_tables(gg_ctx *ctx, const gg_tables_desc *tables);
+int gg_upload_volume(gg_ctx *ctx, const gg_volume_desc *volume);
+int gg_set_world(gg_ctx *ctx, const gg_world_desc *world);
+int gg_set_source(gg_ctx *ctx, const gg_source_desc *source);
+/* Enables the edep / edep-squared tally on the image grid and zeroes it. */
+int gg_add_dose_tally(gg_ctx *ctx, int32_t score_squared);
+int gg_reset_tally(gg_ctx *ctx);
+/* Simulates histories [first_history, first_history + n) with the given seed
+   and adds them to the tally.  Histories are processed in batches (the
+   context's batch size); the result does not depend on launch parameters. */
+int gg_run(gg_ctx *ctx, uint64_t n_histories, uint64_t seed, uint64_t first_history);
+int gg_synchronize(gg_ctx *ctx);
+int gg_get_image(gg_ctx *ctx, int32_t which, double *out, size_t n);
+int gg_get_counters(gg_ctx *ctx, uint64_t *out, size_t n);
+/* Elapsed device time of the transport kernels of the last gg_run, ms. */
+int gg_last_kernel_ms(gg_ctx *ctx, double *transport_ms, double *flush_ms, int32_t *launches);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GATE_GPU_H */

@@ -1,0 +1,143 @@
+"""ctypes binding of libgategpu.so (declarations in include/gate_gpu.h).
+
+The shared library is built in-tree by ``opengate_gb300.build`` into
+``opengate_gb300/_lib/libgategpu.so``.  Loading fails loudly when it is
+missing: there is no CPU fallback for the transport path.
+"""
+
+import ctypes
+import pathlib
+
+import numpy as np
+
+LIB_DIR = pathlib.Path(__file__).resolve().parent / "_lib"
+LIB_PATH = LIB_DIR / "libgategpu.so"
+
+GG_OK = 0
+GG_ERR_ARG = 1
+GG_ERR_CUDA = 2
+GG_ERR_QUEUE_OVERFLOW = 3
+GG_ERR_TIMEOUT = 4
+GG_ERR_DOMAIN = 5
+GG_ERR_STATE = 6
+STATUS_NAMES = {0: "GG_OK", 1: "GG_ERR_ARG", 2: "GG_ERR_CUDA", 3: "GG_ERR_QUEUE_OVERFLOW",
+                4: "GG_ERR_TIMEOUT", 5: "GG_ERR_DOMAIN", 6: "GG_ERR_STATE"}
+
+GG_PREC_F32 = 32
+GG_PREC_F64 = 64
+GG_POS_POINT, GG_POS_BOX, GG_POS_SPHERE, GG_POS_DISC = 0, 1, 2, 3
+GG_DIR_ISO, GG_DIR_MOMENTUM, GG_DIR_FOCUSED = 0, 1, 2
+GG_ENE_MONO, GG_ENE_LINES, GG_ENE_HISTOGRAM, GG_ENE_RANGE = 0, 1, 2, 3
+GG_IMG_EDEP, GG_IMG_EDEP_SQUARED = 0, 1
+GG_N_COUNTERS = 16
+COUNTER_NAMES = ["histories", "woodcock_steps", "real_interactions", "deposits", "tally_entries",
+                 "list_overflows", "world_steps", "escaped", "skipped", "loop_capped",
+                 "stack_overflow", "secondaries", "c12", "c13", "c14", "c15"]
+
+_f32p = ctypes.POINTER(ctypes.c_float)
+_f64p = ctypes.POINTER(ctypes.c_double)
+_i32p = ctypes.POINTER(ctypes.c_int32)
+_u16p = ctypes.POINTER(ctypes.c_uint16)
+_u64p = ctypes.POINTER(ctypes.c_uint64)
+
+
+class TablesDesc(ctypes.Structure):
+    _fields_ = [
+        ("n_e", ctypes.c_int32), ("ln_emin", ctypes.c_float), ("inv_dln", ctypes.c_float),
+        ("e_min", ctypes.c_float), ("e_max", ctypes.c_float), ("n_comp", ctypes.c_int32),
+        ("sig", _f32p), ("cum", _f32p), ("ray_amax", _f32p), ("n_rinv", ctypes.c_int32),
+        ("ray_inv", _f32p), ("n_mat", ctypes.c_int32), ("mat_comp", _i32p), ("mat_rho", _f32p),
+    ]
+
+
+class VolumeDesc(ctypes.Structure):
+    _fields_ = [
+        ("dims", ctypes.c_int32 * 3), ("spacing", ctypes.c_double * 3),
+        ("corner", ctypes.c_double * 3), ("labels", _u16p), ("majorant", _f32p),
+    ]
+
+
+class WorldDesc(ctypes.Structure):
+    _fields_ = [("half_size", ctypes.c_double * 3), ("material", ctypes.c_int32)]
+
+
+class SourceDesc(ctypes.Structure):
+    _fields_ = [
+        ("pos_type", ctypes.c_int32), ("translation", ctypes.c_double * 3),
+        ("rotation", ctypes.c_double * 9), ("half_size", ctypes.c_double * 3),
+        ("radius", ctypes.c_double), ("dir_type", ctypes.c_int32), ("theta", ctypes.c_double * 2),
+        ("phi", ctypes.c_double * 2), ("momentum", ctypes.c_double * 3),
+        ("focus", ctypes.c_double * 3), ("n_accept", ctypes.c_int32), ("accept_boxes", _f64p),
+        ("max_rejection", ctypes.c_int32), ("ene_type", ctypes.c_int32), ("mono", ctypes.c_double),
+        ("n_spec", ctypes.c_int32), ("spec_e", _f64p), ("spec_cdf", _f64p),
+        ("e_lo", ctypes.c_double), ("e_hi", ctypes.c_double),
+    ]
+
+
+class DeviceOpts(ctypes.Structure):
+    _fields_ = [
+        ("device", ctypes.c_int32), ("precision", ctypes.c_int32), ("block_size", ctypes.c_int32),
+        ("blocks_per_sm", ctypes.c_int32), ("chunk", ctypes.c_int32), ("batch", ctypes.c_int64),
+    ]
+
+
+def ptr(arr, ctype):
+    """Pointer to a contiguous numpy array (the caller keeps ``arr`` alive)."""
+    if arr is None:
+        return ctypes.cast(None, ctypes.POINTER(ctype))
+    assert arr.flags["C_CONTIGUOUS"]
+    return arr.ctypes.data_as(ctypes.POINTER(ctype))
+
+
+# Exported symbols and their prototypes: (name, restype, argtypes)
+PROTOTYPES = [
+    ("gg_create", ctypes.c_int, [ctypes.POINTER(DeviceOpts), ctypes.POINTER(ctypes.c_void_p)]),
+    ("gg_destroy", ctypes.c_int, [ctypes.c_void_p]),
+    ("gg_last_error", ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_size_t]),
+    ("gg_upload_tables", ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(TablesDesc)]),
+    ("gg_upload_volume", ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(VolumeDesc)]),
+    ("gg_set_world", ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(WorldDesc)]),
+    ("gg_set_source", ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(SourceDesc)]),
+    ("gg_add_dose_tally", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
+    ("gg_reset_tally", ctypes.c_int, [ctypes.c_void_p]),
+    ("gg_run", ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64]),
+    ("gg_synchronize", ctypes.c_int, [ctypes.c_void_p]),
+    ("gg_get_image", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, _f64p, ctypes.c_size_t]),
+    ("gg_get_counters", ctypes.c_int, [ctypes.c_void_p, _u64p, ctypes.c_size_t]),
+    ("gg_last_kernel_ms", ctypes.c_int,
+     [ctypes.c_void_p, _f64p, _f64p, ctypes.POINTER(ctypes.c_int32)]),
+]
+
+_lib = None
+
+
+def load():
+    """Load libgategpu.so (raises if it was not built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not LIB_PATH.exists():
+        raise RuntimeError(
+            f"{LIB_PATH} is missing: build the CUDA extension first "
+            "(python -c 'import opengate_gb300.build as b; b.build()')"
+        )
+    lib = ctypes.CDLL(str(LIB_PATH))
+    for name, res, args in PROTOTYPES:
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+class GGError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(f"{STATUS_NAMES.get(status, status)}: {msg}")
+        self.status = status
+
+
+def check(lib, ctx, status):
+    if status != GG_OK:
+        buf = ctypes.create_string_buffer(1024)
+        lib.gg_last_error(ctx, buf, len(buf))
+        raise GGError(status, buf.value.decode(errors="replace"))

@@ -1,0 +1,537 @@
+// gg_api.cu - C ABI of libgategpu.so (declared in include/gate_gpu.h).
+//
+// A context owns one CUDA stream and every device buffer of one simulation:
+// physics tables, label image, majorant, source spectra, the per-batch
+// fixed-point tallies and the float64 edep / edep-squared images.  Host
+// buffers passed in are copied; nothing is retained past a call.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/gate_gpu.h"
+#include "gg_device.cuh"
+#include "gg_internal.h"
+
+namespace {
+
+std::string g_create_error;
+
+template <typename T>
+void dfree(T *&p) {
+  if (p) cudaFree((void *)p);
+  p = nullptr;
+}
+
+}  // namespace
+
+struct gg_ctx {
+  int device = 0;
+  int precision = GG_PREC_F32;
+  int block = 256;
+  int blocks_per_sm = 0;
+  int chunk = 256;
+  int64_t batch = 1 << 24;
+  int n_sm = 0;
+  cudaStream_t stream = nullptr;
+  std::string err;
+
+  // tables (device, in working precision)
+  int n_e = 0, n_comp = 0, n_rinv = 0, n_mat = 0;
+  float ln_emin = 0, inv_dln = 0, e_min = 0, e_max = 0;
+  void *d_sig = nullptr, *d_cum = nullptr, *d_ray_amax = nullptr, *d_ray_inv = nullptr, *d_mat_rho = nullptr;
+  int *d_mat_comp = nullptr;
+  std::vector<int> h_mat_comp;
+  std::vector<float> h_mat_rho;
+  bool have_tables = false;
+
+  // volume
+  int dims[3] = {0, 0, 0};
+  double spacing[3] = {0, 0, 0}, corner[3] = {0, 0, 0};
+  uint16_t *d_labels = nullptr;
+  void *d_maj = nullptr;
+  size_t n_vox = 0;
+  bool have_volume = false;
+
+  // world
+  gg_world_desc world{};
+  bool have_world = false;
+
+  // source
+  gg_source_desc src{};
+  void *d_spec_e = nullptr, *d_spec_cdf = nullptr, *d_acc_box = nullptr;
+  bool have_source = false;
+
+  // tally
+  unsigned long long *d_acc_e = nullptr, *d_acc_e2 = nullptr;
+  double *d_edep = nullptr, *d_edep2 = nullptr;
+  bool have_tally = false, squared = false;
+
+  // run bookkeeping
+  unsigned long long *d_counters = nullptr, *d_next = nullptr;
+  unsigned int *d_status = nullptr;
+  std::vector<cudaEvent_t> ev;
+  double last_transport_ms = 0, last_flush_ms = 0;
+  int last_launches = 0;
+
+  int fail(int code, const char *fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    err = buf;
+    return code;
+  }
+  int cuda(cudaError_t e, const char *what) {
+    if (e == cudaSuccess) return GG_OK;
+    return fail(GG_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+  }
+  size_t real_size() const { return precision == GG_PREC_F64 ? sizeof(double) : sizeof(float); }
+
+  // Copies n floats to a new device array in working precision.
+  int upload_real(void *&dst, const float *src, size_t n) {
+    dfree(dst);
+    if (n == 0) n = 1;
+    int st = cuda(cudaMalloc(&dst, n * real_size()), "cudaMalloc");
+    if (st) return st;
+    if (!src) return cuda(cudaMemsetAsync(dst, 0, n * real_size(), stream), "cudaMemset");
+    if (precision == GG_PREC_F64) {
+      std::vector<double> tmp(src, src + n);
+      st = cuda(cudaMemcpy(dst, tmp.data(), n * sizeof(double), cudaMemcpyHostToDevice), "cudaMemcpy");
+    } else {
+      st = cuda(cudaMemcpy(dst, src, n * sizeof(float), cudaMemcpyHostToDevice), "cudaMemcpy");
+    }
+    return st;
+  }
+  int upload_real_d(void *&dst, const double *src, size_t n) {
+    std::vector<float> f;
+    std::vector<double> d;
+    dfree(dst);
+    if (n == 0) n = 1;
+    int st = cuda(cudaMalloc(&dst, n * real_size()), "cudaMalloc");
+    if (st) return st;
+    if (!src) return cuda(cudaMemset(dst, 0, n * real_size()), "cudaMemset");
+    if (precision == GG_PREC_F64) {
+      return cuda(cudaMemcpy(dst, src, n * sizeof(double), cudaMemcpyHostToDevice), "cudaMemcpy");
+    }
+    f.resize(n);
+    for (size_t i = 0; i < n; ++i) f[i] = (float)src[i];
+    return cuda(cudaMemcpy(dst, f.data(), n * sizeof(float), cudaMemcpyHostToDevice), "cudaMemcpy");
+  }
+
+  void release() {
+    dfree(d_sig); dfree(d_cum); dfree(d_ray_amax); dfree(d_ray_inv); dfree(d_mat_rho); dfree(d_mat_comp);
+    dfree(d_labels); dfree(d_maj); dfree(d_spec_e); dfree(d_spec_cdf); dfree(d_acc_box);
+    dfree(d_acc_e); dfree(d_acc_e2); dfree(d_edep); dfree(d_edep2);
+    dfree(d_counters); dfree(d_next); dfree(d_status);
+    for (auto e : ev) cudaEventDestroy(e);
+    ev.clear();
+    if (stream) cudaStreamDestroy(stream);
+    stream = nullptr;
+  }
+
+  template <typename real>
+  gg::Scene<real> scene() const {
+    gg::Scene<real> s;
+    memset(&s, 0, sizeof(s));
+    s.n_e = n_e;
+    s.n_comp = n_comp;
+    s.n_rinv = n_rinv;
+    s.n_mat = n_mat;
+    s.ln_emin = (real)ln_emin;
+    s.inv_dln = (real)inv_dln;
+    s.e_min = (real)e_min;
+    s.sig = (const real *)d_sig;
+    s.cum = (const real *)d_cum;
+    s.ray_amax = (const real *)d_ray_amax;
+    s.ray_inv = (const real *)d_ray_inv;
+    s.mat_rho = (const real *)d_mat_rho;
+    s.mat_comp = d_mat_comp;
+    s.maj = (const real *)d_maj;
+    s.nx = dims[0];
+    s.ny = dims[1];
+    s.nz = dims[2];
+    for (int a = 0; a < 3; ++a) {
+      s.bmin[a] = (real)corner[a];
+      s.bmax[a] = (real)(corner[a] + (double)dims[a] * spacing[a]);
+      s.inv_sp[a] = (real)(1.0 / spacing[a]);
+      s.whalf[a] = (real)world.half_size[a];
+    }
+    s.labels = d_labels;
+    s.world_mat = world.material;
+    s.pos_type = src.pos_type;
+    s.dir_type = src.dir_type;
+    s.ene_type = src.ene_type;
+    s.n_accept = src.n_accept;
+    s.max_rejection = src.max_rejection;
+    s.n_spec = src.n_spec;
+    for (int a = 0; a < 3; ++a) {
+      s.s_t[a] = (real)src.translation[a];
+      s.s_half[a] = (real)src.half_size[a];
+      s.s_focus[a] = (real)src.focus[a];
+    }
+    for (int i = 0; i < 9; ++i) s.s_rot[i] = (real)src.rotation[i];
+    s.s_radius = (real)src.radius;
+    s.s_cos_tmin = (real)cos(src.theta[0]);
+    s.s_cos_tmax = (real)cos(src.theta[1]);
+    s.s_phi0_turn = (real)(src.phi[0] / (2.0 * M_PI));
+    s.s_dphi_turn = (real)((src.phi[1] - src.phi[0]) / (2.0 * M_PI));
+    double mn = sqrt(src.momentum[0] * src.momentum[0] + src.momentum[1] * src.momentum[1] +
+                     src.momentum[2] * src.momentum[2]);
+    for (int a = 0; a < 3; ++a) s.s_mom[a] = (real)(mn > 0 ? src.momentum[a] / mn : 0.0);
+    s.s_mono = (real)src.mono;
+    s.s_elo = (real)src.e_lo;
+    s.s_ehi = (real)src.e_hi;
+    s.spec_e = (const real *)d_spec_e;
+    s.spec_cdf = (const real *)d_spec_cdf;
+    s.acc_box = (const real *)d_acc_box;
+    return s;
+  }
+};
+
+extern "C" {
+
+int gg_create(const gg_device_opts *opts, gg_ctx **out) {
+  if (!out) return GG_ERR_ARG;
+  *out = nullptr;
+  gg_ctx *c = new gg_ctx();
+  if (opts) {
+    c->device = opts->device;
+    if (opts->precision) c->precision = opts->precision;
+    if (opts->block_size) c->block = opts->block_size;
+    if (opts->blocks_per_sm) c->blocks_per_sm = opts->blocks_per_sm;
+    if (opts->chunk) c->chunk = opts->chunk;
+    if (opts->batch) c->batch = opts->batch;
+  }
+  auto bail = [&](const std::string &m) {
+    g_create_error = m;
+    c->release();
+    delete c;
+    return m.rfind("arg", 0) == 0 ? GG_ERR_ARG : GG_ERR_CUDA;
+  };
+  if (c->precision != GG_PREC_F32 && c->precision != GG_PREC_F64) return bail("arg: precision must be 32 or 64");
+  if (c->block <= 0 || c->block > 256 || c->block % 32) return bail("arg: block_size must be a multiple of 32 <= 256");
+  if (c->chunk <= 0) return bail("arg: chunk must be > 0");
+  if (c->batch <= 0) return bail("arg: batch must be > 0");
+  int ndev = 0;
+  cudaError_t e = cudaGetDeviceCount(&ndev);
+  if (e != cudaSuccess || ndev == 0) return bail(std::string("no CUDA device: ") + cudaGetErrorString(e));
+  if (c->device < 0 || c->device >= ndev) return bail("arg: device ordinal out of range");
+  if ((e = cudaSetDevice(c->device)) != cudaSuccess) return bail(cudaGetErrorString(e));
+  cudaDeviceProp prop;
+  if ((e = cudaGetDeviceProperties(&prop, c->device)) != cudaSuccess) return bail(cudaGetErrorString(e));
+  c->n_sm = prop.multiProcessorCount;
+  if ((e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking)) != cudaSuccess) return bail(cudaGetErrorString(e));
+  if ((e = cudaMalloc(&c->d_counters, GG_N_COUNTERS * sizeof(unsigned long long))) != cudaSuccess ||
+      (e = cudaMalloc(&c->d_next, sizeof(unsigned long long))) != cudaSuccess ||
+      (e = cudaMalloc(&c->d_status, sizeof(unsigned int))) != cudaSuccess)
+    return bail(cudaGetErrorString(e));
+  cudaMemset(c->d_counters, 0, GG_N_COUNTERS * sizeof(unsigned long long));
+  cudaMemset(c->d_status, 0, sizeof(unsigned int));
+  *out = c;
+  return GG_OK;
+}
+
+int gg_destroy(gg_ctx *ctx) {
+  if (!ctx) return GG_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  ctx->release();
+  delete ctx;
+  return GG_OK;
+}
+
+int gg_last_error(const gg_ctx *ctx, char *buf, size_t len) {
+  if (!buf || len == 0) return GG_ERR_ARG;
+  const std::string &m = ctx ? ctx->err : g_create_error;
+  size_t n = std::min(len - 1, m.size());
+  memcpy(buf, m.data(), n);
+  buf[n] = 0;
+  return GG_OK;
+}
+
+int gg_upload_tables(gg_ctx *c, const gg_tables_desc *t) {
+  if (!c || !t) return GG_ERR_ARG;
+  cudaSetDevice(c->device);
+  if (t->n_e < 2 || t->n_comp < 1 || t->n_rinv < 2 || t->n_mat < 1 || !t->sig || !t->cum || !t->ray_amax ||
+      !t->ray_inv || !t->mat_comp || !t->mat_rho)
+    return c->fail(GG_ERR_ARG, "gg_upload_tables: incomplete table descriptor");
+  if (!(t->inv_dln > 0) || !(t->e_min > 0) || !(t->e_max > t->e_min))
+    return c->fail(GG_ERR_ARG, "gg_upload_tables: invalid energy grid");
+  for (int m = 0; m < t->n_mat; ++m) {
+    if (t->mat_comp[m] < 0 || t->mat_comp[m] >= t->n_comp)
+      return c->fail(GG_ERR_ARG, "gg_upload_tables: material %d refers to composition %d", m, t->mat_comp[m]);
+    if (!(t->mat_rho[m] > 0)) return c->fail(GG_ERR_ARG, "gg_upload_tables: material %d density <= 0", m);
+  }
+  size_t nce = (size_t)t->n_comp * t->n_e;
+  for (size_t i = 0; i < nce; ++i)
+    if (!(t->sig[i] >= 0) || !std::isfinite(t->sig[i]))
+      return c->fail(GG_ERR_ARG, "gg_upload_tables: attenuation table has a negative or non-finite entry");
+  size_t need = c->precision == GG_PREC_F64 ? gg::transport_smem_bytes<double>(t->n_comp, t->n_e, t->n_mat)
+                                            : gg::transport_smem_bytes<float>(t->n_comp, t->n_e, t->n_mat);
+  if (need > 190 * 1024)
+    return c->fail(GG_ERR_ARG, "gg_upload_tables: tables need %zu bytes of shared memory (max 190 KiB)", need);
+  c->n_e = t->n_e;
+  c->n_comp = t->n_comp;
+  c->n_rinv = t->n_rinv;
+  c->n_mat = t->n_mat;
+  c->ln_emin = t->ln_emin;
+  c->inv_dln = t->inv_dln;
+  c->e_min = t->e_min;
+  c->e_max = t->e_max;
+  int st;
+  if ((st = c->upload_real(c->d_sig, t->sig, nce))) return st;
+  if ((st = c->upload_real(c->d_cum, t->cum, 3 * nce))) return st;
+  if ((st = c->upload_real(c->d_ray_amax, t->ray_amax, nce))) return st;
+  if ((st = c->upload_real(c->d_ray_inv, t->ray_inv, (size_t)t->n_comp * t->n_rinv))) return st;
+  if ((st = c->upload_real(c->d_mat_rho, t->mat_rho, (size_t)t->n_mat))) return st;
+  dfree(c->d_mat_comp);
+  if ((st = c->cuda(cudaMalloc(&c->d_mat_comp, sizeof(int) * t->n_mat), "cudaMalloc"))) return st;
+  if ((st = c->cuda(cudaMemcpy(c->d_mat_comp, t->mat_comp, sizeof(int) * t->n_mat, cudaMemcpyHostToDevice),
+                    "cudaMemcpy")))
+    return st;
+  c->h_mat_comp.assign(t->mat_comp, t->mat_comp + t->n_mat);
+  c->h_mat_rho.assign(t->mat_rho, t->mat_rho + t->n_mat);
+  c->have_tables = true;
+  return GG_OK;
+}
+
+int gg_upload_volume(gg_ctx *c, const gg_volume_desc *v) {
+  if (!c || !v) return GG_ERR_ARG;
+  cudaSetDevice(c->device);
+  if (!c->have_tables) return c->fail(GG_ERR_STATE, "gg_upload_volume: upload the tables first");
+  for (int a = 0; a < 3; ++a) {
+    if (v->dims[a] <= 0) return c->fail(GG_ERR_ARG, "gg_upload_volume: dims must be > 0");
+    if (!(v->spacing[a] > 0)) return c->fail(GG_ERR_ARG, "gg_upload_volume: spacing must be > 0");
+  }
+  if (!v->labels || !v->majorant) return c->fail(GG_ERR_ARG, "gg_upload_volume: null labels or majorant");
+  size_t n = (size_t)v->dims[0] * v->dims[1] * v->dims[2];
+  if (n >= (size_t)UINT32_MAX) return c->fail(GG_ERR_ARG, "gg_upload_volume: more than 2^32-1 voxels");
+  uint16_t lmax = 0;
+  for (size_t i = 0; i < n; ++i) lmax = std::max(lmax, v->labels[i]);
+  if ((int)lmax >= c->n_mat)
+    return c->fail(GG_ERR_ARG, "gg_upload_volume: label %u outside the material table (%d)", lmax, c->n_mat);
+  for (int i = 0; i < c->n_e; ++i)
+    if (!(v->majorant[i] > 0) || !std::isfinite(v->majorant[i]))
+      return c->fail(GG_ERR_ARG, "gg_upload_volume: majorant must be finite and > 0");
+  int st;
+  dfree(c->d_labels);
+  if ((st = c->cuda(cudaMalloc(&c->d_labels, n * sizeof(uint16_t)), "cudaMalloc labels"))) return st;
+  if ((st = c->cuda(cudaMemcpyAsync(c->d_labels, v->labels, n * sizeof(uint16_t), cudaMemcpyHostToDevice, c->stream),
+                    "cudaMemcpy labels")))
+    return st;
+  if ((st = c->upload_real(c->d_maj, v->majorant, (size_t)c->n_e))) return st;
+  if (n != c->n_vox) {
+    dfree(c->d_acc_e); dfree(c->d_acc_e2); dfree(c->d_edep); dfree(c->d_edep2);
+    c->have_tally = false;
+  }
+  for (int a = 0; a < 3; ++a) {
+    c->dims[a] = v->dims[a];
+    c->spacing[a] = v->spacing[a];
+    c->corner[a] = v->corner[a];
+  }
+  c->n_vox = n;
+  c->have_volume = true;
+  return c->cuda(cudaStreamSynchronize(c->stream), "upload volume");
+}
+
+int gg_set_world(gg_ctx *c, const gg_world_desc *w) {
+  if (!c || !w) return GG_ERR_ARG;
+  if (!c->have_tables) return c->fail(GG_ERR_STATE, "gg_set_world: upload the tables first");
+  if (w->material < 0 || w->material >= c->n_mat) return c->fail(GG_ERR_ARG, "gg_set_world: bad material");
+  for (int a = 0; a < 3; ++a)
+    if (!(w->half_size[a] > 0)) return c->fail(GG_ERR_ARG, "gg_set_world: half sizes must be > 0");
+  c->world = *w;
+  c->have_world = true;
+  return GG_OK;
+}
+
+int gg_set_source(gg_ctx *c, const gg_source_desc *s) {
+  if (!c || !s) return GG_ERR_ARG;
+  cudaSetDevice(c->device);
+  if (!c->have_tables) return c->fail(GG_ERR_STATE, "gg_set_source: upload the tables first");
+  if (s->pos_type < GG_POS_POINT || s->pos_type > GG_POS_DISC) return c->fail(GG_ERR_ARG, "gg_set_source: position type");
+  if (s->dir_type < GG_DIR_ISO || s->dir_type > GG_DIR_FOCUSED) return c->fail(GG_ERR_ARG, "gg_set_source: direction type");
+  if (s->ene_type < GG_ENE_MONO || s->ene_type > GG_ENE_RANGE) return c->fail(GG_ERR_ARG, "gg_set_source: energy type");
+  if (s->n_accept < 0 || (s->n_accept > 0 && !s->accept_boxes)) return c->fail(GG_ERR_ARG, "gg_set_source: acceptance boxes");
+  double elo = 0, ehi = 0;
+  if (s->ene_type == GG_ENE_MONO) elo = ehi = s->mono;
+  else if (s->ene_type == GG_ENE_RANGE) { elo = s->e_lo; ehi = s->e_hi; }
+  else {
+    if (s->n_spec < 1 || !s->spec_e || !s->spec_cdf) return c->fail(GG_ERR_ARG, "gg_set_source: empty spectrum");
+    int ne = s->ene_type == GG_ENE_HISTOGRAM ? s->n_spec + 1 : s->n_spec;
+    elo = *std::min_element(s->spec_e, s->spec_e + ne);
+    ehi = *std::max_element(s->spec_e, s->spec_e + ne);
+    for (int i = 1; i < s->n_spec; ++i)
+      if (s->spec_cdf[i] < s->spec_cdf[i - 1]) return c->fail(GG_ERR_ARG, "gg_set_source: cumulative weights decrease");
+  }
+  if (!(elo >= c->e_min) || !(ehi <= c->e_max))
+    return c->fail(GG_ERR_DOMAIN, "gg_set_source: energies [%g, %g] MeV outside the tables [%g, %g]", elo, ehi,
+                   (double)c->e_min, (double)c->e_max);
+  int st;
+  int ne = s->ene_type == GG_ENE_HISTOGRAM ? s->n_spec + 1 : s->n_spec;
+  if ((st = c->upload_real_d(c->d_spec_e, s->spec_e, s->spec_e ? (size_t)ne : 0))) return st;
+  if ((st = c->upload_real_d(c->d_spec_cdf, s->spec_cdf, s->spec_cdf ? (size_t)s->n_spec : 0))) return st;
+  if ((st = c->upload_real_d(c->d_acc_box, s->accept_boxes, (size_t)6 * s->n_accept))) return st;
+  c->src = *s;
+  c->src.spec_e = nullptr;
+  c->src.spec_cdf = nullptr;
+  c->src.accept_boxes = nullptr;
+  c->have_source = true;
+  return GG_OK;
+}
+
+int gg_add_dose_tally(gg_ctx *c, int32_t score_squared) {
+  if (!c) return GG_ERR_ARG;
+  cudaSetDevice(c->device);
+  if (!c->have_volume) return c->fail(GG_ERR_STATE, "gg_add_dose_tally: upload the volume first");
+  int st;
+  size_t n = c->n_vox;
+  if (!c->d_acc_e) {
+    if ((st = c->cuda(cudaMalloc(&c->d_acc_e, n * 8), "cudaMalloc tally"))) return st;
+    if ((st = c->cuda(cudaMalloc(&c->d_edep, n * 8), "cudaMalloc edep"))) return st;
+  }
+  if (score_squared && !c->d_acc_e2) {
+    if ((st = c->cuda(cudaMalloc(&c->d_acc_e2, n * 8), "cudaMalloc tally2"))) return st;
+    if ((st = c->cuda(cudaMalloc(&c->d_edep2, n * 8), "cudaMalloc edep2"))) return st;
+  }
+  c->squared = score_squared != 0;
+  c->have_tally = true;
+  return gg_reset_tally(c);
+}
+
+int gg_reset_tally(gg_ctx *c) {
+  if (!c) return GG_ERR_ARG;
+  if (!c->have_tally) return c->fail(GG_ERR_STATE, "gg_reset_tally: no tally");
+  cudaSetDevice(c->device);
+  size_t n = c->n_vox;
+  int st;
+  if ((st = c->cuda(cudaMemsetAsync(c->d_acc_e, 0, n * 8, c->stream), "memset"))) return st;
+  if ((st = c->cuda(cudaMemsetAsync(c->d_edep, 0, n * 8, c->stream), "memset"))) return st;
+  if (c->d_acc_e2) {
+    if ((st = c->cuda(cudaMemsetAsync(c->d_acc_e2, 0, n * 8, c->stream), "memset"))) return st;
+    if ((st = c->cuda(cudaMemsetAsync(c->d_edep2, 0, n * 8, c->stream), "memset"))) return st;
+  }
+  if ((st = c->cuda(cudaMemsetAsync(c->d_counters, 0, GG_N_COUNTERS * 8, c->stream), "memset"))) return st;
+  return c->cuda(cudaMemsetAsync(c->d_status, 0, sizeof(unsigned int), c->stream), "memset");
+}
+
+static int run_impl(gg_ctx *c, uint64_t n, uint64_t seed, uint64_t first) {
+  size_t smem = c->precision == GG_PREC_F64 ? gg::transport_smem_bytes<double>(c->n_comp, c->n_e, c->n_mat)
+                                            : gg::transport_smem_bytes<float>(c->n_comp, c->n_e, c->n_mat);
+  int bps = c->blocks_per_sm;
+  if (bps <= 0) {
+    cudaError_t e = c->precision == GG_PREC_F64 ? gg::occupancy_blocks<double>(c->block, smem, &bps)
+                                                : gg::occupancy_blocks<float>(c->block, smem, &bps);
+    if (e != cudaSuccess) return c->cuda(e, "occupancy");
+    if (bps < 1) bps = 1;
+  }
+  int grid = c->n_sm * bps;
+  uint64_t nb = (n + (uint64_t)c->batch - 1) / (uint64_t)c->batch;
+  while (c->ev.size() < 2 * nb + 2) {
+    cudaEvent_t e;
+    int st = c->cuda(cudaEventCreate(&e), "cudaEventCreate");
+    if (st) return st;
+    c->ev.push_back(e);
+  }
+  gg::KernelArgs a;
+  a.seed = seed;
+  a.next = c->d_next;
+  a.acc_e = c->d_acc_e;
+  a.acc_e2 = c->squared ? c->d_acc_e2 : nullptr;
+  a.counters = c->d_counters;
+  a.status = c->d_status;
+  a.chunk = c->chunk;
+  int flush_grid = c->n_sm * 8;
+  int st;
+  for (uint64_t b = 0; b < nb; ++b) {
+    a.h_begin = first + b * (uint64_t)c->batch;
+    a.h_end = std::min(first + n, a.h_begin + (uint64_t)c->batch);
+    if ((st = c->cuda(cudaMemsetAsync(c->d_next, 0, 8, c->stream), "memset"))) return st;
+    if ((st = c->cuda(cudaEventRecord(c->ev[2 * b], c->stream), "event"))) return st;
+    cudaError_t e = c->precision == GG_PREC_F64
+                        ? gg::launch_transport<double>(c->scene<double>(), a, grid, c->block, smem, c->stream)
+                        : gg::launch_transport<float>(c->scene<float>(), a, grid, c->block, smem, c->stream);
+    if ((st = c->cuda(e, "transport launch"))) return st;
+    if ((st = c->cuda(cudaEventRecord(c->ev[2 * b + 1], c->stream), "event"))) return st;
+    if ((st = c->cuda(gg::launch_flush(c->d_acc_e, a.acc_e2, c->d_edep, c->squared ? c->d_edep2 : nullptr,
+                                       c->n_vox, flush_grid, c->stream),
+                      "flush launch")))
+      return st;
+  }
+  if ((st = c->cuda(cudaEventRecord(c->ev[2 * nb], c->stream), "event"))) return st;
+  if ((st = c->cuda(cudaStreamSynchronize(c->stream), "transport"))) return st;
+  double tt = 0, tf = 0;
+  for (uint64_t b = 0; b < nb; ++b) {
+    float ms = 0;
+    cudaEventElapsedTime(&ms, c->ev[2 * b], c->ev[2 * b + 1]);
+    tt += ms;
+    cudaEventElapsedTime(&ms, c->ev[2 * b + 1], b + 1 < nb ? c->ev[2 * b + 2] : c->ev[2 * nb]);
+    tf += ms;
+  }
+  c->last_transport_ms = tt;
+  c->last_flush_ms = tf;
+  c->last_launches = (int)(2 * nb);
+  unsigned int status = 0;
+  if ((st = c->cuda(cudaMemcpy(&status, c->d_status, sizeof(status), cudaMemcpyDeviceToHost), "status"))) return st;
+  if (status) {
+    cudaMemset(c->d_status, 0, sizeof(unsigned int));
+    return c->fail(GG_ERR_DOMAIN, "gg_run: source sampling failed (angular acceptance exhausted max_rejection)");
+  }
+  return GG_OK;
+}
+
+int gg_run(gg_ctx *c, uint64_t n, uint64_t seed, uint64_t first) {
+  if (!c) return GG_ERR_ARG;
+  cudaSetDevice(c->device);
+  if (!c->have_tables || !c->have_volume || !c->have_world || !c->have_source || !c->have_tally)
+    return c->fail(GG_ERR_STATE, "gg_run: tables, volume, world, source and tally must be set first");
+  if (n == 0) return GG_OK;
+  if (first + n < first) return c->fail(GG_ERR_ARG, "gg_run: history range overflows");
+  return run_impl(c, n, seed, first);
+}
+
+int gg_synchronize(gg_ctx *c) {
+  if (!c) return GG_ERR_ARG;
+  return c->cuda(cudaStreamSynchronize(c->stream), "synchronize");
+}
+
+int gg_get_image(gg_ctx *c, int32_t which, double *out, size_t n) {
+  if (!c || !out) return GG_ERR_ARG;
+  cudaSetDevice(c->device);
+  if (!c->have_tally) return c->fail(GG_ERR_STATE, "gg_get_image: no tally");
+  if (n != c->n_vox) return c->fail(GG_ERR_ARG, "gg_get_image: buffer has %zu voxels, image %zu", n, c->n_vox);
+  double *src = nullptr;
+  if (which == GG_IMG_EDEP) src = c->d_edep;
+  else if (which == GG_IMG_EDEP_SQUARED) src = c->squared ? c->d_edep2 : nullptr;
+  if (!src) return c->fail(GG_ERR_ARG, "gg_get_image: image %d not scored", which);
+  int st = c->cuda(cudaMemcpyAsync(out, src, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream), "download");
+  if (st) return st;
+  return c->cuda(cudaStreamSynchronize(c->stream), "download");
+}
+
+int gg_get_counters(gg_ctx *c, uint64_t *out, size_t n) {
+  if (!c || !out) return GG_ERR_ARG;
+  cudaSetDevice(c->device);
+  unsigned long long tmp[GG_N_COUNTERS];
+  int st = c->cuda(cudaMemcpy(tmp, c->d_counters, sizeof(tmp), cudaMemcpyDeviceToHost), "counters");
+  if (st) return st;
+  for (size_t i = 0; i < n && i < GG_N_COUNTERS; ++i) out[i] = tmp[i];
+  return GG_OK;
+}
+
+int gg_last_kernel_ms(gg_ctx *c, double *transport_ms, double *flush_ms, int32_t *launches) {
+  if (!c) return GG_ERR_ARG;
+  if (transport_ms) *transport_ms = c->last_transport_ms;
+  if (flush_ms) *flush_ms = c->last_flush_ms;
+  if (launches) *launches = c->last_launches;
+  return GG_OK;
+}
+
+}  // extern "C"

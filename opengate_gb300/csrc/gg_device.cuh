@@ -1,0 +1,477 @@
+// gg_device.cuh - device-side numerics and photon physics of the transport kernels.
+//
+// Every function here is written as an explicit sequence of correctly rounded
+// IEEE operations (the translation unit is compiled with -fmad=false, so no
+// a*b+c is fused unless written as fma()), which makes one history's result
+// reproducible bit for bit, independent of launch shape, and identical to a
+// CPU evaluation of the same sequence.
+//
+// Physics (G4EmStandardPhysics option 0, as selected by
+// physics_list_name = "G4EmStandardPhysics", opengate/physics.py:341-347):
+//   * Compton: Klein-Nishina, composition + rejection sampling of the Geant4
+//     Physics Reference Manual (Butcher & Messel), electron stopped at creation;
+//   * photoelectric: absorption, local deposit (fluorescence off);
+//   * Rayleigh: x^2 sampled from the tabulated form-factor cumulative,
+//     accepted with (1 + cos^2)/2;
+//   * pair: e- and e+ stopped at creation (min_ekine user limit,
+//     opengate/physics.py:699-753), kinetic energy deposited, the positron
+//     annihilates at rest into two back-to-back 511 keV photons.
+#pragma once
+#include <cstdint>
+
+#include "../../include/gate_gpu.h"
+
+namespace gg {
+
+constexpr int kHistList = 8;      // per-history voxel list (registers)
+constexpr int kLoopCap = 1000;    // sampling-loop iteration cap
+constexpr int kStepCap = 1000000; // per-photon step cap (termination guard)
+constexpr double kMC2 = 0.51099895;
+constexpr double kHcMevAngstrom = 12.398419843320026e-3;
+
+template <typename real>
+__device__ __forceinline__ real R(double x) {
+  return static_cast<real>(x);
+}
+
+// ---------------------------------------------------------------------------
+// Philox4x32-10 counter-based generator (Salmon et al., SC'11)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void philox4x32_10(uint32_t c[4], uint32_t k0, uint32_t k1, uint32_t o[4]) {
+  uint32_t c0 = c[0], c1 = c[1], c2 = c[2], c3 = c[3];
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+    if (r > 0) {
+      k0 += 0x9E3779B9u;
+      k1 += 0xBB67AE85u;
+    }
+    uint32_t lo0 = 0xD2511F53u * c0;
+    uint32_t hi0 = __umulhi(0xD2511F53u, c0);
+    uint32_t lo1 = 0xCD9E8D57u * c2;
+    uint32_t hi1 = __umulhi(0xCD9E8D57u, c2);
+    uint32_t n0 = hi1 ^ c1 ^ k0;
+    uint32_t n2 = hi0 ^ c3 ^ k1;
+    c0 = n0;
+    c1 = lo1;
+    c2 = n2;
+    c3 = lo0;
+  }
+  o[0] = c0;
+  o[1] = c1;
+  o[2] = c2;
+  o[3] = c3;
+}
+
+// Stream of one history: key = seed, counter = (block, stream, history lo, hi).
+struct Rng {
+  uint32_t k0, k1;
+  uint32_t blk, stream, h0, h1;
+  uint32_t buf[4];
+  int idx;
+
+  __device__ __forceinline__ void init(uint64_t seed, uint64_t history, uint32_t s) {
+    k0 = (uint32_t)seed;
+    k1 = (uint32_t)(seed >> 32);
+    blk = 0;
+    stream = s;
+    h0 = (uint32_t)history;
+    h1 = (uint32_t)(history >> 32);
+    idx = 4;
+  }
+  __device__ __forceinline__ uint32_t next() {
+    if (idx == 4) {
+      uint32_t c[4] = {blk, stream, h0, h1};
+      philox4x32_10(c, k0, k1, buf);
+      blk += 1u;
+      idx = 0;
+    }
+    // register-resident select instead of a dynamically indexed array
+    uint32_t v = idx == 0 ? buf[0] : (idx == 1 ? buf[1] : (idx == 2 ? buf[2] : buf[3]));
+    ++idx;
+    return v;
+  }
+};
+
+template <typename real>
+__device__ __forceinline__ real u01(Rng &g) {
+  return (real)(g.next() >> 8) * R<real>(5.9604644775390625e-08);
+}
+template <typename real>
+__device__ __forceinline__ real u01_open0(Rng &g) {
+  return (real)((g.next() >> 8) + 1u) * R<real>(5.9604644775390625e-08);
+}
+
+// ---------------------------------------------------------------------------
+// Elementary functions built from + - * / (A&S 4.1.27, 4.2.1, 4.3.65/66)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float gg_log(float x) {
+  uint32_t b = __float_as_uint(x);
+  int e = (int)(b >> 23) - 127;
+  uint32_t mb = (b & 0x007fffffu) | 0x3f800000u;
+  if (mb > 0x3fb504f3u) {
+    mb -= 0x00800000u;
+    e += 1;
+  }
+  float m = __uint_as_float(mb);
+  float num = m - 1.0f;
+  float den = m + 1.0f;
+  float s = num / den;
+  float z = s * s;
+  float p = (float)(1.0 / 11.0);
+  p = p * z + (float)(1.0 / 9.0);
+  p = p * z + (float)(1.0 / 7.0);
+  p = p * z + (float)(1.0 / 5.0);
+  p = p * z + (float)(1.0 / 3.0);
+  float t = s * z;
+  t = t * p;
+  float u = s + t;
+  float lm = u + u;
+  float fe = (float)e;
+  float lo = fe * 1.42860682030941723212e-06f;
+  lo = lo + lm;
+  float hi = fe * 0.693145751953125f;
+  return hi + lo;
+}
+
+__device__ __forceinline__ double gg_log(double x) {
+  uint64_t b = (uint64_t)__double_as_longlong(x);
+  int e = (int)(b >> 52) - 1023;
+  uint64_t mb = (b & 0x000fffffffffffffull) | 0x3ff0000000000000ull;
+  if (mb > 0x3ff6a09e667f3bcdull) {
+    mb -= 0x0010000000000000ull;
+    e += 1;
+  }
+  double m = __longlong_as_double((long long)mb);
+  double num = m - 1.0;
+  double den = m + 1.0;
+  double s = num / den;
+  double z = s * s;
+  double p = 1.0 / 25.0;
+  p = p * z + 1.0 / 23.0;
+  p = p * z + 1.0 / 21.0;
+  p = p * z + 1.0 / 19.0;
+  p = p * z + 1.0 / 17.0;
+  p = p * z + 1.0 / 15.0;
+  p = p * z + 1.0 / 13.0;
+  p = p * z + 1.0 / 11.0;
+  p = p * z + 1.0 / 9.0;
+  p = p * z + 1.0 / 7.0;
+  p = p * z + 1.0 / 5.0;
+  p = p * z + 1.0 / 3.0;
+  double t = s * z;
+  t = t * p;
+  double u = s + t;
+  double lm = u + u;
+  double fe = (double)e;
+  double lo = fe * 1.90821492927058770002e-10;
+  lo = lo + lm;
+  double hi = fe * 6.93147180369123816490e-01;
+  return hi + lo;
+}
+
+__device__ __forceinline__ float gg_exp(float x) {
+  if (x < -87.0f) return 0.0f;
+  float t = x * 1.44269504088896340736f;
+  t = t + 0.5f;
+  int n = (int)t;
+  if ((float)n > t) n = n - 1;
+  float fn = (float)n;
+  float r = x - fn * 0.693145751953125f;
+  r = r - fn * 1.42860682030941723212e-06f;
+  float p = (float)(1.0 / 5040.0);
+  p = p * r + (float)(1.0 / 720.0);
+  p = p * r + (float)(1.0 / 120.0);
+  p = p * r + (float)(1.0 / 24.0);
+  p = p * r + (float)(1.0 / 6.0);
+  p = p * r + 0.5f;
+  p = p * r + 1.0f;
+  p = p * r + 1.0f;
+  float sc = __uint_as_float((uint32_t)(n + 127) << 23);
+  return p * sc;
+}
+
+__device__ __forceinline__ double gg_exp(double x) {
+  if (x < -708.0) return 0.0;
+  double t = x * 1.44269504088896338700e+00;
+  t = t + 0.5;
+  int n = (int)t;
+  if ((double)n > t) n = n - 1;
+  double fn = (double)n;
+  double r = x - fn * 6.93147180369123816490e-01;
+  r = r - fn * 1.90821492927058770002e-10;
+  double p = 1.0 / 6227020800.0;
+  p = p * r + 1.0 / 479001600.0;
+  p = p * r + 1.0 / 39916800.0;
+  p = p * r + 1.0 / 3628800.0;
+  p = p * r + 1.0 / 362880.0;
+  p = p * r + 1.0 / 40320.0;
+  p = p * r + 1.0 / 5040.0;
+  p = p * r + 1.0 / 720.0;
+  p = p * r + 1.0 / 120.0;
+  p = p * r + 1.0 / 24.0;
+  p = p * r + 1.0 / 6.0;
+  p = p * r + 0.5;
+  p = p * r + 1.0;
+  p = p * r + 1.0;
+  double sc = __longlong_as_double((long long)((uint64_t)(n + 1023) << 52));
+  return p * sc;
+}
+
+// sin and cos of 2*pi*f, f in [0, 1): octant reduction on f (exact), Taylor
+// series on [0, pi/4].
+__device__ __forceinline__ void gg_sincos_turn(float f, float &sn, float &cs) {
+  float t = f * 8.0f;
+  int o = (int)t;
+  if (o > 7) o = 7;
+  float fr = t - (float)o;
+  float a = (o & 1) ? (1.0f - fr) : fr;
+  a = a * 0.785398163397448309616f;
+  float z = a * a;
+  float p = (float)(-1.0 / 39916800.0);
+  p = p * z + (float)(1.0 / 362880.0);
+  p = p * z + (float)(-1.0 / 5040.0);
+  p = p * z + (float)(1.0 / 120.0);
+  p = p * z + (float)(-1.0 / 6.0);
+  float st = z * p;
+  st = a * st;
+  float s = a + st;
+  float q = (float)(1.0 / 479001600.0);
+  q = q * z + (float)(-1.0 / 3628800.0);
+  q = q * z + (float)(1.0 / 40320.0);
+  q = q * z + (float)(-1.0 / 720.0);
+  q = q * z + (float)(1.0 / 24.0);
+  q = q * z + (float)(-1.0 / 2.0);
+  float ct = z * q;
+  float c = 1.0f + ct;
+  float ss = (o == 1 || o == 2 || o == 5 || o == 6) ? c : s;
+  float cc = (o == 1 || o == 2 || o == 5 || o == 6) ? s : c;
+  sn = (o >= 4) ? -ss : ss;
+  cs = (o >= 2 && o <= 5) ? -cc : cc;
+}
+
+__device__ __forceinline__ void gg_sincos_turn(double f, double &sn, double &cs) {
+  double t = f * 8.0;
+  int o = (int)t;
+  if (o > 7) o = 7;
+  double fr = t - (double)o;
+  double a = (o & 1) ? (1.0 - fr) : fr;
+  a = a * 0.785398163397448309616;
+  double z = a * a;
+  double p = -1.0 / 121645100408832000.0;
+  p = p * z + 1.0 / 355687428096000.0;
+  p = p * z + -1.0 / 1307674368000.0;
+  p = p * z + 1.0 / 6227020800.0;
+  p = p * z + -1.0 / 39916800.0;
+  p = p * z + 1.0 / 362880.0;
+  p = p * z + -1.0 / 5040.0;
+  p = p * z + 1.0 / 120.0;
+  p = p * z + -1.0 / 6.0;
+  double st = z * p;
+  st = a * st;
+  double s = a + st;
+  double q = 1.0 / 2432902008176640000.0;
+  q = q * z + -1.0 / 6402373705728000.0;
+  q = q * z + 1.0 / 20922789888000.0;
+  q = q * z + -1.0 / 87178291200.0;
+  q = q * z + 1.0 / 479001600.0;
+  q = q * z + -1.0 / 3628800.0;
+  q = q * z + 1.0 / 40320.0;
+  q = q * z + -1.0 / 720.0;
+  q = q * z + 1.0 / 24.0;
+  q = q * z + -1.0 / 2.0;
+  double ct = z * q;
+  double c = 1.0 + ct;
+  double ss = (o == 1 || o == 2 || o == 5 || o == 6) ? c : s;
+  double cc = (o == 1 || o == 2 || o == 5 || o == 6) ? s : c;
+  sn = (o >= 4) ? -ss : ss;
+  cs = (o >= 2 && o <= 5) ? -cc : cc;
+}
+
+__device__ __forceinline__ float gg_sqrt(float x) { return __fsqrt_rn(x); }
+__device__ __forceinline__ double gg_sqrt(double x) { return __dsqrt_rn(x); }
+__device__ __forceinline__ float gg_floor(float x) { return floorf(x); }
+__device__ __forceinline__ double gg_floor(double x) { return floor(x); }
+__device__ __forceinline__ uint64_t to_fixed(float v) { return __float2ull_rn(v * 4294967296.0f); }
+__device__ __forceinline__ uint64_t to_fixed(double v) { return __double2ull_rn(v * 4294967296.0); }
+__device__ __forceinline__ float gg_inf(float) { return __int_as_float(0x7f800000); }
+__device__ __forceinline__ double gg_inf(double) { return __longlong_as_double(0x7ff0000000000000ll); }
+
+// New direction: polar angle (cost, sint) and azimuth (cphi, sphi) measured
+// around the old direction u.
+template <typename real>
+__device__ __forceinline__ void rotate_dir(real &ux, real &uy, real &uz, real cost, real sint, real cphi,
+                                           real sphi) {
+  real sx = sint * cphi;
+  real sy = sint * sphi;
+  real sz = cost;
+  real p2 = ux * ux;
+  p2 = p2 + uy * uy;
+  real nx, ny, nz;
+  if (p2 > R<real>(1e-20)) {
+    real pp = gg_sqrt(p2);
+    real inv = R<real>(1) / pp;
+    real a = ux * uz;
+    a = a * sx;
+    a = a - uy * sy;
+    a = a * inv;
+    nx = a + ux * sz;
+    real b = uy * uz;
+    b = b * sx;
+    b = b + ux * sy;
+    b = b * inv;
+    ny = b + uy * sz;
+    real c = -pp * sx;
+    nz = c + uz * sz;
+  } else if (uz > R<real>(0)) {
+    nx = sx;
+    ny = sy;
+    nz = sz;
+  } else {
+    nx = -sx;
+    ny = sy;
+    nz = -sz;
+  }
+  real n2 = nx * nx;
+  n2 = n2 + ny * ny;
+  n2 = n2 + nz * nz;
+  real rn = R<real>(1) / gg_sqrt(n2);
+  ux = nx * rn;
+  uy = ny * rn;
+  uz = nz * rn;
+}
+
+// ---------------------------------------------------------------------------
+// Scene seen by a kernel; table pointers may point into shared memory.
+// ---------------------------------------------------------------------------
+template <typename real>
+struct Scene {
+  // tables
+  int n_e, n_comp, n_rinv, n_mat;
+  real ln_emin, inv_dln, e_min;
+  const real *sig, *cum, *ray_amax, *ray_inv, *mat_rho, *maj;
+  const int *mat_comp;
+  // image
+  int nx, ny, nz;
+  real bmin[3], bmax[3], inv_sp[3];
+  const uint16_t *labels;
+  // world
+  real whalf[3];
+  int world_mat;
+  // source
+  int pos_type, dir_type, ene_type, n_accept, max_rejection, n_spec;
+  real s_t[3], s_rot[9], s_half[3], s_radius;
+  real s_cos_tmin, s_cos_tmax, s_phi0_turn, s_dphi_turn;
+  real s_mom[3], s_focus[3];
+  real s_mono, s_elo, s_ehi;
+  const real *spec_e, *spec_cdf, *acc_box;
+};
+
+template <typename real>
+struct EIdx {
+  int ie;
+  real fe;
+};
+
+template <typename real>
+__device__ __forceinline__ real interp_row(const real *row, const EIdx<real> &ei) {
+  real a = row[ei.ie];
+  real d = row[ei.ie + 1] - a;
+  d = ei.fe * d;
+  return a + d;
+}
+
+template <typename real>
+__device__ __forceinline__ EIdx<real> energy_index(const Scene<real> &s, real e) {
+  EIdx<real> r;
+  real le = gg_log(e);
+  real t = le - s.ln_emin;
+  t = t * s.inv_dln;
+  int i = (int)t;
+  if (i < 0) i = 0;
+  if (i > s.n_e - 2) i = s.n_e - 2;
+  r.ie = i;
+  r.fe = t - (real)i;
+  return r;
+}
+
+template <typename real>
+__device__ __forceinline__ real exit_distance(const real p[3], const real d[3], const real lo[3],
+                                              const real hi[3]) {
+  real t = gg_inf(real(0));
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    if (d[a] > R<real>(0)) {
+      real ta = (hi[a] - p[a]) / d[a];
+      if (ta < t) t = ta;
+    } else if (d[a] < R<real>(0)) {
+      real ta = (lo[a] - p[a]) / d[a];
+      if (ta < t) t = ta;
+    }
+  }
+  if (t < R<real>(0)) t = R<real>(0);
+  return t;
+}
+
+template <typename real>
+__device__ __forceinline__ real entry_distance(const real p[3], const real d[3], const real lo[3],
+                                               const real hi[3]) {
+  real inf = gg_inf(real(0));
+  real tnear = -inf, tfar = inf;
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    if (d[a] == R<real>(0)) {
+      if (p[a] < lo[a] || p[a] > hi[a]) return inf;
+    } else {
+      real t1 = (lo[a] - p[a]) / d[a];
+      real t2 = (hi[a] - p[a]) / d[a];
+      if (t1 > t2) {
+        real tmp = t1;
+        t1 = t2;
+        t2 = tmp;
+      }
+      if (t1 > tnear) tnear = t1;
+      if (t2 < tfar) tfar = t2;
+    }
+  }
+  if (tnear > tfar || tfar < R<real>(0)) return inf;
+  return tnear > R<real>(0) ? tnear : R<real>(0);
+}
+
+template <typename real>
+__device__ __forceinline__ bool inside_box(const real p[3], const real lo[3], const real hi[3]) {
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+    if (p[a] < lo[a] || p[a] > hi[a]) return false;
+  return true;
+}
+
+template <typename real>
+struct Photon {
+  real pos[3], dir[3], e;
+  real t_exit, mumax, inv_mumax;
+  EIdx<real> ei;
+  int alive, in_image, can_enter, steps;
+};
+
+template <typename real>
+__device__ __forceinline__ void set_energy(const Scene<real> &s, Photon<real> &ph, real e) {
+  ph.e = e;
+  ph.ei = energy_index(s, e);
+  real mm = interp_row(s.maj, ph.ei);
+  ph.mumax = mm;
+  ph.inv_mumax = R<real>(1) / mm;
+}
+
+template <typename real>
+__device__ __forceinline__ void start_photon(const Scene<real> &s, Photon<real> &ph) {
+  ph.steps = 0;
+  if (inside_box(ph.pos, s.bmin, s.bmax)) {
+    ph.in_image = 1;
+    ph.t_exit = exit_distance(ph.pos, ph.dir, s.bmin, s.bmax);
+  } else {
+    ph.in_image = 0;
+    ph.can_enter = 1;
+  }
+}
+
+}  // namespace gg

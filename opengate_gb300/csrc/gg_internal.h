@@ -1,0 +1,35 @@
+// gg_internal.h - declarations shared by the host API and the kernel translation units.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+
+namespace gg {
+
+template <typename real>
+struct Scene;
+
+// Arguments of one transport launch (one tally batch).
+struct KernelArgs {
+  uint64_t seed;
+  uint64_t h_begin, h_end;          // histories [h_begin, h_end)
+  unsigned long long *next;         // claim counter, zero at launch
+  unsigned long long *acc_e;        // per-voxel fixed-point edep of this batch
+  unsigned long long *acc_e2;       // per-voxel fixed-point edep^2 (or null)
+  unsigned long long *counters;     // GG_N_COUNTERS slots
+  unsigned int *status;             // OR of error codes raised by the kernel
+  int chunk;                        // histories claimed per warp refill
+};
+
+template <typename real>
+size_t transport_smem_bytes(int n_comp, int n_e, int n_mat);
+template <typename real>
+cudaError_t launch_transport(const Scene<real> &s, const KernelArgs &a, int grid, int block, size_t smem,
+                             cudaStream_t st);
+template <typename real>
+cudaError_t occupancy_blocks(int block, size_t smem, int *blocks_per_sm);
+cudaError_t launch_flush(unsigned long long *acc_e, unsigned long long *acc_e2, double *edep, double *edep2,
+                         size_t n, int grid, cudaStream_t st);
+
+}  // namespace gg

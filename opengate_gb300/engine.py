@@ -1,0 +1,85 @@
+"""GPU transport engine: one libgategpu context per simulation run.
+
+This is the GB300 counterpart of the reference's SimulationEngine run phase
+(opengate/engines.py:1554-1660): it pushes the scene to the device, runs the
+requested histories in tally batches and fetches the float64 images, the way
+DoseActor.EndOfRunActionMasterThread fetches them from C++
+(opengate/actors/doseactors.py:662-715).
+"""
+
+import ctypes
+
+import numpy as np
+
+from . import _capi as C
+
+
+class DoseEngine:
+    """Drives libgategpu.so for one :class:`~opengate_gb300.scene.Scene`."""
+
+    def __init__(self, scene, device=0, precision=32, block_size=0, blocks_per_sm=0, chunk=0, batch=0,
+                 score_squared=True):
+        self.lib = C.load()
+        self.scene = scene
+        opts = C.DeviceOpts(device, precision, block_size, blocks_per_sm, chunk, batch)
+        ctx = ctypes.c_void_p()
+        st = self.lib.gg_create(ctypes.byref(opts), ctypes.byref(ctx))
+        C.check(self.lib, None, st)
+        self.ctx = ctx
+        self.score_squared = score_squared
+        self.upload()
+
+    def _call(self, name, *args):
+        C.check(self.lib, self.ctx, getattr(self.lib, name)(self.ctx, *args))
+
+    def upload(self):
+        s = self.scene
+        self._call("gg_upload_tables", ctypes.byref(s.tables_desc))
+        self._call("gg_upload_volume", ctypes.byref(s.volume_desc))
+        self._call("gg_set_world", ctypes.byref(s.world_desc))
+        self._call("gg_set_source", ctypes.byref(s.source_desc))
+        self._call("gg_add_dose_tally", 1 if self.score_squared else 0)
+
+    def reset(self):
+        self._call("gg_reset_tally")
+
+    def run(self, n, seed, first=0):
+        self._call("gg_run", ctypes.c_uint64(n), ctypes.c_uint64(seed), ctypes.c_uint64(first))
+
+    def image(self, which):
+        out = np.empty(self.scene.n_voxels, dtype=np.float64)
+        self._call("gg_get_image", which, C.ptr(out, ctypes.c_double), out.size)
+        return out.reshape(self.scene.labels.shape)
+
+    def edep(self):
+        return self.image(C.GG_IMG_EDEP)
+
+    def edep_squared(self):
+        return self.image(C.GG_IMG_EDEP_SQUARED)
+
+    def counters(self):
+        out = np.zeros(C.GG_N_COUNTERS, dtype=np.uint64)
+        self._call("gg_get_counters", C.ptr(out, ctypes.c_uint64), out.size)
+        return {name: int(out[i]) for i, name in enumerate(C.COUNTER_NAMES)}
+
+    def last_kernel_ms(self):
+        t, f, n = ctypes.c_double(), ctypes.c_double(), ctypes.c_int32()
+        self._call("gg_last_kernel_ms", ctypes.byref(t), ctypes.byref(f), ctypes.byref(n))
+        return t.value, f.value, n.value
+
+    def close(self):
+        if self.ctx:
+            self.lib.gg_destroy(self.ctx)
+            self.ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()

@@ -1,0 +1,139 @@
+"""Synthetic, seeded workloads for the photon-transport path.
+
+* :func:`water_pencil` - 64^3 HU-0 water cube, 2 mm voxels, world of air,
+  1 MeV pencil beam from the centre of the entrance face along +z.
+* :func:`ct_phantom` - 256 x 256 x 160 int16 CT image, 1.2 mm voxels: air
+  outside an elliptic-cylinder body (semi-axes 160 x 110 mm) of soft tissue
+  N(40, 20^2), two ellipsoidal lungs N(-800, 50^2), spine and rib cylinders
+  U(700, 1200), five fat ellipsoids N(-90, 15^2).  The ten-interval HU table
+  in ``data/ct10_*.txt`` maps it to materials through the
+  HounsfieldUnit_to_material restatement.  Source: point at 100 cm SSD
+  (anterior, along +y), 10 x 10 cm field at the isocentre plane (angular
+  acceptance box), 60-bin histogram spectrum on [0.1, 6] MeV with density
+  proportional to E exp(-E / 1.5 MeV).
+
+Every array is generated from a numpy seed, so a workload is reproducible
+bit for bit on any machine.
+"""
+
+import math
+import pathlib
+
+import numpy as np
+
+from . import _capi as C
+from . import materials as M
+from . import tables as T
+from .scene import Scene, SourceSpec
+
+DATA = pathlib.Path(__file__).resolve().parent / "data"
+CT10_MATERIALS = DATA / "ct10_materials.txt"
+CT10_DENSITIES = DATA / "ct10_densities.txt"
+
+
+def world_air_materials():
+    db = M.MaterialDatabase()
+    return db
+
+
+def water_pencil(n=64, spacing=2.0, energy=1.0):
+    """Water cube, pencil beam.  Returns a Scene (materials: 0 G4_WATER, 1 G4_AIR)."""
+    db = M.MaterialDatabase()
+    mats = [db.get("G4_WATER"), db.get("G4_AIR")]
+    pt = T.PhysicsTables(mats)
+    labels = np.zeros((n, n, n), dtype=np.uint16)
+    half = n * spacing / 2.0
+    src = SourceSpec()
+    src.pos_type = C.GG_POS_POINT
+    src.translation = [0.0, 0.0, -half]
+    src.dir_type = C.GG_DIR_MOMENTUM
+    src.momentum = [0.0, 0.0, 1.0]
+    src.ene_type = C.GG_ENE_MONO
+    src.mono = energy
+    return Scene(pt, labels, [spacing] * 3, [-half] * 3, [1000.0, 1000.0, 1000.0], 1, src)
+
+
+def ct_hu_image(seed=20240611, shape=(160, 256, 256), spacing=1.2):
+    """int16 HU array [nz][ny][nx] of the synthetic CT phantom."""
+    rng = np.random.default_rng(seed)
+    nz, ny, nx = shape
+    x = (np.arange(nx) + 0.5) * spacing - nx * spacing / 2
+    y = (np.arange(ny) + 0.5) * spacing - ny * spacing / 2
+    z = (np.arange(nz) + 0.5) * spacing - nz * spacing / 2
+    Z, Y, X = np.meshgrid(z, y, x, indexing="ij")
+    hu = np.full(shape, -1000.0, dtype=np.float32)
+    body = (X / 160.0) ** 2 + (Y / 110.0) ** 2 <= 1.0
+    hu[body] = rng.normal(40.0, 20.0, size=int(body.sum()))
+    # five fat ellipsoids inside the body
+    for _ in range(5):
+        cx, cy = rng.uniform(-110, 110), rng.uniform(-70, 70)
+        cz = rng.uniform(-70, 70)
+        ax, ay, az = rng.uniform(10, 25, size=3)
+        m = ((X - cx) / ax) ** 2 + ((Y - cy) / ay) ** 2 + ((Z - cz) / az) ** 2 <= 1.0
+        m &= body
+        hu[m] = rng.normal(-90.0, 15.0, size=int(m.sum()))
+    # two lungs
+    for sx in (-1.0, 1.0):
+        m = ((X - sx * 65.0) / 45.0) ** 2 + ((Y + 5.0) / 60.0) ** 2 + ((Z - 10.0) / 75.0) ** 2 <= 1.0
+        hu[m] = rng.normal(-800.0, 50.0, size=int(m.sum()))
+    # spine: cylinder along z, posterior (+y)
+    m = (X / 16.0) ** 2 + ((Y - 72.0) / 16.0) ** 2 <= 1.0
+    hu[m] = rng.uniform(700.0, 1200.0, size=int(m.sum()))
+    # ribs: thin cylinders along z on an ellipse around the lungs
+    for ang in np.deg2rad([-150, -120, -60, -30, 30, 60, 120, 150]):
+        rx, ry = 132.0 * math.cos(ang), 92.0 * math.sin(ang)
+        m = ((X - rx) / 6.0) ** 2 + ((Y - ry) / 6.0) ** 2 <= 1.0
+        m &= np.abs(Z - 10.0) <= 70.0
+        hu[m] = rng.uniform(700.0, 1200.0, size=int(m.sum()))
+    return np.clip(np.rint(hu), -1024, 3000).astype(np.int16)
+
+
+def ct_materials(density_tolerance=0.05):
+    """Material list (label order) for the CT phantom: label 0 = G4_AIR."""
+    db = M.MaterialDatabase()
+    vm, _ = M.hounsfield_unit_to_material(db, density_tolerance, CT10_MATERIALS, CT10_DENSITIES)
+    lut = M.material_to_label_lut("G4_AIR", vm)
+    names = sorted(lut, key=lut.get)
+    return vm, lut, [db.get(n) for n in names]
+
+
+def spectrum_e_exp(n_bins=60, e_lo=0.1, e_hi=6.0, kt=1.5):
+    """60-bin histogram: edges and normalised cumulative of w_i dE_i, w ~ E exp(-E/kT)."""
+    edges = np.linspace(e_lo, e_hi, n_bins + 1)
+    centres = 0.5 * (edges[1:] + edges[:-1])
+    w = centres * np.exp(-centres / kt)
+    # GateGenericSource::InitializeEnergy (GateGenericSource.cpp:583-644):
+    # accumulate weight x bin width, normalise to the total
+    acc = np.cumsum(w * np.diff(edges))
+    return edges, acc / acc[-1]
+
+
+def ct_phantom(seed=20240611, shape=(160, 256, 256), spacing=1.2, ssd=1000.0, field=100.0,
+               density_tolerance=0.05):
+    hu = ct_hu_image(seed, shape, spacing)
+    vm, lut, mats = ct_materials(density_tolerance)
+    labels = M.create_label_image(hu, "G4_AIR", vm, lut)
+    pt = T.PhysicsTables(mats)
+    nz, ny, nx = shape
+    corner = [-nx * spacing / 2, -ny * spacing / 2, -nz * spacing / 2]
+    src = SourceSpec()
+    src.pos_type = C.GG_POS_POINT
+    sad = ssd + 110.0  # body surface at y = -110 mm, isocentre at the origin
+    src.translation = [0.0, -sad, 0.0]
+    # iso directions (G4 convention: direction = -(sin t cos p, sin t sin p, cos t)),
+    # rotated so the cone axis is +y: theta measured from -z in the local frame;
+    # use a rotation that maps local -z to +y.
+    src.dir_type = C.GG_DIR_ISO
+    half_diag = math.atan(math.hypot(field / 2, field / 2) / sad)
+    src.theta = [math.pi / 2 - half_diag, math.pi / 2 + half_diag]
+    src.phi = [3 * math.pi / 2 - half_diag, 3 * math.pi / 2 + half_diag]
+    # acceptance: the field plane, a thin box at the isocentre depth scaled to
+    # the first plane in front of the image (y just below the image face)
+    y_plane = corner[1] - 1.0
+    scale = (y_plane + sad) / sad
+    hf = field / 2 * scale
+    src.accept_boxes = [((-hf, y_plane - 0.5, -hf), (hf, y_plane + 0.5, hf))]
+    src.ene_type = C.GG_ENE_HISTOGRAM
+    src.spec_e, src.spec_cdf = spectrum_e_exp()
+    air = 0
+    return Scene(pt, labels, [spacing] * 3, corner, [1500.0, 1500.0, 1500.0], air, src), hu

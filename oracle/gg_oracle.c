@@ -1,0 +1,1097 @@
+/*
+ * gg_oracle.c - CPU oracle for the voxelised photon-transport path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This file is the checker: the parity tests, the
+ * smoke check and the CPU-baseline leg of bench.py call it; the product path
+ * (opengate_gb300 + libgategpu.so) never links, loads or calls it.
+ *
+ * It restates, in plain C and one history at a time, what the reference does
+ * on this path:
+ *   - primary generation: GateGenericSource::GeneratePrimaries and the SPS
+ *     samplers (core/opengate_core/opengate_lib/GateGenericSource.cpp:209-262,
+ *     312-664; GateSingleParticleSource.cpp:67-137 for the acceptance loop;
+ *     GateSPSEneDistribution.cpp:116-159 for lines/histogram sampling);
+ *   - the voxel lookup of GateImageNestedParameterisation::ComputeMaterial
+ *     (GateImageNestedParameterisation.cpp:47-75) and the image index of
+ *     GateDoseActor::GetVoxelPosition (GateDoseActor.cpp:144-178,
+ *     GateHelpersImage.txx:60-92);
+ *   - the photon physics of G4EmStandardPhysics as restated from the Geant4
+ *     Physics Reference Manual (Klein-Nishina sampling of Butcher & Messel,
+ *     photoelectric absorption with local deposit, Rayleigh from tabulated
+ *     form factors, pair production with both leptons stopped at creation and
+ *     the positron annihilating at rest into two 511 keV photons, the
+ *     min_ekine user limit of opengate/physics.py:699-753);
+ *   - DoseActor scoring: edep per voxel and the history-by-history squared sum
+ *     (GateDoseActor.cpp:180-243 SteppingAction, 359-397 ScoreSquaredValue /
+ *     FlushSquaredValues).
+ *
+ * The arithmetic is the same operation sequence the CUDA kernels execute
+ * (float or double, no contraction of a*b+c, correctly rounded + - * / sqrt,
+ * logarithm / exponential / sine-cosine built from those operations), with the
+ * same counter-based Philox4x32-10 stream per history, so a GPU run and this
+ * oracle agree bit for bit.  Tallies are 64-bit fixed point (2^-32 MeV and
+ * 2^-32 MeV^2 units) per batch, flushed into float64 images, which makes the
+ * totals independent of the order in which histories finish.
+ *
+ * Build: see oracle/build_oracle.py (gcc -O2 -ffp-contract=off, once with
+ * -DGGO_DOUBLE for the FP64 variant).
+ */
+#include <math.h>
+#include <pthread.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "../include/gate_gpu.h"
+
+#ifdef GGO_DOUBLE
+typedef double real;
+#define R(x) ((double)(x))
+#define GGO_PREFIX(name) ggo64_##name
+#else
+typedef float real;
+#define R(x) ((float)(x))
+#define GGO_PREFIX(name) ggo32_##name
+#endif
+
+#define HIST_LIST 8
+#define LOOP_CAP 1000
+#define STEP_CAP 1000000
+#define MC2 0.51099895
+#define HC_MEV_ANGSTROM 12.398419843320026e-3
+
+/* ------------------------------------------------------------------------ */
+/* Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11)                         */
+/* ------------------------------------------------------------------------ */
+static void philox4x32_10(const uint32_t ctr_in[4], const uint32_t key_in[2], uint32_t out[4]) {
+  uint32_t c0 = ctr_in[0], c1 = ctr_in[1], c2 = ctr_in[2], c3 = ctr_in[3];
+  uint32_t k0 = key_in[0], k1 = key_in[1];
+  for (int r = 0; r < 10; ++r) {
+    if (r > 0) {
+      k0 += 0x9E3779B9u;
+      k1 += 0xBB67AE85u;
+    }
+    uint64_t p0 = (uint64_t)0xD2511F53u * c0;
+    uint64_t p1 = (uint64_t)0xCD9E8D57u * c2;
+    uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0;
+    uint32_t hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
+    uint32_t n0 = hi1 ^ c1 ^ k0;
+    uint32_t n2 = hi0 ^ c3 ^ k1;
+    c0 = n0;
+    c1 = lo1;
+    c2 = n2;
+    c3 = lo0;
+  }
+  out[0] = c0;
+  out[1] = c1;
+  out[2] = c2;
+  out[3] = c3;
+}
+
+typedef struct {
+  uint32_t key[2];
+  uint32_t ctr[4]; /* ctr[0] = block index, ctr[1] = stream, ctr[2..3] = history */
+  uint32_t buf[4];
+  int idx;
+} rng_t;
+
+static void rng_init(rng_t *g, uint64_t seed, uint64_t history, uint32_t stream) {
+  g->key[0] = (uint32_t)seed;
+  g->key[1] = (uint32_t)(seed >> 32);
+  g->ctr[0] = 0;
+  g->ctr[1] = stream;
+  g->ctr[2] = (uint32_t)history;
+  g->ctr[3] = (uint32_t)(history >> 32);
+  g->idx = 4;
+}
+
+static uint32_t rng_u32(rng_t *g) {
+  if (g->idx == 4) {
+    philox4x32_10(g->ctr, g->key, g->buf);
+    g->ctr[0] += 1u;
+    g->idx = 0;
+  }
+  return g->buf[g->idx++];
+}
+
+/* uniform in [0, 1) with 24-bit resolution */
+static real u01(rng_t *g) { return (real)(rng_u32(g) >> 8) * R(5.9604644775390625e-08); }
+/* uniform in (0, 1] */
+static real u01_open0(rng_t *g) { return (real)((rng_u32(g) >> 8) + 1u) * R(5.9604644775390625e-08); }
+
+/* ------------------------------------------------------------------------ */
+/* Elementary functions from + - * / (series of Abramowitz & Stegun 4.1.27,  */
+/* 4.2.1, 4.3.65/66 after Cody-Waite style range reduction)                  */
+/* ------------------------------------------------------------------------ */
+#ifndef GGO_DOUBLE
+static real ggo_log(real x) {
+  uint32_t b;
+  memcpy(&b, &x, 4);
+  int e = (int)(b >> 23) - 127;
+  uint32_t mb = (b & 0x007fffffu) | 0x3f800000u;
+  if (mb > 0x3fb504f3u) {
+    mb -= 0x00800000u;
+    e += 1;
+  }
+  float m;
+  memcpy(&m, &mb, 4);
+  float num = m - 1.0f;
+  float den = m + 1.0f;
+  float s = num / den;
+  float z = s * s;
+  float p = (float)(1.0 / 11.0);
+  p = p * z + (float)(1.0 / 9.0);
+  p = p * z + (float)(1.0 / 7.0);
+  p = p * z + (float)(1.0 / 5.0);
+  p = p * z + (float)(1.0 / 3.0);
+  float t = s * z;
+  t = t * p;
+  float u = s + t;
+  float lm = u + u;
+  float fe = (float)e;
+  float lo = fe * 1.42860682030941723212e-06f;
+  lo = lo + lm;
+  float hi = fe * 0.693145751953125f;
+  return hi + lo;
+}
+
+static real ggo_exp(real x) {
+  if (x < -87.0f) return 0.0f;
+  float t = x * 1.44269504088896340736f;
+  t = t + 0.5f;
+  int n = (int)t;
+  if ((float)n > t) n = n - 1;
+  float fn = (float)n;
+  float r = x - fn * 0.693145751953125f;
+  r = r - fn * 1.42860682030941723212e-06f;
+  float p = (float)(1.0 / 5040.0);
+  p = p * r + (float)(1.0 / 720.0);
+  p = p * r + (float)(1.0 / 120.0);
+  p = p * r + (float)(1.0 / 24.0);
+  p = p * r + (float)(1.0 / 6.0);
+  p = p * r + 0.5f;
+  p = p * r + 1.0f;
+  p = p * r + 1.0f;
+  uint32_t sb = (uint32_t)(n + 127) << 23;
+  float sc;
+  memcpy(&sc, &sb, 4);
+  return p * sc;
+}
+
+static void ggo_sincos_turn(real f, real *sn, real *cs) {
+  float t = f * 8.0f;
+  int o = (int)t;
+  if (o > 7) o = 7;
+  float fr = t - (float)o;
+  float a = (o & 1) ? (1.0f - fr) : fr;
+  a = a * 0.785398163397448309616f;
+  float z = a * a;
+  float p = (float)(-1.0 / 39916800.0);
+  p = p * z + (float)(1.0 / 362880.0);
+  p = p * z + (float)(-1.0 / 5040.0);
+  p = p * z + (float)(1.0 / 120.0);
+  p = p * z + (float)(-1.0 / 6.0);
+  float st = z * p;
+  st = a * st;
+  float s = a + st;
+  float q = (float)(1.0 / 479001600.0);
+  q = q * z + (float)(-1.0 / 3628800.0);
+  q = q * z + (float)(1.0 / 40320.0);
+  q = q * z + (float)(-1.0 / 720.0);
+  q = q * z + (float)(1.0 / 24.0);
+  q = q * z + (float)(-1.0 / 2.0);
+  float ct = z * q;
+  float c = 1.0f + ct;
+  switch (o) {
+  case 0: *sn = s; *cs = c; break;
+  case 1: *sn = c; *cs = s; break;
+  case 2: *sn = c; *cs = -s; break;
+  case 3: *sn = s; *cs = -c; break;
+  case 4: *sn = -s; *cs = -c; break;
+  case 5: *sn = -c; *cs = -s; break;
+  case 6: *sn = -c; *cs = s; break;
+  default: *sn = -s; *cs = c; break;
+  }
+}
+#else
+static real ggo_log(real x) {
+  uint64_t b;
+  memcpy(&b, &x, 8);
+  int e = (int)(b >> 52) - 1023;
+  uint64_t mb = (b & 0x000fffffffffffffull) | 0x3ff0000000000000ull;
+  if (mb > 0x3ff6a09e667f3bcdull) {
+    mb -= 0x0010000000000000ull;
+    e += 1;
+  }
+  double m;
+  memcpy(&m, &mb, 8);
+  double num = m - 1.0;
+  double den = m + 1.0;
+  double s = num / den;
+  double z = s * s;
+  double p = 1.0 / 25.0;
+  p = p * z + 1.0 / 23.0;
+  p = p * z + 1.0 / 21.0;
+  p = p * z + 1.0 / 19.0;
+  p = p * z + 1.0 / 17.0;
+  p = p * z + 1.0 / 15.0;
+  p = p * z + 1.0 / 13.0;
+  p = p * z + 1.0 / 11.0;
+  p = p * z + 1.0 / 9.0;
+  p = p * z + 1.0 / 7.0;
+  p = p * z + 1.0 / 5.0;
+  p = p * z + 1.0 / 3.0;
+  double t = s * z;
+  t = t * p;
+  double u = s + t;
+  double lm = u + u;
+  double fe = (double)e;
+  double lo = fe * 1.90821492927058770002e-10;
+  lo = lo + lm;
+  double hi = fe * 6.93147180369123816490e-01;
+  return hi + lo;
+}
+
+static real ggo_exp(real x) {
+  if (x < -708.0) return 0.0;
+  double t = x * 1.44269504088896338700e+00;
+  t = t + 0.5;
+  int n = (int)t;
+  if ((double)n > t) n = n - 1;
+  double fn = (double)n;
+  double r = x - fn * 6.93147180369123816490e-01;
+  r = r - fn * 1.90821492927058770002e-10;
+  double p = 1.0 / 6227020800.0;
+  p = p * r + 1.0 / 479001600.0;
+  p = p * r + 1.0 / 39916800.0;
+  p = p * r + 1.0 / 3628800.0;
+  p = p * r + 1.0 / 362880.0;
+  p = p * r + 1.0 / 40320.0;
+  p = p * r + 1.0 / 5040.0;
+  p = p * r + 1.0 / 720.0;
+  p = p * r + 1.0 / 120.0;
+  p = p * r + 1.0 / 24.0;
+  p = p * r + 1.0 / 6.0;
+  p = p * r + 0.5;
+  p = p * r + 1.0;
+  p = p * r + 1.0;
+  uint64_t sb = (uint64_t)(n + 1023) << 52;
+  double sc;
+  memcpy(&sc, &sb, 8);
+  return p * sc;
+}
+
+static void ggo_sincos_turn(real f, real *sn, real *cs) {
+  double t = f * 8.0;
+  int o = (int)t;
+  if (o > 7) o = 7;
+  double fr = t - (double)o;
+  double a = (o & 1) ? (1.0 - fr) : fr;
+  a = a * 0.785398163397448309616;
+  double z = a * a;
+  double p = -1.0 / 121645100408832000.0;
+  p = p * z + 1.0 / 355687428096000.0;
+  p = p * z + -1.0 / 1307674368000.0;
+  p = p * z + 1.0 / 6227020800.0;
+  p = p * z + -1.0 / 39916800.0;
+  p = p * z + 1.0 / 362880.0;
+  p = p * z + -1.0 / 5040.0;
+  p = p * z + 1.0 / 120.0;
+  p = p * z + -1.0 / 6.0;
+  double st = z * p;
+  st = a * st;
+  double s = a + st;
+  double q = 1.0 / 2432902008176640000.0;
+  q = q * z + -1.0 / 6402373705728000.0;
+  q = q * z + 1.0 / 20922789888000.0;
+  q = q * z + -1.0 / 87178291200.0;
+  q = q * z + 1.0 / 479001600.0;
+  q = q * z + -1.0 / 3628800.0;
+  q = q * z + 1.0 / 40320.0;
+  q = q * z + -1.0 / 720.0;
+  q = q * z + 1.0 / 24.0;
+  q = q * z + -1.0 / 2.0;
+  double ct = z * q;
+  double c = 1.0 + ct;
+  switch (o) {
+  case 0: *sn = s; *cs = c; break;
+  case 1: *sn = c; *cs = s; break;
+  case 2: *sn = c; *cs = -s; break;
+  case 3: *sn = s; *cs = -c; break;
+  case 4: *sn = -s; *cs = -c; break;
+  case 5: *sn = -c; *cs = -s; break;
+  case 6: *sn = -c; *cs = s; break;
+  default: *sn = -s; *cs = c; break;
+  }
+}
+#endif
+
+static real ggo_sqrt(real x) {
+#ifdef GGO_DOUBLE
+  return sqrt(x);
+#else
+  return sqrtf(x);
+#endif
+}
+
+/* New direction from polar (cos t, sin t) and azimuth (cos p, sin p) around
+   the old direction u: the rotation that takes the z axis onto u. */
+static void rotate_dir(real u[3], real cost, real sint, real cphi, real sphi) {
+  real sx = sint * cphi;
+  real sy = sint * sphi;
+  real sz = cost;
+  real ux = u[0], uy = u[1], uz = u[2];
+  real p2 = ux * ux;
+  p2 = p2 + uy * uy;
+  real nx, ny, nz;
+  if (p2 > R(1e-20)) {
+    real pp = ggo_sqrt(p2);
+    real inv = R(1) / pp;
+    real a = ux * uz;
+    a = a * sx;
+    a = a - uy * sy;
+    a = a * inv;
+    nx = a + ux * sz;
+    real b = uy * uz;
+    b = b * sx;
+    b = b + ux * sy;
+    b = b * inv;
+    ny = b + uy * sz;
+    real c = -pp * sx;
+    nz = c + uz * sz;
+  } else if (uz > R(0)) {
+    nx = sx;
+    ny = sy;
+    nz = sz;
+  } else {
+    nx = -sx;
+    ny = sy;
+    nz = -sz;
+  }
+  real n2 = nx * nx;
+  n2 = n2 + ny * ny;
+  n2 = n2 + nz * nz;
+  real rn = R(1) / ggo_sqrt(n2);
+  u[0] = nx * rn;
+  u[1] = ny * rn;
+  u[2] = nz * rn;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Scene in working precision                                                */
+/* ------------------------------------------------------------------------ */
+typedef struct {
+  /* tables */
+  int n_e, n_comp, n_rinv, n_mat;
+  real ln_emin, inv_dln, e_min, e_max;
+  real *sig, *cum, *ray_amax, *ray_inv, *mat_rho;
+  int *mat_comp;
+  /* image */
+  int nx, ny, nz;
+  real bmin[3], bmax[3], inv_sp[3];
+  const uint16_t *labels;
+  real *maj;
+  /* world */
+  real whalf[3];
+  int world_mat;
+  /* source */
+  gg_source_desc src;
+  real s_t[3], s_rot[9], s_half[3], s_radius;
+  real s_cos_tmin, s_cos_tmax, s_phi0_turn, s_dphi_turn;
+  real s_mom[3], s_focus[3];
+  real s_mono, s_elo, s_ehi;
+  real *s_spec_e, *s_spec_cdf;
+  real *acc_box;
+} scene_t;
+
+typedef struct {
+  int ie;
+  real fe;
+} eidx_t;
+
+static real interp_row(const real *row, eidx_t ei) {
+  real a = row[ei.ie];
+  real d = row[ei.ie + 1] - a;
+  d = ei.fe * d;
+  return a + d;
+}
+
+static eidx_t energy_index(const scene_t *s, real e) {
+  eidx_t r;
+  real le = ggo_log(e);
+  real t = le - s->ln_emin;
+  t = t * s->inv_dln;
+  int i = (int)t;
+  if (i < 0) i = 0;
+  if (i > s->n_e - 2) i = s->n_e - 2;
+  r.ie = i;
+  r.fe = t - (real)i;
+  return r;
+}
+
+/* distance to leave box [lo, hi] from p along d (p assumed inside) */
+static real exit_distance(const real p[3], const real d[3], const real lo[3], const real hi[3]) {
+  real t = R(INFINITY);
+  for (int a = 0; a < 3; ++a) {
+    real ta;
+    if (d[a] > R(0)) {
+      ta = (hi[a] - p[a]) / d[a];
+      if (ta < t) t = ta;
+    } else if (d[a] < R(0)) {
+      ta = (lo[a] - p[a]) / d[a];
+      if (ta < t) t = ta;
+    }
+  }
+  if (t < R(0)) t = R(0);
+  return t;
+}
+
+/* distance to enter box [lo, hi] from p along d; INFINITY if missed */
+static real entry_distance(const real p[3], const real d[3], const real lo[3], const real hi[3]) {
+  real tnear = -R(INFINITY), tfar = R(INFINITY);
+  for (int a = 0; a < 3; ++a) {
+    if (d[a] == R(0)) {
+      if (p[a] < lo[a] || p[a] > hi[a]) return R(INFINITY);
+    } else {
+      real t1 = (lo[a] - p[a]) / d[a];
+      real t2 = (hi[a] - p[a]) / d[a];
+      if (t1 > t2) {
+        real tmp = t1;
+        t1 = t2;
+        t2 = tmp;
+      }
+      if (t1 > tnear) tnear = t1;
+      if (t2 < tfar) tfar = t2;
+    }
+  }
+  if (tnear > tfar || tfar < R(0)) return R(INFINITY);
+  return tnear > R(0) ? tnear : R(0);
+}
+
+/* ------------------------------------------------------------------------ */
+/* History state and tally                                                   */
+/* ------------------------------------------------------------------------ */
+typedef struct {
+  uint64_t *acc_e, *acc_e2; /* shared per batch, updated with atomics */
+  uint64_t cnt[GG_N_COUNTERS];
+} tally_t;
+
+typedef struct {
+  uint32_t vox[HIST_LIST];
+  real acc[HIST_LIST];
+  int n;
+} hlist_t;
+
+static uint64_t to_fixed(real v) {
+  /* v * 2^32 is exact; round to nearest even */
+#ifdef GGO_DOUBLE
+  return (uint64_t)llrint(v * 4294967296.0);
+#else
+  return (uint64_t)llrintf(v * 4294967296.0f);
+#endif
+}
+
+static void hlist_flush(hlist_t *l, tally_t *t) {
+  for (int k = 0; k < l->n; ++k) {
+    real a = l->acc[k];
+    real a2 = a * a;
+    __atomic_fetch_add(&t->acc_e[l->vox[k]], to_fixed(a), __ATOMIC_RELAXED);
+    if (t->acc_e2) __atomic_fetch_add(&t->acc_e2[l->vox[k]], to_fixed(a2), __ATOMIC_RELAXED);
+  }
+  t->cnt[GG_CNT_TALLY_ENTRIES] += (uint64_t)l->n;
+  l->n = 0;
+}
+
+static void deposit(hlist_t *l, tally_t *t, uint32_t v, real e) {
+  if (!(e > R(0))) return;
+  t->cnt[GG_CNT_DEPOSITS]++;
+  for (int k = 0; k < l->n; ++k) {
+    if (l->vox[k] == v) {
+      l->acc[k] = l->acc[k] + e;
+      return;
+    }
+  }
+  if (l->n == HIST_LIST) {
+    t->cnt[GG_CNT_LIST_OVERFLOWS]++;
+    hlist_flush(l, t);
+  }
+  l->vox[l->n] = v;
+  l->acc[l->n] = e;
+  l->n++;
+}
+
+typedef struct {
+  real pos[3], dir[3], e;
+  int alive, in_image, can_enter;
+  real t_exit;
+  eidx_t ei;
+  real mumax, inv_mumax;
+} photon_t;
+
+static void set_energy(const scene_t *s, photon_t *ph, real e) {
+  ph->e = e;
+  ph->ei = energy_index(s, e);
+  real mm = interp_row(s->maj, ph->ei);
+  ph->mumax = mm;
+  ph->inv_mumax = R(1) / mm;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Interactions                                                              */
+/* ------------------------------------------------------------------------ */
+/* Klein-Nishina sampling, composition + rejection method of the Geant4
+   Physics Reference Manual (G4KleinNishinaCompton). */
+static void compton(const scene_t *s, photon_t *ph, rng_t *g, tally_t *t, real *edep_out) {
+  real e = ph->e;
+  real k = e * R(1.0 / MC2);
+  real twok = R(2) * k;
+  real eps0 = R(1) / (R(1) + twok);
+  real eps0sq = eps0 * eps0;
+  real alpha1 = -ggo_log(eps0);
+  real alpha2 = R(1) - eps0sq;
+  alpha2 = R(0.5) * alpha2;
+  alpha2 = alpha1 + alpha2;
+  real eps, epssq, onecost, sint2;
+  int it = 0;
+  for (;;) {
+    real r0 = u01(g), r1 = u01(g), r2 = u01(g);
+    if (alpha1 > alpha2 * r0) {
+      eps = ggo_exp(-alpha1 * r1);
+      epssq = eps * eps;
+    } else {
+      real w = R(1) - eps0sq;
+      w = w * r1;
+      epssq = eps0sq + w;
+      eps = ggo_sqrt(epssq);
+    }
+    real ek = eps * k;
+    onecost = (R(1) - eps) / ek;
+    sint2 = onecost * (R(2) - onecost);
+    real gr = eps * sint2;
+    gr = gr / (R(1) + epssq);
+    gr = R(1) - gr;
+    if (gr >= r2) break;
+    if (++it >= LOOP_CAP) {
+      t->cnt[GG_CNT_LOOP_CAPPED]++;
+      break;
+    }
+  }
+  real e1 = eps * e;
+  *edep_out = e - e1;
+  real cost = R(1) - onecost;
+  real sint = ggo_sqrt(sint2 > R(0) ? sint2 : R(0));
+  real sp, cp;
+  ggo_sincos_turn(u01(g), &sp, &cp);
+  rotate_dir(ph->dir, cost, sint, cp, sp);
+  if (e1 < s->e_min) {
+    *edep_out = *edep_out + e1;
+    ph->alive = 0;
+  } else {
+    set_energy(s, ph, e1);
+  }
+}
+
+static void rayleigh(const scene_t *s, int comp, photon_t *ph, rng_t *g, tally_t *t) {
+  real k = ph->e * R(1.0 / HC_MEV_ANGSTROM);
+  real x2max = k * k;
+  real amax = interp_row(s->ray_amax + (size_t)comp * s->n_e, ph->ei);
+  const real *inv = s->ray_inv + (size_t)comp * s->n_rinv;
+  real cost;
+  int it = 0;
+  for (;;) {
+    real r = u01(g);
+    real tt = r * amax;
+    real pos = tt * (real)(s->n_rinv - 1);
+    int j = (int)pos;
+    if (j > s->n_rinv - 2) j = s->n_rinv - 2;
+    real f = pos - (real)j;
+    real d = inv[j + 1] - inv[j];
+    d = f * d;
+    real x2 = inv[j] + d;
+    real q = R(2) * x2;
+    q = q / x2max;
+    cost = R(1) - q;
+    if (cost < R(-1)) cost = R(-1);
+    real r2 = u01(g);
+    real lhs = R(2) * r2;
+    real rhs = cost * cost;
+    rhs = R(1) + rhs;
+    if (lhs <= rhs) break;
+    if (++it >= LOOP_CAP) {
+      t->cnt[GG_CNT_LOOP_CAPPED]++;
+      break;
+    }
+  }
+  real st2 = cost * cost;
+  st2 = R(1) - st2;
+  real sint = ggo_sqrt(st2 > R(0) ? st2 : R(0));
+  real sp, cp;
+  ggo_sincos_turn(u01(g), &sp, &cp);
+  rotate_dir(ph->dir, cost, sint, cp, sp);
+}
+
+static void iso_dir(rng_t *g, real d[3]) {
+  real cost = R(2) * u01(g);
+  cost = R(1) - cost;
+  real st2 = cost * cost;
+  st2 = R(1) - st2;
+  real sint = ggo_sqrt(st2 > R(0) ? st2 : R(0));
+  real sp, cp;
+  ggo_sincos_turn(u01(g), &sp, &cp);
+  d[0] = sint * cp;
+  d[1] = sint * sp;
+  d[2] = cost;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Source                                                                    */
+/* ------------------------------------------------------------------------ */
+static void rot_apply(const real m[9], const real v[3], real o[3]) {
+  for (int i = 0; i < 3; ++i) {
+    real a = m[3 * i] * v[0];
+    a = a + m[3 * i + 1] * v[1];
+    a = a + m[3 * i + 2] * v[2];
+    o[i] = a;
+  }
+}
+
+static int accept_dir(const scene_t *s, const real p[3], const real d[3]) {
+  for (int b = 0; b < s->src.n_accept; ++b) {
+    const real *bx = s->acc_box + 6 * b;
+    if (entry_distance(p, d, bx, bx + 3) < R(INFINITY)) return 1;
+  }
+  return 0;
+}
+
+static void sample_direction(const scene_t *s, const real p[3], rng_t *g, real d[3]) {
+  if (s->src.dir_type == GG_DIR_ISO) {
+    real u = u01(g);
+    real cost = s->s_cos_tmin - s->s_cos_tmax;
+    cost = u * cost;
+    cost = s->s_cos_tmin - cost;
+    real st2 = cost * cost;
+    st2 = R(1) - st2;
+    real sint = ggo_sqrt(st2 > R(0) ? st2 : R(0));
+    real f = s->s_dphi_turn * u01(g);
+    f = s->s_phi0_turn + f;
+    f = f - (real)floor((double)f);
+    real sp, cp;
+    ggo_sincos_turn(f, &sp, &cp);
+    d[0] = -(sint * cp);
+    d[1] = -(sint * sp);
+    d[2] = -cost;
+  } else if (s->src.dir_type == GG_DIR_MOMENTUM) {
+    d[0] = s->s_mom[0];
+    d[1] = s->s_mom[1];
+    d[2] = s->s_mom[2];
+  } else {
+    real v[3];
+    for (int a = 0; a < 3; ++a) v[a] = s->s_focus[a] - p[a];
+    real n2 = v[0] * v[0];
+    n2 = n2 + v[1] * v[1];
+    n2 = n2 + v[2] * v[2];
+    real rn = R(1) / ggo_sqrt(n2);
+    for (int a = 0; a < 3; ++a) d[a] = v[a] * rn;
+  }
+}
+
+static int sample_primary(const scene_t *s, rng_t *g, photon_t *ph, tally_t *t) {
+  real loc[3] = {R(0), R(0), R(0)};
+  int pt = s->src.pos_type;
+  if (pt == GG_POS_BOX) {
+    for (int a = 0; a < 3; ++a) {
+      real u = R(2) * u01(g);
+      u = u - R(1);
+      loc[a] = u * s->s_half[a];
+    }
+  } else if (pt == GG_POS_SPHERE || pt == GG_POS_DISC) {
+    int it = 0;
+    for (;;) {
+      real r2 = R(0);
+      int na = (pt == GG_POS_SPHERE) ? 3 : 2;
+      for (int a = 0; a < na; ++a) {
+        real u = R(2) * u01(g);
+        u = u - R(1);
+        loc[a] = u * s->s_radius;
+        r2 = r2 + loc[a] * loc[a];
+      }
+      real rr = s->s_radius * s->s_radius;
+      if (r2 <= rr) break;
+      if (++it >= LOOP_CAP) {
+        t->cnt[GG_CNT_LOOP_CAPPED]++;
+        break;
+      }
+    }
+  }
+  real off[3];
+  rot_apply(s->s_rot, loc, off);
+  for (int a = 0; a < 3; ++a) ph->pos[a] = s->s_t[a] + off[a];
+  /* direction, with the acceptance loop of GateSingleParticleSource */
+  int tries = 0;
+  for (;;) {
+    sample_direction(s, ph->pos, g, ph->dir);
+    if (s->src.n_accept == 0 || accept_dir(s, ph->pos, ph->dir)) break;
+    t->cnt[GG_CNT_SKIPPED]++;
+    if (++tries > s->src.max_rejection) return GG_ERR_DOMAIN;
+  }
+  /* energy */
+  real e;
+  int et = s->src.ene_type;
+  if (et == GG_ENE_MONO) {
+    e = s->s_mono;
+  } else if (et == GG_ENE_RANGE) {
+    real w = s->s_ehi - s->s_elo;
+    w = w * u01(g);
+    e = s->s_elo + w;
+  } else {
+    real p = u01(g);
+    int i = 0;
+    while (i < s->src.n_spec - 1 && p >= s->s_spec_cdf[i]) ++i;
+    if (et == GG_ENE_LINES) {
+      e = s->s_spec_e[i];
+    } else {
+      real a = s->s_spec_e[i];
+      real w = s->s_spec_e[i + 1] - a;
+      w = w * u01(g);
+      e = a + w;
+    }
+  }
+  ph->alive = 1;
+  ph->can_enter = 1;
+  ph->in_image = 0;
+  set_energy(s, ph, e);
+  return GG_OK;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Transport of one history                                                  */
+/* ------------------------------------------------------------------------ */
+static int inside_box(const real p[3], const real lo[3], const real hi[3]) {
+  for (int a = 0; a < 3; ++a)
+    if (p[a] < lo[a] || p[a] > hi[a]) return 0;
+  return 1;
+}
+
+static void start_photon(const scene_t *s, photon_t *ph) {
+  if (inside_box(ph->pos, s->bmin, s->bmax)) {
+    ph->in_image = 1;
+    ph->t_exit = exit_distance(ph->pos, ph->dir, s->bmin, s->bmax);
+  } else {
+    ph->in_image = 0;
+    ph->can_enter = 1;
+  }
+}
+
+static void interact(const scene_t *s, photon_t *ph, int mat, rng_t *g, tally_t *t, hlist_t *l,
+                     int scored, uint32_t vox, photon_t *sec, int *has_sec) {
+  int c = s->mat_comp[mat];
+  const real *cu = s->cum + (size_t)c * 3 * s->n_e;
+  real r = u01(g);
+  real fc = interp_row(cu, ph->ei);
+  if (r < fc) {
+    real ed;
+    compton(s, ph, g, t, &ed);
+    if (scored) deposit(l, t, vox, ed);
+    return;
+  }
+  real fp = interp_row(cu + s->n_e, ph->ei);
+  if (r < fp) {
+    if (scored) deposit(l, t, vox, ph->e);
+    ph->alive = 0;
+    return;
+  }
+  real fr = interp_row(cu + 2 * s->n_e, ph->ei);
+  if (r < fr) {
+    rayleigh(s, c, ph, g, t);
+    return;
+  }
+  /* pair: both leptons stopped at creation, positron annihilates at rest */
+  real ekin = ph->e - R(2.0 * MC2);
+  if (scored) deposit(l, t, vox, ekin);
+  real d[3];
+  iso_dir(g, d);
+  if (*has_sec) {
+    t->cnt[GG_CNT_STACK_OVERFLOW]++;
+  } else {
+    *sec = *ph;
+    sec->dir[0] = -d[0];
+    sec->dir[1] = -d[1];
+    sec->dir[2] = -d[2];
+    set_energy(s, sec, R(MC2));
+    *has_sec = 1;
+  }
+  ph->dir[0] = d[0];
+  ph->dir[1] = d[1];
+  ph->dir[2] = d[2];
+  set_energy(s, ph, R(MC2));
+  t->cnt[GG_CNT_SECONDARIES] += 2;
+}
+
+static void transport_photon(const scene_t *s, photon_t *ph, rng_t *g, tally_t *t, hlist_t *l,
+                             photon_t *sec, int *has_sec) {
+  int steps = 0;
+  while (ph->alive) {
+    if (++steps > STEP_CAP) {
+      /* termination guard: a photon never needs this many steps */
+      t->cnt[GG_CNT_LOOP_CAPPED]++;
+      ph->alive = 0;
+      break;
+    }
+    if (ph->in_image) {
+      real u = u01_open0(g);
+      real sd = -ggo_log(u);
+      sd = sd * ph->inv_mumax;
+      if (sd >= ph->t_exit) {
+        for (int a = 0; a < 3; ++a) ph->pos[a] = ph->pos[a] + ph->t_exit * ph->dir[a];
+        ph->in_image = 0;
+        ph->can_enter = 0;
+        continue;
+      }
+      ph->t_exit = ph->t_exit - sd;
+      for (int a = 0; a < 3; ++a) ph->pos[a] = ph->pos[a] + sd * ph->dir[a];
+      t->cnt[GG_CNT_WOODCOCK_STEPS]++;
+      int ix = (int)((ph->pos[0] - s->bmin[0]) * s->inv_sp[0]);
+      int iy = (int)((ph->pos[1] - s->bmin[1]) * s->inv_sp[1]);
+      int iz = (int)((ph->pos[2] - s->bmin[2]) * s->inv_sp[2]);
+      ix = ix < 0 ? 0 : (ix >= s->nx ? s->nx - 1 : ix);
+      iy = iy < 0 ? 0 : (iy >= s->ny ? s->ny - 1 : iy);
+      iz = iz < 0 ? 0 : (iz >= s->nz ? s->nz - 1 : iz);
+      uint32_t v = (uint32_t)ix + (uint32_t)s->nx * ((uint32_t)iy + (uint32_t)s->ny * (uint32_t)iz);
+      int m = s->labels[v];
+      real mu = interp_row(s->sig + (size_t)s->mat_comp[m] * s->n_e, ph->ei);
+      mu = s->mat_rho[m] * mu;
+      real u2 = u01(g);
+      if (u2 * ph->mumax >= mu) continue;
+      t->cnt[GG_CNT_REAL_INTERACTIONS]++;
+      interact(s, ph, m, g, t, l, 1, v, sec, has_sec);
+      if (ph->alive && ph->in_image) ph->t_exit = exit_distance(ph->pos, ph->dir, s->bmin, s->bmax);
+    } else {
+      t->cnt[GG_CNT_WORLD_STEPS]++;
+      real tin = ph->can_enter ? entry_distance(ph->pos, ph->dir, s->bmin, s->bmax) : R(INFINITY);
+      real wlo[3] = {-s->whalf[0], -s->whalf[1], -s->whalf[2]};
+      real tout = exit_distance(ph->pos, ph->dir, wlo, s->whalf);
+      int wm = s->world_mat;
+      real mu = interp_row(s->sig + (size_t)s->mat_comp[wm] * s->n_e, ph->ei);
+      mu = s->mat_rho[wm] * mu;
+      real u = u01_open0(g);
+      real sd = -ggo_log(u);
+      sd = sd / mu;
+      if (sd < tin && sd < tout) {
+        for (int a = 0; a < 3; ++a) ph->pos[a] = ph->pos[a] + sd * ph->dir[a];
+        interact(s, ph, wm, g, t, l, 0, 0, sec, has_sec);
+        ph->can_enter = 1;
+      } else if (tin <= tout) {
+        for (int a = 0; a < 3; ++a) ph->pos[a] = ph->pos[a] + tin * ph->dir[a];
+        ph->in_image = 1;
+        ph->t_exit = exit_distance(ph->pos, ph->dir, s->bmin, s->bmax);
+      } else {
+        ph->alive = 0;
+        t->cnt[GG_CNT_ESCAPED]++;
+      }
+    }
+  }
+}
+
+static int run_history(const scene_t *s, uint64_t seed, uint64_t h, tally_t *t) {
+  rng_t g;
+  rng_init(&g, seed, h, 0u);
+  hlist_t l;
+  l.n = 0;
+  photon_t ph, sec;
+  int has_sec = 0;
+  int st = sample_primary(s, &g, &ph, t);
+  if (st != GG_OK) return st;
+  t->cnt[GG_CNT_HISTORIES]++;
+  start_photon(s, &ph);
+  for (;;) {
+    transport_photon(s, &ph, &g, t, &l, &sec, &has_sec);
+    if (!has_sec) break;
+    ph = sec;
+    has_sec = 0;
+    start_photon(s, &ph);
+  }
+  hlist_flush(&l, t);
+  return GG_OK;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Scene set-up and driver                                                   */
+/* ------------------------------------------------------------------------ */
+static real *conv_f(const float *src, size_t n) {
+  real *d = (real *)malloc(n * sizeof(real));
+  for (size_t i = 0; i < n; ++i) d[i] = (real)src[i];
+  return d;
+}
+
+static real *conv_d(const double *src, size_t n) {
+  real *d = (real *)malloc((n ? n : 1) * sizeof(real));
+  for (size_t i = 0; i < n; ++i) d[i] = (real)src[i];
+  return d;
+}
+
+static void scene_free(scene_t *s) {
+  free(s->sig); free(s->cum); free(s->ray_amax); free(s->ray_inv); free(s->mat_rho);
+  free(s->mat_comp); free(s->maj); free(s->s_spec_e); free(s->s_spec_cdf); free(s->acc_box);
+}
+
+static int scene_init(scene_t *s, const gg_tables_desc *tb, const gg_volume_desc *vol,
+                      const gg_world_desc *w, const gg_source_desc *src) {
+  memset(s, 0, sizeof(*s));
+  s->n_e = tb->n_e; s->n_comp = tb->n_comp; s->n_rinv = tb->n_rinv; s->n_mat = tb->n_mat;
+  s->ln_emin = (real)tb->ln_emin; s->inv_dln = (real)tb->inv_dln;
+  s->e_min = (real)tb->e_min; s->e_max = (real)tb->e_max;
+  s->sig = conv_f(tb->sig, (size_t)tb->n_comp * tb->n_e);
+  s->cum = conv_f(tb->cum, (size_t)tb->n_comp * 3 * tb->n_e);
+  s->ray_amax = conv_f(tb->ray_amax, (size_t)tb->n_comp * tb->n_e);
+  s->ray_inv = conv_f(tb->ray_inv, (size_t)tb->n_comp * tb->n_rinv);
+  s->mat_rho = conv_f(tb->mat_rho, (size_t)tb->n_mat);
+  s->mat_comp = (int *)malloc(sizeof(int) * tb->n_mat);
+  for (int i = 0; i < tb->n_mat; ++i) s->mat_comp[i] = tb->mat_comp[i];
+  s->nx = vol->dims[0]; s->ny = vol->dims[1]; s->nz = vol->dims[2];
+  for (int a = 0; a < 3; ++a) {
+    s->bmin[a] = (real)vol->corner[a];
+    s->bmax[a] = (real)(vol->corner[a] + (double)vol->dims[a] * vol->spacing[a]);
+    s->inv_sp[a] = (real)(1.0 / vol->spacing[a]);
+    s->whalf[a] = (real)w->half_size[a];
+  }
+  s->labels = vol->labels;
+  s->maj = conv_f(vol->majorant, (size_t)tb->n_e);
+  s->world_mat = w->material;
+  s->src = *src;
+  for (int a = 0; a < 3; ++a) {
+    s->s_t[a] = (real)src->translation[a];
+    s->s_half[a] = (real)src->half_size[a];
+    s->s_focus[a] = (real)src->focus[a];
+  }
+  for (int i = 0; i < 9; ++i) s->s_rot[i] = (real)src->rotation[i];
+  s->s_radius = (real)src->radius;
+  s->s_cos_tmin = (real)cos(src->theta[0]);
+  s->s_cos_tmax = (real)cos(src->theta[1]);
+  s->s_phi0_turn = (real)(src->phi[0] / (2.0 * M_PI));
+  s->s_dphi_turn = (real)((src->phi[1] - src->phi[0]) / (2.0 * M_PI));
+  double mn = sqrt(src->momentum[0] * src->momentum[0] + src->momentum[1] * src->momentum[1] +
+                   src->momentum[2] * src->momentum[2]);
+  for (int a = 0; a < 3; ++a) s->s_mom[a] = (real)(mn > 0 ? src->momentum[a] / mn : 0.0);
+  s->s_mono = (real)src->mono;
+  s->s_elo = (real)src->e_lo;
+  s->s_ehi = (real)src->e_hi;
+  int ns = src->n_spec;
+  s->s_spec_e = conv_d(src->spec_e, (size_t)(src->ene_type == GG_ENE_HISTOGRAM ? ns + 1 : ns));
+  s->s_spec_cdf = conv_d(src->spec_cdf, (size_t)ns);
+  s->acc_box = conv_d(src->accept_boxes, (size_t)6 * src->n_accept);
+  return GG_OK;
+}
+
+typedef struct {
+  const scene_t *s;
+  uint64_t seed, h0, h1;
+  tally_t t;
+  int status;
+} worker_t;
+
+static void *worker_main(void *arg) {
+  worker_t *w = (worker_t *)arg;
+  for (uint64_t h = w->h0; h < w->h1; ++h) {
+    int st = run_history(w->s, w->seed, h, &w->t);
+    if (st != GG_OK) {
+      w->status = st;
+      break;
+    }
+  }
+  return NULL;
+}
+
+/* Runs histories [first, first + n) in batches of `batch`, adding the fixed
+   point batch sums into the float64 images edep / edep2 (either may be
+   NULL for the squared image), and adding to counters[GG_N_COUNTERS]. */
+int GGO_PREFIX(run_dose)(const gg_tables_desc *tb, const gg_volume_desc *vol, const gg_world_desc *w,
+                         const gg_source_desc *src, uint64_t seed, uint64_t first, uint64_t n,
+                         uint64_t batch, int n_threads, double *edep, double *edep2,
+                         uint64_t *counters) {
+  scene_t s;
+  scene_init(&s, tb, vol, w, src);
+  size_t nv = (size_t)s.nx * s.ny * s.nz;
+  uint64_t *acc_e = (uint64_t *)calloc(nv, sizeof(uint64_t));
+  uint64_t *acc_e2 = edep2 ? (uint64_t *)calloc(nv, sizeof(uint64_t)) : NULL;
+  if (n_threads < 1) n_threads = 1;
+  if (batch == 0) batch = n ? n : 1;
+  worker_t *ws = (worker_t *)calloc((size_t)n_threads, sizeof(worker_t));
+  pthread_t *th = (pthread_t *)calloc((size_t)n_threads, sizeof(pthread_t));
+  int status = GG_OK;
+  for (uint64_t b0 = first; b0 < first + n && status == GG_OK; b0 += batch) {
+    uint64_t b1 = b0 + batch < first + n ? b0 + batch : first + n;
+    uint64_t per = (b1 - b0 + (uint64_t)n_threads - 1) / (uint64_t)n_threads;
+    for (int i = 0; i < n_threads; ++i) {
+      ws[i].s = &s;
+      ws[i].seed = seed;
+      ws[i].h0 = b0 + per * (uint64_t)i < b1 ? b0 + per * (uint64_t)i : b1;
+      ws[i].h1 = ws[i].h0 + per < b1 ? ws[i].h0 + per : b1;
+      ws[i].t.acc_e = acc_e;
+      ws[i].t.acc_e2 = acc_e2;
+      ws[i].status = GG_OK;
+      if (n_threads > 1) pthread_create(&th[i], NULL, worker_main, &ws[i]);
+      else worker_main(&ws[i]);
+    }
+    if (n_threads > 1)
+      for (int i = 0; i < n_threads; ++i) pthread_join(th[i], NULL);
+    for (int i = 0; i < n_threads; ++i)
+      if (ws[i].status != GG_OK) status = ws[i].status;
+    for (size_t v = 0; v < nv; ++v) {
+      if (acc_e[v]) {
+        edep[v] += (double)acc_e[v] * 2.3283064365386963e-10;
+        acc_e[v] = 0;
+      }
+      if (acc_e2 && acc_e2[v]) {
+        edep2[v] += (double)acc_e2[v] * 2.3283064365386963e-10;
+        acc_e2[v] = 0;
+      }
+    }
+  }
+  for (int i = 0; i < n_threads; ++i)
+    for (int c = 0; c < GG_N_COUNTERS; ++c) counters[c] += ws[i].t.cnt[c];
+  free(ws);
+  free(th);
+  free(acc_e);
+  free(acc_e2);
+  scene_free(&s);
+  return status;
+}
+
+/* ---- small exported probes for the unit tests ---- */
+void GGO_PREFIX(philox)(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]) {
+  philox4x32_10(ctr, key, out);
+}
+double GGO_PREFIX(log)(double x) { return (double)ggo_log((real)x); }
+double GGO_PREFIX(exp)(double x) { return (double)ggo_exp((real)x); }
+void GGO_PREFIX(sincos_turn)(double f, double *s, double *c) {
+  real a, b;
+  ggo_sincos_turn((real)f, &a, &b);
+  *s = (double)a;
+  *c = (double)b;
+}
+/* Samples n Klein-Nishina scatterings at energy e (MeV): writes E'/E and cos(theta). */
+void GGO_PREFIX(sample_compton)(double e, uint64_t seed, int n, double *eps_out, double *cost_out) {
+  scene_t s;
+  memset(&s, 0, sizeof(s));
+  static real maj2[2] = {R(1), R(1)};
+  s.n_e = 2;
+  s.maj = maj2;
+  s.ln_emin = R(-10);
+  s.inv_dln = R(0.01);
+  s.e_min = R(0);
+  tally_t t;
+  memset(&t, 0, sizeof(t));
+  for (int i = 0; i < n; ++i) {
+    rng_t g;
+    rng_init(&g, seed, (uint64_t)i, 0u);
+    photon_t ph;
+    memset(&ph, 0, sizeof(ph));
+    ph.dir[2] = R(1);
+    ph.alive = 1;
+    set_energy(&s, &ph, (real)e);
+    real ed;
+    compton(&s, &ph, &g, &t, &ed);
+    eps_out[i] = (double)ph.e / e;
+    cost_out[i] = (double)ph.dir[2];
+  }
+}

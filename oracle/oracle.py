@@ -1,0 +1,94 @@
+"""ctypes front-end of the CPU oracle (test infrastructure only).
+
+Only the tests, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
+``bench.py`` import this module.  It runs a :class:`opengate_gb300.scene.Scene`
+through ``libggo32.so`` / ``libggo64.so`` and returns the float64 edep and
+edep-squared images plus the counters, in the same layout as the GPU path.
+"""
+
+import ctypes
+import pathlib
+import sys
+
+import numpy as np
+
+HERE = pathlib.Path(__file__).resolve().parent
+sys.path.insert(0, str(HERE.parent))
+
+from opengate_gb300 import _capi as C  # noqa: E402
+
+from . import build_oracle  # noqa: E402
+
+_libs = {}
+
+
+def lib(precision=32):
+    if precision not in _libs:
+        build_oracle.build()
+        L = ctypes.CDLL(str(HERE / "_build" / f"libggo{precision}.so"))
+        pre = f"ggo{precision}_"
+        fn = getattr(L, pre + "run_dose")
+        fn.restype = ctypes.c_int
+        fn.argtypes = [ctypes.POINTER(C.TablesDesc), ctypes.POINTER(C.VolumeDesc),
+                       ctypes.POINTER(C.WorldDesc), ctypes.POINTER(C.SourceDesc), ctypes.c_uint64,
+                       ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int,
+                       ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double),
+                       ctypes.POINTER(ctypes.c_uint64)]
+        for name in ("log", "exp"):
+            f = getattr(L, pre + name)
+            f.restype = ctypes.c_double
+            f.argtypes = [ctypes.c_double]
+        f = getattr(L, pre + "sincos_turn")
+        f.argtypes = [ctypes.c_double, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
+        f = getattr(L, pre + "philox")
+        f.argtypes = [ctypes.POINTER(ctypes.c_uint32)] * 3
+        f = getattr(L, pre + "sample_compton")
+        f.argtypes = [ctypes.c_double, ctypes.c_uint64, ctypes.c_int,
+                      ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
+        _libs[precision] = L
+    return _libs[precision]
+
+
+def run_dose(scene, n, seed, first=0, batch=0, threads=1, precision=32, squared=True):
+    """Oracle run of histories [first, first + n): (edep, edep2 or None, counters dict)."""
+    L = lib(precision)
+    nv = scene.n_voxels
+    edep = np.zeros(nv, dtype=np.float64)
+    edep2 = np.zeros(nv, dtype=np.float64) if squared else None
+    cnt = np.zeros(C.GG_N_COUNTERS, dtype=np.uint64)
+    st = getattr(L, f"ggo{precision}_run_dose")(
+        ctypes.byref(scene.tables_desc), ctypes.byref(scene.volume_desc), ctypes.byref(scene.world_desc),
+        ctypes.byref(scene.source_desc), seed, first, n, batch, threads,
+        C.ptr(edep, ctypes.c_double), C.ptr(edep2, ctypes.c_double), C.ptr(cnt, ctypes.c_uint64))
+    if st != 0:
+        raise RuntimeError(f"oracle run failed with status {st}")
+    shape = scene.labels.shape
+    counters = {name: int(cnt[i]) for i, name in enumerate(C.COUNTER_NAMES)}
+    return edep.reshape(shape), (edep2.reshape(shape) if squared else None), counters
+
+
+def philox(ctr, key, precision=32):
+    L = lib(precision)
+    c = (ctypes.c_uint32 * 4)(*ctr)
+    k = (ctypes.c_uint32 * 2)(*key)
+    o = (ctypes.c_uint32 * 4)()
+    getattr(L, f"ggo{precision}_philox")(c, k, o)
+    return list(o)
+
+
+def math_fn(name, x, precision=32):
+    return getattr(lib(precision), f"ggo{precision}_{name}")(float(x))
+
+
+def sincos_turn(f, precision=32):
+    s, c = ctypes.c_double(), ctypes.c_double()
+    getattr(lib(precision), f"ggo{precision}_sincos_turn")(float(f), ctypes.byref(s), ctypes.byref(c))
+    return s.value, c.value
+
+
+def sample_compton(e, n, seed=1, precision=32):
+    eps = np.zeros(n)
+    cost = np.zeros(n)
+    getattr(lib(precision), f"ggo{precision}_sample_compton")(
+        float(e), seed, n, C.ptr(eps, ctypes.c_double), C.ptr(cost, ctypes.c_double))
+    return eps, cost
