@@ -1,0 +1,324 @@
+"""Benchmark: primaries/s of voxelised photon transport with DoseActor scoring.
+
+Workload (one step): the heterogeneous CT phantom - 256 x 256 x 160 int16 HU
+image, 1.2 mm voxels, ten-interval HU table, point source at 100 cm SSD with a
+10 x 10 cm field and a 60-bin E*exp(-E/1.5 MeV) spectrum on [0.1, 6] MeV -
+1e8 primaries per step, FP32 transport, FP64 edep and edep-squared images
+(history-by-history).  Inputs are synthetic and seeded.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line (rank 0).  ``value`` is device-timed (CUDA events on
+the launching stream, inputs resident); ``e2e`` goes through the C ABI with
+host buffers (scene upload and image download inside the timed region).
+``--impl reference`` times the CPU restatement of the path (the reference's
+Geant4 stack cannot be installed here) on all host cores.
+"""
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+METRIC = "primaries/s at matched sigma (plain GPU transport, CT phantom dose)"
+UNIT = "primaries/s"
+PRIMARIES_PER_STEP = 100_000_000
+WORKLOAD = "ct_phantom_256x256x160_1.2mm_ssd100_field10x10_spectrum60_0.1-6MeV"
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """Samples SM clocks and throttle reasons with nvidia-smi while running."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.rows = []
+        self._stop = threading.Event()
+        self._th = None
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(
+                    ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+                     "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=5).stdout
+                for line in out.strip().splitlines():
+                    self.rows.append([x.strip() for x in line.split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._th = threading.Thread(target=self._run, daemon=True)
+        self._th.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        if self._th:
+            self._th.join(timeout=10)
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in self.rows:
+            for name, v in zip(names, r[4:8]):
+                if v.strip().lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.rows)}
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def dist_init(ws, use_cuda):
+    if ws <= 1:
+        return None
+    import torch.distributed as dist
+
+    dist.init_process_group("nccl" if use_cuda else "gloo")
+    return dist
+
+
+def dist_max(dist, value, use_cuda):
+    if dist is None:
+        return value
+    import torch
+
+    t = torch.tensor([value], dtype=torch.float64, device="cuda" if use_cuda else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def mean_relative_uncertainty(edep, edep2, n, frac=0.1):
+    """Mean history-by-history relative sigma over voxels above frac * max edep."""
+    mean = edep / n
+    var = np.clip((edep2 / n - mean * mean) / (n - 1), 0, None)
+    sel = edep > frac * edep.max()
+    rel = np.sqrt(var[sel]) / mean[sel]
+    return float(rel.mean()) if sel.any() else None
+
+
+def cpu_sample(scene, threads, target_s=10.0, seed=424242):
+    """Times the CPU restatement of the path on a bounded sample."""
+    from oracle import oracle as O
+
+    # each oracle call has a fixed cost (table conversion, tally allocation and
+    # the final image flush); grow the sample until it dominates, then size the
+    # timed sample from the marginal rate
+    n = 200_000
+    t_prev, n_prev = None, None
+    while True:
+        t0 = time.perf_counter()
+        O.run_dose(scene, n, seed, threads=threads)
+        dt = time.perf_counter() - t0
+        if dt > 0.25 * target_s or n >= 5e7:
+            break
+        t_prev, n_prev = dt, n
+        n *= 4
+    rate = (n - n_prev) / max(dt - t_prev, 1e-6) if n_prev else n / dt
+    n2 = int(min(max(n, rate * target_s), 4e8))
+    t0 = time.perf_counter()
+    O.run_dose(scene, n2, seed + 1, threads=threads)
+    dt2 = time.perf_counter() - t0
+    return n2 / dt2, n2, dt2
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    from opengate_gb300 import workloads as W
+
+    scene, _ = W.ct_phantom()
+    threads = os.cpu_count() or 1
+    rates = []
+    t_all = time.perf_counter()
+    for _ in range(args.warmup):
+        cpu_sample(scene, threads, target_s=1.0)
+    samples = []
+    for _ in range(args.steps):
+        r, n, dt = cpu_sample(scene, threads, target_s=8.0)
+        rates.append(r)
+        samples.append(n)
+    value = float(np.median(rates))
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": PRIMARIES_PER_STEP / value * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded CT phantom)",
+        "config": {"workload": WORKLOAD, "primaries_per_step": PRIMARIES_PER_STEP,
+                   "note": "CPU restatement of the path (C, pthreads); Geant4/opengate_core not installable offline"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{int(np.median(samples))} primaries of the same workload per step, all host threads"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "wall_s": time.perf_counter() - t_all,
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args):
+    ws, rank, local = dist_env()
+    import torch
+
+    use_cuda = torch.cuda.is_available()
+    if not use_cuda:
+        raise RuntimeError("bench.py needs a CUDA GPU for --impl ours")
+    torch.cuda.set_device(local)
+    dist = dist_init(ws, use_cuda)
+    from opengate_gb300 import _capi as C
+    from opengate_gb300 import workloads as W
+    from opengate_gb300.engine import DoseEngine
+
+    scene, _ = W.ct_phantom()
+    n = args.primaries
+    eng = DoseEngine(scene, device=local, precision=32, batch=args.batch)
+    l2_flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=f"cuda:{local}")
+    # history ranges are disjoint across ranks and steps
+    def first_of(step):
+        return ((rank * (args.warmup + args.steps + 1)) + step) * n
+
+    for w in range(args.warmup):
+        eng.reset()
+        eng.run(n, args.seed, first_of(w))
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    dev_ms = []
+    launches = 0
+    counters = None
+    t0 = time.perf_counter()
+    with ClockSampler(local) as clk:
+        for k in range(args.steps):
+            l2_flush.zero_()
+            torch.cuda.synchronize()
+            eng.reset()
+            eng.run(n, args.seed, first_of(args.warmup + k))
+            tg, tt, tf, nl = eng.last_kernel_ms()
+            dev_ms.append(tg + tt + tf)
+            launches += nl
+            if k == args.steps - 1:
+                counters = eng.counters()
+                transport_ms = tt
+                transport_launches = nl // 3
+                stage_ms = {"generate": tg, "transport": tt, "flush": tf}
+        torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    if dist:
+        dist.barrier()
+    total_ms = dist_max(dist, float(np.sum(dev_ms)), use_cuda)
+    value = ws * n * args.steps / (total_ms / 1e3)
+
+    # sigma reached by one step (mean relative uncertainty, voxels > 10 % max)
+    edep, edep2 = eng.edep(), eng.edep_squared()
+    sigma = mean_relative_uncertainty(edep, edep2, n)
+
+    # e2e through the C ABI with host buffers: scene upload (H2D), run, image download (D2H)
+    h2d = scene.labels.nbytes + scene._sig.nbytes + scene._cum.nbytes + scene._ray_amax.nbytes + \
+        scene._ray_cum.nbytes + scene.majorant.nbytes
+    d2h = 2 * scene.n_voxels * 8
+    torch.cuda.synchronize()
+    e2e_t = []
+    for k in range(max(1, min(args.steps, 3))):
+        t1 = time.perf_counter()
+        eng.upload()
+        eng.run(n, args.seed, first_of(args.warmup + args.steps + k))
+        a, b = eng.edep(), eng.edep_squared()
+        e2e_t.append(time.perf_counter() - t1)
+    e2e_s = dist_max(dist, float(np.mean(e2e_t)), use_cuda)
+    e2e_value = ws * n / e2e_s
+
+    # roofline of the transport kernel: algorithmic bytes per launch
+    peak, peak_kind = measured_peaks()
+    bytes_alg = 32.0 * counters["woodcock_steps"] + 64.0 * counters["tally_entries"]
+    achieved = bytes_alg / (transport_ms / 1e3) / 1e9
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "traffic": args.traffic,
+                "peak_kind": peak_kind, "kernel": "k_transport<float>",
+                "bytes_alg_per_step": bytes_alg,
+                "units": {"woodcock_steps": counters["woodcock_steps"], "tally_entries": counters["tally_entries"],
+                          "transport_launches_per_step": transport_launches},
+                "stage_ms_per_step": stage_ms}
+
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        r, ns, dt = cpu_sample(scene, threads, target_s=args.cpu_seconds)
+        cpu = {"value": r, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"{ns} primaries of the same workload, {dt:.1f} s on {threads} host threads"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded CT phantom)",
+            "config": {"workload": WORKLOAD, "primaries_per_step": n, "tally": "fp64 edep + edep^2, history-by-history",
+                       "l2": "flushed between steps (256 MiB write)", "batch": args.batch,
+                       "parallelism": f"replicas x{ws}, disjoint history ranges"},
+            "sigma": {"mean_relative_uncertainty_gt10pct_max": sigma, "primaries": n},
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+            "roofline": roofline,
+            "cpu_baseline": cpu,
+            "clocks": clk.summary(),
+            "gpu_launches": int(launches),
+            "wall_s": wall,
+        }
+        print(json.dumps(line), flush=True)
+    eng.close()
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--primaries", type=int, default=PRIMARIES_PER_STEP)
+    ap.add_argument("--batch", type=int, default=1 << 27)
+    ap.add_argument("--seed", type=int, default=20240611)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--traffic", type=float, default=None,
+                    help="DRAM bytes per transport launch from an ncu capture (reported as-is)")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -103,9 +103,10 @@ typedef struct {
   int32_t n_comp;
   const float *sig;      /* [n_comp][n_e] mm^-1 per g/cm3 */
   const float *cum;      /* [n_comp][3][n_e] Compton, +photo, +Rayleigh */
-  const float *ray_amax; /* [n_comp][n_e] */
-  int32_t n_rinv;
-  const float *ray_inv; /* [n_comp][n_rinv] x^2 in 1/Angstrom^2 */
+  const float *ray_amax; /* [n_comp][n_e] Rayleigh cumulative reached at E (x^2 = (E/hc)^2) */
+  int32_t n_ray;         /* Rayleigh x^2 grid points */
+  const float *ray_x2;   /* [n_ray] increasing x^2 nodes in 1/Angstrom^2, ray_x2[0] = 0 */
+  const float *ray_cum; /* [n_comp][n_ray] normalised cumulative of F^2 dx^2 at the nodes */
   int32_t n_mat;
   const int32_t *mat_comp; /* [n_mat] */
   const float *mat_rho;    /* [n_mat] g/cm3 */
@@ -162,6 +163,8 @@ typedef struct {
   int32_t blocks_per_sm; /* 0 = default */
   int32_t chunk;      /* histories a warp claims per queue fetch, 0 = default */
   int64_t batch;      /* histories per tally batch, 0 = default */
+  int32_t refill_min;   /* 1..32: lanes waiting for a history that trigger a refill phase, 0 = default */
+  int32_t interact_min; /* 1..32: pending collisions that trigger an interaction phase, 0 = default */
 } gg_device_opts;
 
 int gg_create(const gg_device_opts *opts, gg_ctx **out);
@@ -184,8 +187,11 @@ int gg_run(gg_ctx *ctx, uint64_t n_histories, uint64_t seed, uint64_t first_hist
 int gg_synchronize(gg_ctx *ctx);
 int gg_get_image(gg_ctx *ctx, int32_t which, double *out, size_t n);
 int gg_get_counters(gg_ctx *ctx, uint64_t *out, size_t n);
-/* Elapsed device time of the transport kernels of the last gg_run, ms. */
-int gg_last_kernel_ms(gg_ctx *ctx, double *transport_ms, double *flush_ms, int32_t *launches);
+/* Device time (CUDA events on the context's stream) of the last gg_run, ms:
+   source stage, transport kernel and tally flush, summed over batches, and
+   the number of kernel launches. */
+int gg_last_kernel_ms(gg_ctx *ctx, double *generate_ms, double *transport_ms, double *flush_ms,
+                      int32_t *launches);
 
 #ifdef __cplusplus
 }

@@ -45,8 +45,9 @@ class TablesDesc(ctypes.Structure):
     _fields_ = [
         ("n_e", ctypes.c_int32), ("ln_emin", ctypes.c_float), ("inv_dln", ctypes.c_float),
         ("e_min", ctypes.c_float), ("e_max", ctypes.c_float), ("n_comp", ctypes.c_int32),
-        ("sig", _f32p), ("cum", _f32p), ("ray_amax", _f32p), ("n_rinv", ctypes.c_int32),
-        ("ray_inv", _f32p), ("n_mat", ctypes.c_int32), ("mat_comp", _i32p), ("mat_rho", _f32p),
+        ("sig", _f32p), ("cum", _f32p), ("ray_amax", _f32p), ("n_ray", ctypes.c_int32),
+        ("ray_x2", _f32p), ("ray_cum", _f32p), ("n_mat", ctypes.c_int32), ("mat_comp", _i32p),
+        ("mat_rho", _f32p),
     ]
 
 
@@ -78,6 +79,7 @@ class DeviceOpts(ctypes.Structure):
     _fields_ = [
         ("device", ctypes.c_int32), ("precision", ctypes.c_int32), ("block_size", ctypes.c_int32),
         ("blocks_per_sm", ctypes.c_int32), ("chunk", ctypes.c_int32), ("batch", ctypes.c_int64),
+        ("refill_min", ctypes.c_int32), ("interact_min", ctypes.c_int32),
     ]
 
 
@@ -105,7 +107,7 @@ PROTOTYPES = [
     ("gg_get_image", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, _f64p, ctypes.c_size_t]),
     ("gg_get_counters", ctypes.c_int, [ctypes.c_void_p, _u64p, ctypes.c_size_t]),
     ("gg_last_kernel_ms", ctypes.c_int,
-     [ctypes.c_void_p, _f64p, _f64p, ctypes.POINTER(ctypes.c_int32)]),
+     [ctypes.c_void_p, _f64p, _f64p, _f64p, ctypes.POINTER(ctypes.c_int32)]),
 ]
 
 _lib = None

@@ -37,14 +37,17 @@ struct gg_ctx {
   int blocks_per_sm = 0;
   int chunk = 256;
   int64_t batch = 1 << 24;
+  int refill_min = 8;
+  int interact_min = 16;
   int n_sm = 0;
   cudaStream_t stream = nullptr;
   std::string err;
 
   // tables (device, in working precision)
-  int n_e = 0, n_comp = 0, n_rinv = 0, n_mat = 0;
+  int n_e = 0, n_comp = 0, n_ray = 0, n_mat = 0;
   float ln_emin = 0, inv_dln = 0, e_min = 0, e_max = 0;
-  void *d_sig = nullptr, *d_cum = nullptr, *d_ray_amax = nullptr, *d_ray_inv = nullptr, *d_mat_rho = nullptr;
+  void *d_sig = nullptr, *d_cum = nullptr, *d_ray_amax = nullptr, *d_ray_cum = nullptr, *d_mat_rho = nullptr;
+  void *d_ray_x2 = nullptr;
   int *d_mat_comp = nullptr;
   std::vector<int> h_mat_comp;
   std::vector<float> h_mat_rho;
@@ -75,8 +78,10 @@ struct gg_ctx {
   // run bookkeeping
   unsigned long long *d_counters = nullptr, *d_next = nullptr;
   unsigned int *d_status = nullptr;
+  void *d_records = nullptr;
+  size_t rec_cap = 0;
   std::vector<cudaEvent_t> ev;
-  double last_transport_ms = 0, last_flush_ms = 0;
+  double last_generate_ms = 0, last_transport_ms = 0, last_flush_ms = 0;
   int last_launches = 0;
 
   int fail(int code, const char *fmt, ...) {
@@ -126,10 +131,12 @@ struct gg_ctx {
   }
 
   void release() {
-    dfree(d_sig); dfree(d_cum); dfree(d_ray_amax); dfree(d_ray_inv); dfree(d_mat_rho); dfree(d_mat_comp);
+    dfree(d_sig); dfree(d_cum); dfree(d_ray_amax); dfree(d_ray_cum); dfree(d_mat_rho); dfree(d_mat_comp);
+    dfree(d_ray_x2);
     dfree(d_labels); dfree(d_maj); dfree(d_spec_e); dfree(d_spec_cdf); dfree(d_acc_box);
     dfree(d_acc_e); dfree(d_acc_e2); dfree(d_edep); dfree(d_edep2);
-    dfree(d_counters); dfree(d_next); dfree(d_status);
+    dfree(d_counters); dfree(d_next); dfree(d_status); dfree(d_records);
+    rec_cap = 0;
     for (auto e : ev) cudaEventDestroy(e);
     ev.clear();
     if (stream) cudaStreamDestroy(stream);
@@ -142,7 +149,7 @@ struct gg_ctx {
     memset(&s, 0, sizeof(s));
     s.n_e = n_e;
     s.n_comp = n_comp;
-    s.n_rinv = n_rinv;
+    s.n_ray = n_ray;
     s.n_mat = n_mat;
     s.ln_emin = (real)ln_emin;
     s.inv_dln = (real)inv_dln;
@@ -150,7 +157,8 @@ struct gg_ctx {
     s.sig = (const real *)d_sig;
     s.cum = (const real *)d_cum;
     s.ray_amax = (const real *)d_ray_amax;
-    s.ray_inv = (const real *)d_ray_inv;
+    s.ray_cum = (const real *)d_ray_cum;
+    s.ray_x2 = (const real *)d_ray_x2;
     s.mat_rho = (const real *)d_mat_rho;
     s.mat_comp = d_mat_comp;
     s.maj = (const real *)d_maj;
@@ -208,6 +216,8 @@ int gg_create(const gg_device_opts *opts, gg_ctx **out) {
     if (opts->blocks_per_sm) c->blocks_per_sm = opts->blocks_per_sm;
     if (opts->chunk) c->chunk = opts->chunk;
     if (opts->batch) c->batch = opts->batch;
+    if (opts->refill_min) c->refill_min = opts->refill_min;
+    if (opts->interact_min) c->interact_min = opts->interact_min;
   }
   auto bail = [&](const std::string &m) {
     g_create_error = m;
@@ -219,6 +229,8 @@ int gg_create(const gg_device_opts *opts, gg_ctx **out) {
   if (c->block <= 0 || c->block > 256 || c->block % 32) return bail("arg: block_size must be a multiple of 32 <= 256");
   if (c->chunk <= 0) return bail("arg: chunk must be > 0");
   if (c->batch <= 0) return bail("arg: batch must be > 0");
+  if (c->refill_min < 1 || c->refill_min > 32 || c->interact_min < 1 || c->interact_min > 32)
+    return bail("arg: refill_min and interact_min must be in 1..32");
   int ndev = 0;
   cudaError_t e = cudaGetDeviceCount(&ndev);
   if (e != cudaSuccess || ndev == 0) return bail(std::string("no CUDA device: ") + cudaGetErrorString(e));
@@ -259,8 +271,8 @@ int gg_last_error(const gg_ctx *ctx, char *buf, size_t len) {
 int gg_upload_tables(gg_ctx *c, const gg_tables_desc *t) {
   if (!c || !t) return GG_ERR_ARG;
   cudaSetDevice(c->device);
-  if (t->n_e < 2 || t->n_comp < 1 || t->n_rinv < 2 || t->n_mat < 1 || !t->sig || !t->cum || !t->ray_amax ||
-      !t->ray_inv || !t->mat_comp || !t->mat_rho)
+  if (t->n_e < 2 || t->n_comp < 1 || t->n_ray < 2 || t->n_mat < 1 || !t->sig || !t->cum || !t->ray_amax ||
+      !t->ray_cum || !t->ray_x2 || !t->mat_comp || !t->mat_rho)
     return c->fail(GG_ERR_ARG, "gg_upload_tables: incomplete table descriptor");
   if (!(t->inv_dln > 0) || !(t->e_min > 0) || !(t->e_max > t->e_min))
     return c->fail(GG_ERR_ARG, "gg_upload_tables: invalid energy grid");
@@ -279,7 +291,7 @@ int gg_upload_tables(gg_ctx *c, const gg_tables_desc *t) {
     return c->fail(GG_ERR_ARG, "gg_upload_tables: tables need %zu bytes of shared memory (max 190 KiB)", need);
   c->n_e = t->n_e;
   c->n_comp = t->n_comp;
-  c->n_rinv = t->n_rinv;
+  c->n_ray = t->n_ray;
   c->n_mat = t->n_mat;
   c->ln_emin = t->ln_emin;
   c->inv_dln = t->inv_dln;
@@ -289,7 +301,11 @@ int gg_upload_tables(gg_ctx *c, const gg_tables_desc *t) {
   if ((st = c->upload_real(c->d_sig, t->sig, nce))) return st;
   if ((st = c->upload_real(c->d_cum, t->cum, 3 * nce))) return st;
   if ((st = c->upload_real(c->d_ray_amax, t->ray_amax, nce))) return st;
-  if ((st = c->upload_real(c->d_ray_inv, t->ray_inv, (size_t)t->n_comp * t->n_rinv))) return st;
+  if ((st = c->upload_real(c->d_ray_cum, t->ray_cum, (size_t)t->n_comp * t->n_ray))) return st;
+  if ((st = c->upload_real(c->d_ray_x2, t->ray_x2, (size_t)t->n_ray))) return st;
+  for (int i = 1; i < t->n_ray; ++i)
+    if (!(t->ray_x2[i] > t->ray_x2[i - 1]))
+      return c->fail(GG_ERR_ARG, "gg_upload_tables: Rayleigh x^2 nodes must increase");
   if ((st = c->upload_real(c->d_mat_rho, t->mat_rho, (size_t)t->n_mat))) return st;
   dfree(c->d_mat_comp);
   if ((st = c->cuda(cudaMalloc(&c->d_mat_comp, sizeof(int) * t->n_mat), "cudaMalloc"))) return st;
@@ -425,16 +441,27 @@ int gg_reset_tally(gg_ctx *c) {
 static int run_impl(gg_ctx *c, uint64_t n, uint64_t seed, uint64_t first) {
   size_t smem = c->precision == GG_PREC_F64 ? gg::transport_smem_bytes<double>(c->n_comp, c->n_e, c->n_mat)
                                             : gg::transport_smem_bytes<float>(c->n_comp, c->n_e, c->n_mat);
-  int bps = c->blocks_per_sm;
-  if (bps <= 0) {
-    cudaError_t e = c->precision == GG_PREC_F64 ? gg::occupancy_blocks<double>(c->block, smem, &bps)
-                                                : gg::occupancy_blocks<float>(c->block, smem, &bps);
+  // kernel variant: register budget for `minb` resident 256-thread blocks
+  int minb = c->blocks_per_sm > 0 ? std::min(c->blocks_per_sm, 4) : (c->precision == GG_PREC_F64 ? 2 : 3);
+  int bps = 0;
+  {
+    cudaError_t e = c->precision == GG_PREC_F64 ? gg::occupancy_blocks<double>(c->block, smem, minb, &bps)
+                                                : gg::occupancy_blocks<float>(c->block, smem, minb, &bps);
     if (e != cudaSuccess) return c->cuda(e, "occupancy");
     if (bps < 1) bps = 1;
   }
   int grid = c->n_sm * bps;
   uint64_t nb = (n + (uint64_t)c->batch - 1) / (uint64_t)c->batch;
-  while (c->ev.size() < 2 * nb + 2) {
+  size_t cap = (size_t)std::min<uint64_t>(n, (uint64_t)c->batch);
+  if (cap > c->rec_cap) {
+    dfree(c->d_records);
+    c->rec_cap = 0;
+    size_t bytes = c->precision == GG_PREC_F64 ? gg::record_bytes<double>(cap) : gg::record_bytes<float>(cap);
+    int st = c->cuda(cudaMalloc(&c->d_records, bytes), "cudaMalloc primary records");
+    if (st) return st;
+    c->rec_cap = cap;
+  }
+  while (c->ev.size() < 3 * nb + 1) {
     cudaEvent_t e;
     int st = c->cuda(cudaEventCreate(&e), "cudaEventCreate");
     if (st) return st;
@@ -448,36 +475,48 @@ static int run_impl(gg_ctx *c, uint64_t n, uint64_t seed, uint64_t first) {
   a.counters = c->d_counters;
   a.status = c->d_status;
   a.chunk = c->chunk;
+  a.records = c->d_records;
+  a.rec_cap = c->rec_cap;
+  a.refill_min = c->refill_min;
+  a.interact_min = c->interact_min;
   int flush_grid = c->n_sm * 8;
   int st;
+  // per batch: [ev 3b] generate [ev 3b+1] transport [ev 3b+2] flush [ev 3b+3]
   for (uint64_t b = 0; b < nb; ++b) {
     a.h_begin = first + b * (uint64_t)c->batch;
     a.h_end = std::min(first + n, a.h_begin + (uint64_t)c->batch);
     if ((st = c->cuda(cudaMemsetAsync(c->d_next, 0, 8, c->stream), "memset"))) return st;
-    if ((st = c->cuda(cudaEventRecord(c->ev[2 * b], c->stream), "event"))) return st;
-    cudaError_t e = c->precision == GG_PREC_F64
-                        ? gg::launch_transport<double>(c->scene<double>(), a, grid, c->block, smem, c->stream)
-                        : gg::launch_transport<float>(c->scene<float>(), a, grid, c->block, smem, c->stream);
+    if ((st = c->cuda(cudaEventRecord(c->ev[3 * b], c->stream), "event"))) return st;
+    cudaError_t e = c->precision == GG_PREC_F64 ? gg::launch_generate<double>(c->scene<double>(), a, c->stream)
+                                                : gg::launch_generate<float>(c->scene<float>(), a, c->stream);
+    if ((st = c->cuda(e, "generate launch"))) return st;
+    if ((st = c->cuda(cudaEventRecord(c->ev[3 * b + 1], c->stream), "event"))) return st;
+    e = c->precision == GG_PREC_F64
+            ? gg::launch_transport<double>(c->scene<double>(), a, grid, c->block, smem, minb, c->stream)
+            : gg::launch_transport<float>(c->scene<float>(), a, grid, c->block, smem, minb, c->stream);
     if ((st = c->cuda(e, "transport launch"))) return st;
-    if ((st = c->cuda(cudaEventRecord(c->ev[2 * b + 1], c->stream), "event"))) return st;
+    if ((st = c->cuda(cudaEventRecord(c->ev[3 * b + 2], c->stream), "event"))) return st;
     if ((st = c->cuda(gg::launch_flush(c->d_acc_e, a.acc_e2, c->d_edep, c->squared ? c->d_edep2 : nullptr,
                                        c->n_vox, flush_grid, c->stream),
                       "flush launch")))
       return st;
   }
-  if ((st = c->cuda(cudaEventRecord(c->ev[2 * nb], c->stream), "event"))) return st;
+  if ((st = c->cuda(cudaEventRecord(c->ev[3 * nb], c->stream), "event"))) return st;
   if ((st = c->cuda(cudaStreamSynchronize(c->stream), "transport"))) return st;
-  double tt = 0, tf = 0;
+  double tg = 0, tt = 0, tf = 0;
   for (uint64_t b = 0; b < nb; ++b) {
     float ms = 0;
-    cudaEventElapsedTime(&ms, c->ev[2 * b], c->ev[2 * b + 1]);
+    cudaEventElapsedTime(&ms, c->ev[3 * b], c->ev[3 * b + 1]);
+    tg += ms;
+    cudaEventElapsedTime(&ms, c->ev[3 * b + 1], c->ev[3 * b + 2]);
     tt += ms;
-    cudaEventElapsedTime(&ms, c->ev[2 * b + 1], b + 1 < nb ? c->ev[2 * b + 2] : c->ev[2 * nb]);
+    cudaEventElapsedTime(&ms, c->ev[3 * b + 2], c->ev[3 * b + 3]);
     tf += ms;
   }
+  c->last_generate_ms = tg;
   c->last_transport_ms = tt;
   c->last_flush_ms = tf;
-  c->last_launches = (int)(2 * nb);
+  c->last_launches = (int)(3 * nb);
   unsigned int status = 0;
   if ((st = c->cuda(cudaMemcpy(&status, c->d_status, sizeof(status), cudaMemcpyDeviceToHost), "status"))) return st;
   if (status) {
@@ -526,8 +565,10 @@ int gg_get_counters(gg_ctx *c, uint64_t *out, size_t n) {
   return GG_OK;
 }
 
-int gg_last_kernel_ms(gg_ctx *c, double *transport_ms, double *flush_ms, int32_t *launches) {
+int gg_last_kernel_ms(gg_ctx *c, double *generate_ms, double *transport_ms, double *flush_ms,
+                      int32_t *launches) {
   if (!c) return GG_ERR_ARG;
+  if (generate_ms) *generate_ms = c->last_generate_ms;
   if (transport_ms) *transport_ms = c->last_transport_ms;
   if (flush_ms) *flush_ms = c->last_flush_ms;
   if (launches) *launches = c->last_launches;

@@ -62,6 +62,17 @@ __device__ __forceinline__ void philox4x32_10(uint32_t c[4], uint32_t k0, uint32
   o[3] = c3;
 }
 
+// One Philox block as a single out-of-line function: the generator is drawn
+// from a dozen call sites and inlining the ten rounds at each of them would
+// multiply the kernel's instruction footprint.
+static __device__ __noinline__ uint4 philox_block(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uint32_t k0,
+                                           uint32_t k1) {
+  uint32_t c[4] = {c0, c1, c2, c3};
+  uint32_t o[4];
+  philox4x32_10(c, k0, k1, o);
+  return make_uint4(o[0], o[1], o[2], o[3]);
+}
+
 // Stream of one history: key = seed, counter = (block, stream, history lo, hi).
 struct Rng {
   uint32_t k0, k1;
@@ -80,8 +91,11 @@ struct Rng {
   }
   __device__ __forceinline__ uint32_t next() {
     if (idx == 4) {
-      uint32_t c[4] = {blk, stream, h0, h1};
-      philox4x32_10(c, k0, k1, buf);
+      uint4 b = philox_block(blk, stream, h0, h1, k0, k1);
+      buf[0] = b.x;
+      buf[1] = b.y;
+      buf[2] = b.z;
+      buf[3] = b.w;
       blk += 1u;
       idx = 0;
     }
@@ -104,7 +118,7 @@ __device__ __forceinline__ real u01_open0(Rng &g) {
 // ---------------------------------------------------------------------------
 // Elementary functions built from + - * / (A&S 4.1.27, 4.2.1, 4.3.65/66)
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ float gg_log(float x) {
+static __device__ __noinline__ float gg_log(float x) {
   uint32_t b = __float_as_uint(x);
   int e = (int)(b >> 23) - 127;
   uint32_t mb = (b & 0x007fffffu) | 0x3f800000u;
@@ -133,7 +147,7 @@ __device__ __forceinline__ float gg_log(float x) {
   return hi + lo;
 }
 
-__device__ __forceinline__ double gg_log(double x) {
+static __device__ __noinline__ double gg_log(double x) {
   uint64_t b = (uint64_t)__double_as_longlong(x);
   int e = (int)(b >> 52) - 1023;
   uint64_t mb = (b & 0x000fffffffffffffull) | 0x3ff0000000000000ull;
@@ -346,9 +360,9 @@ __device__ __forceinline__ void rotate_dir(real &ux, real &uy, real &uz, real co
 template <typename real>
 struct Scene {
   // tables
-  int n_e, n_comp, n_rinv, n_mat;
+  int n_e, n_comp, n_ray, n_mat;
   real ln_emin, inv_dln, e_min;
-  const real *sig, *cum, *ray_amax, *ray_inv, *mat_rho, *maj;
+  const real *sig, *cum, *ray_amax, *ray_x2, *ray_cum, *mat_rho, *maj;
   const int *mat_comp;
   // image
   int nx, ny, nz;
@@ -454,12 +468,42 @@ struct Photon {
 };
 
 template <typename real>
+struct EState {
+  int ie;
+  real fe, mumax, inv_mumax;
+};
+
+// Energy-grid position and majorant of energy e (out of line: it is reached
+// from the source stage, every Compton scattering, pair conversion and
+// secondary pop).
+template <typename real>
+static __device__ __noinline__ EState<real> energy_state(const real *maj, real ln_emin, real inv_dln, int n_e, real e) {
+  EState<real> r;
+  real le = gg_log(e);
+  real t = le - ln_emin;
+  t = t * inv_dln;
+  int i = (int)t;
+  if (i < 0) i = 0;
+  if (i > n_e - 2) i = n_e - 2;
+  r.ie = i;
+  r.fe = t - (real)i;
+  real a = maj[i];
+  real d = maj[i + 1] - a;
+  d = r.fe * d;
+  real mm = a + d;
+  r.mumax = mm;
+  r.inv_mumax = R<real>(1) / mm;
+  return r;
+}
+
+template <typename real>
 __device__ __forceinline__ void set_energy(const Scene<real> &s, Photon<real> &ph, real e) {
   ph.e = e;
-  ph.ei = energy_index(s, e);
-  real mm = interp_row(s.maj, ph.ei);
-  ph.mumax = mm;
-  ph.inv_mumax = R<real>(1) / mm;
+  EState<real> st = energy_state(s.maj, s.ln_emin, s.inv_dln, s.n_e, e);
+  ph.ei.ie = st.ie;
+  ph.ei.fe = st.fe;
+  ph.mumax = st.mumax;
+  ph.inv_mumax = st.inv_mumax;
 }
 
 template <typename real>

@@ -20,15 +20,24 @@ struct KernelArgs {
   unsigned long long *counters;     // GG_N_COUNTERS slots
   unsigned int *status;             // OR of error codes raised by the kernel
   int chunk;                        // histories claimed per warp refill
+  void *records;                    // primary records of the batch (k_generate -> k_transport)
+  size_t rec_cap;                   // records capacity (histories per batch)
+  int refill_min;                   // lanes that must wait for a history before a refill phase
+  int interact_min;                 // pending collisions that trigger an interaction phase
 };
 
 template <typename real>
 size_t transport_smem_bytes(int n_comp, int n_e, int n_mat);
 template <typename real>
-cudaError_t launch_transport(const Scene<real> &s, const KernelArgs &a, int grid, int block, size_t smem,
-                             cudaStream_t st);
+size_t record_bytes(size_t cap);
 template <typename real>
-cudaError_t occupancy_blocks(int block, size_t smem, int *blocks_per_sm);
+cudaError_t launch_generate(const Scene<real> &s, const KernelArgs &a, cudaStream_t st);
+// minb selects the kernel variant compiled for that many resident blocks per SM
+template <typename real>
+cudaError_t launch_transport(const Scene<real> &s, const KernelArgs &a, int grid, int block, size_t smem,
+                             int minb, cudaStream_t st);
+template <typename real>
+cudaError_t occupancy_blocks(int block, size_t smem, int minb, int *blocks_per_sm);
 cudaError_t launch_flush(unsigned long long *acc_e, unsigned long long *acc_e2, double *edep, double *edep2,
                          size_t n, int grid, cudaStream_t st);
 

@@ -154,32 +154,43 @@ __device__ __forceinline__ void rayleigh(const Scene<real> &s, int comp, Photon<
   real k = ph.e * R<real>(1.0 / kHcMevAngstrom);
   real x2max = k * k;
   real amax = interp_row(s.ray_amax + (size_t)comp * s.n_e, ph.ei);
-  const real *inv = s.ray_inv + (size_t)comp * s.n_rinv;
-  real cost;
+  const real *cu = s.ray_cum + (size_t)comp * s.n_ray;
+  const real *xn = s.ray_x2;
+  real cost = R<real>(1);
   int it = 0;
   for (;;) {
+    if (++it > kLoopCap) {
+      atomicAdd(&bc->loop_capped, 1u);
+      break;
+    }
     real r = u01<real>(g);
     real tt = r * amax;
-    real pos = tt * (real)(s.n_rinv - 1);
-    int j = (int)pos;
-    if (j > s.n_rinv - 2) j = s.n_rinv - 2;
-    real f = pos - (real)j;
-    real d = inv[j + 1] - inv[j];
+    // exact inversion of the piecewise-linear cumulative: bisection for the
+    // node interval, then linear in x^2 inside it
+    int lo = 0, hi = s.n_ray - 1;
+    while (hi - lo > 1) {
+      int mid = (lo + hi) >> 1;
+      if (cu[mid] <= tt) lo = mid;
+      else hi = mid;
+    }
+    real den = cu[lo + 1] - cu[lo];
+    real f = R<real>(0);
+    if (den > R<real>(0)) {
+      f = tt - cu[lo];
+      f = f / den;
+    }
+    real d = xn[lo + 1] - xn[lo];
     d = f * d;
-    real x2 = inv[j] + d;
+    real x2 = xn[lo] + d;
+    if (x2 > x2max) continue;  // beyond the momentum transfer reachable at E
     real q = R<real>(2) * x2;
     q = q / x2max;
     cost = R<real>(1) - q;
-    if (cost < R<real>(-1)) cost = R<real>(-1);
     real r2 = u01<real>(g);
     real lhs = R<real>(2) * r2;
     real rhs = cost * cost;
     rhs = R<real>(1) + rhs;
     if (lhs <= rhs) break;
-    if (++it >= kLoopCap) {
-      atomicAdd(&bc->loop_capped, 1u);
-      break;
-    }
   }
   real st2 = cost * cost;
   st2 = R<real>(1) - st2;
@@ -203,13 +214,15 @@ __device__ __forceinline__ void iso_dir(Rng &g, real d[3]) {
   d[2] = cost;
 }
 
-// One secondary slot: after a pair conversion the photon continues as one
-// 511 keV photon and the other waits here.  511 keV cannot convert again,
-// so one slot always suffices.
+// One secondary slot per thread, in shared memory: after a pair conversion the
+// photon continues as one 511 keV photon and the other waits here.  511 keV
+// cannot convert again, so one slot always suffices.
 template <typename real>
 struct Secondary {
-  real pos[3], dir[3];
+  real *base;  // [6][stride]: pos xyz, dir xyz
+  int stride, tid;
   int has;
+  __device__ __forceinline__ real &at(int k) { return base[k * stride + tid]; }
 };
 
 // Interaction at ph.pos in material `mat`.  Returns the energy deposited
@@ -240,8 +253,8 @@ __device__ __forceinline__ real interact(const Scene<real> &s, Photon<real> &ph,
   } else {
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
-      sec.pos[a] = ph.pos[a];
-      sec.dir[a] = -d[a];
+      sec.at(a) = ph.pos[a];
+      sec.at(3 + a) = -d[a];
     }
     sec.has = 1;
   }
@@ -365,9 +378,17 @@ __device__ __forceinline__ int sample_primary(const Scene<real> &s, Rng &g, Phot
     w = w * u01<real>(g);
     e = s.s_elo + w;
   } else {
+    // first index with p < cdf[i] (the linear scan of
+    // GateSPSEneDistribution::IndexForProbability), found by bisection on the
+    // non-decreasing cumulative weights
     real p = u01<real>(g);
-    int i = 0;
-    while (i < s.n_spec - 1 && p >= s.spec_cdf[i]) ++i;
+    int lo = 0, hi = s.n_spec - 1;
+    while (lo < hi) {
+      int mid = (lo + hi) >> 1;
+      if (p >= s.spec_cdf[mid]) lo = mid + 1;
+      else hi = mid;
+    }
+    int i = lo;
     if (et == GG_ENE_LINES) {
       e = s.spec_e[i];
     } else {
@@ -384,17 +405,129 @@ __device__ __forceinline__ int sample_primary(const Scene<real> &s, Rng &g, Phot
   return GG_OK;
 }
 
-// One transport event: a Woodcock tentative step in the image (with the
-// interaction if it is real), or a free flight in the world.
+// Primary records written by k_generate and consumed by k_transport (SoA,
+// one entry per history of the batch).  The state field says how the first
+// transport iteration left the photon; the RNG position lets the transport
+// kernel continue the history's Philox stream exactly where it stopped.
+enum : uint32_t { kRecDead = 0, kRecInImage = 1, kRecPendingWorld = 2 };
+
 template <typename real>
-__device__ __forceinline__ void step(const Scene<real> &s, Photon<real> &ph, Rng &g, BlockCounters *bc,
-                                     HistList<real> &l, const Tally<real> &t, Secondary<real> &sec,
-                                     unsigned int &n_wood, unsigned int &n_real, unsigned int &n_dep,
-                                     unsigned int &n_world) {
+struct Records {
+  uint4 *rng_buf;
+  real *px, *py, *pz, *dx, *dy, *dz, *e;
+  uint32_t *flags;    // bits 0-1 state, bit 2 steps already taken (0/1)
+  uint32_t *rng_pos;  // block << 3 | index in buffer
+
+  __device__ __forceinline__ static Records carve(void *base, size_t cap) {
+    Records r;
+    unsigned char *p = reinterpret_cast<unsigned char *>(base);
+    r.rng_buf = reinterpret_cast<uint4 *>(p);
+    p += cap * sizeof(uint4);
+    real **f[7] = {&r.px, &r.py, &r.pz, &r.dx, &r.dy, &r.dz, &r.e};
+    for (int i = 0; i < 7; ++i) {
+      *f[i] = reinterpret_cast<real *>(p);
+      p += cap * sizeof(real);
+    }
+    r.flags = reinterpret_cast<uint32_t *>(p);
+    p += cap * sizeof(uint32_t);
+    r.rng_pos = reinterpret_cast<uint32_t *>(p);
+    return r;
+  }
+};
+
+// Source stage: one thread per history.  Samples the primary
+// (GateGenericSource::GeneratePrimaries order), places it, and performs the
+// first transport iteration when the photon starts in the world (free flight
+// to the image, to an air interaction, or out of the world).
+template <typename real>
+__global__ void __launch_bounds__(256) k_generate(Scene<real> s, KernelArgs a) {
+  __shared__ BlockCounters bc;
+  __shared__ unsigned int n_world;
+  if (threadIdx.x == 0) {
+    bc = BlockCounters{0, 0, 0, 0, 0, 0, 0, 0};
+    n_world = 0;
+  }
+  __syncthreads();
+  const uint64_t n = a.h_end - a.h_begin;
+  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) {
+    Records<real> rec = Records<real>::carve(a.records, a.rec_cap);
+    Rng g;
+    g.init(a.seed, a.h_begin + i, 0u);
+    Photon<real> ph;
+    uint32_t state = kRecDead, steps = 0;
+    int st = sample_primary(s, g, ph, &bc);
+    if (st != GG_OK) {
+      atomicOr(a.status, (unsigned int)st);
+    } else {
+      atomicAdd(&bc.histories, 1u);
+      start_photon(s, ph);
+      if (ph.in_image) {
+        state = kRecInImage;
+      } else {
+        steps = 1;
+        atomicAdd(&n_world, 1u);
+        real inf = gg_inf(real(0));
+        real tin = ph.can_enter ? entry_distance(ph.pos, ph.dir, s.bmin, s.bmax) : inf;
+        real wlo[3] = {-s.whalf[0], -s.whalf[1], -s.whalf[2]};
+        real tout = exit_distance(ph.pos, ph.dir, wlo, s.whalf);
+        int wm = s.world_mat;
+        real mu = interp_row(s.sig + (size_t)s.mat_comp[wm] * s.n_e, ph.ei);
+        mu = s.mat_rho[wm] * mu;
+        real u = u01_open0<real>(g);
+        real sd = -gg_log(u);
+        sd = sd / mu;
+        if (sd < tin && sd < tout) {
+#pragma unroll
+          for (int k = 0; k < 3; ++k) ph.pos[k] = ph.pos[k] + sd * ph.dir[k];
+          state = kRecPendingWorld;
+        } else if (tin <= tout) {
+#pragma unroll
+          for (int k = 0; k < 3; ++k) ph.pos[k] = ph.pos[k] + tin * ph.dir[k];
+          state = kRecInImage;
+        } else {
+          atomicAdd(&bc.escaped, 1u);
+        }
+      }
+    }
+    rec.px[i] = ph.pos[0];
+    rec.py[i] = ph.pos[1];
+    rec.pz[i] = ph.pos[2];
+    rec.dx[i] = ph.dir[0];
+    rec.dy[i] = ph.dir[1];
+    rec.dz[i] = ph.dir[2];
+    rec.e[i] = ph.e;
+    rec.flags[i] = state | (steps << 2);
+    rec.rng_pos[i] = (g.blk << 3) | (uint32_t)g.idx;
+    rec.rng_buf[i] = make_uint4(g.buf[0], g.buf[1], g.buf[2], g.buf[3]);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned long long *cnt = a.counters;
+    if (bc.histories) atomicAdd(&cnt[GG_CNT_HISTORIES], (unsigned long long)bc.histories);
+    if (bc.skipped) atomicAdd(&cnt[GG_CNT_SKIPPED], (unsigned long long)bc.skipped);
+    if (bc.escaped) atomicAdd(&cnt[GG_CNT_ESCAPED], (unsigned long long)bc.escaped);
+    if (bc.loop_capped) atomicAdd(&cnt[GG_CNT_LOOP_CAPPED], (unsigned long long)bc.loop_capped);
+    if (n_world) atomicAdd(&cnt[GG_CNT_WORLD_STEPS], (unsigned long long)n_world);
+  }
+}
+
+// Lane states of the phase-batched transport loop.
+enum : int { kDone = 0, kRefill = 1, kFly = 2, kInteract = 3 };
+
+// Flight: one Woodcock tentative step in the image, or one free flight in the
+// world.  A real collision is not handled here: the lane records it
+// (material, voxel, scored) and waits in state kInteract until its warp runs
+// an interaction phase.  Returns the lane's next state; kRefill means the
+// photon died.
+template <typename real>
+__device__ __forceinline__ int flight(const Scene<real> &s, Photon<real> &ph, Rng &g, BlockCounters *bc, int &pmat,
+                                      uint32_t &pv, int &pscored, unsigned int &n_wood, unsigned int &n_real,
+                                      unsigned int &n_world) {
   if (++ph.steps > kStepCap) {
     atomicAdd(&bc->loop_capped, 1u);
     ph.alive = 0;
-    return;
+    return kRefill;
   }
   if (ph.in_image) {
     real u = u01_open0<real>(g);
@@ -405,7 +538,7 @@ __device__ __forceinline__ void step(const Scene<real> &s, Photon<real> &ph, Rng
       for (int a = 0; a < 3; ++a) ph.pos[a] = ph.pos[a] + ph.t_exit * ph.dir[a];
       ph.in_image = 0;
       ph.can_enter = 0;
-      return;
+      return kFly;
     }
     ph.t_exit = ph.t_exit - sd;
 #pragma unroll
@@ -422,44 +555,86 @@ __device__ __forceinline__ void step(const Scene<real> &s, Photon<real> &ph, Rng
     real mu = interp_row(s.sig + (size_t)s.mat_comp[m] * s.n_e, ph.ei);
     mu = s.mat_rho[m] * mu;
     real u2 = u01<real>(g);
-    if (u2 * ph.mumax >= mu) return;
+    if (u2 * ph.mumax >= mu) return kFly;
     ++n_real;
-    real ed = interact(s, ph, m, g, bc, sec);
-    deposit(l, t, bc, v, ed, n_dep);
+    pmat = m;
+    pv = v;
+    pscored = 1;
+    return kInteract;
+  }
+  ++n_world;
+  real inf = gg_inf(real(0));
+  real tin = ph.can_enter ? entry_distance(ph.pos, ph.dir, s.bmin, s.bmax) : inf;
+  real wlo[3] = {-s.whalf[0], -s.whalf[1], -s.whalf[2]};
+  real tout = exit_distance(ph.pos, ph.dir, wlo, s.whalf);
+  int wm = s.world_mat;
+  real mu = interp_row(s.sig + (size_t)s.mat_comp[wm] * s.n_e, ph.ei);
+  mu = s.mat_rho[wm] * mu;
+  real u = u01_open0<real>(g);
+  real sd = -gg_log(u);
+  sd = sd / mu;
+  if (sd < tin && sd < tout) {
+#pragma unroll
+    for (int a = 0; a < 3; ++a) ph.pos[a] = ph.pos[a] + sd * ph.dir[a];
+    pmat = wm;
+    pscored = 0;
+    return kInteract;
+  }
+  if (tin <= tout) {
+#pragma unroll
+    for (int a = 0; a < 3; ++a) ph.pos[a] = ph.pos[a] + tin * ph.dir[a];
+    ph.in_image = 1;
+    ph.t_exit = exit_distance(ph.pos, ph.dir, s.bmin, s.bmax);
+    return kFly;
+  }
+  ph.alive = 0;
+  atomicAdd(&bc->escaped, 1u);
+  return kRefill;
+}
+
+// The interaction a lane recorded during its last flight.
+template <typename real>
+__device__ __forceinline__ int do_interaction(const Scene<real> &s, Photon<real> &ph, Rng &g, BlockCounters *bc,
+                                              int pmat, uint32_t pv, int pscored, HistList<real> &l,
+                                              const Tally<real> &t, Secondary<real> &sec, unsigned int &n_dep) {
+  real ed = interact(s, ph, pmat, g, bc, sec);
+  if (pscored) {
+    deposit(l, t, bc, pv, ed, n_dep);
     if (ph.alive && ph.in_image) ph.t_exit = exit_distance(ph.pos, ph.dir, s.bmin, s.bmax);
   } else {
-    ++n_world;
-    real inf = gg_inf(real(0));
-    real tin = ph.can_enter ? entry_distance(ph.pos, ph.dir, s.bmin, s.bmax) : inf;
-    real wlo[3] = {-s.whalf[0], -s.whalf[1], -s.whalf[2]};
-    real tout = exit_distance(ph.pos, ph.dir, wlo, s.whalf);
-    int wm = s.world_mat;
-    real mu = interp_row(s.sig + (size_t)s.mat_comp[wm] * s.n_e, ph.ei);
-    mu = s.mat_rho[wm] * mu;
-    real u = u01_open0<real>(g);
-    real sd = -gg_log(u);
-    sd = sd / mu;
-    if (sd < tin && sd < tout) {
-#pragma unroll
-      for (int a = 0; a < 3; ++a) ph.pos[a] = ph.pos[a] + sd * ph.dir[a];
-      interact(s, ph, wm, g, bc, sec);
-      ph.can_enter = 1;
-    } else if (tin <= tout) {
-#pragma unroll
-      for (int a = 0; a < 3; ++a) ph.pos[a] = ph.pos[a] + tin * ph.dir[a];
-      ph.in_image = 1;
-      ph.t_exit = exit_distance(ph.pos, ph.dir, s.bmin, s.bmax);
-    } else {
-      ph.alive = 0;
-      atomicAdd(&bc->escaped, 1u);
-    }
+    ph.can_enter = 1;
   }
+  return ph.alive ? kFly : kRefill;
 }
 
 template <typename real>
-__global__ void __launch_bounds__(256) k_transport(Scene<real> sg, KernelArgs args) {
+__device__ __forceinline__ void pop_secondary(const Scene<real> &s, Photon<real> &ph, Secondary<real> &sec) {
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    ph.pos[a] = sec.at(a);
+    ph.dir[a] = sec.at(3 + a);
+  }
+  sec.has = 0;
+  ph.alive = 1;
+  set_energy(s, ph, R<real>(kMC2));
+  start_photon(s, ph);
+}
+
+// Transport stage.  Persistent grid; each lane carries one history at a time
+// and is in one of the states kRefill (needs a history), kFly (next event is
+// a flight) or kInteract (a collision is pending).  Every iteration the warp
+// picks ONE phase by ballot - refill when at least refill_min lanes wait for a
+// history, interact when at least interact_min collisions are pending,
+// otherwise fly - and only the lanes in that state execute it.  Expensive
+// code (source-record loads, tally flushes, Compton sampling) therefore runs
+// with many lanes active instead of one lane at a time, while the order of
+// operations inside each history, and hence its result, is unchanged.
+// MINB = resident blocks per SM the register budget is sized for.
+template <typename real, int MINB>
+__global__ void __launch_bounds__(256, MINB) k_transport(Scene<real> sg, KernelArgs args) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ BlockCounters bc;
+  __shared__ real sec_store[6 * 256];
   // ---- stage tables in shared memory --------------------------------------
   Scene<real> s = sg;
   {
@@ -482,6 +657,7 @@ __global__ void __launch_bounds__(256) k_transport(Scene<real> sg, KernelArgs ar
     s.mat_rho = srho;
     s.mat_comp = scomp;
   }
+  const Records<real> rec = Records<real>::carve(args.records, args.rec_cap);
   Tally<real> t{args.acc_e, args.acc_e2};
   const unsigned lane = threadIdx.x & 31u;
   const unsigned lt_mask = (1u << lane) - 1u;
@@ -492,38 +668,37 @@ __global__ void __launch_bounds__(256) k_transport(Scene<real> sg, KernelArgs ar
   Photon<real> ph;
   ph.alive = 0;
   Secondary<real> sec;
+  sec.base = sec_store;
+  sec.stride = blockDim.x;
+  sec.tid = threadIdx.x;
   sec.has = 0;
   HistList<real> l;
   l.n = 0;
   Rng g;
-  bool done = false, in_hist = false;
+  int state = kRefill;
+  bool in_hist = false;
+  int pmat = 0, pscored = 0;
+  uint32_t pv = 0;
   unsigned int n_wood = 0, n_real = 0, n_dep = 0, n_world = 0;
 
   for (;;) {
-    bool need = false;
-    if (!done && !ph.alive) {
-      if (sec.has) {
-#pragma unroll
-        for (int a = 0; a < 3; ++a) {
-          ph.pos[a] = sec.pos[a];
-          ph.dir[a] = sec.dir[a];
-        }
-        sec.has = 0;
-        ph.alive = 1;
-        set_energy(s, ph, R<real>(kMC2));
-        start_photon(s, ph);
-      } else {
-        if (in_hist) {
-          hlist_flush(l, t, &bc);
-          in_hist = false;
-        }
-        need = true;
+    const unsigned m_ref = __ballot_sync(0xffffffffu, state == kRefill);
+    const unsigned m_fly = __ballot_sync(0xffffffffu, state == kFly);
+    const unsigned m_int = __ballot_sync(0xffffffffu, state == kInteract);
+    if ((m_ref | m_fly | m_int) == 0u) break;
+    int phase;
+    if (__popc(m_ref) >= args.refill_min || (m_fly | m_int) == 0u) phase = kRefill;
+    else if (__popc(m_int) >= args.interact_min || m_fly == 0u) phase = kInteract;
+    else phase = kFly;
+
+    if (phase == kRefill) {
+      const bool need = state == kRefill;
+      if (need && in_hist) {
+        hlist_flush(l, t, &bc);
+        in_hist = false;
       }
-    }
-    const unsigned need_mask = __ballot_sync(0xffffffffu, need);
-    if (need_mask) {
-      const unsigned n_need = __popc(need_mask);
-      const unsigned rank = __popc(need_mask & lt_mask);
+      const unsigned n_need = __popc(m_ref);
+      const unsigned rank = __popc(m_ref & lt_mask);
       const uint64_t avail = pool_end - pool_next;
       uint64_t h;
       if (avail >= n_need) {
@@ -539,23 +714,66 @@ __global__ void __launch_bounds__(256) k_transport(Scene<real> sg, KernelArgs ar
       }
       if (need) {
         if (h >= n_hist) {
-          done = true;
+          state = kDone;
         } else {
-          g.init(args.seed, args.h_begin + h, 0u);
-          int st = sample_primary(s, g, ph, &bc);
-          if (st != GG_OK) {
-            atomicOr(args.status, (unsigned int)st);
-            done = true;
-          } else {
-            atomicAdd(&bc.histories, 1u);
+          const uint32_t f = rec.flags[h];
+          const uint32_t rs = f & 3u;
+          if (rs != kRecDead) {
+            ph.pos[0] = rec.px[h];
+            ph.pos[1] = rec.py[h];
+            ph.pos[2] = rec.pz[h];
+            ph.dir[0] = rec.dx[h];
+            ph.dir[1] = rec.dy[h];
+            ph.dir[2] = rec.dz[h];
+            set_energy(s, ph, rec.e[h]);
+            ph.steps = (int)((f >> 2) & 1u);
+            ph.alive = 1;
+            ph.can_enter = 1;
+            const uint64_t hid = args.h_begin + h;
+            const uint32_t rp = rec.rng_pos[h];
+            const uint4 b = rec.rng_buf[h];
+            g.k0 = (uint32_t)args.seed;
+            g.k1 = (uint32_t)(args.seed >> 32);
+            g.stream = 0u;
+            g.h0 = (uint32_t)hid;
+            g.h1 = (uint32_t)(hid >> 32);
+            g.blk = rp >> 3;
+            g.idx = (int)(rp & 7u);
+            g.buf[0] = b.x;
+            g.buf[1] = b.y;
+            g.buf[2] = b.z;
+            g.buf[3] = b.w;
+            if (rs == kRecInImage) {
+              ph.in_image = 1;
+              ph.t_exit = exit_distance(ph.pos, ph.dir, s.bmin, s.bmax);
+              state = kFly;
+            } else {
+              ph.in_image = 0;
+              pmat = s.world_mat;
+              pscored = 0;
+              state = kInteract;
+            }
             in_hist = true;
-            start_photon(s, ph);
           }
         }
       }
+    } else if (phase == kInteract) {
+      if (state == kInteract) {
+        state = do_interaction(s, ph, g, &bc, pmat, pv, pscored, l, t, sec, n_dep);
+        if (state == kRefill && sec.has) {
+          pop_secondary(s, ph, sec);
+          state = kFly;
+        }
+      }
+    } else {
+      if (state == kFly) {
+        state = flight(s, ph, g, &bc, pmat, pv, pscored, n_wood, n_real, n_world);
+        if (state == kRefill && sec.has) {
+          pop_secondary(s, ph, sec);
+          state = kFly;
+        }
+      }
     }
-    if (__all_sync(0xffffffffu, done)) break;
-    if (!done && ph.alive) step(s, ph, g, &bc, l, t, sec, n_wood, n_real, n_dep, n_world);
   }
   // ---- counters -------------------------------------------------------------
   unsigned long long *cnt = args.counters;
@@ -571,11 +789,9 @@ __global__ void __launch_bounds__(256) k_transport(Scene<real> sg, KernelArgs ar
   warp_add(n_world, GG_CNT_WORLD_STEPS);
   __syncthreads();
   if (threadIdx.x == 0) {
-    atomicAdd(&cnt[GG_CNT_HISTORIES], (unsigned long long)bc.histories);
     atomicAdd(&cnt[GG_CNT_TALLY_ENTRIES], (unsigned long long)bc.tally_entries);
     atomicAdd(&cnt[GG_CNT_LIST_OVERFLOWS], (unsigned long long)bc.list_overflows);
     atomicAdd(&cnt[GG_CNT_ESCAPED], (unsigned long long)bc.escaped);
-    atomicAdd(&cnt[GG_CNT_SKIPPED], (unsigned long long)bc.skipped);
     atomicAdd(&cnt[GG_CNT_LOOP_CAPPED], (unsigned long long)bc.loop_capped);
     atomicAdd(&cnt[GG_CNT_STACK_OVERFLOW], (unsigned long long)bc.stack_overflow);
     atomicAdd(&cnt[GG_CNT_SECONDARIES], (unsigned long long)bc.secondaries);
@@ -609,17 +825,38 @@ size_t transport_smem_bytes(int n_comp, int n_e, int n_mat) {
 }
 
 template <typename real>
-cudaError_t launch_transport(const Scene<real> &s, const KernelArgs &a, int grid, int block, size_t smem,
-                             cudaStream_t st) {
+size_t record_bytes(size_t cap) {
+  return cap * (sizeof(uint4) + 7 * sizeof(real) + 2 * sizeof(uint32_t));
+}
+
+template <typename real>
+cudaError_t launch_generate(const Scene<real> &s, const KernelArgs &a, cudaStream_t st) {
+  uint64_t n = a.h_end - a.h_begin;
+  unsigned int blocks = (unsigned int)((n + 255) / 256);
+  k_generate<real><<<blocks, 256, 0, st>>>(s, a);
+  return cudaGetLastError();
+}
+
+template <typename real, int MINB>
+static cudaError_t launch_transport_v(const Scene<real> &s, const KernelArgs &a, int grid, int block, size_t smem,
+                                      cudaStream_t st) {
   static bool configured = false;
   if (!configured) {
-    cudaError_t e = cudaFuncSetAttribute(k_transport<real>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaError_t e = cudaFuncSetAttribute(k_transport<real, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          200 * 1024);
     if (e != cudaSuccess) return e;
     configured = true;
   }
-  k_transport<real><<<grid, block, smem, st>>>(s, a);
+  k_transport<real, MINB><<<grid, block, smem, st>>>(s, a);
   return cudaGetLastError();
+}
+
+template <typename real>
+cudaError_t launch_transport(const Scene<real> &s, const KernelArgs &a, int grid, int block, size_t smem,
+                             int minb, cudaStream_t st) {
+  if (minb <= 2) return launch_transport_v<real, 2>(s, a, grid, block, smem, st);
+  if (minb == 3) return launch_transport_v<real, 3>(s, a, grid, block, smem, st);
+  return launch_transport_v<real, 4>(s, a, grid, block, smem, st);
 }
 
 cudaError_t launch_flush(unsigned long long *acc_e, unsigned long long *acc_e2, double *edep, double *edep2,
@@ -629,17 +866,23 @@ cudaError_t launch_flush(unsigned long long *acc_e, unsigned long long *acc_e2, 
 }
 
 template <typename real>
-cudaError_t occupancy_blocks(int block, size_t smem, int *blocks_per_sm) {
-  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k_transport<real>, block, smem);
+cudaError_t occupancy_blocks(int block, size_t smem, int minb, int *blocks_per_sm) {
+  if (minb <= 2) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k_transport<real, 2>, block, smem);
+  if (minb == 3) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k_transport<real, 3>, block, smem);
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k_transport<real, 4>, block, smem);
 }
 
+template size_t record_bytes<float>(size_t);
+template size_t record_bytes<double>(size_t);
+template cudaError_t launch_generate<float>(const Scene<float> &, const KernelArgs &, cudaStream_t);
+template cudaError_t launch_generate<double>(const Scene<double> &, const KernelArgs &, cudaStream_t);
 template size_t transport_smem_bytes<float>(int, int, int);
 template size_t transport_smem_bytes<double>(int, int, int);
-template cudaError_t launch_transport<float>(const Scene<float> &, const KernelArgs &, int, int, size_t,
+template cudaError_t launch_transport<float>(const Scene<float> &, const KernelArgs &, int, int, size_t, int,
                                              cudaStream_t);
-template cudaError_t launch_transport<double>(const Scene<double> &, const KernelArgs &, int, int, size_t,
+template cudaError_t launch_transport<double>(const Scene<double> &, const KernelArgs &, int, int, size_t, int,
                                               cudaStream_t);
-template cudaError_t occupancy_blocks<float>(int, size_t, int *);
-template cudaError_t occupancy_blocks<double>(int, size_t, int *);
+template cudaError_t occupancy_blocks<float>(int, size_t, int, int *);
+template cudaError_t occupancy_blocks<double>(int, size_t, int, int *);
 
 }  // namespace gg

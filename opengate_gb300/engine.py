@@ -18,10 +18,10 @@ class DoseEngine:
     """Drives libgategpu.so for one :class:`~opengate_gb300.scene.Scene`."""
 
     def __init__(self, scene, device=0, precision=32, block_size=0, blocks_per_sm=0, chunk=0, batch=0,
-                 score_squared=True):
+                 refill_min=0, interact_min=0, score_squared=True):
         self.lib = C.load()
         self.scene = scene
-        opts = C.DeviceOpts(device, precision, block_size, blocks_per_sm, chunk, batch)
+        opts = C.DeviceOpts(device, precision, block_size, blocks_per_sm, chunk, batch, refill_min, interact_min)
         ctx = ctypes.c_void_p()
         st = self.lib.gg_create(ctypes.byref(opts), ctypes.byref(ctx))
         C.check(self.lib, None, st)
@@ -63,9 +63,10 @@ class DoseEngine:
         return {name: int(out[i]) for i, name in enumerate(C.COUNTER_NAMES)}
 
     def last_kernel_ms(self):
-        t, f, n = ctypes.c_double(), ctypes.c_double(), ctypes.c_int32()
-        self._call("gg_last_kernel_ms", ctypes.byref(t), ctypes.byref(f), ctypes.byref(n))
-        return t.value, f.value, n.value
+        """(generate_ms, transport_ms, flush_ms, launches) of the last run."""
+        g, t, f, n = ctypes.c_double(), ctypes.c_double(), ctypes.c_double(), ctypes.c_int32()
+        self._call("gg_last_kernel_ms", ctypes.byref(g), ctypes.byref(t), ctypes.byref(f), ctypes.byref(n))
+        return g.value, t.value, f.value, n.value
 
     def close(self):
         if self.ctx:

@@ -77,7 +77,7 @@ class Scene:
         self._sig = np.ascontiguousarray(pt.sig, dtype=np.float32)
         self._cum = np.ascontiguousarray(pt.cum, dtype=np.float32)
         self._ray_amax = np.ascontiguousarray(pt.ray_amax, dtype=np.float32)
-        self._ray_inv = np.ascontiguousarray(pt.ray_inv, dtype=np.float32)
+        self._ray_cum = np.ascontiguousarray(pt.ray_cum, dtype=np.float32)
         self._mat_comp = np.ascontiguousarray(pt.mat_comp, dtype=np.int32)
         self._mat_rho = np.ascontiguousarray(pt.mat_rho, dtype=np.float32)
         t = C.TablesDesc()
@@ -90,8 +90,10 @@ class Scene:
         t.sig = C.ptr(self._sig, C.ctypes.c_float)
         t.cum = C.ptr(self._cum, C.ctypes.c_float)
         t.ray_amax = C.ptr(self._ray_amax, C.ctypes.c_float)
-        t.n_rinv = T.N_RINV
-        t.ray_inv = C.ptr(self._ray_inv, C.ctypes.c_float)
+        t.n_ray = T.N_RAY
+        self._ray_x2 = np.ascontiguousarray(T.rayleigh_x2_nodes(), dtype=np.float32)
+        t.ray_x2 = C.ptr(self._ray_x2, C.ctypes.c_float)
+        t.ray_cum = C.ptr(self._ray_cum, C.ctypes.c_float)
         t.n_mat = len(pt.materials)
         t.mat_comp = C.ptr(self._mat_comp, C.ctypes.c_int32)
         t.mat_rho = C.ptr(self._mat_rho, C.ctypes.c_float)

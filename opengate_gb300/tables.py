@@ -12,7 +12,8 @@ the CPU oracle, which receives the very same float32 arrays):
     Compton, +photoelectric, +Rayleigh (pair takes the rest);
   - ``ray_amax[c, i]``: normalised cumulative of the Rayleigh form-factor
     law at the largest momentum transfer reachable at E_i;
-  - ``ray_inv[c, j]``: x^2 (1/Angstrom^2) at cumulative fraction j/(N_RINV-1).
+  - ``ray_cum[c, j]``: normalised cumulative of F^2(x^2) dx^2 at the shared
+    x^2 nodes ``ray_x2[j]`` (1/Angstrom^2), piecewise linear in between.
 * per material ``m`` (label): its composition index and density.
 
 Values between grid points are linear in ln(E).  The per-element partial
@@ -28,11 +29,16 @@ from . import xsection
 N_E = 512
 E_MIN = 1e-3  # MeV; photons below are absorbed locally
 E_MAX = 20.0  # MeV
-N_RINV = 512
+N_RAY = 1024
 
 
 def energy_grid():
     return np.exp(np.linspace(np.log(E_MIN), np.log(E_MAX), N_E))
+
+
+def rayleigh_x2_nodes():
+    """x^2 nodes (1/Angstrom^2) of the Rayleigh cumulative: 0, then log-spaced 1e-6..1e7."""
+    return np.concatenate([[0.0], np.geomspace(1e-6, 1e7, N_RAY - 1)]).astype(np.float32).astype(np.float64)
 
 
 @functools.lru_cache(maxsize=None)
@@ -63,15 +69,16 @@ class CompositionTable:
         below = energy_grid() <= 2.0 * xsection.ELECTRON_MASS_MEV
         c2 = np.where(below, 1.0, c2)
         self.cum = np.stack([c0, c1, c2])
-        # Rayleigh sampling tables
+        # Rayleigh sampling tables: the cumulative of F^2 dx^2, piecewise linear in
+        # x^2 between the nodes of rayleigh_x2_nodes(); the sampler inverts
+        # exactly this piecewise-linear function, and ray_amax is evaluated on it
+        x2n = rayleigh_x2_nodes()
         x2, a, _ = xsection.rayleigh_cumulative(self.z_list, self.w_list)
-        a_inf = a[-1]
+        cum = np.interp(x2n, np.concatenate([[0.0], x2]), np.concatenate([[0.0], a]))
+        cum /= cum[-1]
+        self.ray_cum = cum
         k2 = (energy_grid() / xsection.HC_MEV_ANGSTROM) ** 2
-        self.ray_amax = np.interp(k2, x2, a / a_inf)
-        targets = np.linspace(0.0, 1.0, N_RINV)
-        an = a / a_inf
-        inv = np.interp(targets, np.concatenate([[0.0], an]), np.concatenate([[0.0], x2]))
-        self.ray_inv = inv
+        self.ray_amax = np.interp(k2, x2n, cum)
 
 
 class PhysicsTables:
@@ -94,12 +101,12 @@ class PhysicsTables:
         self.sig = np.zeros((nc, N_E), dtype=np.float32)
         self.cum = np.zeros((nc, 3, N_E), dtype=np.float32)
         self.ray_amax = np.zeros((nc, N_E), dtype=np.float32)
-        self.ray_inv = np.zeros((nc, N_RINV), dtype=np.float32)
+        self.ray_cum = np.zeros((nc, N_RAY), dtype=np.float32)
         for c, ct in enumerate(self.comps):
             self.sig[c] = (0.1 * ct.mu_rho).astype(np.float32)
             self.cum[c] = ct.cum.astype(np.float32)
             self.ray_amax[c] = ct.ray_amax.astype(np.float32)
-            self.ray_inv[c] = ct.ray_inv.astype(np.float32)
+            self.ray_cum[c] = ct.ray_cum.astype(np.float32)
 
     @property
     def n_comp(self):

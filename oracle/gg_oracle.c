@@ -382,9 +382,9 @@ static void rotate_dir(real u[3], real cost, real sint, real cphi, real sphi) {
 /* ------------------------------------------------------------------------ */
 typedef struct {
   /* tables */
-  int n_e, n_comp, n_rinv, n_mat;
+  int n_e, n_comp, n_ray, n_mat;
   real ln_emin, inv_dln, e_min, e_max;
-  real *sig, *cum, *ray_amax, *ray_inv, *mat_rho;
+  real *sig, *cum, *ray_amax, *ray_x2, *ray_cum, *mat_rho;
   int *mat_comp;
   /* image */
   int nx, ny, nz;
@@ -591,36 +591,49 @@ static void compton(const scene_t *s, photon_t *ph, rng_t *g, tally_t *t, real *
   }
 }
 
+/* Rayleigh scattering: x^2 = (sin(theta/2)/lambda)^2 drawn from the
+   tabulated form-factor cumulative (exact inversion of the piecewise-linear
+   cumulative by bisection), x^2 beyond (E/hc)^2 rejected, then the angle kept
+   with probability (1 + cos^2 theta)/2. */
 static void rayleigh(const scene_t *s, int comp, photon_t *ph, rng_t *g, tally_t *t) {
   real k = ph->e * R(1.0 / HC_MEV_ANGSTROM);
   real x2max = k * k;
   real amax = interp_row(s->ray_amax + (size_t)comp * s->n_e, ph->ei);
-  const real *inv = s->ray_inv + (size_t)comp * s->n_rinv;
-  real cost;
+  const real *cu = s->ray_cum + (size_t)comp * s->n_ray;
+  const real *xn = s->ray_x2;
+  real cost = R(1);
   int it = 0;
   for (;;) {
+    if (++it > LOOP_CAP) {
+      t->cnt[GG_CNT_LOOP_CAPPED]++;
+      break;
+    }
     real r = u01(g);
     real tt = r * amax;
-    real pos = tt * (real)(s->n_rinv - 1);
-    int j = (int)pos;
-    if (j > s->n_rinv - 2) j = s->n_rinv - 2;
-    real f = pos - (real)j;
-    real d = inv[j + 1] - inv[j];
+    int lo = 0, hi = s->n_ray - 1;
+    while (hi - lo > 1) {
+      int mid = (lo + hi) >> 1;
+      if (cu[mid] <= tt) lo = mid;
+      else hi = mid;
+    }
+    real den = cu[lo + 1] - cu[lo];
+    real f = R(0);
+    if (den > R(0)) {
+      f = tt - cu[lo];
+      f = f / den;
+    }
+    real d = xn[lo + 1] - xn[lo];
     d = f * d;
-    real x2 = inv[j] + d;
+    real x2 = xn[lo] + d;
+    if (x2 > x2max) continue;
     real q = R(2) * x2;
     q = q / x2max;
     cost = R(1) - q;
-    if (cost < R(-1)) cost = R(-1);
     real r2 = u01(g);
     real lhs = R(2) * r2;
     real rhs = cost * cost;
     rhs = R(1) + rhs;
     if (lhs <= rhs) break;
-    if (++it >= LOOP_CAP) {
-      t->cnt[GG_CNT_LOOP_CAPPED]++;
-      break;
-    }
   }
   real st2 = cost * cost;
   st2 = R(1) - st2;
@@ -930,20 +943,21 @@ static real *conv_d(const double *src, size_t n) {
 }
 
 static void scene_free(scene_t *s) {
-  free(s->sig); free(s->cum); free(s->ray_amax); free(s->ray_inv); free(s->mat_rho);
+  free(s->sig); free(s->cum); free(s->ray_amax); free(s->ray_x2); free(s->ray_cum); free(s->mat_rho);
   free(s->mat_comp); free(s->maj); free(s->s_spec_e); free(s->s_spec_cdf); free(s->acc_box);
 }
 
 static int scene_init(scene_t *s, const gg_tables_desc *tb, const gg_volume_desc *vol,
                       const gg_world_desc *w, const gg_source_desc *src) {
   memset(s, 0, sizeof(*s));
-  s->n_e = tb->n_e; s->n_comp = tb->n_comp; s->n_rinv = tb->n_rinv; s->n_mat = tb->n_mat;
+  s->n_e = tb->n_e; s->n_comp = tb->n_comp; s->n_ray = tb->n_ray; s->n_mat = tb->n_mat;
   s->ln_emin = (real)tb->ln_emin; s->inv_dln = (real)tb->inv_dln;
   s->e_min = (real)tb->e_min; s->e_max = (real)tb->e_max;
   s->sig = conv_f(tb->sig, (size_t)tb->n_comp * tb->n_e);
   s->cum = conv_f(tb->cum, (size_t)tb->n_comp * 3 * tb->n_e);
   s->ray_amax = conv_f(tb->ray_amax, (size_t)tb->n_comp * tb->n_e);
-  s->ray_inv = conv_f(tb->ray_inv, (size_t)tb->n_comp * tb->n_rinv);
+  s->ray_x2 = conv_f(tb->ray_x2, (size_t)tb->n_ray);
+  s->ray_cum = conv_f(tb->ray_cum, (size_t)tb->n_comp * tb->n_ray);
   s->mat_rho = conv_f(tb->mat_rho, (size_t)tb->n_mat);
   s->mat_comp = (int *)malloc(sizeof(int) * tb->n_mat);
   for (int i = 0; i < tb->n_mat; ++i) s->mat_comp[i] = tb->mat_comp[i];
@@ -1094,4 +1108,103 @@ void GGO_PREFIX(sample_compton)(double e, uint64_t seed, int n, double *eps_out,
     eps_out[i] = (double)ph.e / e;
     cost_out[i] = (double)ph.dir[2];
   }
+}
+
+/* Samples n primaries (history ids 0..n-1): position, direction, energy. */
+int GGO_PREFIX(sample_source)(const gg_tables_desc *tb, const gg_volume_desc *vol, const gg_world_desc *w,
+                              const gg_source_desc *src, uint64_t seed, int n, double *pos, double *dir,
+                              double *ene, uint64_t *counters) {
+  scene_t s;
+  scene_init(&s, tb, vol, w, src);
+  tally_t t;
+  memset(&t, 0, sizeof(t));
+  int st = GG_OK;
+  for (int i = 0; i < n && st == GG_OK; ++i) {
+    rng_t g;
+    rng_init(&g, seed, (uint64_t)i, 0u);
+    photon_t ph;
+    st = sample_primary(&s, &g, &ph, &t);
+    for (int a = 0; a < 3; ++a) {
+      pos[3 * i + a] = (double)ph.pos[a];
+      dir[3 * i + a] = (double)ph.dir[a];
+    }
+    ene[i] = (double)ph.e;
+  }
+  for (int c = 0; c < GG_N_COUNTERS; ++c) counters[c] += t.cnt[c];
+  scene_free(&s);
+  return st;
+}
+
+/* Samples n Rayleigh scatterings of a photon of energy e in composition comp;
+   writes cos(theta). */
+void GGO_PREFIX(sample_rayleigh)(const gg_tables_desc *tb, int comp, double e, uint64_t seed, int n,
+                                 double *cost_out) {
+  scene_t s;
+  memset(&s, 0, sizeof(s));
+  s.n_e = tb->n_e; s.n_comp = tb->n_comp; s.n_ray = tb->n_ray;
+  s.ln_emin = (real)tb->ln_emin; s.inv_dln = (real)tb->inv_dln; s.e_min = (real)tb->e_min;
+  s.ray_amax = conv_f(tb->ray_amax, (size_t)tb->n_comp * tb->n_e);
+  s.ray_x2 = conv_f(tb->ray_x2, (size_t)tb->n_ray);
+  s.ray_cum = conv_f(tb->ray_cum, (size_t)tb->n_comp * tb->n_ray);
+  s.maj = conv_f(tb->sig, (size_t)tb->n_e); /* any positive row */
+  tally_t t;
+  memset(&t, 0, sizeof(t));
+  for (int i = 0; i < n; ++i) {
+    rng_t g;
+    rng_init(&g, seed, (uint64_t)i, 0u);
+    photon_t ph;
+    memset(&ph, 0, sizeof(ph));
+    ph.dir[2] = R(1);
+    set_energy(&s, &ph, (real)e);
+    rayleigh(&s, comp, &ph, &g, &t);
+    cost_out[i] = (double)ph.dir[2];
+  }
+  free(s.ray_amax); free(s.ray_x2); free(s.ray_cum); free(s.maj);
+}
+
+/* First flight of n primaries: counts histories whose photon leaves the image
+   box without a real interaction (out[0]) and those that interact in it
+   (out[1]); primaries that never reach the image are not counted. */
+int GGO_PREFIX(first_flight)(const gg_tables_desc *tb, const gg_volume_desc *vol, const gg_world_desc *w,
+                             const gg_source_desc *src, uint64_t seed, int n, uint64_t *out) {
+  scene_t s;
+  scene_init(&s, tb, vol, w, src);
+  tally_t t;
+  memset(&t, 0, sizeof(t));
+  out[0] = out[1] = 0;
+  for (int i = 0; i < n; ++i) {
+    rng_t g;
+    rng_init(&g, seed, (uint64_t)i, 0u);
+    photon_t ph;
+    if (sample_primary(&s, &g, &ph, &t) != GG_OK) { scene_free(&s); return GG_ERR_DOMAIN; }
+    start_photon(&s, &ph);
+    if (!ph.in_image) {
+      real tin = entry_distance(ph.pos, ph.dir, s.bmin, s.bmax);
+      if (!(tin < R(INFINITY))) continue;
+      for (int a = 0; a < 3; ++a) ph.pos[a] = ph.pos[a] + tin * ph.dir[a];
+      ph.in_image = 1;
+      ph.t_exit = exit_distance(ph.pos, ph.dir, s.bmin, s.bmax);
+    }
+    for (;;) {
+      real u = u01_open0(&g);
+      real sd = -ggo_log(u);
+      sd = sd * ph.inv_mumax;
+      if (sd >= ph.t_exit) { out[0]++; break; }
+      ph.t_exit = ph.t_exit - sd;
+      for (int a = 0; a < 3; ++a) ph.pos[a] = ph.pos[a] + sd * ph.dir[a];
+      int ix = (int)((ph.pos[0] - s.bmin[0]) * s.inv_sp[0]);
+      int iy = (int)((ph.pos[1] - s.bmin[1]) * s.inv_sp[1]);
+      int iz = (int)((ph.pos[2] - s.bmin[2]) * s.inv_sp[2]);
+      ix = ix < 0 ? 0 : (ix >= s.nx ? s.nx - 1 : ix);
+      iy = iy < 0 ? 0 : (iy >= s.ny ? s.ny - 1 : iy);
+      iz = iz < 0 ? 0 : (iz >= s.nz ? s.nz - 1 : iz);
+      uint32_t v = (uint32_t)ix + (uint32_t)s.nx * ((uint32_t)iy + (uint32_t)s.ny * (uint32_t)iz);
+      int m = s.labels[v];
+      real mu = interp_row(s.sig + (size_t)s.mat_comp[m] * s.n_e, ph.ei);
+      mu = s.mat_rho[m] * mu;
+      if (u01(&g) * ph.mumax < mu) { out[1]++; break; }
+    }
+  }
+  scene_free(&s);
+  return GG_OK;
 }

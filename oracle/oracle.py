@@ -45,6 +45,19 @@ def lib(precision=32):
         f = getattr(L, pre + "sample_compton")
         f.argtypes = [ctypes.c_double, ctypes.c_uint64, ctypes.c_int,
                       ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
+        descs = [ctypes.POINTER(C.TablesDesc), ctypes.POINTER(C.VolumeDesc), ctypes.POINTER(C.WorldDesc),
+                 ctypes.POINTER(C.SourceDesc)]
+        f = getattr(L, pre + "sample_source")
+        f.restype = ctypes.c_int
+        f.argtypes = descs + [ctypes.c_uint64, ctypes.c_int, ctypes.POINTER(ctypes.c_double),
+                              ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double),
+                              ctypes.POINTER(ctypes.c_uint64)]
+        f = getattr(L, pre + "sample_rayleigh")
+        f.argtypes = [ctypes.POINTER(C.TablesDesc), ctypes.c_int, ctypes.c_double, ctypes.c_uint64, ctypes.c_int,
+                      ctypes.POINTER(ctypes.c_double)]
+        f = getattr(L, pre + "first_flight")
+        f.restype = ctypes.c_int
+        f.argtypes = descs + [ctypes.c_uint64, ctypes.c_int, ctypes.POINTER(ctypes.c_uint64)]
         _libs[precision] = L
     return _libs[precision]
 
@@ -92,3 +105,39 @@ def sample_compton(e, n, seed=1, precision=32):
     getattr(lib(precision), f"ggo{precision}_sample_compton")(
         float(e), seed, n, C.ptr(eps, ctypes.c_double), C.ptr(cost, ctypes.c_double))
     return eps, cost
+
+
+def _descs(scene):
+    return (ctypes.byref(scene.tables_desc), ctypes.byref(scene.volume_desc), ctypes.byref(scene.world_desc),
+            ctypes.byref(scene.source_desc))
+
+
+def sample_source(scene, n, seed=1, precision=32):
+    """Primary positions, directions and energies of histories 0..n-1."""
+    pos = np.zeros((n, 3))
+    d = np.zeros((n, 3))
+    e = np.zeros(n)
+    cnt = np.zeros(C.GG_N_COUNTERS, dtype=np.uint64)
+    st = getattr(lib(precision), f"ggo{precision}_sample_source")(
+        *_descs(scene), seed, n, C.ptr(pos, ctypes.c_double), C.ptr(d, ctypes.c_double),
+        C.ptr(e, ctypes.c_double), C.ptr(cnt, ctypes.c_uint64))
+    if st != 0:
+        raise RuntimeError(f"source sampling failed with status {st}")
+    return pos, d, e, {name: int(cnt[i]) for i, name in enumerate(C.COUNTER_NAMES)}
+
+
+def sample_rayleigh(scene, comp, e, n, seed=1, precision=32):
+    cost = np.zeros(n)
+    getattr(lib(precision), f"ggo{precision}_sample_rayleigh")(
+        ctypes.byref(scene.tables_desc), comp, float(e), seed, n, C.ptr(cost, ctypes.c_double))
+    return cost
+
+
+def first_flight(scene, n, seed=1, precision=32):
+    """(transmitted, interacted) counts of the first flight through the image."""
+    out = np.zeros(2, dtype=np.uint64)
+    st = getattr(lib(precision), f"ggo{precision}_first_flight")(*_descs(scene), seed, n,
+                                                                   C.ptr(out, ctypes.c_uint64))
+    if st != 0:
+        raise RuntimeError(f"first flight failed with status {st}")
+    return int(out[0]), int(out[1])
