@@ -193,6 +193,48 @@ int gg_get_counters(gg_ctx *ctx, uint64_t *out, size_t n);
 int gg_last_kernel_ms(gg_ctx *ctx, double *generate_ms, double *transport_ms, double *flush_ms,
                       int32_t *launches);
 
+/* ---- dose run that allocates no device memory ------------------------------
+ * No counterpart in the reference.  For callers that cannot call cudaMalloc
+ * while they work: cudaMalloc/cudaFree synchronise the whole device (a caller
+ * keeping other streams busy, such as an optimisation loop calling the dose
+ * engine many times, cannot afford that) and a caller whose device memory is
+ * already handed out by its own pool may have none left for another
+ * allocator.  The run uses the same kernels as gg_run; every scratch buffer
+ * lives in one static device array of GG_NOALLOC_SCRATCH_BYTES, which each GPU
+ * that loads the library reserves until the process exits.
+ *
+ * Inputs are the host descriptors of gg_upload_tables / gg_upload_volume /
+ * gg_set_world / gg_set_source; outputs are device pointers owned by the
+ * caller: d_edep (and d_edep2, or NULL to skip the squared image), n voxels
+ * of float64 each, overwritten with the edep / edep-squared images of
+ * histories [first_history, first_history + n_histories).  FP32 transport,
+ * batches of GG_NOALLOC_BATCH histories: the images equal those of gg_run
+ * with the same seed, histories and batch size.  Work runs on `stream`
+ * (cudaStream_t, NULL = legacy default stream) and is complete on return.
+ * counters (host, GG_N_COUNTERS slots) may be NULL; on error a message is
+ * written to err (err_len bytes, NUL-terminated).
+ *
+ * Sizes beyond the GG_NOALLOC_MAX_* limits are rejected with GG_ERR_ARG.
+ * All calls share the scratch array: each call clears the parts that must
+ * start at zero, and calls whose GPU work overlaps (other threads or
+ * unordered streams) race on it - serialise them.  The first call on a device
+ * looks up the array's device address (cudaGetSymbolAddress) with that device
+ * current; make that first call before any stream capture on the device.
+ */
+#define GG_NOALLOC_SCRATCH_BYTES (24u << 20)
+#define GG_NOALLOC_MAX_VOXELS (1u << 20)
+#define GG_NOALLOC_BATCH 65536
+#define GG_NOALLOC_MAX_ENERGIES 512
+#define GG_NOALLOC_MAX_COMPOSITIONS 16
+#define GG_NOALLOC_MAX_RAYLEIGH 1024
+#define GG_NOALLOC_MAX_MATERIALS 4096
+#define GG_NOALLOC_MAX_SPECTRUM 1024
+#define GG_NOALLOC_MAX_ACCEPT 16
+int gg_dose_run_noalloc(int32_t device, void *stream, const gg_tables_desc *tables, const gg_volume_desc *volume,
+                        const gg_world_desc *world, const gg_source_desc *source, uint64_t n_histories,
+                        uint64_t seed, uint64_t first_history, double *d_edep, double *d_edep2,
+                        uint64_t *counters, char *err, size_t err_len);
+
 #ifdef __cplusplus
 }
 #endif

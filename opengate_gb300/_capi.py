@@ -108,7 +108,15 @@ PROTOTYPES = [
     ("gg_get_counters", ctypes.c_int, [ctypes.c_void_p, _u64p, ctypes.c_size_t]),
     ("gg_last_kernel_ms", ctypes.c_int,
      [ctypes.c_void_p, _f64p, _f64p, _f64p, ctypes.POINTER(ctypes.c_int32)]),
+    ("gg_dose_run_noalloc", ctypes.c_int,
+     [ctypes.c_int32, ctypes.c_void_p, ctypes.POINTER(TablesDesc), ctypes.POINTER(VolumeDesc),
+      ctypes.POINTER(WorldDesc), ctypes.POINTER(SourceDesc), ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64,
+      ctypes.c_void_p, ctypes.c_void_p, _u64p, ctypes.c_char_p, ctypes.c_size_t]),
 ]
+
+# limits of gg_dose_run_noalloc (include/gate_gpu.h)
+GG_NOALLOC_MAX_VOXELS = 1 << 20
+GG_NOALLOC_BATCH = 65536
 
 _lib = None
 
