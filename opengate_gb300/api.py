@@ -1,0 +1,486 @@
+"""opengate-shaped Python API of the GPU path.
+
+Mirrors the subset of the reference's user API that the voxel photon path
+uses, with the same names, units and semantics:
+
+* ``Simulation`` (opengate/managers.py:1805): ``add_volume``, ``add_source``,
+  ``add_actor``, ``world``, ``physics_manager``, ``random_seed``,
+  ``output_dir``, ``run()``;
+* volumes: the world box, ``Box`` (only as a virtual volume in the world
+  material, e.g. an angular-acceptance target) and ``Image``
+  (``ImageVolume``, opengate/geometry/volumes.py:882) with ``image``,
+  ``material``, ``voxel_materials``, ``translation``;
+* ``HounsfieldUnit_to_material(sim, density_tolerance, file_mat,
+  file_density)`` (opengate/geometry/materials.py:149);
+* ``physics_manager.physics_list_name``, ``set_min_ekine``,
+  ``set_user_limits_particles`` (opengate/managers.py:701, 1071, 1102);
+* ``GenericSource`` (opengate/sources/generic.py:333) with ``n``,
+  ``position``, ``direction`` (incl. ``angular_acceptance``), ``energy``;
+* ``DoseActor`` (opengate/actors/doseactors.py:317): edep / edep_squared /
+  edep_uncertainty / dose / dose_squared / dose_uncertainty outputs,
+  ``number_of_samples``; ``SimulationStatisticsActor`` (miscactors.py:30).
+
+Options the GPU path does not implement raise errors at ``run()`` instead of
+being ignored; electron transport is not modelled, so the simulation must
+stop e-/e+ at creation with the user limits, exactly as the reference is
+configured for this path.
+"""
+
+import copy
+import math
+import os
+import pathlib
+import time
+
+import numpy as np
+
+from . import _capi as C
+from . import dose as D
+from . import image_io
+from . import materials as M
+from . import tables as T
+from .scene import Scene, SourceSpec
+from .units import g4_units
+
+u = g4_units
+
+
+class Box(dict):
+    """dict with attribute access; nested dicts become Boxes (python-box subset)."""
+
+    def __init__(self, *a, **k):
+        super().__init__(*a, **k)
+        for key, v in list(self.items()):
+            if isinstance(v, dict) and not isinstance(v, Box):
+                self[key] = Box(v)
+
+    def __getattr__(self, k):
+        try:
+            return self[k]
+        except KeyError as e:
+            raise AttributeError(k) from e
+
+    def __setattr__(self, k, v):
+        self[k] = Box(v) if isinstance(v, dict) and not isinstance(v, Box) else v
+
+
+class GateObject:
+    """Named object holding user parameters with defaults (GateObject pattern, base.py:362)."""
+
+    type_name = "GateObject"
+    user_info_defaults = {}
+
+    def __init__(self, name, simulation=None, **kw):
+        object.__setattr__(self, "name", name)
+        object.__setattr__(self, "simulation", simulation)
+        for k, v in self.user_info_defaults.items():
+            object.__setattr__(self, k, copy.deepcopy(v))
+        for k, v in kw.items():
+            setattr(self, k, v)
+
+    def __setattr__(self, k, v):
+        if k not in self.user_info_defaults and not k.startswith("_") and k not in ("name", "simulation"):
+            raise AttributeError(f"{self.type_name} '{self.name}' has no parameter '{k}'")
+        if isinstance(v, dict) and not isinstance(v, Box):
+            v = Box(v)
+        object.__setattr__(self, k, v)
+
+
+# --------------------------------------------------------------------------- volumes
+class BoxVolume(GateObject):
+    type_name = "Box"
+    user_info_defaults = {"mother": "world", "size": [10 * u.cm] * 3, "translation": [0.0, 0.0, 0.0],
+                          "rotation": np.eye(3), "material": "G4_AIR", "color": [1, 1, 1, 1]}
+
+
+class ImageVolume(GateObject):
+    type_name = "Image"
+    user_info_defaults = {"mother": "world", "image": "", "material": "G4_AIR",
+                          "voxel_materials": [[-np.inf, np.inf, "G4_AIR"]], "translation": [0.0, 0.0, 0.0],
+                          "rotation": np.eye(3), "dump_label_image": None, "color": [1, 1, 1, 1]}
+
+    def load_image(self):
+        """HU image as an image_io.Image (array [z][y][x], spacing in mm)."""
+        img = self.image
+        if isinstance(img, image_io.Image):
+            return img
+        if isinstance(img, (str, pathlib.Path)) and str(img):
+            return image_io.read_mhd(img)
+        raise ValueError(f"ImageVolume '{self.name}': set .image to an .mhd path or an image_io.Image")
+
+
+class VolumeManager:
+    def __init__(self, simulation):
+        self.simulation = simulation
+        self.material_database = M.MaterialDatabase()
+        self.world = BoxVolume("world", simulation, size=[3 * u.m] * 3, material="G4_AIR", mother=None)
+        self.volumes = {"world": self.world}
+
+    def add_volume(self, volume_type, name):
+        if name in self.volumes:
+            raise ValueError(f"a volume named '{name}' already exists")
+        cls = {"Box": BoxVolume, "BoxVolume": BoxVolume, "Image": ImageVolume, "ImageVolume": ImageVolume}.get(
+            volume_type)
+        if cls is None:
+            raise NotImplementedError(f"volume type '{volume_type}' is not supported by the GPU path")
+        v = cls(name, self.simulation)
+        self.volumes[name] = v
+        return v
+
+
+def HounsfieldUnit_to_material(simulation, density_tolerance, file_mat, file_density):
+    """Same signature as the reference's; the tolerance carries G4 density units."""
+    return M.hounsfield_unit_to_material(simulation.volume_manager.material_database,
+                                         density_tolerance / u.g_cm3, file_mat, file_density)
+
+
+# --------------------------------------------------------------------------- physics
+class PhysicsManager:
+    def __init__(self, simulation):
+        self.simulation = simulation
+        self.physics_list_name = "QGSP_BERT_EMV"
+        self.min_ekine = {}
+        self.user_limits_particles = set()
+        self.production_cuts = {}
+
+    def set_min_ekine(self, volume_name, value):
+        self.min_ekine[volume_name] = float(value)
+
+    def set_user_limits_particles(self, particles):
+        for p in ([particles] if isinstance(particles, str) else particles):
+            self.user_limits_particles.add(p)
+
+    def set_production_cut(self, volume_name, particle_name, value):
+        self.production_cuts[(volume_name, particle_name)] = value
+
+    def check_supported(self, max_energy):
+        if self.physics_list_name != "G4EmStandardPhysics":
+            raise NotImplementedError(
+                f"physics list '{self.physics_list_name}': the GPU path implements G4EmStandardPhysics photons")
+        if not {"e-", "e+"} <= self.user_limits_particles:
+            raise NotImplementedError("electron transport is not modelled: call "
+                                      "set_user_limits_particles(['e-', 'e+']) and set_min_ekine above the "
+                                      "source energy so electrons and positrons stop at creation")
+        if not self.min_ekine or min(self.min_ekine.values()) < max_energy:
+            raise NotImplementedError("set_min_ekine(<world or image volume>, value) must exceed the highest "
+                                      "source energy so e-/e+ stop at creation")
+
+
+# --------------------------------------------------------------------------- sources
+def _default_angular_acceptance():
+    # same keys and defaults as generic_source_default_aa (actors/biasingactors.py:16-66)
+    return Box({"policy": None, "skip_policy": "SkipEvents", "max_rejection": 10000, "target_volumes": [],
+                "enable_intersection_check": False, "enable_angle_check": False,
+                "angle_check_reference_vector": [0, 0, 1], "angle_check_proximity_distance": 0.0,
+                "angle_tolerance_proximal": 90 * u.deg, "angle_tolerance_min": 0.0,
+                "angle_tolerance_max": 6 * u.deg})
+
+
+class GenericSource(GateObject):
+    """Parameters as in opengate/sources/generic.py:24-77, 353-422 (photons)."""
+
+    type_name = "GenericSource"
+    user_info_defaults = {
+        "attached_to": "world", "particle": "gamma", "n": 0, "activity": 0.0, "half_life": -1,
+        "weight": -1, "weight_sigma": -1,
+        "position": Box({"type": "point", "radius": 0.0, "sigma_x": 0.0, "sigma_y": 0.0, "size": [0, 0, 0],
+                         "translation": [0, 0, 0], "rotation": np.eye(3), "confine": None, "dz": None}),
+        "direction": Box({"type": "iso", "theta": [0.0, 180 * u.deg], "phi": [0.0, 360 * u.deg],
+                          "momentum": [0, 0, 1], "focus_point": [0, 0, 0], "sigma": [0, 0],
+                          "angular_acceptance": _default_angular_acceptance()}),
+        "energy": Box({"type": "mono", "mono": 0.0, "sigma_gauss": 0.0, "is_cdf": False, "min_energy": None,
+                       "max_energy": None, "spectrum_weights": [], "spectrum_energies": [],
+                       "spectrum_energy_bin_edges": [], "spectrum_histogram_interpolation": None}),
+    }
+
+    def to_spec(self, volumes):
+        """SourceSpec (mm, rad, MeV) of this source; raises on unsupported options."""
+        if self.particle != "gamma":
+            raise NotImplementedError(f"source '{self.name}': only gamma primaries are transported")
+        if self.attached_to != "world":
+            raise NotImplementedError(f"source '{self.name}': sources must be attached to the world")
+        if self.weight not in (-1, 1) or self.weight_sigma > 0:
+            raise NotImplementedError(f"source '{self.name}': primary weights are not supported")
+        s = SourceSpec()
+        p = self.position
+        s.pos_type = {"point": C.GG_POS_POINT, "box": C.GG_POS_BOX, "sphere": C.GG_POS_SPHERE,
+                      "disc": C.GG_POS_DISC}.get(p.type)
+        if s.pos_type is None or p.confine:
+            raise NotImplementedError(f"source '{self.name}': position type '{p.type}' / confine unsupported")
+        s.translation = [float(x) for x in p.translation]
+        s.rotation = np.asarray(p.rotation, dtype=np.float64)
+        s.half_size = [float(x) / 2.0 for x in p.size]
+        s.radius = float(p.radius)
+        d = self.direction
+        s.dir_type = {"iso": C.GG_DIR_ISO, "momentum": C.GG_DIR_MOMENTUM, "focused": C.GG_DIR_FOCUSED}.get(d.type)
+        if s.dir_type is None:
+            raise NotImplementedError(f"source '{self.name}': direction type '{d.type}' unsupported")
+        s.theta = [float(x) for x in d.theta]
+        s.phi = [float(x) for x in d.phi]
+        s.momentum = [float(x) for x in d.momentum]
+        s.focus = [float(x) for x in d.focus_point]
+        aa = d.angular_acceptance
+        if aa.policy:
+            if aa.policy != "Rejection" or aa.skip_policy != "SkipEvents" or aa.enable_angle_check or \
+                    not aa.enable_intersection_check:
+                raise NotImplementedError("angular acceptance: only policy 'Rejection' with 'SkipEvents' and "
+                                          "the intersection check is supported")
+            if s.dir_type != C.GG_DIR_ISO:
+                raise ValueError("'SkipEvents' needs an 'iso' direction (GateAcceptanceAngleManager)")
+            for vname in aa.target_volumes:
+                v = volumes[vname]
+                if not isinstance(v, BoxVolume) or not np.allclose(v.rotation, np.eye(3)):
+                    raise NotImplementedError("acceptance targets must be unrotated Box volumes")
+                c = np.asarray(v.translation, dtype=np.float64)
+                h = np.asarray(v.size, dtype=np.float64) / 2.0
+                s.accept_boxes.append((tuple(c - h), tuple(c + h)))
+            s.max_rejection = int(aa.max_rejection)
+        e = self.energy
+        if e.type == "mono":
+            s.ene_type, s.mono = C.GG_ENE_MONO, float(e.mono)
+        elif e.type == "range":
+            s.ene_type, s.e_lo, s.e_hi = C.GG_ENE_RANGE, float(e.min_energy), float(e.max_energy)
+        elif e.type == "spectrum_discrete":
+            w = np.cumsum(np.asarray(e.spectrum_weights, dtype=np.float64))
+            s.ene_type, s.spec_e, s.spec_cdf = C.GG_ENE_LINES, np.asarray(e.spectrum_energies, float), w / w[-1]
+        elif e.type == "spectrum_histogram":
+            if e.spectrum_histogram_interpolation not in (None, "None", "none"):
+                raise NotImplementedError("spectrum_histogram: only interpolation None is supported")
+            edges = np.asarray(e.spectrum_energy_bin_edges, dtype=np.float64)
+            w = np.asarray(e.spectrum_weights, dtype=np.float64)
+            if len(edges) != len(w) + 1:
+                raise ValueError("spectrum_energy_bin_edges must have one more element than spectrum_weights")
+            acc = np.cumsum(w * np.diff(edges))  # GateGenericSource.cpp:602-608
+            s.ene_type, s.spec_e, s.spec_cdf = C.GG_ENE_HISTOGRAM, edges, acc / acc[-1]
+        else:
+            raise NotImplementedError(f"source '{self.name}': energy type '{e.type}' unsupported")
+        return s
+
+    def n_events(self):
+        if self.activity and not self.n:
+            raise NotImplementedError("activity-driven sources: set n (number of primaries)")
+        return int(self.n)
+
+
+# --------------------------------------------------------------------------- actors
+class ActorOutput:
+    """One output image of an actor (edep, dose, uncertainty ...)."""
+
+    def __init__(self, actor, suffix, active=False, write_to_disk=True):
+        self.actor = actor
+        self.suffix = suffix
+        self.active = active
+        self.write_to_disk = write_to_disk
+        self.image = None
+        self.number_of_samples = 0
+
+    def get_data(self):
+        return self.image
+
+    def get_output_path(self):
+        base = self.actor.output_filename
+        if base in (None, "auto", ""):
+            base = f"{self.actor.name}.mhd"
+        base = pathlib.Path(base)
+        sim = self.actor.simulation
+        return pathlib.Path(sim.output_dir) / f"{base.stem}_{self.suffix}.mhd"
+
+
+class DoseActor(GateObject):
+    """Parameters as in VoxelDepositActor / DoseActor (doseactors.py:50-116, 317-440)."""
+
+    type_name = "DoseActor"
+    user_info_defaults = {"attached_to": "world", "size": [10, 10, 10], "spacing": [1.0, 1.0, 1.0],
+                          "translation": [0.0, 0.0, 0.0], "rotation": np.eye(3), "repeated_volume_index": 0,
+                          "hit_type": "random", "output_coordinate_system": "local", "output_filename": "auto",
+                          "score_in": "material", "uncertainty_goal": None, "priority": 100}
+
+    def __init__(self, name, simulation=None, **kw):
+        super().__init__(name, simulation, **kw)
+        for suffix, active in (("edep", True), ("edep_squared", False), ("edep_uncertainty", False),
+                               ("dose", False), ("dose_squared", False), ("dose_uncertainty", False)):
+            object.__setattr__(self, suffix, ActorOutput(self, suffix, active))
+
+    def check(self, image_volume, image):
+        if self.attached_to != image_volume.name:
+            raise NotImplementedError("the DoseActor must be attached to the ImageVolume")
+        if self.uncertainty_goal is not None:
+            raise NotImplementedError("uncertainty_goal (early stop) is not supported yet")
+        if self.score_in not in ("material", None):
+            raise NotImplementedError("score_in other than 'material' is not supported")
+        if self.hit_type not in ("random", "pre", "post", "middle"):
+            raise ValueError(f"hit_type '{self.hit_type}'")
+        same = list(self.size) == list(image.size) and np.allclose(self.spacing, image.spacing) and \
+            np.allclose(self.translation, 0.0)
+        if not same:
+            raise NotImplementedError("the dose grid must be the image grid (size and spacing of the image)")
+
+    @property
+    def number_of_samples(self):
+        return self.edep.number_of_samples
+
+
+class SimulationStatisticsActor(GateObject):
+    type_name = "SimulationStatisticsActor"
+    user_info_defaults = {"attached_to": "world", "track_types_flag": False, "output_filename": "auto"}
+
+    def __init__(self, name, simulation=None, **kw):
+        super().__init__(name, simulation, **kw)
+        object.__setattr__(self, "counts", Box({"runs": 0, "events": 0, "tracks": 0, "steps": 0,
+                                                "duration": 0.0, "pps": 0, "sps": 0}))
+
+    def __str__(self):
+        c = self.counts
+        return (f"runs {c.runs}\nevents {c.events}\ntracks {c.tracks}\nsteps {c.steps}\n"
+                f"duration {c.duration / u.s:.4f} s\nPPS {c.pps}")
+
+
+# --------------------------------------------------------------------------- simulation
+class Simulation:
+    """Configuration object graph and run entry point (opengate/managers.py:1805)."""
+
+    def __init__(self, name="simulation"):
+        self.name = name
+        self.output_dir = "."
+        self.random_seed = "auto"
+        self.random_engine = "MixMaxRng"  # accepted; the GPU path uses Philox4x32-10 streams
+        self.number_of_threads = 1  # accepted; histories run on the GPU
+        self.verbose_level = "INFO"
+        self.run_timing_intervals = [[0, 1 * u.s]]
+        self.device = 0  # CUDA device ordinal
+        self.precision = 32  # transport arithmetic: 32 or 64
+        self.batch = 0  # histories per tally batch, 0 = library default
+        self.volume_manager = VolumeManager(self)
+        self.physics_manager = PhysicsManager(self)
+        self.sources = {}
+        self.actors = {}
+        self.last_seed = None
+
+    # -- object graph -------------------------------------------------------
+    @property
+    def world(self):
+        return self.volume_manager.world
+
+    @property
+    def volumes(self):
+        return self.volume_manager.volumes
+
+    def add_volume(self, volume_type, name):
+        return self.volume_manager.add_volume(volume_type, name)
+
+    def add_source(self, source_type, name):
+        if name in self.sources:
+            raise ValueError(f"a source named '{name}' already exists")
+        if source_type != "GenericSource":
+            raise NotImplementedError(f"source type '{source_type}' is not supported by the GPU path")
+        s = GenericSource(name, self)
+        self.sources[name] = s
+        return s
+
+    def add_actor(self, actor_type, name):
+        if name in self.actors:
+            raise ValueError(f"an actor named '{name}' already exists")
+        cls = {"DoseActor": DoseActor, "SimulationStatisticsActor": SimulationStatisticsActor}.get(actor_type)
+        if cls is None:
+            raise NotImplementedError(f"actor type '{actor_type}' is not supported by the GPU path")
+        a = cls(name, self)
+        self.actors[name] = a
+        return a
+
+    def get_output_path(self, name):
+        return pathlib.Path(self.output_dir) / name
+
+    # -- run ---------------------------------------------------------------
+    def _seed(self):
+        if self.random_seed in (None, "auto"):
+            return int.from_bytes(os.urandom(8), "little")
+        return int(self.random_seed) & 0xFFFFFFFFFFFFFFFF
+
+    def build_scene(self):
+        """(scene, image volume, HU image, material names by label, sources) for this configuration."""
+        images = [v for v in self.volumes.values() if isinstance(v, ImageVolume)]
+        if len(images) != 1:
+            raise NotImplementedError("the GPU path transports through exactly one ImageVolume")
+        vol = images[0]
+        if vol.mother != "world" or not np.allclose(vol.rotation, np.eye(3)):
+            raise NotImplementedError("the ImageVolume must be an unrotated daughter of the world")
+        for v in self.volumes.values():
+            if isinstance(v, BoxVolume) and v is not self.world and v.material != self.world.material:
+                raise NotImplementedError(f"volume '{v.name}': only the image and virtual boxes in the world "
+                                          "material are supported")
+        hu = vol.load_image()
+        db = self.volume_manager.material_database
+        lut = M.material_to_label_lut(vol.material, vol.voxel_materials)
+        names = sorted(lut, key=lut.get)
+        labels = M.create_label_image(hu.array, vol.material, vol.voxel_materials, lut)
+        if self.world.material not in names:
+            names.append(self.world.material)
+        mats = [db.get(n) for n in names]
+        pt = T.PhysicsTables(mats)
+        spacing = hu.spacing
+        size = np.array(hu.size, dtype=np.float64)
+        corner = np.asarray(vol.translation, dtype=np.float64) - size * spacing / 2.0
+        sources = [s for s in self.sources.values()]
+        if not sources:
+            raise ValueError("no source")
+        specs = [s.to_spec(self.volumes) for s in sources]
+        emax = max(sp.energy_bounds()[1] for sp in specs)
+        self.physics_manager.check_supported(emax)
+        half = [float(x) / 2.0 for x in self.world.size]
+        scene = Scene(pt, labels, spacing, corner, half, names.index(self.world.material), specs[0])
+        return scene, vol, hu, names, list(zip(sources, specs))
+
+    def run(self, start_new_process=False):
+        from .engine import DoseEngine
+
+        if len(self.run_timing_intervals) != 1:
+            raise NotImplementedError("one run (run_timing_intervals of length 1) for the dose path")
+        t0 = time.perf_counter()
+        scene, vol, hu, names, sources = self.build_scene()
+        seed = self._seed()
+        self.last_seed = seed
+        doses = [a for a in self.actors.values() if isinstance(a, DoseActor)]
+        for a in doses:
+            a.check(vol, hu)
+        if vol.dump_label_image:
+            image_io.write_mhd(self.get_output_path(vol.dump_label_image),
+                               image_io.Image(scene.labels, hu.spacing, hu.origin))
+        eng = DoseEngine(scene, device=self.device, precision=self.precision, batch=self.batch)
+        try:
+            first = 0
+            for k, (src, spec) in enumerate(sources):
+                if k:
+                    eng.set_source(spec)
+                n = src.n_events()
+                eng.run(n, seed, first)
+                first += n
+            edep, edep2, cnt = eng.edep(), eng.edep_squared(), eng.counters()
+        finally:
+            eng.close()
+        elapsed = time.perf_counter() - t0
+        n_events = first
+        rho = scene.voxel_density()
+        for a in doses:
+            origin = hu.origin if a.output_coordinate_system == "attached_to_image" else None
+            dose = D.edep_to_dose(edep, rho, hu.spacing)
+            dose2 = D.edep_to_dose(edep2, rho, hu.spacing, squared=True)
+            data = {"edep": edep, "edep_squared": edep2,
+                    "edep_uncertainty": D.variance_or_uncertainty(edep, edep2, n_events, "uncertainty"),
+                    "dose": dose, "dose_squared": dose2,
+                    "dose_uncertainty": D.variance_or_uncertainty(dose, dose2, n_events, "uncertainty")}
+            for key, arr in data.items():
+                out = getattr(a, key)
+                out.image = image_io.Image(arr, hu.spacing, origin)
+                out.number_of_samples = n_events
+                if out.active and out.write_to_disk:
+                    image_io.write_mhd(out.get_output_path(), out.image)
+        for a in self.actors.values():
+            if isinstance(a, SimulationStatisticsActor):
+                a.counts.runs = 1
+                a.counts.events = n_events
+                a.counts.tracks = n_events + cnt["secondaries"]
+                a.counts.steps = cnt["woodcock_steps"] + cnt["world_steps"]
+                a.counts.duration = elapsed * u.s
+                a.counts.pps = int(n_events / elapsed) if elapsed > 0 else 0
+                a.counts.sps = int(a.counts.steps / elapsed) if elapsed > 0 else 0
+        return cnt

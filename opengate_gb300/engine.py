@@ -40,6 +40,11 @@ class DoseEngine:
         self._call("gg_set_source", ctypes.byref(s.source_desc))
         self._call("gg_add_dose_tally", 1 if self.score_squared else 0)
 
+    def set_source(self, source):
+        """Switches to another source (tables, volume and tally are kept)."""
+        self.scene.set_source(source)
+        self._call("gg_set_source", ctypes.byref(self.scene.source_desc))
+
     def reset(self):
         self._call("gg_reset_tally")
 

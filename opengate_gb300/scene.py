@@ -142,6 +142,14 @@ class Scene:
         d.e_hi = float(s.e_hi)
         self.source_desc = d
 
+    def set_source(self, source):
+        """Replaces the source (validated like the constructor) and rebuilds the descriptors."""
+        lo, hi = source.energy_bounds()
+        if lo < T.E_MIN or hi > T.E_MAX:
+            raise ValueError(f"source energies [{lo}, {hi}] MeV outside the tables [{T.E_MIN}, {T.E_MAX}]")
+        self.source = source
+        self._build_descs()
+
     @property
     def n_voxels(self):
         return int(self.labels.size)

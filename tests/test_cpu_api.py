@@ -1,0 +1,135 @@
+"""opengate-shaped API: configuration, validation and image I/O (no GPU)."""
+
+import numpy as np
+import pytest
+
+import opengate_gb300 as gate
+from opengate_gb300 import _capi as C
+from opengate_gb300 import workloads as W
+
+u = gate.g4_units
+
+
+def water_sim(tmp_path, n=1000):
+    """The 64^3 water cube / 1 MeV pencil beam written the way an opengate script does it."""
+    sim = gate.Simulation()
+    sim.output_dir = tmp_path
+    sim.random_seed = 12345678
+    sim.world.size = [2 * u.m, 2 * u.m, 2 * u.m]
+    sim.world.material = "G4_AIR"
+    img = sim.add_volume("Image", "phantom")
+    img.image = gate.Image(np.zeros((64, 64, 64), np.int16), spacing=(2.0, 2.0, 2.0))
+    img.material = "G4_AIR"
+    img.voxel_materials = [[-1000, 1000, "G4_WATER"]]
+    sim.physics_manager.physics_list_name = "G4EmStandardPhysics"
+    sim.physics_manager.set_min_ekine("world", 10 * u.MeV)
+    sim.physics_manager.set_user_limits_particles(["e-", "e+"])
+    src = sim.add_source("GenericSource", "beam")
+    src.particle = "gamma"
+    src.n = n
+    src.position.type = "point"
+    src.position.translation = [0, 0, -64 * u.mm]
+    src.direction.type = "momentum"
+    src.direction.momentum = [0, 0, 1]
+    src.energy.type = "mono"
+    src.energy.mono = 1 * u.MeV
+    dose = sim.add_actor("DoseActor", "dose")
+    dose.attached_to = "phantom"
+    dose.size = [64, 64, 64]
+    dose.spacing = [2 * u.mm] * 3
+    dose.edep_uncertainty.active = True
+    dose.dose.active = True
+    dose.dose_uncertainty.active = True
+    sim.add_actor("SimulationStatisticsActor", "stats")
+    return sim
+
+
+def test_api_scene_equals_workload_scene(tmp_path):
+    sim = water_sim(tmp_path)
+    scene, vol, hu, names, sources = sim.build_scene()
+    ref = W.water_pencil()
+    assert names == ["G4_AIR", "G4_WATER"]
+    # label 0 = image material (air), 1 = water: all voxels are water here
+    assert np.all(scene.labels == 1)
+    assert scene.corner == ref.corner and scene.spacing == ref.spacing
+    s, r = scene.source_desc, ref.source_desc
+    assert list(s.translation) == list(r.translation) and s.mono == r.mono and s.dir_type == r.dir_type
+    water = names.index("G4_WATER")
+    np.testing.assert_array_equal(scene.pt.sig[scene.pt.mat_comp[water]], ref.pt.sig[ref.pt.mat_comp[0]])
+
+
+def test_unsupported_options_raise(tmp_path):
+    sim = water_sim(tmp_path)
+    sim.physics_manager.physics_list_name = "QGSP_BERT_EMV"
+    with pytest.raises(NotImplementedError):
+        sim.build_scene()
+    sim = water_sim(tmp_path)
+    sim.physics_manager.user_limits_particles = set()
+    with pytest.raises(NotImplementedError):
+        sim.build_scene()
+    sim = water_sim(tmp_path)
+    sim.sources["beam"].energy.type = "F18_analytic"
+    with pytest.raises(NotImplementedError):
+        sim.build_scene()
+    with pytest.raises(AttributeError):
+        sim.sources["beam"].not_a_parameter = 3
+    with pytest.raises(NotImplementedError):
+        sim.add_actor("LETActor", "let")
+    sim = water_sim(tmp_path)
+    sim.actors["dose"].spacing = [4 * u.mm] * 3
+    scene, vol, hu, names, sources = sim.build_scene()
+    with pytest.raises(NotImplementedError):
+        sim.actors["dose"].check(vol, hu)
+
+
+def test_spectrum_and_acceptance_conversion(tmp_path):
+    sim = water_sim(tmp_path)
+    src = sim.sources["beam"]
+    src.energy.type = "spectrum_histogram"
+    src.energy.spectrum_energy_bin_edges = [0.1, 0.2, 0.4]
+    src.energy.spectrum_weights = [2.0, 1.0]
+    src.direction.type = "iso"
+    field = sim.add_volume("Box", "field")
+    field.size = [10 * u.cm, 1 * u.mm, 10 * u.cm]
+    field.translation = [0, -20 * u.cm, 0]
+    src.direction.angular_acceptance.policy = "Rejection"
+    src.direction.angular_acceptance.enable_intersection_check = True
+    src.direction.angular_acceptance.target_volumes = ["field"]
+    spec = src.to_spec(sim.volumes)
+    assert spec.ene_type == C.GG_ENE_HISTOGRAM
+    np.testing.assert_allclose(spec.spec_cdf, [0.2 / 0.4, 1.0])  # cumulative of w * dE
+    assert spec.accept_boxes == [((-50.0, -200.5, -50.0), (50.0, -199.5, 50.0))]
+    src.energy.type = "spectrum_discrete"
+    src.energy.spectrum_energies = [0.1405, 0.364]
+    src.energy.spectrum_weights = [0.89, 0.11]
+    spec = src.to_spec(sim.volumes)
+    np.testing.assert_allclose(spec.spec_cdf, [0.89, 1.0])
+
+
+def test_hounsfield_api_wrapper_uses_g4_density_units(tmp_path):
+    sim = gate.Simulation()
+    vm, created = gate.HounsfieldUnit_to_material(sim, 0.05 * u.g_cm3, W.CT10_MATERIALS, W.CT10_DENSITIES)
+    ref_vm, _ = W.ct_materials(0.05)[:2]
+    assert vm == ref_vm
+    assert sim.volume_manager.material_database.get(created[0]).density == pytest.approx(0.0012)
+
+
+def test_mhd_round_trip(tmp_path):
+    rng = np.random.default_rng(1)
+    for dt in (np.int16, np.float32, np.float64, np.uint16):
+        arr = (rng.normal(size=(5, 6, 7)) * 100).astype(dt)
+        img = gate.Image(arr, spacing=(1.5, 2.0, 2.5), origin=(-3.0, 4.0, 5.5))
+        p = gate.write_mhd(tmp_path / f"img_{np.dtype(dt).name}.mhd", img)
+        back = gate.read_mhd(p)
+        assert back.array.dtype == arr.dtype
+        np.testing.assert_array_equal(back.array, arr)
+        np.testing.assert_array_equal(back.spacing, img.spacing)
+        np.testing.assert_array_equal(back.origin, img.origin)
+        assert back.size == (7, 6, 5)
+
+
+def test_units_follow_clhep():
+    assert u.mm == 1 and u.MeV == 1 and u.cm == 10
+    assert u.g_cm3 == pytest.approx(6.241509074460763e18, rel=1e-12)
+    assert u.Gy == pytest.approx(1e-12, rel=1e-12)
+    assert u.deg == pytest.approx(np.pi / 180)
