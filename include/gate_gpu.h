@@ -62,6 +62,7 @@ extern "C" {
 #define GG_POS_BOX 1
 #define GG_POS_SPHERE 2
 #define GG_POS_DISC 3
+#define GG_POS_VOXELS 4 /* VoxelSource: activity image, 3-level CDF */
 
 /* direction types (GenericSource direction.type) */
 #define GG_DIR_ISO 0
@@ -91,6 +92,8 @@ extern "C" {
 #define GG_CNT_LOOP_CAPPED 9    /* sampling loops stopped at their iteration cap */
 #define GG_CNT_STACK_OVERFLOW 10
 #define GG_CNT_SECONDARIES 11   /* annihilation photons created */
+#define GG_CNT_HEAD_STEPS 12    /* transport steps inside SPECT heads */
+#define GG_CNT_SINGLES 13       /* events with energy deposited in a crystal */
 #define GG_N_COUNTERS 16
 
 /* Physics tables: see opengate_gb300/tables.py for the contract. */
@@ -152,7 +155,43 @@ typedef struct {
   const double *spec_e; /* lines: [n]; histogram: [n+1] edges; MeV */
   const double *spec_cdf; /* [n], normalised cumulative weights */
   double e_lo, e_hi;    /* range */
+  /* GG_POS_VOXELS (GateSPSVoxelsPosDistribution): voxel (k, j, i) chosen by
+     lower_bound on cdf_z, then cdf_y[i], then cdf_x[i][j] (draws in (0, 1]),
+     position = corner + (index + 0.5) * spacing + (u - 0.5) * spacing */
+  int32_t vox_dims[3];      /* nx, ny, nz of the activity image */
+  double vox_spacing[3];    /* mm */
+  double vox_corner[3];     /* mm, outer corner of voxel (0, 0, 0), world */
+  const float *cdf_z;       /* [nz] */
+  const float *cdf_y;       /* [nz][ny] */
+  const float *cdf_x;       /* [nz][ny][nx] */
 } gg_source_desc;
+
+/* SPECT heads: parallel-hole collimator + crystal, and the projection digitizer
+   (Hits -> Adder EnergyWinnerPosition -> EnergyWindows -> Projection).
+   Head-local frame: w along the head's outward normal with the collimator
+   front face at w = 0, (a1, a2) along the detector axes e1, e2.  The head box
+   is |a1|, |a2| <= half_width, 0 <= w <= collimator + gap + crystal.  The
+   collimator is the collimator material with hexagonal holes (vacuum) of
+   apothem hole_apothem on two rectangular lattices of pitch (pitch_x,
+   pitch_y), the second shifted by half a pitch in both axes; hole faces are
+   normal to 30, 90 and 150 degrees in the (a1, a2) plane. */
+typedef struct {
+  double half_width;           /* mm */
+  double collimator_thickness; /* mm */
+  double gap;                  /* mm, vacuum between collimator and crystal */
+  double crystal_thickness;    /* mm */
+  double hole_apothem;         /* mm (flat-to-flat / 2) */
+  double pitch_x, pitch_y;     /* mm */
+  int32_t collimator_material; /* material table index */
+  int32_t crystal_material;    /* material table index */
+  int32_t n_windows;           /* <= 8 */
+  double window_lo[8];         /* MeV, window k = [lo, hi) */
+  double window_hi[8];
+  int32_t size[2];             /* projection pixels along e1, e2 */
+  double spacing[2];           /* mm */
+  int32_t n_heads;             /* 1 or 2 */
+  int32_t n_runs;              /* gantry positions; projection slice = window + run * n_windows */
+} gg_spect_desc;
 
 typedef struct gg_ctx gg_ctx;
 
@@ -193,6 +232,20 @@ int gg_get_counters(gg_ctx *ctx, uint64_t *out, size_t n);
 int gg_last_kernel_ms(gg_ctx *ctx, double *generate_ms, double *transport_ms, double *flush_ms,
                       int32_t *launches);
 
+/* SPECT (replaces the NM670 head of contrib/spect/ge_discovery_nm670.py:125-164,
+   464-490 and GateDigitizerHitsCollectionActor / GateDigiAdderInVolume /
+   GateDigitizerEnergyWindowsActor / GateDigitizerProjectionActor,
+   core/opengate_core/opengate_lib/digitizer/*.cpp).  gg_spect_setup enables
+   the head transport and zeroes the projection counts; the dose tally is not
+   needed.  gg_spect_set_heads places the heads for one run (gantry position):
+   frames[n_heads][12] = collimator front-face centre xyz, outward normal xyz,
+   e1 xyz, e2 xyz (world, unit vectors); the following gg_run calls score into
+   that run's slices.  gg_get_projection returns the counts as float64,
+   [head][run][window][size[1]][size[0]]. */
+int gg_spect_setup(gg_ctx *ctx, const gg_spect_desc *spect);
+int gg_spect_set_heads(gg_ctx *ctx, int32_t run, const double *frames);
+int gg_get_projection(gg_ctx *ctx, double *out, size_t n);
+
 /* ---- dose run that allocates no device memory ------------------------------
  * No counterpart in the reference.  For callers that cannot call cudaMalloc
  * while they work: cudaMalloc/cudaFree synchronise the whole device (a caller
@@ -214,14 +267,15 @@ int gg_last_kernel_ms(gg_ctx *ctx, double *generate_ms, double *transport_ms, do
  * counters (host, GG_N_COUNTERS slots) may be NULL; on error a message is
  * written to err (err_len bytes, NUL-terminated).
  *
- * Sizes beyond the GG_NOALLOC_MAX_* limits are rejected with GG_ERR_ARG.
+ * Sizes beyond the GG_NOALLOC_MAX_* limits, and voxel (activity image)
+ * sources, are rejected with GG_ERR_ARG.
  * All calls share the scratch array: each call clears the parts that must
  * start at zero, and calls whose GPU work overlaps (other threads or
  * unordered streams) race on it - serialise them.  The first call on a device
  * looks up the array's device address (cudaGetSymbolAddress) with that device
  * current; make that first call before any stream capture on the device.
  */
-#define GG_NOALLOC_SCRATCH_BYTES (24u << 20)
+#define GG_NOALLOC_SCRATCH_BYTES (32u << 20)
 #define GG_NOALLOC_MAX_VOXELS (1u << 20)
 #define GG_NOALLOC_BATCH 65536
 #define GG_NOALLOC_MAX_ENERGIES 512

@@ -25,14 +25,14 @@ STATUS_NAMES = {0: "GG_OK", 1: "GG_ERR_ARG", 2: "GG_ERR_CUDA", 3: "GG_ERR_QUEUE_
 
 GG_PREC_F32 = 32
 GG_PREC_F64 = 64
-GG_POS_POINT, GG_POS_BOX, GG_POS_SPHERE, GG_POS_DISC = 0, 1, 2, 3
+GG_POS_POINT, GG_POS_BOX, GG_POS_SPHERE, GG_POS_DISC, GG_POS_VOXELS = 0, 1, 2, 3, 4
 GG_DIR_ISO, GG_DIR_MOMENTUM, GG_DIR_FOCUSED = 0, 1, 2
 GG_ENE_MONO, GG_ENE_LINES, GG_ENE_HISTOGRAM, GG_ENE_RANGE = 0, 1, 2, 3
 GG_IMG_EDEP, GG_IMG_EDEP_SQUARED = 0, 1
 GG_N_COUNTERS = 16
 COUNTER_NAMES = ["histories", "woodcock_steps", "real_interactions", "deposits", "tally_entries",
                  "list_overflows", "world_steps", "escaped", "skipped", "loop_capped",
-                 "stack_overflow", "secondaries", "c12", "c13", "c14", "c15"]
+                 "stack_overflow", "secondaries", "head_steps", "singles", "c14", "c15"]
 
 _f32p = ctypes.POINTER(ctypes.c_float)
 _f64p = ctypes.POINTER(ctypes.c_double)
@@ -72,6 +72,20 @@ class SourceDesc(ctypes.Structure):
         ("max_rejection", ctypes.c_int32), ("ene_type", ctypes.c_int32), ("mono", ctypes.c_double),
         ("n_spec", ctypes.c_int32), ("spec_e", _f64p), ("spec_cdf", _f64p),
         ("e_lo", ctypes.c_double), ("e_hi", ctypes.c_double),
+        ("vox_dims", ctypes.c_int32 * 3), ("vox_spacing", ctypes.c_double * 3),
+        ("vox_corner", ctypes.c_double * 3), ("cdf_z", _f32p), ("cdf_y", _f32p), ("cdf_x", _f32p),
+    ]
+
+
+class SpectDesc(ctypes.Structure):
+    _fields_ = [
+        ("half_width", ctypes.c_double), ("collimator_thickness", ctypes.c_double), ("gap", ctypes.c_double),
+        ("crystal_thickness", ctypes.c_double), ("hole_apothem", ctypes.c_double),
+        ("pitch_x", ctypes.c_double), ("pitch_y", ctypes.c_double),
+        ("collimator_material", ctypes.c_int32), ("crystal_material", ctypes.c_int32),
+        ("n_windows", ctypes.c_int32), ("window_lo", ctypes.c_double * 8), ("window_hi", ctypes.c_double * 8),
+        ("size", ctypes.c_int32 * 2), ("spacing", ctypes.c_double * 2), ("n_heads", ctypes.c_int32),
+        ("n_runs", ctypes.c_int32),
     ]
 
 
@@ -108,6 +122,9 @@ PROTOTYPES = [
     ("gg_get_counters", ctypes.c_int, [ctypes.c_void_p, _u64p, ctypes.c_size_t]),
     ("gg_last_kernel_ms", ctypes.c_int,
      [ctypes.c_void_p, _f64p, _f64p, _f64p, ctypes.POINTER(ctypes.c_int32)]),
+    ("gg_spect_setup", ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(SpectDesc)]),
+    ("gg_spect_set_heads", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, _f64p]),
+    ("gg_get_projection", ctypes.c_int, [ctypes.c_void_p, _f64p, ctypes.c_size_t]),
     ("gg_dose_run_noalloc", ctypes.c_int,
      [ctypes.c_int32, ctypes.c_void_p, ctypes.POINTER(TablesDesc), ctypes.POINTER(VolumeDesc),
       ctypes.POINTER(WorldDesc), ctypes.POINTER(SourceDesc), ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64,

@@ -69,6 +69,16 @@ struct gg_ctx {
   gg_source_desc src{};
   void *d_spec_e = nullptr, *d_spec_cdf = nullptr, *d_acc_box = nullptr;
   bool have_source = false;
+  double src_emax = 0;
+  void *d_cdf_z = nullptr, *d_cdf_y = nullptr, *d_cdf_x = nullptr;
+
+  // SPECT
+  gg_spect_desc spect{};
+  bool have_spect = false;
+  int spect_run = 0;
+  double frames[2][12] = {};
+  unsigned long long *d_proj = nullptr;
+  size_t n_proj = 0;
 
   // tally
   unsigned long long *d_acc_e = nullptr, *d_acc_e2 = nullptr;
@@ -136,6 +146,7 @@ struct gg_ctx {
     dfree(d_labels); dfree(d_maj); dfree(d_spec_e); dfree(d_spec_cdf); dfree(d_acc_box);
     dfree(d_acc_e); dfree(d_acc_e2); dfree(d_edep); dfree(d_edep2);
     dfree(d_counters); dfree(d_next); dfree(d_status); dfree(d_records);
+    dfree(d_cdf_z); dfree(d_cdf_y); dfree(d_cdf_x); dfree(d_proj);
     rec_cap = 0;
     for (auto e : ev) cudaEventDestroy(e);
     ev.clear();
@@ -199,6 +210,58 @@ struct gg_ctx {
     s.spec_e = (const real *)d_spec_e;
     s.spec_cdf = (const real *)d_spec_cdf;
     s.acc_box = (const real *)d_acc_box;
+    // voxel source (same conversions as the oracle)
+    s.vnx = src.vox_dims[0];
+    s.vny = src.vox_dims[1];
+    s.vnz = src.vox_dims[2];
+    for (int a = 0; a < 3; ++a) {
+      s.v_org[a] = (real)(src.vox_corner[a] + 0.5 * src.vox_spacing[a]);
+      s.v_sp[a] = (real)src.vox_spacing[a];
+    }
+    s.cdf_z = (const real *)d_cdf_z;
+    s.cdf_y = (const real *)d_cdf_y;
+    s.cdf_x = (const real *)d_cdf_x;
+    // SPECT heads and digitizer
+    s.spect = have_spect ? 1 : 0;
+    if (have_spect) {
+      const gg_spect_desc &sp = spect;
+      s.n_heads = sp.n_heads;
+      s.n_runs = sp.n_runs;
+      s.n_win = sp.n_windows;
+      s.pnx = sp.size[0];
+      s.pny = sp.size[1];
+      s.run = spect_run;
+      s.half_w = (real)sp.half_width;
+      s.zb[0] = (real)0;
+      s.zb[1] = (real)sp.collimator_thickness;
+      s.zb[2] = (real)(sp.collimator_thickness + sp.gap);
+      s.zb[3] = (real)(sp.collimator_thickness + sp.gap + sp.crystal_thickness);
+      s.apo = (real)sp.hole_apothem;
+      s.px = (real)sp.pitch_x;
+      s.py = (real)sp.pitch_y;
+      s.hpx = (real)(0.5 * sp.pitch_x);
+      s.hpy = (real)(0.5 * sp.pitch_y);
+      s.inv_px = (real)(1.0 / sp.pitch_x);
+      s.inv_py = (real)(1.0 / sp.pitch_y);
+      s.mat_coll = sp.collimator_material;
+      s.mat_cr = sp.crystal_material;
+      for (int k = 0; k < sp.n_windows; ++k) {
+        s.wlo[k] = (real)sp.window_lo[k];
+        s.whi[k] = (real)sp.window_hi[k];
+      }
+      for (int a = 0; a < 2; ++a) {
+        s.pix_half[a] = (real)(0.5 * sp.size[a] * sp.spacing[a]);
+        s.inv_psp[a] = (real)(1.0 / sp.spacing[a]);
+      }
+      for (int h = 0; h < sp.n_heads; ++h)
+        for (int a = 0; a < 3; ++a) {
+          s.hc[h][a] = (real)frames[h][a];
+          s.hu[h][a] = (real)frames[h][3 + a];
+          s.he1[h][a] = (real)frames[h][6 + a];
+          s.he2[h][a] = (real)frames[h][9 + a];
+        }
+      s.proj = d_proj;
+    }
     return s;
   }
 };
@@ -372,7 +435,7 @@ int gg_set_source(gg_ctx *c, const gg_source_desc *s) {
   if (!c || !s) return GG_ERR_ARG;
   cudaSetDevice(c->device);
   if (!c->have_tables) return c->fail(GG_ERR_STATE, "gg_set_source: upload the tables first");
-  if (s->pos_type < GG_POS_POINT || s->pos_type > GG_POS_DISC) return c->fail(GG_ERR_ARG, "gg_set_source: position type");
+  if (s->pos_type < GG_POS_POINT || s->pos_type > GG_POS_VOXELS) return c->fail(GG_ERR_ARG, "gg_set_source: position type");
   if (s->dir_type < GG_DIR_ISO || s->dir_type > GG_DIR_FOCUSED) return c->fail(GG_ERR_ARG, "gg_set_source: direction type");
   if (s->ene_type < GG_ENE_MONO || s->ene_type > GG_ENE_RANGE) return c->fail(GG_ERR_ARG, "gg_set_source: energy type");
   if (s->n_accept < 0 || (s->n_accept > 0 && !s->accept_boxes)) return c->fail(GG_ERR_ARG, "gg_set_source: acceptance boxes");
@@ -387,6 +450,7 @@ int gg_set_source(gg_ctx *c, const gg_source_desc *s) {
     for (int i = 1; i < s->n_spec; ++i)
       if (s->spec_cdf[i] < s->spec_cdf[i - 1]) return c->fail(GG_ERR_ARG, "gg_set_source: cumulative weights decrease");
   }
+  c->src_emax = ehi;
   if (!(elo >= c->e_min) || !(ehi <= c->e_max))
     return c->fail(GG_ERR_DOMAIN, "gg_set_source: energies [%g, %g] MeV outside the tables [%g, %g]", elo, ehi,
                    (double)c->e_min, (double)c->e_max);
@@ -395,7 +459,19 @@ int gg_set_source(gg_ctx *c, const gg_source_desc *s) {
   if ((st = c->upload_real_d(c->d_spec_e, s->spec_e, s->spec_e ? (size_t)ne : 0))) return st;
   if ((st = c->upload_real_d(c->d_spec_cdf, s->spec_cdf, s->spec_cdf ? (size_t)s->n_spec : 0))) return st;
   if ((st = c->upload_real_d(c->d_acc_box, s->accept_boxes, (size_t)6 * s->n_accept))) return st;
+  if (s->pos_type == GG_POS_VOXELS) {
+    size_t nz = (size_t)s->vox_dims[2], ny = (size_t)s->vox_dims[1], nx = (size_t)s->vox_dims[0];
+    if (!s->vox_dims[0] || !s->vox_dims[1] || !s->vox_dims[2] || s->vox_dims[0] < 0 || s->vox_dims[1] < 0 ||
+        s->vox_dims[2] < 0 || !s->cdf_z || !s->cdf_y || !s->cdf_x)
+      return c->fail(GG_ERR_ARG, "gg_set_source: voxel source needs dims and the three CDFs");
+    for (int a = 0; a < 3; ++a)
+      if (!(s->vox_spacing[a] > 0)) return c->fail(GG_ERR_ARG, "gg_set_source: voxel spacing must be > 0");
+    if ((st = c->upload_real(c->d_cdf_z, s->cdf_z, nz))) return st;
+    if ((st = c->upload_real(c->d_cdf_y, s->cdf_y, nz * ny))) return st;
+    if ((st = c->upload_real(c->d_cdf_x, s->cdf_x, nz * ny * nx))) return st;
+  }
   c->src = *s;
+  c->src.cdf_z = c->src.cdf_y = c->src.cdf_x = nullptr;
   c->src.spec_e = nullptr;
   c->src.spec_cdf = nullptr;
   c->src.accept_boxes = nullptr;
@@ -414,7 +490,7 @@ int gg_add_dose_tally(gg_ctx *c, int32_t score_squared) {
     if ((st = c->cuda(cudaMalloc(&c->d_edep, n * 8), "cudaMalloc edep"))) return st;
   }
   if (score_squared && !c->d_acc_e2) {
-    if ((st = c->cuda(cudaMalloc(&c->d_acc_e2, n * 8), "cudaMalloc tally2"))) return st;
+    if ((st = c->cuda(cudaMalloc(&c->d_acc_e2, n * 16), "cudaMalloc tally2"))) return st;  // 128-bit per voxel
     if ((st = c->cuda(cudaMalloc(&c->d_edep2, n * 8), "cudaMalloc edep2"))) return st;
   }
   c->squared = score_squared != 0;
@@ -431,7 +507,7 @@ int gg_reset_tally(gg_ctx *c) {
   if ((st = c->cuda(cudaMemsetAsync(c->d_acc_e, 0, n * 8, c->stream), "memset"))) return st;
   if ((st = c->cuda(cudaMemsetAsync(c->d_edep, 0, n * 8, c->stream), "memset"))) return st;
   if (c->d_acc_e2) {
-    if ((st = c->cuda(cudaMemsetAsync(c->d_acc_e2, 0, n * 8, c->stream), "memset"))) return st;
+    if ((st = c->cuda(cudaMemsetAsync(c->d_acc_e2, 0, n * 16, c->stream), "memset"))) return st;
     if ((st = c->cuda(cudaMemsetAsync(c->d_edep2, 0, n * 8, c->stream), "memset"))) return st;
   }
   if ((st = c->cuda(cudaMemsetAsync(c->d_counters, 0, GG_N_COUNTERS * 8, c->stream), "memset"))) return st;
@@ -445,8 +521,10 @@ static int run_impl(gg_ctx *c, uint64_t n, uint64_t seed, uint64_t first) {
   int minb = c->blocks_per_sm > 0 ? std::min(c->blocks_per_sm, 4) : (c->precision == GG_PREC_F64 ? 2 : 3);
   int bps = 0;
   {
-    cudaError_t e = c->precision == GG_PREC_F64 ? gg::occupancy_blocks<double>(c->block, smem, minb, &bps)
-                                                : gg::occupancy_blocks<float>(c->block, smem, minb, &bps);
+    cudaError_t e = c->precision == GG_PREC_F64 ? gg::occupancy_blocks<double>(c->block, smem, minb, &bps,
+                                                                                c->have_spect)
+                                                : gg::occupancy_blocks<float>(c->block, smem, minb, &bps,
+                                                                               c->have_spect);
     if (e != cudaSuccess) return c->cuda(e, "occupancy");
     if (bps < 1) bps = 1;
   }
@@ -496,7 +574,8 @@ static int run_impl(gg_ctx *c, uint64_t n, uint64_t seed, uint64_t first) {
             : gg::launch_transport<float>(c->scene<float>(), a, grid, c->block, smem, minb, c->stream);
     if ((st = c->cuda(e, "transport launch"))) return st;
     if ((st = c->cuda(cudaEventRecord(c->ev[3 * b + 2], c->stream), "event"))) return st;
-    if ((st = c->cuda(gg::launch_flush(c->d_acc_e, a.acc_e2, c->d_edep, c->squared ? c->d_edep2 : nullptr,
+    if (c->have_tally &&
+        (st = c->cuda(gg::launch_flush(c->d_acc_e, a.acc_e2, c->d_edep, c->squared ? c->d_edep2 : nullptr,
                                        c->n_vox, flush_grid, c->stream),
                       "flush launch")))
       return st;
@@ -529,7 +608,11 @@ static int run_impl(gg_ctx *c, uint64_t n, uint64_t seed, uint64_t first) {
 int gg_run(gg_ctx *c, uint64_t n, uint64_t seed, uint64_t first) {
   if (!c) return GG_ERR_ARG;
   cudaSetDevice(c->device);
-  if (!c->have_tables || !c->have_volume || !c->have_world || !c->have_source || !c->have_tally)
+  // SPECT heads are tracked for photons below the pair threshold only (no
+  // secondary can be created inside a head)
+  if (c->have_spect && !(c->src_emax < 2.0 * gg::kMC2))
+    return c->fail(GG_ERR_DOMAIN, "gg_run: SPECT transport needs source energies below 1.022 MeV");
+  if (!c->have_tables || !c->have_volume || !c->have_world || !c->have_source || !(c->have_tally || c->have_spect))
     return c->fail(GG_ERR_STATE, "gg_run: tables, volume, world, source and tally must be set first");
   if (n == 0) return GG_OK;
   if (first + n < first) return c->fail(GG_ERR_ARG, "gg_run: history range overflows");
@@ -572,6 +655,67 @@ int gg_last_kernel_ms(gg_ctx *c, double *generate_ms, double *transport_ms, doub
   if (transport_ms) *transport_ms = c->last_transport_ms;
   if (flush_ms) *flush_ms = c->last_flush_ms;
   if (launches) *launches = c->last_launches;
+  return GG_OK;
+}
+
+int gg_spect_setup(gg_ctx *c, const gg_spect_desc *sp) {
+  if (!c || !sp) return GG_ERR_ARG;
+  cudaSetDevice(c->device);
+  if (!c->have_tables) return c->fail(GG_ERR_STATE, "gg_spect_setup: upload the tables first");
+  if (sp->n_heads < 1 || sp->n_heads > 2) return c->fail(GG_ERR_ARG, "gg_spect_setup: 1 or 2 heads");
+  if (sp->n_windows < 1 || sp->n_windows > 8) return c->fail(GG_ERR_ARG, "gg_spect_setup: 1..8 energy windows");
+  if (sp->n_runs < 1 || sp->size[0] < 1 || sp->size[1] < 1 || !(sp->spacing[0] > 0) || !(sp->spacing[1] > 0))
+    return c->fail(GG_ERR_ARG, "gg_spect_setup: runs, projection size and spacing must be > 0");
+  if (!(sp->half_width > 0) || !(sp->collimator_thickness > 0) || !(sp->gap >= 0) || !(sp->crystal_thickness > 0) ||
+      !(sp->hole_apothem > 0) || !(sp->pitch_x > 0) || !(sp->pitch_y > 0))
+    return c->fail(GG_ERR_ARG, "gg_spect_setup: head dimensions must be > 0");
+  if (!(2.0 * sp->hole_apothem < sp->pitch_y))
+    return c->fail(GG_ERR_ARG, "gg_spect_setup: holes wider than their pitch would overlap");
+  if (sp->collimator_material < 0 || sp->collimator_material >= c->n_mat || sp->crystal_material < 0 ||
+      sp->crystal_material >= c->n_mat)
+    return c->fail(GG_ERR_ARG, "gg_spect_setup: head materials outside the material table");
+  for (int k = 0; k < sp->n_windows; ++k)
+    if (!(sp->window_hi[k] > sp->window_lo[k])) return c->fail(GG_ERR_ARG, "gg_spect_setup: empty window");
+  size_t n = (size_t)sp->n_heads * sp->n_runs * sp->n_windows * sp->size[0] * sp->size[1];
+  int st;
+  if (n != c->n_proj) {
+    dfree(c->d_proj);
+    if ((st = c->cuda(cudaMalloc(&c->d_proj, n * 8), "cudaMalloc projections"))) return st;
+    c->n_proj = n;
+  }
+  if ((st = c->cuda(cudaMemsetAsync(c->d_proj, 0, n * 8, c->stream), "memset projections"))) return st;
+  c->spect = *sp;
+  c->have_spect = true;
+  c->spect_run = 0;
+  memset(c->frames, 0, sizeof(c->frames));
+  return c->cuda(cudaStreamSynchronize(c->stream), "spect setup");
+}
+
+int gg_spect_set_heads(gg_ctx *c, int32_t run, const double *frames) {
+  if (!c || !frames) return GG_ERR_ARG;
+  if (!c->have_spect) return c->fail(GG_ERR_STATE, "gg_spect_set_heads: call gg_spect_setup first");
+  if (run < 0 || run >= c->spect.n_runs) return c->fail(GG_ERR_ARG, "gg_spect_set_heads: run out of range");
+  for (int h = 0; h < c->spect.n_heads; ++h) {
+    const double *f = frames + 12 * h;
+    for (int v = 1; v < 4; ++v) {
+      double n2 = f[3 * v] * f[3 * v] + f[3 * v + 1] * f[3 * v + 1] + f[3 * v + 2] * f[3 * v + 2];
+      if (std::fabs(n2 - 1.0) > 1e-6) return c->fail(GG_ERR_ARG, "gg_spect_set_heads: axes must be unit vectors");
+    }
+    for (int a = 0; a < 12; ++a) c->frames[h][a] = f[a];
+  }
+  c->spect_run = run;
+  return GG_OK;
+}
+
+int gg_get_projection(gg_ctx *c, double *out, size_t n) {
+  if (!c || !out) return GG_ERR_ARG;
+  cudaSetDevice(c->device);
+  if (!c->have_spect) return c->fail(GG_ERR_STATE, "gg_get_projection: no SPECT heads");
+  if (n != c->n_proj) return c->fail(GG_ERR_ARG, "gg_get_projection: buffer has %zu values, need %zu", n, c->n_proj);
+  std::vector<unsigned long long> tmp(n);
+  int st = c->cuda(cudaMemcpy(tmp.data(), c->d_proj, n * 8, cudaMemcpyDeviceToHost), "download projections");
+  if (st) return st;
+  for (size_t i = 0; i < n; ++i) out[i] = (double)tmp[i];
   return GG_OK;
 }
 

@@ -378,6 +378,17 @@ struct Scene {
   real s_mom[3], s_focus[3];
   real s_mono, s_elo, s_ehi;
   const real *spec_e, *spec_cdf, *acc_box;
+  // voxel source
+  int vnx, vny, vnz;
+  real v_org[3], v_sp[3];
+  const real *cdf_z, *cdf_y, *cdf_x;
+  // SPECT heads and digitizer (spect = 0: dose path)
+  int spect, n_heads, n_win, pnx, pny, n_runs, run;
+  real hc[2][3], hu[2][3], he1[2][3], he2[2][3];
+  real half_w, zb[4], apo, px, py, hpx, hpy, inv_px, inv_py;
+  int mat_coll, mat_cr;
+  real wlo[8], whi[8], pix_half[2], inv_psp[2];
+  unsigned long long *proj;
 };
 
 template <typename real>
@@ -465,6 +476,9 @@ struct Photon {
   real t_exit, mumax, inv_mumax;
   EIdx<real> ei;
   int alive, in_image, can_enter, steps;
+  // SPECT: box not to re-enter before the next direction change (-1 none,
+  // 0 image, 1 + h head h); head-local state while in_head
+  int in_head, head, hreg, left_hole, exclude;
 };
 
 template <typename real>
@@ -509,6 +523,8 @@ __device__ __forceinline__ void set_energy(const Scene<real> &s, Photon<real> &p
 template <typename real>
 __device__ __forceinline__ void start_photon(const Scene<real> &s, Photon<real> &ph) {
   ph.steps = 0;
+  ph.in_head = 0;
+  ph.exclude = -1;
   if (inside_box(ph.pos, s.bmin, s.bmax)) {
     ph.in_image = 1;
     ph.t_exit = exit_distance(ph.pos, ph.dir, s.bmin, s.bmax);

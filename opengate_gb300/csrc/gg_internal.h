@@ -37,7 +37,7 @@ template <typename real>
 cudaError_t launch_transport(const Scene<real> &s, const KernelArgs &a, int grid, int block, size_t smem,
                              int minb, cudaStream_t st);
 template <typename real>
-cudaError_t occupancy_blocks(int block, size_t smem, int minb, int *blocks_per_sm);
+cudaError_t occupancy_blocks(int block, size_t smem, int minb, int *blocks_per_sm, bool spect = false);
 cudaError_t launch_flush(unsigned long long *acc_e, unsigned long long *acc_e2, double *edep, double *edep2,
                          size_t n, int grid, cudaStream_t st);
 

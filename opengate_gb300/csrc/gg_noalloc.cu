@@ -74,7 +74,7 @@ Layout make_layout(int n_comp, int n_e, int n_ray, int n_mat, size_t n_vox) {
   L.acc_box = take(sizeof(float) * 6 * GG_NOALLOC_MAX_ACCEPT);
   L.labels = take(sizeof(uint16_t) * n_vox);
   L.acc_e = take(8 * n_vox);
-  L.acc_e2 = take(8 * n_vox);
+  L.acc_e2 = take(16 * n_vox);  // 128-bit edep^2 accumulator per voxel
   L.records = take(gg::record_bytes<float>((size_t)GG_NOALLOC_BATCH));
   L.counters = take(8 * GG_N_COUNTERS);
   L.next = take(8);
@@ -135,6 +135,13 @@ extern "C" int gg_dose_run_noalloc(int32_t device, void *stream, const gg_tables
   if (n_vox > GG_NOALLOC_MAX_VOXELS)
     return fail(err, err_len, GG_ERR_ARG, "image has %zu voxels; the no-allocation run handles at most %u",
                 n_vox, (unsigned)GG_NOALLOC_MAX_VOXELS);
+  // voxel (activity image) sources need their CDF arrays on the device: gg_run only
+  if (src->pos_type < GG_POS_POINT || src->pos_type > GG_POS_DISC)
+    return fail(err, err_len, GG_ERR_ARG, "position type %d not handled by the no-allocation run", src->pos_type);
+  if (src->dir_type < GG_DIR_ISO || src->dir_type > GG_DIR_FOCUSED)
+    return fail(err, err_len, GG_ERR_ARG, "direction type %d", src->dir_type);
+  if (src->ene_type < GG_ENE_MONO || src->ene_type > GG_ENE_RANGE)
+    return fail(err, err_len, GG_ERR_ARG, "energy type %d", src->ene_type);
   int n_spec_e = src->ene_type == GG_ENE_HISTOGRAM ? src->n_spec + 1 : src->n_spec;
   bool spectrum = src->ene_type == GG_ENE_LINES || src->ene_type == GG_ENE_HISTOGRAM;
   if (spectrum && (src->n_spec < 1 || src->n_spec > GG_NOALLOC_MAX_SPECTRUM || !src->spec_e || !src->spec_cdf))
@@ -210,7 +217,7 @@ extern "C" int gg_dose_run_noalloc(int32_t device, void *stream, const gg_tables
       break;
     }
     // ---- state that must start at zero ---------------------------------------
-    size_t zero[][2] = {{L.acc_e, 8 * n_vox}, {L.acc_e2, 8 * n_vox}, {L.counters, 8 * GG_N_COUNTERS},
+    size_t zero[][2] = {{L.acc_e, 8 * n_vox}, {L.acc_e2, 16 * n_vox}, {L.counters, 8 * GG_N_COUNTERS},
                         {L.status, 4}};
     for (auto &z : zero)
       if (e == cudaSuccess) e = cudaMemsetAsync(b + z[0], 0, z[1], st);

@@ -1,0 +1,303 @@
+// gg_spect.cuh - SPECT head transport and the projection digitizer (device side).
+//
+// Head model (local frame: a1 along e1, a2 along e2, w along the outward
+// normal, collimator front face at w = 0): collimator slab with hexagonal
+// vacuum holes on two offset rectangular lattices (faces normal to 30, 90,
+// 150 degrees), vacuum gap, crystal.  In the collimator the photon is
+// tracked with Woodcock steps against the collimator attenuation (points that
+// land in a hole are null collisions) and crosses a hole it starts in
+// analytically up to the hole wall.  Crystal interactions add to the event's
+// per-head sum and energy-winner position (GateDigiAdderInVolume::Update,
+// EnergyWinnerPosition, core/opengate_core/opengate_lib/digitizer/
+// GateDigiAdderInVolume.cpp:29-77); at the end of the event each head's single
+// is classified into the windows [lo, hi)
+// (GateDigitizerEnergyWindowsActor.cpp:116-132) and counted in the detector
+// pixel of its position (GateDigitizerProjectionActor.cpp:127-177).
+#pragma once
+#include "gg_device.cuh"
+
+namespace gg {
+
+constexpr double kCos30 = 0.86602540378443864676;
+
+template <typename real>
+__device__ __forceinline__ real dot3(const real a[3], const real b[3]) {
+  real r = a[0] * b[0];
+  r = r + a[1] * b[1];
+  r = r + a[2] * b[2];
+  return r;
+}
+
+template <typename real>
+__device__ __forceinline__ void to_local(const Scene<real> &s, int h, const real p[3], const real d[3], real lp[3],
+                                         real ld[3]) {
+  real q[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) q[a] = p[a] - s.hc[h][a];
+  lp[0] = dot3(q, s.he1[h]);
+  lp[1] = dot3(q, s.he2[h]);
+  lp[2] = dot3(q, s.hu[h]);
+  ld[0] = dot3(d, s.he1[h]);
+  ld[1] = dot3(d, s.he2[h]);
+  ld[2] = dot3(d, s.hu[h]);
+}
+
+template <typename real>
+__device__ __forceinline__ void to_world(const Scene<real> &s, int h, const real lp[3], const real ld[3], real p[3],
+                                         real d[3]) {
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    real x = lp[0] * s.he1[h][a];
+    x = s.hc[h][a] + x;
+    x = x + lp[1] * s.he2[h][a];
+    p[a] = x + lp[2] * s.hu[h][a];
+    real y = ld[0] * s.he1[h][a];
+    y = y + ld[1] * s.he2[h][a];
+    d[a] = y + ld[2] * s.hu[h][a];
+  }
+}
+
+template <typename real>
+__device__ __forceinline__ real gg_fabs(real x) {
+  return x < R<real>(0) ? -x : x;
+}
+
+template <typename real>
+__device__ __forceinline__ bool find_hole(const Scene<real> &s, real a1, real a2, real &cx, real &cy) {
+#pragma unroll
+  for (int lat = 0; lat < 2; ++lat) {
+    real ox = lat ? s.hpx : R<real>(0), oy = lat ? s.hpy : R<real>(0);
+    real fx = a1 - ox;
+    fx = fx * s.inv_px;
+    fx = fx + R<real>(0.5);
+    fx = gg_floor(fx);
+    real fy = a2 - oy;
+    fy = fy * s.inv_py;
+    fy = fy + R<real>(0.5);
+    fy = gg_floor(fy);
+    real x = fx * s.px;
+    x = x + ox;
+    real y = fy * s.py;
+    y = y + oy;
+    real qx = a1 - x, qy = a2 - y;
+    real t0 = qx * R<real>(kCos30), t1 = qy * R<real>(0.5);
+    real n0 = t1 + t0, n2 = t1 - t0;
+    if (gg_fabs(qy) <= s.apo && gg_fabs(n0) <= s.apo && gg_fabs(n2) <= s.apo) {
+      cx = x;
+      cy = y;
+      return true;
+    }
+  }
+  return false;
+}
+
+template <typename real>
+__device__ __forceinline__ real hex_exit(const Scene<real> &s, real qx, real qy, real d1, real d2) {
+  real t0 = qx * R<real>(kCos30), t1 = qy * R<real>(0.5);
+  real u0 = d1 * R<real>(kCos30), u1 = d2 * R<real>(0.5);
+  real qn[3] = {t1 + t0, qy, t1 - t0};
+  real dn[3] = {u1 + u0, d2, u1 - u0};
+  real t = gg_inf(real(0));
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    real tk;
+    if (dn[k] > R<real>(0)) {
+      tk = s.apo - qn[k];
+      tk = tk / dn[k];
+      if (tk < t) t = tk;
+    } else if (dn[k] < R<real>(0)) {
+      tk = -s.apo - qn[k];
+      tk = tk / dn[k];
+      if (tk < t) t = tk;
+    }
+  }
+  return t < R<real>(0) ? R<real>(0) : t;
+}
+
+template <typename real>
+__device__ __forceinline__ void move3(real p[3], const real d[3], real t) {
+#pragma unroll
+  for (int a = 0; a < 3; ++a) p[a] = p[a] + t * d[a];
+}
+
+// per-event crystal accumulation of each head
+template <typename real>
+struct Event {
+  real esum[2], emax[2], wpos[2][3];
+  __device__ __forceinline__ void clear() {
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      esum[h] = R<real>(0);
+      emax[h] = R<real>(0);
+      wpos[h][0] = wpos[h][1] = wpos[h][2] = R<real>(0);
+    }
+  }
+};
+
+template <typename real>
+__device__ __forceinline__ void head_cross(const Scene<real> &s, Photon<real> &ph, bool leave) {
+  if (leave) {
+    real p[3], d[3];
+    to_world(s, ph.head, ph.pos, ph.dir, p, d);
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      ph.pos[a] = p[a];
+      ph.dir[a] = d[a];
+    }
+    ph.in_head = 0;
+    ph.exclude = 1 + ph.head;
+  } else {
+    ph.hreg += ph.dir[2] > R<real>(0) ? 1 : -1;
+    ph.left_hole = 0;
+  }
+}
+
+// Geometric part of one head step.  Returns true when the step continues
+// with a sampled collision in material `mat` (collimator or crystal), after
+// moving the photon to the tentative point; the caller then draws the
+// interaction unless the point lies in a hole (null collision).
+template <typename real>
+__device__ __forceinline__ int head_flight(const Scene<real> &s, Photon<real> &ph, Rng &g, int &mat) {
+  real *l = ph.pos, *d = ph.dir;
+  real lo[3] = {-s.half_w, -s.half_w, R<real>(0)};
+  real hi[3] = {s.half_w, s.half_w, s.zb[3]};
+  real tbox = exit_distance(l, d, lo, hi);
+  real treg = gg_inf(real(0));
+  if (d[2] > R<real>(0)) {
+    treg = s.zb[ph.hreg + 1] - l[2];
+    treg = treg / d[2];
+  } else if (d[2] < R<real>(0)) {
+    treg = s.zb[ph.hreg] - l[2];
+    treg = treg / d[2];
+  }
+  if (treg < R<real>(0)) treg = R<real>(0);
+  bool leave = tbox <= treg;
+  real tlim = leave ? tbox : treg;
+  if (ph.hreg == 0 && !ph.left_hole) {
+    real cx, cy;
+    if (find_hole(s, l[0], l[1], cx, cy)) {
+      real th = hex_exit(s, l[0] - cx, l[1] - cy, d[0], d[1]);
+      ph.left_hole = 1;
+      if (th < tlim) {
+        move3(l, d, th);
+        return 0;
+      }
+      move3(l, d, tlim);
+      head_cross(s, ph, leave);
+      return 0;
+    }
+  }
+  ph.left_hole = 0;
+  if (ph.hreg == 1) {
+    move3(l, d, tlim);
+    head_cross(s, ph, leave);
+    return 0;
+  }
+  mat = ph.hreg == 0 ? s.mat_coll : s.mat_cr;
+  real mu = interp_row(s.sig + (size_t)s.mat_comp[mat] * s.n_e, ph.ei);
+  mu = s.mat_rho[mat] * mu;
+  real u = u01_open0<real>(g);
+  real sd = -gg_log(u);
+  sd = sd / mu;
+  if (sd >= tlim) {
+    move3(l, d, tlim);
+    head_cross(s, ph, leave);
+    return 0;
+  }
+  move3(l, d, sd);
+  if (ph.hreg == 0) {
+    real cx, cy;
+    if (find_hole(s, l[0], l[1], cx, cy)) return 0;  // null collision inside a hole
+  }
+  return 1;
+}
+
+// World step with the image box and the head boxes as targets.  Returns
+// 1 for an air interaction at the new position, 0 otherwise (ph.alive = 0
+// when the photon left the world).
+template <typename real>
+__device__ __forceinline__ int spect_world_flight(const Scene<real> &s, Photon<real> &ph, Rng &g) {
+  real inf = gg_inf(real(0));
+  real tb = ph.exclude != 0 ? entry_distance(ph.pos, ph.dir, s.bmin, s.bmax) : inf;
+  int box = 0;
+  real hlo[3] = {-s.half_w, -s.half_w, R<real>(0)};
+  real hhi[3] = {s.half_w, s.half_w, s.zb[3]};
+  for (int h = 0; h < s.n_heads; ++h) {
+    if (ph.exclude == 1 + h) continue;
+    real lp[3], ld[3];
+    to_local(s, h, ph.pos, ph.dir, lp, ld);
+    real th = entry_distance(lp, ld, hlo, hhi);
+    if (th < tb) {
+      tb = th;
+      box = 1 + h;
+    }
+  }
+  real wlo[3] = {-s.whalf[0], -s.whalf[1], -s.whalf[2]};
+  real tout = exit_distance(ph.pos, ph.dir, wlo, s.whalf);
+  int wm = s.world_mat;
+  real mu = interp_row(s.sig + (size_t)s.mat_comp[wm] * s.n_e, ph.ei);
+  mu = s.mat_rho[wm] * mu;
+  real u = u01_open0<real>(g);
+  real sd = -gg_log(u);
+  sd = sd / mu;
+  if (sd < tb && sd < tout) {
+    move3(ph.pos, ph.dir, sd);
+    return 1;
+  }
+  if (tb <= tout) {
+    move3(ph.pos, ph.dir, tb);
+    if (box == 0) {
+      ph.in_image = 1;
+      ph.t_exit = exit_distance(ph.pos, ph.dir, s.bmin, s.bmax);
+    } else {
+      int h = box - 1;
+      real lp[3], ld[3];
+      to_local(s, h, ph.pos, ph.dir, lp, ld);
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        ph.pos[a] = lp[a];
+        ph.dir[a] = ld[a];
+      }
+      ph.in_head = 1;
+      ph.head = h;
+      ph.hreg = lp[2] < s.zb[1] ? 0 : (lp[2] < s.zb[2] ? 1 : 2);
+      ph.left_hole = 0;
+    }
+    return 0;
+  }
+  ph.alive = 0;
+  return 0;
+}
+
+// Singles of one event: windows and projection pixel per head.
+template <typename real>
+__device__ __forceinline__ unsigned score_singles(const Scene<real> &s, const Event<real> &ev) {
+  unsigned n_singles = 0;
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    if (h >= s.n_heads) break;
+    real e = ev.esum[h];
+    if (!(e > R<real>(0))) continue;
+    ++n_singles;
+    real q[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) q[a] = ev.wpos[h][a] - s.hc[h][a];
+    real fx = dot3(q, s.he1[h]);
+    fx = fx + s.pix_half[0];
+    fx = fx * s.inv_psp[0];
+    real fy = dot3(q, s.he2[h]);
+    fy = fy + s.pix_half[1];
+    fy = fy * s.inv_psp[1];
+    if (!(fx >= R<real>(0) && fx < (real)s.pnx && fy >= R<real>(0) && fy < (real)s.pny)) continue;
+    int i = (int)fx, j = (int)fy;
+    for (int k = 0; k < s.n_win; ++k) {
+      if (e >= s.wlo[k] && e < s.whi[k]) {
+        size_t idx = ((((size_t)h * s.n_runs + s.run) * s.n_win + k) * s.pny + j) * s.pnx + i;
+        atomicAdd(s.proj + idx, 1ull);
+      }
+    }
+  }
+  return n_singles;
+}
+
+}  // namespace gg

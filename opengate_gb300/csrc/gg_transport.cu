@@ -29,6 +29,7 @@
 
 #include "gg_device.cuh"
 #include "gg_internal.h"
+#include "gg_spect.cuh"
 
 namespace gg {
 
@@ -50,15 +51,27 @@ struct Tally {
   unsigned long long *acc_e2;
 };
 
+// One history's entry: q = edep in units of 2^-32 MeV goes to acc_e[v]; its
+// exact square q^2 (units of 2^-64 MeV^2, up to 2^74) goes to the 128-bit
+// accumulator acc_e2[2v] (low word) / acc_e2[2v+1] (high word), the carry out
+// of the low word moving to the high word.  Integer sums do not depend on the
+// order of the atomics, and a voxel hit by one history has edep^2 == edep * edep
+// exactly in these units.
 template <typename real>
 __device__ __forceinline__ void hlist_flush(HistList<real> &l, const Tally<real> &t, BlockCounters *bc) {
 #pragma unroll
   for (int k = 0; k < kHistList; ++k) {
     if (k < l.n) {
-      real a = l.acc[k];
-      real a2 = a * a;
-      atomicAdd(&t.acc_e[l.vox[k]], (unsigned long long)to_fixed(a));
-      if (t.acc_e2) atomicAdd(&t.acc_e2[l.vox[k]], (unsigned long long)to_fixed(a2));
+      const unsigned long long q = (unsigned long long)to_fixed(l.acc[k]);
+      const uint32_t v = l.vox[k];
+      atomicAdd(&t.acc_e[v], q);
+      if (t.acc_e2) {
+        const unsigned long long lo = q * q;
+        unsigned long long hi = __umul64hi(q, q);
+        const unsigned long long old = atomicAdd(&t.acc_e2[2 * (size_t)v], lo);
+        hi += (old + lo < old) ? 1ull : 0ull;
+        if (hi) atomicAdd(&t.acc_e2[2 * (size_t)v + 1], hi);
+      }
     }
   }
   if (l.n) atomicAdd(&bc->tally_entries, (unsigned int)l.n);
@@ -358,10 +371,49 @@ __device__ __forceinline__ int sample_primary(const Scene<real> &s, Rng &g, Phot
       }
     }
   }
-  real off[3];
-  rot_apply(s.s_rot, loc, off);
+  if (pt == GG_POS_VOXELS) {
+    // GateSPSVoxelsPosDistribution::VGenerateOne: z, then y | z, then x | z, y;
+    // lower_bound (first entry >= p) with p in (0, 1]
+    int idx[3];
+    const int len[3] = {s.vnz, s.vny, s.vnx};
 #pragma unroll
-  for (int a = 0; a < 3; ++a) ph.pos[a] = s.s_t[a] + off[a];
+    for (int lev = 0; lev < 3; ++lev) {
+      const real *c = lev == 0   ? s.cdf_z
+                      : lev == 1 ? s.cdf_y + (size_t)idx[0] * s.vny
+                                 : s.cdf_x + ((size_t)idx[0] * s.vny + (size_t)idx[1]) * s.vnx;
+      int k, it = 0;
+      do {
+        real p = u01_open0<real>(g);
+        int lo = 0, hi = len[lev];
+        while (lo < hi) {
+          int mid = (lo + hi) >> 1;
+          if (c[mid] < p) lo = mid + 1;
+          else hi = mid;
+        }
+        k = lo;
+        if (++it >= kLoopCap) {
+          atomicAdd(&bc->loop_capped, 1u);
+          if (k >= len[lev]) k = len[lev] - 1;
+          break;
+        }
+      } while (k >= len[lev]);
+      idx[lev] = k;
+    }
+    const int ind[3] = {idx[2], idx[1], idx[0]};
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      real x = (real)ind[a] * s.v_sp[a];
+      x = s.v_org[a] + x;
+      real j = u01<real>(g) - R<real>(0.5);
+      j = j * s.v_sp[a];
+      ph.pos[a] = x + j;
+    }
+  } else {
+    real off[3];
+    rot_apply(s.s_rot, loc, off);
+#pragma unroll
+    for (int a = 0; a < 3; ++a) ph.pos[a] = s.s_t[a] + off[a];
+  }
   int tries = 0;
   for (;;) {
     sample_direction(s, ph.pos, g, ph.dir);
@@ -409,7 +461,7 @@ __device__ __forceinline__ int sample_primary(const Scene<real> &s, Rng &g, Phot
 // one entry per history of the batch).  The state field says how the first
 // transport iteration left the photon; the RNG position lets the transport
 // kernel continue the history's Philox stream exactly where it stopped.
-enum : uint32_t { kRecDead = 0, kRecInImage = 1, kRecPendingWorld = 2 };
+enum : uint32_t { kRecDead = 0, kRecInImage = 1, kRecPendingWorld = 2, kRecWorld = 3 };
 
 template <typename real>
 struct Records {
@@ -464,6 +516,8 @@ __global__ void __launch_bounds__(256) k_generate(Scene<real> s, KernelArgs a) {
       start_photon(s, ph);
       if (ph.in_image) {
         state = kRecInImage;
+      } else if (s.spect) {
+        state = kRecWorld;  // the world step also targets the heads: left to the transport stage
       } else {
         steps = 1;
         atomicAdd(&n_world, 1u);
@@ -520,10 +574,12 @@ enum : int { kDone = 0, kRefill = 1, kFly = 2, kInteract = 3 };
 // (material, voxel, scored) and waits in state kInteract until its warp runs
 // an interaction phase.  Returns the lane's next state; kRefill means the
 // photon died.
-template <typename real>
+// pscored: what the pending interaction scores - 0 nothing (world), 1 the dose
+// voxel pv, 2 the crystal of the current head, 3 nothing (collimator).
+template <typename real, bool SPECT>
 __device__ __forceinline__ int flight(const Scene<real> &s, Photon<real> &ph, Rng &g, BlockCounters *bc, int &pmat,
                                       uint32_t &pv, int &pscored, unsigned int &n_wood, unsigned int &n_real,
-                                      unsigned int &n_world) {
+                                      unsigned int &n_world, unsigned int &n_head) {
   if (++ph.steps > kStepCap) {
     atomicAdd(&bc->loop_capped, 1u);
     ph.alive = 0;
@@ -538,6 +594,7 @@ __device__ __forceinline__ int flight(const Scene<real> &s, Photon<real> &ph, Rn
       for (int a = 0; a < 3; ++a) ph.pos[a] = ph.pos[a] + ph.t_exit * ph.dir[a];
       ph.in_image = 0;
       ph.can_enter = 0;
+      ph.exclude = 0;
       return kFly;
     }
     ph.t_exit = ph.t_exit - sd;
@@ -561,6 +618,29 @@ __device__ __forceinline__ int flight(const Scene<real> &s, Photon<real> &ph, Rn
     pv = v;
     pscored = 1;
     return kInteract;
+  }
+  if constexpr (SPECT) {
+    if (ph.in_head) {
+      ++n_head;
+      int mat;
+      if (head_flight(s, ph, g, mat)) {
+        pmat = mat;
+        pscored = ph.hreg == 2 ? 2 : 3;
+        return kInteract;
+      }
+      return kFly;
+    }
+    ++n_world;
+    if (spect_world_flight(s, ph, g)) {
+      pmat = s.world_mat;
+      pscored = 0;
+      return kInteract;
+    }
+    if (!ph.alive) {
+      atomicAdd(&bc->escaped, 1u);
+      return kRefill;
+    }
+    return kFly;
   }
   ++n_world;
   real inf = gg_inf(real(0));
@@ -593,16 +673,36 @@ __device__ __forceinline__ int flight(const Scene<real> &s, Photon<real> &ph, Rn
 }
 
 // The interaction a lane recorded during its last flight.
-template <typename real>
+template <typename real, int H>
+__device__ __forceinline__ void event_add(const Scene<real> &s, Event<real> &ev, const Photon<real> &ph, real ed) {
+  ev.esum[H] = ev.esum[H] + ed;
+  if (ed > ev.emax[H]) {
+    real p[3], dd[3];
+    to_world(s, H, ph.pos, ph.dir, p, dd);
+    ev.emax[H] = ed;
+    ev.wpos[H][0] = p[0];
+    ev.wpos[H][1] = p[1];
+    ev.wpos[H][2] = p[2];
+  }
+}
+
+template <typename real, bool SPECT>
 __device__ __forceinline__ int do_interaction(const Scene<real> &s, Photon<real> &ph, Rng &g, BlockCounters *bc,
                                               int pmat, uint32_t pv, int pscored, HistList<real> &l,
-                                              const Tally<real> &t, Secondary<real> &sec, unsigned int &n_dep) {
+                                              const Tally<real> &t, Secondary<real> &sec, unsigned int &n_dep,
+                                              Event<real> &ev) {
   real ed = interact(s, ph, pmat, g, bc, sec);
-  if (pscored) {
-    deposit(l, t, bc, pv, ed, n_dep);
+  if (pscored == 1) {
+    if constexpr (!SPECT) deposit(l, t, bc, pv, ed, n_dep);
     if (ph.alive && ph.in_image) ph.t_exit = exit_distance(ph.pos, ph.dir, s.bmin, s.bmax);
-  } else {
+  } else if (pscored == 0) {
     ph.can_enter = 1;
+    ph.exclude = -1;
+  } else if constexpr (SPECT) {
+    if (pscored == 2 && ed > R<real>(0)) {
+      if (ph.head == 0) event_add<real, 0>(s, ev, ph, ed);
+      else event_add<real, 1>(s, ev, ph, ed);
+    }
   }
   return ph.alive ? kFly : kRefill;
 }
@@ -630,7 +730,8 @@ __device__ __forceinline__ void pop_secondary(const Scene<real> &s, Photon<real>
 // with many lanes active instead of one lane at a time, while the order of
 // operations inside each history, and hence its result, is unchanged.
 // MINB = resident blocks per SM the register budget is sized for.
-template <typename real, int MINB>
+// SPECT selects the head transport and projection scoring instead of the dose tally.
+template <typename real, int MINB, bool SPECT>
 __global__ void __launch_bounds__(256, MINB) k_transport(Scene<real> sg, KernelArgs args) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ BlockCounters bc;
@@ -674,12 +775,14 @@ __global__ void __launch_bounds__(256, MINB) k_transport(Scene<real> sg, KernelA
   sec.has = 0;
   HistList<real> l;
   l.n = 0;
+  Event<real> ev;
+  ev.clear();
   Rng g;
   int state = kRefill;
   bool in_hist = false;
   int pmat = 0, pscored = 0;
   uint32_t pv = 0;
-  unsigned int n_wood = 0, n_real = 0, n_dep = 0, n_world = 0;
+  unsigned int n_wood = 0, n_real = 0, n_dep = 0, n_world = 0, n_head = 0, n_singles = 0;
 
   for (;;) {
     const unsigned m_ref = __ballot_sync(0xffffffffu, state == kRefill);
@@ -694,7 +797,8 @@ __global__ void __launch_bounds__(256, MINB) k_transport(Scene<real> sg, KernelA
     if (phase == kRefill) {
       const bool need = state == kRefill;
       if (need && in_hist) {
-        hlist_flush(l, t, &bc);
+        if constexpr (SPECT) n_singles += score_singles(s, ev);
+        else hlist_flush(l, t, &bc);
         in_hist = false;
       }
       const unsigned n_need = __popc(m_ref);
@@ -729,6 +833,9 @@ __global__ void __launch_bounds__(256, MINB) k_transport(Scene<real> sg, KernelA
             ph.steps = (int)((f >> 2) & 1u);
             ph.alive = 1;
             ph.can_enter = 1;
+            ph.in_head = 0;
+            ph.exclude = -1;
+            if constexpr (SPECT) ev.clear();
             const uint64_t hid = args.h_begin + h;
             const uint32_t rp = rec.rng_pos[h];
             const uint4 b = rec.rng_buf[h];
@@ -747,6 +854,9 @@ __global__ void __launch_bounds__(256, MINB) k_transport(Scene<real> sg, KernelA
               ph.in_image = 1;
               ph.t_exit = exit_distance(ph.pos, ph.dir, s.bmin, s.bmax);
               state = kFly;
+            } else if (rs == kRecWorld) {
+              ph.in_image = 0;
+              state = kFly;
             } else {
               ph.in_image = 0;
               pmat = s.world_mat;
@@ -759,7 +869,7 @@ __global__ void __launch_bounds__(256, MINB) k_transport(Scene<real> sg, KernelA
       }
     } else if (phase == kInteract) {
       if (state == kInteract) {
-        state = do_interaction(s, ph, g, &bc, pmat, pv, pscored, l, t, sec, n_dep);
+        state = do_interaction<real, SPECT>(s, ph, g, &bc, pmat, pv, pscored, l, t, sec, n_dep, ev);
         if (state == kRefill && sec.has) {
           pop_secondary(s, ph, sec);
           state = kFly;
@@ -767,7 +877,7 @@ __global__ void __launch_bounds__(256, MINB) k_transport(Scene<real> sg, KernelA
       }
     } else {
       if (state == kFly) {
-        state = flight(s, ph, g, &bc, pmat, pv, pscored, n_wood, n_real, n_world);
+        state = flight<real, SPECT>(s, ph, g, &bc, pmat, pv, pscored, n_wood, n_real, n_world, n_head);
         if (state == kRefill && sec.has) {
           pop_secondary(s, ph, sec);
           state = kFly;
@@ -787,6 +897,8 @@ __global__ void __launch_bounds__(256, MINB) k_transport(Scene<real> sg, KernelA
   warp_add(n_real, GG_CNT_REAL_INTERACTIONS);
   warp_add(n_dep, GG_CNT_DEPOSITS);
   warp_add(n_world, GG_CNT_WORLD_STEPS);
+  warp_add(n_head, GG_CNT_HEAD_STEPS);
+  warp_add(n_singles, GG_CNT_SINGLES);
   __syncthreads();
   if (threadIdx.x == 0) {
     atomicAdd(&cnt[GG_CNT_TALLY_ENTRIES], (unsigned long long)bc.tally_entries);
@@ -809,10 +921,12 @@ __global__ void k_flush(unsigned long long *acc_e, unsigned long long *acc_e2, d
       acc_e[i] = 0ull;
     }
     if (acc_e2) {
-      unsigned long long b = acc_e2[i];
-      if (b) {
-        edep2[i] += (double)b * 2.3283064365386963e-10;
-        acc_e2[i] = 0ull;
+      const ulonglong2 b = reinterpret_cast<const ulonglong2 *>(acc_e2)[i];  // (low, high)
+      if (b.x | b.y) {
+        double lo = (double)b.x;
+        lo = lo * 5.421010862427522e-20;  // 2^-64
+        edep2[i] += (double)b.y + lo;
+        reinterpret_cast<ulonglong2 *>(acc_e2)[i] = make_ulonglong2(0ull, 0ull);
       }
     }
   }
@@ -837,26 +951,31 @@ cudaError_t launch_generate(const Scene<real> &s, const KernelArgs &a, cudaStrea
   return cudaGetLastError();
 }
 
-template <typename real, int MINB>
+template <typename real, int MINB, bool SPECT>
 static cudaError_t launch_transport_v(const Scene<real> &s, const KernelArgs &a, int grid, int block, size_t smem,
                                       cudaStream_t st) {
   static bool configured = false;
   if (!configured) {
-    cudaError_t e = cudaFuncSetAttribute(k_transport<real, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         200 * 1024);
+    cudaError_t e = cudaFuncSetAttribute(k_transport<real, MINB, SPECT>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     if (e != cudaSuccess) return e;
     configured = true;
   }
-  k_transport<real, MINB><<<grid, block, smem, st>>>(s, a);
+  k_transport<real, MINB, SPECT><<<grid, block, smem, st>>>(s, a);
   return cudaGetLastError();
 }
 
 template <typename real>
 cudaError_t launch_transport(const Scene<real> &s, const KernelArgs &a, int grid, int block, size_t smem,
                              int minb, cudaStream_t st) {
-  if (minb <= 2) return launch_transport_v<real, 2>(s, a, grid, block, smem, st);
-  if (minb == 3) return launch_transport_v<real, 3>(s, a, grid, block, smem, st);
-  return launch_transport_v<real, 4>(s, a, grid, block, smem, st);
+  if (s.spect) {
+    if (minb <= 2) return launch_transport_v<real, 2, true>(s, a, grid, block, smem, st);
+    if (minb == 3) return launch_transport_v<real, 3, true>(s, a, grid, block, smem, st);
+    return launch_transport_v<real, 4, true>(s, a, grid, block, smem, st);
+  }
+  if (minb <= 2) return launch_transport_v<real, 2, false>(s, a, grid, block, smem, st);
+  if (minb == 3) return launch_transport_v<real, 3, false>(s, a, grid, block, smem, st);
+  return launch_transport_v<real, 4, false>(s, a, grid, block, smem, st);
 }
 
 cudaError_t launch_flush(unsigned long long *acc_e, unsigned long long *acc_e2, double *edep, double *edep2,
@@ -865,11 +984,17 @@ cudaError_t launch_flush(unsigned long long *acc_e, unsigned long long *acc_e2, 
   return cudaGetLastError();
 }
 
+template <typename real, bool SPECT>
+static cudaError_t occupancy_v(int block, size_t smem, int minb, int *bps) {
+  if (minb <= 2) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(bps, k_transport<real, 2, SPECT>, block, smem);
+  if (minb == 3) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(bps, k_transport<real, 3, SPECT>, block, smem);
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(bps, k_transport<real, 4, SPECT>, block, smem);
+}
+
 template <typename real>
-cudaError_t occupancy_blocks(int block, size_t smem, int minb, int *blocks_per_sm) {
-  if (minb <= 2) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k_transport<real, 2>, block, smem);
-  if (minb == 3) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k_transport<real, 3>, block, smem);
-  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k_transport<real, 4>, block, smem);
+cudaError_t occupancy_blocks(int block, size_t smem, int minb, int *blocks_per_sm, bool spect) {
+  return spect ? occupancy_v<real, true>(block, smem, minb, blocks_per_sm)
+               : occupancy_v<real, false>(block, smem, minb, blocks_per_sm);
 }
 
 template size_t record_bytes<float>(size_t);
@@ -882,7 +1007,7 @@ template cudaError_t launch_transport<float>(const Scene<float> &, const KernelA
                                              cudaStream_t);
 template cudaError_t launch_transport<double>(const Scene<double> &, const KernelArgs &, int, int, size_t, int,
                                               cudaStream_t);
-template cudaError_t occupancy_blocks<float>(int, size_t, int, int *);
-template cudaError_t occupancy_blocks<double>(int, size_t, int, int *);
+template cudaError_t occupancy_blocks<float>(int, size_t, int, int *, bool);
+template cudaError_t occupancy_blocks<double>(int, size_t, int, int *, bool);
 
 }  // namespace gg

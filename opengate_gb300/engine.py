@@ -89,3 +89,49 @@ class DoseEngine:
 
     def __exit__(self, *a):
         self.close()
+
+
+class SpectEngine(DoseEngine):
+    """SPECT projections: heads + digitizer, one gg_run per gantry position.
+
+    Mirrors a reference SPECT simulation with one run per angle
+    (run_timing_intervals, contrib/spect/ge_discovery_nm670.py:1056-1080
+    rotate_gantry): for run r the heads are placed with spect.frames(r) and
+    n_per_run histories are simulated (history ids continue across runs).
+    """
+
+    def __init__(self, scene, spect, **kw):
+        self.spect = spect
+        super().__init__(scene, **kw)
+
+    def upload(self):
+        s = self.scene
+        self._call("gg_upload_tables", ctypes.byref(s.tables_desc))
+        self._call("gg_upload_volume", ctypes.byref(s.volume_desc))
+        self._call("gg_set_world", ctypes.byref(s.world_desc))
+        self._call("gg_set_source", ctypes.byref(s.source_desc))
+        self._desc = self.spect.desc()
+        self._call("gg_spect_setup", ctypes.byref(self._desc))
+
+    def reset(self):
+        self._call("gg_spect_setup", ctypes.byref(self._desc))
+
+    def run(self, n_per_run, seed, first=0):
+        self.kernel_ms = [0.0, 0.0, 0.0, 0]
+        for r in range(self.spect.n_runs):
+            frames = np.ascontiguousarray(self.spect.frames(r), dtype=np.float64)
+            self._call("gg_spect_set_heads", r, C.ptr(frames, ctypes.c_double))
+            self._call("gg_run", ctypes.c_uint64(n_per_run), ctypes.c_uint64(seed),
+                       ctypes.c_uint64(first + r * n_per_run))
+            g, t, f, n = super().last_kernel_ms()
+            self.kernel_ms = [self.kernel_ms[0] + g, self.kernel_ms[1] + t, self.kernel_ms[2] + f,
+                              self.kernel_ms[3] + n]
+
+    def last_kernel_ms(self):
+        return tuple(self.kernel_ms)
+
+    def projection(self):
+        shape = self.spect.projection_shape()
+        out = np.empty(int(np.prod(shape)), dtype=np.float64)
+        self._call("gg_get_projection", C.ptr(out, ctypes.c_double), out.size)
+        return out.reshape(shape)

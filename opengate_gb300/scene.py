@@ -36,6 +36,22 @@ class SourceSpec:
         self.spec_cdf = None
         self.e_lo = 0.0
         self.e_hi = 0.0
+        # VoxelSource (pos_type GG_POS_VOXELS): activity grid and its CDFs
+        self.vox_dims = [0, 0, 0]
+        self.vox_spacing = [1.0, 1.0, 1.0]
+        self.vox_corner = [0.0, 0.0, 0.0]
+        self.cdf_z = self.cdf_y = self.cdf_x = None
+
+    def set_activity_image(self, activity, spacing, corner):
+        """VoxelSource placement: activity [z][y][x], spacing and outer corner (mm, world)."""
+        from .spect import voxel_cdfs
+
+        act = np.asarray(activity)
+        self.pos_type = C.GG_POS_VOXELS
+        self.vox_dims = [int(act.shape[2]), int(act.shape[1]), int(act.shape[0])]
+        self.vox_spacing = [float(v) for v in spacing]
+        self.vox_corner = [float(v) for v in corner]
+        self.cdf_z, self.cdf_y, self.cdf_x = voxel_cdfs(act)
 
     def energy_bounds(self):
         if self.ene_type == C.GG_ENE_MONO:
@@ -140,6 +156,12 @@ class Scene:
         d.spec_cdf = C.ptr(self._spec_cdf, C.ctypes.c_double)
         d.e_lo = float(s.e_lo)
         d.e_hi = float(s.e_hi)
+        d.vox_dims[:] = s.vox_dims
+        d.vox_spacing[:] = s.vox_spacing
+        d.vox_corner[:] = s.vox_corner
+        self._cdfs = [np.ascontiguousarray(c if c is not None else np.ones(1), dtype=np.float32)
+                      for c in (s.cdf_z, s.cdf_y, s.cdf_x)]
+        d.cdf_z, d.cdf_y, d.cdf_x = (C.ptr(c, C.ctypes.c_float) for c in self._cdfs)
         self.source_desc = d
 
     def set_source(self, source):

@@ -1,0 +1,128 @@
+"""SPECT heads, gantry positions and the projection digitizer.
+
+The head model follows the parallel-hole heads of the reference
+(contrib/spect/ge_discovery_nm670.py:125-164 add_spect_head, 464-490
+lehr_collimator_repeater; contrib/spect/siemens_intevo.py:367-410 for the
+medium-energy collimator): a lead collimator slab with hexagonal holes
+(G4Polyhedra, "radius" = apothem) repeated on two offset rectangular
+lattices, then the NaI crystal.  Shielding, cover and back compartment are
+not modelled (their backscatter contribution to the low windows is left out).
+
+Digitizer: per event and head the crystal deposits are summed and placed at
+the energy-winner position (GateDigiAdderInVolume::Update, EnergyWinnerPosition),
+classified into energy windows [lo, hi) (GateDigitizerEnergyWindowsActor::
+ApplyThreshold) and counted in the projection pixel of that position on the
+detector plane (GateDigitizerProjectionActor::ProcessSlice), slice = window +
+run * n_windows.
+
+Gantry: head h at run r sits at angle theta = start + r * step + h * 360/n_heads
+about the z axis; its outward normal is (sin theta, -cos theta, 0) (theta = 0:
+anterior, -y), e1 = (cos theta, sin theta, 0), e2 = (0, 0, 1), and the
+collimator front face is at ``radius`` from the axis.
+"""
+
+import math
+
+import numpy as np
+
+from . import _capi as C
+
+# parallel-hole collimators: (hole apothem, hole length, pitch between adjacent holes) in mm
+LEHR = dict(hole_apothem=0.75, collimator_thickness=35.0, hole_pitch=1.7)  # 1.5 mm holes, 0.2 mm septa
+MELP = dict(hole_apothem=1.47, collimator_thickness=40.6, hole_pitch=4.08)  # 2.94 mm holes, 1.14 mm septa
+
+
+class SpectSpec:
+    def __init__(self, collimator=LEHR, crystal_thickness=9.525, gap=0.0, radius=250.0, n_heads=2,
+                 n_runs=60, start_angle_deg=0.0, step_angle_deg=6.0, windows=((0.126, 0.154), (0.108, 0.126)),
+                 size=(128, 128), spacing=(4.42, 4.42), collimator_material=0, crystal_material=0):
+        if n_heads not in (1, 2):
+            raise ValueError("1 or 2 heads")
+        if len(windows) > 8:
+            raise ValueError("at most 8 energy windows")
+        self.hole_apothem = float(collimator["hole_apothem"])
+        self.collimator_thickness = float(collimator["collimator_thickness"])
+        pitch = float(collimator["hole_pitch"])
+        # adjacent holes at 30 degrees: lattice repeat (2 pitch cos 30, pitch)
+        self.pitch_x = 2.0 * pitch * math.cos(math.radians(30.0))
+        self.pitch_y = pitch
+        self.crystal_thickness = float(crystal_thickness)
+        self.gap = float(gap)
+        self.radius = float(radius)
+        self.n_heads = int(n_heads)
+        self.n_runs = int(n_runs)
+        self.start_angle = math.radians(start_angle_deg)
+        self.step_angle = math.radians(step_angle_deg)
+        self.windows = [(float(a), float(b)) for a, b in windows]
+        self.size = [int(v) for v in size]
+        self.spacing = [float(v) for v in spacing]
+        self.half_width = 0.5 * max(self.size[0] * self.spacing[0], self.size[1] * self.spacing[1])
+        self.collimator_material = int(collimator_material)
+        self.crystal_material = int(crystal_material)
+
+    @property
+    def n_windows(self):
+        return len(self.windows)
+
+    def desc(self):
+        d = C.SpectDesc()
+        d.half_width = self.half_width
+        d.collimator_thickness = self.collimator_thickness
+        d.gap = self.gap
+        d.crystal_thickness = self.crystal_thickness
+        d.hole_apothem = self.hole_apothem
+        d.pitch_x = self.pitch_x
+        d.pitch_y = self.pitch_y
+        d.collimator_material = self.collimator_material
+        d.crystal_material = self.crystal_material
+        d.n_windows = self.n_windows
+        for k, (lo, hi) in enumerate(self.windows):
+            d.window_lo[k] = lo
+            d.window_hi[k] = hi
+        d.size[:] = self.size
+        d.spacing[:] = self.spacing
+        d.n_heads = self.n_heads
+        d.n_runs = self.n_runs
+        return d
+
+    def angle(self, run, head):
+        return self.start_angle + run * self.step_angle + head * 2.0 * math.pi / self.n_heads
+
+    def frames(self, run):
+        """[n_heads][12]: front-face centre, outward normal, e1, e2 (float64)."""
+        out = np.zeros((self.n_heads, 12))
+        for h in range(self.n_heads):
+            t = self.angle(run, h)
+            u = np.array([math.sin(t), -math.cos(t), 0.0])
+            e1 = np.array([math.cos(t), math.sin(t), 0.0])
+            out[h] = np.concatenate([self.radius * u, u, e1, [0.0, 0.0, 1.0]])
+        return out
+
+    def all_frames(self):
+        return np.ascontiguousarray(np.stack([self.frames(r) for r in range(self.n_runs)]))
+
+    def projection_shape(self):
+        """(head, run * window, y, x), the slice order of the reference's projection image."""
+        return self.n_heads, self.n_runs * self.n_windows, self.size[1], self.size[0]
+
+
+def voxel_cdfs(activity):
+    """(cdf_z, cdf_y, cdf_x) float32 arrays of an activity image [z][y][x].
+
+    Restates compute_image_3D_CDF (opengate/image.py:313-360): normalise the
+    image, cumulative sums along x per (z, y) row (normalised when the row sum
+    is not zero), along y of the x-sums per z slice, and along z of the xy-sums.
+    """
+    a = np.asarray(activity, dtype=np.float64)
+    a = a / np.sum(a)
+    sumx = a.sum(axis=2)
+    sumxy = sumx.sum(axis=1)
+    cdf_x = np.cumsum(a, axis=2)
+    last = cdf_x[:, :, -1:]
+    cdf_x = np.divide(cdf_x, last, out=cdf_x.copy(), where=last != 0)
+    cdf_y = np.cumsum(sumx, axis=1)
+    lasty = cdf_y[:, -1:]
+    cdf_y = np.divide(cdf_y, lasty, out=cdf_y.copy(), where=lasty != 0)
+    cdf_z = np.cumsum(sumxy) / np.sum(sumxy)
+    return (np.ascontiguousarray(cdf_z, np.float32), np.ascontiguousarray(cdf_y, np.float32),
+            np.ascontiguousarray(cdf_x, np.float32))

@@ -137,3 +137,67 @@ def ct_phantom(seed=20240611, shape=(160, 256, 256), spacing=1.2, ssd=1000.0, fi
     src.spec_e, src.spec_cdf = spectrum_e_exp()
     air = 0
     return Scene(pt, labels, [spacing] * 3, corner, [1500.0, 1500.0, 1500.0], air, src), hu
+
+
+def activity_phantom(hu, spacing=1.2, seed=424242, n_spheres=6, background=1.0):
+    """Activity image [z][y][x] on the CT grid: uniform background in the body plus hot spheres.
+
+    Spheres: radius 5-20 mm, contrast 4-10 x background, centres drawn inside the
+    body (soft tissue) away from its edge.  Units: relative activity per voxel.
+    """
+    rng = np.random.default_rng(seed)
+    nz, ny, nx = hu.shape
+    x = (np.arange(nx) + 0.5) * spacing - nx * spacing / 2
+    y = (np.arange(ny) + 0.5) * spacing - ny * spacing / 2
+    z = (np.arange(nz) + 0.5) * spacing - nz * spacing / 2
+    Z, Y, X = np.meshgrid(z, y, x, indexing="ij")
+    body = (X / 160.0) ** 2 + (Y / 110.0) ** 2 <= 1.0
+    act = np.where(body, background, 0.0)
+    zmax = nz * spacing / 2 - 25.0
+    for _ in range(n_spheres):
+        r = rng.uniform(5.0, 20.0)
+        c = rng.uniform(4.0, 10.0)
+        while True:
+            cx, cy, cz = rng.uniform(-120, 120), rng.uniform(-80, 80), rng.uniform(-zmax, zmax)
+            if (cx / (160.0 - r - 10)) ** 2 + (cy / (110.0 - r - 10)) ** 2 <= 1.0:
+                break
+        m = (X - cx) ** 2 + (Y - cy) ** 2 + (Z - cz) ** 2 <= r * r
+        act[m] = background * c
+    return act
+
+
+# radionuclide photon lines (MeV, yield per decay)
+TC99M = ([0.1405], [0.89])
+LU177 = ([0.1129, 0.2084], [0.062, 0.104])
+
+
+def spect_phantom(shape=(160, 256, 256), spacing=1.2, nuclide=TC99M, collimator=None, n_runs=60,
+                  windows=((0.126, 0.154), (0.108, 0.126)), density_tolerance=0.05, seed=20240611):
+    """SPECT workload: CT phantom as attenuation map, body + sphere activity, two heads.
+
+    Returns (scene, spect_spec, activity).  Materials: the CT labels, then
+    G4_Pb (collimator) and G4_SODIUM_IODIDE (crystal).
+    """
+    from . import spect as S
+
+    hu = ct_hu_image(seed, shape, spacing)
+    vm, lut, mats = ct_materials(density_tolerance)
+    labels = M.create_label_image(hu, "G4_AIR", vm, lut)
+    db = M.MaterialDatabase()
+    mats = mats + [db.get("G4_Pb"), db.get("G4_SODIUM_IODIDE")]
+    pt = T.PhysicsTables(mats)
+    nz, ny, nx = shape
+    corner = [-nx * spacing / 2, -ny * spacing / 2, -nz * spacing / 2]
+    act = activity_phantom(hu, spacing)
+    src = SourceSpec()
+    src.set_activity_image(act, [spacing] * 3, corner)
+    src.dir_type = C.GG_DIR_ISO
+    src.ene_type = C.GG_ENE_LINES
+    e, w = nuclide
+    src.spec_e = np.array(e, dtype=np.float64)
+    src.spec_cdf = np.cumsum(w) / np.sum(w)
+    scene = Scene(pt, labels, [spacing] * 3, corner, [1500.0] * 3, 0, src)
+    sp = S.SpectSpec(collimator=collimator or S.LEHR, n_runs=n_runs, windows=windows,
+                     step_angle_deg=360.0 / n_runs, collimator_material=len(mats) - 2,
+                     crystal_material=len(mats) - 1)
+    return scene, sp, act

@@ -402,6 +402,17 @@ typedef struct {
   real s_mono, s_elo, s_ehi;
   real *s_spec_e, *s_spec_cdf;
   real *acc_box;
+  /* voxel source (GateSPSVoxelsPosDistribution) */
+  int vnx, vny, vnz;
+  real v_org[3], v_sp[3]; /* centre of voxel (0,0,0), spacing */
+  real *cdf_z, *cdf_y, *cdf_x;
+  /* SPECT heads and projection digitizer */
+  int spect, n_heads, n_win, pnx, pny, n_runs, run;
+  real hc[2][3], hu[2][3], he1[2][3], he2[2][3];
+  real half_w, zb[4], apo, px, py, hpx, hpy, inv_px, inv_py;
+  int mat_coll, mat_cr;
+  real wlo[8], whi[8], pix_half[2], inv_psp[2];
+  uint64_t *proj; /* [head][run][window][pny][pnx], shared, atomics */
 } scene_t;
 
 typedef struct {
@@ -491,12 +502,21 @@ static uint64_t to_fixed(real v) {
 #endif
 }
 
+/* q = to_fixed(history's voxel sum) goes to acc_e[v]; q^2 (units 2^-64 MeV^2)
+   goes to the 128-bit pair acc_e2[2v] (low) / acc_e2[2v+1] (high), with the
+   carry out of the low word added to the high word. */
 static void hlist_flush(hlist_t *l, tally_t *t) {
   for (int k = 0; k < l->n; ++k) {
-    real a = l->acc[k];
-    real a2 = a * a;
-    __atomic_fetch_add(&t->acc_e[l->vox[k]], to_fixed(a), __ATOMIC_RELAXED);
-    if (t->acc_e2) __atomic_fetch_add(&t->acc_e2[l->vox[k]], to_fixed(a2), __ATOMIC_RELAXED);
+    uint64_t q = to_fixed(l->acc[k]);
+    size_t v = l->vox[k];
+    __atomic_fetch_add(&t->acc_e[v], q, __ATOMIC_RELAXED);
+    if (t->acc_e2) {
+      unsigned __int128 sq = (unsigned __int128)q * q;
+      uint64_t lo = (uint64_t)sq, hi = (uint64_t)(sq >> 64);
+      uint64_t old = __atomic_fetch_add(&t->acc_e2[2 * v], lo, __ATOMIC_RELAXED);
+      hi += (old + lo < old) ? 1u : 0u;
+      if (hi) __atomic_fetch_add(&t->acc_e2[2 * v + 1], hi, __ATOMIC_RELAXED);
+    }
   }
   t->cnt[GG_CNT_TALLY_ENTRIES] += (uint64_t)l->n;
   l->n = 0;
@@ -521,12 +541,21 @@ static void deposit(hlist_t *l, tally_t *t, uint32_t v, real e) {
 }
 
 typedef struct {
-  real pos[3], dir[3], e;
+  real pos[3], dir[3], e; /* world frame; head-local frame while in_head */
   int alive, in_image, can_enter;
   real t_exit;
   eidx_t ei;
   real mumax, inv_mumax;
+  /* SPECT: exclude = box not to re-enter before the next direction change
+     (-1 none, 0 image, 1 + h head h); head, hreg (0 collimator, 1 gap,
+     2 crystal) and left_hole while inside a head */
+  int in_head, head, hreg, left_hole, exclude;
 } photon_t;
+
+/* per-event crystal accumulation of each head (adder, EnergyWinnerPosition) */
+typedef struct {
+  real esum[2], emax[2], wpos[2][3];
+} event_t;
 
 static void set_energy(const scene_t *s, photon_t *ph, real e) {
   ph->e = e;
@@ -736,9 +765,47 @@ static int sample_primary(const scene_t *s, rng_t *g, photon_t *ph, tally_t *t) 
       }
     }
   }
-  real off[3];
-  rot_apply(s->s_rot, loc, off);
-  for (int a = 0; a < 3; ++a) ph->pos[a] = s->s_t[a] + off[a];
+  if (pt == GG_POS_VOXELS) {
+    /* GateSPSVoxelsPosDistribution::VGenerateOne: z, then y | z, then x | z, y */
+    int idx[3];
+    const real *rows[3] = {s->cdf_z, NULL, NULL};
+    int len[3] = {s->vnz, s->vny, s->vnx};
+    for (int lev = 0; lev < 3; ++lev) {
+      const real *c = lev == 0 ? s->cdf_z
+                     : lev == 1 ? s->cdf_y + (size_t)idx[0] * s->vny
+                                : s->cdf_x + ((size_t)idx[0] * s->vny + (size_t)idx[1]) * s->vnx;
+      (void)rows;
+      int k, it = 0;
+      do {
+        real p = u01_open0(g);
+        int lo = 0, hi = len[lev];
+        while (lo < hi) { /* lower_bound: first entry >= p */
+          int mid = (lo + hi) >> 1;
+          if (c[mid] < p) lo = mid + 1;
+          else hi = mid;
+        }
+        k = lo;
+        if (++it >= LOOP_CAP) {
+          t->cnt[GG_CNT_LOOP_CAPPED]++;
+          if (k >= len[lev]) k = len[lev] - 1;
+          break;
+        }
+      } while (k >= len[lev]);
+      idx[lev] = k;
+    }
+    int ind[3] = {idx[2], idx[1], idx[0]}; /* x, y, z */
+    for (int a = 0; a < 3; ++a) {
+      real x = (real)ind[a] * s->v_sp[a];
+      x = s->v_org[a] + x;
+      real j = u01(g) - R(0.5);
+      j = j * s->v_sp[a];
+      ph->pos[a] = x + j;
+    }
+  } else {
+    real off[3];
+    rot_apply(s->s_rot, loc, off);
+    for (int a = 0; a < 3; ++a) ph->pos[a] = s->s_t[a] + off[a];
+  }
   /* direction, with the acceptance loop of GateSingleParticleSource */
   int tries = 0;
   for (;;) {
@@ -786,6 +853,8 @@ static int inside_box(const real p[3], const real lo[3], const real hi[3]) {
 }
 
 static void start_photon(const scene_t *s, photon_t *ph) {
+  ph->in_head = 0;
+  ph->exclude = -1;
   if (inside_box(ph->pos, s->bmin, s->bmax)) {
     ph->in_image = 1;
     ph->t_exit = exit_distance(ph->pos, ph->dir, s->bmin, s->bmax);
@@ -795,8 +864,10 @@ static void start_photon(const scene_t *s, photon_t *ph) {
   }
 }
 
-static void interact(const scene_t *s, photon_t *ph, int mat, rng_t *g, tally_t *t, hlist_t *l,
-                     int scored, uint32_t vox, photon_t *sec, int *has_sec) {
+/* Interaction at ph->pos in material mat; returns the energy deposited
+   locally (the caller scores it where a tally applies). */
+static real interact(const scene_t *s, photon_t *ph, int mat, rng_t *g, tally_t *t, photon_t *sec,
+                     int *has_sec) {
   int c = s->mat_comp[mat];
   const real *cu = s->cum + (size_t)c * 3 * s->n_e;
   real r = u01(g);
@@ -804,26 +875,23 @@ static void interact(const scene_t *s, photon_t *ph, int mat, rng_t *g, tally_t 
   if (r < fc) {
     real ed;
     compton(s, ph, g, t, &ed);
-    if (scored) deposit(l, t, vox, ed);
-    return;
+    return ed;
   }
   real fp = interp_row(cu + s->n_e, ph->ei);
   if (r < fp) {
-    if (scored) deposit(l, t, vox, ph->e);
     ph->alive = 0;
-    return;
+    return ph->e;
   }
   real fr = interp_row(cu + 2 * s->n_e, ph->ei);
   if (r < fr) {
     rayleigh(s, c, ph, g, t);
-    return;
+    return R(0);
   }
   /* pair: both leptons stopped at creation, positron annihilates at rest */
   real ekin = ph->e - R(2.0 * MC2);
-  if (scored) deposit(l, t, vox, ekin);
   real d[3];
   iso_dir(g, d);
-  if (*has_sec) {
+  if (!has_sec || *has_sec) {
     t->cnt[GG_CNT_STACK_OVERFLOW]++;
   } else {
     *sec = *ph;
@@ -838,10 +906,266 @@ static void interact(const scene_t *s, photon_t *ph, int mat, rng_t *g, tally_t 
   ph->dir[2] = d[2];
   set_energy(s, ph, R(MC2));
   t->cnt[GG_CNT_SECONDARIES] += 2;
+  return ekin;
+}
+
+/* ---- SPECT heads ------------------------------------------------------- */
+#define C30 0.86602540378443864676 /* cos 30 degrees */
+
+static real dot3(const real a[3], const real b[3]) {
+  real r = a[0] * b[0];
+  r = r + a[1] * b[1];
+  r = r + a[2] * b[2];
+  return r;
+}
+
+/* world -> head-local (a1 along e1, a2 along e2, w along the outward normal) */
+static void to_local(const scene_t *s, int h, const real p[3], const real d[3], real lp[3], real ld[3]) {
+  real q[3];
+  for (int a = 0; a < 3; ++a) q[a] = p[a] - s->hc[h][a];
+  lp[0] = dot3(q, s->he1[h]);
+  lp[1] = dot3(q, s->he2[h]);
+  lp[2] = dot3(q, s->hu[h]);
+  ld[0] = dot3(d, s->he1[h]);
+  ld[1] = dot3(d, s->he2[h]);
+  ld[2] = dot3(d, s->hu[h]);
+}
+
+static void to_world(const scene_t *s, int h, const real lp[3], const real ld[3], real p[3], real d[3]) {
+  for (int a = 0; a < 3; ++a) {
+    real x = lp[0] * s->he1[h][a];
+    x = s->hc[h][a] + x;
+    x = x + lp[1] * s->he2[h][a];
+    p[a] = x + lp[2] * s->hu[h][a];
+    real y = ld[0] * s->he1[h][a];
+    y = y + ld[1] * s->he2[h][a];
+    d[a] = y + ld[2] * s->hu[h][a];
+  }
+}
+
+/* Hole containing (a1, a2), if any: centres on two rectangular lattices of
+   pitch (px, py), the second offset by half a pitch; a point is in a hole when
+   its distance along each face normal (30, 90, 150 degrees) is <= apothem. */
+static int find_hole(const scene_t *s, real a1, real a2, real *cx, real *cy) {
+  for (int lat = 0; lat < 2; ++lat) {
+    real ox = lat ? s->hpx : R(0), oy = lat ? s->hpy : R(0);
+    real fx = a1 - ox;
+    fx = fx * s->inv_px;
+    fx = fx + R(0.5);
+    fx = (real)floor((double)fx);
+    real fy = a2 - oy;
+    fy = fy * s->inv_py;
+    fy = fy + R(0.5);
+    fy = (real)floor((double)fy);
+    real x = fx * s->px;
+    x = x + ox;
+    real y = fy * s->py;
+    y = y + oy;
+    real qx = a1 - x, qy = a2 - y;
+    real t0 = qx * R(C30), t1 = qy * R(0.5);
+    real n0 = t1 + t0, n2 = t1 - t0;
+    if (fabs((double)qy) <= (double)s->apo && fabs((double)n0) <= (double)s->apo &&
+        fabs((double)n2) <= (double)s->apo) {
+      *cx = x;
+      *cy = y;
+      return 1;
+    }
+  }
+  return 0;
+}
+
+/* distance to leave the hexagonal prism of a hole from q (relative to its
+   centre) along (d1, d2) */
+static real hex_exit(const scene_t *s, real qx, real qy, real d1, real d2) {
+  real t0 = qx * R(C30), t1 = qy * R(0.5);
+  real u0 = d1 * R(C30), u1 = d2 * R(0.5);
+  real qn[3] = {t1 + t0, qy, t1 - t0};
+  real dn[3] = {u1 + u0, d2, u1 - u0};
+  real t = R(INFINITY);
+  for (int k = 0; k < 3; ++k) {
+    real tk;
+    if (dn[k] > R(0)) {
+      tk = s->apo - qn[k];
+      tk = tk / dn[k];
+      if (tk < t) t = tk;
+    } else if (dn[k] < R(0)) {
+      tk = -s->apo - qn[k];
+      tk = tk / dn[k];
+      if (tk < t) t = tk;
+    }
+  }
+  return t < R(0) ? R(0) : t;
+}
+
+static void move(real p[3], const real d[3], real t) {
+  for (int a = 0; a < 3; ++a) p[a] = p[a] + t * d[a];
+}
+
+/* leave the head box (to the world) or move to the next head region */
+static void head_cross(const scene_t *s, photon_t *ph, int leave) {
+  if (leave) {
+    real p[3], d[3];
+    to_world(s, ph->head, ph->pos, ph->dir, p, d);
+    for (int a = 0; a < 3; ++a) {
+      ph->pos[a] = p[a];
+      ph->dir[a] = d[a];
+    }
+    ph->in_head = 0;
+    ph->exclude = 1 + ph->head;
+  } else {
+    ph->hreg += ph->dir[2] > R(0) ? 1 : -1;
+    ph->left_hole = 0;
+  }
+}
+
+/* One step inside a head (photon in head-local coordinates). */
+static void head_step(const scene_t *s, photon_t *ph, rng_t *g, tally_t *t, event_t *ev) {
+  t->cnt[GG_CNT_HEAD_STEPS]++;
+  real *l = ph->pos, *d = ph->dir;
+  real lo[3] = {-s->half_w, -s->half_w, R(0)};
+  real hi[3] = {s->half_w, s->half_w, s->zb[3]};
+  real tbox = exit_distance(l, d, lo, hi);
+  real treg = R(INFINITY);
+  if (d[2] > R(0)) {
+    treg = s->zb[ph->hreg + 1] - l[2];
+    treg = treg / d[2];
+  } else if (d[2] < R(0)) {
+    treg = s->zb[ph->hreg] - l[2];
+    treg = treg / d[2];
+  }
+  if (treg < R(0)) treg = R(0);
+  int leave = tbox <= treg;
+  real tlim = leave ? tbox : treg;
+  if (ph->hreg == 0 && !ph->left_hole) {
+    real cx, cy;
+    if (find_hole(s, l[0], l[1], &cx, &cy)) {
+      real th = hex_exit(s, l[0] - cx, l[1] - cy, d[0], d[1]);
+      ph->left_hole = 1;
+      if (th < tlim) {
+        move(l, d, th);
+        return;
+      }
+      move(l, d, tlim);
+      head_cross(s, ph, leave);
+      return;
+    }
+  }
+  ph->left_hole = 0;
+  if (ph->hreg == 1) {
+    move(l, d, tlim);
+    head_cross(s, ph, leave);
+    return;
+  }
+  int mat = ph->hreg == 0 ? s->mat_coll : s->mat_cr;
+  real mu = interp_row(s->sig + (size_t)s->mat_comp[mat] * s->n_e, ph->ei);
+  mu = s->mat_rho[mat] * mu;
+  real u = u01_open0(g);
+  real sd = -ggo_log(u);
+  sd = sd / mu;
+  if (sd >= tlim) {
+    move(l, d, tlim);
+    head_cross(s, ph, leave);
+    return;
+  }
+  move(l, d, sd);
+  if (ph->hreg == 0) {
+    real cx, cy;
+    if (find_hole(s, l[0], l[1], &cx, &cy)) return; /* null collision inside a hole */
+  }
+  real ed = interact(s, ph, mat, g, t, NULL, NULL);
+  if (ph->hreg == 2 && ed > R(0)) {
+    int h = ph->head;
+    ev->esum[h] = ev->esum[h] + ed;
+    if (ed > ev->emax[h]) {
+      real p[3], dd[3];
+      to_world(s, h, l, d, p, dd);
+      ev->emax[h] = ed;
+      for (int a = 0; a < 3; ++a) ev->wpos[h][a] = p[a];
+    }
+  }
+}
+
+/* World step with the image box and the head boxes as possible targets. */
+static void spect_world_step(const scene_t *s, photon_t *ph, rng_t *g, tally_t *t, photon_t *sec,
+                             int *has_sec) {
+  t->cnt[GG_CNT_WORLD_STEPS]++;
+  real tb = ph->exclude != 0 ? entry_distance(ph->pos, ph->dir, s->bmin, s->bmax) : R(INFINITY);
+  int box = 0;
+  real hlo[3] = {-s->half_w, -s->half_w, R(0)};
+  real hhi[3] = {s->half_w, s->half_w, s->zb[3]};
+  for (int h = 0; h < s->n_heads; ++h) {
+    if (ph->exclude == 1 + h) continue;
+    real lp[3], ld[3];
+    to_local(s, h, ph->pos, ph->dir, lp, ld);
+    real th = entry_distance(lp, ld, hlo, hhi);
+    if (th < tb) {
+      tb = th;
+      box = 1 + h;
+    }
+  }
+  real wlo[3] = {-s->whalf[0], -s->whalf[1], -s->whalf[2]};
+  real tout = exit_distance(ph->pos, ph->dir, wlo, s->whalf);
+  int wm = s->world_mat;
+  real mu = interp_row(s->sig + (size_t)s->mat_comp[wm] * s->n_e, ph->ei);
+  mu = s->mat_rho[wm] * mu;
+  real u = u01_open0(g);
+  real sd = -ggo_log(u);
+  sd = sd / mu;
+  if (sd < tb && sd < tout) {
+    move(ph->pos, ph->dir, sd);
+    interact(s, ph, wm, g, t, sec, has_sec);
+    ph->exclude = -1;
+  } else if (tb <= tout) {
+    move(ph->pos, ph->dir, tb);
+    if (box == 0) {
+      ph->in_image = 1;
+      ph->t_exit = exit_distance(ph->pos, ph->dir, s->bmin, s->bmax);
+    } else {
+      int h = box - 1;
+      real lp[3], ld[3];
+      to_local(s, h, ph->pos, ph->dir, lp, ld);
+      for (int a = 0; a < 3; ++a) {
+        ph->pos[a] = lp[a];
+        ph->dir[a] = ld[a];
+      }
+      ph->in_head = 1;
+      ph->head = h;
+      ph->hreg = lp[2] < s->zb[1] ? 0 : (lp[2] < s->zb[2] ? 1 : 2);
+      ph->left_hole = 0;
+    }
+  } else {
+    ph->alive = 0;
+    t->cnt[GG_CNT_ESCAPED]++;
+  }
+}
+
+/* Singles of one event: energy windows and projection pixel per head. */
+static void score_singles(const scene_t *s, const event_t *ev, tally_t *t) {
+  for (int h = 0; h < s->n_heads; ++h) {
+    real e = ev->esum[h];
+    if (!(e > R(0))) continue;
+    t->cnt[GG_CNT_SINGLES]++;
+    real q[3];
+    for (int a = 0; a < 3; ++a) q[a] = ev->wpos[h][a] - s->hc[h][a];
+    real fx = dot3(q, s->he1[h]);
+    fx = fx + s->pix_half[0];
+    fx = fx * s->inv_psp[0];
+    real fy = dot3(q, s->he2[h]);
+    fy = fy + s->pix_half[1];
+    fy = fy * s->inv_psp[1];
+    if (!(fx >= R(0) && fx < (real)s->pnx && fy >= R(0) && fy < (real)s->pny)) continue;
+    int i = (int)fx, j = (int)fy;
+    for (int k = 0; k < s->n_win; ++k) {
+      if (e >= s->wlo[k] && e < s->whi[k]) {
+        size_t idx = ((((size_t)h * s->n_runs + s->run) * s->n_win + k) * s->pny + j) * s->pnx + i;
+        __atomic_fetch_add(&s->proj[idx], 1ull, __ATOMIC_RELAXED);
+      }
+    }
+  }
 }
 
 static void transport_photon(const scene_t *s, photon_t *ph, rng_t *g, tally_t *t, hlist_t *l,
-                             photon_t *sec, int *has_sec) {
+                             photon_t *sec, int *has_sec, event_t *ev) {
   int steps = 0;
   while (ph->alive) {
     if (++steps > STEP_CAP) {
@@ -858,6 +1182,7 @@ static void transport_photon(const scene_t *s, photon_t *ph, rng_t *g, tally_t *
         for (int a = 0; a < 3; ++a) ph->pos[a] = ph->pos[a] + ph->t_exit * ph->dir[a];
         ph->in_image = 0;
         ph->can_enter = 0;
+        ph->exclude = 0;
         continue;
       }
       ph->t_exit = ph->t_exit - sd;
@@ -876,8 +1201,13 @@ static void transport_photon(const scene_t *s, photon_t *ph, rng_t *g, tally_t *
       real u2 = u01(g);
       if (u2 * ph->mumax >= mu) continue;
       t->cnt[GG_CNT_REAL_INTERACTIONS]++;
-      interact(s, ph, m, g, t, l, 1, v, sec, has_sec);
+      real ed = interact(s, ph, m, g, t, sec, has_sec);
+      if (!s->spect) deposit(l, t, v, ed);
       if (ph->alive && ph->in_image) ph->t_exit = exit_distance(ph->pos, ph->dir, s->bmin, s->bmax);
+    } else if (ph->in_head) {
+      head_step(s, ph, g, t, ev);
+    } else if (s->spect) {
+      spect_world_step(s, ph, g, t, sec, has_sec);
     } else {
       t->cnt[GG_CNT_WORLD_STEPS]++;
       real tin = ph->can_enter ? entry_distance(ph->pos, ph->dir, s->bmin, s->bmax) : R(INFINITY);
@@ -891,7 +1221,7 @@ static void transport_photon(const scene_t *s, photon_t *ph, rng_t *g, tally_t *
       sd = sd / mu;
       if (sd < tin && sd < tout) {
         for (int a = 0; a < 3; ++a) ph->pos[a] = ph->pos[a] + sd * ph->dir[a];
-        interact(s, ph, wm, g, t, l, 0, 0, sec, has_sec);
+        interact(s, ph, wm, g, t, sec, has_sec);
         ph->can_enter = 1;
       } else if (tin <= tout) {
         for (int a = 0; a < 3; ++a) ph->pos[a] = ph->pos[a] + tin * ph->dir[a];
@@ -912,18 +1242,21 @@ static int run_history(const scene_t *s, uint64_t seed, uint64_t h, tally_t *t) 
   l.n = 0;
   photon_t ph, sec;
   int has_sec = 0;
+  event_t ev;
+  memset(&ev, 0, sizeof(ev));
   int st = sample_primary(s, &g, &ph, t);
   if (st != GG_OK) return st;
   t->cnt[GG_CNT_HISTORIES]++;
   start_photon(s, &ph);
   for (;;) {
-    transport_photon(s, &ph, &g, t, &l, &sec, &has_sec);
+    transport_photon(s, &ph, &g, t, &l, &sec, &has_sec, &ev);
     if (!has_sec) break;
     ph = sec;
     has_sec = 0;
     start_photon(s, &ph);
   }
-  hlist_flush(&l, t);
+  if (s->spect) score_singles(s, &ev, t);
+  else hlist_flush(&l, t);
   return GG_OK;
 }
 
@@ -945,6 +1278,7 @@ static real *conv_d(const double *src, size_t n) {
 static void scene_free(scene_t *s) {
   free(s->sig); free(s->cum); free(s->ray_amax); free(s->ray_x2); free(s->ray_cum); free(s->mat_rho);
   free(s->mat_comp); free(s->maj); free(s->s_spec_e); free(s->s_spec_cdf); free(s->acc_box);
+  free(s->cdf_z); free(s->cdf_y); free(s->cdf_x);
 }
 
 static int scene_init(scene_t *s, const gg_tables_desc *tb, const gg_volume_desc *vol,
@@ -993,7 +1327,62 @@ static int scene_init(scene_t *s, const gg_tables_desc *tb, const gg_volume_desc
   s->s_spec_e = conv_d(src->spec_e, (size_t)(src->ene_type == GG_ENE_HISTOGRAM ? ns + 1 : ns));
   s->s_spec_cdf = conv_d(src->spec_cdf, (size_t)ns);
   s->acc_box = conv_d(src->accept_boxes, (size_t)6 * src->n_accept);
+  if (src->pos_type == GG_POS_VOXELS) {
+    s->vnx = src->vox_dims[0];
+    s->vny = src->vox_dims[1];
+    s->vnz = src->vox_dims[2];
+    for (int a = 0; a < 3; ++a) {
+      s->v_org[a] = (real)(src->vox_corner[a] + 0.5 * src->vox_spacing[a]);
+      s->v_sp[a] = (real)src->vox_spacing[a];
+    }
+    s->cdf_z = conv_f(src->cdf_z, (size_t)s->vnz);
+    s->cdf_y = conv_f(src->cdf_y, (size_t)s->vnz * s->vny);
+    s->cdf_x = conv_f(src->cdf_x, (size_t)s->vnz * s->vny * s->vnx);
+  }
   return GG_OK;
+}
+
+static void spect_init(scene_t *s, const gg_spect_desc *sp) {
+  s->spect = 1;
+  s->n_heads = sp->n_heads;
+  s->n_runs = sp->n_runs;
+  s->n_win = sp->n_windows;
+  s->pnx = sp->size[0];
+  s->pny = sp->size[1];
+  s->half_w = (real)sp->half_width;
+  s->zb[0] = R(0);
+  s->zb[1] = (real)sp->collimator_thickness;
+  s->zb[2] = (real)(sp->collimator_thickness + sp->gap);
+  s->zb[3] = (real)(sp->collimator_thickness + sp->gap + sp->crystal_thickness);
+  s->apo = (real)sp->hole_apothem;
+  s->px = (real)sp->pitch_x;
+  s->py = (real)sp->pitch_y;
+  s->hpx = (real)(0.5 * sp->pitch_x);
+  s->hpy = (real)(0.5 * sp->pitch_y);
+  s->inv_px = (real)(1.0 / sp->pitch_x);
+  s->inv_py = (real)(1.0 / sp->pitch_y);
+  s->mat_coll = sp->collimator_material;
+  s->mat_cr = sp->crystal_material;
+  for (int k = 0; k < sp->n_windows; ++k) {
+    s->wlo[k] = (real)sp->window_lo[k];
+    s->whi[k] = (real)sp->window_hi[k];
+  }
+  for (int a = 0; a < 2; ++a) {
+    s->pix_half[a] = (real)(0.5 * sp->size[a] * sp->spacing[a]);
+    s->inv_psp[a] = (real)(1.0 / sp->spacing[a]);
+  }
+}
+
+static void spect_set_heads(scene_t *s, int run, const double *frames) {
+  s->run = run;
+  for (int h = 0; h < s->n_heads; ++h) {
+    for (int a = 0; a < 3; ++a) {
+      s->hc[h][a] = (real)frames[12 * h + a];
+      s->hu[h][a] = (real)frames[12 * h + 3 + a];
+      s->he1[h][a] = (real)frames[12 * h + 6 + a];
+      s->he2[h][a] = (real)frames[12 * h + 9 + a];
+    }
+  }
 }
 
 typedef struct {
@@ -1026,7 +1415,7 @@ int GGO_PREFIX(run_dose)(const gg_tables_desc *tb, const gg_volume_desc *vol, co
   scene_init(&s, tb, vol, w, src);
   size_t nv = (size_t)s.nx * s.ny * s.nz;
   uint64_t *acc_e = (uint64_t *)calloc(nv, sizeof(uint64_t));
-  uint64_t *acc_e2 = edep2 ? (uint64_t *)calloc(nv, sizeof(uint64_t)) : NULL;
+  uint64_t *acc_e2 = edep2 ? (uint64_t *)calloc(2 * nv, sizeof(uint64_t)) : NULL;
   if (n_threads < 1) n_threads = 1;
   if (batch == 0) batch = n ? n : 1;
   worker_t *ws = (worker_t *)calloc((size_t)n_threads, sizeof(worker_t));
@@ -1055,9 +1444,11 @@ int GGO_PREFIX(run_dose)(const gg_tables_desc *tb, const gg_volume_desc *vol, co
         edep[v] += (double)acc_e[v] * 2.3283064365386963e-10;
         acc_e[v] = 0;
       }
-      if (acc_e2 && acc_e2[v]) {
-        edep2[v] += (double)acc_e2[v] * 2.3283064365386963e-10;
-        acc_e2[v] = 0;
+      if (acc_e2 && (acc_e2[2 * v] | acc_e2[2 * v + 1])) {
+        double lo = (double)acc_e2[2 * v];
+        lo = lo * 5.421010862427522e-20; /* 2^-64 */
+        edep2[v] += (double)acc_e2[2 * v + 1] + lo;
+        acc_e2[2 * v] = acc_e2[2 * v + 1] = 0;
       }
     }
   }
@@ -1067,6 +1458,48 @@ int GGO_PREFIX(run_dose)(const gg_tables_desc *tb, const gg_volume_desc *vol, co
   free(th);
   free(acc_e);
   free(acc_e2);
+  scene_free(&s);
+  return status;
+}
+
+/* SPECT projections: for each run r (gantry position, head frames
+   frames[r][n_heads][12]) simulates histories [first + r * n_per_run,
+   first + (r + 1) * n_per_run) and adds singles counts into proj
+   ([head][run][window][pny][pnx], zeroed by the caller). */
+int GGO_PREFIX(run_spect)(const gg_tables_desc *tb, const gg_volume_desc *vol, const gg_world_desc *w,
+                          const gg_source_desc *src, const gg_spect_desc *sp, const double *frames,
+                          uint64_t seed, uint64_t first, uint64_t n_per_run, int n_threads, uint64_t *proj,
+                          uint64_t *counters) {
+  scene_t s;
+  scene_init(&s, tb, vol, w, src);
+  spect_init(&s, sp);
+  s.proj = proj;
+  if (n_threads < 1) n_threads = 1;
+  worker_t *ws = (worker_t *)calloc((size_t)n_threads, sizeof(worker_t));
+  pthread_t *th = (pthread_t *)calloc((size_t)n_threads, sizeof(pthread_t));
+  int status = GG_OK;
+  for (int r = 0; r < sp->n_runs && status == GG_OK; ++r) {
+    spect_set_heads(&s, r, frames + (size_t)r * sp->n_heads * 12);
+    uint64_t b0 = first + (uint64_t)r * n_per_run, b1 = b0 + n_per_run;
+    uint64_t per = (n_per_run + (uint64_t)n_threads - 1) / (uint64_t)n_threads;
+    for (int i = 0; i < n_threads; ++i) {
+      ws[i].s = &s;
+      ws[i].seed = seed;
+      ws[i].h0 = b0 + per * (uint64_t)i < b1 ? b0 + per * (uint64_t)i : b1;
+      ws[i].h1 = ws[i].h0 + per < b1 ? ws[i].h0 + per : b1;
+      ws[i].status = GG_OK;
+      if (n_threads > 1) pthread_create(&th[i], NULL, worker_main, &ws[i]);
+      else worker_main(&ws[i]);
+    }
+    if (n_threads > 1)
+      for (int i = 0; i < n_threads; ++i) pthread_join(th[i], NULL);
+    for (int i = 0; i < n_threads; ++i)
+      if (ws[i].status != GG_OK) status = ws[i].status;
+  }
+  for (int i = 0; i < n_threads; ++i)
+    for (int c = 0; c < GG_N_COUNTERS; ++c) counters[c] += ws[i].t.cnt[c];
+  free(ws);
+  free(th);
   scene_free(&s);
   return status;
 }
@@ -1207,4 +1640,24 @@ int GGO_PREFIX(first_flight)(const gg_tables_desc *tb, const gg_volume_desc *vol
   }
   scene_free(&s);
   return GG_OK;
+}
+
+/* Hole lattice probe: 1 and the hole centre when (a1, a2) lies in a hole. */
+int GGO_PREFIX(find_hole)(const gg_spect_desc *sp, double a1, double a2, double *cx, double *cy) {
+  scene_t s;
+  memset(&s, 0, sizeof(s));
+  spect_init(&s, sp);
+  real x = 0, y = 0;
+  int in = find_hole(&s, (real)a1, (real)a2, &x, &y);
+  *cx = (double)x;
+  *cy = (double)y;
+  return in;
+}
+
+/* Distance from (qx, qy) (relative to a hole centre) to the hole wall along (d1, d2). */
+double GGO_PREFIX(hex_exit)(const gg_spect_desc *sp, double qx, double qy, double d1, double d2) {
+  scene_t s;
+  memset(&s, 0, sizeof(s));
+  spect_init(&s, sp);
+  return (double)hex_exit(&s, (real)qx, (real)qy, (real)d1, (real)d2);
 }

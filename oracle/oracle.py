@@ -141,3 +141,45 @@ def first_flight(scene, n, seed=1, precision=32):
     if st != 0:
         raise RuntimeError(f"first flight failed with status {st}")
     return int(out[0]), int(out[1])
+
+
+def run_spect(scene, spect, n_per_run, seed, first=0, threads=1, precision=32):
+    """Oracle SPECT run: (projection counts [head][run*window][y][x] float64, counters)."""
+    L = lib(precision)
+    fn = getattr(L, f"ggo{precision}_run_spect")
+    fn.restype = ctypes.c_int
+    fn.argtypes = [ctypes.POINTER(C.TablesDesc), ctypes.POINTER(C.VolumeDesc), ctypes.POINTER(C.WorldDesc),
+                   ctypes.POINTER(C.SourceDesc), ctypes.POINTER(C.SpectDesc), ctypes.POINTER(ctypes.c_double),
+                   ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int,
+                   ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64)]
+    shape = spect.projection_shape()
+    proj = np.zeros(int(np.prod(shape)), dtype=np.uint64)
+    cnt = np.zeros(C.GG_N_COUNTERS, dtype=np.uint64)
+    desc = spect.desc()
+    frames = spect.all_frames()
+    st = fn(*_descs(scene), ctypes.byref(desc), C.ptr(frames, ctypes.c_double), seed, first, n_per_run, threads,
+            C.ptr(proj, ctypes.c_uint64), C.ptr(cnt, ctypes.c_uint64))
+    if st != 0:
+        raise RuntimeError(f"oracle SPECT run failed with status {st}")
+    return proj.astype(np.float64).reshape(shape), {name: int(cnt[i]) for i, name in enumerate(C.COUNTER_NAMES)}
+
+
+def find_hole(spect, a1, a2, precision=32):
+    L = lib(precision)
+    f = getattr(L, f"ggo{precision}_find_hole")
+    f.restype = ctypes.c_int
+    f.argtypes = [ctypes.POINTER(C.SpectDesc), ctypes.c_double, ctypes.c_double, ctypes.POINTER(ctypes.c_double),
+                  ctypes.POINTER(ctypes.c_double)]
+    cx, cy = ctypes.c_double(), ctypes.c_double()
+    d = spect.desc()
+    inside = f(ctypes.byref(d), float(a1), float(a2), ctypes.byref(cx), ctypes.byref(cy))
+    return bool(inside), cx.value, cy.value
+
+
+def hex_exit(spect, qx, qy, d1, d2, precision=32):
+    L = lib(precision)
+    f = getattr(L, f"ggo{precision}_hex_exit")
+    f.restype = ctypes.c_double
+    f.argtypes = [ctypes.POINTER(C.SpectDesc)] + [ctypes.c_double] * 4
+    d = spect.desc()
+    return f(ctypes.byref(d), float(qx), float(qy), float(d1), float(d2))

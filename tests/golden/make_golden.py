@@ -196,6 +196,20 @@ def nist_fixtures(ref):
                         muen_rho=muen.reshape(len(zs), len(es)))
 
 
+def voxel_cdf_fixtures(ref):
+    """compute_image_3D_CDF (opengate/image.py:313-360) on an activity image with empty rows/slices."""
+    ns = {"np": np, "itk": types.SimpleNamespace(array_from_image=lambda im: np.array(im))}
+    _exec_functions(ref / "opengate/image.py", ["compute_image_3D_CDF"], ns)
+    rng = np.random.default_rng(3)
+    act = rng.gamma(0.6, 1.0, size=(6, 7, 9))
+    act[2] = 0.0  # an empty z slice
+    act[4, 3] = 0.0  # an empty row
+    act[act < 0.2] = 0.0
+    cdf_x, cdf_y, cdf_z = ns["compute_image_3D_CDF"](act)
+    np.savez_compressed(OUT / "voxel_cdf.npz", activity=act, cdf_x=np.array(cdf_x), cdf_y=np.array(cdf_y),
+                        cdf_z=np.array(cdf_z))
+
+
 def main(ref):
     ref = pathlib.Path(ref)
     # the Schneider 2000 HU tables are inputs of the HU fixtures; keep copies of
@@ -207,6 +221,7 @@ def main(ref):
     label_fixtures(ref, hu)
     variance_fixtures(ref)
     nist_fixtures(ref)
+    voxel_cdf_fixtures(ref)
     print("golden fixtures written to", OUT)
 
 
