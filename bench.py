@@ -34,6 +34,14 @@ UNIT = "primaries/s"
 PRIMARIES_PER_STEP = 100_000_000
 WORKLOAD = "ct_phantom_256x256x160_1.2mm_ssd100_field10x10_spectrum60_0.1-6MeV"
 
+# SPECT acquisition: CT phantom as attenuation map, Tc-99m activity image,
+# two LEHR heads at 25 cm, 60 gantry positions, 1e9 decays (0.89 photons each)
+SPECT_METRIC = "primaries/s at matched sigma (plain GPU collimator tracking, SPECT projections)"
+SPECT_DECAYS = 1_000_000_000
+SPECT_YIELD = 0.89
+SPECT_WORKLOAD = ("spect_tc99m_lehr_2heads_60angles_r250mm_128x128x4.42mm_windows126-154_108-126keV_"
+                  "ct_phantom_256x256x160_1.2mm")
+
 
 def measured_peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
@@ -154,10 +162,35 @@ def cpu_sample(scene, threads, target_s=10.0, seed=424242):
     return n2 / dt2, n2, dt2
 
 
+def spect_cpu_sample(scene, sp, threads, target_s=10.0, seed=424242):
+    """Times the CPU restatement of the SPECT path on a bounded sample (all 60 positions)."""
+    from oracle import oracle as O
+
+    n_runs = sp.n_runs
+    n = 2000
+    t_prev, n_prev = None, None
+    while True:
+        t0 = time.perf_counter()
+        O.run_spect(scene, sp, n, seed, threads=threads)
+        dt = time.perf_counter() - t0
+        if dt > 0.25 * target_s or n * n_runs >= 5e7:
+            break
+        t_prev, n_prev = dt, n
+        n *= 4
+    rate = (n - n_prev) * n_runs / max(dt - t_prev, 1e-6) if n_prev else n * n_runs / dt
+    n2 = int(min(max(n, rate * target_s / n_runs), 4e8 / n_runs))
+    t0 = time.perf_counter()
+    O.run_spect(scene, sp, n2, seed + 1, threads=threads)
+    dt2 = time.perf_counter() - t0
+    return n2 * n_runs / dt2, n2 * n_runs, dt2
+
+
 def run_reference(args):
     ws, rank, _ = dist_env()
     if rank != 0:
         return 0
+    if args.workload == "spect":
+        return run_reference_spect(args)
     from opengate_gb300 import workloads as W
 
     scene, _ = W.ct_phantom()
@@ -188,6 +221,143 @@ def run_reference(args):
     return 0
 
 
+def run_reference_spect(args):
+    from opengate_gb300 import workloads as W
+
+    scene, sp, _ = W.spect_phantom()
+    threads = os.cpu_count() or 1
+    n_step = int(SPECT_DECAYS * SPECT_YIELD)
+    t_all = time.perf_counter()
+    for _ in range(args.warmup):
+        spect_cpu_sample(scene, sp, threads, target_s=1.0)
+    rates, samples = [], []
+    for _ in range(args.steps):
+        r, n, dt = spect_cpu_sample(scene, sp, threads, target_s=8.0)
+        rates.append(r)
+        samples.append(n)
+    value = float(np.median(rates))
+    line = {
+        "impl": "reference", "metric": SPECT_METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": n_step / value * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded CT phantom + activity image)",
+        "config": {"workload": SPECT_WORKLOAD, "primaries_per_step": n_step,
+                   "note": "CPU restatement of the path (C, pthreads); Geant4/opengate_core not installable offline"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{int(np.median(samples))} primaries over the 60 positions per step, "
+                                   "all host threads"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "wall_s": time.perf_counter() - t_all,
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours_spect(args, ws, rank, local, dist, use_cuda):
+    import torch
+
+    from opengate_gb300 import spect as S
+    from opengate_gb300 import workloads as W
+    from opengate_gb300.engine import SpectEngine
+
+    scene, sp, _ = W.spect_phantom()
+    n_step = args.primaries if args.primaries != PRIMARIES_PER_STEP else int(SPECT_DECAYS * SPECT_YIELD)
+    n_per_run = n_step // sp.n_runs
+    n = n_per_run * sp.n_runs
+    eng = SpectEngine(scene, sp, device=local, precision=32, batch=args.batch)
+    l2_flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=f"cuda:{local}")
+
+    def first_of(step):
+        return ((rank * (args.warmup + args.steps + 4)) + step) * n
+
+    for w in range(args.warmup):
+        eng.reset()
+        eng.run(n_per_run, args.seed, first_of(w))
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    dev_ms, launches = [], 0
+    t0 = time.perf_counter()
+    with ClockSampler(local) as clk:
+        for k in range(args.steps):
+            l2_flush.zero_()
+            torch.cuda.synchronize()
+            eng.reset()
+            eng.run(n_per_run, args.seed, first_of(args.warmup + k))
+            tg, tt, tf, nl = eng.last_kernel_ms()
+            dev_ms.append(tg + tt + tf)
+            launches += nl
+            if k == args.steps - 1:
+                counters = eng.counters()
+                transport_ms = tt
+                stage_ms = {"generate": tg, "transport": tt, "flush": tf}
+                launches_last = nl
+        torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    if dist:
+        dist.barrier()
+    total_ms = dist_max(dist, float(np.sum(dev_ms)), use_cuda)
+    value = ws * n * args.steps / (total_ms / 1e3)
+    proj = eng.projection()
+    peak = proj[:, 0::sp.n_windows]  # photopeak window of every head and position
+    sigma = S.mean_relative_uncertainty(peak, peak, n)  # one count per event: squared counts == counts
+
+    # e2e through the C ABI with host buffers: scene + heads upload, all positions, projection download
+    h2d = scene.labels.nbytes + scene._sig.nbytes + scene._cum.nbytes + scene._ray_amax.nbytes + \
+        scene._ray_cum.nbytes + scene.majorant.nbytes + scene.source_desc_bytes() + sp.all_frames().nbytes
+    d2h = int(np.prod(sp.projection_shape())) * 8
+    torch.cuda.synchronize()
+    e2e_t = []
+    for k in range(max(1, min(args.steps, 3))):
+        t1 = time.perf_counter()
+        eng.upload()
+        eng.run(n_per_run, args.seed, first_of(args.warmup + args.steps + k))
+        eng.projection()
+        e2e_t.append(time.perf_counter() - t1)
+    e2e_s = dist_max(dist, float(np.mean(e2e_t)), use_cuda)
+
+    peak_bw, peak_kind = measured_peaks()
+    bytes_alg = 32.0 * counters["woodcock_steps"] + 8.0 * counters["singles"]
+    achieved = bytes_alg / (transport_ms / 1e3) / 1e9
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak_bw, "unit": "GB/s",
+                "frac": achieved / peak_bw, "traffic": args.traffic, "peak_kind": peak_kind,
+                "kernel": "k_spect_phantom<float> + k_spect_head<float> (phantom and head stages)",
+                "bytes_alg_per_step": bytes_alg,
+                "units": {"woodcock_steps": counters["woodcock_steps"], "head_steps": counters["head_steps"],
+                          "singles": counters["singles"], "launches_per_step": launches_last},
+                "stage_ms_per_step": stage_ms}
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        r, ns, dt = spect_cpu_sample(scene, sp, threads, target_s=args.cpu_seconds)
+        cpu = {"value": r, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"{ns} primaries over the 60 positions, {dt:.1f} s on {threads} host threads"}
+    if rank == 0:
+        line = {
+            "metric": SPECT_METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded CT phantom + activity image)",
+            "config": {"workload": SPECT_WORKLOAD, "primaries_per_step": n, "decays_per_step": n / SPECT_YIELD,
+                       "l2": "flushed between steps (256 MiB write)", "batch": args.batch,
+                       "parallelism": f"replicas x{ws}, disjoint history ranges"},
+            "sigma": {"mean_relative_uncertainty_peak_window_gt10pct_max": sigma, "primaries": n,
+                      "counts_peak_window": float(peak.sum())},
+            "e2e": {"value": ws * n / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h)},
+            "roofline": roofline,
+            "cpu_baseline": cpu,
+            "clocks": clk.summary(),
+            "gpu_launches": int(launches),
+            "wall_s": wall,
+        }
+        print(json.dumps(line), flush=True)
+    eng.close()
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
 def run_ours(args):
     ws, rank, local = dist_env()
     import torch
@@ -197,6 +367,8 @@ def run_ours(args):
         raise RuntimeError("bench.py needs a CUDA GPU for --impl ours")
     torch.cuda.set_device(local)
     dist = dist_init(ws, use_cuda)
+    if args.workload == "spect":
+        return run_ours_spect(args, ws, rank, local, dist, use_cuda)
     from opengate_gb300 import _capi as C
     from opengate_gb300 import workloads as W
     from opengate_gb300.engine import DoseEngine
@@ -307,6 +479,8 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="dose", choices=["dose", "spect"],
+                    help="dose: CT phantom DoseActor (default); spect: Tc-99m SPECT acquisition, 60 positions")
     ap.add_argument("--primaries", type=int, default=PRIMARIES_PER_STEP)
     ap.add_argument("--batch", type=int, default=1 << 27)
     ap.add_argument("--seed", type=int, default=20240611)

@@ -236,14 +236,22 @@ int gg_last_kernel_ms(gg_ctx *ctx, double *generate_ms, double *transport_ms, do
    464-490 and GateDigitizerHitsCollectionActor / GateDigiAdderInVolume /
    GateDigitizerEnergyWindowsActor / GateDigitizerProjectionActor,
    core/opengate_core/opengate_lib/digitizer/*.cpp).  gg_spect_setup enables
-   the head transport and zeroes the projection counts; the dose tally is not
-   needed.  gg_spect_set_heads places the heads for one run (gantry position):
+   the head transport and zeroes the projection counts and the counters; the
+   dose tally is not needed.  gg_spect_set_heads places the heads for one run (gantry position):
    frames[n_heads][12] = collimator front-face centre xyz, outward normal xyz,
    e1 xyz, e2 xyz (world, unit vectors); the following gg_run calls score into
-   that run's slices.  gg_get_projection returns the counts as float64,
+   that run's slices.  gg_spect_run simulates every run in one call (the
+   reference's run_timing_intervals loop with one head position per run,
+   contrib/spect/ge_discovery_nm670.py:1056-1080 rotate_gantry): run r gets
+   histories [first + r n_per_run, first + (r + 1) n_per_run) and the head
+   frames frames[r][n_heads][12] (NULL: the frames given so far by
+   gg_spect_set_heads); all runs go through one set of launches, so results
+   equal n_runs gg_spect_set_heads + gg_run calls with the same histories.
+   gg_get_projection returns the counts as float64,
    [head][run][window][size[1]][size[0]]. */
 int gg_spect_setup(gg_ctx *ctx, const gg_spect_desc *spect);
 int gg_spect_set_heads(gg_ctx *ctx, int32_t run, const double *frames);
+int gg_spect_run(gg_ctx *ctx, uint64_t n_per_run, uint64_t seed, uint64_t first, const double *frames);
 int gg_get_projection(gg_ctx *ctx, double *out, size_t n);
 
 /* ---- dose run that allocates no device memory ------------------------------

@@ -76,7 +76,11 @@ struct gg_ctx {
   gg_spect_desc spect{};
   bool have_spect = false;
   int spect_run = 0;
-  double frames[2][12] = {};
+  std::vector<double> frames;  // [n_runs][n_heads][12], host copy
+  void *d_frames = nullptr;    // same in working precision
+  bool frames_dirty = true;
+  uint64_t run_first = 0, run_len = 1;  // history h -> run run_base + (h - run_first) / run_len
+  int run_base = 0;
   unsigned long long *d_proj = nullptr;
   size_t n_proj = 0;
 
@@ -90,9 +94,13 @@ struct gg_ctx {
   unsigned int *d_status = nullptr;
   void *d_records = nullptr;
   size_t rec_cap = 0;
+  // SPECT stage queues (head queue, return queue) and their lengths
+  void *d_queue[2] = {nullptr, nullptr};
+  size_t q_cap = 0;
+  unsigned long long *d_qn = nullptr;
   std::vector<cudaEvent_t> ev;
   double last_generate_ms = 0, last_transport_ms = 0, last_flush_ms = 0;
-  int last_launches = 0;
+  int last_launches = 0, last_stage_launches = 0, run_stage_launches = 0;
 
   int fail(int code, const char *fmt, ...) {
     char buf[512];
@@ -146,7 +154,9 @@ struct gg_ctx {
     dfree(d_labels); dfree(d_maj); dfree(d_spec_e); dfree(d_spec_cdf); dfree(d_acc_box);
     dfree(d_acc_e); dfree(d_acc_e2); dfree(d_edep); dfree(d_edep2);
     dfree(d_counters); dfree(d_next); dfree(d_status); dfree(d_records);
-    dfree(d_cdf_z); dfree(d_cdf_y); dfree(d_cdf_x); dfree(d_proj);
+    dfree(d_queue[0]); dfree(d_queue[1]); dfree(d_qn);
+    q_cap = 0;
+    dfree(d_cdf_z); dfree(d_cdf_y); dfree(d_cdf_x); dfree(d_proj); dfree(d_frames);
     rec_cap = 0;
     for (auto e : ev) cudaEventDestroy(e);
     ev.clear();
@@ -230,7 +240,10 @@ struct gg_ctx {
       s.n_win = sp.n_windows;
       s.pnx = sp.size[0];
       s.pny = sp.size[1];
-      s.run = spect_run;
+      s.frames = (const real *)d_frames;
+      s.run_first = run_first;
+      s.run_len = run_len;
+      s.run_base = run_base;
       s.half_w = (real)sp.half_width;
       s.zb[0] = (real)0;
       s.zb[1] = (real)sp.collimator_thickness;
@@ -253,13 +266,6 @@ struct gg_ctx {
         s.pix_half[a] = (real)(0.5 * sp.size[a] * sp.spacing[a]);
         s.inv_psp[a] = (real)(1.0 / sp.spacing[a]);
       }
-      for (int h = 0; h < sp.n_heads; ++h)
-        for (int a = 0; a < 3; ++a) {
-          s.hc[h][a] = (real)frames[h][a];
-          s.hu[h][a] = (real)frames[h][3 + a];
-          s.he1[h][a] = (real)frames[h][6 + a];
-          s.he2[h][a] = (real)frames[h][9 + a];
-        }
       s.proj = d_proj;
     }
     return s;
@@ -514,6 +520,61 @@ int gg_reset_tally(gg_ctx *c) {
   return c->cuda(cudaMemsetAsync(c->d_status, 0, sizeof(unsigned int), c->stream), "memset");
 }
 
+static int upload_frames(gg_ctx *c) {
+  if (!c->frames_dirty && c->d_frames) return GG_OK;
+  int st = c->upload_real_d(c->d_frames, c->frames.data(), c->frames.size());
+  if (st) return st;
+  c->frames_dirty = false;
+  return GG_OK;
+}
+
+// SPECT transport of one batch: phantom stage on the primary records, head
+// stage on the head queue, then phantom / head passes on the photons that
+// flew back into the image until the return queue stays empty.
+static int spect_stages(gg_ctx *c, gg::KernelArgs a, size_t smem, int minb) {
+  int bps[2] = {0, 0};
+  for (int stage = 0; stage < 2; ++stage) {
+    cudaError_t e = c->precision == GG_PREC_F64
+                        ? gg::spect_stage_occupancy<double>(stage, c->block, smem, minb, &bps[stage])
+                        : gg::spect_stage_occupancy<float>(stage, c->block, smem, minb, &bps[stage]);
+    if (e != cudaSuccess) return c->cuda(e, "occupancy");
+    if (bps[stage] < 1) bps[stage] = 1;
+  }
+  unsigned long long *nh = c->d_qn, *nr = c->d_qn + 1;
+  auto stage_run = [&](int stage, void *in_q, const unsigned long long *in_n, void *out_q,
+                       unsigned long long *out_n) -> int {
+    gg::StageArgs q{in_q, in_n, out_q, out_n, c->q_cap};
+    int st;
+    if ((st = c->cuda(cudaMemsetAsync(out_n, 0, sizeof(unsigned long long), c->stream), "memset"))) return st;
+    if ((st = c->cuda(cudaMemsetAsync(c->d_next, 0, 8, c->stream), "memset"))) return st;
+    int grid = c->n_sm * bps[stage];
+    cudaError_t e = c->precision == GG_PREC_F64
+                        ? gg::launch_spect_stage<double>(stage, c->scene<double>(), a, q, grid, c->block, smem, minb,
+                                                         c->stream)
+                        : gg::launch_spect_stage<float>(stage, c->scene<float>(), a, q, grid, c->block, smem, minb,
+                                                        c->stream);
+    return c->cuda(e, "SPECT stage launch");
+  };
+  int st;
+  if ((st = stage_run(0, nullptr, nullptr, c->d_queue[0], nh))) return st;
+  if ((st = stage_run(1, c->d_queue[0], nh, c->d_queue[1], nr))) return st;
+  c->last_stage_launches = 2;
+  for (int pass = 1;; ++pass) {
+    unsigned long long back = 0;
+    if ((st = c->cuda(cudaMemcpyAsync(&back, nr, sizeof(back), cudaMemcpyDeviceToHost, c->stream), "queue length")))
+      return st;
+    if ((st = c->cuda(cudaStreamSynchronize(c->stream), "SPECT stages"))) return st;
+    if (back == 0) break;
+    // a photon re-enters the image at most once per phantom / head pass; the
+    // per-photon step cap ends every history, so this loop ends too
+    if (pass > 100000) return c->fail(GG_ERR_DOMAIN, "SPECT stages: photons keep returning to the image");
+    if ((st = stage_run(0, c->d_queue[1], nr, c->d_queue[0], nh))) return st;
+    if ((st = stage_run(1, c->d_queue[0], nh, c->d_queue[1], nr))) return st;
+    c->last_stage_launches += 2;
+  }
+  return GG_OK;
+}
+
 static int run_impl(gg_ctx *c, uint64_t n, uint64_t seed, uint64_t first) {
   size_t smem = c->precision == GG_PREC_F64 ? gg::transport_smem_bytes<double>(c->n_comp, c->n_e, c->n_mat)
                                             : gg::transport_smem_bytes<float>(c->n_comp, c->n_e, c->n_mat);
@@ -521,10 +582,8 @@ static int run_impl(gg_ctx *c, uint64_t n, uint64_t seed, uint64_t first) {
   int minb = c->blocks_per_sm > 0 ? std::min(c->blocks_per_sm, 4) : (c->precision == GG_PREC_F64 ? 2 : 3);
   int bps = 0;
   {
-    cudaError_t e = c->precision == GG_PREC_F64 ? gg::occupancy_blocks<double>(c->block, smem, minb, &bps,
-                                                                                c->have_spect)
-                                                : gg::occupancy_blocks<float>(c->block, smem, minb, &bps,
-                                                                               c->have_spect);
+    cudaError_t e = c->precision == GG_PREC_F64 ? gg::occupancy_blocks<double>(c->block, smem, minb, &bps)
+                                                : gg::occupancy_blocks<float>(c->block, smem, minb, &bps);
     if (e != cudaSuccess) return c->cuda(e, "occupancy");
     if (bps < 1) bps = 1;
   }
@@ -538,6 +597,17 @@ static int run_impl(gg_ctx *c, uint64_t n, uint64_t seed, uint64_t first) {
     int st = c->cuda(cudaMalloc(&c->d_records, bytes), "cudaMalloc primary records");
     if (st) return st;
     c->rec_cap = cap;
+  }
+  if (c->have_spect && cap > c->q_cap) {
+    dfree(c->d_queue[0]);
+    dfree(c->d_queue[1]);
+    c->q_cap = 0;
+    size_t qb = c->precision == GG_PREC_F64 ? gg::queue_bytes<double>(cap) : gg::queue_bytes<float>(cap);
+    int st = c->cuda(cudaMalloc(&c->d_queue[0], qb), "cudaMalloc head queue");
+    if (!st) st = c->cuda(cudaMalloc(&c->d_queue[1], qb), "cudaMalloc return queue");
+    if (!st && !c->d_qn) st = c->cuda(cudaMalloc(&c->d_qn, 2 * sizeof(unsigned long long)), "cudaMalloc queue lengths");
+    if (st) return st;
+    c->q_cap = cap;
   }
   while (c->ev.size() < 3 * nb + 1) {
     cudaEvent_t e;
@@ -558,6 +628,7 @@ static int run_impl(gg_ctx *c, uint64_t n, uint64_t seed, uint64_t first) {
   a.refill_min = c->refill_min;
   a.interact_min = c->interact_min;
   int flush_grid = c->n_sm * 8;
+  c->run_stage_launches = 0;
   int st;
   // per batch: [ev 3b] generate [ev 3b+1] transport [ev 3b+2] flush [ev 3b+3]
   for (uint64_t b = 0; b < nb; ++b) {
@@ -569,10 +640,15 @@ static int run_impl(gg_ctx *c, uint64_t n, uint64_t seed, uint64_t first) {
                                                 : gg::launch_generate<float>(c->scene<float>(), a, c->stream);
     if ((st = c->cuda(e, "generate launch"))) return st;
     if ((st = c->cuda(cudaEventRecord(c->ev[3 * b + 1], c->stream), "event"))) return st;
-    e = c->precision == GG_PREC_F64
-            ? gg::launch_transport<double>(c->scene<double>(), a, grid, c->block, smem, minb, c->stream)
-            : gg::launch_transport<float>(c->scene<float>(), a, grid, c->block, smem, minb, c->stream);
-    if ((st = c->cuda(e, "transport launch"))) return st;
+    if (c->have_spect) {
+      if ((st = spect_stages(c, a, smem, minb))) return st;
+      c->run_stage_launches += c->last_stage_launches;
+    } else {
+      e = c->precision == GG_PREC_F64
+              ? gg::launch_transport<double>(c->scene<double>(), a, grid, c->block, smem, minb, c->stream)
+              : gg::launch_transport<float>(c->scene<float>(), a, grid, c->block, smem, minb, c->stream);
+      if ((st = c->cuda(e, "transport launch"))) return st;
+    }
     if ((st = c->cuda(cudaEventRecord(c->ev[3 * b + 2], c->stream), "event"))) return st;
     if (c->have_tally &&
         (st = c->cuda(gg::launch_flush(c->d_acc_e, a.acc_e2, c->d_edep, c->squared ? c->d_edep2 : nullptr,
@@ -595,11 +671,13 @@ static int run_impl(gg_ctx *c, uint64_t n, uint64_t seed, uint64_t first) {
   c->last_generate_ms = tg;
   c->last_transport_ms = tt;
   c->last_flush_ms = tf;
-  c->last_launches = (int)(3 * nb);
+  c->last_launches = (int)(nb + (c->have_spect ? (uint64_t)c->run_stage_launches : nb) + (c->have_tally ? nb : 0));
   unsigned int status = 0;
   if ((st = c->cuda(cudaMemcpy(&status, c->d_status, sizeof(status), cudaMemcpyDeviceToHost), "status"))) return st;
   if (status) {
     cudaMemset(c->d_status, 0, sizeof(unsigned int));
+    if (status & gg::kStatusQueueOverflow)
+      return c->fail(GG_ERR_QUEUE_OVERFLOW, "gg_run: a SPECT stage queue overflowed (photons were dropped)");
     return c->fail(GG_ERR_DOMAIN, "gg_run: source sampling failed (angular acceptance exhausted max_rejection)");
   }
   return GG_OK;
@@ -616,6 +694,14 @@ int gg_run(gg_ctx *c, uint64_t n, uint64_t seed, uint64_t first) {
     return c->fail(GG_ERR_STATE, "gg_run: tables, volume, world, source and tally must be set first");
   if (n == 0) return GG_OK;
   if (first + n < first) return c->fail(GG_ERR_ARG, "gg_run: history range overflows");
+  if (c->have_spect) {
+    // every history of this call belongs to the run of the last gg_spect_set_heads
+    c->run_base = c->spect_run;
+    c->run_first = first;
+    c->run_len = n;
+    int st = upload_frames(c);
+    if (st) return st;
+  }
   return run_impl(c, n, seed, first);
 }
 
@@ -684,27 +770,64 @@ int gg_spect_setup(gg_ctx *c, const gg_spect_desc *sp) {
     c->n_proj = n;
   }
   if ((st = c->cuda(cudaMemsetAsync(c->d_proj, 0, n * 8, c->stream), "memset projections"))) return st;
+  if ((st = c->cuda(cudaMemsetAsync(c->d_counters, 0, GG_N_COUNTERS * 8, c->stream), "memset counters"))) return st;
   c->spect = *sp;
   c->have_spect = true;
   c->spect_run = 0;
-  memset(c->frames, 0, sizeof(c->frames));
+  c->frames.assign((size_t)sp->n_runs * sp->n_heads * 12, 0.0);
+  c->frames_dirty = true;
   return c->cuda(cudaStreamSynchronize(c->stream), "spect setup");
+}
+
+static bool frames_valid(const double *frames, int n_heads) {
+  for (int h = 0; h < n_heads; ++h) {
+    const double *f = frames + 12 * h;
+    for (int v = 1; v < 4; ++v) {
+      double n2 = f[3 * v] * f[3 * v] + f[3 * v + 1] * f[3 * v + 1] + f[3 * v + 2] * f[3 * v + 2];
+      if (!(std::fabs(n2 - 1.0) <= 1e-6)) return false;
+    }
+  }
+  return true;
 }
 
 int gg_spect_set_heads(gg_ctx *c, int32_t run, const double *frames) {
   if (!c || !frames) return GG_ERR_ARG;
   if (!c->have_spect) return c->fail(GG_ERR_STATE, "gg_spect_set_heads: call gg_spect_setup first");
   if (run < 0 || run >= c->spect.n_runs) return c->fail(GG_ERR_ARG, "gg_spect_set_heads: run out of range");
-  for (int h = 0; h < c->spect.n_heads; ++h) {
-    const double *f = frames + 12 * h;
-    for (int v = 1; v < 4; ++v) {
-      double n2 = f[3 * v] * f[3 * v] + f[3 * v + 1] * f[3 * v + 1] + f[3 * v + 2] * f[3 * v + 2];
-      if (std::fabs(n2 - 1.0) > 1e-6) return c->fail(GG_ERR_ARG, "gg_spect_set_heads: axes must be unit vectors");
-    }
-    for (int a = 0; a < 12; ++a) c->frames[h][a] = f[a];
-  }
+  if (!frames_valid(frames, c->spect.n_heads))
+    return c->fail(GG_ERR_ARG, "gg_spect_set_heads: axes must be unit vectors");
+  std::copy(frames, frames + 12 * c->spect.n_heads, c->frames.begin() + (size_t)run * c->spect.n_heads * 12);
+  c->frames_dirty = true;
   c->spect_run = run;
   return GG_OK;
+}
+
+int gg_spect_run(gg_ctx *c, uint64_t n_per_run, uint64_t seed, uint64_t first, const double *frames) {
+  if (!c) return GG_ERR_ARG;
+  cudaSetDevice(c->device);
+  if (!c->have_spect) return c->fail(GG_ERR_STATE, "gg_spect_run: call gg_spect_setup first");
+  const gg_spect_desc &sp = c->spect;
+  if (frames) {
+    for (int r = 0; r < sp.n_runs; ++r)
+      if (!frames_valid(frames + (size_t)r * sp.n_heads * 12, sp.n_heads))
+        return c->fail(GG_ERR_ARG, "gg_spect_run: run %d: axes must be unit vectors", r);
+    std::copy(frames, frames + (size_t)sp.n_runs * sp.n_heads * 12, c->frames.begin());
+    c->frames_dirty = true;
+  }
+  if (!(c->src_emax < 2.0 * gg::kMC2))
+    return c->fail(GG_ERR_DOMAIN, "gg_spect_run: SPECT transport needs source energies below 1.022 MeV");
+  if (!c->have_tables || !c->have_volume || !c->have_world || !c->have_source)
+    return c->fail(GG_ERR_STATE, "gg_spect_run: tables, volume, world and source must be set first");
+  if (n_per_run == 0) return GG_OK;
+  const uint64_t n = n_per_run * (uint64_t)sp.n_runs;
+  if (n / (uint64_t)sp.n_runs != n_per_run || first + n < first)
+    return c->fail(GG_ERR_ARG, "gg_spect_run: history range overflows");
+  c->run_base = 0;
+  c->run_first = first;
+  c->run_len = n_per_run;
+  int st = upload_frames(c);
+  if (st) return st;
+  return run_impl(c, n, seed, first);
 }
 
 int gg_get_projection(gg_ctx *c, double *out, size_t n) {

@@ -383,8 +383,12 @@ struct Scene {
   real v_org[3], v_sp[3];
   const real *cdf_z, *cdf_y, *cdf_x;
   // SPECT heads and digitizer (spect = 0: dose path)
-  int spect, n_heads, n_win, pnx, pny, n_runs, run;
-  real hc[2][3], hu[2][3], he1[2][3], he2[2][3];
+  int spect, n_heads, n_win, pnx, pny, n_runs;
+  // head frames [n_runs][n_heads][12] (front-face centre, outward normal, e1,
+  // e2); history h belongs to run run_base + (h - run_first) / run_len
+  const real *frames;
+  uint64_t run_first, run_len;
+  int run_base;
   real half_w, zb[4], apo, px, py, hpx, hpy, inv_px, inv_py;
   int mat_coll, mat_cr;
   real wlo[8], whi[8], pix_half[2], inv_psp[2];
@@ -479,6 +483,7 @@ struct Photon {
   // SPECT: box not to re-enter before the next direction change (-1 none,
   // 0 image, 1 + h head h); head-local state while in_head
   int in_head, head, hreg, left_hole, exclude;
+  int run;  // SPECT gantry position of the history
 };
 
 template <typename real>

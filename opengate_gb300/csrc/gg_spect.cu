@@ -1,0 +1,627 @@
+// gg_spect.cu - SPECT acquisition as a two-stage wavefront.
+//
+// A SPECT history crosses three very different kinds of geometry: the
+// voxelised phantom (Woodcock steps and label gathers), the air of the world,
+// and the heads (collimator hole lattice, crystal and the digitizer event).
+// One kernel that carries all three keeps every warp's lanes spread over the
+// three code paths.  Here the work is split by where the photon is:
+//
+//   * phantom stage: source records (or photons handed back by the head
+//     stage) are tracked in the image and the world; a photon that reaches a
+//     head box is written, with its RNG position and event, to the head queue
+//     and its lane takes the next history;
+//   * head stage: queued photons are tracked through collimator, gap and
+//     crystal (and the world between the heads); the event is scored into the
+//     projection when the photon dies; a photon that flies back into the
+//     image is written to the return queue for another phantom pass.
+//
+// The host alternates the stages until the return queue stays empty.  Every
+// photon executes the same operations in the same order as in a single
+// kernel (the queues only change which lane runs them), so projections and
+// counters equal those of the CPU oracle bit for bit.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "gg_device.cuh"
+#include "gg_internal.h"
+#include "gg_physics.cuh"
+#include "gg_spect.cuh"
+
+namespace gg {
+
+// Photons handed between the stages, SoA.  meta: bits 0-19 steps taken,
+// bit 20 head, bits 21-22 head region, bit 23 event present, bits 24-26
+// exclude + 1.  ev: esum[2], emax[2], wpos[2][2] of the history's event.
+template <typename real>
+struct PQueue {
+  uint4 *rng_buf;
+  unsigned long long *hid;
+  real *px, *py, *pz, *dx, *dy, *dz, *e;
+  real *ev[8];
+  uint32_t *rng_pos, *meta;
+
+  __device__ __forceinline__ static PQueue carve(void *base, size_t cap) {
+    PQueue q;
+    unsigned char *p = reinterpret_cast<unsigned char *>(base);
+    q.rng_buf = reinterpret_cast<uint4 *>(p);
+    p += cap * sizeof(uint4);
+    q.hid = reinterpret_cast<unsigned long long *>(p);
+    p += cap * sizeof(unsigned long long);
+    real **f[7] = {&q.px, &q.py, &q.pz, &q.dx, &q.dy, &q.dz, &q.e};
+    for (int i = 0; i < 7; ++i) {
+      *f[i] = reinterpret_cast<real *>(p);
+      p += cap * sizeof(real);
+    }
+    for (int i = 0; i < 8; ++i) {
+      q.ev[i] = reinterpret_cast<real *>(p);
+      p += cap * sizeof(real);
+    }
+    q.rng_pos = reinterpret_cast<uint32_t *>(p);
+    p += cap * sizeof(uint32_t);
+    q.meta = reinterpret_cast<uint32_t *>(p);
+    return q;
+  }
+};
+
+template <typename real>
+size_t queue_bytes(size_t cap) {
+  return cap * (sizeof(uint4) + sizeof(unsigned long long) + 15 * sizeof(real) + 2 * sizeof(uint32_t));
+}
+
+constexpr uint32_t kMetaSteps = (1u << 20) - 1u;
+constexpr int kPush = 4;  // lane state: photon leaves this stage through the output queue
+
+// Tables of the block in shared memory (majorant, attenuation rows, label ->
+// composition / density), as in the dose transport kernel.
+template <typename real>
+__device__ __forceinline__ void stage_tables(const Scene<real> &sg, Scene<real> &s, unsigned char *smem_raw,
+                                             BlockCounters &bc) {
+  real *sh = reinterpret_cast<real *>(smem_raw);
+  const int nsig = sg.n_comp * sg.n_e;
+  real *ssig = sh;
+  real *smaj = ssig + nsig;
+  real *srho = smaj + sg.n_e;
+  int *scomp = reinterpret_cast<int *>(srho + sg.n_mat);
+  for (int i = threadIdx.x; i < nsig; i += blockDim.x) ssig[i] = sg.sig[i];
+  for (int i = threadIdx.x; i < sg.n_e; i += blockDim.x) smaj[i] = sg.maj[i];
+  for (int i = threadIdx.x; i < sg.n_mat; i += blockDim.x) {
+    srho[i] = sg.mat_rho[i];
+    scomp[i] = sg.mat_comp[i];
+  }
+  if (threadIdx.x == 0) bc = BlockCounters{0, 0, 0, 0, 0, 0, 0, 0};
+  __syncthreads();
+  s.sig = ssig;
+  s.maj = smaj;
+  s.mat_rho = srho;
+  s.mat_comp = scomp;
+}
+
+__device__ __forceinline__ void rng_resume(Rng &g, uint64_t seed, uint64_t hid, uint32_t rp, uint4 b) {
+  g.k0 = (uint32_t)seed;
+  g.k1 = (uint32_t)(seed >> 32);
+  g.stream = 0u;
+  g.h0 = (uint32_t)hid;
+  g.h1 = (uint32_t)(hid >> 32);
+  g.blk = rp >> 3;
+  g.idx = (int)(rp & 7u);
+  g.buf[0] = b.x;
+  g.buf[1] = b.y;
+  g.buf[2] = b.z;
+  g.buf[3] = b.w;
+}
+
+template <typename real>
+__device__ __forceinline__ int run_of(const Scene<real> &s, uint64_t hid) {
+  return s.run_base + (int)((hid - s.run_first) / s.run_len);
+}
+
+// Writes the lane's photon (and event) to slot k of the output queue.
+template <typename real>
+__device__ __forceinline__ void queue_put(const PQueue<real> &q, size_t k, const Photon<real> &ph, const Rng &g,
+                                          uint64_t hid, const real ev[8], bool has_ev) {
+  q.rng_buf[k] = make_uint4(g.buf[0], g.buf[1], g.buf[2], g.buf[3]);
+  q.rng_pos[k] = (g.blk << 3) | (uint32_t)g.idx;
+  q.hid[k] = hid;
+  q.px[k] = ph.pos[0];
+  q.py[k] = ph.pos[1];
+  q.pz[k] = ph.pos[2];
+  q.dx[k] = ph.dir[0];
+  q.dy[k] = ph.dir[1];
+  q.dz[k] = ph.dir[2];
+  q.e[k] = ph.e;
+  if (has_ev) {
+#pragma unroll
+    for (int i = 0; i < 8; ++i) q.ev[i][k] = ev[i];
+  }
+  q.meta[k] = ((uint32_t)ph.steps & kMetaSteps) | ((uint32_t)ph.head << 20) | ((uint32_t)ph.hreg << 21) |
+              ((has_ev ? 1u : 0u) << 23) | ((uint32_t)(ph.exclude + 1) << 24);
+}
+
+// Reads slot k of an input queue into the lane (photon state as it was when
+// it entered the queue: at a head-box entry in head-local coordinates, or at
+// an image-box entry in world coordinates).
+template <typename real>
+__device__ __forceinline__ uint64_t queue_get(const Scene<real> &s, const PQueue<real> &q, size_t k, Photon<real> &ph,
+                                              Rng &g, uint64_t seed, bool &has_ev) {
+  const uint64_t hid = q.hid[k];
+  rng_resume(g, seed, hid, q.rng_pos[k], q.rng_buf[k]);
+  ph.pos[0] = q.px[k];
+  ph.pos[1] = q.py[k];
+  ph.pos[2] = q.pz[k];
+  ph.dir[0] = q.dx[k];
+  ph.dir[1] = q.dy[k];
+  ph.dir[2] = q.dz[k];
+  set_energy(s, ph, q.e[k]);
+  const uint32_t m = q.meta[k];
+  ph.steps = (int)(m & kMetaSteps);
+  ph.head = (int)((m >> 20) & 1u);
+  ph.hreg = (int)((m >> 21) & 3u);
+  has_ev = ((m >> 23) & 1u) != 0u;
+  ph.exclude = (int)((m >> 24) & 7u) - 1;
+  ph.alive = 1;
+  ph.can_enter = 1;
+  ph.left_hole = 0;
+  ph.run = run_of(s, hid);
+  return hid;
+}
+
+// Phantom-stage flight: Woodcock step in the image or one world step; a photon
+// whose world step ends at a head-box entry leaves the stage (kPush).
+template <typename real>
+__device__ __forceinline__ int phantom_flight(const Scene<real> &s, Photon<real> &ph, Rng &g, BlockCounters *bc,
+                                              int &pmat, uint32_t &pv, int &pscored, unsigned int &n_wood,
+                                              unsigned int &n_real, unsigned int &n_world) {
+  if (++ph.steps > kStepCap) {
+    atomicAdd(&bc->loop_capped, 1u);
+    ph.alive = 0;
+    return kRefill;
+  }
+  if (ph.in_image) return image_flight(s, ph, g, pmat, pv, pscored, n_wood, n_real);
+  ++n_world;
+  if (spect_world_flight(s, ph, g)) {
+    pmat = s.world_mat;
+    pscored = 0;
+    return kInteract;
+  }
+  if (!ph.alive) {
+    atomicAdd(&bc->escaped, 1u);
+    return kRefill;
+  }
+  return ph.in_head ? kPush : kFly;
+}
+
+// Head-stage flight: one step in a head, or one world step; a photon whose
+// world step ends at the image-box entry leaves the stage (kPush).
+template <typename real>
+__device__ __forceinline__ int head_stage_flight(const Scene<real> &s, Photon<real> &ph, Rng &g, BlockCounters *bc,
+                                                 int &pmat, int &pscored, unsigned int &n_world,
+                                                 unsigned int &n_head) {
+  if (++ph.steps > kStepCap) {
+    atomicAdd(&bc->loop_capped, 1u);
+    ph.alive = 0;
+    return kRefill;
+  }
+  if (ph.in_head) {
+    ++n_head;
+    int mat;
+    if (head_flight(s, ph, g, mat)) {
+      pmat = mat;
+      pscored = ph.hreg == 2 ? 2 : 3;
+      return kInteract;
+    }
+    return kFly;
+  }
+  ++n_world;
+  if (spect_world_flight(s, ph, g)) {
+    pmat = s.world_mat;
+    pscored = 0;
+    return kInteract;
+  }
+  if (!ph.alive) {
+    atomicAdd(&bc->escaped, 1u);
+    return kRefill;
+  }
+  return ph.in_image ? kPush : kFly;
+}
+
+// Per-warp slot allocation in an output queue for the lanes with `push` set;
+// returns the lane's slot (meaningful only where push is set).
+__device__ __forceinline__ size_t queue_claim(unsigned long long *count, bool push, unsigned lane, unsigned lt_mask) {
+  const unsigned m = __ballot_sync(0xffffffffu, push);
+  unsigned long long base = 0;
+  if (m) {
+    if (lane == (unsigned)(__ffs(m) - 1)) base = atomicAdd(count, (unsigned long long)__popc(m));
+    base = __shfl_sync(0xffffffffu, base, __ffs(m) - 1);
+  }
+  return (size_t)(base + __popc(m & lt_mask));
+}
+
+template <typename real>
+__device__ __forceinline__ void load_event(const PQueue<real> &q, size_t k, real ev[8]) {
+#pragma unroll
+  for (int i = 0; i < 8; ++i) ev[i] = q.ev[i][k];
+}
+
+template <typename real>
+__device__ __forceinline__ void event_from(const real v[8], Event<real> &ev) {
+  ev.esum[0] = v[0];
+  ev.esum[1] = v[1];
+  ev.emax[0] = v[2];
+  ev.emax[1] = v[3];
+  ev.wpos[0][0] = v[4];
+  ev.wpos[0][1] = v[5];
+  ev.wpos[1][0] = v[6];
+  ev.wpos[1][1] = v[7];
+}
+
+template <typename real>
+__device__ __forceinline__ void event_to(const Event<real> &ev, real v[8]) {
+  v[0] = ev.esum[0];
+  v[1] = ev.esum[1];
+  v[2] = ev.emax[0];
+  v[3] = ev.emax[1];
+  v[4] = ev.wpos[0][0];
+  v[5] = ev.wpos[0][1];
+  v[6] = ev.wpos[1][0];
+  v[7] = ev.wpos[1][1];
+}
+
+// Block counters and per-lane step counts into the global counters.
+__device__ __forceinline__ void stage_counters(unsigned long long *cnt, const BlockCounters &bc, unsigned lane,
+                                               unsigned int n_wood, unsigned int n_real, unsigned int n_world,
+                                               unsigned int n_head, unsigned int n_singles) {
+  auto warp_add = [&](unsigned int v, int slot) {
+    unsigned long long x = v;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+    if (lane == 0 && x) atomicAdd(&cnt[slot], x);
+  };
+  warp_add(n_wood, GG_CNT_WOODCOCK_STEPS);
+  warp_add(n_real, GG_CNT_REAL_INTERACTIONS);
+  warp_add(n_world, GG_CNT_WORLD_STEPS);
+  warp_add(n_head, GG_CNT_HEAD_STEPS);
+  warp_add(n_singles, GG_CNT_SINGLES);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    if (bc.escaped) atomicAdd(&cnt[GG_CNT_ESCAPED], (unsigned long long)bc.escaped);
+    if (bc.loop_capped) atomicAdd(&cnt[GG_CNT_LOOP_CAPPED], (unsigned long long)bc.loop_capped);
+    if (bc.stack_overflow) atomicAdd(&cnt[GG_CNT_STACK_OVERFLOW], (unsigned long long)bc.stack_overflow);
+    if (bc.secondaries) atomicAdd(&cnt[GG_CNT_SECONDARIES], (unsigned long long)bc.secondaries);
+    if (bc.list_overflows) atomicAdd(&cnt[GG_CNT_LIST_OVERFLOWS], (unsigned long long)bc.list_overflows);
+  }
+}
+
+// Phantom stage.  Input: the batch's primary records (q.in_q == null) or the
+// return queue; output: the head queue.  Persistent grid with the
+// phase-batched lane loop of the dose transport kernel (refill / fly /
+// interact, one phase per warp iteration).
+template <typename real, int MINB>
+__global__ void __launch_bounds__(256, MINB) k_spect_phantom(Scene<real> sg, KernelArgs args, StageArgs q) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ BlockCounters bc;
+  __shared__ real sec_store[6 * 256];
+  Scene<real> s = sg;
+  stage_tables(sg, s, smem_raw, bc);
+  const bool from_queue = q.in_q != nullptr;
+  const Records<real> rec = Records<real>::carve(args.records, args.rec_cap);
+  PQueue<real> in{};
+  if (from_queue) in = PQueue<real>::carve(q.in_q, q.q_cap);
+  const PQueue<real> out = PQueue<real>::carve(q.out_q, q.q_cap);
+  // a queue length above the capacity means entries were dropped (status
+  // GG_ERR_QUEUE_OVERFLOW): never read past the capacity
+  const uint64_t n_items = from_queue ? min((uint64_t)*q.in_n, (uint64_t)q.q_cap) : args.h_end - args.h_begin;
+  const unsigned lane = threadIdx.x & 31u;
+  const unsigned lt_mask = (1u << lane) - 1u;
+  uint64_t pool_next = 0, pool_end = 0;
+
+  Photon<real> ph;
+  ph.alive = 0;
+  ph.in_head = 0;
+  ph.head = 0;
+  ph.hreg = 0;
+  Secondary<real> sec;
+  sec.base = sec_store;
+  sec.stride = blockDim.x;
+  sec.tid = threadIdx.x;
+  sec.has = 0;
+  HistList<real> l;
+  l.n = 0;
+  Tally<real> t{nullptr, nullptr};
+  Event<real> ev_unused;
+  Rng g;
+  int state = kRefill;
+  bool in_hist = false, has_ev = false;
+  uint64_t hid = 0, slot = 0;
+  int pmat = 0, pscored = 0;
+  uint32_t pv = 0;
+  unsigned int n_wood = 0, n_real = 0, n_dep = 0, n_world = 0, n_singles = 0;
+
+  for (;;) {
+    const unsigned m_ref = __ballot_sync(0xffffffffu, state == kRefill);
+    const unsigned m_fly = __ballot_sync(0xffffffffu, state == kFly);
+    const unsigned m_int = __ballot_sync(0xffffffffu, state == kInteract);
+    if ((m_ref | m_fly | m_int) == 0u) break;
+    int phase;
+    if (__popc(m_ref) >= args.refill_min || (m_fly | m_int) == 0u) phase = kRefill;
+    else if (__popc(m_int) >= args.interact_min || m_fly == 0u) phase = kInteract;
+    else phase = kFly;
+
+    if (phase == kRefill) {
+      const bool need = state == kRefill;
+      if (need && in_hist && has_ev) {
+        // a photon that came back from a head died here: score its event
+        Event<real> ev;
+        real v[8];
+        load_event(in, slot, v);
+        event_from(v, ev);
+        n_singles += score_singles(s, ev, ph.run);
+      }
+      if (need) in_hist = false;
+      const unsigned n_need = __popc(m_ref);
+      const unsigned rank = __popc(m_ref & lt_mask);
+      const uint64_t avail = pool_end - pool_next;
+      uint64_t h;
+      if (avail >= n_need) {
+        h = pool_next + rank;
+        pool_next += n_need;
+      } else {
+        unsigned long long base = 0;
+        if (lane == 0) base = atomicAdd(args.next, (unsigned long long)args.chunk);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        h = rank < avail ? pool_next + rank : base + (rank - avail);
+        pool_next = base + (n_need - avail);
+        pool_end = base + (uint64_t)args.chunk;
+      }
+      if (need) {
+        if (h >= n_items) {
+          state = kDone;
+        } else if (from_queue) {
+          hid = queue_get(s, in, h, ph, g, args.seed, has_ev);
+          slot = h;
+          ph.in_head = 0;
+          ph.in_image = 1;
+          ph.t_exit = exit_distance(ph.pos, ph.dir, s.bmin, s.bmax);
+          state = kFly;
+          in_hist = true;
+        } else {
+          const uint32_t f = rec.flags[h];
+          const uint32_t rs = f & 3u;
+          if (rs != kRecDead) {
+            ph.pos[0] = rec.px[h];
+            ph.pos[1] = rec.py[h];
+            ph.pos[2] = rec.pz[h];
+            ph.dir[0] = rec.dx[h];
+            ph.dir[1] = rec.dy[h];
+            ph.dir[2] = rec.dz[h];
+            set_energy(s, ph, rec.e[h]);
+            ph.steps = (int)((f >> 2) & 1u);
+            ph.alive = 1;
+            ph.can_enter = 1;
+            ph.in_head = 0;
+            ph.exclude = -1;
+            hid = args.h_begin + h;
+            ph.run = run_of(s, hid);
+            has_ev = false;
+            rng_resume(g, args.seed, hid, rec.rng_pos[h], rec.rng_buf[h]);
+            if (rs == kRecInImage) {
+              ph.in_image = 1;
+              ph.t_exit = exit_distance(ph.pos, ph.dir, s.bmin, s.bmax);
+              state = kFly;
+            } else if (rs == kRecWorld) {
+              ph.in_image = 0;
+              state = kFly;
+            } else {
+              ph.in_image = 0;
+              pmat = s.world_mat;
+              pscored = 0;
+              state = kInteract;
+            }
+            in_hist = true;
+          }
+        }
+      }
+    } else if (phase == kInteract) {
+      if (state == kInteract) {
+        state = do_interaction<real, true>(s, ph, g, &bc, pmat, pv, pscored, l, t, sec, n_dep, ev_unused);
+        if (state == kRefill && sec.has) {
+          pop_secondary(s, ph, sec);
+          state = kFly;
+        }
+      }
+    } else {
+      if (state == kFly) {
+        state = phantom_flight(s, ph, g, &bc, pmat, pv, pscored, n_wood, n_real, n_world);
+        if (state == kRefill && sec.has) {
+          pop_secondary(s, ph, sec);
+          state = kFly;
+        }
+      }
+      const bool push = state == kPush;
+      const size_t k = queue_claim(q.out_n, push, lane, lt_mask);
+      if (push) {
+        if (k < q.q_cap) {
+          real v[8];
+          if (has_ev) load_event(in, slot, v);
+          queue_put(out, k, ph, g, hid, v, has_ev);
+        } else {
+          atomicOr(args.status, kStatusQueueOverflow);
+        }
+        in_hist = false;
+        state = kRefill;
+      }
+    }
+  }
+  stage_counters(args.counters, bc, lane, n_wood, n_real, n_world, 0u, n_singles);
+}
+
+// Head stage.  Input: the head queue; output: the return queue.  Each lane
+// carries its photon's event in registers and scores it when the photon
+// dies.
+template <typename real, int MINB>
+__global__ void __launch_bounds__(256, MINB) k_spect_head(Scene<real> sg, KernelArgs args, StageArgs q) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ BlockCounters bc;
+  __shared__ real sec_store[6 * 256];
+  Scene<real> s = sg;
+  stage_tables(sg, s, smem_raw, bc);
+  const PQueue<real> in = PQueue<real>::carve(q.in_q, q.q_cap);
+  const PQueue<real> out = PQueue<real>::carve(q.out_q, q.q_cap);
+  const uint64_t n_items = min((uint64_t)*q.in_n, (uint64_t)q.q_cap);
+  const unsigned lane = threadIdx.x & 31u;
+  const unsigned lt_mask = (1u << lane) - 1u;
+  uint64_t pool_next = 0, pool_end = 0;
+
+  Photon<real> ph;
+  ph.alive = 0;
+  ph.run = 0;
+  Secondary<real> sec;
+  sec.base = sec_store;
+  sec.stride = blockDim.x;
+  sec.tid = threadIdx.x;
+  sec.has = 0;
+  HistList<real> l;
+  l.n = 0;
+  Tally<real> t{nullptr, nullptr};
+  Event<real> ev;
+  ev.clear();
+  Rng g;
+  int state = kRefill;
+  bool in_hist = false;
+  uint64_t hid = 0;
+  int pmat = 0, pscored = 0;
+  uint32_t pv = 0;
+  unsigned int n_dep = 0, n_world = 0, n_head = 0, n_singles = 0;
+
+  for (;;) {
+    const unsigned m_ref = __ballot_sync(0xffffffffu, state == kRefill);
+    const unsigned m_fly = __ballot_sync(0xffffffffu, state == kFly);
+    const unsigned m_int = __ballot_sync(0xffffffffu, state == kInteract);
+    if ((m_ref | m_fly | m_int) == 0u) break;
+    int phase;
+    if (__popc(m_ref) >= args.refill_min || (m_fly | m_int) == 0u) phase = kRefill;
+    else if (__popc(m_int) >= args.interact_min || m_fly == 0u) phase = kInteract;
+    else phase = kFly;
+
+    if (phase == kRefill) {
+      const bool need = state == kRefill;
+      if (need && in_hist) {
+        n_singles += score_singles(s, ev, ph.run);
+        in_hist = false;
+      }
+      const unsigned n_need = __popc(m_ref);
+      const unsigned rank = __popc(m_ref & lt_mask);
+      const uint64_t avail = pool_end - pool_next;
+      uint64_t h;
+      if (avail >= n_need) {
+        h = pool_next + rank;
+        pool_next += n_need;
+      } else {
+        unsigned long long base = 0;
+        if (lane == 0) base = atomicAdd(args.next, (unsigned long long)args.chunk);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        h = rank < avail ? pool_next + rank : base + (rank - avail);
+        pool_next = base + (n_need - avail);
+        pool_end = base + (uint64_t)args.chunk;
+      }
+      if (need) {
+        if (h >= n_items) {
+          state = kDone;
+        } else {
+          bool has_ev;
+          hid = queue_get(s, in, h, ph, g, args.seed, has_ev);
+          if (has_ev) {
+            real v[8];
+            load_event(in, h, v);
+            event_from(v, ev);
+          } else {
+            ev.clear();
+          }
+          ph.in_head = 1;
+          ph.in_image = 0;
+          state = kFly;
+          in_hist = true;
+        }
+      }
+    } else if (phase == kInteract) {
+      if (state == kInteract) {
+        state = do_interaction<real, true>(s, ph, g, &bc, pmat, pv, pscored, l, t, sec, n_dep, ev);
+        if (state == kRefill && sec.has) {
+          pop_secondary(s, ph, sec);
+          state = kFly;
+        }
+      }
+    } else {
+      if (state == kFly) {
+        state = head_stage_flight(s, ph, g, &bc, pmat, pscored, n_world, n_head);
+        if (state == kRefill && sec.has) {
+          pop_secondary(s, ph, sec);
+          state = kFly;
+        }
+      }
+      const bool push = state == kPush;
+      const size_t k = queue_claim(q.out_n, push, lane, lt_mask);
+      if (push) {
+        if (k < q.q_cap) {
+          real v[8];
+          event_to(ev, v);
+          queue_put(out, k, ph, g, hid, v, true);
+        } else {
+          atomicOr(args.status, kStatusQueueOverflow);
+        }
+        in_hist = false;
+        state = kRefill;
+      }
+    }
+  }
+  stage_counters(args.counters, bc, lane, 0u, 0u, n_world, n_head, n_singles);
+}
+
+template <typename real, int MINB>
+static cudaError_t launch_stage_v(int stage, const Scene<real> &s, const KernelArgs &a, const StageArgs &q, int grid,
+                                  int block, size_t smem, cudaStream_t st) {
+  static bool configured[2] = {false, false};
+  if (!configured[stage]) {
+    cudaError_t e = stage == 0 ? cudaFuncSetAttribute(k_spect_phantom<real, MINB>,
+                                                      cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024)
+                               : cudaFuncSetAttribute(k_spect_head<real, MINB>,
+                                                      cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    if (e != cudaSuccess) return e;
+    configured[stage] = true;
+  }
+  if (stage == 0) k_spect_phantom<real, MINB><<<grid, block, smem, st>>>(s, a, q);
+  else k_spect_head<real, MINB><<<grid, block, smem, st>>>(s, a, q);
+  return cudaGetLastError();
+}
+
+template <typename real>
+cudaError_t launch_spect_stage(int stage, const Scene<real> &s, const KernelArgs &a, const StageArgs &q, int grid,
+                               int block, size_t smem, int minb, cudaStream_t st) {
+  if (minb <= 2) return launch_stage_v<real, 2>(stage, s, a, q, grid, block, smem, st);
+  if (minb == 3) return launch_stage_v<real, 3>(stage, s, a, q, grid, block, smem, st);
+  return launch_stage_v<real, 4>(stage, s, a, q, grid, block, smem, st);
+}
+
+template <typename real, int MINB>
+static cudaError_t stage_occupancy_v(int stage, int block, size_t smem, int *bps) {
+  return stage == 0 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(bps, k_spect_phantom<real, MINB>, block, smem)
+                    : cudaOccupancyMaxActiveBlocksPerMultiprocessor(bps, k_spect_head<real, MINB>, block, smem);
+}
+
+template <typename real>
+cudaError_t spect_stage_occupancy(int stage, int block, size_t smem, int minb, int *blocks_per_sm) {
+  if (minb <= 2) return stage_occupancy_v<real, 2>(stage, block, smem, blocks_per_sm);
+  if (minb == 3) return stage_occupancy_v<real, 3>(stage, block, smem, blocks_per_sm);
+  return stage_occupancy_v<real, 4>(stage, block, smem, blocks_per_sm);
+}
+
+template size_t queue_bytes<float>(size_t);
+template size_t queue_bytes<double>(size_t);
+template cudaError_t launch_spect_stage<float>(int, const Scene<float> &, const KernelArgs &, const StageArgs &, int,
+                                               int, size_t, int, cudaStream_t);
+template cudaError_t launch_spect_stage<double>(int, const Scene<double> &, const KernelArgs &, const StageArgs &,
+                                                int, int, size_t, int, cudaStream_t);
+template cudaError_t spect_stage_occupancy<float>(int, int, size_t, int, int *);
+template cudaError_t spect_stage_occupancy<double>(int, int, size_t, int, int *);
+
+}  // namespace gg

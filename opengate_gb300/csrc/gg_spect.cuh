@@ -28,32 +28,53 @@ __device__ __forceinline__ real dot3(const real a[3], const real b[3]) {
   return r;
 }
 
+// Frame of head h at gantry position `run`: 12 values c[3], u[3], e1[3], e2[3]
+// loaded from the read-only frame table.
 template <typename real>
-__device__ __forceinline__ void to_local(const Scene<real> &s, int h, const real p[3], const real d[3], real lp[3],
-                                         real ld[3]) {
-  real q[3];
+struct HeadFrame {
+  real c[3], u[3], e1[3], e2[3];
+};
+
+template <typename real>
+__device__ __forceinline__ HeadFrame<real> head_frame(const Scene<real> &s, int run, int h) {
+  const real *f = s.frames + ((size_t)run * s.n_heads + h) * 12;
+  HeadFrame<real> r;
 #pragma unroll
-  for (int a = 0; a < 3; ++a) q[a] = p[a] - s.hc[h][a];
-  lp[0] = dot3(q, s.he1[h]);
-  lp[1] = dot3(q, s.he2[h]);
-  lp[2] = dot3(q, s.hu[h]);
-  ld[0] = dot3(d, s.he1[h]);
-  ld[1] = dot3(d, s.he2[h]);
-  ld[2] = dot3(d, s.hu[h]);
+  for (int a = 0; a < 3; ++a) {
+    r.c[a] = __ldg(f + a);
+    r.u[a] = __ldg(f + 3 + a);
+    r.e1[a] = __ldg(f + 6 + a);
+    r.e2[a] = __ldg(f + 9 + a);
+  }
+  return r;
 }
 
 template <typename real>
-__device__ __forceinline__ void to_world(const Scene<real> &s, int h, const real lp[3], const real ld[3], real p[3],
+__device__ __forceinline__ void to_local(const HeadFrame<real> &f, const real p[3], const real d[3], real lp[3],
+                                         real ld[3]) {
+  real q[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) q[a] = p[a] - f.c[a];
+  lp[0] = dot3(q, f.e1);
+  lp[1] = dot3(q, f.e2);
+  lp[2] = dot3(q, f.u);
+  ld[0] = dot3(d, f.e1);
+  ld[1] = dot3(d, f.e2);
+  ld[2] = dot3(d, f.u);
+}
+
+template <typename real>
+__device__ __forceinline__ void to_world(const HeadFrame<real> &f, const real lp[3], const real ld[3], real p[3],
                                          real d[3]) {
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
-    real x = lp[0] * s.he1[h][a];
-    x = s.hc[h][a] + x;
-    x = x + lp[1] * s.he2[h][a];
-    p[a] = x + lp[2] * s.hu[h][a];
-    real y = ld[0] * s.he1[h][a];
-    y = y + ld[1] * s.he2[h][a];
-    d[a] = y + ld[2] * s.hu[h][a];
+    real x = lp[0] * f.e1[a];
+    x = f.c[a] + x;
+    x = x + lp[1] * f.e2[a];
+    p[a] = x + lp[2] * f.u[a];
+    real y = ld[0] * f.e1[a];
+    y = y + ld[1] * f.e2[a];
+    d[a] = y + ld[2] * f.u[a];
   }
 }
 
@@ -120,16 +141,17 @@ __device__ __forceinline__ void move3(real p[3], const real d[3], real t) {
   for (int a = 0; a < 3; ++a) p[a] = p[a] + t * d[a];
 }
 
-// per-event crystal accumulation of each head
+// per-event crystal accumulation of each head; wpos = head-local (a1, a2) of
+// the energy winner, which is also its position on the detector plane
 template <typename real>
 struct Event {
-  real esum[2], emax[2], wpos[2][3];
+  real esum[2], emax[2], wpos[2][2];
   __device__ __forceinline__ void clear() {
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
       esum[h] = R<real>(0);
       emax[h] = R<real>(0);
-      wpos[h][0] = wpos[h][1] = wpos[h][2] = R<real>(0);
+      wpos[h][0] = wpos[h][1] = R<real>(0);
     }
   }
 };
@@ -138,7 +160,7 @@ template <typename real>
 __device__ __forceinline__ void head_cross(const Scene<real> &s, Photon<real> &ph, bool leave) {
   if (leave) {
     real p[3], d[3];
-    to_world(s, ph.head, ph.pos, ph.dir, p, d);
+    to_world(head_frame(s, ph.run, ph.head), ph.pos, ph.dir, p, d);
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
       ph.pos[a] = p[a];
@@ -163,11 +185,15 @@ __device__ __forceinline__ int head_flight(const Scene<real> &s, Photon<real> &p
   real hi[3] = {s.half_w, s.half_w, s.zb[3]};
   real tbox = exit_distance(l, d, lo, hi);
   real treg = gg_inf(real(0));
+  // region bounds zb[hreg] (below) and zb[hreg + 1] (above), selected without
+  // indexing the scene (an indexed access would move it to local memory)
+  const real zlo = ph.hreg == 0 ? s.zb[0] : (ph.hreg == 1 ? s.zb[1] : s.zb[2]);
+  const real zhi = ph.hreg == 0 ? s.zb[1] : (ph.hreg == 1 ? s.zb[2] : s.zb[3]);
   if (d[2] > R<real>(0)) {
-    treg = s.zb[ph.hreg + 1] - l[2];
+    treg = zhi - l[2];
     treg = treg / d[2];
   } else if (d[2] < R<real>(0)) {
-    treg = s.zb[ph.hreg] - l[2];
+    treg = zlo - l[2];
     treg = treg / d[2];
   }
   if (treg < R<real>(0)) treg = R<real>(0);
@@ -225,7 +251,7 @@ __device__ __forceinline__ int spect_world_flight(const Scene<real> &s, Photon<r
   for (int h = 0; h < s.n_heads; ++h) {
     if (ph.exclude == 1 + h) continue;
     real lp[3], ld[3];
-    to_local(s, h, ph.pos, ph.dir, lp, ld);
+    to_local(head_frame(s, ph.run, h), ph.pos, ph.dir, lp, ld);
     real th = entry_distance(lp, ld, hlo, hhi);
     if (th < tb) {
       tb = th;
@@ -252,7 +278,7 @@ __device__ __forceinline__ int spect_world_flight(const Scene<real> &s, Photon<r
     } else {
       int h = box - 1;
       real lp[3], ld[3];
-      to_local(s, h, ph.pos, ph.dir, lp, ld);
+      to_local(head_frame(s, ph.run, h), ph.pos, ph.dir, lp, ld);
 #pragma unroll
       for (int a = 0; a < 3; ++a) {
         ph.pos[a] = lp[a];
@@ -271,7 +297,7 @@ __device__ __forceinline__ int spect_world_flight(const Scene<real> &s, Photon<r
 
 // Singles of one event: windows and projection pixel per head.
 template <typename real>
-__device__ __forceinline__ unsigned score_singles(const Scene<real> &s, const Event<real> &ev) {
+__device__ __forceinline__ unsigned score_singles(const Scene<real> &s, const Event<real> &ev, int run) {
   unsigned n_singles = 0;
 #pragma unroll
   for (int h = 0; h < 2; ++h) {
@@ -279,20 +305,16 @@ __device__ __forceinline__ unsigned score_singles(const Scene<real> &s, const Ev
     real e = ev.esum[h];
     if (!(e > R<real>(0))) continue;
     ++n_singles;
-    real q[3];
-#pragma unroll
-    for (int a = 0; a < 3; ++a) q[a] = ev.wpos[h][a] - s.hc[h][a];
-    real fx = dot3(q, s.he1[h]);
-    fx = fx + s.pix_half[0];
+    real fx = ev.wpos[h][0] + s.pix_half[0];
     fx = fx * s.inv_psp[0];
-    real fy = dot3(q, s.he2[h]);
-    fy = fy + s.pix_half[1];
+    real fy = ev.wpos[h][1] + s.pix_half[1];
     fy = fy * s.inv_psp[1];
     if (!(fx >= R<real>(0) && fx < (real)s.pnx && fy >= R<real>(0) && fy < (real)s.pny)) continue;
     int i = (int)fx, j = (int)fy;
-    for (int k = 0; k < s.n_win; ++k) {
-      if (e >= s.wlo[k] && e < s.whi[k]) {
-        size_t idx = ((((size_t)h * s.n_runs + s.run) * s.n_win + k) * s.pny + j) * s.pnx + i;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      if (k < s.n_win && e >= s.wlo[k] && e < s.whi[k]) {
+        size_t idx = ((((size_t)h * s.n_runs + run) * s.n_win + k) * s.pny + j) * s.pnx + i;
         atomicAdd(s.proj + idx, 1ull);
       }
     }

@@ -117,6 +117,14 @@ class SpectEngine(DoseEngine):
         self._call("gg_spect_setup", ctypes.byref(self._desc))
 
     def run(self, n_per_run, seed, first=0):
+        """All gantry positions in one gg_spect_run call (one set of launches)."""
+        frames = self.spect.all_frames()
+        self._call("gg_spect_run", ctypes.c_uint64(n_per_run), ctypes.c_uint64(seed), ctypes.c_uint64(first),
+                   C.ptr(frames, ctypes.c_double))
+        self.kernel_ms = list(super().last_kernel_ms())
+
+    def run_per_angle(self, n_per_run, seed, first=0):
+        """Same histories as run(), one gg_spect_set_heads + gg_run per gantry position."""
         self.kernel_ms = [0.0, 0.0, 0.0, 0]
         for r in range(self.spect.n_runs):
             frames = np.ascontiguousarray(self.spect.frames(r), dtype=np.float64)

@@ -172,6 +172,10 @@ class Scene:
         self.source = source
         self._build_descs()
 
+    def source_desc_bytes(self):
+        """Bytes of the source arrays a gg_set_source call copies to the device."""
+        return int(self._acc.nbytes + self._spec_e.nbytes + self._spec_cdf.nbytes + sum(c.nbytes for c in self._cdfs))
+
     @property
     def n_voxels(self):
         return int(self.labels.size)

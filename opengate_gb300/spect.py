@@ -126,3 +126,50 @@ def voxel_cdfs(activity):
     cdf_z = np.cumsum(sumxy) / np.sum(sumxy)
     return (np.ascontiguousarray(cdf_z, np.float32), np.ascontiguousarray(cdf_y, np.float32),
             np.ascontiguousarray(cdf_x, np.float32))
+
+
+# ---------------------------------------------------------------------------
+# projection noise and efficiency (contrib/spect/spect_helpers.py:374-387, 480-536, 582-591)
+def compute_poisson_relative_uncertainty(counts):
+    """sqrt(counts) / counts, 0 where counts == 0."""
+    c = np.asarray(counts, dtype=np.float64)
+    return np.divide(np.sqrt(c), c, out=np.zeros_like(c), where=c != 0)
+
+
+def compute_history_by_history_relative_uncertainty(img, img_squared, n):
+    """sqrt((sum x^2 / n - (sum x / n)^2) / (n - 1)) / (sum x / n), 0 where the mean is 0."""
+    mean = np.asarray(img, dtype=np.float64) / n
+    variance = (np.asarray(img_squared, dtype=np.float64) / n - mean * mean) / (n - 1)
+    return np.divide(np.sqrt(variance), mean, out=np.zeros_like(variance), where=mean != 0)
+
+
+def compute_efficiency(uncert, duration):
+    """1 / (sigma^2 * T), 0 where sigma == 0."""
+    u = np.asarray(uncert, dtype=np.float64)
+    return np.divide(np.ones_like(u), u * u * duration, out=np.zeros_like(u), where=u != 0)
+
+
+def compute_zscore(ref_counts, test_counts, var_ref, var_test):
+    """(test - ref) / sqrt(var_ref + var_test) where both counts are non-zero."""
+    ref = np.asarray(ref_counts, dtype=np.float64)
+    test = np.asarray(test_counts, dtype=np.float64)
+    both = (ref != 0) & (test != 0)
+    return np.divide(test - ref, np.sqrt(np.asarray(var_ref) + np.asarray(var_test)), out=np.zeros_like(ref),
+                     where=both)
+
+
+def compute_speedup(ref_uncert, test_uncert, ref_duration, test_duration):
+    """Efficiency ratio eff(test) / eff(ref), 0 where eff(ref) == 0."""
+    e_ref = compute_efficiency(ref_uncert, ref_duration)
+    e_test = compute_efficiency(test_uncert, test_duration)
+    return np.divide(e_test, e_ref, out=np.zeros_like(e_test), where=e_ref != 0)
+
+
+def mean_relative_uncertainty(counts, counts_squared, n, frac=0.1):
+    """Mean history-by-history relative sigma over pixels above frac * max counts."""
+    c = np.asarray(counts, dtype=np.float64)
+    if not c.any():
+        return None
+    rel = compute_history_by_history_relative_uncertainty(c, counts_squared, n)
+    sel = c > frac * c.max()
+    return float(rel[sel].mean())

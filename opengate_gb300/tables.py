@@ -65,8 +65,11 @@ class CompositionTable:
             c0 = np.where(tot > 0, parts["compton"] / tot, 1.0)
             c1 = np.where(tot > 0, (parts["compton"] + parts["photo"]) / tot, 1.0)
             c2 = np.where(tot > 0, (parts["compton"] + parts["photo"] + parts["rayleigh"]) / tot, 1.0)
-        # pair fraction exactly zero below threshold
+        # pair fraction exactly zero below threshold, and at the first grid
+        # node above it, so that the linear interpolation inside the interval
+        # that straddles 2 m_e c^2 cannot select a pair conversion below it
         below = energy_grid() <= 2.0 * xsection.ELECTRON_MASS_MEV
+        below[1:] |= below[:-1]
         c2 = np.where(below, 1.0, c2)
         self.cum = np.stack([c0, c1, c2])
         # Rayleigh sampling tables: the cumulative of F^2 dx^2, piecewise linear in

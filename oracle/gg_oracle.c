@@ -503,8 +503,8 @@ static uint64_t to_fixed(real v) {
 }
 
 /* q = to_fixed(history's voxel sum) goes to acc_e[v]; q^2 (units 2^-64 MeV^2)
-   goes to the 128-bit pair acc_e2[2v] (low) / acc_e2[2v+1] (high), with the
-   carry out of the low word added to the high word. */
+   is split into its low 32 bits, added to acc_e2[2v], and q^2 >> 32 (units
+   2^-32 MeV^2), added to acc_e2[2v+1]; sum = acc_e2[2v+1] 2^-32 + acc_e2[2v] 2^-64. */
 static void hlist_flush(hlist_t *l, tally_t *t) {
   for (int k = 0; k < l->n; ++k) {
     uint64_t q = to_fixed(l->acc[k]);
@@ -512,10 +512,8 @@ static void hlist_flush(hlist_t *l, tally_t *t) {
     __atomic_fetch_add(&t->acc_e[v], q, __ATOMIC_RELAXED);
     if (t->acc_e2) {
       unsigned __int128 sq = (unsigned __int128)q * q;
-      uint64_t lo = (uint64_t)sq, hi = (uint64_t)(sq >> 64);
-      uint64_t old = __atomic_fetch_add(&t->acc_e2[2 * v], lo, __ATOMIC_RELAXED);
-      hi += (old + lo < old) ? 1u : 0u;
-      if (hi) __atomic_fetch_add(&t->acc_e2[2 * v + 1], hi, __ATOMIC_RELAXED);
+      __atomic_fetch_add(&t->acc_e2[2 * v], (uint64_t)sq & 0xffffffffu, __ATOMIC_RELAXED);
+      __atomic_fetch_add(&t->acc_e2[2 * v + 1], (uint64_t)(sq >> 32), __ATOMIC_RELAXED);
     }
   }
   t->cnt[GG_CNT_TALLY_ENTRIES] += (uint64_t)l->n;
@@ -552,9 +550,10 @@ typedef struct {
   int in_head, head, hreg, left_hole, exclude;
 } photon_t;
 
-/* per-event crystal accumulation of each head (adder, EnergyWinnerPosition) */
+/* per-event crystal accumulation of each head (adder, EnergyWinnerPosition);
+   wpos = head-local (a1, a2) of the energy winner */
 typedef struct {
-  real esum[2], emax[2], wpos[2][3];
+  real esum[2], emax[2], wpos[2][2];
 } event_t;
 
 static void set_energy(const scene_t *s, photon_t *ph, real e) {
@@ -1077,10 +1076,9 @@ static void head_step(const scene_t *s, photon_t *ph, rng_t *g, tally_t *t, even
     int h = ph->head;
     ev->esum[h] = ev->esum[h] + ed;
     if (ed > ev->emax[h]) {
-      real p[3], dd[3];
-      to_world(s, h, l, d, p, dd);
       ev->emax[h] = ed;
-      for (int a = 0; a < 3; ++a) ev->wpos[h][a] = p[a];
+      ev->wpos[h][0] = l[0];
+      ev->wpos[h][1] = l[1];
     }
   }
 }
@@ -1145,13 +1143,9 @@ static void score_singles(const scene_t *s, const event_t *ev, tally_t *t) {
     real e = ev->esum[h];
     if (!(e > R(0))) continue;
     t->cnt[GG_CNT_SINGLES]++;
-    real q[3];
-    for (int a = 0; a < 3; ++a) q[a] = ev->wpos[h][a] - s->hc[h][a];
-    real fx = dot3(q, s->he1[h]);
-    fx = fx + s->pix_half[0];
+    real fx = ev->wpos[h][0] + s->pix_half[0];
     fx = fx * s->inv_psp[0];
-    real fy = dot3(q, s->he2[h]);
-    fy = fy + s->pix_half[1];
+    real fy = ev->wpos[h][1] + s->pix_half[1];
     fy = fy * s->inv_psp[1];
     if (!(fx >= R(0) && fx < (real)s->pnx && fy >= R(0) && fy < (real)s->pny)) continue;
     int i = (int)fx, j = (int)fy;
@@ -1447,7 +1441,9 @@ int GGO_PREFIX(run_dose)(const gg_tables_desc *tb, const gg_volume_desc *vol, co
       if (acc_e2 && (acc_e2[2 * v] | acc_e2[2 * v + 1])) {
         double lo = (double)acc_e2[2 * v];
         lo = lo * 5.421010862427522e-20; /* 2^-64 */
-        edep2[v] += (double)acc_e2[2 * v + 1] + lo;
+        double hi = (double)acc_e2[2 * v + 1];
+        hi = hi * 2.3283064365386963e-10; /* 2^-32 */
+        edep2[v] += hi + lo;
         acc_e2[2 * v] = acc_e2[2 * v + 1] = 0;
       }
     }

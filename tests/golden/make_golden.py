@@ -17,9 +17,13 @@ used by these functions):
 * opengate/utility.py: calculate_variance (lines 551-560);
 * opengate/actors/dataitems.py:
   SingleItkImageWithVariance.get_variance_or_uncertainty (lines 1956-1993);
-* opengate/data/PhotonAttenuation.py: PhotonAttenuationEl (NIST mu/rho).
+* opengate/data/PhotonAttenuation.py: PhotonAttenuationEl (NIST mu/rho);
+* opengate/image.py: compute_image_3D_CDF (lines 313-360);
+* opengate/contrib/spect/spect_helpers.py: projection noise and efficiency
+  helpers (lines 374-387, 480-536, 582-591).
 
-Outputs (small, committed): hu_*.json, labels.npz, variance.npz, nist_mu.npz.
+Outputs (small, committed): hu_*.json, labels.npz, variance.npz, nist_mu.npz,
+voxel_cdf.npz, spect_metrics.npz.
 """
 
 import ast
@@ -210,6 +214,27 @@ def voxel_cdf_fixtures(ref):
                         cdf_z=np.array(cdf_z))
 
 
+def spect_metric_fixtures(ref):
+    """contrib/spect/spect_helpers.py: Poisson / history-by-history uncertainty, efficiency, z-score, speedup."""
+    ns = {"np": np}
+    _exec_functions(ref / "opengate/contrib/spect/spect_helpers.py",
+                    ["compute_poisson_relative_uncertainty", "compute_efficiency",
+                     "compute_history_by_history_relative_uncertainty", "compute_zscore", "compute_speedup"], ns)
+    rng = np.random.default_rng(21)
+    n = 5000
+    counts = rng.poisson(3.0, size=(3, 8, 9)).astype(np.float64)
+    counts2 = counts + rng.poisson(0.5, size=counts.shape) * counts  # multi-count events in some pixels
+    test = rng.poisson(3.0, size=counts.shape).astype(np.float64)
+    u_ref = ns["compute_history_by_history_relative_uncertainty"](counts, counts2, n)
+    u_test = ns["compute_poisson_relative_uncertainty"](test)
+    out = {"counts": counts, "counts2": counts2, "test": test, "n": np.array(n), "u_ref": u_ref, "u_test": u_test,
+           "poisson": ns["compute_poisson_relative_uncertainty"](counts),
+           "efficiency": ns["compute_efficiency"](u_ref, 12.5),
+           "zscore": ns["compute_zscore"](counts, test, (u_ref * counts) ** 2, (u_test * test) ** 2),
+           "speedup": ns["compute_speedup"](u_ref, u_test, 12.5, 0.8)}
+    np.savez_compressed(OUT / "spect_metrics.npz", **out)
+
+
 def main(ref):
     ref = pathlib.Path(ref)
     # the Schneider 2000 HU tables are inputs of the HU fixtures; keep copies of
@@ -222,6 +247,7 @@ def main(ref):
     variance_fixtures(ref)
     nist_fixtures(ref)
     voxel_cdf_fixtures(ref)
+    spect_metric_fixtures(ref)
     print("golden fixtures written to", OUT)
 
 

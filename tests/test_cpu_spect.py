@@ -168,3 +168,16 @@ def test_voxel_source_follows_activity():
     assert set(got) == {(1, 2, 3), (3, 0, 0), (0, 4, 5)}
     for k, p in ((1, 2, 3), 0.375), ((3, 0, 0), 0.125), ((0, 4, 5), 0.5):
         assert abs(got[k] - p) < 0.01
+
+
+def test_projection_metrics_match_reference():
+    g = np.load(GOLDEN / "spect_metrics.npz")
+    n = int(g["n"])
+    u_ref = S.compute_history_by_history_relative_uncertainty(g["counts"], g["counts2"], n)
+    np.testing.assert_array_equal(u_ref, g["u_ref"])
+    np.testing.assert_array_equal(S.compute_poisson_relative_uncertainty(g["test"]), g["u_test"])
+    np.testing.assert_array_equal(S.compute_poisson_relative_uncertainty(g["counts"]), g["poisson"])
+    np.testing.assert_array_equal(S.compute_efficiency(u_ref, 12.5), g["efficiency"])
+    z = S.compute_zscore(g["counts"], g["test"], (u_ref * g["counts"]) ** 2, (g["u_test"] * g["test"]) ** 2)
+    np.testing.assert_array_equal(z, g["zscore"])
+    np.testing.assert_array_equal(S.compute_speedup(u_ref, g["u_test"], 12.5, 0.8), g["speedup"])

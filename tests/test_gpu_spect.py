@@ -75,3 +75,23 @@ def test_spect_reset_and_history_offset():
         later = eng.projection()
     ref, _ = O.run_spect(scene, sp, 100_000, seed=7, first=200_000, threads=8)
     np.testing.assert_array_equal(later, ref)
+
+
+def test_all_angles_in_one_call_equal_per_angle_calls():
+    """gg_spect_run (one set of launches for every gantry position) == gg_spect_set_heads + gg_run per position."""
+    from opengate_gb300.engine import SpectEngine
+
+    scene, sp, _ = _case("tc99m_lehr", n_runs=3)
+    with SpectEngine(scene, sp) as eng:
+        eng.run(150_000, 13, first=1000)
+        one = eng.projection()
+        c_one = eng.counters()
+        n_launch = eng.last_kernel_ms()[3]
+        # one batch: the source stage, then phantom + head stage passes
+        assert n_launch >= 3 and (n_launch - 1) % 2 == 0
+    with SpectEngine(scene, sp) as eng:
+        eng.run_per_angle(150_000, 13, first=1000)
+        per = eng.projection()
+        c_per = eng.counters()
+    np.testing.assert_array_equal(one, per)
+    assert c_one == c_per
