@@ -193,6 +193,20 @@ typedef struct {
   int32_t n_runs;              /* gantry positions; projection slice = window + run * n_windows */
 } gg_spect_desc;
 
+/* ARF training photons (replaces the source + plane of
+   contrib/spect/ge_discovery_nm670.py:994-1027 add_source_for_arf_training_dataset /
+   add_actor_for_arf_training_dataset): photons start on the collimator front
+   face of one head, position uniform in |a1| <= half_extent[0],
+   |a2| <= half_extent[1], direction isotropic in the cone theta <=
+   acos(cos_theta_max) about the head normal (into the head), energy uniform
+   in [e_min, e_max]. */
+typedef struct {
+  double e_min, e_max;      /* MeV */
+  double cos_theta_max;
+  double half_extent[2];    /* mm */
+  double russian_roulette;  /* rows of photons detected in no window are kept with probability 1 / this (>= 1) */
+} gg_arf_sampling;
+
 typedef struct gg_ctx gg_ctx;
 
 typedef struct {
@@ -253,6 +267,64 @@ int gg_spect_setup(gg_ctx *ctx, const gg_spect_desc *spect);
 int gg_spect_set_heads(gg_ctx *ctx, int32_t run, const double *frames);
 int gg_spect_run(gg_ctx *ctx, uint64_t n_per_run, uint64_t seed, uint64_t first, const double *frames);
 int gg_get_projection(gg_ctx *ctx, double *out, size_t n);
+
+/* ---- ARF surrogate ---------------------------------------------------------
+   gg_arf_dataset replaces the ARF training-dataset simulation
+   (GateARFTrainingDatasetActor, core/opengate_core/opengate_lib/
+   GateARFTrainingDatasetActor.cpp:76-137, fed by
+   contrib/spect/ge_discovery_nm670.py:994-1027): samples [first, first + n)
+   of `sampling` are tracked through the head of gg_spect_setup (collimator,
+   gap, crystal, energy windows) and give rows (E MeV, theta deg, phi deg, w)
+   of float32, w = last window containing the crystal energy + 1, 0 = none
+   (kept with probability 1 / russian_roulette).  Rows are in sample order;
+   *n_rows = rows produced, the first min(*n_rows, capacity) are written. */
+int gg_arf_dataset(gg_ctx *ctx, const gg_arf_sampling *sampling, uint64_t n, uint64_t seed, uint64_t first,
+                   float *rows, uint64_t capacity, uint64_t *n_rows);
+
+/* The ARF network (the garf model the reference's ARFActor loads from a .pth
+   file, opengate/actors/arfactors.py:299-331): x = standardised (theta deg,
+   phi deg, E MeV) -> 128 ReLU -> 128 ReLU -> 128 ReLU -> n_classes logits ->
+   softmax; class 0 = no window, class k = window k.  Parameters are
+   GG_ARF_N_PARAMS floats: W1[128][3], b1[128], W2[128][128], b2[128],
+   W3[128][128], b3[128], W4[16][128] (rows >= n_classes zero), b4[16]
+   (weights stored [out][in]).  Layers 2-4 run on the tensor cores in BF16
+   with FP32 accumulation. */
+#define GG_ARF_N_PARAMS 35600
+typedef struct {
+  int32_t n_classes;          /* energy windows + 1, <= 9 */
+  float x_mean[3], x_std[3];  /* standardisation of (theta, phi, E) */
+  double russian_roulette;    /* class-0 keep factor of the training rows; class 0 is re-weighted by it */
+  double e_min, e_max;        /* trained energy domain, MeV */
+  double theta_max_deg;       /* trained angular domain */
+  double distance_to_crystal; /* mm from the collimator face to the projection plane */
+} gg_arf_model;
+
+typedef struct {
+  uint64_t n_samples;   /* training photons (rows come from gg_arf_dataset of these samples) */
+  uint64_t seed;        /* dataset seed (Philox stream 1) */
+  uint64_t init_seed;   /* weight initialisation (He-uniform) */
+  int32_t batch;        /* rows per Adam step, a multiple of 64, <= 65536 */
+  int32_t epochs;
+  float lr, beta1, beta2, eps;
+} gg_arf_train_opts;
+
+/* Generates the training rows of `sampling` on the device and trains the
+   network with Adam (cross-entropy, mean over the batch); model_out gets the
+   standardisation and domain (theta from sampling, energies from sampling),
+   distance_to_crystal = collimator + gap + half the crystal.  loss (epochs
+   values, or NULL) = mean loss of each epoch.  The trained model becomes the
+   context's ARF model. */
+int gg_arf_train(gg_ctx *ctx, const gg_arf_sampling *sampling, const gg_arf_train_opts *opts,
+                 gg_arf_model *model_out, double *loss);
+/* Sets / reads the context's ARF model (params: GG_ARF_N_PARAMS floats). */
+int gg_arf_set_model(gg_ctx *ctx, const gg_arf_model *model, const float *params);
+int gg_arf_get_params(gg_ctx *ctx, float *params, size_t n);
+/* Network outputs (softmax, before the class-0 re-weighting) of n rows
+   (E, theta, phi, -) -> probs[n][n_classes]. */
+int gg_arf_predict(gg_ctx *ctx, const float *rows, uint64_t n, float *probs);
+/* Gradient of the mean cross-entropy of n rows (n a multiple of 64) at the
+   current parameters, no update: grad[GG_ARF_N_PARAMS], *loss = mean loss. */
+int gg_arf_gradient(gg_ctx *ctx, const float *rows, uint64_t n, float *grad, double *loss);
 
 /* ---- dose run that allocates no device memory ------------------------------
  * No counterpart in the reference.  For callers that cannot call cudaMalloc

@@ -89,6 +89,46 @@ class SpectDesc(ctypes.Structure):
     ]
 
 
+class ArfSampling(ctypes.Structure):
+    _fields_ = [
+        ("e_min", ctypes.c_double),
+        ("e_max", ctypes.c_double),
+        ("cos_theta_max", ctypes.c_double),
+        ("half_extent", ctypes.c_double * 2),
+        ("russian_roulette", ctypes.c_double),
+    ]
+
+
+class ArfModel(ctypes.Structure):
+    _fields_ = [
+        ("n_classes", ctypes.c_int32),
+        ("x_mean", ctypes.c_float * 3),
+        ("x_std", ctypes.c_float * 3),
+        ("russian_roulette", ctypes.c_double),
+        ("e_min", ctypes.c_double),
+        ("e_max", ctypes.c_double),
+        ("theta_max_deg", ctypes.c_double),
+        ("distance_to_crystal", ctypes.c_double),
+    ]
+
+
+class ArfTrainOpts(ctypes.Structure):
+    _fields_ = [
+        ("n_samples", ctypes.c_uint64),
+        ("seed", ctypes.c_uint64),
+        ("init_seed", ctypes.c_uint64),
+        ("batch", ctypes.c_int32),
+        ("epochs", ctypes.c_int32),
+        ("lr", ctypes.c_float),
+        ("beta1", ctypes.c_float),
+        ("beta2", ctypes.c_float),
+        ("eps", ctypes.c_float),
+    ]
+
+
+GG_ARF_N_PARAMS = 35600
+
+
 class DeviceOpts(ctypes.Structure):
     _fields_ = [
         ("device", ctypes.c_int32), ("precision", ctypes.c_int32), ("block_size", ctypes.c_int32),
@@ -126,6 +166,17 @@ PROTOTYPES = [
     ("gg_spect_set_heads", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, _f64p]),
     ("gg_spect_run", ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64, _f64p]),
     ("gg_get_projection", ctypes.c_int, [ctypes.c_void_p, _f64p, ctypes.c_size_t]),
+    ("gg_arf_train", ctypes.c_int,
+     [ctypes.c_void_p, ctypes.POINTER(ArfSampling), ctypes.POINTER(ArfTrainOpts), ctypes.POINTER(ArfModel), _f64p]),
+    ("gg_arf_set_model", ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ArfModel), ctypes.POINTER(ctypes.c_float)]),
+    ("gg_arf_get_params", ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_float), ctypes.c_size_t]),
+    ("gg_arf_predict", ctypes.c_int,
+     [ctypes.c_void_p, ctypes.POINTER(ctypes.c_float), ctypes.c_uint64, ctypes.POINTER(ctypes.c_float)]),
+    ("gg_arf_gradient", ctypes.c_int,
+     [ctypes.c_void_p, ctypes.POINTER(ctypes.c_float), ctypes.c_uint64, ctypes.POINTER(ctypes.c_float), _f64p]),
+    ("gg_arf_dataset", ctypes.c_int,
+     [ctypes.c_void_p, ctypes.POINTER(ArfSampling), ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64,
+      ctypes.POINTER(ctypes.c_float), ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint64)]),
     ("gg_dose_run_noalloc", ctypes.c_int,
      [ctypes.c_int32, ctypes.c_void_p, ctypes.POINTER(TablesDesc), ctypes.POINTER(VolumeDesc),
       ctypes.POINTER(WorldDesc), ctypes.POINTER(SourceDesc), ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64,

@@ -17,6 +17,7 @@
 #include "../../include/gate_gpu.h"
 #include "gg_device.cuh"
 #include "gg_internal.h"
+#include "gg_mlp.cuh"
 
 namespace {
 
@@ -98,6 +99,25 @@ struct gg_ctx {
   void *d_queue[2] = {nullptr, nullptr};
   size_t q_cap = 0;
   unsigned long long *d_qn = nullptr;
+
+  // ARF training rows (device): staging, block counts/offsets, rows, identity head frame
+  float4 *d_arf_stage = nullptr, *d_arf_rows = nullptr;
+  unsigned int *d_arf_bcount = nullptr;
+  unsigned long long *d_arf_boff = nullptr, *d_arf_total = nullptr;
+  uint64_t arf_rows_cap = 0, arf_n_rows = 0;
+  void *d_frame_id = nullptr;
+
+  // ARF network: FP32 parameters, BF16 weight copies, Adam moments, per-tile gradients
+  float *d_params = nullptr, *d_adam_m = nullptr, *d_adam_v = nullptr, *d_grad = nullptr;
+  float *d_partial = nullptr, *d_loss_part = nullptr;
+  double *d_loss_acc = nullptr;
+  __nv_bfloat16 *d_wbf = nullptr;
+  int partial_tiles = 0;
+  float4 *d_io_rows = nullptr;
+  float *d_io_out = nullptr;
+  size_t io_cap = 0;
+  gg_arf_model arf{};
+  bool have_arf = false;
   std::vector<cudaEvent_t> ev;
   double last_generate_ms = 0, last_transport_ms = 0, last_flush_ms = 0;
   int last_launches = 0, last_stage_launches = 0, run_stage_launches = 0;
@@ -117,6 +137,18 @@ struct gg_ctx {
   }
   size_t real_size() const { return precision == GG_PREC_F64 ? sizeof(double) : sizeof(float); }
 
+  // Copies ordered with the context's kernels: the context stream is
+  // non-blocking, so plain cudaMemcpy / cudaMemset (legacy stream) would not
+  // wait for them.  Both return after the copy has completed.
+  int h2d(void *dst, const void *src, size_t bytes, const char *what) {
+    int st = cuda(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, stream), what);
+    return st ? st : cuda(cudaStreamSynchronize(stream), what);
+  }
+  int d2h(void *dst, const void *src, size_t bytes, const char *what) {
+    int st = cuda(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, stream), what);
+    return st ? st : cuda(cudaStreamSynchronize(stream), what);
+  }
+
   // Copies n floats to a new device array in working precision.
   int upload_real(void *&dst, const float *src, size_t n) {
     dfree(dst);
@@ -126,9 +158,9 @@ struct gg_ctx {
     if (!src) return cuda(cudaMemsetAsync(dst, 0, n * real_size(), stream), "cudaMemset");
     if (precision == GG_PREC_F64) {
       std::vector<double> tmp(src, src + n);
-      st = cuda(cudaMemcpy(dst, tmp.data(), n * sizeof(double), cudaMemcpyHostToDevice), "cudaMemcpy");
+      st = h2d(dst, tmp.data(), n * sizeof(double), "cudaMemcpy");
     } else {
-      st = cuda(cudaMemcpy(dst, src, n * sizeof(float), cudaMemcpyHostToDevice), "cudaMemcpy");
+      st = h2d(dst, src, n * sizeof(float), "cudaMemcpy");
     }
     return st;
   }
@@ -139,13 +171,13 @@ struct gg_ctx {
     if (n == 0) n = 1;
     int st = cuda(cudaMalloc(&dst, n * real_size()), "cudaMalloc");
     if (st) return st;
-    if (!src) return cuda(cudaMemset(dst, 0, n * real_size()), "cudaMemset");
+    if (!src) return cuda(cudaMemsetAsync(dst, 0, n * real_size(), stream), "cudaMemset");
     if (precision == GG_PREC_F64) {
-      return cuda(cudaMemcpy(dst, src, n * sizeof(double), cudaMemcpyHostToDevice), "cudaMemcpy");
+      return h2d(dst, src, n * sizeof(double), "cudaMemcpy");
     }
     f.resize(n);
     for (size_t i = 0; i < n; ++i) f[i] = (float)src[i];
-    return cuda(cudaMemcpy(dst, f.data(), n * sizeof(float), cudaMemcpyHostToDevice), "cudaMemcpy");
+    return h2d(dst, f.data(), n * sizeof(float), "cudaMemcpy");
   }
 
   void release() {
@@ -155,6 +187,13 @@ struct gg_ctx {
     dfree(d_acc_e); dfree(d_acc_e2); dfree(d_edep); dfree(d_edep2);
     dfree(d_counters); dfree(d_next); dfree(d_status); dfree(d_records);
     dfree(d_queue[0]); dfree(d_queue[1]); dfree(d_qn);
+    dfree(d_arf_stage); dfree(d_arf_rows); dfree(d_arf_bcount); dfree(d_arf_boff); dfree(d_arf_total);
+    dfree(d_frame_id);
+    arf_rows_cap = 0;
+    dfree(d_params); dfree(d_adam_m); dfree(d_adam_v); dfree(d_grad); dfree(d_partial); dfree(d_loss_part);
+    dfree(d_loss_acc); dfree(d_wbf); dfree(d_io_rows); dfree(d_io_out);
+    partial_tiles = 0;
+    io_cap = 0;
     q_cap = 0;
     dfree(d_cdf_z); dfree(d_cdf_y); dfree(d_cdf_x); dfree(d_proj); dfree(d_frames);
     rec_cap = 0;
@@ -272,6 +311,148 @@ struct gg_ctx {
   }
 };
 
+// ARF chunk size: samples per k_arf_sample launch
+static const uint64_t kArfChunk = 1ull << 22;
+
+// Generates ARF training rows of n samples into c->d_arf_rows (capacity rows,
+// reallocated when larger); c->arf_n_rows = rows produced (may exceed the
+// capacity: only the first `capacity` are stored).
+template <typename real>
+static int arf_generate(gg_ctx *c, const gg_arf_sampling *a, uint64_t n, uint64_t seed, uint64_t first,
+                        uint64_t capacity) {
+  int st;
+  if (!c->d_arf_stage) {
+    const uint64_t blocks = kArfChunk / 256;
+    if ((st = c->cuda(cudaMalloc(&c->d_arf_stage, kArfChunk * sizeof(float4)), "cudaMalloc ARF staging"))) return st;
+    if ((st = c->cuda(cudaMalloc(&c->d_arf_bcount, blocks * sizeof(unsigned int)), "cudaMalloc"))) return st;
+    if ((st = c->cuda(cudaMalloc(&c->d_arf_boff, blocks * sizeof(unsigned long long)), "cudaMalloc"))) return st;
+    if ((st = c->cuda(cudaMalloc(&c->d_arf_total, sizeof(unsigned long long)), "cudaMalloc"))) return st;
+    static const double id[12] = {0, 0, 0, 0, 0, 1, 1, 0, 0, 0, 1, 0};
+    if ((st = c->upload_real_d(c->d_frame_id, id, 12))) return st;
+  }
+  if (capacity > c->arf_rows_cap) {
+    dfree(c->d_arf_rows);
+    c->arf_rows_cap = 0;
+    if ((st = c->cuda(cudaMalloc(&c->d_arf_rows, (capacity ? capacity : 1) * sizeof(float4)), "cudaMalloc ARF rows")))
+      return st;
+    c->arf_rows_cap = capacity;
+  }
+  gg::Scene<real> s = c->scene<real>();
+  s.spect = 1;
+  s.n_heads = 1;
+  s.n_runs = 1;
+  s.frames = (const real *)c->d_frame_id;
+  s.run_base = 0;
+  s.run_first = 0;
+  s.run_len = 1;
+  gg::ArfArgs p;
+  p.seed = seed;
+  p.e_min = a->e_min;
+  p.e_max = a->e_max;
+  p.cos_theta_max = a->cos_theta_max;
+  p.half_extent[0] = a->half_extent[0];
+  p.half_extent[1] = a->half_extent[1];
+  p.russian_roulette = a->russian_roulette;
+  p.stage = c->d_arf_stage;
+  p.block_count = c->d_arf_bcount;
+  p.block_off = c->d_arf_boff;
+  p.counters = c->d_counters;
+  if ((st = c->cuda(cudaMemsetAsync(c->d_arf_total, 0, sizeof(unsigned long long), c->stream), "memset"))) return st;
+  for (uint64_t done = 0; done < n; done += kArfChunk) {
+    p.first = first + done;
+    p.n = std::min<uint64_t>(kArfChunk, n - done);
+    if ((st = c->cuda(gg::launch_arf_dataset<real>(s, p, c->d_arf_rows, capacity, c->d_arf_total, c->stream),
+                      "ARF dataset launch")))
+      return st;
+  }
+  unsigned long long total = 0;
+  if ((st = c->cuda(cudaMemcpyAsync(&total, c->d_arf_total, sizeof(total), cudaMemcpyDeviceToHost, c->stream),
+                    "ARF row count")))
+    return st;
+  if ((st = c->cuda(cudaStreamSynchronize(c->stream), "ARF dataset"))) return st;
+  c->arf_n_rows = total;
+  return GG_OK;
+}
+
+// ---- ARF network helpers -----------------------------------------------------
+static int arf_alloc(gg_ctx *c, int tiles) {
+  int st;
+  if (!c->d_params) {
+    if ((st = c->cuda(cudaMalloc(&c->d_params, gg::kNParams * sizeof(float)), "cudaMalloc ARF params"))) return st;
+    if ((st = c->cuda(cudaMalloc(&c->d_adam_m, gg::kNParams * sizeof(float)), "cudaMalloc"))) return st;
+    if ((st = c->cuda(cudaMalloc(&c->d_adam_v, gg::kNParams * sizeof(float)), "cudaMalloc"))) return st;
+    if ((st = c->cuda(cudaMalloc(&c->d_grad, gg::kNParams * sizeof(float)), "cudaMalloc"))) return st;
+    if ((st = c->cuda(cudaMalloc(&c->d_wbf, gg::kNBf * sizeof(__nv_bfloat16)), "cudaMalloc"))) return st;
+    if ((st = c->cuda(cudaMalloc(&c->d_loss_acc, 1024 * sizeof(double)), "cudaMalloc"))) return st;
+  }
+  if (tiles > c->partial_tiles) {
+    dfree(c->d_partial);
+    dfree(c->d_loss_part);
+    c->partial_tiles = 0;
+    if ((st = c->cuda(cudaMalloc(&c->d_partial, (size_t)tiles * gg::kNParams * sizeof(float)), "cudaMalloc")))
+      return st;
+    if ((st = c->cuda(cudaMalloc(&c->d_loss_part, (size_t)tiles * sizeof(float)), "cudaMalloc"))) return st;
+    c->partial_tiles = tiles;
+  }
+  return GG_OK;
+}
+
+static int io_alloc(gg_ctx *c, size_t rows) {
+  if (rows <= c->io_cap) return GG_OK;
+  dfree(c->d_io_rows);
+  dfree(c->d_io_out);
+  c->io_cap = 0;
+  int st;
+  if ((st = c->cuda(cudaMalloc(&c->d_io_rows, rows * sizeof(float4)), "cudaMalloc"))) return st;
+  if ((st = c->cuda(cudaMalloc(&c->d_io_out, rows * 16 * sizeof(float)), "cudaMalloc"))) return st;
+  c->io_cap = rows;
+  return GG_OK;
+}
+
+// splitmix64: the weight initialisation stream
+static uint64_t splitmix64(uint64_t &x) {
+  uint64_t z = (x += 0x9E3779B97F4A7C15ull);
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+// He-uniform weights U(-sqrt(6 / fan_in), +sqrt(6 / fan_in)), zero biases,
+// output rows >= n_classes zero.
+static std::vector<float> arf_init_params(uint64_t seed, int n_classes) {
+  std::vector<float> w(gg::kNParams, 0.0f);
+  uint64_t st = seed;
+  auto uni = [&](double lim) { return (float)(((double)(splitmix64(st) >> 11) * (1.0 / 9007199254740992.0) * 2.0 - 1.0) * lim); };
+  for (int e = 0; e < gg::kHid * 3; ++e) w[gg::kOffW1 + e] = uni(std::sqrt(6.0 / 3.0));
+  for (int e = 0; e < gg::kHid * gg::kHid; ++e) w[gg::kOffW2 + e] = uni(std::sqrt(6.0 / gg::kHid));
+  for (int e = 0; e < gg::kHid * gg::kHid; ++e) w[gg::kOffW3 + e] = uni(std::sqrt(6.0 / gg::kHid));
+  for (int r = 0; r < n_classes; ++r)
+    for (int k = 0; k < gg::kHid; ++k) w[gg::kOffW4 + r * gg::kHid + k] = uni(std::sqrt(6.0 / gg::kHid));
+  return w;
+}
+
+static gg::MlpTrainArgs arf_args(const gg_ctx *c) {
+  gg::MlpTrainArgs a{};
+  a.params = c->d_params;
+  a.wbf = c->d_wbf;
+  a.partial = c->d_partial;
+  a.loss_part = c->d_loss_part;
+  for (int k = 0; k < 3; ++k) {
+    a.mean[k] = c->arf.x_mean[k];
+    a.inv_std[k] = 1.0f / c->arf.x_std[k];
+  }
+  a.n_classes = c->arf.n_classes;
+  return a;
+}
+
+static int arf_model_check(gg_ctx *c, const gg_arf_model *m) {
+  if (m->n_classes < 2 || m->n_classes > 9) return c->fail(GG_ERR_ARG, "ARF model: n_classes must be 2..9");
+  for (int k = 0; k < 3; ++k)
+    if (!(m->x_std[k] > 0.0f)) return c->fail(GG_ERR_ARG, "ARF model: x_std must be > 0");
+  if (!(m->russian_roulette >= 1.0)) return c->fail(GG_ERR_ARG, "ARF model: russian_roulette must be >= 1");
+  return GG_OK;
+}
+
 extern "C" {
 
 int gg_create(const gg_device_opts *opts, gg_ctx **out) {
@@ -313,8 +494,9 @@ int gg_create(const gg_device_opts *opts, gg_ctx **out) {
       (e = cudaMalloc(&c->d_next, sizeof(unsigned long long))) != cudaSuccess ||
       (e = cudaMalloc(&c->d_status, sizeof(unsigned int))) != cudaSuccess)
     return bail(cudaGetErrorString(e));
-  cudaMemset(c->d_counters, 0, GG_N_COUNTERS * sizeof(unsigned long long));
-  cudaMemset(c->d_status, 0, sizeof(unsigned int));
+  cudaMemsetAsync(c->d_counters, 0, GG_N_COUNTERS * sizeof(unsigned long long), c->stream);
+  cudaMemsetAsync(c->d_status, 0, sizeof(unsigned int), c->stream);
+  cudaStreamSynchronize(c->stream);
   *out = c;
   return GG_OK;
 }
@@ -378,7 +560,7 @@ int gg_upload_tables(gg_ctx *c, const gg_tables_desc *t) {
   if ((st = c->upload_real(c->d_mat_rho, t->mat_rho, (size_t)t->n_mat))) return st;
   dfree(c->d_mat_comp);
   if ((st = c->cuda(cudaMalloc(&c->d_mat_comp, sizeof(int) * t->n_mat), "cudaMalloc"))) return st;
-  if ((st = c->cuda(cudaMemcpy(c->d_mat_comp, t->mat_comp, sizeof(int) * t->n_mat, cudaMemcpyHostToDevice),
+  if ((st = c->h2d(c->d_mat_comp, t->mat_comp, sizeof(int) * t->n_mat,
                     "cudaMemcpy")))
     return st;
   c->h_mat_comp.assign(t->mat_comp, t->mat_comp + t->n_mat);
@@ -673,9 +855,10 @@ static int run_impl(gg_ctx *c, uint64_t n, uint64_t seed, uint64_t first) {
   c->last_flush_ms = tf;
   c->last_launches = (int)(nb + (c->have_spect ? (uint64_t)c->run_stage_launches : nb) + (c->have_tally ? nb : 0));
   unsigned int status = 0;
-  if ((st = c->cuda(cudaMemcpy(&status, c->d_status, sizeof(status), cudaMemcpyDeviceToHost), "status"))) return st;
+  if ((st = c->d2h(&status, c->d_status, sizeof(status), "status"))) return st;
   if (status) {
-    cudaMemset(c->d_status, 0, sizeof(unsigned int));
+    cudaMemsetAsync(c->d_status, 0, sizeof(unsigned int), c->stream);
+    cudaStreamSynchronize(c->stream);
     if (status & gg::kStatusQueueOverflow)
       return c->fail(GG_ERR_QUEUE_OVERFLOW, "gg_run: a SPECT stage queue overflowed (photons were dropped)");
     return c->fail(GG_ERR_DOMAIN, "gg_run: source sampling failed (angular acceptance exhausted max_rejection)");
@@ -728,7 +911,7 @@ int gg_get_counters(gg_ctx *c, uint64_t *out, size_t n) {
   if (!c || !out) return GG_ERR_ARG;
   cudaSetDevice(c->device);
   unsigned long long tmp[GG_N_COUNTERS];
-  int st = c->cuda(cudaMemcpy(tmp, c->d_counters, sizeof(tmp), cudaMemcpyDeviceToHost), "counters");
+  int st = c->d2h(tmp, c->d_counters, sizeof(tmp), "counters");
   if (st) return st;
   for (size_t i = 0; i < n && i < GG_N_COUNTERS; ++i) out[i] = tmp[i];
   return GG_OK;
@@ -830,13 +1013,206 @@ int gg_spect_run(gg_ctx *c, uint64_t n_per_run, uint64_t seed, uint64_t first, c
   return run_impl(c, n, seed, first);
 }
 
+int gg_arf_dataset(gg_ctx *c, const gg_arf_sampling *a, uint64_t n, uint64_t seed, uint64_t first, float *rows,
+                   uint64_t capacity, uint64_t *n_rows) {
+  if (!c || !a || !n_rows || (capacity && !rows)) return GG_ERR_ARG;
+  cudaSetDevice(c->device);
+  if (!c->have_tables || !c->have_spect)
+    return c->fail(GG_ERR_STATE, "gg_arf_dataset: upload the tables and call gg_spect_setup first");
+  if (!(a->e_min > 0) || !(a->e_max >= a->e_min) || !(a->e_min >= c->e_min) || !(a->e_max <= c->e_max) ||
+      !(a->e_max < 2.0 * gg::kMC2))
+    return c->fail(GG_ERR_DOMAIN, "gg_arf_dataset: energies must lie in the tables and below 1.022 MeV");
+  if (!(a->cos_theta_max >= 0.0 && a->cos_theta_max <= 1.0) || !(a->half_extent[0] >= 0) ||
+      !(a->half_extent[1] >= 0) || !(a->russian_roulette >= 1.0))
+    return c->fail(GG_ERR_ARG, "gg_arf_dataset: cos_theta_max in [0, 1], half extents >= 0, russian_roulette >= 1");
+  int st = c->precision == GG_PREC_F64 ? arf_generate<double>(c, a, n, seed, first, capacity)
+                                       : arf_generate<float>(c, a, n, seed, first, capacity);
+  if (st) return st;
+  *n_rows = c->arf_n_rows;
+  const uint64_t m = std::min<uint64_t>(c->arf_n_rows, capacity);
+  if (m) {
+    st = c->d2h(rows, c->d_arf_rows, m * sizeof(float4), "download ARF rows");
+    if (st) return st;
+  }
+  return GG_OK;
+}
+
+int gg_arf_set_model(gg_ctx *c, const gg_arf_model *m, const float *params) {
+  if (!c || !m || !params) return GG_ERR_ARG;
+  cudaSetDevice(c->device);
+  int st;
+  if ((st = arf_model_check(c, m))) return st;
+  if ((st = arf_alloc(c, 1))) return st;
+  std::vector<float> w(params, params + gg::kNParams);
+  for (int r = m->n_classes; r < gg::kOutPad; ++r) {
+    for (int k = 0; k < gg::kHid; ++k) w[gg::kOffW4 + r * gg::kHid + k] = 0.0f;
+    w[gg::kOffB4 + r] = 0.0f;
+  }
+  if ((st = c->h2d(c->d_params, w.data(), w.size() * sizeof(float), "upload")))
+    return st;
+  if ((st = c->cuda(gg::launch_mlp_to_bf16(c->d_params, c->d_wbf, c->stream), "ARF weights"))) return st;
+  if ((st = c->cuda(cudaStreamSynchronize(c->stream), "ARF weights"))) return st;
+  c->arf = *m;
+  c->have_arf = true;
+  return GG_OK;
+}
+
+int gg_arf_get_params(gg_ctx *c, float *params, size_t n) {
+  if (!c || !params) return GG_ERR_ARG;
+  cudaSetDevice(c->device);
+  if (!c->have_arf) return c->fail(GG_ERR_STATE, "gg_arf_get_params: no ARF model");
+  if (n != (size_t)gg::kNParams) return c->fail(GG_ERR_ARG, "gg_arf_get_params: need %d floats", gg::kNParams);
+  return c->d2h(params, c->d_params, n * sizeof(float), "download");
+}
+
+int gg_arf_predict(gg_ctx *c, const float *rows, uint64_t n, float *probs) {
+  if (!c || (n && (!rows || !probs))) return GG_ERR_ARG;
+  cudaSetDevice(c->device);
+  if (!c->have_arf) return c->fail(GG_ERR_STATE, "gg_arf_predict: no ARF model");
+  if (n == 0) return GG_OK;
+  int st;
+  if ((st = io_alloc(c, (size_t)n))) return st;
+  if ((st = c->h2d(c->d_io_rows, rows, n * sizeof(float4), "upload"))) return st;
+  gg::MlpTrainArgs a = arf_args(c);
+  a.rows = c->d_io_rows;
+  a.n_rows = n;
+  const uint64_t tiles = (n + gg::kTileM - 1) / gg::kTileM;
+  const int grid = (int)std::min<uint64_t>(tiles, (uint64_t)c->n_sm * 8);
+  if ((st = c->cuda(gg::launch_mlp_predict(a, c->d_io_out, n, grid, c->stream), "ARF predict"))) return st;
+  return c->d2h(probs, c->d_io_out, n * c->arf.n_classes * sizeof(float), "download");
+}
+
+int gg_arf_gradient(gg_ctx *c, const float *rows, uint64_t n, float *grad, double *loss) {
+  if (!c || !rows || !grad) return GG_ERR_ARG;
+  cudaSetDevice(c->device);
+  if (!c->have_arf) return c->fail(GG_ERR_STATE, "gg_arf_gradient: no ARF model");
+  if (n == 0 || n % gg::kTileM || n > 65536) return c->fail(GG_ERR_ARG, "gg_arf_gradient: n must be a multiple of 64, <= 65536");
+  const int tiles = (int)(n / gg::kTileM);
+  int st;
+  if ((st = arf_alloc(c, tiles)) || (st = io_alloc(c, (size_t)n))) return st;
+  if ((st = c->h2d(c->d_io_rows, rows, n * sizeof(float4), "upload"))) return st;
+  for (uint64_t i = 0; i < n; ++i)
+    if (!(rows[4 * i + 3] >= 0.0f) || rows[4 * i + 3] >= (float)c->arf.n_classes)
+      return c->fail(GG_ERR_ARG, "gg_arf_gradient: row %llu: class outside [0, n_classes)", (unsigned long long)i);
+  gg::MlpTrainArgs a = arf_args(c);
+  a.rows = c->d_io_rows;
+  a.row0 = 0;
+  a.n_rows = n;
+  a.inv_batch = 1.0f / (float)n;
+  if ((st = c->cuda(gg::launch_mlp_train(a, tiles, c->stream), "ARF gradient"))) return st;
+  gg::MlpAdamArgs g{};
+  g.partial = c->d_partial;
+  g.n_tiles = tiles;
+  g.params = c->d_params;
+  g.wbf = c->d_wbf;
+  g.grad_out = c->d_grad;
+  g.lr = 0.0f;
+  if ((st = c->cuda(gg::launch_mlp_adam(g, c->stream), "ARF gradient sum"))) return st;
+  std::vector<float> lp(tiles);
+  if ((st = c->d2h(grad, c->d_grad, gg::kNParams * sizeof(float), "download")))
+    return st;
+  if ((st = c->d2h(lp.data(), c->d_loss_part, tiles * sizeof(float), "download")))
+    return st;
+  if (loss) {
+    double sum = 0.0;
+    for (float v : lp) sum += v;
+    *loss = sum / (double)n;
+  }
+  return GG_OK;
+}
+
+int gg_arf_train(gg_ctx *c, const gg_arf_sampling *smp, const gg_arf_train_opts *o, gg_arf_model *model_out,
+                 double *loss) {
+  if (!c || !smp || !o) return GG_ERR_ARG;
+  cudaSetDevice(c->device);
+  if (!c->have_tables || !c->have_spect)
+    return c->fail(GG_ERR_STATE, "gg_arf_train: upload the tables and call gg_spect_setup first");
+  if (o->batch < gg::kTileM || o->batch % gg::kTileM || o->batch > 65536 || o->epochs < 1 || o->epochs > 1024 ||
+      !(o->lr > 0.0f) || o->n_samples == 0)
+    return c->fail(GG_ERR_ARG, "gg_arf_train: batch a multiple of 64 (<= 65536), 1..1024 epochs, lr > 0, samples > 0");
+  // training rows on the device
+  uint64_t n_rows = 0;
+  {
+    if (!(smp->e_min > 0) || !(smp->e_max > smp->e_min) || !(smp->e_min >= c->e_min) || !(smp->e_max <= c->e_max) ||
+        !(smp->e_max < 2.0 * gg::kMC2) || !(smp->cos_theta_max >= 0.0 && smp->cos_theta_max < 1.0) ||
+        !(smp->russian_roulette >= 1.0))
+      return c->fail(GG_ERR_ARG, "gg_arf_train: invalid sampling");
+    int st = c->precision == GG_PREC_F64 ? arf_generate<double>(c, smp, o->n_samples, o->seed, 0, o->n_samples)
+                                         : arf_generate<float>(c, smp, o->n_samples, o->seed, 0, o->n_samples);
+    if (st) return st;
+    n_rows = c->arf_n_rows;
+    if (n_rows < (uint64_t)o->batch) return c->fail(GG_ERR_DOMAIN, "gg_arf_train: fewer rows than one batch");
+  }
+  gg_arf_model m{};
+  m.n_classes = c->spect.n_windows + 1;
+  const double th = std::acos(smp->cos_theta_max) * (180.0 / M_PI);
+  m.x_mean[0] = (float)(0.5 * th);
+  m.x_std[0] = (float)(th / std::sqrt(12.0));
+  m.x_mean[1] = 0.0f;
+  m.x_std[1] = (float)(360.0 / std::sqrt(12.0));
+  m.x_mean[2] = (float)(0.5 * (smp->e_min + smp->e_max));
+  m.x_std[2] = (float)((smp->e_max - smp->e_min) / std::sqrt(12.0));
+  m.russian_roulette = smp->russian_roulette;
+  m.e_min = smp->e_min;
+  m.e_max = smp->e_max;
+  m.theta_max_deg = th;
+  m.distance_to_crystal = c->spect.collimator_thickness + c->spect.gap + 0.5 * c->spect.crystal_thickness;
+  int st;
+  if ((st = arf_model_check(c, &m))) return st;
+  std::vector<float> w0 = arf_init_params(o->init_seed, m.n_classes);
+  if ((st = gg_arf_set_model(c, &m, w0.data()))) return st;
+  const int tiles = o->batch / gg::kTileM;
+  if ((st = arf_alloc(c, tiles))) return st;
+  if ((st = c->cuda(cudaMemsetAsync(c->d_adam_m, 0, gg::kNParams * sizeof(float), c->stream), "memset"))) return st;
+  if ((st = c->cuda(cudaMemsetAsync(c->d_adam_v, 0, gg::kNParams * sizeof(float), c->stream), "memset"))) return st;
+  if ((st = c->cuda(cudaMemsetAsync(c->d_loss_acc, 0, 1024 * sizeof(double), c->stream), "memset"))) return st;
+  gg::MlpTrainArgs a = arf_args(c);
+  a.rows = c->d_arf_rows;
+  a.n_rows = n_rows;
+  a.inv_batch = 1.0f / (float)o->batch;
+  gg::MlpAdamArgs g{};
+  g.partial = c->d_partial;
+  g.n_tiles = tiles;
+  g.params = c->d_params;
+  g.wbf = c->d_wbf;
+  g.m = c->d_adam_m;
+  g.v = c->d_adam_v;
+  g.lr = o->lr;
+  g.beta1 = o->beta1;
+  g.beta2 = o->beta2;
+  g.eps = o->eps;
+  g.loss_part = c->d_loss_part;
+  const uint64_t steps_per_epoch = (n_rows + (uint64_t)o->batch - 1) / (uint64_t)o->batch;
+  uint64_t t = 0;
+  for (int ep = 0; ep < o->epochs; ++ep) {
+    g.loss_acc = c->d_loss_acc + ep;
+    for (uint64_t k = 0; k < steps_per_epoch; ++k, ++t) {
+      a.row0 = (t * (uint64_t)o->batch) % n_rows;
+      if ((st = c->cuda(gg::launch_mlp_train(a, tiles, c->stream), "ARF train step"))) return st;
+      g.c1 = (float)(1.0 / (1.0 - std::pow((double)o->beta1, (double)(t + 1))));
+      g.c2 = (float)(1.0 / (1.0 - std::pow((double)o->beta2, (double)(t + 1))));
+      if ((st = c->cuda(gg::launch_mlp_adam(g, c->stream), "ARF Adam step"))) return st;
+    }
+  }
+  std::vector<double> lacc(o->epochs);
+  if ((st = c->cuda(cudaMemcpyAsync(lacc.data(), c->d_loss_acc, o->epochs * sizeof(double), cudaMemcpyDeviceToHost,
+                                    c->stream),
+                    "download")))
+    return st;
+  if ((st = c->cuda(cudaStreamSynchronize(c->stream), "ARF training"))) return st;
+  if (loss)
+    for (int ep = 0; ep < o->epochs; ++ep) loss[ep] = lacc[ep] / ((double)steps_per_epoch * o->batch);
+  if (model_out) *model_out = m;
+  return GG_OK;
+}
+
 int gg_get_projection(gg_ctx *c, double *out, size_t n) {
   if (!c || !out) return GG_ERR_ARG;
   cudaSetDevice(c->device);
   if (!c->have_spect) return c->fail(GG_ERR_STATE, "gg_get_projection: no SPECT heads");
   if (n != c->n_proj) return c->fail(GG_ERR_ARG, "gg_get_projection: buffer has %zu values, need %zu", n, c->n_proj);
   std::vector<unsigned long long> tmp(n);
-  int st = c->cuda(cudaMemcpy(tmp.data(), c->d_proj, n * 8, cudaMemcpyDeviceToHost), "download projections");
+  int st = c->d2h(tmp.data(), c->d_proj, n * 8, "download projections");
   if (st) return st;
   for (size_t i = 0; i < n; ++i) out[i] = (double)tmp[i];
   return GG_OK;

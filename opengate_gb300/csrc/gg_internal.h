@@ -1,5 +1,6 @@
 // gg_internal.h - declarations shared by the host API and the kernel translation units.
 #pragma once
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include <cstddef>
@@ -39,8 +40,54 @@ struct StageArgs {
   size_t q_cap;                    // capacity of each queue (entries)
 };
 
+// One launch of the ARF training-row generator (see gg_arf.cu).
+struct ArfArgs {
+  uint64_t seed, first, n;        // samples [first, first + n), Philox stream 1
+  double e_min, e_max, cos_theta_max, half_extent[2], russian_roulette;
+  float4 *stage;                  // [n] row per sample (w = -1: dropped)
+  unsigned int *block_count;      // [blocks] kept rows per block
+  unsigned long long *block_off;  // [blocks] first output row of each block
+  unsigned long long *counters;   // GG_N_COUNTERS slots
+};
+
+// One training step (or a prediction) of the ARF network (see gg_mlp.cu).
+struct MlpTrainArgs {
+  const float4 *rows;            // (E, theta, phi, class) rows
+  uint64_t row0, n_rows;         // tile t reads rows (row0 + 64 t + r) % n_rows
+  const float *params;           // FP32 parameters
+  const __nv_bfloat16 *wbf;      // BF16 copies of W2, W3, W4
+  float *partial;                // [tiles][kNParams] gradient of each tile
+  float *loss_part;              // [tiles] loss sum of each tile
+  float mean[3], inv_std[3];     // standardisation of (theta, phi, E)
+  int n_classes;
+  float inv_batch;               // 1 / rows in the step
+};
+
+struct MlpAdamArgs {
+  const float *partial;
+  int n_tiles;
+  float *params;
+  __nv_bfloat16 *wbf;
+  float *m, *v;                  // Adam moments
+  float *grad_out;               // summed gradient (or null)
+  float lr, beta1, beta2, eps;   // lr = 0: gradient only, no update
+  float c1, c2;                  // 1 / (1 - beta1^t), 1 / (1 - beta2^t)
+  const float *loss_part;        // [n_tiles] tile loss sums, added to *loss_acc (or null)
+  double *loss_acc;
+};
+
+size_t mlp_smem_bytes();
+cudaError_t launch_mlp_train(const MlpTrainArgs &a, int n_tiles, cudaStream_t st);
+cudaError_t launch_mlp_adam(const MlpAdamArgs &a, cudaStream_t st);
+cudaError_t launch_mlp_to_bf16(const float *params, __nv_bfloat16 *wbf, cudaStream_t st);
+cudaError_t launch_mlp_predict(const MlpTrainArgs &a, float *out, uint64_t n, int grid, cudaStream_t st);
+
 template <typename real>
 size_t transport_smem_bytes(int n_comp, int n_e, int n_mat);
+// Rows of p.n samples appended to rows[*total ...] (capacity rows); *total advances on the device.
+template <typename real>
+cudaError_t launch_arf_dataset(const Scene<real> &s, const ArfArgs &p, float4 *rows, uint64_t capacity,
+                               unsigned long long *total, cudaStream_t st);
 template <typename real>
 size_t queue_bytes(size_t cap);
 // stage 0: phantom stage, 1: head stage

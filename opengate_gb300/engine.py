@@ -143,3 +143,73 @@ class SpectEngine(DoseEngine):
         out = np.empty(int(np.prod(shape)), dtype=np.float64)
         self._call("gg_get_projection", C.ptr(out, ctypes.c_double), out.size)
         return out.reshape(shape)
+
+
+class ArfNetwork:
+    """ARF surrogate of a SPECT head on the context of a SpectEngine.
+
+    Training rows come from the head transport (gg_arf_dataset); the network
+    (3 -> 128 -> 128 -> 128 -> n_classes, BF16 tensor-core GEMMs) is trained
+    on the GPU by gg_arf_train.  Mirrors the garf model the reference's
+    ARFActor loads (opengate/actors/arfactors.py:299-331).
+    """
+
+    def __init__(self, engine):
+        self.eng = engine
+        self.model = None
+
+    @staticmethod
+    def sampling(e_min, e_max, theta_max_deg, half_extent, russian_roulette):
+        a = C.ArfSampling()
+        a.e_min, a.e_max = float(e_min), float(e_max)
+        a.cos_theta_max = float(np.cos(np.radians(theta_max_deg)))
+        a.half_extent[:] = [float(half_extent[0]), float(half_extent[1])]
+        a.russian_roulette = float(russian_roulette)
+        return a
+
+    def dataset(self, sampling, n, seed, first=0):
+        rows = np.zeros((max(n, 1), 4), dtype=np.float32)
+        m = ctypes.c_uint64()
+        self.eng._call("gg_arf_dataset", ctypes.byref(sampling), ctypes.c_uint64(n), ctypes.c_uint64(seed),
+                       ctypes.c_uint64(first), C.ptr(rows, ctypes.c_float), ctypes.c_uint64(n), ctypes.byref(m))
+        return rows[: m.value].copy()
+
+    def train(self, sampling, n_samples, seed, epochs=4, batch=8192, lr=1e-3, init_seed=1, beta1=0.9,
+              beta2=0.999, eps=1e-8):
+        o = C.ArfTrainOpts()
+        o.n_samples, o.seed, o.init_seed = int(n_samples), int(seed), int(init_seed)
+        o.batch, o.epochs = int(batch), int(epochs)
+        o.lr, o.beta1, o.beta2, o.eps = lr, beta1, beta2, eps
+        model = C.ArfModel()
+        loss = np.zeros(epochs, dtype=np.float64)
+        self.eng._call("gg_arf_train", ctypes.byref(sampling), ctypes.byref(o), ctypes.byref(model),
+                       C.ptr(loss, ctypes.c_double))
+        self.model = model
+        return model, loss
+
+    def set_model(self, model, params):
+        params = np.ascontiguousarray(params, dtype=np.float32)
+        if params.size != C.GG_ARF_N_PARAMS:
+            raise ValueError(f"need {C.GG_ARF_N_PARAMS} parameters")
+        self.eng._call("gg_arf_set_model", ctypes.byref(model), C.ptr(params, ctypes.c_float))
+        self.model = model
+
+    def params(self):
+        out = np.zeros(C.GG_ARF_N_PARAMS, dtype=np.float32)
+        self.eng._call("gg_arf_get_params", C.ptr(out, ctypes.c_float), out.size)
+        return out
+
+    def predict(self, rows):
+        rows = np.ascontiguousarray(rows, dtype=np.float32)
+        out = np.zeros((len(rows), self.model.n_classes), dtype=np.float32)
+        self.eng._call("gg_arf_predict", C.ptr(rows, ctypes.c_float), ctypes.c_uint64(len(rows)),
+                       C.ptr(out, ctypes.c_float))
+        return out
+
+    def gradient(self, rows):
+        rows = np.ascontiguousarray(rows, dtype=np.float32)
+        g = np.zeros(C.GG_ARF_N_PARAMS, dtype=np.float32)
+        loss = ctypes.c_double()
+        self.eng._call("gg_arf_gradient", C.ptr(rows, ctypes.c_float), ctypes.c_uint64(len(rows)),
+                       C.ptr(g, ctypes.c_float), ctypes.byref(loss))
+        return loss.value, g

@@ -1500,6 +1500,163 @@ int GGO_PREFIX(run_spect)(const gg_tables_desc *tb, const gg_volume_desc *vol, c
   return status;
 }
 
+/* ARF training rows (GateARFTrainingDatasetActor::SteppingAction /
+   EndOfEventAction, core/opengate_core/opengate_lib/GateARFTrainingDatasetActor.cpp:76-137):
+   sample i of [first, first + n) starts on the collimator front face of head 0
+   (head-local frame = world frame), is tracked through the head until it is
+   absorbed or leaves the head box, and gives the row (E, theta, phi, w) of
+   its direction at the face: theta = acos(dz), phi = atan2(dy, dx) in
+   degrees, w = last window containing the event's crystal energy + 1, 0 for
+   none; w = 0 rows are kept with probability 1 / russian_roulette.  Rows are
+   written in sample order to rows[4 * k]; *n_rows = rows written.  Philox
+   stream 1 of history i. */
+static int arf_sample(const scene_t *s, const gg_arf_sampling *a, uint64_t seed, uint64_t i, tally_t *t,
+                      float row[4]) {
+  rng_t g;
+  rng_init(&g, seed, i, 1u);
+  photon_t ph;
+  memset(&ph, 0, sizeof(ph));
+  real hx = (real)a->half_extent[0], hy = (real)a->half_extent[1];
+  real u = R(2) * u01(&g);
+  u = u - R(1);
+  ph.pos[0] = u * hx;
+  u = R(2) * u01(&g);
+  u = u - R(1);
+  ph.pos[1] = u * hy;
+  ph.pos[2] = R(0);
+  real w = R(1) - (real)a->cos_theta_max;
+  w = u01(&g) * w;
+  real ct = R(1) - w;
+  real sp, cp;
+  ggo_sincos_turn(u01(&g), &sp, &cp);
+  real st2 = ct * ct;
+  st2 = R(1) - st2;
+  real st = ggo_sqrt(st2 > R(0) ? st2 : R(0));
+  ph.dir[0] = st * cp;
+  ph.dir[1] = st * sp;
+  ph.dir[2] = ct;
+  real de = (real)a->e_max - (real)a->e_min;
+  de = de * u01(&g);
+  real e = (real)a->e_min + de;
+  row[0] = (float)e;
+  row[1] = (float)(acos((double)ph.dir[2]) * (180.0 / M_PI));
+  row[2] = (float)(atan2((double)ph.dir[1], (double)ph.dir[0]) * (180.0 / M_PI));
+  set_energy(s, &ph, e);
+  ph.alive = 1;
+  ph.in_head = 1;
+  ph.head = 0;
+  ph.hreg = 0;
+  ph.left_hole = 0;
+  ph.exclude = -1;
+  event_t ev;
+  memset(&ev, 0, sizeof(ev));
+  int steps = 0;
+  while (ph.alive && ph.in_head) {
+    if (++steps > STEP_CAP) {
+      t->cnt[GG_CNT_LOOP_CAPPED]++;
+      break;
+    }
+    head_step(s, &ph, &g, t, &ev);
+  }
+  int label = 0;
+  real ed = ev.esum[0];
+  if (ed > R(0)) {
+    t->cnt[GG_CNT_SINGLES]++;
+    for (int k = 0; k < s->n_win; ++k)
+      if (ed >= s->wlo[k] && ed < s->whi[k]) label = k + 1;
+  }
+  row[3] = (float)label;
+  if (label == 0) {
+    real r = u01(&g) * (real)a->russian_roulette;
+    if (!(r < R(1))) return 0;
+  }
+  return 1;
+}
+
+typedef struct {
+  const scene_t *s;
+  const gg_arf_sampling *a;
+  uint64_t seed, i0, i1, first;
+  float *rows;
+  uint8_t *keep;
+  tally_t t;
+} arf_worker_t;
+
+static void *arf_worker(void *arg) {
+  arf_worker_t *w = (arf_worker_t *)arg;
+  for (uint64_t i = w->i0; i < w->i1; ++i)
+    w->keep[i - w->first] = (uint8_t)arf_sample(w->s, w->a, w->seed, i, &w->t, w->rows + 4 * (i - w->first));
+  return NULL;
+}
+
+int GGO_PREFIX(arf_dataset)(const gg_tables_desc *tb, const gg_spect_desc *sp, const gg_arf_sampling *a,
+                            uint64_t seed, uint64_t first, uint64_t n, int n_threads, float *rows,
+                            uint64_t *n_rows, uint64_t *counters) {
+  /* head-only scene: no image (one air voxel far away), identity head frame */
+  static const uint16_t label0 = 0;
+  gg_volume_desc vol;
+  memset(&vol, 0, sizeof(vol));
+  vol.dims[0] = vol.dims[1] = vol.dims[2] = 1;
+  vol.spacing[0] = vol.spacing[1] = vol.spacing[2] = 1.0;
+  vol.corner[0] = vol.corner[1] = vol.corner[2] = 1.0e6;
+  vol.labels = &label0;
+  float *maj = (float *)malloc((size_t)tb->n_e * sizeof(float));
+  for (int k = 0; k < tb->n_e; ++k) maj[k] = 1.0f; /* the image is never entered */
+  vol.majorant = maj;
+  gg_world_desc wd;
+  memset(&wd, 0, sizeof(wd));
+  wd.half_size[0] = wd.half_size[1] = wd.half_size[2] = 2.0e6;
+  gg_source_desc src;
+  memset(&src, 0, sizeof(src));
+  src.ene_type = GG_ENE_MONO;
+  src.mono = a->e_max;
+  scene_t s;
+  scene_init(&s, tb, &vol, &wd, &src);
+  gg_spect_desc one = *sp;
+  one.n_heads = 1;
+  one.n_runs = 1;
+  spect_init(&s, &one);
+  static const double frame[12] = {0, 0, 0, 0, 0, 1, 1, 0, 0, 0, 1, 0};
+  spect_set_heads(&s, 0, frame);
+  if (n_threads < 1) n_threads = 1;
+  float *all = (float *)malloc((n ? n : 1) * 4 * sizeof(float));
+  uint8_t *keep = (uint8_t *)calloc(n ? n : 1, 1);
+  arf_worker_t *ws = (arf_worker_t *)calloc((size_t)n_threads, sizeof(arf_worker_t));
+  pthread_t *th = (pthread_t *)calloc((size_t)n_threads, sizeof(pthread_t));
+  uint64_t per = (n + (uint64_t)n_threads - 1) / (uint64_t)n_threads;
+  for (int k = 0; k < n_threads; ++k) {
+    ws[k].s = &s;
+    ws[k].a = a;
+    ws[k].seed = seed;
+    ws[k].first = first;
+    ws[k].i0 = first + (per * (uint64_t)k < n ? per * (uint64_t)k : n);
+    ws[k].i1 = first + (per * (uint64_t)(k + 1) < n ? per * (uint64_t)(k + 1) : n);
+    ws[k].rows = all;
+    ws[k].keep = keep;
+    if (n_threads > 1) pthread_create(&th[k], NULL, arf_worker, &ws[k]);
+    else arf_worker(&ws[k]);
+  }
+  if (n_threads > 1)
+    for (int k = 0; k < n_threads; ++k) pthread_join(th[k], NULL);
+  uint64_t m = 0;
+  for (uint64_t i = 0; i < n; ++i)
+    if (keep[i]) {
+      memcpy(rows + 4 * m, all + 4 * i, 4 * sizeof(float));
+      ++m;
+    }
+  *n_rows = m;
+  for (int k = 0; k < n_threads; ++k)
+    for (int c = 0; c < GG_N_COUNTERS; ++c) counters[c] += ws[k].t.cnt[c];
+  counters[GG_CNT_HISTORIES] += n;
+  free(all);
+  free(keep);
+  free(ws);
+  free(th);
+  free(maj);
+  scene_free(&s);
+  return GG_OK;
+}
+
 /* ---- small exported probes for the unit tests ---- */
 void GGO_PREFIX(philox)(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]) {
   philox4x32_10(ctr, key, out);

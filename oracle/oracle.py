@@ -183,3 +183,22 @@ def hex_exit(spect, qx, qy, d1, d2, precision=32):
     f.argtypes = [ctypes.POINTER(C.SpectDesc)] + [ctypes.c_double] * 4
     d = spect.desc()
     return f(ctypes.byref(d), float(qx), float(qy), float(d1), float(d2))
+
+
+def arf_dataset(tables_desc, spect, sampling, n, seed, first=0, threads=8, precision=32):
+    """Oracle ARF training rows: (rows [m][4] float32 = E, theta, phi, window, counters)."""
+    L = lib(precision)
+    fn = getattr(L, f"ggo{precision}_arf_dataset")
+    fn.restype = ctypes.c_int
+    fn.argtypes = [ctypes.POINTER(C.TablesDesc), ctypes.POINTER(C.SpectDesc), ctypes.POINTER(C.ArfSampling),
+                   ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int, ctypes.POINTER(ctypes.c_float),
+                   ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64)]
+    rows = np.zeros((max(n, 1), 4), dtype=np.float32)
+    m = ctypes.c_uint64()
+    cnt = np.zeros(C.GG_N_COUNTERS, dtype=np.uint64)
+    desc = spect.desc()
+    st = fn(ctypes.byref(tables_desc), ctypes.byref(desc), ctypes.byref(sampling), seed, first, n, threads,
+            C.ptr(rows, ctypes.c_float), ctypes.byref(m), C.ptr(cnt, ctypes.c_uint64))
+    if st != 0:
+        raise RuntimeError(f"oracle ARF dataset failed with status {st}")
+    return rows[: m.value].copy(), {name: int(cnt[i]) for i, name in enumerate(C.COUNTER_NAMES)}

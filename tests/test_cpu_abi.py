@@ -51,7 +51,8 @@ def test_ctypes_struct_layout_matches_header(tmp_path):
     import subprocess
 
     structs = {"gg_tables_desc": C.TablesDesc, "gg_volume_desc": C.VolumeDesc, "gg_spect_desc": C.SpectDesc,
-               "gg_world_desc": C.WorldDesc, "gg_source_desc": C.SourceDesc, "gg_device_opts": C.DeviceOpts}
+               "gg_world_desc": C.WorldDesc, "gg_source_desc": C.SourceDesc, "gg_device_opts": C.DeviceOpts,
+               "gg_arf_sampling": C.ArfSampling}
     lines = ['#include <stdio.h>', '#include <stddef.h>', f'#include "{HEADER}"', "int main(void) {"]
     for cname, py in structs.items():
         lines.append(f'  printf("{cname} %zu\\n", sizeof({cname}));')

@@ -1,0 +1,110 @@
+"""ARF surrogate on the GPU against the CPU oracles.
+
+* training rows: same rows as the oracle (energies and classes bit for bit,
+  angles within float rounding of acos / atan2);
+* network: forward probabilities and the gradient of the mean cross-entropy
+  from the BF16 tensor-core kernels against the FP64 oracle, with BF16
+  rounding emulated at the kernels' storage points (tight) and in plain FP64
+  (looser: the BF16 error itself);
+* training: the loss falls and the trained network reproduces the measured
+  detection probability of the photopeak window.
+"""
+
+import math
+
+import numpy as np
+import pytest
+
+from opengate_gb300 import _capi as C
+from opengate_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+O = pytest.importorskip("oracle.oracle")
+M = pytest.importorskip("oracle.arf_mlp")
+
+from .test_cpu_arf import MEAN, STD, _arf_case, random_params  # noqa: E402
+
+
+def _engine(scene, sp):
+    from opengate_gb300.engine import ArfNetwork, SpectEngine
+
+    eng = SpectEngine(scene, sp)
+    return eng, ArfNetwork(eng)
+
+
+def _model(n_classes, rr=1.0):
+    m = C.ArfModel()
+    m.n_classes = n_classes
+    m.x_mean[:] = MEAN
+    m.x_std[:] = STD
+    m.russian_roulette = rr
+    m.e_min, m.e_max, m.theta_max_deg, m.distance_to_crystal = 0.05, 0.25, 30.0, 40.0
+    return m
+
+
+def test_training_rows_match_oracle():
+    scene, sp, a = _arf_case()
+    eng, net = _engine(scene, sp)
+    with eng:
+        rows = net.dataset(a, 300_000, seed=7, first=11)
+    ref, _ = O.arf_dataset(scene.tables_desc, sp, a, 300_000, seed=7, first=11, threads=8)
+    assert rows.shape == ref.shape and len(rows) > 1000
+    np.testing.assert_array_equal(rows[:, 0], ref[:, 0])
+    np.testing.assert_array_equal(rows[:, 3], ref[:, 3])
+    np.testing.assert_allclose(rows[:, 1], ref[:, 1], rtol=0, atol=2e-4)
+    np.testing.assert_allclose(rows[:, 2], ref[:, 2], rtol=0, atol=2e-4)
+
+
+def _rows(n, n_classes, seed):
+    rng = np.random.default_rng(seed)
+    return np.stack([rng.uniform(0.05, 0.25, n), rng.uniform(0, 30, n), rng.uniform(-180, 180, n),
+                     rng.integers(0, n_classes, n)], axis=1).astype(np.float32)
+
+
+def _rel(a, b):
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30))
+
+
+@pytest.mark.parametrize("n_classes", [3, 4])
+def test_forward_and_gradient_match_oracle(n_classes):
+    scene, sp, _ = _arf_case()
+    params = random_params(11 + n_classes, n_classes)
+    rows = _rows(512, n_classes, 3)
+    eng, net = _engine(scene, sp)
+    with eng:
+        net.set_model(_model(n_classes), params.astype(np.float32))
+        p_gpu = net.predict(rows)
+        loss_gpu, g_gpu = net.gradient(rows)
+    p_ref, _ = M.forward(params, rows, MEAN, STD, n_classes, bf16_points=True)
+    np.testing.assert_allclose(p_gpu, p_ref, atol=3e-3)
+    loss_ref, g_ref = M.loss_and_grad(params, rows, MEAN, STD, n_classes, bf16_points=True)
+    _, g64 = M.loss_and_grad(params, rows, MEAN, STD, n_classes, bf16_points=False)
+    assert abs(loss_gpu - loss_ref) < 2e-3 * loss_ref
+    g_gpu = g_gpu.astype(np.float64)
+    for name in ("W1", "b1", "W2", "b2", "W3", "b3", "W4", "b4"):
+        o, size = M.OFF[name]
+        assert _rel(g_gpu[o:o + size], g_ref[o:o + size]) < 2e-2, name
+        assert _rel(g_gpu[o:o + size], g64[o:o + size]) < 6e-2, name
+    assert _rel(g_gpu, g_ref) < 1e-2
+
+
+def test_training_learns_detection_probability():
+    scene, sp, a = _arf_case(rr=5.0)
+    eng, net = _engine(scene, sp)
+    with eng:
+        model, loss = net.train(a, 20_000_000, seed=21, epochs=8, batch=8192, lr=2e-3)
+        held = net.dataset(a, 4_000_000, seed=99)
+        probs = net.predict(held)
+    assert model.n_classes == 3
+    assert np.all(np.isfinite(loss)) and loss[-1] < loss[0]
+    w = M.arf_weights(probs, model.russian_roulette)
+    # measured photopeak fraction (w = 1) vs the network's, undoing the roulette of class 0
+    e, th, cls = held[:, 0], held[:, 1], held[:, 3]
+    keep0 = cls == 0
+    weight = np.where(keep0, model.russian_roulette, 1.0)
+    for lo, hi in ((0.0, 1.5), (1.5, 3.0), (3.0, 6.0)):
+        sel = (th >= lo) & (th < hi) & (e > 0.13)
+        measured = float((weight[sel] * (cls[sel] == 1)).sum() / weight[sel].sum())
+        predicted = float(w[sel, 1].mean())
+        assert abs(predicted - measured) < 0.1 * measured + 2e-3, (lo, hi, measured, predicted)
