@@ -94,6 +94,8 @@ extern "C" {
 #define GG_CNT_SECONDARIES 11   /* annihilation photons created */
 #define GG_CNT_HEAD_STEPS 12    /* transport steps inside SPECT heads */
 #define GG_CNT_SINGLES 13       /* events with energy deposited in a crystal */
+#define GG_CNT_ARF_PHOTONS 14   /* photons at a collimator face scored by the ARF network */
+#define GG_CNT_ARF_FALLBACK 15  /* photons at a head the ARF stage left to plain tracking */
 #define GG_N_COUNTERS 16
 
 /* Physics tables: see opengate_gb300/tables.py for the contract. */
@@ -325,6 +327,21 @@ int gg_arf_predict(gg_ctx *ctx, const float *rows, uint64_t n, float *probs);
 /* Gradient of the mean cross-entropy of n rows (n a multiple of 64) at the
    current parameters, no update: grad[GG_ARF_N_PARAMS], *loss = mean loss. */
 int gg_arf_gradient(gg_ctx *ctx, const float *rows, uint64_t n, float *grad, double *loss);
+
+/* ARF detectors in the SPECT acquisition (GateARFActor::SteppingAction +
+   ARFActor.apply, core/opengate_core/opengate_lib/GateARFActor.cpp:60-113,
+   opengate/actors/arfactors.py:349-415).  With the ARF stage on, a photon
+   that enters a head through the collimator face inside the model's energy
+   / angle domain is scored by the network instead of being tracked: window
+   weights p_k / (russian_roulette p_0 + sum_k>0 p_k) at the pixel where its
+   line crosses the plane distance_to_crystal behind the face.  Photons
+   entering elsewhere or outside the domain are tracked as before (counts in
+   gg_get_projection); photons below every window are dropped.  The model
+   needs n_windows + 1 classes.  gg_get_arf_projection returns the weights
+   (and their history-by-history squares, or NULL) in the projection layout;
+   gg_spect_setup zeroes them. */
+int gg_spect_use_arf(gg_ctx *ctx, int32_t enable);
+int gg_get_arf_projection(gg_ctx *ctx, double *counts, double *squared, size_t n);
 
 /* ---- dose run that allocates no device memory ------------------------------
  * No counterpart in the reference.  For callers that cannot call cudaMalloc

@@ -32,7 +32,7 @@ GG_IMG_EDEP, GG_IMG_EDEP_SQUARED = 0, 1
 GG_N_COUNTERS = 16
 COUNTER_NAMES = ["histories", "woodcock_steps", "real_interactions", "deposits", "tally_entries",
                  "list_overflows", "world_steps", "escaped", "skipped", "loop_capped",
-                 "stack_overflow", "secondaries", "head_steps", "singles", "c14", "c15"]
+                 "stack_overflow", "secondaries", "head_steps", "singles", "arf_photons", "arf_fallback"]
 
 _f32p = ctypes.POINTER(ctypes.c_float)
 _f64p = ctypes.POINTER(ctypes.c_double)
@@ -174,6 +174,8 @@ PROTOTYPES = [
      [ctypes.c_void_p, ctypes.POINTER(ctypes.c_float), ctypes.c_uint64, ctypes.POINTER(ctypes.c_float)]),
     ("gg_arf_gradient", ctypes.c_int,
      [ctypes.c_void_p, ctypes.POINTER(ctypes.c_float), ctypes.c_uint64, ctypes.POINTER(ctypes.c_float), _f64p]),
+    ("gg_spect_use_arf", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
+    ("gg_get_arf_projection", ctypes.c_int, [ctypes.c_void_p, _f64p, _f64p, ctypes.c_size_t]),
     ("gg_arf_dataset", ctypes.c_int,
      [ctypes.c_void_p, ctypes.POINTER(ArfSampling), ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64,
       ctypes.POINTER(ctypes.c_float), ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint64)]),

@@ -96,8 +96,12 @@ struct gg_ctx {
   void *d_records = nullptr;
   size_t rec_cap = 0;
   // SPECT stage queues (head queue, return queue) and their lengths
-  void *d_queue[2] = {nullptr, nullptr};
+  void *d_queue[3] = {nullptr, nullptr, nullptr};  // head, return, ARF fallback
   size_t q_cap = 0;
+  // ARF stage in the SPECT acquisition
+  bool arf_on = false;
+  unsigned long long *d_arf_proj = nullptr, *d_arf_proj2 = nullptr;
+  size_t arf_proj_n = 0;
   unsigned long long *d_qn = nullptr;
 
   // ARF training rows (device): staging, block counts/offsets, rows, identity head frame
@@ -186,7 +190,9 @@ struct gg_ctx {
     dfree(d_labels); dfree(d_maj); dfree(d_spec_e); dfree(d_spec_cdf); dfree(d_acc_box);
     dfree(d_acc_e); dfree(d_acc_e2); dfree(d_edep); dfree(d_edep2);
     dfree(d_counters); dfree(d_next); dfree(d_status); dfree(d_records);
-    dfree(d_queue[0]); dfree(d_queue[1]); dfree(d_qn);
+    dfree(d_queue[0]); dfree(d_queue[1]); dfree(d_queue[2]); dfree(d_qn);
+    dfree(d_arf_proj); dfree(d_arf_proj2);
+    arf_proj_n = 0;
     dfree(d_arf_stage); dfree(d_arf_rows); dfree(d_arf_bcount); dfree(d_arf_boff); dfree(d_arf_total);
     dfree(d_frame_id);
     arf_rows_cap = 0;
@@ -451,6 +457,21 @@ static int arf_model_check(gg_ctx *c, const gg_arf_model *m) {
     if (!(m->x_std[k] > 0.0f)) return c->fail(GG_ERR_ARG, "ARF model: x_std must be > 0");
   if (!(m->russian_roulette >= 1.0)) return c->fail(GG_ERR_ARG, "ARF model: russian_roulette must be >= 1");
   return GG_OK;
+}
+
+// ARF projection tallies (n pixels of the projection layout), zeroed.
+static int arf_projection_alloc(gg_ctx *c, size_t n) {
+  int st;
+  if (n != c->arf_proj_n) {
+    dfree(c->d_arf_proj);
+    dfree(c->d_arf_proj2);
+    c->arf_proj_n = 0;
+    if ((st = c->cuda(cudaMalloc(&c->d_arf_proj, n * 8), "cudaMalloc ARF projection"))) return st;
+    if ((st = c->cuda(cudaMalloc(&c->d_arf_proj2, n * 16), "cudaMalloc ARF projection squared"))) return st;
+    c->arf_proj_n = n;
+  }
+  if ((st = c->cuda(cudaMemsetAsync(c->d_arf_proj, 0, n * 8, c->stream), "memset"))) return st;
+  return c->cuda(cudaMemsetAsync(c->d_arf_proj2, 0, n * 16, c->stream), "memset");
 }
 
 extern "C" {
@@ -722,7 +743,7 @@ static int spect_stages(gg_ctx *c, gg::KernelArgs a, size_t smem, int minb) {
     if (e != cudaSuccess) return c->cuda(e, "occupancy");
     if (bps[stage] < 1) bps[stage] = 1;
   }
-  unsigned long long *nh = c->d_qn, *nr = c->d_qn + 1;
+  unsigned long long *nh = c->d_qn, *nr = c->d_qn + 1, *nf = c->d_qn + 2;
   auto stage_run = [&](int stage, void *in_q, const unsigned long long *in_n, void *out_q,
                        unsigned long long *out_n) -> int {
     gg::StageArgs q{in_q, in_n, out_q, out_n, c->q_cap};
@@ -737,10 +758,53 @@ static int spect_stages(gg_ctx *c, gg::KernelArgs a, size_t smem, int minb) {
                                                         c->stream);
     return c->cuda(e, "SPECT stage launch");
   };
+  // ARF stage between the phantom and the head stage: head queue -> network
+  // (projection weights) + fallback queue for the head stage
+  auto arf_run = [&]() -> int {
+    int st;
+    if ((st = c->cuda(cudaMemsetAsync(nf, 0, sizeof(unsigned long long), c->stream), "memset"))) return st;
+    gg::ArfStageArgs q{};
+    q.in_q = c->d_queue[0];
+    q.in_n = nh;
+    q.out_q = c->d_queue[2];
+    q.out_n = nf;
+    q.q_cap = c->q_cap;
+    q.params = c->d_params;
+    q.wbf = c->d_wbf;
+    for (int k = 0; k < 3; ++k) {
+      q.mean[k] = c->arf.x_mean[k];
+      q.inv_std[k] = 1.0f / c->arf.x_std[k];
+    }
+    q.n_classes = c->arf.n_classes;
+    q.rr = (float)c->arf.russian_roulette;
+    q.e_min = c->arf.e_min;
+    q.e_max = c->arf.e_max;
+    q.cos_theta_max = std::cos(c->arf.theta_max_deg * (M_PI / 180.0));
+    double lo = c->spect.window_lo[0];
+    for (int k = 1; k < c->spect.n_windows; ++k) lo = std::min(lo, c->spect.window_lo[k]);
+    q.e_detect_min = lo;
+    q.dc = c->arf.distance_to_crystal;
+    q.proj = c->d_arf_proj;
+    q.proj2 = c->d_arf_proj2;
+    q.counters = c->d_counters;
+    q.status = c->d_status;
+    cudaError_t e = c->precision == GG_PREC_F64 ? gg::launch_spect_arf<double>(c->scene<double>(), q, c->n_sm, c->stream)
+                                                : gg::launch_spect_arf<float>(c->scene<float>(), q, c->n_sm, c->stream);
+    return c->cuda(e, "ARF stage launch");
+  };
+  auto head_pass = [&]() -> int {
+    int st;
+    if (c->arf_on) {
+      if ((st = arf_run())) return st;
+      return stage_run(1, c->d_queue[2], nf, c->d_queue[1], nr);
+    }
+    return stage_run(1, c->d_queue[0], nh, c->d_queue[1], nr);
+  };
+  const int per_pass = c->arf_on ? 3 : 2;
   int st;
   if ((st = stage_run(0, nullptr, nullptr, c->d_queue[0], nh))) return st;
-  if ((st = stage_run(1, c->d_queue[0], nh, c->d_queue[1], nr))) return st;
-  c->last_stage_launches = 2;
+  if ((st = head_pass())) return st;
+  c->last_stage_launches = per_pass;
   for (int pass = 1;; ++pass) {
     unsigned long long back = 0;
     if ((st = c->cuda(cudaMemcpyAsync(&back, nr, sizeof(back), cudaMemcpyDeviceToHost, c->stream), "queue length")))
@@ -751,8 +815,8 @@ static int spect_stages(gg_ctx *c, gg::KernelArgs a, size_t smem, int minb) {
     // per-photon step cap ends every history, so this loop ends too
     if (pass > 100000) return c->fail(GG_ERR_DOMAIN, "SPECT stages: photons keep returning to the image");
     if ((st = stage_run(0, c->d_queue[1], nr, c->d_queue[0], nh))) return st;
-    if ((st = stage_run(1, c->d_queue[0], nh, c->d_queue[1], nr))) return st;
-    c->last_stage_launches += 2;
+    if ((st = head_pass())) return st;
+    c->last_stage_launches += per_pass;
   }
   return GG_OK;
 }
@@ -780,14 +844,14 @@ static int run_impl(gg_ctx *c, uint64_t n, uint64_t seed, uint64_t first) {
     if (st) return st;
     c->rec_cap = cap;
   }
-  if (c->have_spect && cap > c->q_cap) {
-    dfree(c->d_queue[0]);
-    dfree(c->d_queue[1]);
+  if (c->have_spect && (cap > c->q_cap || (c->arf_on && !c->d_queue[2]))) {
+    for (int k = 0; k < 3; ++k) dfree(c->d_queue[k]);
     c->q_cap = 0;
     size_t qb = c->precision == GG_PREC_F64 ? gg::queue_bytes<double>(cap) : gg::queue_bytes<float>(cap);
     int st = c->cuda(cudaMalloc(&c->d_queue[0], qb), "cudaMalloc head queue");
     if (!st) st = c->cuda(cudaMalloc(&c->d_queue[1], qb), "cudaMalloc return queue");
-    if (!st && !c->d_qn) st = c->cuda(cudaMalloc(&c->d_qn, 2 * sizeof(unsigned long long)), "cudaMalloc queue lengths");
+    if (!st && c->arf_on) st = c->cuda(cudaMalloc(&c->d_queue[2], qb), "cudaMalloc ARF fallback queue");
+    if (!st && !c->d_qn) st = c->cuda(cudaMalloc(&c->d_qn, 3 * sizeof(unsigned long long)), "cudaMalloc queue lengths");
     if (st) return st;
     c->q_cap = cap;
   }
@@ -954,6 +1018,7 @@ int gg_spect_setup(gg_ctx *c, const gg_spect_desc *sp) {
   }
   if ((st = c->cuda(cudaMemsetAsync(c->d_proj, 0, n * 8, c->stream), "memset projections"))) return st;
   if ((st = c->cuda(cudaMemsetAsync(c->d_counters, 0, GG_N_COUNTERS * 8, c->stream), "memset counters"))) return st;
+  if (c->arf_on && (st = arf_projection_alloc(c, n))) return st;
   c->spect = *sp;
   c->have_spect = true;
   c->spect_run = 0;
@@ -1203,6 +1268,46 @@ int gg_arf_train(gg_ctx *c, const gg_arf_sampling *smp, const gg_arf_train_opts 
   if (loss)
     for (int ep = 0; ep < o->epochs; ++ep) loss[ep] = lacc[ep] / ((double)steps_per_epoch * o->batch);
   if (model_out) *model_out = m;
+  return GG_OK;
+}
+
+int gg_spect_use_arf(gg_ctx *c, int32_t enable) {
+  if (!c) return GG_ERR_ARG;
+  cudaSetDevice(c->device);
+  if (!enable) {
+    c->arf_on = false;
+    return GG_OK;
+  }
+  if (!c->have_spect || !c->have_arf) return c->fail(GG_ERR_STATE, "gg_spect_use_arf: needs gg_spect_setup and an ARF model");
+  if (c->arf.n_classes != c->spect.n_windows + 1)
+    return c->fail(GG_ERR_ARG, "gg_spect_use_arf: the model has %d classes, the heads %d windows + 1", c->arf.n_classes,
+                   c->spect.n_windows);
+  c->arf_on = true;
+  int st = arf_projection_alloc(c, c->n_proj);
+  if (st) return st;
+  return c->cuda(cudaStreamSynchronize(c->stream), "ARF projection");
+}
+
+int gg_get_arf_projection(gg_ctx *c, double *counts, double *squared, size_t n) {
+  if (!c || !counts) return GG_ERR_ARG;
+  cudaSetDevice(c->device);
+  if (!c->arf_on || !c->d_arf_proj) return c->fail(GG_ERR_STATE, "gg_get_arf_projection: the ARF stage is off");
+  if (n != c->arf_proj_n) return c->fail(GG_ERR_ARG, "gg_get_arf_projection: buffer has %zu values, need %zu", n, c->arf_proj_n);
+  std::vector<unsigned long long> tmp(n);
+  int st = c->d2h(tmp.data(), c->d_arf_proj, n * 8, "download ARF projection");
+  if (st) return st;
+  for (size_t i = 0; i < n; ++i) counts[i] = (double)tmp[i] * 2.3283064365386963e-10;
+  if (squared) {
+    std::vector<unsigned long long> t2(2 * n);
+    if ((st = c->d2h(t2.data(), c->d_arf_proj2, n * 16, "download ARF projection squared"))) return st;
+    for (size_t i = 0; i < n; ++i) {
+      double lo = (double)t2[2 * i];
+      lo = lo * 5.421010862427522e-20;
+      double hi = (double)t2[2 * i + 1];
+      hi = hi * 2.3283064365386963e-10;
+      squared[i] = hi + lo;
+    }
+  }
   return GG_OK;
 }
 

@@ -1,0 +1,202 @@
+// gg_arf_stage.cu - ARF stage of the SPECT wavefront.
+//
+// Replaces GateARFActor::SteppingAction + ARFActor.apply /
+// arf_build_image_from_projected_points (core/opengate_core/opengate_lib/
+// GateARFActor.cpp:60-113, opengate/actors/arfactors.py:349-415): a photon
+// that reaches a head's collimator face is not tracked through the head;
+// the network gives its probability for every energy window, and the
+// probabilities are added to the projection at the point where its line
+// crosses the crystal plane (distance_to_crystal behind the face).
+//
+// Input is the head queue of the phantom stage.  Per photon:
+//   * energy below every window: dropped (no window can be reached);
+//   * entering through the collimator face, energy and angle inside the
+//     trained domain, no crystal event yet: handled by the network;
+//   * otherwise (side entry, outside the domain): copied to the fallback
+//     queue, which the plain head stage tracks - the plain path both covers
+//     and bounds what the network does not know.
+// The network runs on tiles of 64 queued photons per CTA with the same
+// tensor-core layers as training.  Window weights are w_k = p_k / (RR p_0 +
+// sum_k>0 p_k) (class 0 re-weighted by the Russian roulette of its training
+// rows) and go to fixed-point projection tallies (2^-32 units, with the exact
+// square for the history-by-history variance), so projections are
+// bit-reproducible.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "gg_device.cuh"
+#include "gg_internal.h"
+#include "gg_mlp.cuh"
+#include "gg_physics.cuh"
+#include "gg_queue.cuh"
+#include "gg_spect.cuh"
+
+namespace gg {
+
+constexpr float kArfRadToDeg = 57.295779513082320876f;
+
+template <typename real>
+__device__ __forceinline__ void queue_copy(const PQueue<real> &in, size_t k, const PQueue<real> &out, size_t j) {
+  out.rng_buf[j] = in.rng_buf[k];
+  out.hid[j] = in.hid[k];
+  out.px[j] = in.px[k];
+  out.py[j] = in.py[k];
+  out.pz[j] = in.pz[k];
+  out.dx[j] = in.dx[k];
+  out.dy[j] = in.dy[k];
+  out.dz[j] = in.dz[k];
+  out.e[j] = in.e[k];
+#pragma unroll
+  for (int i = 0; i < 8; ++i) out.ev[i][j] = in.ev[i][k];
+  out.rng_pos[j] = in.rng_pos[k];
+  out.meta[j] = in.meta[k];
+}
+
+enum : int { kArfNone = 0, kArfNet = 1, kArfFallback = 2 };
+
+template <typename real>
+__global__ void __launch_bounds__(kMlpThreads) k_spect_arf(Scene<real> s, ArfStageArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  MlpSmem &sm = *reinterpret_cast<MlpSmem *>(smem_raw);
+  __shared__ long long t_pix[kTileM];  // projection offset of window 1, -1: not scored
+  __shared__ float t_p[kTileM][kOutPad];
+  __shared__ unsigned int n_net, n_fb, n_drop;
+  if (threadIdx.x == 0) {
+    n_net = 0;
+    n_fb = 0;
+    n_drop = 0;
+  }
+  mlp_load_weights(sm, a.params, a.wbf);
+  const PQueue<real> in = PQueue<real>::carve(a.in_q, a.q_cap);
+  const PQueue<real> out = PQueue<real>::carve(a.out_q, a.q_cap);
+  const uint64_t n_items = min((uint64_t)*a.in_n, (uint64_t)a.q_cap);
+  const uint64_t n_tiles = (n_items + kTileM - 1) / kTileM;
+  const unsigned lane = threadIdx.x & 31u;
+  const unsigned lt_mask = (1u << lane) - 1u;
+  const size_t plane = (size_t)s.pny * s.pnx;
+
+  for (uint64_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
+    __syncthreads();  // previous tile done with the shared arrays
+    if (threadIdx.x < kTileM) {  // warps 0 and 1, whole warps
+      const int r = threadIdx.x;
+      const uint64_t k = tile * kTileM + (uint64_t)r;
+      int mode = kArfNone;
+      float x0 = 0.f, x1 = 0.f, x2 = 0.f;
+      long long pix = -1;
+      if (k < n_items) {
+        const uint32_t meta = in.meta[k];
+        const bool has_ev = ((meta >> 23) & 1u) != 0u;
+        const real e = in.e[k];
+        const real lz = in.pz[k];
+        const real dz = in.dz[k];
+        if (has_ev) {
+          mode = kArfFallback;
+        } else if (e < (real)a.e_detect_min) {
+          mode = kArfNone;
+          atomicAdd(&n_drop, 1u);
+        } else if (lz < (real)1e-3 && dz > (real)0 && e >= (real)a.e_min && e <= (real)a.e_max &&
+                   dz >= (real)a.cos_theta_max) {
+          mode = kArfNet;
+          const real dx = in.dx[k], dy = in.dy[k];
+          const float th = acosf((float)dz) * kArfRadToDeg;
+          const float ph = atan2f((float)dy, (float)dx) * kArfRadToDeg;
+          x0 = (th - a.mean[0]) * a.inv_std[0];
+          x1 = (ph - a.mean[1]) * a.inv_std[1];
+          x2 = ((float)e - a.mean[2]) * a.inv_std[2];
+          // the photon's line at the crystal plane (head-local)
+          real t = (real)a.dc / dz;
+          real u = in.px[k] + t * dx;
+          real v = in.py[k] + t * dy;
+          real fx = u + s.pix_half[0];
+          fx = fx * s.inv_psp[0];
+          real fy = v + s.pix_half[1];
+          fy = fy * s.inv_psp[1];
+          if (fx >= (real)0 && fx < (real)s.pnx && fy >= (real)0 && fy < (real)s.pny) {
+            const int i = (int)fx, j = (int)fy;
+            const int head = (int)((meta >> 20) & 1u);
+            const int run = run_of(s, in.hid[k]);
+            pix = (long long)((((size_t)head * s.n_runs + run) * s.n_win) * plane + (size_t)j * s.pnx + i);
+          }
+        } else {
+          mode = kArfFallback;
+        }
+      }
+      const bool fb = mode == kArfFallback;
+      const size_t slot = queue_claim(a.out_n, fb, lane, lt_mask);
+      if (fb) {
+        if (slot < a.q_cap) queue_copy(in, k, out, slot);
+        else atomicOr(a.status, kStatusQueueOverflow);
+        atomicAdd(&n_fb, 1u);
+      }
+      if (mode == kArfNet) atomicAdd(&n_net, 1u);
+      sm.x[r][0] = x0;
+      sm.x[r][1] = x1;
+      sm.x[r][2] = x2;
+      t_pix[r] = pix;
+    }
+    __syncthreads();
+    mlp_layer1(sm);
+    __syncthreads();
+    mlp_hidden(sm.h1, sm.w2, sm.b2, sm.h2);
+    __syncthreads();
+    mlp_hidden(sm.h2, sm.w3, sm.b3, sm.h3);
+    __syncthreads();
+    {
+      float acc[1][2][4];
+      mlp_logits(sm, acc);
+      mlp_softmax(acc, a.n_classes);
+      const int m0 = 16 * (threadIdx.x >> 5);
+#pragma unroll
+      for (int nt = 0; nt < 2; ++nt)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          int rr, cc;
+          acc_pos(q, rr, cc);
+          t_p[m0 + rr][8 * nt + cc] = acc[0][nt][q];
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x < kTileM && t_pix[threadIdx.x] >= 0) {
+      const int r = threadIdx.x;
+      float norm = t_p[r][0] * a.rr;
+      for (int c = 1; c < a.n_classes; ++c) norm += t_p[r][c];
+      const float inv = norm > 0.0f ? 1.0f / norm : 0.0f;
+      for (int c = 1; c < a.n_classes; ++c) {
+        const float w = t_p[r][c] * inv;
+        const unsigned long long q = __float2ull_rn(w * 4294967296.0f);
+        if (!q) continue;
+        const size_t idx = (size_t)t_pix[r] + (size_t)(c - 1) * plane;
+        atomicAdd(a.proj + idx, q);
+        const unsigned long long lo = q * q;
+        const unsigned long long hi = __umul64hi(q, q);
+        atomicAdd(a.proj2 + 2 * idx, lo & 0xffffffffull);
+        atomicAdd(a.proj2 + 2 * idx + 1, (hi << 32) | (lo >> 32));
+      }
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    if (n_net) atomicAdd(&a.counters[GG_CNT_ARF_PHOTONS], (unsigned long long)n_net);
+    if (n_fb) atomicAdd(&a.counters[GG_CNT_ARF_FALLBACK], (unsigned long long)n_fb);
+  }
+}
+
+template <typename real>
+cudaError_t launch_spect_arf(const Scene<real> &s, const ArfStageArgs &a, int grid, cudaStream_t st) {
+  static bool configured = false;
+  if (!configured) {
+    cudaError_t e = cudaFuncSetAttribute(k_spect_arf<real>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)sizeof(MlpSmem));
+    if (e != cudaSuccess) return e;
+    configured = true;
+  }
+  k_spect_arf<real><<<grid, kMlpThreads, sizeof(MlpSmem), st>>>(s, a);
+  return cudaGetLastError();
+}
+
+template cudaError_t launch_spect_arf<float>(const Scene<float> &, const ArfStageArgs &, int, cudaStream_t);
+template cudaError_t launch_spect_arf<double>(const Scene<double> &, const ArfStageArgs &, int, cudaStream_t);
+
+}  // namespace gg

@@ -76,11 +76,34 @@ struct MlpAdamArgs {
   double *loss_acc;
 };
 
+// One launch of the ARF stage of the SPECT wavefront (see gg_arf_stage.cu).
+struct ArfStageArgs {
+  void *in_q;                      // head queue of the phantom stage
+  const unsigned long long *in_n;
+  void *out_q;                     // fallback queue for the plain head stage
+  unsigned long long *out_n;
+  size_t q_cap;
+  const float *params;             // network
+  const __nv_bfloat16 *wbf;
+  float mean[3], inv_std[3];
+  int n_classes;
+  float rr;                        // class-0 Russian-roulette factor of the training rows
+  double e_min, e_max, cos_theta_max;  // trained domain
+  double e_detect_min;             // lowest window edge: photons below reach no window
+  double dc;                       // collimator face -> crystal plane, mm
+  unsigned long long *proj;        // fixed-point window weights, 2^-32 units, projection layout
+  unsigned long long *proj2;       // their squares: (low 32 bits, rest) per pixel, 2^-64 / 2^-32 MeV^2 units
+  unsigned long long *counters;
+  unsigned int *status;
+};
+
 size_t mlp_smem_bytes();
 cudaError_t launch_mlp_train(const MlpTrainArgs &a, int n_tiles, cudaStream_t st);
 cudaError_t launch_mlp_adam(const MlpAdamArgs &a, cudaStream_t st);
 cudaError_t launch_mlp_to_bf16(const float *params, __nv_bfloat16 *wbf, cudaStream_t st);
 cudaError_t launch_mlp_predict(const MlpTrainArgs &a, float *out, uint64_t n, int grid, cudaStream_t st);
+template <typename real>
+cudaError_t launch_spect_arf(const Scene<real> &s, const ArfStageArgs &a, int grid, cudaStream_t st);
 
 template <typename real>
 size_t transport_smem_bytes(int n_comp, int n_e, int n_mat);

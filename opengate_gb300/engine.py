@@ -138,6 +138,19 @@ class SpectEngine(DoseEngine):
     def last_kernel_ms(self):
         return tuple(self.kernel_ms)
 
+    def use_arf(self, enable=True):
+        """ARF detectors (a model must be set on the context, e.g. by ArfNetwork.train)."""
+        self._call("gg_spect_use_arf", 1 if enable else 0)
+
+    def arf_projection(self, squared=False):
+        """ARF window weights (and their history-by-history squares) in the projection layout."""
+        shape = self.spect.projection_shape()
+        n = int(np.prod(shape))
+        out = np.empty(n, dtype=np.float64)
+        sq = np.empty(n, dtype=np.float64) if squared else None
+        self._call("gg_get_arf_projection", C.ptr(out, ctypes.c_double), C.ptr(sq, ctypes.c_double), n)
+        return (out.reshape(shape), sq.reshape(shape)) if squared else out.reshape(shape)
+
     def projection(self):
         shape = self.spect.projection_shape()
         out = np.empty(int(np.prod(shape)), dtype=np.float64)

@@ -413,6 +413,7 @@ typedef struct {
   int mat_coll, mat_cr;
   real wlo[8], whi[8], pix_half[2], inv_psp[2];
   uint64_t *proj; /* [head][run][window][pny][pnx], shared, atomics */
+  const struct arf_s *arf; /* ARF detector model, or NULL */
 } scene_t;
 
 typedef struct {
@@ -548,6 +549,10 @@ typedef struct {
      (-1 none, 0 image, 1 + h head h); head, hreg (0 collimator, 1 gap,
      2 crystal) and left_hole while inside a head */
   int in_head, head, hreg, left_hole, exclude;
+  /* ARF: visited_head = the photon was tracked in a head before (it then
+     always stays with plain tracking); head_stage = it is being tracked with
+     the heads since its last image entry (head-to-head flights skip the ARF) */
+  int visited_head, head_stage;
 } photon_t;
 
 /* per-event crystal accumulation of each head (adder, EnergyWinnerPosition);
@@ -854,6 +859,8 @@ static int inside_box(const real p[3], const real lo[3], const real hi[3]) {
 static void start_photon(const scene_t *s, photon_t *ph) {
   ph->in_head = 0;
   ph->exclude = -1;
+  ph->visited_head = 0;
+  ph->head_stage = 0;
   if (inside_box(ph->pos, s->bmin, s->bmax)) {
     ph->in_image = 1;
     ph->t_exit = exit_distance(ph->pos, ph->dir, s->bmin, s->bmax);
@@ -1083,6 +1090,109 @@ static void head_step(const scene_t *s, photon_t *ph, rng_t *g, tally_t *t, even
   }
 }
 
+/* ---- ARF detector ------------------------------------------------------- */
+/* The network of the ARF stage (3 -> 128 -> 128 -> 128 -> nc, softmax) in
+   FP64, with W2, W3, W4 and the hidden activations rounded to bfloat16 where
+   the GPU stores them; window weights p_k / (rr p_0 + sum_k>0 p_k) go to
+   fixed-point projection tallies like the GPU's (2^-32 units). */
+typedef struct arf_s {
+  int nc;
+  double w1[128 * 3], b1[128], w2[128 * 128], b2[128], w3[128 * 128], b3[128], w4[16 * 128], b4[16];
+  float mean[3], inv[3];
+  double rr;
+  real emin, emax, ctmax, edet, dc;
+  uint64_t *proj, *proj2;
+} arf_t;
+
+static double bf16r(double x) {
+  float f = (float)x;
+  uint32_t b;
+  memcpy(&b, &f, 4);
+  b = (b + 0x7FFFu + ((b >> 16) & 1u)) & 0xFFFF0000u;
+  memcpy(&f, &b, 4);
+  return (double)f;
+}
+
+static void arf_forward(const arf_t *a, const float x[3], double *p) {
+  double h1[128], h2[128], h3[128];
+  for (int j = 0; j < 128; ++j) {
+    double z = a->b1[j] + a->w1[3 * j] * x[0] + a->w1[3 * j + 1] * x[1] + a->w1[3 * j + 2] * x[2];
+    h1[j] = bf16r(z > 0 ? z : 0);
+  }
+  for (int j = 0; j < 128; ++j) {
+    double z = a->b2[j];
+    for (int i = 0; i < 128; ++i) z += a->w2[128 * j + i] * h1[i];
+    h2[j] = bf16r(z > 0 ? z : 0);
+  }
+  for (int j = 0; j < 128; ++j) {
+    double z = a->b3[j];
+    for (int i = 0; i < 128; ++i) z += a->w3[128 * j + i] * h2[i];
+    h3[j] = bf16r(z > 0 ? z : 0);
+  }
+  double mx = -INFINITY, sum = 0;
+  for (int c = 0; c < a->nc; ++c) {
+    double z = a->b4[c];
+    for (int i = 0; i < 128; ++i) z += a->w4[128 * c + i] * h3[i];
+    p[c] = z;
+    if (z > mx) mx = z;
+  }
+  for (int c = 0; c < a->nc; ++c) {
+    p[c] = exp(p[c] - mx);
+    sum += p[c];
+  }
+  for (int c = 0; c < a->nc; ++c) p[c] /= sum;
+}
+
+/* A photon entering a head from the phantom side: plain tracking (returns),
+   dropped, or scored by the network (photon ends). */
+static void arf_at_head(const scene_t *s, photon_t *ph, tally_t *t) {
+  const arf_t *a = s->arf;
+  if (ph->visited_head) {
+    t->cnt[GG_CNT_ARF_FALLBACK]++;
+    return;
+  }
+  real e = ph->e, lz = ph->pos[2], dz = ph->dir[2];
+  if (e < a->edet) {
+    ph->alive = 0;
+    ph->in_head = 0;
+    return;
+  }
+  if (!(lz < (real)1e-3 && dz > R(0) && e >= a->emin && e <= a->emax && dz >= a->ctmax)) {
+    t->cnt[GG_CNT_ARF_FALLBACK]++;
+    return;
+  }
+  t->cnt[GG_CNT_ARF_PHOTONS]++;
+  float th = acosf((float)dz) * 57.295779513082320876f;
+  float phi = atan2f((float)ph->dir[1], (float)ph->dir[0]) * 57.295779513082320876f;
+  float x[3] = {(th - a->mean[0]) * a->inv[0], (phi - a->mean[1]) * a->inv[1], ((float)e - a->mean[2]) * a->inv[2]};
+  real tt = a->dc / dz;
+  real u = ph->pos[0] + tt * ph->dir[0];
+  real v = ph->pos[1] + tt * ph->dir[1];
+  real fx = u + s->pix_half[0];
+  fx = fx * s->inv_psp[0];
+  real fy = v + s->pix_half[1];
+  fy = fy * s->inv_psp[1];
+  ph->alive = 0;
+  ph->in_head = 0;
+  if (!(fx >= R(0) && fx < (real)s->pnx && fy >= R(0) && fy < (real)s->pny)) return;
+  int i = (int)fx, j = (int)fy;
+  double p[16];
+  arf_forward(a, x, p);
+  double norm = a->rr * p[0];
+  for (int c = 1; c < a->nc; ++c) norm += p[c];
+  size_t plane = (size_t)s->pny * s->pnx;
+  for (int c = 1; c < a->nc; ++c) {
+    double w = norm > 0 ? p[c] / norm : 0.0;
+    uint64_t q = (uint64_t)llrint(w * 4294967296.0);
+    if (!q) continue;
+    size_t idx = ((((size_t)ph->head * s->n_runs + s->run) * s->n_win + (c - 1)) * plane) + (size_t)j * s->pnx + i;
+    unsigned __int128 sq = (unsigned __int128)q * q;
+    __atomic_fetch_add(&a->proj[idx], q, __ATOMIC_RELAXED);
+    __atomic_fetch_add(&a->proj2[2 * idx], (uint64_t)sq & 0xffffffffu, __ATOMIC_RELAXED);
+    __atomic_fetch_add(&a->proj2[2 * idx + 1], (uint64_t)(sq >> 32), __ATOMIC_RELAXED);
+  }
+}
+
 /* World step with the image box and the head boxes as possible targets. */
 static void spect_world_step(const scene_t *s, photon_t *ph, rng_t *g, tally_t *t, photon_t *sec,
                              int *has_sec) {
@@ -1118,6 +1228,7 @@ static void spect_world_step(const scene_t *s, photon_t *ph, rng_t *g, tally_t *
     if (box == 0) {
       ph->in_image = 1;
       ph->t_exit = exit_distance(ph->pos, ph->dir, s->bmin, s->bmax);
+      ph->head_stage = 0;
     } else {
       int h = box - 1;
       real lp[3], ld[3];
@@ -1130,6 +1241,11 @@ static void spect_world_step(const scene_t *s, photon_t *ph, rng_t *g, tally_t *
       ph->head = h;
       ph->hreg = lp[2] < s->zb[1] ? 0 : (lp[2] < s->zb[2] ? 1 : 2);
       ph->left_hole = 0;
+      if (s->arf && !ph->head_stage) arf_at_head(s, ph, t);
+      if (ph->alive) {
+        ph->visited_head = 1;
+        ph->head_stage = 1;
+      }
     }
   } else {
     ph->alive = 0;
@@ -1462,14 +1578,15 @@ int GGO_PREFIX(run_dose)(const gg_tables_desc *tb, const gg_volume_desc *vol, co
    frames[r][n_heads][12]) simulates histories [first + r * n_per_run,
    first + (r + 1) * n_per_run) and adds singles counts into proj
    ([head][run][window][pny][pnx], zeroed by the caller). */
-int GGO_PREFIX(run_spect)(const gg_tables_desc *tb, const gg_volume_desc *vol, const gg_world_desc *w,
+static int run_spect_impl(const gg_tables_desc *tb, const gg_volume_desc *vol, const gg_world_desc *w,
                           const gg_source_desc *src, const gg_spect_desc *sp, const double *frames,
                           uint64_t seed, uint64_t first, uint64_t n_per_run, int n_threads, uint64_t *proj,
-                          uint64_t *counters) {
+                          uint64_t *counters, const arf_t *arf) {
   scene_t s;
   scene_init(&s, tb, vol, w, src);
   spect_init(&s, sp);
   s.proj = proj;
+  s.arf = arf;
   if (n_threads < 1) n_threads = 1;
   worker_t *ws = (worker_t *)calloc((size_t)n_threads, sizeof(worker_t));
   pthread_t *th = (pthread_t *)calloc((size_t)n_threads, sizeof(pthread_t));
@@ -1655,6 +1772,60 @@ int GGO_PREFIX(arf_dataset)(const gg_tables_desc *tb, const gg_spect_desc *sp, c
   free(maj);
   scene_free(&s);
   return GG_OK;
+}
+
+int GGO_PREFIX(run_spect)(const gg_tables_desc *tb, const gg_volume_desc *vol, const gg_world_desc *w,
+                          const gg_source_desc *src, const gg_spect_desc *sp, const double *frames,
+                          uint64_t seed, uint64_t first, uint64_t n_per_run, int n_threads, uint64_t *proj,
+                          uint64_t *counters) {
+  return run_spect_impl(tb, vol, w, src, sp, frames, seed, first, n_per_run, n_threads, proj, counters, NULL);
+}
+
+/* SPECT with ARF detectors (the GPU's gg_spect_use_arf): as run_spect, with
+   the network `params` (GG_ARF_N_PARAMS floats) of `model` applied where a
+   photon reaches a head from the phantom side; window weights go to
+   arf_proj / arf_proj2 (fixed point, 2^-32 and 2^-64 / 2^-32 units, zeroed by
+   the caller). */
+int GGO_PREFIX(run_spect_arf)(const gg_tables_desc *tb, const gg_volume_desc *vol, const gg_world_desc *w,
+                              const gg_source_desc *src, const gg_spect_desc *sp, const double *frames,
+                              uint64_t seed, uint64_t first, uint64_t n_per_run, int n_threads, uint64_t *proj,
+                              uint64_t *counters, const gg_arf_model *m, const float *params, uint64_t *arf_proj,
+                              uint64_t *arf_proj2) {
+  arf_t *a = (arf_t *)calloc(1, sizeof(arf_t));
+  a->nc = m->n_classes;
+  const float *pw = params;
+  for (int k = 0; k < 128 * 3; ++k) a->w1[k] = pw[k];
+  pw += 128 * 3;
+  for (int k = 0; k < 128; ++k) a->b1[k] = pw[k];
+  pw += 128;
+  for (int k = 0; k < 128 * 128; ++k) a->w2[k] = bf16r(pw[k]);
+  pw += 128 * 128;
+  for (int k = 0; k < 128; ++k) a->b2[k] = pw[k];
+  pw += 128;
+  for (int k = 0; k < 128 * 128; ++k) a->w3[k] = bf16r(pw[k]);
+  pw += 128 * 128;
+  for (int k = 0; k < 128; ++k) a->b3[k] = pw[k];
+  pw += 128;
+  for (int k = 0; k < 16 * 128; ++k) a->w4[k] = bf16r(pw[k]);
+  pw += 16 * 128;
+  for (int k = 0; k < 16; ++k) a->b4[k] = pw[k];
+  for (int k = 0; k < 3; ++k) {
+    a->mean[k] = m->x_mean[k];
+    a->inv[k] = 1.0f / m->x_std[k];
+  }
+  a->rr = m->russian_roulette;
+  a->emin = (real)m->e_min;
+  a->emax = (real)m->e_max;
+  a->ctmax = (real)cos(m->theta_max_deg * (M_PI / 180.0));
+  double lo = sp->window_lo[0];
+  for (int k = 1; k < sp->n_windows; ++k) lo = sp->window_lo[k] < lo ? sp->window_lo[k] : lo;
+  a->edet = (real)lo;
+  a->dc = (real)m->distance_to_crystal;
+  a->proj = arf_proj;
+  a->proj2 = arf_proj2;
+  int st = run_spect_impl(tb, vol, w, src, sp, frames, seed, first, n_per_run, n_threads, proj, counters, a);
+  free(a);
+  return st;
 }
 
 /* ---- small exported probes for the unit tests ---- */

@@ -202,3 +202,33 @@ def arf_dataset(tables_desc, spect, sampling, n, seed, first=0, threads=8, preci
     if st != 0:
         raise RuntimeError(f"oracle ARF dataset failed with status {st}")
     return rows[: m.value].copy(), {name: int(cnt[i]) for i, name in enumerate(C.COUNTER_NAMES)}
+
+
+def run_spect_arf(scene, spect, n_per_run, seed, model, params, first=0, threads=1, precision=32):
+    """Oracle SPECT run with ARF detectors: (counts, arf_counts, arf_squared, counters), projection layout."""
+    L = lib(precision)
+    fn = getattr(L, f"ggo{precision}_run_spect_arf")
+    fn.restype = ctypes.c_int
+    fn.argtypes = [ctypes.POINTER(C.TablesDesc), ctypes.POINTER(C.VolumeDesc), ctypes.POINTER(C.WorldDesc),
+                   ctypes.POINTER(C.SourceDesc), ctypes.POINTER(C.SpectDesc), ctypes.POINTER(ctypes.c_double),
+                   ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int,
+                   ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(C.ArfModel),
+                   ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64)]
+    shape = spect.projection_shape()
+    n = int(np.prod(shape))
+    proj = np.zeros(n, dtype=np.uint64)
+    aproj = np.zeros(n, dtype=np.uint64)
+    aproj2 = np.zeros(2 * n, dtype=np.uint64)
+    cnt = np.zeros(C.GG_N_COUNTERS, dtype=np.uint64)
+    desc = spect.desc()
+    frames = spect.all_frames()
+    params = np.ascontiguousarray(params, dtype=np.float32)
+    st = fn(*_descs(scene), ctypes.byref(desc), C.ptr(frames, ctypes.c_double), seed, first, n_per_run, threads,
+            C.ptr(proj, ctypes.c_uint64), C.ptr(cnt, ctypes.c_uint64), ctypes.byref(model),
+            C.ptr(params, ctypes.c_float), C.ptr(aproj, ctypes.c_uint64), C.ptr(aproj2, ctypes.c_uint64))
+    if st != 0:
+        raise RuntimeError(f"oracle SPECT ARF run failed with status {st}")
+    arf = aproj.astype(np.float64) * 2.0 ** -32
+    arf2 = aproj2[1::2].astype(np.float64) * 2.0 ** -32 + aproj2[0::2].astype(np.float64) * 2.0 ** -64
+    return (proj.astype(np.float64).reshape(shape), arf.reshape(shape), arf2.reshape(shape),
+            {name: int(cnt[i]) for i, name in enumerate(C.COUNTER_NAMES)})

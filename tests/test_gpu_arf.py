@@ -108,3 +108,39 @@ def test_training_learns_detection_probability():
         measured = float((weight[sel] * (cls[sel] == 1)).sum() / weight[sel].sum())
         predicted = float(w[sel, 1].mean())
         assert abs(predicted - measured) < 0.1 * measured + 2e-3, (lo, hi, measured, predicted)
+
+
+@pytest.mark.parametrize("rr", [1.0, 7.0])
+def test_arf_stage_matches_oracle(rr):
+    """SPECT with ARF detectors: tracked counts bit for bit, network weights within FP32 rounding."""
+    from opengate_gb300.engine import SpectEngine
+
+    scene, sp, _ = W.spect_phantom(shape=(40, 64, 64), spacing=4.8, n_runs=3)
+    n_classes = sp.n_windows + 1
+    params = random_params(31, n_classes).astype(np.float32)
+    model = _model(n_classes, rr=rr)
+    model.e_min, model.e_max, model.theta_max_deg, model.distance_to_crystal = 0.10, 0.16, 12.0, 39.8
+    n = 60_000
+    with SpectEngine(scene, sp) as eng:
+        from opengate_gb300.engine import ArfNetwork
+
+        ArfNetwork(eng).set_model(model, params)
+        eng.use_arf(True)
+        eng.reset()
+        eng.run(n, seed=5)
+        counts, arf, arf2, cnt = eng.projection(), *eng.arf_projection(squared=True), eng.counters()
+    ref, rarf, rarf2, rcnt = O.run_spect_arf(scene, sp, n, 5, model, params, threads=8)
+    np.testing.assert_array_equal(counts, ref)
+    assert cnt == rcnt
+    assert cnt["arf_photons"] > 1000 and cnt["arf_fallback"] > 1000
+    assert arf.sum() > 0
+    # per photon the GPU and oracle networks differ by FP32 accumulation order;
+    # a BF16 rounding flip of a hidden activation (rare) moves one photon's
+    # weight by up to ~2 %
+    for got, want in ((arf, rarf), (arf2, rarf2)):
+        close = np.isclose(got, want, rtol=4e-3, atol=2e-6 * want.max())
+        assert close.mean() > 0.999
+        assert np.abs(got - want).max() < 0.02
+        for w in range(sp.n_windows):
+            tot, rtot = got[:, w::sp.n_windows].sum(), want[:, w::sp.n_windows].sum()
+            assert abs(tot - rtot) <= 2e-4 * rtot + 1e-6
