@@ -42,6 +42,18 @@ SPECT_YIELD = 0.89
 SPECT_WORKLOAD = ("spect_tc99m_lehr_2heads_60angles_r250mm_128x128x4.42mm_windows126-154_108-126keV_"
                   "ct_phantom_256x256x160_1.2mm")
 
+# SPECT with ARF detectors: Lu-177 (113 keV 6.2 %, 208 keV 10.4 %), medium-energy
+# collimator, 120 gantry positions, 1e10 decays; the network is trained on
+# 2e8 photons of the plain collimator tracking, and the plain acquisition of
+# the same decays is run beside it for the matched-sigma comparison
+ARF_METRIC = "primaries/s at matched sigma (ARF GPU vs plain GPU collimator tracking, SPECT projections)"
+ARF_DECAYS = 10_000_000_000
+ARF_YIELD = 0.166
+ARF_WINDOWS = ((0.1872, 0.2288), (0.166, 0.187), (0.1017, 0.1243))
+ARF_TRAIN_SAMPLES = 200_000_000
+ARF_WORKLOAD = ("spect_lu177_melp_2heads_120angles_r250mm_128x128x4.42mm_windows187-229_166-187_101-125keV_"
+                "ct_phantom_256x256x160_1.2mm_arf_mlp3x128_bf16")
+
 
 def measured_peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
@@ -291,6 +303,8 @@ def run_ours_spect(args, ws, rank, local, dist, use_cuda):
                 counters = eng.counters()
                 transport_ms = tt
                 stage_ms = {"generate": tg, "transport": tt, "flush": tf}
+                ph_ms, hd_ms, _ = eng.last_stage_ms()
+                stage_ms.update({"phantom_stage": ph_ms, "head_stage": hd_ms})
                 launches_last = nl
         torch.cuda.synchronize()
     wall = time.perf_counter() - t0
@@ -317,11 +331,12 @@ def run_ours_spect(args, ws, rank, local, dist, use_cuda):
     e2e_s = dist_max(dist, float(np.mean(e2e_t)), use_cuda)
 
     peak_bw, peak_kind = measured_peaks()
-    bytes_alg = 32.0 * counters["woodcock_steps"] + 8.0 * counters["singles"]
-    achieved = bytes_alg / (transport_ms / 1e3) / 1e9
+    # dominant kernel: the phantom stage (label gathers of its Woodcock steps)
+    bytes_alg = 32.0 * counters["woodcock_steps"]
+    achieved = bytes_alg / (stage_ms["phantom_stage"] / 1e3) / 1e9
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak_bw, "unit": "GB/s",
                 "frac": achieved / peak_bw, "traffic": args.traffic, "peak_kind": peak_kind,
-                "kernel": "k_spect_phantom<float> + k_spect_head<float> (phantom and head stages)",
+                "kernel": "k_spect_phantom<float> (phantom stage)",
                 "bytes_alg_per_step": bytes_alg,
                 "units": {"woodcock_steps": counters["woodcock_steps"], "head_steps": counters["head_steps"],
                           "singles": counters["singles"], "launches_per_step": launches_last},
@@ -358,6 +373,159 @@ def run_ours_spect(args, ws, rank, local, dist, use_cuda):
     return 0
 
 
+def projection_sigma(tot, tot2, n, n_win):
+    """(per-pixel sigma of the peak window as for the plain bench, mean relative
+    uncertainty of the per-projection window totals)."""
+    from opengate_gb300 import spect as S
+
+    pix = S.mean_relative_uncertainty(tot[:, 0::n_win], tot2[:, 0::n_win], n)
+    # per projection (head, position, window): totals and history-by-history squares
+    t = tot.sum(axis=(2, 3))
+    t2 = tot2.sum(axis=(2, 3))  # a history adds to one pixel of a projection at most
+    rel = S.compute_history_by_history_relative_uncertainty(t, t2, n)
+    return pix, float(rel[t > 0].mean())
+
+
+def run_ours_arf(args, ws, rank, local, dist, use_cuda):
+    import torch
+
+    from opengate_gb300 import spect as S
+    from opengate_gb300 import workloads as W
+    from opengate_gb300.engine import ArfNetwork, SpectEngine
+
+    scene, sp, _ = W.spect_phantom(nuclide=W.LU177, collimator=S.MELP, n_runs=120, windows=ARF_WINDOWS)
+    n_step = args.primaries if args.primaries != PRIMARIES_PER_STEP else int(ARF_DECAYS * ARF_YIELD)
+    n_per_run = n_step // sp.n_runs
+    n = n_per_run * sp.n_runs
+    nw = sp.n_windows
+    eng = SpectEngine(scene, sp, device=local, precision=32, batch=min(args.batch, 1 << 26))
+    net = ArfNetwork(eng)
+    # training (not timed): rows from the plain head transport, theta uniform to 85 degrees
+    smp = ArfNetwork.sampling(min(lo for lo, _ in ARF_WINDOWS), 0.21, 85.0, (200.0, 200.0), 40.0)
+    t0 = time.perf_counter()
+    model, loss = net.train(smp, args.arf_train_samples, seed=args.seed + 7, epochs=args.arf_epochs, batch=8192,
+                            lr=2e-3, lr_final=1e-5)
+    train_s = time.perf_counter() - t0
+    l2_flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=f"cuda:{local}")
+
+    def first_of(step):
+        return ((rank * (args.warmup + args.steps + 8)) + step) * n
+
+    def acquire(arf, step):
+        eng.use_arf(arf)
+        l2_flush.zero_()
+        torch.cuda.synchronize()
+        eng.reset()
+        eng.run(n_per_run, args.seed, first_of(step))
+        tg, tt, tf, nl = eng.last_kernel_ms()
+        return tg + tt + tf, nl
+
+    for w in range(args.warmup):
+        acquire(True, w)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    dev_ms, launches = [], 0
+    t0 = time.perf_counter()
+    with ClockSampler(local) as clk:
+        for k in range(args.steps):
+            ms, nl = acquire(True, args.warmup + k)
+            dev_ms.append(ms)
+            launches += nl
+        torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    if dist:
+        dist.barrier()
+    total_ms = dist_max(dist, float(np.sum(dev_ms)), use_cuda)
+    value = ws * n * args.steps / (total_ms / 1e3)
+    counters = eng.counters()
+    ph_ms, hd_ms, arf_ms = eng.last_stage_ms()
+    a_counts, (a_w, a_w2) = eng.projection(), eng.arf_projection(squared=True)
+    tot_a, tot2_a = a_counts + a_w, a_counts + a_w2
+    stage_ms = dict(zip(("generate", "transport", "flush"), eng.last_kernel_ms()[:3]))
+    stage_ms.update({"phantom_stage": ph_ms, "head_stage": hd_ms, "arf_stage": arf_ms})
+    # the plain acquisition of the same histories (last timed step) for the matched-sigma comparison
+    plain_ms, _ = acquire(False, args.warmup + args.steps - 1)
+    tot_p = eng.projection()
+    sig_a = projection_sigma(tot_a, tot2_a, n, nw)
+    sig_p = projection_sigma(tot_p, tot_p, n, nw)
+    t_a = total_ms / args.steps
+    gain_pix = (sig_p[0] ** 2 * plain_ms) / (sig_a[0] ** 2 * t_a)
+    gain_proj = (sig_p[1] ** 2 * plain_ms) / (sig_a[1] ** 2 * t_a)
+    win_ratio = [float(tot_a[:, k::nw].sum() / max(tot_p[:, k::nw].sum(), 1e-30)) for k in range(nw)]
+
+    # e2e through the C ABI with host buffers: scene + heads + network upload, acquisition, projections download
+    params = net.params()
+    h2d = scene.labels.nbytes + scene._sig.nbytes + scene._cum.nbytes + scene._ray_amax.nbytes + \
+        scene._ray_cum.nbytes + scene.majorant.nbytes + scene.source_desc_bytes() + sp.all_frames().nbytes + \
+        params.nbytes
+    d2h = 3 * int(np.prod(sp.projection_shape())) * 8
+    torch.cuda.synchronize()
+    e2e_t = []
+    for k in range(max(1, min(args.steps, 2))):
+        t1 = time.perf_counter()
+        eng.upload()
+        net.set_model(model, params)
+        eng.use_arf(True)
+        eng.run(n_per_run, args.seed, first_of(args.warmup + args.steps + 1 + k))
+        eng.projection()
+        eng.arf_projection(squared=True)
+        e2e_t.append(time.perf_counter() - t1)
+    e2e_s = dist_max(dist, float(np.mean(e2e_t)), use_cuda)
+    # the network's arithmetic: forward FLOP per scored photon
+    flop_photon = 2.0 * (3 * 128 + 2 * 128 * 128 + 128 * 16)
+    peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
+        os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
+    if rank == 0:
+        line = {
+            "metric": ARF_METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 transport, bf16 network (f32 accumulate)",
+            "data": "synthetic (seeded CT phantom + activity image)",
+            "config": {"workload": ARF_WORKLOAD, "primaries_per_step": n, "decays_per_step": n / ARF_YIELD,
+                       "l2": "flushed between steps (256 MiB write)", "training_samples": args.arf_train_samples,
+                       "parallelism": f"replicas x{ws}, disjoint history ranges"},
+            "matched_sigma": {
+                "plain_primaries_per_s": n / (plain_ms / 1e3),
+                "plain_equivalent_primaries_per_s_pixel": value * sig_p[0] ** 2 / sig_a[0] ** 2,
+                "plain_equivalent_primaries_per_s_projection": value * sig_p[1] ** 2 / sig_a[1] ** 2,
+                "sigma_pixel": {"arf": sig_a[0], "plain": sig_p[0]},
+                "sigma_projection_total": {"arf": sig_a[1], "plain": sig_p[1]},
+                "efficiency_gain_pixel": gain_pix, "efficiency_gain_projection": gain_proj,
+                "window_counts_arf_over_plain": win_ratio,
+                "note": "efficiency = 1 / (sigma^2 T), contrib/spect/spect_helpers.py:480-488, 582-591"},
+            "training": {"seconds": train_s, "loss_first_last": [float(loss[0]), float(loss[-1])],
+                         "epochs": args.arf_epochs},
+            "e2e": {"value": ws * n / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h)},
+            "roofline": {"bound": "hbm", "kernel": "k_spect_phantom<float> (phantom stage, dominant)",
+                         "achieved": 32.0 * counters["woodcock_steps"] / (ph_ms / 1e3) / 1e9,
+                         "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
+                         "frac": 32.0 * counters["woodcock_steps"] / (ph_ms / 1e3) / 1e9 / peaks.get("hbm_gbs", 1.0),
+                         "traffic": args.traffic, "bytes_alg_per_step": 32.0 * counters["woodcock_steps"]},
+            "roofline_network": {"bound": "tensor", "kernel": "k_spect_arf<float> (ARF stage, network layers)",
+                                 "flop_per_scored_photon": flop_photon,
+                                 "scored_photons_per_step": counters["arf_photons"],
+                                 "achieved": flop_photon * counters["arf_photons"] / (arf_ms / 1e3) / 1e12,
+                                 "peak": peaks.get("bf16_tflops"), "unit": "TFLOP/s",
+                                 "frac": flop_photon * counters["arf_photons"] / (arf_ms / 1e3) / 1e12 /
+                                 peaks.get("bf16_tflops", 1.0),
+                                 "note": "mma.sync m16n8k16 BF16, FP32 accumulate; arf_stage_ms includes the "
+                                         "queue classification and the projection atomics"},
+            "units": {k: counters[k] for k in ("woodcock_steps", "head_steps", "arf_photons", "arf_fallback", "singles")},
+            "stage_ms_per_step": stage_ms,
+            "cpu_baseline": None,
+            "clocks": clk.summary(),
+            "gpu_launches": int(launches),
+            "wall_s": wall,
+        }
+        print(json.dumps(line), flush=True)
+    eng.close()
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
 def run_ours(args):
     ws, rank, local = dist_env()
     import torch
@@ -369,6 +537,8 @@ def run_ours(args):
     dist = dist_init(ws, use_cuda)
     if args.workload == "spect":
         return run_ours_spect(args, ws, rank, local, dist, use_cuda)
+    if args.workload == "spect_arf":
+        return run_ours_arf(args, ws, rank, local, dist, use_cuda)
     from opengate_gb300 import _capi as C
     from opengate_gb300 import workloads as W
     from opengate_gb300.engine import DoseEngine
@@ -479,9 +649,12 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="dose", choices=["dose", "spect"],
-                    help="dose: CT phantom DoseActor (default); spect: Tc-99m SPECT acquisition, 60 positions")
+    ap.add_argument("--workload", default="dose", choices=["dose", "spect", "spect_arf"],
+                    help="dose: CT phantom DoseActor (default); spect: Tc-99m SPECT acquisition, 60 positions; "
+                         "spect_arf: Lu-177 SPECT with ARF detectors vs plain tracking, 120 positions")
     ap.add_argument("--primaries", type=int, default=PRIMARIES_PER_STEP)
+    ap.add_argument("--arf-train-samples", type=int, default=ARF_TRAIN_SAMPLES)
+    ap.add_argument("--arf-epochs", type=int, default=80)
     ap.add_argument("--batch", type=int, default=1 << 27)
     ap.add_argument("--seed", type=int, default=20240611)
     ap.add_argument("--no-cpu", action="store_true")

@@ -199,14 +199,18 @@ typedef struct {
    contrib/spect/ge_discovery_nm670.py:994-1027 add_source_for_arf_training_dataset /
    add_actor_for_arf_training_dataset): photons start on the collimator front
    face of one head, position uniform in |a1| <= half_extent[0],
-   |a2| <= half_extent[1], direction isotropic in the cone theta <=
-   acos(cos_theta_max) about the head normal (into the head), energy uniform
-   in [e_min, e_max]. */
+   |a2| <= half_extent[1], direction in the cone theta <= acos(cos_theta_max)
+   about the head normal (into the head) - isotropic, or with theta uniform
+   in [0, theta_max] when theta_uniform is set (more rows near the hole axis,
+   where the detection probability varies; the network learns the window
+   probability given the direction, which does not depend on how the
+   directions were drawn) - and energy uniform in [e_min, e_max]. */
 typedef struct {
   double e_min, e_max;      /* MeV */
   double cos_theta_max;
   double half_extent[2];    /* mm */
   double russian_roulette;  /* rows of photons detected in no window are kept with probability 1 / this (>= 1) */
+  int32_t theta_uniform;    /* 0: isotropic directions, 1: theta uniform */
 } gg_arf_sampling;
 
 typedef struct gg_ctx gg_ctx;
@@ -308,6 +312,7 @@ typedef struct {
   int32_t batch;        /* rows per Adam step, a multiple of 64, <= 65536 */
   int32_t epochs;
   float lr, beta1, beta2, eps;
+  float lr_final;       /* learning rate decays exponentially from lr to lr_final over the steps (0: constant) */
 } gg_arf_train_opts;
 
 /* Generates the training rows of `sampling` on the device and trains the
@@ -341,6 +346,9 @@ int gg_arf_gradient(gg_ctx *ctx, const float *rows, uint64_t n, float *grad, dou
    (and their history-by-history squares, or NULL) in the projection layout;
    gg_spect_setup zeroes them. */
 int gg_spect_use_arf(gg_ctx *ctx, int32_t enable);
+/* Device time of the last gg_run / gg_spect_run per SPECT stage (sums of
+   CUDA-event intervals around the stage launches, ms). */
+int gg_last_stage_ms(gg_ctx *ctx, double *phantom_ms, double *head_ms, double *arf_ms);
 int gg_get_arf_projection(gg_ctx *ctx, double *counts, double *squared, size_t n);
 
 /* ---- dose run that allocates no device memory ------------------------------

@@ -96,6 +96,7 @@ class ArfSampling(ctypes.Structure):
         ("cos_theta_max", ctypes.c_double),
         ("half_extent", ctypes.c_double * 2),
         ("russian_roulette", ctypes.c_double),
+        ("theta_uniform", ctypes.c_int32),
     ]
 
 
@@ -123,6 +124,7 @@ class ArfTrainOpts(ctypes.Structure):
         ("beta1", ctypes.c_float),
         ("beta2", ctypes.c_float),
         ("eps", ctypes.c_float),
+        ("lr_final", ctypes.c_float),
     ]
 
 
@@ -175,6 +177,7 @@ PROTOTYPES = [
     ("gg_arf_gradient", ctypes.c_int,
      [ctypes.c_void_p, ctypes.POINTER(ctypes.c_float), ctypes.c_uint64, ctypes.POINTER(ctypes.c_float), _f64p]),
     ("gg_spect_use_arf", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
+    ("gg_last_stage_ms", ctypes.c_int, [ctypes.c_void_p, _f64p, _f64p, _f64p]),
     ("gg_get_arf_projection", ctypes.c_int, [ctypes.c_void_p, _f64p, _f64p, ctypes.c_size_t]),
     ("gg_arf_dataset", ctypes.c_int,
      [ctypes.c_void_p, ctypes.POINTER(ArfSampling), ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64,

@@ -125,6 +125,10 @@ struct gg_ctx {
   std::vector<cudaEvent_t> ev;
   double last_generate_ms = 0, last_transport_ms = 0, last_flush_ms = 0;
   int last_launches = 0, last_stage_launches = 0, run_stage_launches = 0;
+  // SPECT stage timing of the last run: events around each stage launch
+  std::vector<cudaEvent_t> stage_ev;
+  std::vector<int> stage_kind;  // 0 phantom, 1 head, 2 ARF, per event pair
+  double stage_ms[3] = {0, 0, 0};
 
   int fail(int code, const char *fmt, ...) {
     char buf[512];
@@ -359,6 +363,8 @@ static int arf_generate(gg_ctx *c, const gg_arf_sampling *a, uint64_t n, uint64_
   p.half_extent[0] = a->half_extent[0];
   p.half_extent[1] = a->half_extent[1];
   p.russian_roulette = a->russian_roulette;
+  p.theta_uniform = a->theta_uniform ? 1 : 0;
+  p.theta_max_turn = std::acos(a->cos_theta_max) / (2.0 * M_PI);
   p.stage = c->d_arf_stage;
   p.block_count = c->d_arf_bcount;
   p.block_off = c->d_arf_boff;
@@ -731,6 +737,31 @@ static int upload_frames(gg_ctx *c) {
   return GG_OK;
 }
 
+// Records a start / end event of a stage launch (events are reused across runs).
+static int stage_event(gg_ctx *c, int kind, bool start) {
+  const size_t k = c->stage_kind.size() * 2 + (start ? 0 : 1);
+  while (c->stage_ev.size() <= k) {
+    cudaEvent_t e;
+    int st = c->cuda(cudaEventCreate(&e), "cudaEventCreate");
+    if (st) return st;
+    c->stage_ev.push_back(e);
+  }
+  int st = c->cuda(cudaEventRecord(c->stage_ev[k], c->stream), "event");
+  if (st) return st;
+  if (!start) c->stage_kind.push_back(kind);
+  return GG_OK;
+}
+
+// Adds the times of the recorded stage launches (stream synchronised) and forgets them.
+static void stage_collect(gg_ctx *c) {
+  for (size_t i = 0; i < c->stage_kind.size(); ++i) {
+    float ms = 0;
+    if (cudaEventElapsedTime(&ms, c->stage_ev[2 * i], c->stage_ev[2 * i + 1]) == cudaSuccess)
+      c->stage_ms[c->stage_kind[i]] += ms;
+  }
+  c->stage_kind.clear();
+}
+
 // SPECT transport of one batch: phantom stage on the primary records, head
 // stage on the head queue, then phantom / head passes on the photons that
 // flew back into the image until the return queue stays empty.
@@ -751,19 +782,23 @@ static int spect_stages(gg_ctx *c, gg::KernelArgs a, size_t smem, int minb) {
     if ((st = c->cuda(cudaMemsetAsync(out_n, 0, sizeof(unsigned long long), c->stream), "memset"))) return st;
     if ((st = c->cuda(cudaMemsetAsync(c->d_next, 0, 8, c->stream), "memset"))) return st;
     int grid = c->n_sm * bps[stage];
+    if ((st = stage_event(c, stage, true))) return st;
     cudaError_t e = c->precision == GG_PREC_F64
                         ? gg::launch_spect_stage<double>(stage, c->scene<double>(), a, q, grid, c->block, smem, minb,
                                                          c->stream)
                         : gg::launch_spect_stage<float>(stage, c->scene<float>(), a, q, grid, c->block, smem, minb,
                                                         c->stream);
-    return c->cuda(e, "SPECT stage launch");
+    if ((st = c->cuda(e, "SPECT stage launch"))) return st;
+    return stage_event(c, stage, false);
   };
   // ARF stage between the phantom and the head stage: head queue -> network
   // (projection weights) + fallback queue for the head stage
   auto arf_run = [&]() -> int {
     int st;
     if ((st = c->cuda(cudaMemsetAsync(nf, 0, sizeof(unsigned long long), c->stream), "memset"))) return st;
+    if ((st = c->cuda(cudaMemsetAsync(c->d_next, 0, sizeof(unsigned long long), c->stream), "memset"))) return st;
     gg::ArfStageArgs q{};
+    q.claim = c->d_next;
     q.in_q = c->d_queue[0];
     q.in_n = nh;
     q.out_q = c->d_queue[2];
@@ -788,9 +823,11 @@ static int spect_stages(gg_ctx *c, gg::KernelArgs a, size_t smem, int minb) {
     q.proj2 = c->d_arf_proj2;
     q.counters = c->d_counters;
     q.status = c->d_status;
+    if ((st = stage_event(c, 2, true))) return st;
     cudaError_t e = c->precision == GG_PREC_F64 ? gg::launch_spect_arf<double>(c->scene<double>(), q, c->n_sm, c->stream)
                                                 : gg::launch_spect_arf<float>(c->scene<float>(), q, c->n_sm, c->stream);
-    return c->cuda(e, "ARF stage launch");
+    if ((st = c->cuda(e, "ARF stage launch"))) return st;
+    return stage_event(c, 2, false);
   };
   auto head_pass = [&]() -> int {
     int st;
@@ -810,6 +847,7 @@ static int spect_stages(gg_ctx *c, gg::KernelArgs a, size_t smem, int minb) {
     if ((st = c->cuda(cudaMemcpyAsync(&back, nr, sizeof(back), cudaMemcpyDeviceToHost, c->stream), "queue length")))
       return st;
     if ((st = c->cuda(cudaStreamSynchronize(c->stream), "SPECT stages"))) return st;
+    stage_collect(c);
     if (back == 0) break;
     // a photon re-enters the image at most once per phantom / head pass; the
     // per-photon step cap ends every history, so this loop ends too
@@ -875,6 +913,8 @@ static int run_impl(gg_ctx *c, uint64_t n, uint64_t seed, uint64_t first) {
   a.interact_min = c->interact_min;
   int flush_grid = c->n_sm * 8;
   c->run_stage_launches = 0;
+  c->stage_ms[0] = c->stage_ms[1] = c->stage_ms[2] = 0;
+  c->stage_kind.clear();
   int st;
   // per batch: [ev 3b] generate [ev 3b+1] transport [ev 3b+2] flush [ev 3b+3]
   for (uint64_t b = 0; b < nb; ++b) {
@@ -1248,12 +1288,15 @@ int gg_arf_train(gg_ctx *c, const gg_arf_sampling *smp, const gg_arf_train_opts 
   g.eps = o->eps;
   g.loss_part = c->d_loss_part;
   const uint64_t steps_per_epoch = (n_rows + (uint64_t)o->batch - 1) / (uint64_t)o->batch;
+  const double total_steps = (double)steps_per_epoch * (double)o->epochs;
+  const double decay = o->lr_final > 0.0f ? std::log((double)o->lr_final / (double)o->lr) : 0.0;
   uint64_t t = 0;
   for (int ep = 0; ep < o->epochs; ++ep) {
     g.loss_acc = c->d_loss_acc + ep;
     for (uint64_t k = 0; k < steps_per_epoch; ++k, ++t) {
       a.row0 = (t * (uint64_t)o->batch) % n_rows;
       if ((st = c->cuda(gg::launch_mlp_train(a, tiles, c->stream), "ARF train step"))) return st;
+      g.lr = (float)((double)o->lr * std::exp(decay * (double)t / total_steps));
       g.c1 = (float)(1.0 / (1.0 - std::pow((double)o->beta1, (double)(t + 1))));
       g.c2 = (float)(1.0 / (1.0 - std::pow((double)o->beta2, (double)(t + 1))));
       if ((st = c->cuda(gg::launch_mlp_adam(g, c->stream), "ARF Adam step"))) return st;
@@ -1268,6 +1311,14 @@ int gg_arf_train(gg_ctx *c, const gg_arf_sampling *smp, const gg_arf_train_opts 
   if (loss)
     for (int ep = 0; ep < o->epochs; ++ep) loss[ep] = lacc[ep] / ((double)steps_per_epoch * o->batch);
   if (model_out) *model_out = m;
+  return GG_OK;
+}
+
+int gg_last_stage_ms(gg_ctx *c, double *phantom_ms, double *head_ms, double *arf_ms) {
+  if (!c) return GG_ERR_ARG;
+  if (phantom_ms) *phantom_ms = c->stage_ms[0];
+  if (head_ms) *head_ms = c->stage_ms[1];
+  if (arf_ms) *arf_ms = c->stage_ms[2];
   return GG_OK;
 }
 

@@ -52,14 +52,20 @@ __global__ void __launch_bounds__(256) k_arf_sample(Scene<real> s, ArfArgs p) {
     u = u - R<real>(1);
     ph.pos[1] = u * hy;
     ph.pos[2] = R<real>(0);
-    real w = R<real>(1) - (real)p.cos_theta_max;
-    w = u01<real>(g) * w;
-    const real ct = R<real>(1) - w;
+    real ct, st;
+    if (p.theta_uniform) {
+      const real f = u01<real>(g) * (real)p.theta_max_turn;
+      gg_sincos_turn(f, st, ct);
+    } else {
+      real w = R<real>(1) - (real)p.cos_theta_max;
+      w = u01<real>(g) * w;
+      ct = R<real>(1) - w;
+      real st2 = ct * ct;
+      st2 = R<real>(1) - st2;
+      st = gg_sqrt(st2 > R<real>(0) ? st2 : R<real>(0));
+    }
     real sp, cp;
     gg_sincos_turn(u01<real>(g), sp, cp);
-    real st2 = ct * ct;
-    st2 = R<real>(1) - st2;
-    const real st = gg_sqrt(st2 > R<real>(0) ? st2 : R<real>(0));
     ph.dir[0] = st * cp;
     ph.dir[1] = st * sp;
     ph.dir[2] = ct;

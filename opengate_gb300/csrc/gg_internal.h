@@ -44,6 +44,8 @@ struct StageArgs {
 struct ArfArgs {
   uint64_t seed, first, n;        // samples [first, first + n), Philox stream 1
   double e_min, e_max, cos_theta_max, half_extent[2], russian_roulette;
+  int theta_uniform;              // theta = u theta_max instead of cos(theta) uniform
+  double theta_max_turn;          // acos(cos_theta_max) / (2 pi)
   float4 *stage;                  // [n] row per sample (w = -1: dropped)
   unsigned int *block_count;      // [blocks] kept rows per block
   unsigned long long *block_off;  // [blocks] first output row of each block
@@ -95,6 +97,7 @@ struct ArfStageArgs {
   unsigned long long *proj2;       // their squares: (low 32 bits, rest) per pixel, 2^-64 / 2^-32 MeV^2 units
   unsigned long long *counters;
   unsigned int *status;
+  unsigned long long *claim;       // chunk claim counter, zero at launch
 };
 
 size_t mlp_smem_bytes();

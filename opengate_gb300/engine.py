@@ -138,6 +138,12 @@ class SpectEngine(DoseEngine):
     def last_kernel_ms(self):
         return tuple(self.kernel_ms)
 
+    def last_stage_ms(self):
+        """(phantom, head, ARF) stage device times of the last run, ms."""
+        v = [ctypes.c_double() for _ in range(3)]
+        self._call("gg_last_stage_ms", *(ctypes.byref(x) for x in v))
+        return tuple(x.value for x in v)
+
     def use_arf(self, enable=True):
         """ARF detectors (a model must be set on the context, e.g. by ArfNetwork.train)."""
         self._call("gg_spect_use_arf", 1 if enable else 0)
@@ -172,8 +178,9 @@ class ArfNetwork:
         self.model = None
 
     @staticmethod
-    def sampling(e_min, e_max, theta_max_deg, half_extent, russian_roulette):
+    def sampling(e_min, e_max, theta_max_deg, half_extent, russian_roulette, theta_uniform=True):
         a = C.ArfSampling()
+        a.theta_uniform = 1 if theta_uniform else 0
         a.e_min, a.e_max = float(e_min), float(e_max)
         a.cos_theta_max = float(np.cos(np.radians(theta_max_deg)))
         a.half_extent[:] = [float(half_extent[0]), float(half_extent[1])]
@@ -188,11 +195,12 @@ class ArfNetwork:
         return rows[: m.value].copy()
 
     def train(self, sampling, n_samples, seed, epochs=4, batch=8192, lr=1e-3, init_seed=1, beta1=0.9,
-              beta2=0.999, eps=1e-8):
+              beta2=0.999, eps=1e-8, lr_final=None):
         o = C.ArfTrainOpts()
         o.n_samples, o.seed, o.init_seed = int(n_samples), int(seed), int(init_seed)
         o.batch, o.epochs = int(batch), int(epochs)
         o.lr, o.beta1, o.beta2, o.eps = lr, beta1, beta2, eps
+        o.lr_final = lr / 100.0 if lr_final is None else lr_final
         model = C.ArfModel()
         loss = np.zeros(epochs, dtype=np.float64)
         self.eng._call("gg_arf_train", ctypes.byref(sampling), ctypes.byref(o), ctypes.byref(model),

@@ -1641,14 +1641,20 @@ static int arf_sample(const scene_t *s, const gg_arf_sampling *a, uint64_t seed,
   u = u - R(1);
   ph.pos[1] = u * hy;
   ph.pos[2] = R(0);
-  real w = R(1) - (real)a->cos_theta_max;
-  w = u01(&g) * w;
-  real ct = R(1) - w;
+  real ct, st;
+  if (a->theta_uniform) {
+    real f = u01(&g) * (real)(acos(a->cos_theta_max) / (2.0 * M_PI));
+    ggo_sincos_turn(f, &st, &ct);
+  } else {
+    real w = R(1) - (real)a->cos_theta_max;
+    w = u01(&g) * w;
+    ct = R(1) - w;
+    real st2 = ct * ct;
+    st2 = R(1) - st2;
+    st = ggo_sqrt(st2 > R(0) ? st2 : R(0));
+  }
   real sp, cp;
   ggo_sincos_turn(u01(&g), &sp, &cp);
-  real st2 = ct * ct;
-  st2 = R(1) - st2;
-  real st = ggo_sqrt(st2 > R(0) ? st2 : R(0));
   ph.dir[0] = st * cp;
   ph.dir[1] = st * sp;
   ph.dir[2] = ct;

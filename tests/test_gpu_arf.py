@@ -90,24 +90,37 @@ def test_forward_and_gradient_match_oracle(n_classes):
 
 
 def test_training_learns_detection_probability():
+    """The trained network predicts the window counts of held-out photons.
+
+    Held-out rows are isotropic (the incidence of the training-dataset
+    simulation), rows of class 0 carry the Russian-roulette weight; the
+    network's expected counts per window must agree within 5 %, and per
+    angular bin within 15 % (the network smooths the sharp window edges in
+    energy).
+    """
+    from opengate_gb300.engine import ArfNetwork
+
     scene, sp, a = _arf_case(rr=5.0)
+    train = ArfNetwork.sampling(0.05, 0.16, 20.0, (150.0, 150.0), 5.0, theta_uniform=True)
     eng, net = _engine(scene, sp)
     with eng:
-        model, loss = net.train(a, 20_000_000, seed=21, epochs=8, batch=8192, lr=2e-3)
-        held = net.dataset(a, 4_000_000, seed=99)
+        model, loss = net.train(train, 100_000_000, seed=21, epochs=30, batch=8192, lr=2e-3, lr_final=1e-5)
+        held = net.dataset(a, 8_000_000, seed=99)
         probs = net.predict(held)
     assert model.n_classes == 3
     assert np.all(np.isfinite(loss)) and loss[-1] < loss[0]
     w = M.arf_weights(probs, model.russian_roulette)
-    # measured photopeak fraction (w = 1) vs the network's, undoing the roulette of class 0
-    e, th, cls = held[:, 0], held[:, 1], held[:, 3]
-    keep0 = cls == 0
-    weight = np.where(keep0, model.russian_roulette, 1.0)
-    for lo, hi in ((0.0, 1.5), (1.5, 3.0), (3.0, 6.0)):
-        sel = (th >= lo) & (th < hi) & (e > 0.13)
-        measured = float((weight[sel] * (cls[sel] == 1)).sum() / weight[sel].sum())
-        predicted = float(w[sel, 1].mean())
-        assert abs(predicted - measured) < 0.1 * measured + 2e-3, (lo, hi, measured, predicted)
+    th, cls = held[:, 1], held[:, 3]
+    weight = np.where(cls == 0, model.russian_roulette, 1.0)
+    for k in (1, 2):
+        measured = float((weight * (cls == k)).sum())
+        predicted = float((weight * w[:, k]).sum())
+        assert abs(predicted / measured - 1.0) < 0.05, (k, measured, predicted)
+    for lo, hi in ((0.0, 1.5), (1.5, 3.0)):
+        sel = (th >= lo) & (th < hi)
+        measured = float((weight[sel] * (cls[sel] == 1)).sum())
+        predicted = float((weight[sel] * w[sel, 1]).sum())
+        assert abs(predicted / measured - 1.0) < 0.15, (lo, hi, measured, predicted)
 
 
 @pytest.mark.parametrize("rr", [1.0, 7.0])
