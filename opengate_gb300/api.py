@@ -109,6 +109,23 @@ class ImageVolume(GateObject):
         raise ValueError(f"ImageVolume '{self.name}': set .image to an .mhd path or an image_io.Image")
 
 
+class SpectHead(GateObject):
+    """A SPECT head as one volume: parallel-hole collimator (hexagonal holes), gap and NaI crystal
+    (the heads built by contrib/spect/ge_discovery_nm670.py:125-164 add_spect_head and
+    siemens_intevo.py:84-130), placed by rotate_gantry (ge_discovery_nm670.py:1056-1080): at run r
+    the collimator face is at `radius` from the z axis, angle start_angle_deg + r step_angle_deg."""
+
+    type_name = "SpectHead"
+    user_info_defaults = {"mother": "world", "collimator_type": "lehr", "crystal_size": "3/8",
+                          "radius": 25 * u.cm, "start_angle_deg": 0.0, "step_angle_deg": 1.0, "nb_angle": 1,
+                          "gap": 0.0, "half_width": None, "collimator_material": "G4_Pb",
+                          "crystal_material": "G4_SODIUM_IODIDE"}
+
+    @property
+    def crystal_name(self):
+        return f"{self.name}_crystal"
+
+
 class VolumeManager:
     def __init__(self, simulation):
         self.simulation = simulation
@@ -119,8 +136,8 @@ class VolumeManager:
     def add_volume(self, volume_type, name):
         if name in self.volumes:
             raise ValueError(f"a volume named '{name}' already exists")
-        cls = {"Box": BoxVolume, "BoxVolume": BoxVolume, "Image": ImageVolume, "ImageVolume": ImageVolume}.get(
-            volume_type)
+        cls = {"Box": BoxVolume, "BoxVolume": BoxVolume, "Image": ImageVolume, "ImageVolume": ImageVolume,
+               "SpectHead": SpectHead}.get(volume_type)
         if cls is None:
             raise NotImplementedError(f"volume type '{volume_type}' is not supported by the GPU path")
         v = cls(name, self.simulation)
@@ -256,10 +273,82 @@ class GenericSource(GateObject):
             raise NotImplementedError(f"source '{self.name}': energy type '{e.type}' unsupported")
         return s
 
-    def n_events(self):
-        if self.activity and not self.n:
-            raise NotImplementedError("activity-driven sources: set n (number of primaries)")
-        return int(self.n)
+
+
+class VoxelSource(GenericSource):
+    """Activity image source (opengate/sources/voxelsources.py:15-122): the activity image (.mhd path
+    or image_io.Image, [z][y][x]) is centred on position.translation; emission points follow the
+    3-level CDF of compute_image_3D_CDF (image.py:313-360) with a uniform jitter in the voxel."""
+
+    type_name = "VoxelSource"
+    user_info_defaults = dict(GenericSource.user_info_defaults, image=None)
+
+    def to_spec(self, volumes):
+        p = self.position
+        if p.type not in ("point", None) or p.confine:
+            raise NotImplementedError("VoxelSource: position.type / confine are set by the image")
+        s = GenericSource.to_spec(self, volumes)
+        img = self.image
+        if isinstance(img, (str, pathlib.Path)):
+            img = image_io.read_mhd(img)
+        if not isinstance(img, image_io.Image):
+            raise ValueError(f"VoxelSource '{self.name}': set .image to an .mhd path or an image_io.Image")
+        arr = np.asarray(img.array, dtype=np.float64)
+        if not np.any(arr > 0):
+            raise ValueError(f"VoxelSource '{self.name}': the activity image is empty")
+        spacing = np.asarray(img.spacing, dtype=np.float64)
+        size = np.array([arr.shape[2], arr.shape[1], arr.shape[0]], dtype=np.float64)
+        corner = np.asarray(p.translation, dtype=np.float64) - size * spacing / 2.0
+        s.set_activity_image(arr, spacing, corner)
+        return s
+
+
+def expected_number_of_events(activity, half_life, t0, t1):
+    """Expected events of an activity source in [t0, t1] (GateVSource::GetExpectedNumberOfEvents,
+    core/opengate_core/opengate_lib/GateVSource.cpp:127-141): round(A (t1 - t0)) without decay,
+    round(A / lambda (exp(-lambda t0) - exp(-lambda t1))) with half-life; A in Bq, times in s."""
+    if half_life is None or half_life <= 0:
+        return int(round(activity * (t1 - t0)))
+    lam = math.log(2.0) / half_life
+    return int(round(activity / lam * (math.exp(-lam * t0) - math.exp(-lam * t1))))
+
+
+def sample_number_of_events(activity, half_life, t0, t1, rng):
+    """Events of an activity source in [t0, t1]: the reference draws decay times with exponential
+    spacing at the (decaying) activity (GateVSource.cpp:55-92), a Poisson process whose count is
+    Poisson with the expected value above (unrounded)."""
+    if half_life is None or half_life <= 0:
+        mu = activity * (t1 - t0)
+    else:
+        lam = math.log(2.0) / half_life
+        mu = activity / lam * (math.exp(-lam * t0) - math.exp(-lam * t1))
+    return int(rng.poisson(max(mu, 0.0)))
+
+
+def activity_yield(source):
+    """Activity factor of a spectrum_discrete source: the sum of the line weights
+    (GateGenericSource.cpp:561-574 normalises the weights and multiplies the activity)."""
+    if source.energy.type == "spectrum_discrete":
+        return float(np.sum(np.asarray(source.energy.spectrum_weights, dtype=np.float64)))
+    return 1.0
+
+
+def events_per_run(source, run_timing_intervals, rng):
+    """Primaries of `source` in each run: `n` (an int for every run, or one value per run) or the
+    activity over each run interval (times in g4 units)."""
+    runs = len(run_timing_intervals)
+    if source.n:
+        n = source.n
+        if np.ndim(n) == 0:
+            return [int(n)] * runs
+        if len(n) != runs:
+            raise ValueError(f"source '{source.name}': n has {len(n)} values for {runs} runs")
+        return [int(x) for x in n]
+    if source.activity:
+        a = float(source.activity) / u.Bq * activity_yield(source)
+        hl = float(source.half_life) / u.s if source.half_life and source.half_life > 0 else None
+        return [sample_number_of_events(a, hl, t0 / u.s, t1 / u.s, rng) for t0, t1 in run_timing_intervals]
+    raise ValueError(f"source '{source.name}': set n or activity")
 
 
 # --------------------------------------------------------------------------- actors
@@ -293,7 +382,9 @@ class DoseActor(GateObject):
     user_info_defaults = {"attached_to": "world", "size": [10, 10, 10], "spacing": [1.0, 1.0, 1.0],
                           "translation": [0.0, 0.0, 0.0], "rotation": np.eye(3), "repeated_volume_index": 0,
                           "hit_type": "random", "output_coordinate_system": "local", "output_filename": "auto",
-                          "score_in": "material", "uncertainty_goal": None, "priority": 100}
+                          "score_in": "material", "uncertainty_goal": None, "priority": 100,
+                          "uncertainty_first_check_after_n_events": 1e4, "uncertainty_top_voxels_count": 10,
+                          "uncertainty_voxel_edep_threshold": 0.7, "uncertainty_overshoot_factor_N_events": 1.05}
 
     def __init__(self, name, simulation=None, **kw):
         super().__init__(name, simulation, **kw)
@@ -304,8 +395,8 @@ class DoseActor(GateObject):
     def check(self, image_volume, image):
         if self.attached_to != image_volume.name:
             raise NotImplementedError("the DoseActor must be attached to the ImageVolume")
-        if self.uncertainty_goal is not None:
-            raise NotImplementedError("uncertainty_goal (early stop) is not supported yet")
+        if self.uncertainty_goal is not None and not 0.0 < self.uncertainty_goal < 1.0:
+            raise ValueError(f"Uncertainty goal must be > 0 and < 1, where 1 means 100%: {self.uncertainty_goal}")
         if self.score_in not in ("material", None):
             raise NotImplementedError("score_in other than 'material' is not supported")
         if self.hit_type not in ("random", "pre", "post", "middle"):
@@ -318,6 +409,25 @@ class DoseActor(GateObject):
     @property
     def number_of_samples(self):
         return self.edep.number_of_samples
+
+
+class DigitizerProjectionActor(GateObject):
+    """Projection of the singles of one SPECT head's crystal (GateDigitizerProjectionActor,
+    core/opengate_core/opengate_lib/digitizer/GateDigitizerProjectionActor.cpp:127-223;
+    opengate/actors/digitizers.py:1140-1395): counts [run * n_channels + channel][y][x] in the
+    energy windows `channels` ({"name", "min", "max"}, [min, max)), singles = per-event crystal
+    energy at the energy-winner position (GateDigiAdderInVolume EnergyWinnerPosition)."""
+
+    type_name = "DigitizerProjectionActor"
+    user_info_defaults = {"attached_to": None, "input_digi_collections": [], "channels": [],
+                          "size": [128, 128], "spacing": [4.42 * u.mm, 4.42 * u.mm], "output_filename": "auto",
+                          "write_to_disk": True, "detector_orientation_matrix": np.eye(3),
+                          "squared_counts": False, "priority": 100}
+
+    def __init__(self, name, simulation=None, **kw):
+        super().__init__(name, simulation, **kw)
+        object.__setattr__(self, "counts", ActorOutput(self, "counts", True))
+        object.__setattr__(self, "counts_squared", ActorOutput(self, "squared_counts", False))
 
 
 class SimulationStatisticsActor(GateObject):
@@ -371,16 +481,18 @@ class Simulation:
     def add_source(self, source_type, name):
         if name in self.sources:
             raise ValueError(f"a source named '{name}' already exists")
-        if source_type != "GenericSource":
+        cls = {"GenericSource": GenericSource, "VoxelSource": VoxelSource}.get(source_type)
+        if cls is None:
             raise NotImplementedError(f"source type '{source_type}' is not supported by the GPU path")
-        s = GenericSource(name, self)
+        s = cls(name, self)
         self.sources[name] = s
         return s
 
     def add_actor(self, actor_type, name):
         if name in self.actors:
             raise ValueError(f"an actor named '{name}' already exists")
-        cls = {"DoseActor": DoseActor, "SimulationStatisticsActor": SimulationStatisticsActor}.get(actor_type)
+        cls = {"DoseActor": DoseActor, "SimulationStatisticsActor": SimulationStatisticsActor,
+               "DigitizerProjectionActor": DigitizerProjectionActor}.get(actor_type)
         if cls is None:
             raise NotImplementedError(f"actor type '{actor_type}' is not supported by the GPU path")
         a = cls(name, self)
@@ -396,7 +508,7 @@ class Simulation:
             return int.from_bytes(os.urandom(8), "little")
         return int(self.random_seed) & 0xFFFFFFFFFFFFFFFF
 
-    def build_scene(self):
+    def build_scene(self, extra_materials=()):
         """(scene, image volume, HU image, material names by label, sources) for this configuration."""
         images = [v for v in self.volumes.values() if isinstance(v, ImageVolume)]
         if len(images) != 1:
@@ -415,6 +527,9 @@ class Simulation:
         labels = M.create_label_image(hu.array, vol.material, vol.voxel_materials, lut)
         if self.world.material not in names:
             names.append(self.world.material)
+        for m in extra_materials:
+            if m not in names:
+                names.append(m)
         mats = [db.get(n) for n in names]
         pt = T.PhysicsTables(mats)
         spacing = hu.spacing
@@ -430,30 +545,158 @@ class Simulation:
         scene = Scene(pt, labels, spacing, corner, half, names.index(self.world.material), specs[0])
         return scene, vol, hu, names, list(zip(sources, specs))
 
+    def build_spect(self):
+        """(scene, SpectSpec, sources, projection actors, head index per actor crystal) of a SPECT set-up."""
+        from . import spect as S
+
+        heads = [v for v in self.volumes.values() if isinstance(v, SpectHead)]
+        if len(heads) > 2:
+            raise NotImplementedError("at most two SPECT heads")
+        h0 = heads[0]
+        for h in heads[1:]:
+            for k in ("collimator_type", "crystal_size", "radius", "step_angle_deg", "nb_angle", "gap"):
+                if getattr(h, k) != getattr(h0, k):
+                    raise NotImplementedError(f"SPECT heads must share '{k}'")
+        runs = self.run_timing_intervals
+        if h0.nb_angle not in (1, len(runs)):
+            raise ValueError(f"rotate_gantry gave {h0.nb_angle} positions for {len(runs)} runs")
+        step = h0.step_angle_deg if h0.nb_angle > 1 else 0.0
+        projs = [a for a in self.actors.values() if isinstance(a, DigitizerProjectionActor)]
+        if not projs:
+            raise ValueError("a SPECT simulation needs a DigitizerProjectionActor")
+        head_of = {h.crystal_name: i for i, h in enumerate(heads)}
+        for a in projs:
+            if a.attached_to not in head_of:
+                raise ValueError(f"projection actor '{a.name}' must be attached to a head crystal "
+                                 f"({', '.join(head_of)})")
+            if a.channels != projs[0].channels or list(a.size) != list(projs[0].size) or \
+                    not np.allclose(a.spacing, projs[0].spacing):
+                raise NotImplementedError("projection actors must share channels, size and spacing")
+        channels = projs[0].channels
+        windows = [(float(c["min"]) / u.MeV, float(c["max"]) / u.MeV) for c in channels]
+        extra = [h0.collimator_material, h0.crystal_material]
+        scene, vol, hu, names, sources = self.build_scene(extra_materials=extra)
+        coll = S.COLLIMATORS.get(str(h0.collimator_type).lower())
+        if coll is None:
+            raise NotImplementedError(f"collimator '{h0.collimator_type}'")
+        spacing = [float(x) / u.mm for x in projs[0].spacing]
+        half_w = h0.half_width / u.mm if h0.half_width else None
+        sp = S.SpectSpec(collimator=coll, crystal_thickness=S.CRYSTALS[h0.crystal_size], gap=h0.gap / u.mm,
+                         radius=h0.radius / u.mm, n_heads=len(heads), n_runs=len(runs), windows=windows,
+                         size=[int(x) for x in projs[0].size], spacing=spacing,
+                         step_angle_deg=step, collimator_material=names.index(h0.collimator_material),
+                         crystal_material=names.index(h0.crystal_material),
+                         head_start_deg=[h.start_angle_deg for h in heads])
+        if half_w:
+            sp.half_width = half_w
+        return scene, sp, sources, projs, head_of
+
+    def _run_spect(self):
+        """SPECT acquisition: heads + projection actors, one gantry position per run."""
+        from .engine import SpectEngine
+
+        t0 = time.perf_counter()
+        scene, sp, sources, projs, head_of = self.build_spect()
+        runs = self.run_timing_intervals
+        spacing = sp.spacing
+        seed = self._seed()
+        self.last_seed = seed
+        rng = np.random.default_rng(seed)
+        plan = [events_per_run(src, runs, rng) for src, _ in sources]
+        eng = SpectEngine(scene, sp, device=self.device, precision=self.precision, batch=self.batch)
+        try:
+            first = 0
+            for r in range(len(runs)):
+                frames = np.ascontiguousarray(sp.frames(r), dtype=np.float64)
+                eng._call("gg_spect_set_heads", r, C.ptr(frames, C.ctypes.c_double))
+                for k, (src, spec) in enumerate(sources):
+                    if len(sources) > 1 or k:
+                        eng.set_source(spec)
+                    if plan[k][r]:
+                        eng._call("gg_run", C.ctypes.c_uint64(plan[k][r]), C.ctypes.c_uint64(seed),
+                                  C.ctypes.c_uint64(first))
+                    first += plan[k][r]
+            proj, cnt = eng.projection(), eng.counters()
+        finally:
+            eng.close()
+        elapsed = time.perf_counter() - t0
+        for a in projs:
+            h = head_of[a.attached_to]
+            sx, sy = spacing
+            origin = [-a.size[0] * sx / 2 + sx / 2, -a.size[1] * sy / 2 + sy / 2, 0.0]
+            img = image_io.Image(proj[h], [sx, sy, 1.0], origin)
+            a.counts.image = img
+            a.counts.number_of_samples = first
+            a.counts_squared.image = image_io.Image(proj[h].copy(), [sx, sy, 1.0], origin)
+            if a.write_to_disk:
+                out = a.output_filename
+                path = self.get_output_path(f"{a.name}_counts.mhd" if out in (None, "", "auto") else out)
+                image_io.write_mhd(path, img)
+        for a in self.actors.values():
+            if isinstance(a, SimulationStatisticsActor):
+                a.counts.runs = len(runs)
+                a.counts.events = first
+                a.counts.tracks = first
+                a.counts.steps = cnt["woodcock_steps"] + cnt["world_steps"] + cnt["head_steps"]
+                a.counts.duration = elapsed * u.s
+                a.counts.pps = int(first / elapsed) if elapsed > 0 else 0
+                a.counts.sps = int(a.counts.steps / elapsed) if elapsed > 0 else 0
+        return cnt
+
     def run(self, start_new_process=False):
         from .engine import DoseEngine
 
-        if len(self.run_timing_intervals) != 1:
-            raise NotImplementedError("one run (run_timing_intervals of length 1) for the dose path")
+        if any(isinstance(v, SpectHead) for v in self.volumes.values()):
+            return self._run_spect()
         t0 = time.perf_counter()
         scene, vol, hu, names, sources = self.build_scene()
         seed = self._seed()
         self.last_seed = seed
+        rng = np.random.default_rng(seed)
+        runs = self.run_timing_intervals
+        plan = [events_per_run(src, runs, rng) for src, _ in sources]
         doses = [a for a in self.actors.values() if isinstance(a, DoseActor)]
         for a in doses:
             a.check(vol, hu)
         if vol.dump_label_image:
             image_io.write_mhd(self.get_output_path(vol.dump_label_image),
                                image_io.Image(scene.labels, hu.spacing, hu.origin))
+        goals = [a for a in doses if a.uncertainty_goal is not None]
+        if len(goals) > 1:
+            raise NotImplementedError("one DoseActor with an uncertainty goal")
+        if goals and (len(sources) > 1 or len(runs) > 1):
+            raise NotImplementedError("the uncertainty goal needs one source and one run")
         eng = DoseEngine(scene, device=self.device, precision=self.precision, batch=self.batch)
         try:
             first = 0
-            for k, (src, spec) in enumerate(sources):
-                if k:
-                    eng.set_source(spec)
-                n = src.n_events()
-                eng.run(n, seed, first)
-                first += n
+            for r in range(len(runs)):
+                for k, (src, spec) in enumerate(sources):
+                    if len(sources) > 1:
+                        eng.set_source(spec)
+                    n = plan[k][r]
+                    if not goals:
+                        eng.run(n, seed, first)
+                        first += n
+                        continue
+                    # uncertainty goal: GateDoseActor::EndOfEventAction (GateDoseActor.cpp:245-276)
+                    g = goals[0]
+                    n_next = int(g.uncertainty_first_check_after_n_events)
+                    unc = 1.0
+                    checks = []
+                    while first < n:
+                        todo = max(min(n_next, n) - first, 1)
+                        eng.run(todo, seed, first)
+                        first += todo
+                        unc = D.compute_mean_uncertainty(eng.edep(), eng.edep_squared(), first,
+                                                         g.uncertainty_voxel_edep_threshold,
+                                                         g.uncertainty_top_voxels_count)
+                        checks.append((first, unc))
+                        object.__setattr__(g, "uncertainty_checks", checks)
+                        if unc <= g.uncertainty_goal:
+                            break
+                        n_next = max(D.next_uncertainty_check(unc, g.uncertainty_goal, first,
+                                                              g.uncertainty_overshoot_factor_N_events), first + 1)
+                    object.__setattr__(g, "_uncertainty_reached", unc)
             edep, edep2, cnt = eng.edep(), eng.edep_squared(), eng.counters()
         finally:
             eng.close()
@@ -476,7 +719,7 @@ class Simulation:
                     image_io.write_mhd(out.get_output_path(), out.image)
         for a in self.actors.values():
             if isinstance(a, SimulationStatisticsActor):
-                a.counts.runs = 1
+                a.counts.runs = len(runs)
                 a.counts.events = n_events
                 a.counts.tracks = n_events + cnt["secondaries"]
                 a.counts.steps = cnt["woodcock_steps"] + cnt["world_steps"]

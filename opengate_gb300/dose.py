@@ -59,3 +59,38 @@ def mean_relative_uncertainty(edep, edep2, n, threshold=0.1):
     unc = variance_or_uncertainty(edep, edep2, n, "uncertainty")
     sel = edep > threshold * edep.max()
     return float(unc[sel].mean()) if np.any(sel) else float("nan")
+
+
+def mean_of_highest_n(image, n):
+    """Mean of the n largest voxel values (GateDoseActor::GetMeanOfHighestNValues,
+    core/opengate_core/opengate_lib/GateDoseActor.cpp:401-430)."""
+    v = np.asarray(image, dtype=np.float64).ravel()
+    if v.size == 0 or n <= 0:
+        return 0.0
+    n = min(int(n), v.size)
+    return float(np.partition(v, v.size - n)[v.size - n:].mean())
+
+
+def compute_mean_uncertainty(edep, edep_squared, n_events, threshold=0.7, top_voxels=10):
+    """Mean relative uncertainty of the voxels above threshold x (mean of the
+    top_voxels largest edep) - the uncertainty-goal criterion of
+    GateDoseActor::ComputeMeanUncertainty (GateDoseActor.cpp:261-317): events
+    counted at least 2, per-voxel variance clipped at 0 and relative
+    uncertainty at 1; 1 when no voxel qualifies."""
+    e = np.asarray(edep, dtype=np.float64).ravel()
+    e2 = np.asarray(edep_squared, dtype=np.float64).ravel()
+    n = max(float(n_events), 2.0)
+    sel = e > mean_of_highest_n(e, top_voxels) * threshold
+    if not sel.any():
+        return 1.0
+    val = e[sel] / n
+    unc = (e2[sel] / n - val * val) / (n - 1.0)
+    unc = np.sqrt(np.clip(unc, 0.0, None)) / val
+    unc = np.minimum(unc, 1.0)
+    m = float(unc.mean())
+    return m if m > 0 else 1.0
+
+
+def next_uncertainty_check(current, goal, n_events, overshoot=1.05):
+    """Events at which the next check happens (GateDoseActor.cpp:269-274)."""
+    return int((current / goal) * (current / goal) * n_events * overshoot)

@@ -30,12 +30,17 @@ from . import _capi as C
 # parallel-hole collimators: (hole apothem, hole length, pitch between adjacent holes) in mm
 LEHR = dict(hole_apothem=0.75, collimator_thickness=35.0, hole_pitch=1.7)  # 1.5 mm holes, 0.2 mm septa
 MELP = dict(hole_apothem=1.47, collimator_thickness=40.6, hole_pitch=4.08)  # 2.94 mm holes, 1.14 mm septa
+MEGP = dict(hole_apothem=1.5, collimator_thickness=58.0, hole_pitch=4.05)  # 3 mm holes, 1.05 mm septa
+HEGP = dict(hole_apothem=2.0, collimator_thickness=66.0, hole_pitch=5.8)  # 4 mm holes, 1.8 mm septa
+COLLIMATORS = {"lehr": LEHR, "melp": MELP, "megp": MEGP, "hegp": HEGP, "he": HEGP}
+CRYSTALS = {"3/8": 9.525, "5/8": 15.875}  # NaI thickness, mm
 
 
 class SpectSpec:
     def __init__(self, collimator=LEHR, crystal_thickness=9.525, gap=0.0, radius=250.0, n_heads=2,
                  n_runs=60, start_angle_deg=0.0, step_angle_deg=6.0, windows=((0.126, 0.154), (0.108, 0.126)),
-                 size=(128, 128), spacing=(4.42, 4.42), collimator_material=0, crystal_material=0):
+                 size=(128, 128), spacing=(4.42, 4.42), collimator_material=0, crystal_material=0,
+                 head_start_deg=None):
         if n_heads not in (1, 2):
             raise ValueError("1 or 2 heads")
         if len(windows) > 8:
@@ -59,6 +64,8 @@ class SpectSpec:
         self.half_width = 0.5 * max(self.size[0] * self.spacing[0], self.size[1] * self.spacing[1])
         self.collimator_material = int(collimator_material)
         self.crystal_material = int(crystal_material)
+        # start angle of each head (default: evenly spread from start_angle_deg)
+        self.head_start = None if head_start_deg is None else [math.radians(a) for a in head_start_deg]
 
     @property
     def n_windows(self):
@@ -86,6 +93,8 @@ class SpectSpec:
         return d
 
     def angle(self, run, head):
+        if self.head_start is not None:
+            return self.head_start[head] + run * self.step_angle
         return self.start_angle + run * self.step_angle + head * 2.0 * math.pi / self.n_heads
 
     def frames(self, run):

@@ -1,0 +1,113 @@
+"""opengate-shaped API on the CPU: activity-driven primaries, uncertainty goal, SPECT set-up."""
+
+import math
+
+import numpy as np
+import pytest
+
+import opengate_gb300 as gate
+from opengate_gb300 import api as A
+from opengate_gb300 import dose as D
+from opengate_gb300 import units as U
+from opengate_gb300.contrib.spect import ge_discovery_nm670 as nm670
+from opengate_gb300.contrib.spect import spect_helpers
+
+u = U.g4_units
+
+
+def test_expected_number_of_events():
+    # GateVSource::GetExpectedNumberOfEvents: round(A dt), or with decay A/l (e^-l t0 - e^-l t1)
+    assert A.expected_number_of_events(1000.0, None, 0.0, 2.5) == 2500
+    hl = 6.0
+    lam = math.log(2) / hl
+    assert A.expected_number_of_events(1000.0, hl, 1.0, 3.0) == round(1000.0 / lam * (math.exp(-lam) - math.exp(-3 * lam)))
+
+
+def _source(sim, **kw):
+    s = sim.add_source("GenericSource", "src")
+    s.particle = "gamma"
+    for k, v in kw.items():
+        setattr(s, k, v)
+    return s
+
+
+def test_events_per_run_from_activity_and_n():
+    sim = gate.Simulation()
+    sim.run_timing_intervals = [[0, 1 * u.s], [1 * u.s, 3 * u.s]]
+    s = _source(sim, activity=2000 * u.Bq)
+    s.energy.type = "spectrum_discrete"
+    s.energy.spectrum_energies = [0.113, 0.208]
+    s.energy.spectrum_weights = [0.062, 0.104]  # yield 0.166: activity x 0.166
+    rng = np.random.default_rng(1)
+    draws = np.array([A.events_per_run(s, sim.run_timing_intervals, rng) for _ in range(400)])
+    expect = np.array([2000 * 0.166 * 1, 2000 * 0.166 * 2])
+    np.testing.assert_allclose(draws.mean(axis=0), expect, rtol=0.03)
+    np.testing.assert_allclose(draws.var(axis=0), expect, rtol=0.2)  # Poisson
+    s2 = _source(gate.Simulation(), n=[5, 7])
+    assert A.events_per_run(s2, [[0, 1], [1, 2]], rng) == [5, 7]
+    s3 = _source(gate.Simulation(), n=9)
+    assert A.events_per_run(s3, [[0, 1], [1, 2], [2, 3]], rng) == [9, 9, 9]
+
+
+def test_mean_uncertainty_criterion():
+    rng = np.random.default_rng(2)
+    n = 1000
+    e = rng.gamma(2.0, 1.0, size=(8, 9, 10))
+    e2 = e * e / n * 1.5 + 1e-3
+    top = np.sort(e.ravel())[-10:].mean()
+    sel = e > 0.7 * top
+    val = e[sel] / n
+    unc = np.sqrt(np.clip((e2[sel] / n - val ** 2) / (n - 1), 0, None)) / val
+    expect = float(np.minimum(unc, 1.0).mean())
+    assert D.compute_mean_uncertainty(e, e2, n) == pytest.approx(expect, rel=1e-12)
+    assert D.compute_mean_uncertainty(np.zeros((2, 2, 2)), np.zeros((2, 2, 2)), n) == 1.0
+    assert D.next_uncertainty_check(0.2, 0.1, 1000, 1.05) == int(4 * 1000 * 1.05)
+
+
+def spect_sim(tmp_path, n_per_run=1000, angles=3):
+    sim = gate.Simulation()
+    sim.output_dir = tmp_path
+    sim.world.size = [2 * u.m] * 3
+    sim.world.material = "G4_AIR"
+    sim.physics_manager.physics_list_name = "G4EmStandardPhysics"
+    sim.physics_manager.set_min_ekine("world", 1 * u.MeV)
+    sim.physics_manager.set_user_limits_particles(["e-", "e+"])
+    img = sim.add_volume("Image", "ct")
+    hu = np.full((20, 32, 32), -1000, np.int16)
+    hu[4:16, 8:24, 8:24] = 0
+    img.image = gate.Image(hu, spacing=(6.0, 6.0, 6.0))
+    img.material = "G4_AIR"
+    img.voxel_materials = [[-1100, -500, "G4_AIR"], [-500, 1000, "G4_WATER"]]
+    heads = []
+    for i, start in enumerate((0, 180)):
+        head, _, crystal = nm670.add_spect_head(sim, f"spect{i}", "lehr")
+        nm670.rotate_gantry(head, 25 * u.cm, start, 120, angles)
+        d = nm670.add_digitizer(sim, crystal.name, channels=spect_helpers.get_default_energy_windows("tc99m"),
+                                size=[64, 64], spacing=[8.84 * u.mm] * 2)
+        heads.append((head, d))
+    act = np.zeros((20, 32, 32))
+    act[6:14, 12:20, 12:20] = 1.0
+    src = sim.add_source("VoxelSource", "act")
+    src.particle = "gamma"
+    src.image = gate.Image(act, spacing=(6.0, 6.0, 6.0))
+    src.energy.type = "mono"
+    src.energy.mono = 140.5 * u.keV
+    src.n = n_per_run
+    sim.run_timing_intervals = [[k * u.s, (k + 1) * u.s] for k in range(angles)]
+    return sim, heads
+
+
+def test_spect_setup_from_the_helpers(tmp_path):
+    sim, heads = spect_sim(tmp_path)
+    scene, sp, sources, projs, head_of = sim.build_spect()
+    assert sp.n_heads == 2 and sp.n_runs == 3 and sp.n_windows == 2
+    assert sp.windows[1] == pytest.approx((0.12959, 0.15061))
+    assert [round(math.degrees(sp.angle(r, h))) for r in range(3) for h in range(2)] == [0, 180, 120, 300, 240, 420]
+    assert sp.collimator_thickness == 35.0 and sp.crystal_thickness == pytest.approx(9.525)
+    fr = sp.frames(1)
+    np.testing.assert_allclose(np.linalg.norm(fr[0, :3]), 250.0)
+    spec = sources[0][1]
+    assert spec.pos_type == 4 and spec.vox_dims == [32, 32, 20]
+    np.testing.assert_allclose(spec.vox_corner, [-96.0, -96.0, -60.0])
+    assert head_of == {"spect0_crystal": 0, "spect1_crystal": 1}
+    assert len(scene.pt.mat_rho) >= 4 and sp.collimator_material != sp.crystal_material

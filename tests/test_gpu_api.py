@@ -33,3 +33,52 @@ def test_simulation_run_matches_oracle_and_writes_outputs(tmp_path, built_lib):
     assert np.all((unc >= 0) & (unc <= 1.0 + 1e-12))
     # dose uncertainty equals edep uncertainty when the dose grid is the image grid
     np.testing.assert_allclose(dose.dose_uncertainty.get_data().array, unc, rtol=1e-12, atol=1e-15)
+
+
+def test_uncertainty_goal_stops_early(tmp_path, built_lib):
+    """DoseActor.uncertainty_goal: the run stops once the mean uncertainty of the high-dose voxels
+    reaches the goal; the images equal the oracle's for the events simulated."""
+    from oracle import oracle as O
+
+    sim = water_sim(tmp_path, n=2_000_000)
+    dose = sim.actors["dose"]
+    dose.uncertainty_goal = 0.05
+    dose.uncertainty_first_check_after_n_events = 20_000
+    sim.run()
+    n = dose.number_of_samples
+    assert 20_000 <= n < 2_000_000
+    edep = dose.edep.get_data().array
+    e2 = dose.edep_squared.get_data().array
+    from opengate_gb300 import dose as D
+
+    assert D.compute_mean_uncertainty(edep, e2, n) <= 0.05
+    # the run went in chunks between the checks: the oracle replays the same chunks
+    scene, *_ = sim.build_scene()
+    e = np.zeros_like(edep)
+    e2o = np.zeros_like(e2)
+    done = 0
+    for upto, _ in dose.uncertainty_checks:
+        a, b, _ = O.run_dose(scene, upto - done, sim.last_seed, first=done, threads=8)
+        e += a
+        e2o += b
+        done = upto
+    assert done == n and len(dose.uncertainty_checks) >= 2
+    assert np.array_equal(edep, e) and np.array_equal(e2, e2o)
+
+
+def test_spect_simulation_matches_oracle(tmp_path, built_lib):
+    """SPECT through the API (contrib helpers, VoxelSource, projection actors) equals the oracle."""
+    from oracle import oracle as O
+
+    from .test_cpu_api_spect import spect_sim
+
+    sim, heads = spect_sim(tmp_path, n_per_run=300_000, angles=3)
+    sim.random_seed = 4321
+    sim.run()
+    scene, sp, sources, projs, head_of = sim.build_spect()
+    ref, _ = O.run_spect(scene, sp, 300_000, 4321, threads=8)
+    for head, digi in heads:
+        proj = digi.projection.counts.get_data().array
+        np.testing.assert_array_equal(proj, ref[head_of[digi.projection.attached_to]])
+        assert digi.projection.counts.get_output_path().exists()
+    assert ref.sum() > 0
