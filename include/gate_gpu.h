@@ -351,6 +351,39 @@ int gg_spect_use_arf(gg_ctx *ctx, int32_t enable);
 int gg_last_stage_ms(gg_ctx *ctx, double *phantom_ms, double *head_ms, double *arf_ms);
 int gg_get_arf_projection(gg_ctx *ctx, double *counts, double *squared, size_t n);
 
+/* ---- batched simulations (one set of launches for many simulations) ---------
+   Many independent dose simulations - each with its own image, source,
+   primaries, seed and DoseActor tally - sharing the tables and the world run
+   through one persistent launch per batch of histories (the uneven
+   simulations of a parameter study or a multi-patient queue; the reference
+   runs them as separate Simulation objects, opengate/managers.py:1805).
+   History i of simulation k uses the Philox stream (seed_k, i), so each
+   simulation's images equal those of a gg_run of it alone (same seed,
+   first history 0).  Sources: point/box/sphere/disc, iso/momentum/focused,
+   mono/range (no spectra, voxel sources or acceptance boxes).
+   gg_batch_setup replaces the context's volume, source and tally (upload the
+   tables and set the world first); every simulation keeps its own majorant.  gg_batch_run simulates all primaries;
+   gg_batch_capture records the launch sequence of one gg_batch_run in a CUDA
+   graph and gg_batch_replay replays it (the same histories again, images
+   accumulate: call gg_reset_tally between replays to repeat a step).
+   gg_batch_autotune times gg_batch_run for a few launch configurations
+   (blocks per SM, refill / interaction thresholds) and keeps the fastest in
+   the context (*best, may be NULL); images are reset afterwards.
+   gg_batch_get_image returns simulation `sim`'s image (its n voxels). */
+typedef struct {
+  gg_volume_desc volume;
+  gg_source_desc source;
+  uint64_t n_primaries;
+  uint64_t seed;
+} gg_sim_desc;
+
+int gg_batch_setup(gg_ctx *ctx, const gg_sim_desc *sims, int32_t n_sims);
+int gg_batch_run(gg_ctx *ctx);
+int gg_batch_capture(gg_ctx *ctx);
+int gg_batch_replay(gg_ctx *ctx);
+int gg_batch_autotune(gg_ctx *ctx, gg_device_opts *best);
+int gg_batch_get_image(gg_ctx *ctx, int32_t sim, int32_t which, double *out, size_t n);
+
 /* ---- dose run that allocates no device memory ------------------------------
  * No counterpart in the reference.  For callers that cannot call cudaMalloc
  * while they work: cudaMalloc/cudaFree synchronise the whole device (a caller

@@ -128,6 +128,15 @@ class ArfTrainOpts(ctypes.Structure):
     ]
 
 
+class SimDescC(ctypes.Structure):
+    _fields_ = [
+        ("volume", VolumeDesc),
+        ("source", SourceDesc),
+        ("n_primaries", ctypes.c_uint64),
+        ("seed", ctypes.c_uint64),
+    ]
+
+
 GG_ARF_N_PARAMS = 35600
 
 
@@ -176,6 +185,12 @@ PROTOTYPES = [
      [ctypes.c_void_p, ctypes.POINTER(ctypes.c_float), ctypes.c_uint64, ctypes.POINTER(ctypes.c_float)]),
     ("gg_arf_gradient", ctypes.c_int,
      [ctypes.c_void_p, ctypes.POINTER(ctypes.c_float), ctypes.c_uint64, ctypes.POINTER(ctypes.c_float), _f64p]),
+    ("gg_batch_setup", ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(SimDescC), ctypes.c_int32]),
+    ("gg_batch_run", ctypes.c_int, [ctypes.c_void_p]),
+    ("gg_batch_capture", ctypes.c_int, [ctypes.c_void_p]),
+    ("gg_batch_replay", ctypes.c_int, [ctypes.c_void_p]),
+    ("gg_batch_autotune", ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(DeviceOpts)]),
+    ("gg_batch_get_image", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, _f64p, ctypes.c_size_t]),
     ("gg_spect_use_arf", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
     ("gg_last_stage_ms", ctypes.c_int, [ctypes.c_void_p, _f64p, _f64p, _f64p]),
     ("gg_get_arf_projection", ctypes.c_int, [ctypes.c_void_p, _f64p, _f64p, ctypes.c_size_t]),

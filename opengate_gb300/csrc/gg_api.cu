@@ -122,6 +122,15 @@ struct gg_ctx {
   size_t io_cap = 0;
   gg_arf_model arf{};
   bool have_arf = false;
+
+  // batched simulations
+  bool have_batch = false;
+  int n_sims = 0;
+  std::vector<uint64_t> sim_vox_off, sim_vox_n;
+  uint64_t batch_total = 0;
+  void *d_sims = nullptr, *d_sim_maj = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t graph_exec = nullptr;
   std::vector<cudaEvent_t> ev;
   double last_generate_ms = 0, last_transport_ms = 0, last_flush_ms = 0;
   int last_launches = 0, last_stage_launches = 0, run_stage_launches = 0;
@@ -202,6 +211,11 @@ struct gg_ctx {
     arf_rows_cap = 0;
     dfree(d_params); dfree(d_adam_m); dfree(d_adam_v); dfree(d_grad); dfree(d_partial); dfree(d_loss_part);
     dfree(d_loss_acc); dfree(d_wbf); dfree(d_io_rows); dfree(d_io_out);
+    dfree(d_sims); dfree(d_sim_maj);
+    if (graph_exec) cudaGraphExecDestroy(graph_exec);
+    if (graph) cudaGraphDestroy(graph);
+    graph_exec = nullptr;
+    graph = nullptr;
     partial_tiles = 0;
     io_cap = 0;
     q_cap = 0;
@@ -242,6 +256,9 @@ struct gg_ctx {
       s.whalf[a] = (real)world.half_size[a];
     }
     s.labels = d_labels;
+    s.sims = have_batch ? (const gg::SimDesc<real> *)d_sims : nullptr;
+    s.sim_maj = have_batch ? (const real *)d_sim_maj : nullptr;
+    s.n_sims = have_batch ? n_sims : 0;
     s.world_mat = world.material;
     s.pos_type = src.pos_type;
     s.dir_type = src.dir_type;
@@ -480,6 +497,71 @@ static int arf_projection_alloc(gg_ctx *c, size_t n) {
   return c->cuda(cudaMemsetAsync(c->d_arf_proj2, 0, n * 16, c->stream), "memset");
 }
 
+// ---- batched simulations -----------------------------------------------------
+// Descriptor of one simulation with the same conversions as gg_ctx::scene()
+// for a single simulation (so a batched simulation equals its run alone).
+template <typename real>
+static gg::SimDesc<real> sim_desc(const gg_sim_desc &d, uint64_t h_begin, uint64_t vox_off) {
+  gg::SimDesc<real> o;
+  memset(&o, 0, sizeof(o));
+  o.h_begin = h_begin;
+  o.n = d.n_primaries;
+  o.seed = d.seed;
+  o.vox_off = vox_off;
+  const gg_volume_desc &v = d.volume;
+  o.nx = v.dims[0];
+  o.ny = v.dims[1];
+  o.nz = v.dims[2];
+  for (int a = 0; a < 3; ++a) {
+    o.bmin[a] = (real)v.corner[a];
+    o.bmax[a] = (real)(v.corner[a] + (double)v.dims[a] * v.spacing[a]);
+    o.inv_sp[a] = (real)(1.0 / v.spacing[a]);
+  }
+  const gg_source_desc &src = d.source;
+  o.pos_type = src.pos_type;
+  o.dir_type = src.dir_type;
+  o.ene_type = src.ene_type;
+  for (int a = 0; a < 3; ++a) {
+    o.s_t[a] = (real)src.translation[a];
+    o.s_half[a] = (real)src.half_size[a];
+    o.s_focus[a] = (real)src.focus[a];
+  }
+  for (int k = 0; k < 9; ++k) o.s_rot[k] = (real)src.rotation[k];
+  o.s_radius = (real)src.radius;
+  o.s_cos_tmin = (real)cos(src.theta[0]);
+  o.s_cos_tmax = (real)cos(src.theta[1]);
+  o.s_phi0_turn = (real)(src.phi[0] / (2.0 * M_PI));
+  o.s_dphi_turn = (real)((src.phi[1] - src.phi[0]) / (2.0 * M_PI));
+  double mn = sqrt(src.momentum[0] * src.momentum[0] + src.momentum[1] * src.momentum[1] +
+                   src.momentum[2] * src.momentum[2]);
+  for (int a = 0; a < 3; ++a) o.s_mom[a] = (real)(mn > 0 ? src.momentum[a] / mn : 0.0);
+  o.s_mono = (real)src.mono;
+  o.s_elo = (real)src.e_lo;
+  o.s_ehi = (real)src.e_hi;
+  return o;
+}
+
+template <typename real>
+static int upload_sims(gg_ctx *c, const gg_sim_desc *sims, int n) {
+  std::vector<gg::SimDesc<real>> h(n);
+  uint64_t hb = 0;
+  for (int k = 0; k < n; ++k) {
+    h[k] = sim_desc<real>(sims[k], hb, c->sim_vox_off[k]);
+    hb += sims[k].n_primaries;
+  }
+  dfree(c->d_sims);
+  int st = c->cuda(cudaMalloc(&c->d_sims, n * sizeof(gg::SimDesc<real>)), "cudaMalloc simulations");
+  if (st) return st;
+  return c->h2d(c->d_sims, h.data(), n * sizeof(gg::SimDesc<real>), "upload simulations");
+}
+
+static void drop_graph(gg_ctx *c) {
+  if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
+  if (c->graph) cudaGraphDestroy(c->graph);
+  c->graph_exec = nullptr;
+  c->graph = nullptr;
+}
+
 extern "C" {
 
 int gg_create(const gg_device_opts *opts, gg_ctx **out) {
@@ -597,6 +679,10 @@ int gg_upload_tables(gg_ctx *c, const gg_tables_desc *t) {
 }
 
 int gg_upload_volume(gg_ctx *c, const gg_volume_desc *v) {
+  if (c) {
+    c->have_batch = false;  // a single image replaces the batched simulations
+    drop_graph(c);
+  }
   if (!c || !v) return GG_ERR_ARG;
   cudaSetDevice(c->device);
   if (!c->have_tables) return c->fail(GG_ERR_STATE, "gg_upload_volume: upload the tables first");
@@ -648,6 +734,7 @@ int gg_set_world(gg_ctx *c, const gg_world_desc *w) {
 
 int gg_set_source(gg_ctx *c, const gg_source_desc *s) {
   if (!c || !s) return GG_ERR_ARG;
+  if (c->have_batch) return c->fail(GG_ERR_STATE, "gg_set_source: batched simulations carry their own sources");
   cudaSetDevice(c->device);
   if (!c->have_tables) return c->fail(GG_ERR_STATE, "gg_set_source: upload the tables first");
   if (s->pos_type < GG_POS_POINT || s->pos_type > GG_POS_VOXELS) return c->fail(GG_ERR_ARG, "gg_set_source: position type");
@@ -859,11 +946,15 @@ static int spect_stages(gg_ctx *c, gg::KernelArgs a, size_t smem, int minb) {
   return GG_OK;
 }
 
-static int run_impl(gg_ctx *c, uint64_t n, uint64_t seed, uint64_t first) {
+// capturing: enqueue the launches only (no events, no host synchronisation),
+// for a CUDA-graph capture of the stream
+static int run_impl(gg_ctx *c, uint64_t n, uint64_t seed, uint64_t first, bool capturing = false) {
   size_t smem = c->precision == GG_PREC_F64 ? gg::transport_smem_bytes<double>(c->n_comp, c->n_e, c->n_mat)
                                             : gg::transport_smem_bytes<float>(c->n_comp, c->n_e, c->n_mat);
   // kernel variant: register budget for `minb` resident 256-thread blocks
-  int minb = c->blocks_per_sm > 0 ? std::min(c->blocks_per_sm, 4) : (c->precision == GG_PREC_F64 ? 2 : 3);
+  // batched simulations bind their geometry per history: more live registers, default 2 blocks / SM
+  int minb = c->blocks_per_sm > 0 ? std::min(c->blocks_per_sm, 4)
+                                  : ((c->precision == GG_PREC_F64 || c->have_batch) ? 2 : 3);
   int bps = 0;
   {
     cudaError_t e = c->precision == GG_PREC_F64 ? gg::occupancy_blocks<double>(c->block, smem, minb, &bps)
@@ -921,11 +1012,11 @@ static int run_impl(gg_ctx *c, uint64_t n, uint64_t seed, uint64_t first) {
     a.h_begin = first + b * (uint64_t)c->batch;
     a.h_end = std::min(first + n, a.h_begin + (uint64_t)c->batch);
     if ((st = c->cuda(cudaMemsetAsync(c->d_next, 0, 8, c->stream), "memset"))) return st;
-    if ((st = c->cuda(cudaEventRecord(c->ev[3 * b], c->stream), "event"))) return st;
+    if (!capturing && (st = c->cuda(cudaEventRecord(c->ev[3 * b], c->stream), "event"))) return st;
     cudaError_t e = c->precision == GG_PREC_F64 ? gg::launch_generate<double>(c->scene<double>(), a, c->stream)
                                                 : gg::launch_generate<float>(c->scene<float>(), a, c->stream);
     if ((st = c->cuda(e, "generate launch"))) return st;
-    if ((st = c->cuda(cudaEventRecord(c->ev[3 * b + 1], c->stream), "event"))) return st;
+    if (!capturing && (st = c->cuda(cudaEventRecord(c->ev[3 * b + 1], c->stream), "event"))) return st;
     if (c->have_spect) {
       if ((st = spect_stages(c, a, smem, minb))) return st;
       c->run_stage_launches += c->last_stage_launches;
@@ -935,13 +1026,14 @@ static int run_impl(gg_ctx *c, uint64_t n, uint64_t seed, uint64_t first) {
               : gg::launch_transport<float>(c->scene<float>(), a, grid, c->block, smem, minb, c->stream);
       if ((st = c->cuda(e, "transport launch"))) return st;
     }
-    if ((st = c->cuda(cudaEventRecord(c->ev[3 * b + 2], c->stream), "event"))) return st;
+    if (!capturing && (st = c->cuda(cudaEventRecord(c->ev[3 * b + 2], c->stream), "event"))) return st;
     if (c->have_tally &&
         (st = c->cuda(gg::launch_flush(c->d_acc_e, a.acc_e2, c->d_edep, c->squared ? c->d_edep2 : nullptr,
                                        c->n_vox, flush_grid, c->stream),
                       "flush launch")))
       return st;
   }
+  if (capturing) return GG_OK;
   if ((st = c->cuda(cudaEventRecord(c->ev[3 * nb], c->stream), "event"))) return st;
   if ((st = c->cuda(cudaStreamSynchronize(c->stream), "transport"))) return st;
   double tg = 0, tt = 0, tf = 0;
@@ -972,6 +1064,7 @@ static int run_impl(gg_ctx *c, uint64_t n, uint64_t seed, uint64_t first) {
 
 int gg_run(gg_ctx *c, uint64_t n, uint64_t seed, uint64_t first) {
   if (!c) return GG_ERR_ARG;
+  if (c->have_batch) return c->fail(GG_ERR_STATE, "gg_run: batched simulations run with gg_batch_run");
   cudaSetDevice(c->device);
   // SPECT heads are tracked for photons below the pair threshold only (no
   // secondary can be created inside a head)
@@ -1360,6 +1453,189 @@ int gg_get_arf_projection(gg_ctx *c, double *counts, double *squared, size_t n) 
     }
   }
   return GG_OK;
+}
+
+int gg_batch_setup(gg_ctx *c, const gg_sim_desc *sims, int32_t n) {
+  if (!c || !sims || n < 1) return GG_ERR_ARG;
+  cudaSetDevice(c->device);
+  if (!c->have_tables || !c->have_world)
+    return c->fail(GG_ERR_STATE, "gg_batch_setup: upload the tables and set the world first");
+  if (c->have_spect) return c->fail(GG_ERR_STATE, "gg_batch_setup: SPECT heads are set up on this context");
+  std::vector<uint64_t> off(n), nv(n);
+  uint64_t total = 0, hist = 0;
+  double emax = 0;
+  for (int k = 0; k < n; ++k) {
+    const gg_volume_desc &v = sims[k].volume;
+    const gg_source_desc &src = sims[k].source;
+    uint64_t m = 1;
+    for (int a = 0; a < 3; ++a) {
+      if (v.dims[a] <= 0 || !(v.spacing[a] > 0)) return c->fail(GG_ERR_ARG, "sim %d: dims and spacing must be > 0", k);
+      if (!(std::fabs(v.corner[a]) + v.dims[a] * v.spacing[a] <= 2.0 * c->world.half_size[a]))
+        return c->fail(GG_ERR_ARG, "sim %d: the image is not inside the world", k);
+      m *= (uint64_t)v.dims[a];
+    }
+    if (!v.labels || !v.majorant) return c->fail(GG_ERR_ARG, "sim %d: labels and majorant needed", k);
+    for (uint64_t i = 0; i < m; ++i)
+      if (v.labels[i] >= c->n_mat) return c->fail(GG_ERR_ARG, "sim %d: label outside the material table", k);
+    for (int i = 0; i < c->n_e; ++i)
+      if (!(v.majorant[i] > 0) || !std::isfinite(v.majorant[i])) return c->fail(GG_ERR_ARG, "sim %d: bad majorant", k);
+    if (src.pos_type < GG_POS_POINT || src.pos_type > GG_POS_DISC || src.dir_type < GG_DIR_ISO ||
+        src.dir_type > GG_DIR_FOCUSED || (src.ene_type != GG_ENE_MONO && src.ene_type != GG_ENE_RANGE) ||
+        src.n_accept != 0)
+      return c->fail(GG_ERR_ARG, "sim %d: batched sources are point/box/sphere/disc, mono or range, no acceptance", k);
+    const double lo = src.ene_type == GG_ENE_MONO ? src.mono : src.e_lo;
+    const double hi = src.ene_type == GG_ENE_MONO ? src.mono : src.e_hi;
+    if (!(lo >= c->e_min) || !(hi <= c->e_max)) return c->fail(GG_ERR_DOMAIN, "sim %d: energies outside the tables", k);
+    emax = std::max(emax, hi);
+    off[k] = total;
+    nv[k] = m;
+    total += m;
+    hist += sims[k].n_primaries;
+  }
+  drop_graph(c);
+  // concatenated labels and majorants (each simulation keeps its own); the
+  // element-wise maximum serves as the context's majorant
+  std::vector<uint16_t> labels(total);
+  std::vector<float> maj(c->n_e, 0.0f), all_maj((size_t)n * c->n_e);
+  for (int k = 0; k < n; ++k) {
+    memcpy(labels.data() + off[k], sims[k].volume.labels, nv[k] * sizeof(uint16_t));
+    for (int i = 0; i < c->n_e; ++i) {
+      maj[i] = std::max(maj[i], sims[k].volume.majorant[i]);
+      all_maj[(size_t)k * c->n_e + i] = sims[k].volume.majorant[i];
+    }
+  }
+  int st;
+  dfree(c->d_labels);
+  if ((st = c->cuda(cudaMalloc(&c->d_labels, total * sizeof(uint16_t)), "cudaMalloc labels"))) return st;
+  if ((st = c->h2d(c->d_labels, labels.data(), total * sizeof(uint16_t), "upload labels"))) return st;
+  if ((st = c->upload_real(c->d_maj, maj.data(), (size_t)c->n_e))) return st;
+  if ((st = c->upload_real(c->d_sim_maj, all_maj.data(), all_maj.size()))) return st;
+  if (total != c->n_vox) {
+    dfree(c->d_acc_e); dfree(c->d_acc_e2); dfree(c->d_edep); dfree(c->d_edep2);
+    c->have_tally = false;
+  }
+  c->n_vox = total;
+  c->dims[0] = c->dims[1] = c->dims[2] = 1;
+  c->have_volume = true;
+  c->sim_vox_off = off;
+  c->sim_vox_n = nv;
+  c->n_sims = n;
+  c->batch_total = hist;
+  st = c->precision == GG_PREC_F64 ? upload_sims<double>(c, sims, n) : upload_sims<float>(c, sims, n);
+  if (st) return st;
+  c->src = sims[0].source;
+  c->src.spec_e = c->src.spec_cdf = nullptr;
+  c->src.accept_boxes = nullptr;
+  c->src.cdf_z = c->src.cdf_y = c->src.cdf_x = nullptr;
+  c->src_emax = emax;
+  c->have_source = true;
+  c->have_batch = true;
+  return gg_add_dose_tally(c, 1);
+}
+
+int gg_batch_run(gg_ctx *c) {
+  if (!c) return GG_ERR_ARG;
+  cudaSetDevice(c->device);
+  if (!c->have_batch || !c->have_tally) return c->fail(GG_ERR_STATE, "gg_batch_run: call gg_batch_setup first");
+  if (c->batch_total == 0) return GG_OK;
+  return run_impl(c, c->batch_total, 0, 0);
+}
+
+int gg_batch_capture(gg_ctx *c) {
+  if (!c) return GG_ERR_ARG;
+  cudaSetDevice(c->device);
+  if (!c->have_batch || !c->have_tally) return c->fail(GG_ERR_STATE, "gg_batch_capture: call gg_batch_setup first");
+  int st;
+  // one regular run first (buffers, kernel attributes, events), then discarded
+  if ((st = gg_batch_run(c))) return st;
+  if ((st = gg_reset_tally(c))) return st;
+  if ((st = c->cuda(cudaStreamSynchronize(c->stream), "capture"))) return st;
+  drop_graph(c);
+  if ((st = c->cuda(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "begin capture"))) return st;
+  int rc = run_impl(c, c->batch_total, 0, 0, true);
+  cudaGraph_t g = nullptr;
+  cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+  if (rc) {
+    if (g) cudaGraphDestroy(g);
+    return rc;
+  }
+  if ((st = c->cuda(e, "end capture"))) return st;
+  c->graph = g;
+  return c->cuda(cudaGraphInstantiate(&c->graph_exec, c->graph, 0), "graph instantiate");
+}
+
+int gg_batch_replay(gg_ctx *c) {
+  if (!c) return GG_ERR_ARG;
+  cudaSetDevice(c->device);
+  if (!c->graph_exec) return c->fail(GG_ERR_STATE, "gg_batch_replay: call gg_batch_capture first");
+  if (c->ev.empty()) return c->fail(GG_ERR_STATE, "gg_batch_replay: no events");
+  int st;
+  if ((st = c->cuda(cudaEventRecord(c->ev[0], c->stream), "event"))) return st;
+  if ((st = c->cuda(cudaGraphLaunch(c->graph_exec, c->stream), "graph launch"))) return st;
+  if ((st = c->cuda(cudaEventRecord(c->ev[1], c->stream), "event"))) return st;
+  if ((st = c->cuda(cudaStreamSynchronize(c->stream), "graph replay"))) return st;
+  float ms = 0;
+  cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]);
+  c->last_generate_ms = 0;
+  c->last_transport_ms = ms;
+  c->last_flush_ms = 0;
+  unsigned int status = 0;
+  if ((st = c->d2h(&status, c->d_status, sizeof(status), "status"))) return st;
+  if (status) return c->fail(GG_ERR_DOMAIN, "gg_batch_replay: kernel status %u", status);
+  return GG_OK;
+}
+
+int gg_batch_autotune(gg_ctx *c, gg_device_opts *best) {
+  if (!c) return GG_ERR_ARG;
+  cudaSetDevice(c->device);
+  if (!c->have_batch || !c->have_tally) return c->fail(GG_ERR_STATE, "gg_batch_autotune: call gg_batch_setup first");
+  const int minbs[3] = {2, 3, 4};
+  const int thresholds[3][2] = {{8, 16}, {4, 8}, {12, 24}};
+  double best_ms = 1e300;
+  int bm = c->blocks_per_sm, br = c->refill_min, bi = c->interact_min;
+  int st;
+  for (int a = 0; a < 3; ++a)
+    for (int b = 0; b < 3; ++b) {
+      c->blocks_per_sm = minbs[a];
+      c->refill_min = thresholds[b][0];
+      c->interact_min = thresholds[b][1];
+      if ((st = gg_reset_tally(c)) || (st = gg_batch_run(c))) return st;
+      const double ms = c->last_generate_ms + c->last_transport_ms + c->last_flush_ms;
+      if (ms < best_ms) {
+        best_ms = ms;
+        bm = minbs[a];
+        br = thresholds[b][0];
+        bi = thresholds[b][1];
+      }
+    }
+  c->blocks_per_sm = bm;
+  c->refill_min = br;
+  c->interact_min = bi;
+  drop_graph(c);
+  if ((st = gg_reset_tally(c))) return st;
+  if (best) {
+    best->device = c->device;
+    best->precision = c->precision;
+    best->block_size = c->block;
+    best->blocks_per_sm = bm;
+    best->chunk = c->chunk;
+    best->batch = (int64_t)c->batch;
+    best->refill_min = br;
+    best->interact_min = bi;
+  }
+  return c->cuda(cudaStreamSynchronize(c->stream), "autotune");
+}
+
+int gg_batch_get_image(gg_ctx *c, int32_t sim, int32_t which, double *out, size_t n) {
+  if (!c || !out) return GG_ERR_ARG;
+  cudaSetDevice(c->device);
+  if (!c->have_batch || !c->have_tally) return c->fail(GG_ERR_STATE, "gg_batch_get_image: no batch");
+  if (sim < 0 || sim >= c->n_sims) return c->fail(GG_ERR_ARG, "gg_batch_get_image: simulation %d of %d", sim, c->n_sims);
+  if (n != c->sim_vox_n[sim]) return c->fail(GG_ERR_ARG, "gg_batch_get_image: buffer has %zu voxels, image %llu", n,
+                                             (unsigned long long)c->sim_vox_n[sim]);
+  const double *src = which == GG_IMG_EDEP ? c->d_edep : (which == GG_IMG_EDEP_SQUARED ? c->d_edep2 : nullptr);
+  if (!src) return c->fail(GG_ERR_ARG, "gg_batch_get_image: image %d", which);
+  return c->d2h(out, src + c->sim_vox_off[sim], n * sizeof(double), "download");
 }
 
 int gg_get_projection(gg_ctx *c, double *out, size_t n) {

@@ -356,6 +356,25 @@ __device__ __forceinline__ void rotate_dir(real &ux, real &uy, real &uz, real co
 
 // ---------------------------------------------------------------------------
 // Scene seen by a kernel; table pointers may point into shared memory.
+// One simulation of a batched launch: many independent simulations (own
+// image, source, seed and tally) share the tables, the world and one set of
+// launches.  History h of the batch belongs to the simulation whose range
+// [h_begin, h_begin + n) contains it; its Philox stream is (seed, h - h_begin),
+// exactly the stream it gets when the simulation runs alone.
+template <typename real>
+struct SimDesc {
+  uint64_t h_begin, n;  // history range in the batch
+  uint64_t seed;        // Philox key
+  uint64_t vox_off;     // first voxel in the concatenated labels and tallies
+  int nx, ny, nz;
+  int pos_type, dir_type, ene_type;
+  real bmin[3], bmax[3], inv_sp[3];
+  real s_t[3], s_half[3], s_mom[3], s_focus[3];
+  real s_rot[9];
+  real s_radius, s_mono, s_elo, s_ehi;
+  real s_cos_tmin, s_cos_tmax, s_phi0_turn, s_dphi_turn;
+};
+
 // ---------------------------------------------------------------------------
 template <typename real>
 struct Scene {
@@ -368,6 +387,11 @@ struct Scene {
   int nx, ny, nz;
   real bmin[3], bmax[3], inv_sp[3];
   const uint16_t *labels;
+  // batched simulations (n_sims > 0: labels is the concatenation of their
+  // images, sim_maj their majorants [n_sims][n_e])
+  const SimDesc<real> *sims;
+  const real *sim_maj;
+  int n_sims;
   // world
   real whalf[3];
   int world_mat;

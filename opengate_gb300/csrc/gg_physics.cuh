@@ -452,6 +452,7 @@ struct Records {
   real *px, *py, *pz, *dx, *dy, *dz, *e;
   uint32_t *flags;    // bits 0-1 state, bit 2 steps already taken (0/1)
   uint32_t *rng_pos;  // block << 3 | index in buffer
+  uint32_t *sim;      // simulation of the history (batched launches)
 
   __device__ __forceinline__ static Records carve(void *base, size_t cap) {
     Records r;
@@ -466,6 +467,8 @@ struct Records {
     r.flags = reinterpret_cast<uint32_t *>(p);
     p += cap * sizeof(uint32_t);
     r.rng_pos = reinterpret_cast<uint32_t *>(p);
+    p += cap * sizeof(uint32_t);
+    r.sim = reinterpret_cast<uint32_t *>(p);
     return r;
   }
 };
@@ -626,6 +629,62 @@ __device__ __forceinline__ void pop_secondary(const Scene<real> &s, Photon<real>
   ph.alive = 1;
   set_energy(s, ph, R<real>(kMC2));
   start_photon(s, ph);
+}
+
+// Batched launches: the lane's scene geometry, source and tally pointers
+// become those of simulation d (bound once per history; the rest of the
+// transport code then runs unchanged).
+template <typename real>
+__device__ __forceinline__ void bind_geometry(Scene<real> &s, const SimDesc<real> &d, const uint16_t *labels_base,
+                                              const real *maj) {
+  s.maj = maj;  // the simulation's own majorant: its Woodcock steps equal those of a run alone
+  s.nx = d.nx;
+  s.ny = d.ny;
+  s.nz = d.nz;
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    s.bmin[a] = d.bmin[a];
+    s.bmax[a] = d.bmax[a];
+    s.inv_sp[a] = d.inv_sp[a];
+  }
+  s.labels = labels_base + d.vox_off;
+}
+
+template <typename real>
+__device__ __forceinline__ void bind_source(Scene<real> &s, const SimDesc<real> &d) {
+  s.pos_type = d.pos_type;
+  s.dir_type = d.dir_type;
+  s.ene_type = d.ene_type;
+  s.n_accept = 0;
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    s.s_t[a] = d.s_t[a];
+    s.s_half[a] = d.s_half[a];
+    s.s_mom[a] = d.s_mom[a];
+    s.s_focus[a] = d.s_focus[a];
+  }
+#pragma unroll
+  for (int k = 0; k < 9; ++k) s.s_rot[k] = d.s_rot[k];
+  s.s_radius = d.s_radius;
+  s.s_mono = d.s_mono;
+  s.s_elo = d.s_elo;
+  s.s_ehi = d.s_ehi;
+  s.s_cos_tmin = d.s_cos_tmin;
+  s.s_cos_tmax = d.s_cos_tmax;
+  s.s_phi0_turn = d.s_phi0_turn;
+  s.s_dphi_turn = d.s_dphi_turn;
+}
+
+// Simulation containing batch history h (binary search over the ranges).
+template <typename real>
+__device__ __forceinline__ int find_sim(const SimDesc<real> *sims, int n_sims, uint64_t h) {
+  int lo = 0, hi = n_sims - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (sims[mid].h_begin <= h) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
 }
 
 }  // namespace gg

@@ -38,7 +38,9 @@ namespace gg {
 // (GateGenericSource::GeneratePrimaries order), places it, and performs the
 // first transport iteration when the photon starts in the world (free flight
 // to the image, to an air interaction, or out of the world).
-template <typename real>
+// MULTI: batched simulations (Scene::sims): the thread's history picks its
+// simulation, whose geometry, source and Philox key it then uses.
+template <typename real, bool MULTI>
 __global__ void __launch_bounds__(256) k_generate(Scene<real> s, KernelArgs a) {
   __shared__ BlockCounters bc;
   __shared__ unsigned int n_world;
@@ -52,7 +54,17 @@ __global__ void __launch_bounds__(256) k_generate(Scene<real> s, KernelArgs a) {
   if (i < n) {
     Records<real> rec = Records<real>::carve(a.records, a.rec_cap);
     Rng g;
-    g.init(a.seed, a.h_begin + i, 0u);
+    uint32_t sim = 0;
+    if constexpr (MULTI) {
+      const uint64_t h = a.h_begin + i;
+      sim = (uint32_t)find_sim(s.sims, s.n_sims, h);
+      const SimDesc<real> &d = s.sims[sim];
+      bind_geometry(s, d, s.labels, s.sim_maj + (size_t)sim * s.n_e);
+      bind_source(s, d);
+      g.init(d.seed, h - d.h_begin, 0u);
+    } else {
+      g.init(a.seed, a.h_begin + i, 0u);
+    }
     Photon<real> ph;
     uint32_t state = kRecDead, steps = 0;
     int st = sample_primary(s, g, ph, &bc);
@@ -101,6 +113,7 @@ __global__ void __launch_bounds__(256) k_generate(Scene<real> s, KernelArgs a) {
     rec.flags[i] = state | (steps << 2);
     rec.rng_pos[i] = (g.blk << 3) | (uint32_t)g.idx;
     rec.rng_buf[i] = make_uint4(g.buf[0], g.buf[1], g.buf[2], g.buf[3]);
+    rec.sim[i] = sim;
   }
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -124,7 +137,7 @@ __global__ void __launch_bounds__(256) k_generate(Scene<real> s, KernelArgs a) {
 // operations inside each history, and hence its result, is unchanged.
 // MINB = resident blocks per SM the register budget is sized for.
 // SPECT selects the head transport and projection scoring instead of the dose tally.
-template <typename real, int MINB, bool SPECT>
+template <typename real, int MINB, bool SPECT, bool MULTI>
 __global__ void __launch_bounds__(256, MINB) k_transport(Scene<real> sg, KernelArgs args) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ BlockCounters bc;
@@ -216,6 +229,18 @@ __global__ void __launch_bounds__(256, MINB) k_transport(Scene<real> sg, KernelA
           const uint32_t f = rec.flags[h];
           const uint32_t rs = f & 3u;
           if (rs != kRecDead) {
+            uint64_t hid = args.h_begin + h;
+            uint64_t key = args.seed;
+            if constexpr (MULTI) {
+              // batched simulations: this history's geometry, majorant, tally and Philox stream
+              const uint32_t k = rec.sim[h];
+              const SimDesc<real> &d = sg.sims[k];
+              bind_geometry(s, d, sg.labels, sg.sim_maj + (size_t)k * sg.n_e);
+              t.acc_e = args.acc_e + d.vox_off;
+              t.acc_e2 = args.acc_e2 ? args.acc_e2 + 2 * d.vox_off : nullptr;
+              key = d.seed;
+              hid = hid - d.h_begin;
+            }
             ph.pos[0] = rec.px[h];
             ph.pos[1] = rec.py[h];
             ph.pos[2] = rec.pz[h];
@@ -228,15 +253,14 @@ __global__ void __launch_bounds__(256, MINB) k_transport(Scene<real> sg, KernelA
             ph.can_enter = 1;
             ph.in_head = 0;
             ph.exclude = -1;
-            const uint64_t hid = args.h_begin + h;
             if constexpr (SPECT) {
               ev.clear();
               ph.run = s.run_base + (int)((hid - s.run_first) / s.run_len);
             }
             const uint32_t rp = rec.rng_pos[h];
             const uint4 b = rec.rng_buf[h];
-            g.k0 = (uint32_t)args.seed;
-            g.k1 = (uint32_t)(args.seed >> 32);
+            g.k0 = (uint32_t)key;
+            g.k1 = (uint32_t)(key >> 32);
             g.stream = 0u;
             g.h0 = (uint32_t)hid;
             g.h1 = (uint32_t)(hid >> 32);
@@ -338,28 +362,29 @@ size_t transport_smem_bytes(int n_comp, int n_e, int n_mat) {
 
 template <typename real>
 size_t record_bytes(size_t cap) {
-  return cap * (sizeof(uint4) + 7 * sizeof(real) + 2 * sizeof(uint32_t));
+  return cap * (sizeof(uint4) + 7 * sizeof(real) + 3 * sizeof(uint32_t));
 }
 
 template <typename real>
 cudaError_t launch_generate(const Scene<real> &s, const KernelArgs &a, cudaStream_t st) {
   uint64_t n = a.h_end - a.h_begin;
   unsigned int blocks = (unsigned int)((n + 255) / 256);
-  k_generate<real><<<blocks, 256, 0, st>>>(s, a);
+  if (s.n_sims > 0) k_generate<real, true><<<blocks, 256, 0, st>>>(s, a);
+  else k_generate<real, false><<<blocks, 256, 0, st>>>(s, a);
   return cudaGetLastError();
 }
 
-template <typename real, int MINB, bool SPECT>
+template <typename real, int MINB, bool MULTI>
 static cudaError_t launch_transport_v(const Scene<real> &s, const KernelArgs &a, int grid, int block, size_t smem,
                                       cudaStream_t st) {
   static bool configured = false;
   if (!configured) {
-    cudaError_t e = cudaFuncSetAttribute(k_transport<real, MINB, SPECT>,
+    cudaError_t e = cudaFuncSetAttribute(k_transport<real, MINB, false, MULTI>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     if (e != cudaSuccess) return e;
     configured = true;
   }
-  k_transport<real, MINB, SPECT><<<grid, block, smem, st>>>(s, a);
+  k_transport<real, MINB, false, MULTI><<<grid, block, smem, st>>>(s, a);
   return cudaGetLastError();
 }
 
@@ -368,6 +393,11 @@ cudaError_t launch_transport(const Scene<real> &s, const KernelArgs &a, int grid
                              int minb, cudaStream_t st) {
   // SPECT runs use the two-stage kernels of gg_spect.cu
   if (s.spect) return cudaErrorInvalidValue;
+  if (s.n_sims > 0) {
+    if (minb <= 2) return launch_transport_v<real, 2, true>(s, a, grid, block, smem, st);
+    if (minb == 3) return launch_transport_v<real, 3, true>(s, a, grid, block, smem, st);
+    return launch_transport_v<real, 4, true>(s, a, grid, block, smem, st);
+  }
   if (minb <= 2) return launch_transport_v<real, 2, false>(s, a, grid, block, smem, st);
   if (minb == 3) return launch_transport_v<real, 3, false>(s, a, grid, block, smem, st);
   return launch_transport_v<real, 4, false>(s, a, grid, block, smem, st);
@@ -381,9 +411,9 @@ cudaError_t launch_flush(unsigned long long *acc_e, unsigned long long *acc_e2, 
 
 template <typename real>
 cudaError_t occupancy_blocks(int block, size_t smem, int minb, int *bps) {
-  if (minb <= 2) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(bps, k_transport<real, 2, false>, block, smem);
-  if (minb == 3) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(bps, k_transport<real, 3, false>, block, smem);
-  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(bps, k_transport<real, 4, false>, block, smem);
+  if (minb <= 2) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(bps, k_transport<real, 2, false, false>, block, smem);
+  if (minb == 3) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(bps, k_transport<real, 3, false, false>, block, smem);
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(bps, k_transport<real, 4, false, false>, block, smem);
 }
 
 template size_t record_bytes<float>(size_t);

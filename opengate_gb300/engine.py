@@ -234,3 +234,87 @@ class ArfNetwork:
         self.eng._call("gg_arf_gradient", C.ptr(rows, ctypes.c_float), ctypes.c_uint64(len(rows)),
                        C.ptr(g, ctypes.c_float), ctypes.byref(loss))
         return loss.value, g
+
+
+class BatchEngine:
+    """Many dose simulations in one set of launches (gg_batch_*): `sims` is a
+    list of (Scene, n_primaries, seed) sharing one material table and world."""
+
+    def __init__(self, sims, device=0, precision=32, batch=0, blocks_per_sm=0):
+        self.lib = C.load()
+        self.sims = sims
+        opts = C.DeviceOpts(device, precision, 0, blocks_per_sm, 0, batch, 0, 0)
+        ctx = ctypes.c_void_p()
+        C.check(self.lib, None, self.lib.gg_create(ctypes.byref(opts), ctypes.byref(ctx)))
+        self.ctx = ctx
+        self.upload()
+
+    def _call(self, name, *args):
+        C.check(self.lib, self.ctx, getattr(self.lib, name)(self.ctx, *args))
+
+    def upload(self):
+        first = self.sims[0][0]
+        self._call("gg_upload_tables", ctypes.byref(first.tables_desc))
+        self._call("gg_set_world", ctypes.byref(first.world_desc))
+        arr = (C.SimDescC * len(self.sims))()
+        for k, (scene, n, seed) in enumerate(self.sims):
+            arr[k].volume = scene.volume_desc
+            arr[k].source = scene.source_desc
+            arr[k].n_primaries = int(n)
+            arr[k].seed = int(seed)
+        self._descs = arr  # the descriptors point into the scenes' arrays
+        self._call("gg_batch_setup", arr, len(self.sims))
+
+    @property
+    def total_primaries(self):
+        return int(sum(n for _, n, _ in self.sims))
+
+    def run(self):
+        self._call("gg_batch_run")
+
+    def capture(self):
+        self._call("gg_batch_capture")
+
+    def replay(self):
+        self._call("gg_batch_replay")
+
+    def autotune(self):
+        best = C.DeviceOpts()
+        self._call("gg_batch_autotune", ctypes.byref(best))
+        return best
+
+    def reset(self):
+        self._call("gg_reset_tally")
+
+    def image(self, k, which):
+        scene = self.sims[k][0]
+        out = np.empty(scene.n_voxels, dtype=np.float64)
+        self._call("gg_batch_get_image", k, which, C.ptr(out, ctypes.c_double), out.size)
+        return out.reshape(scene.labels.shape)
+
+    def counters(self):
+        out = np.zeros(C.GG_N_COUNTERS, dtype=np.uint64)
+        self._call("gg_get_counters", C.ptr(out, ctypes.c_uint64), out.size)
+        return {name: int(out[i]) for i, name in enumerate(C.COUNTER_NAMES)}
+
+    def last_kernel_ms(self):
+        g, t, f, n = ctypes.c_double(), ctypes.c_double(), ctypes.c_double(), ctypes.c_int32()
+        self._call("gg_last_kernel_ms", ctypes.byref(g), ctypes.byref(t), ctypes.byref(f), ctypes.byref(n))
+        return g.value, t.value, f.value, n.value
+
+    def close(self):
+        if self.ctx:
+            self.lib.gg_destroy(self.ctx)
+            self.ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()

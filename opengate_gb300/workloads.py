@@ -201,3 +201,48 @@ def spect_phantom(shape=(160, 256, 256), spacing=1.2, nuclide=TC99M, collimator=
                      step_angle_deg=360.0 / n_runs, collimator_material=len(mats) - 2,
                      crystal_material=len(mats) - 1)
     return scene, sp, act
+
+
+# Slab HU values of the batched workload: one per interval of the CT10 table
+# (air, lung, fat, water, muscle, soft tissue, three bone densities)
+SLAB_HU = (-1000, -800, -90, 0, 40, 60, 300, 700, 1200)
+
+
+def batched_phantoms(n_sims=48, seed=20241203, sides=(32, 48, 64, 96, 128), spacing_range=(1.0, 3.0),
+                     energy_range=(0.05, 2.0), primaries_range=(1e5, 1e7), density_tolerance=0.05):
+    """Uneven simulations of one batched launch: (tables, [(Scene, n_primaries, seed), ...]).
+
+    Each simulation: a cube of `side` voxels (drawn from `sides`) with spacing
+    uniform in spacing_range, 1-4 slabs along z of HU drawn from SLAB_HU
+    (through the CT10 HU -> material table), a monoenergetic disc beam (1 cm
+    radius, +z, on the entrance face) with energy log-uniform in energy_range
+    and primaries log-uniform in primaries_range.  All simulations share the
+    material table and the 1 m air world.
+    """
+    rng = np.random.default_rng(seed)
+    vm, lut, mats = ct_materials(density_tolerance)
+    pt = T.PhysicsTables(mats)
+    out = []
+    for k in range(n_sims):
+        side = int(rng.choice(sides))
+        sp = float(rng.uniform(*spacing_range))
+        n_slabs = int(rng.integers(1, 5))
+        cuts = np.sort(rng.choice(np.arange(1, side), size=n_slabs - 1, replace=False)) if n_slabs > 1 else []
+        hu = np.zeros((side, side, side), np.int16)
+        edges = [0, *cuts, side]
+        for a, b in zip(edges[:-1], edges[1:]):
+            hu[a:b] = int(rng.choice(SLAB_HU))
+        labels = M.create_label_image(hu, "G4_AIR", vm, lut)
+        half = side * sp / 2.0
+        src = SourceSpec()
+        src.pos_type = C.GG_POS_DISC
+        src.radius = 10.0
+        src.translation = [0.0, 0.0, -half - 1.0]
+        src.dir_type = C.GG_DIR_MOMENTUM
+        src.momentum = [0.0, 0.0, 1.0]
+        src.ene_type = C.GG_ENE_MONO
+        src.mono = float(np.exp(rng.uniform(np.log(energy_range[0]), np.log(energy_range[1]))))
+        n = int(np.exp(rng.uniform(np.log(primaries_range[0]), np.log(primaries_range[1]))))
+        scene = Scene(pt, labels, [sp] * 3, [-half] * 3, [500.0] * 3, 0, src)
+        out.append((scene, n, int(seed) * 1000 + k))
+    return pt, out
