@@ -954,7 +954,7 @@ static int run_impl(gg_ctx *c, uint64_t n, uint64_t seed, uint64_t first, bool c
   // kernel variant: register budget for `minb` resident 256-thread blocks
   // batched simulations bind their geometry per history: more live registers, default 2 blocks / SM
   int minb = c->blocks_per_sm > 0 ? std::min(c->blocks_per_sm, 4)
-                                  : ((c->precision == GG_PREC_F64 || c->have_batch) ? 2 : 3);
+                                  : ((c->precision == GG_PREC_F64 || c->have_batch) ? 2 : 4);
   int bps = 0;
   {
     cudaError_t e = c->precision == GG_PREC_F64 ? gg::occupancy_blocks<double>(c->block, smem, minb, &bps)

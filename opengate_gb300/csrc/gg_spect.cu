@@ -161,13 +161,17 @@ __global__ void __launch_bounds__(256, MINB) k_spect_phantom(Scene<real> sg, Ker
   unsigned int n_wood = 0, n_real = 0, n_dep = 0, n_world = 0, n_singles = 0;
 
   for (;;) {
+    // phase chosen per block: all warps run the same code region at the same
+    // time (instruction-cache locality); thresholds are per warp
     const unsigned m_ref = __ballot_sync(0xffffffffu, state == kRefill);
-    const unsigned m_fly = __ballot_sync(0xffffffffu, state == kFly);
-    const unsigned m_int = __ballot_sync(0xffffffffu, state == kInteract);
-    if ((m_ref | m_fly | m_int) == 0u) break;
+    const int c_ref = __syncthreads_count(state == kRefill);
+    const int c_fly = __syncthreads_count(state == kFly);
+    const int c_int = __syncthreads_count(state == kInteract);
+    if (c_ref + c_fly + c_int == 0) break;
+    const int n_warps = (int)(blockDim.x >> 5);
     int phase;
-    if (__popc(m_ref) >= args.refill_min || (m_fly | m_int) == 0u) phase = kRefill;
-    else if (__popc(m_int) >= args.interact_min || m_fly == 0u) phase = kInteract;
+    if (c_ref >= args.refill_min * n_warps || (c_fly + c_int) == 0) phase = kRefill;
+    else if (c_int >= args.interact_min * n_warps || c_fly == 0) phase = kInteract;
     else phase = kFly;
 
     if (phase == kRefill) {
@@ -317,13 +321,17 @@ __global__ void __launch_bounds__(256, MINB) k_spect_head(Scene<real> sg, Kernel
   unsigned int n_dep = 0, n_world = 0, n_head = 0, n_singles = 0;
 
   for (;;) {
+    // phase chosen per block: all warps run the same code region at the same
+    // time (instruction-cache locality); thresholds are per warp
     const unsigned m_ref = __ballot_sync(0xffffffffu, state == kRefill);
-    const unsigned m_fly = __ballot_sync(0xffffffffu, state == kFly);
-    const unsigned m_int = __ballot_sync(0xffffffffu, state == kInteract);
-    if ((m_ref | m_fly | m_int) == 0u) break;
+    const int c_ref = __syncthreads_count(state == kRefill);
+    const int c_fly = __syncthreads_count(state == kFly);
+    const int c_int = __syncthreads_count(state == kInteract);
+    if (c_ref + c_fly + c_int == 0) break;
+    const int n_warps = (int)(blockDim.x >> 5);
     int phase;
-    if (__popc(m_ref) >= args.refill_min || (m_fly | m_int) == 0u) phase = kRefill;
-    else if (__popc(m_int) >= args.interact_min || m_fly == 0u) phase = kInteract;
+    if (c_ref >= args.refill_min * n_warps || (c_fly + c_int) == 0) phase = kRefill;
+    else if (c_int >= args.interact_min * n_warps || c_fly == 0) phase = kInteract;
     else phase = kFly;
 
     if (phase == kRefill) {

@@ -128,13 +128,16 @@ __global__ void __launch_bounds__(256) k_generate(Scene<real> s, KernelArgs a) {
 
 // Transport stage.  Persistent grid; each lane carries one history at a time
 // and is in one of the states kRefill (needs a history), kFly (next event is
-// a flight) or kInteract (a collision is pending).  Every iteration the warp
-// picks ONE phase by ballot - refill when at least refill_min lanes wait for a
-// history, interact when at least interact_min collisions are pending,
-// otherwise fly - and only the lanes in that state execute it.  Expensive
-// code (source-record loads, tally flushes, Compton sampling) therefore runs
-// with many lanes active instead of one lane at a time, while the order of
-// operations inside each history, and hence its result, is unchanged.
+// a flight) or kInteract (a collision is pending).  Every iteration the block
+// picks ONE phase from counts of its lanes' states - refill when at least
+// refill_min lanes per warp wait for a history, interact when at least
+// interact_min collisions per warp are pending, otherwise fly - and only the
+// lanes in that state execute it.  Expensive code (source-record loads, tally
+// flushes, Compton sampling) therefore runs with many lanes active instead of
+// one lane at a time, all warps of a block execute the same code region at
+// the same time (the kernel is bound by instruction fetch, not arithmetic),
+// and the order of operations inside each history, hence its result, is
+// unchanged.
 // MINB = resident blocks per SM the register budget is sized for.
 // SPECT selects the head transport and projection scoring instead of the dose tally.
 template <typename real, int MINB, bool SPECT, bool MULTI>
@@ -191,13 +194,17 @@ __global__ void __launch_bounds__(256, MINB) k_transport(Scene<real> sg, KernelA
   unsigned int n_wood = 0, n_real = 0, n_dep = 0, n_world = 0, n_head = 0, n_singles = 0;
 
   for (;;) {
+    // phase chosen per block: all warps run the same code region at the same
+    // time (instruction-cache locality); thresholds are per warp
     const unsigned m_ref = __ballot_sync(0xffffffffu, state == kRefill);
-    const unsigned m_fly = __ballot_sync(0xffffffffu, state == kFly);
-    const unsigned m_int = __ballot_sync(0xffffffffu, state == kInteract);
-    if ((m_ref | m_fly | m_int) == 0u) break;
+    const int c_ref = __syncthreads_count(state == kRefill);
+    const int c_fly = __syncthreads_count(state == kFly);
+    const int c_int = __syncthreads_count(state == kInteract);
+    if (c_ref + c_fly + c_int == 0) break;
+    const int n_warps = (int)(blockDim.x >> 5);
     int phase;
-    if (__popc(m_ref) >= args.refill_min || (m_fly | m_int) == 0u) phase = kRefill;
-    else if (__popc(m_int) >= args.interact_min || m_fly == 0u) phase = kInteract;
+    if (c_ref >= args.refill_min * n_warps || (c_fly + c_int) == 0) phase = kRefill;
+    else if (c_int >= args.interact_min * n_warps || c_fly == 0) phase = kInteract;
     else phase = kFly;
 
     if (phase == kRefill) {
