@@ -627,6 +627,28 @@ def run_ours_batched(args, ws, rank, local, dist, use_cuda):
     return 0
 
 
+def fp64_error(scene, n, seed, device, batch):
+    """Dose images of n histories in the FP32 and the FP64 build of the same
+    kernels (same seed, same histories) and the error of the first against the
+    second (opengate_gb300.dose.precision_error), with both builds' rates."""
+    import torch
+    from opengate_gb300.dose import precision_error
+    from opengate_gb300.engine import DoseEngine
+
+    imgs, rate = {}, {}
+    for prec in (32, 64):
+        with DoseEngine(scene, device=device, precision=prec, batch=batch) as e:
+            e.run(n, seed, 0)
+            torch.cuda.synchronize()
+            tg, tt, tf, _ = e.last_kernel_ms()
+            rate[prec] = n / ((tg + tt + tf) / 1e3)
+            imgs[prec] = (e.edep(), e.edep_squared())
+    err = precision_error(imgs[32][0], imgs[32][1], imgs[64][0], imgs[64][1], n)
+    err.update({"primaries": n, "seed": seed, "voxels_gt": "10 % of max",
+                "rate_f32": rate[32], "rate_f64": rate[64]})
+    return err
+
+
 def run_ours(args):
     ws, rank, local = dist_env()
     import torch
@@ -716,6 +738,11 @@ def run_ours(args):
                           "transport_launches_per_step": transport_launches},
                 "stage_ms_per_step": stage_ms}
 
+    # error of the FP32 transport against the FP64 build on the same random stream (untimed)
+    fp64 = None
+    if rank == 0 and args.fp64_primaries > 0:
+        fp64 = fp64_error(scene, args.fp64_primaries, args.seed, local, args.batch)
+
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:
         threads = os.cpu_count() or 1
@@ -732,6 +759,7 @@ def run_ours(args):
                        "l2": "flushed between steps (256 MiB write)", "batch": args.batch,
                        "parallelism": f"replicas x{ws}, disjoint history ranges"},
             "sigma": {"mean_relative_uncertainty_gt10pct_max": sigma, "primaries": n},
+            "fp64_error": fp64,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
             "roofline": roofline,
             "cpu_baseline": cpu,
@@ -761,6 +789,8 @@ def main():
     ap.add_argument("--batch", type=int, default=1 << 27)
     ap.add_argument("--seed", type=int, default=20240611)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--fp64-primaries", type=int, default=10_000_000,
+                    help="histories of the FP32-vs-FP64 comparison of the dose workload (0: skip)")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--traffic", type=float, default=None,
                     help="DRAM bytes per transport launch from an ncu capture (reported as-is)")

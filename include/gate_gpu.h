@@ -21,7 +21,8 @@
  *   gg_set_world                world volume (opengate/managers.py:1435 VolumeManager)
  *   gg_set_source               GateGenericSource::InitializePosition/Direction/Energy
  *                               (core/opengate_core/opengate_lib/GateGenericSource.cpp:312-664)
- *   gg_set_voxel_source         GateVoxelSource / GateSPSVoxelsPosDistribution
+ *   gg_set_source, position type GG_POS_VOXELS
+ *                               GateVoxelSource / GateSPSVoxelsPosDistribution
  *                               (core/opengate_core/opengate_lib/GateSPSVoxelsPosDistribution.cpp:29-74)
  *   gg_add_dose_tally           GateDoseActor::InitializeCpp / BeginOfRunAction
  *                               (core/opengate_core/opengate_lib/GateDoseActor.cpp:100-137)

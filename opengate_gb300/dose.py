@@ -16,6 +16,9 @@ Restates the reference's end-of-run arithmetic:
   divide by Gy x voxel volume, squared for the squared image).  When the dose
   grid is the image grid every deposit in a voxel sees that voxel's
   material, so the per-voxel division is exact.
+
+:func:`precision_error` states the error of an FP32 build against the FP64
+build of the same kernels on the same random stream.
 """
 
 import numpy as np
@@ -94,3 +97,44 @@ def compute_mean_uncertainty(edep, edep_squared, n_events, threshold=0.7, top_vo
 def next_uncertainty_check(current, goal, n_events, overshoot=1.05):
     """Events at which the next check happens (GateDoseActor.cpp:269-274)."""
     return int((current / goal) * (current / goal) * n_events * overshoot)
+
+
+def precision_error(edep_a, edep2_a, edep_b, edep2_b, n, threshold=0.1):
+    """Error of image ``a`` against image ``b``, both edep sums of the same ``n``
+    histories on the same random stream (an FP32 build against the FP64 build of
+    the same kernels).
+
+    Histories follow the same draws until a rounding difference changes a
+    decision, so most voxels agree to rounding and the rest differ by a few
+    histories.  Reported over the voxels above ``threshold`` x max of ``b``:
+    integral relative difference (all voxels), fraction of voxels within 2
+    combined standard deviations of the sum (the statistical criterion applied
+    to two independent runs), the largest and the median |a - b| / sigma, the
+    median relative difference, and the fraction of voxels that are equal.
+    """
+    a = np.asarray(edep_a, dtype=np.float64).ravel()
+    b = np.asarray(edep_b, dtype=np.float64).ravel()
+    qa = np.asarray(edep2_a, dtype=np.float64).ravel()
+    qb = np.asarray(edep2_b, dtype=np.float64).ravel()
+    tb = float(b.sum())
+    integral = abs(float(a.sum()) - tb) / tb if tb > 0 else 0.0
+    mask = b > threshold * b.max() if b.size and b.max() > 0 else np.zeros(b.shape, bool)
+    if not mask.any():
+        return {"integral_rel": integral, "voxels": 0}
+    # standard deviation of a sum of n history values: sqrt(n var) = sqrt(q - s^2 / n) * sqrt(n / (n - 1))
+    f = n / (n - 1.0) if n > 1 else 1.0
+    va = np.clip(qa[mask] - a[mask] ** 2 / n, 0, None) * f
+    vb = np.clip(qb[mask] - b[mask] ** 2 / n, 0, None) * f
+    sig = np.sqrt(va + vb)
+    d = np.abs(a[mask] - b[mask])
+    z = np.where(sig > 0, d / np.where(sig > 0, sig, 1.0), np.where(d > 0, np.inf, 0.0))
+    rel = d / b[mask]
+    return {
+        "integral_rel": integral,
+        "voxels": int(mask.sum()),
+        "within_2sigma": float(np.mean(z <= 2.0)),
+        "max_z": float(z.max()),
+        "median_z": float(np.median(z)),
+        "median_rel": float(np.median(rel)),
+        "equal": float(np.mean(d == 0)),
+    }

@@ -64,6 +64,30 @@ def test_mean_uncertainty_criterion():
     assert D.next_uncertainty_check(0.2, 0.1, 1000, 1.05) == int(4 * 1000 * 1.05)
 
 
+def test_precision_error_statement():
+    rng = np.random.default_rng(3)
+    n = 1000
+    # per-history values: sum and sum of squares of n draws per voxel
+    h = rng.exponential(1.0, size=(n, 200))
+    e, e2 = h.sum(0), (h * h).sum(0)
+    same = D.precision_error(e, e2, e.copy(), e2.copy(), n)
+    assert same["integral_rel"] == 0 and same["equal"] == 1.0 and same["within_2sigma"] == 1.0
+    assert same["max_z"] == 0.0
+    # one voxel shifted by 3 combined sigma, one by a rounding-sized amount
+    sig = np.sqrt(2 * (e2 - e * e / n) * n / (n - 1))
+    f = e.copy()
+    f[0] += 3 * sig[0]
+    f[1] *= 1 + 1e-12
+    err = D.precision_error(f, e2, e, e2, n, threshold=0.0)
+    assert err["voxels"] == 200
+    va = np.clip(e2[0] - f[0] ** 2 / n, 0, None) * n / (n - 1)
+    vb = (e2[0] - e[0] ** 2 / n) * n / (n - 1)
+    assert err["max_z"] == pytest.approx(3 * sig[0] / np.sqrt(va + vb), rel=1e-9)
+    assert err["within_2sigma"] == pytest.approx(199 / 200)
+    assert err["equal"] == pytest.approx(198 / 200)
+    assert err["integral_rel"] == pytest.approx((f.sum() - e.sum()) / e.sum(), rel=1e-9)
+
+
 def spect_sim(tmp_path, n_per_run=1000, angles=3):
     sim = gate.Simulation()
     sim.output_dir = tmp_path
