@@ -516,7 +516,8 @@ def run_ours_arf(args, ws, rank, local, dist, use_cuda):
                                  "peak": peaks.get("bf16_tflops"), "unit": "TFLOP/s",
                                  "frac": flop_photon * counters["arf_photons"] / (arf_ms / 1e3) / 1e12 /
                                  peaks.get("bf16_tflops", 1.0),
-                                 "note": "mma.sync m16n8k16 BF16, FP32 accumulate; arf_stage_ms includes the "
+                                 "note": "tcgen05.mma kind::f16 (M 128, N 128 / 16, K 16) BF16, FP32 accumulate "
+                                         "in TMEM; arf_stage_ms includes the "
                                          "queue classification and the projection atomics"},
             "units": {k: counters[k] for k in ("woodcock_steps", "head_steps", "arf_photons", "arf_fallback", "singles")},
             "stage_ms_per_step": stage_ms,

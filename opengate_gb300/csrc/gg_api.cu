@@ -1057,6 +1057,8 @@ static int run_impl(gg_ctx *c, uint64_t n, uint64_t seed, uint64_t first, bool c
     cudaStreamSynchronize(c->stream);
     if (status & gg::kStatusQueueOverflow)
       return c->fail(GG_ERR_QUEUE_OVERFLOW, "gg_run: a SPECT stage queue overflowed (photons were dropped)");
+    if (status & gg::kStatusWaitTimeout)
+      return c->fail(GG_ERR_TIMEOUT, "gg_run: a tensor-core wait of the ARF stage ran out");
     return c->fail(GG_ERR_DOMAIN, "gg_run: source sampling failed (angular acceptance exhausted max_rejection)");
   }
   return GG_OK;
@@ -1263,6 +1265,18 @@ int gg_arf_get_params(gg_ctx *c, float *params, size_t n) {
   return c->d2h(params, c->d_params, n * sizeof(float), "download");
 }
 
+// Reads and clears the status word after a tensor-core kernel.
+static int check_tc_status(gg_ctx *c, const char *what) {
+  unsigned int status = 0;
+  int st;
+  if ((st = c->d2h(&status, c->d_status, sizeof(status), "status"))) return st;
+  if (!status) return GG_OK;
+  cudaMemsetAsync(c->d_status, 0, sizeof(unsigned int), c->stream);
+  cudaStreamSynchronize(c->stream);
+  if (status & gg::kStatusWaitTimeout) return c->fail(GG_ERR_TIMEOUT, "%s: a tensor-core wait ran out", what);
+  return c->fail(GG_ERR_DOMAIN, "%s: kernel status %u", what, status);
+}
+
 int gg_arf_predict(gg_ctx *c, const float *rows, uint64_t n, float *probs) {
   if (!c || (n && (!rows || !probs))) return GG_ERR_ARG;
   cudaSetDevice(c->device);
@@ -1274,10 +1288,13 @@ int gg_arf_predict(gg_ctx *c, const float *rows, uint64_t n, float *probs) {
   gg::MlpTrainArgs a = arf_args(c);
   a.rows = c->d_io_rows;
   a.n_rows = n;
-  const uint64_t tiles = (n + gg::kTileM - 1) / gg::kTileM;
-  const int grid = (int)std::min<uint64_t>(tiles, (uint64_t)c->n_sm * 8);
-  if ((st = c->cuda(gg::launch_mlp_predict(a, c->d_io_out, n, grid, c->stream), "ARF predict"))) return st;
-  return c->d2h(probs, c->d_io_out, n * c->arf.n_classes * sizeof(float), "download");
+  // one CTA per SM (tensor memory and ~200 KB of shared memory each), four 128-row tiles at a time
+  const uint64_t tiles = (n + 511) / 512;
+  const int grid = (int)std::min<uint64_t>(tiles, (uint64_t)c->n_sm);
+  if ((st = c->cuda(gg::launch_mlp_predict(a, c->d_io_out, n, grid, c->d_status, c->stream), "ARF predict")))
+    return st;
+  if ((st = c->d2h(probs, c->d_io_out, n * c->arf.n_classes * sizeof(float), "download"))) return st;
+  return check_tc_status(c, "gg_arf_predict");
 }
 
 int gg_arf_gradient(gg_ctx *c, const float *rows, uint64_t n, float *grad, double *loss) {

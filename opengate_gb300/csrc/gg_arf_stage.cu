@@ -15,10 +15,11 @@
 //   * otherwise (side entry, outside the domain): copied to the fallback
 //     queue, which the plain head stage tracks - the plain path both covers
 //     and bounds what the network does not know.
-// Each warp of a CTA runs its own pipeline over chunks of 32 queued photons
-// (classify, layer 1 on the CUDA cores, layers 2-4 on the tensor cores from
-// the CTA's shared weights, softmax, scatter) with warp-level
-// synchronisation only.  Window weights are w_k = p_k / (RR p_0 +
+// Each warpgroup of a CTA runs its own pipeline over tiles of 128 queued
+// photons, one photon per thread (classify, network forward on tcgen05 from
+// the CTA's shared weights - gg_mlp_tc.cuh -, softmax, scatter) with
+// named-barrier synchronisation inside the group only, so the groups overlap
+// one another's MMAs and epilogues.  Window weights are w_k = p_k / (RR p_0 +
 // sum_k>0 p_k) (class 0 re-weighted by the Russian roulette of its training
 // rows) and go to fixed-point projection tallies (2^-32 units, with the exact
 // square for the history-by-history variance), so projections are
@@ -31,6 +32,7 @@
 #include "gg_device.cuh"
 #include "gg_internal.h"
 #include "gg_mlp.cuh"
+#include "gg_mlp_tc.cuh"
 #include "gg_physics.cuh"
 #include "gg_queue.cuh"
 #include "gg_spect.cuh"
@@ -58,88 +60,36 @@ __device__ __forceinline__ void queue_copy(const PQueue<real> &in, size_t k, con
 
 enum : int { kArfNone = 0, kArfNet = 1, kArfFallback = 2 };
 
-constexpr int kArfWarps = 8;      // warps per CTA, each an independent 32-photon pipeline
-constexpr int kArfRows = 32;      // photons per warp chunk
-
-// Shared memory of the ARF stage: the network's weights once per CTA, and
-// per warp two BF16 activation buffers (ping-pong between layers), the
-// chunk's inputs and projection offsets.
-struct ArfSmem {
-  __nv_bfloat16 w2[kHid * kLds], w3[kHid * kLds], w4[kOutPad * kLds];
-  float w1[kHid * 3], b1[kHid], b2[kHid], b3[kHid], b4[kOutPad];
-  __nv_bfloat16 act[kArfWarps][2][kArfRows * kLds];
-  float x[kArfWarps][kArfRows][3];
-  long long pix[kArfWarps][kArfRows];  // projection offset of window 1, -1: not scored
-};
-
-// One hidden layer for the warp's 32 rows: out = bf16(relu(in W^T + b)).
-__device__ __forceinline__ void arf_hidden(const __nv_bfloat16 *in, const __nv_bfloat16 *w, const float *b,
-                                           __nv_bfloat16 *out) {
-#pragma unroll
-  for (int half = 0; half < 2; ++half) {
-    float acc[2][8][4];
-    zero_acc(acc);
-    warp_gemm<2, 8, false, false>(acc, in, kLds, 0, w, kLds, 64 * half, kHid);
-#pragma unroll
-    for (int mt = 0; mt < 2; ++mt)
-#pragma unroll
-      for (int nt = 0; nt < 8; ++nt)
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          int rr, cc;
-          acc_pos(q, rr, cc);
-          const int col = 64 * half + 8 * nt + cc;
-          const float z = acc[mt][nt][q] + b[col];
-          out[(16 * mt + rr) * kLds + col] = __float2bfloat16_rn(z > 0.0f ? z : 0.0f);
-        }
-  }
-}
-
 template <typename real>
-__global__ void __launch_bounds__(kArfWarps * 32) k_spect_arf(Scene<real> s, ArfStageArgs a) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  ArfSmem &sm = *reinterpret_cast<ArfSmem *>(smem_raw);
+__global__ void __launch_bounds__(kTcThreads, 1) k_spect_arf(Scene<real> s, ArfStageArgs a) {
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  TcNetSmem &sm = *reinterpret_cast<TcNetSmem *>(smem_raw);
   __shared__ unsigned int n_net, n_fb;
   if (threadIdx.x == 0) {
     n_net = 0;
     n_fb = 0;
   }
-  for (int e = threadIdx.x; e < kHid * kHid; e += blockDim.x) {
-    const int row = e / kHid, col = e % kHid;
-    sm.w2[row * kLds + col] = a.wbf[kBfW2 + e];
-    sm.w3[row * kLds + col] = a.wbf[kBfW3 + e];
-  }
-  for (int e = threadIdx.x; e < kOutPad * kHid; e += blockDim.x) {
-    const int row = e / kHid, col = e % kHid;
-    sm.w4[row * kLds + col] = a.wbf[kBfW4 + e];
-  }
-  for (int e = threadIdx.x; e < kHid * 3; e += blockDim.x) sm.w1[e] = a.params[kOffW1 + e];
-  for (int e = threadIdx.x; e < kHid; e += blockDim.x) {
-    sm.b1[e] = a.params[kOffB1 + e];
-    sm.b2[e] = a.params[kOffB2 + e];
-    sm.b3[e] = a.params[kOffB3 + e];
-  }
-  for (int e = threadIdx.x; e < kOutPad; e += blockDim.x) sm.b4[e] = a.params[kOffB4 + e];
-  __syncthreads();
+  tc_net_load(sm, a.params, a.wbf);
+  tc_net_setup(sm);
 
   const PQueue<real> in = PQueue<real>::carve(a.in_q, a.q_cap);
   const PQueue<real> out = PQueue<real>::carve(a.out_q, a.q_cap);
   const uint64_t n_items = min((uint64_t)*a.in_n, (uint64_t)a.q_cap);
-  const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  const unsigned lane = threadIdx.x & 31u;
   const unsigned lt_mask = (1u << lane) - 1u;
+  const int g = threadIdx.x >> 7, r = threadIdx.x & 127, bar = 1 + g;
   const size_t plane = (size_t)s.pny * s.pnx;
-  __nv_bfloat16 *buf0 = sm.act[warp][0], *buf1 = sm.act[warp][1];
-  float (*x)[3] = sm.x[warp];
-  long long *pix = sm.pix[warp];
+  uint32_t phase = 0;
   unsigned int my_net = 0, my_fb = 0;
 
   for (;;) {
-    unsigned long long base = 0;
-    if (lane == 0) base = atomicAdd(a.claim, (unsigned long long)kArfRows);
-    base = __shfl_sync(0xffffffffu, base, 0);
+    // ---- claim a tile of 128 queued photons for the group ----
+    if (r == 0) sm.claim[g] = atomicAdd(a.claim, (unsigned long long)kTcRows);
+    named_bar(bar, kTcRows);
+    const unsigned long long base = sm.claim[g];
     if (base >= n_items) break;
-    // ---- classify the chunk (one photon per lane) ----
-    const uint64_t k = base + lane;
+    // ---- classify (one photon per thread) ----
+    const uint64_t k = base + r;
     int mode = kArfNone;
     float x0 = 0.f, x1 = 0.f, x2 = 0.f;
     long long p_off = -1;
@@ -188,64 +138,26 @@ __global__ void __launch_bounds__(kArfWarps * 32) k_spect_arf(Scene<real> s, Arf
       ++my_fb;
     }
     if (mode == kArfNet) ++my_net;
-    x[lane][0] = x0;
-    x[lane][1] = x1;
-    x[lane][2] = x2;
-    pix[lane] = p_off;
-    // skip the network when no photon of the chunk is scored
-    if (__ballot_sync(0xffffffffu, p_off >= 0) == 0u) continue;
-    __syncwarp();
-    // ---- layer 1 (CUDA cores) ----
-    for (int e = lane; e < kArfRows * kHid; e += 32) {
-      const int r = e / kHid, j = e % kHid;
-      float z = sm.b1[j];
-      z = fmaf(sm.w1[3 * j + 0], x[r][0], z);
-      z = fmaf(sm.w1[3 * j + 1], x[r][1], z);
-      z = fmaf(sm.w1[3 * j + 2], x[r][2], z);
-      buf0[r * kLds + j] = __float2bfloat16_rn(z > 0.0f ? z : 0.0f);
+    // skip the network when no photon of the tile is scored
+    if (!named_bar_any(bar, kTcRows, p_off >= 0)) continue;
+    // ---- network (tensor cores) ----
+    float p[16];
+    if (!tc_net_forward(sm, g, r, phase, x0, x1, x2, p)) {
+      if (r == 0) atomicOr(a.status, kStatusWaitTimeout);
+      break;
     }
-    __syncwarp();
-    arf_hidden(buf0, sm.w2, sm.b2, buf1);
-    __syncwarp();
-    arf_hidden(buf1, sm.w3, sm.b3, buf0);
-    __syncwarp();
-    // ---- output layer + softmax, probabilities to buf1 (FP32 [32][16]) ----
-    float *prob = reinterpret_cast<float *>(buf1);
-    {
-      float acc[2][2][4];
-      zero_acc(acc);
-      warp_gemm<2, 2, false, false>(acc, buf0, kLds, 0, sm.w4, kLds, 0, kHid);
-#pragma unroll
-      for (int mt = 0; mt < 2; ++mt) {
-        float t[1][2][4];
-#pragma unroll
-        for (int nt = 0; nt < 2; ++nt)
-#pragma unroll
-          for (int q = 0; q < 4; ++q) {
-            int rr, cc;
-            acc_pos(q, rr, cc);
-            t[0][nt][q] = acc[mt][nt][q] + sm.b4[8 * nt + cc];
-          }
-        mlp_softmax(t, a.n_classes);
-#pragma unroll
-        for (int nt = 0; nt < 2; ++nt)
-#pragma unroll
-          for (int q = 0; q < 4; ++q) {
-            int rr, cc;
-            acc_pos(q, rr, cc);
-            prob[(16 * mt + rr) * kOutPad + 8 * nt + cc] = t[0][nt][q];
-          }
-      }
-    }
-    __syncwarp();
     // ---- window weights into the projection tallies ----
     if (p_off >= 0) {
-      const float *pr = prob + lane * kOutPad;
-      float norm = pr[0] * a.rr;
-      for (int c = 1; c < a.n_classes; ++c) norm += pr[c];
+      tc_softmax(p, a.n_classes);
+      float norm = p[0] * a.rr;
+#pragma unroll
+      for (int c = 1; c < 16; ++c)
+        if (c < a.n_classes) norm += p[c];
       const float inv = norm > 0.0f ? 1.0f / norm : 0.0f;
-      for (int c = 1; c < a.n_classes; ++c) {
-        const unsigned long long q = __float2ull_rn((pr[c] * inv) * 4294967296.0f);
+#pragma unroll
+      for (int c = 1; c < 16; ++c) {
+        if (c >= a.n_classes) break;
+        const unsigned long long q = __float2ull_rn((p[c] * inv) * 4294967296.0f);
         if (!q) continue;
         const size_t idx = (size_t)p_off + (size_t)(c - 1) * plane;
         atomicAdd(a.proj + idx, q);
@@ -255,11 +167,10 @@ __global__ void __launch_bounds__(kArfWarps * 32) k_spect_arf(Scene<real> s, Arf
         if (rest) atomicAdd(a.proj2 + 2 * idx + 1, rest);
       }
     }
-    __syncwarp();
   }
   if (my_net) atomicAdd(&n_net, my_net);
   if (my_fb) atomicAdd(&n_fb, my_fb);
-  __syncthreads();
+  tc_net_teardown(sm);
   if (threadIdx.x == 0) {
     if (n_net) atomicAdd(&a.counters[GG_CNT_ARF_PHOTONS], (unsigned long long)n_net);
     if (n_fb) atomicAdd(&a.counters[GG_CNT_ARF_FALLBACK], (unsigned long long)n_fb);
@@ -271,11 +182,11 @@ cudaError_t launch_spect_arf(const Scene<real> &s, const ArfStageArgs &a, int gr
   static bool configured = false;
   if (!configured) {
     cudaError_t e = cudaFuncSetAttribute(k_spect_arf<real>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)sizeof(ArfSmem));
+                                         (int)sizeof(TcNetSmem));
     if (e != cudaSuccess) return e;
     configured = true;
   }
-  k_spect_arf<real><<<grid, kArfWarps * 32, sizeof(ArfSmem), st>>>(s, a);
+  k_spect_arf<real><<<grid, kTcThreads, sizeof(TcNetSmem), st>>>(s, a);
   return cudaGetLastError();
 }
 

@@ -30,6 +30,9 @@ struct KernelArgs {
 // Bit of the kernel status word set when a stage queue overflowed (the low
 // bits carry the source stage's GG_ERR_* code).
 constexpr unsigned int kStatusQueueOverflow = 0x100u;
+// Bit set when a bounded wait of a tensor-core kernel ran out (the kernel
+// stopped early and freed its tensor memory).
+constexpr unsigned int kStatusWaitTimeout = 0x200u;
 
 // Queues of one SPECT stage launch (see gg_spect.cu).
 struct StageArgs {
@@ -104,7 +107,9 @@ size_t mlp_smem_bytes();
 cudaError_t launch_mlp_train(const MlpTrainArgs &a, int n_tiles, cudaStream_t st);
 cudaError_t launch_mlp_adam(const MlpAdamArgs &a, cudaStream_t st);
 cudaError_t launch_mlp_to_bf16(const float *params, __nv_bfloat16 *wbf, cudaStream_t st);
-cudaError_t launch_mlp_predict(const MlpTrainArgs &a, float *out, uint64_t n, int grid, cudaStream_t st);
+size_t mlp_tc_smem_bytes();
+cudaError_t launch_mlp_predict(const MlpTrainArgs &a, float *out, uint64_t n, int grid, unsigned int *status,
+                               cudaStream_t st);
 template <typename real>
 cudaError_t launch_spect_arf(const Scene<real> &s, const ArfStageArgs &a, int grid, cudaStream_t st);
 

@@ -9,6 +9,7 @@
 //     copies of W2 / W3 / W4 refreshed for the next step.
 // The weight-gradient GEMMs reduce over the tile's samples on the tensor
 // cores (dW = dZ^T H: both operands read transposed by ldmatrix.trans).
+// Batch inference (k_mlp_predict) runs the forward pass on tcgen05 (gg_mlp_tc.cuh).
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -16,6 +17,7 @@
 
 #include "gg_internal.h"
 #include "gg_mlp.cuh"
+#include "gg_mlp_tc.cuh"
 
 namespace gg {
 
@@ -212,41 +214,36 @@ __global__ void k_mlp_to_bf16(const float *params, __nv_bfloat16 *wbf) {
   if (e < kOutPad * kHid) wbf[kBfW4 + e] = __float2bfloat16_rn(params[kOffW4 + e]);
 }
 
-// Class probabilities of n rows (features of float4 rows as in training): out[i][c], c < n_classes.
-__global__ void __launch_bounds__(kMlpThreads) k_mlp_predict(MlpTrainArgs a, float *out, uint64_t n) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  MlpSmem &sm = *reinterpret_cast<MlpSmem *>(smem_raw);
-  const int m0 = 16 * (threadIdx.x >> 5);
-  mlp_load_weights(sm, a.params, a.wbf);
-  for (uint64_t base = (uint64_t)blockIdx.x * kTileM; base < n; base += (uint64_t)gridDim.x * kTileM) {
-    __syncthreads();
-    for (int r = threadIdx.x; r < kTileM; r += blockDim.x) {
-      const float4 v = base + r < n ? a.rows[base + r] : make_float4(0.f, 0.f, 0.f, 0.f);
-      sm.x[r][0] = (v.y - a.mean[0]) * a.inv_std[0];
-      sm.x[r][1] = (v.z - a.mean[1]) * a.inv_std[1];
-      sm.x[r][2] = (v.x - a.mean[2]) * a.inv_std[2];
+// Class probabilities of n rows on the 5th-generation tensor cores
+// (gg_mlp_tc.cuh): each warpgroup of a CTA takes tiles of 128 rows in turn.
+__global__ void __launch_bounds__(kTcThreads, 1)
+    k_mlp_predict(MlpTrainArgs a, float *out, uint64_t n, unsigned int *status) {
+  extern __shared__ __align__(1024) unsigned char tc_smem_raw[];
+  TcNetSmem &sm = *reinterpret_cast<TcNetSmem *>(tc_smem_raw);
+  tc_net_load(sm, a.params, a.wbf);
+  tc_net_setup(sm);
+  const int g = threadIdx.x >> 7, r = threadIdx.x & 127;
+  uint32_t phase = 0;
+  const uint64_t n_tiles = (n + kTcRows - 1) / kTcRows;
+  for (uint64_t t = (uint64_t)blockIdx.x * kTcGroups + g; t < n_tiles; t += (uint64_t)gridDim.x * kTcGroups) {
+    const uint64_t row = t * kTcRows + r;
+    const float4 v = row < n ? a.rows[row] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float x0 = (v.y - a.mean[0]) * a.inv_std[0];
+    const float x1 = (v.z - a.mean[1]) * a.inv_std[1];
+    const float x2 = (v.x - a.mean[2]) * a.inv_std[2];
+    float p[16];
+    if (!tc_net_forward(sm, g, r, phase, x0, x1, x2, p)) {
+      if (r == 0) atomicOr(status, kStatusWaitTimeout);
+      break;
     }
-    __syncthreads();
-    mlp_layer1(sm);
-    __syncthreads();
-    mlp_hidden(sm.h1, sm.w2, sm.b2, sm.h2);
-    __syncthreads();
-    mlp_hidden(sm.h2, sm.w3, sm.b3, sm.h3);
-    __syncthreads();
-    float acc[1][2][4];
-    mlp_logits(sm, acc);
-    mlp_softmax(acc, a.n_classes);
+    tc_softmax(p, a.n_classes);
+    if (row < n) {
 #pragma unroll
-    for (int nt = 0; nt < 2; ++nt)
-#pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        int rr, cc;
-        acc_pos(q, rr, cc);
-        const uint64_t row = base + m0 + rr;
-        const int col = 8 * nt + cc;
-        if (row < n && col < a.n_classes) out[row * a.n_classes + col] = acc[0][nt][q];
-      }
+      for (int c = 0; c < 16; ++c)
+        if (c < a.n_classes) out[row * a.n_classes + c] = p[c];
+    }
   }
+  tc_net_teardown(sm);
 }
 
 size_t mlp_smem_bytes() { return sizeof(MlpSmem); }
@@ -273,15 +270,18 @@ cudaError_t launch_mlp_to_bf16(const float *params, __nv_bfloat16 *wbf, cudaStre
   return cudaGetLastError();
 }
 
-cudaError_t launch_mlp_predict(const MlpTrainArgs &a, float *out, uint64_t n, int grid, cudaStream_t st) {
+size_t mlp_tc_smem_bytes() { return sizeof(TcNetSmem); }
+
+cudaError_t launch_mlp_predict(const MlpTrainArgs &a, float *out, uint64_t n, int grid, unsigned int *status,
+                               cudaStream_t st) {
   static bool configured = false;
   if (!configured) {
     cudaError_t e = cudaFuncSetAttribute(k_mlp_predict, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)sizeof(MlpSmem));
+                                         (int)sizeof(TcNetSmem));
     if (e != cudaSuccess) return e;
     configured = true;
   }
-  k_mlp_predict<<<grid, kMlpThreads, sizeof(MlpSmem), st>>>(a, out, n);
+  k_mlp_predict<<<grid, kTcThreads, sizeof(TcNetSmem), st>>>(a, out, n, status);
   return cudaGetLastError();
 }
 
