@@ -476,8 +476,9 @@ struct Records {
 // Lane states of the phase-batched transport loop.
 enum : int { kDone = 0, kRefill = 1, kFly = 2, kInteract = 3 };
 
-// Flight: one Woodcock tentative step in the image, or one free flight in the
-// world.  A real collision is not handled here: the lane records it
+// Flight: one Woodcock tentative step in the image (followed, when it leaves
+// the image box, by the world flight), or one free flight in the world.  A
+// real collision is not handled here: the lane records it
 // (material, voxel, scored) and waits in state kInteract until its warp runs
 // an interaction phase.  Returns the lane's next state; kRefill means the
 // photon died.
@@ -532,7 +533,18 @@ __device__ __forceinline__ int flight(const Scene<real> &s, Photon<real> &ph, Rn
     ph.alive = 0;
     return kRefill;
   }
-  if (ph.in_image) return image_flight(s, ph, g, pmat, pv, pscored, n_wood, n_real);
+  if (ph.in_image) {
+    const int r = image_flight(s, ph, g, pmat, pv, pscored, n_wood, n_real);
+    if constexpr (SPECT) return r;
+    if (r != kFly || ph.in_image) return r;
+    // Left the image box: take the world step at once (the same flight
+    // count and draws as a separate phase, one block iteration fewer).
+    if (++ph.steps > kStepCap) {
+      atomicAdd(&bc->loop_capped, 1u);
+      ph.alive = 0;
+      return kRefill;
+    }
+  }
   if constexpr (SPECT) {
     if (ph.in_head) {
       ++n_head;
