@@ -203,67 +203,107 @@ def spect_cpu_sample(scene, sp, threads, target_s=10.0, seed=424242):
     return n2 * n_runs / dt2, n2 * n_runs, dt2
 
 
+def grow_sample(run, target_s, n0, n_max):
+    """Times run(n, seed) (the CPU restatement) on a bounded sample: grows n until
+    a call takes a quarter of target_s (each call has a fixed set-up cost), then
+    runs the size the marginal rate gives for target_s.  Returns (n / s, n, s)."""
+    n, t_prev, n_prev = n0, None, None
+    while True:
+        t0 = time.perf_counter()
+        run(n, 424242)
+        dt = time.perf_counter() - t0
+        if dt > 0.25 * target_s or n >= n_max:
+            break
+        t_prev, n_prev = dt, n
+        n *= 4
+    rate = (n - n_prev) / max(dt - t_prev, 1e-6) if n_prev else n / dt
+    n2 = int(min(max(n, rate * target_s), n_max))
+    t0 = time.perf_counter()
+    run(n2, 424243)
+    dt2 = time.perf_counter() - t0
+    return n2 / dt2, n2, dt2
+
+
+def reference_workload(args, threads):
+    """(metric, workload, data, primaries per step, run(n, seed) in primaries, note) of
+    the CPU restatement for the chosen workload, on the same configuration as --impl ours."""
+    from oracle import oracle as O
+    from opengate_gb300 import workloads as W
+
+    if args.workload in ("spect", "spect_arf"):
+        from opengate_gb300 import spect as S
+
+        if args.workload == "spect":
+            scene, sp, _ = W.spect_phantom()
+            meta = (SPECT_METRIC, SPECT_WORKLOAD, int(SPECT_DECAYS * SPECT_YIELD))
+        else:
+            scene, sp, _ = W.spect_phantom(nuclide=W.LU177, collimator=S.MELP, n_runs=120, windows=ARF_WINDOWS)
+            meta = (ARF_METRIC, ARF_WORKLOAD, int(ARF_DECAYS * ARF_YIELD))
+        runs = sp.n_runs
+
+        def run(n, seed):
+            O.run_spect(scene, sp, max(n // runs, 1), seed, threads=threads)
+
+        note = (f"plain collimator tracking over all {runs} positions" +
+                (" (the reference's CPU method; the network is not part of its CPU path)"
+                 if args.workload == "spect_arf" else ""))
+        return meta + ("synthetic (seeded CT phantom + activity image)", run, note, 2000 * runs, int(4e8))
+    if args.workload == "batched":
+        _, sims = W.batched_phantoms(seed=args.seed)
+        total = int(sum(k for _, k, _ in sims))
+
+        def run(n, seed):
+            # the same fraction of every simulation's primaries
+            f = n / total
+            for sc, k, sd in sims:
+                O.run_dose(sc, max(int(k * f), 1), sd + seed, threads=threads)
+
+        return (BATCH_METRIC, BATCH_WORKLOAD, total, "synthetic (seeded slab phantoms)", run,
+                "every simulation, the same fraction of its primaries", 100_000, total)
+    if args.workload == "tle":
+        scene = W.water_pencil()
+        tle = scene.tle_desc(np.inf, 0.0, "EPDL")
+
+        def run(n, seed):
+            O.run_dose(scene, n, seed, threads=threads, tle=tle)
+
+        return ("primaries/s at matched sigma (TLE dose vs analog dose, 64^3 water, 1 MeV pencil)",
+                "water_64x64x64_2mm_pencil_1MeV_tle_none_epdl", 10_000_000, "synthetic (uniform water phantom)",
+                run, "track-length estimator", 50_000, int(2e8))
+    scene, _ = W.ct_phantom()
+
+    def run(n, seed):
+        O.run_dose(scene, n, seed, threads=threads)
+
+    return (METRIC, WORKLOAD, PRIMARIES_PER_STEP, "synthetic (seeded CT phantom)", run, "analog DoseActor",
+            200_000, int(4e8))
+
+
 def run_reference(args):
     ws, rank, _ = dist_env()
     if rank != 0:
         return 0
-    if args.workload == "spect":
-        return run_reference_spect(args)
-    from opengate_gb300 import workloads as W
-
-    scene, _ = W.ct_phantom()
     threads = os.cpu_count() or 1
-    rates = []
+    metric, workload, n_step, data, run, note, n0, n_max = reference_workload(args, threads)
     t_all = time.perf_counter()
     for _ in range(args.warmup):
-        cpu_sample(scene, threads, target_s=1.0)
-    samples = []
-    for _ in range(args.steps):
-        r, n, dt = cpu_sample(scene, threads, target_s=8.0)
-        rates.append(r)
-        samples.append(n)
-    value = float(np.median(rates))
-    line = {
-        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": PRIMARIES_PER_STEP / value * 1e3,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic (seeded CT phantom)",
-        "config": {"workload": WORKLOAD, "primaries_per_step": PRIMARIES_PER_STEP,
-                   "note": "CPU restatement of the path (C, pthreads); Geant4/opengate_core not installable offline"},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": f"{int(np.median(samples))} primaries of the same workload per step, all host threads"},
-        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-        "wall_s": time.perf_counter() - t_all,
-    }
-    print(json.dumps(line), flush=True)
-    return 0
-
-
-def run_reference_spect(args):
-    from opengate_gb300 import workloads as W
-
-    scene, sp, _ = W.spect_phantom()
-    threads = os.cpu_count() or 1
-    n_step = int(SPECT_DECAYS * SPECT_YIELD)
-    t_all = time.perf_counter()
-    for _ in range(args.warmup):
-        spect_cpu_sample(scene, sp, threads, target_s=1.0)
+        grow_sample(run, 1.0, n0, n_max)
     rates, samples = [], []
     for _ in range(args.steps):
-        r, n, dt = spect_cpu_sample(scene, sp, threads, target_s=8.0)
+        r, n, dt = grow_sample(run, 8.0, n0, n_max)
         rates.append(r)
         samples.append(n)
     value = float(np.median(rates))
     line = {
-        "impl": "reference", "metric": SPECT_METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "impl": "reference", "metric": metric, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": n_step / value * 1e3,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic (seeded CT phantom + activity image)",
-        "config": {"workload": SPECT_WORKLOAD, "primaries_per_step": n_step,
-                   "note": "CPU restatement of the path (C, pthreads); Geant4/opengate_core not installable offline"},
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": data,
+        "config": {"workload": workload, "primaries_per_step": n_step,
+                   "note": f"CPU restatement of the path (C, pthreads), {note}; "
+                           "Geant4/opengate_core not installable offline"},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": f"{int(np.median(samples))} primaries over the 60 positions per step, "
-                                   "all host threads"},
+                         "sample": f"{int(np.median(samples))} primaries of the same workload per step, "
+                                   f"{threads} host threads"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "wall_s": time.perf_counter() - t_all,
     }
@@ -650,6 +690,119 @@ def fp64_error(scene, n, seed, device, batch):
     return err
 
 
+def run_ours_tle(args, ws, rank, local, dist, use_cuda):
+    """Track-length estimator (TLEDoseActor) against analog scoring at matched sigma:
+    64^3 water, 2 mm voxels, 1 MeV pencil beam on the entrance face (the small dose
+    configuration), TLE threshold type "None", EPDL mu_en."""
+    import torch
+
+    from opengate_gb300 import workloads as W
+    from opengate_gb300.engine import DoseEngine
+
+    scene = W.water_pencil()
+    n = args.primaries if args.primaries != PRIMARIES_PER_STEP else 10_000_000
+    l2_flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=f"cuda:{local}")
+
+    def first_of(step):
+        return ((rank * (args.warmup + args.steps + 1)) + step) * n
+
+    def timed(eng, steps, base):
+        ms, launches = [], 0
+        for k in range(steps):
+            l2_flush.zero_()
+            torch.cuda.synchronize()
+            eng.reset()
+            eng.run(n, args.seed, first_of(base + k))
+            tg, tt, tf, nl = eng.last_kernel_ms()
+            ms.append(tg + tt + tf)
+            launches += nl
+        return ms, launches
+
+    tle = DoseEngine(scene, device=local, precision=32, batch=args.batch)
+    tle.set_tle(np.inf, 0.0, "EPDL")
+    timed(tle, args.warmup, 0)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    with ClockSampler(local) as clk:
+        ms, launches = timed(tle, args.steps, args.warmup)
+        torch.cuda.synchronize()
+    total_ms = dist_max(dist, float(np.sum(ms)), use_cuda)
+    value = ws * n * args.steps / (total_ms / 1e3)
+    sig_t = mean_relative_uncertainty(tle.edep(), tle.edep_squared(), n)
+    counters = tle.counters()
+    stage = tle.last_kernel_ms()
+    # e2e through the C ABI with host buffers: scene upload + estimator table, run, images back
+    h2d = scene.labels.nbytes + scene._sig.nbytes + scene._cum.nbytes + scene._ray_amax.nbytes + \
+        scene._ray_cum.nbytes + scene.majorant.nbytes + scene.pt.n_comp * 512 * 4
+    d2h = 2 * scene.n_voxels * 8
+    e2e_t = []
+    for k in range(max(1, min(args.steps, 3))):
+        t1 = time.perf_counter()
+        tle.upload()
+        tle.set_tle(np.inf, 0.0, "EPDL")
+        tle.run(n, args.seed, first_of(args.warmup + args.steps + k))
+        tle.edep(), tle.edep_squared()
+        e2e_t.append(time.perf_counter() - t1)
+    e2e_value = ws * n / dist_max(dist, float(np.mean(e2e_t)), use_cuda)
+    tle.close()
+    # analog scoring of the same histories
+    ana = DoseEngine(scene, device=local, precision=32, batch=args.batch)
+    timed(ana, args.warmup, 0)
+    ams, _ = timed(ana, args.steps, args.warmup)
+    sig_a = mean_relative_uncertainty(ana.edep(), ana.edep_squared(), n)
+    ana.close()
+    t_t, t_a = float(np.sum(ms)) / args.steps, float(np.sum(ams)) / args.steps
+    gain = (sig_a ** 2 * t_a) / (sig_t ** 2 * t_t)
+    peak, peak_kind = measured_peaks()
+    bytes_alg = 32.0 * counters["woodcock_steps"] + 64.0 * counters["tally_entries"]
+    achieved = bytes_alg / (stage[1] / 1e3) / 1e9
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        from oracle import oracle as O
+
+        threads = os.cpu_count() or 1
+        ns = 200_000
+        t1 = time.perf_counter()
+        O.run_dose(scene, ns, args.seed, threads=threads, tle=scene.tle_desc(np.inf, 0.0, "EPDL"))
+        dt = time.perf_counter() - t1
+        ns = max(ns, int(ns * args.cpu_seconds / max(dt, 1e-3)))
+        t1 = time.perf_counter()
+        O.run_dose(scene, ns, args.seed + 1, threads=threads, tle=scene.tle_desc(np.inf, 0.0, "EPDL"))
+        dt = time.perf_counter() - t1
+        cpu = {"value": ns / dt, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"{ns} primaries of the same workload with the estimator, {dt:.1f} s on {threads} threads"}
+    if rank == 0:
+        line = {
+            "metric": "primaries/s at matched sigma (TLE dose vs analog dose, 64^3 water, 1 MeV pencil)",
+            "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (uniform water phantom)",
+            "config": {"workload": "water_64x64x64_2mm_pencil_1MeV_tle_none_epdl", "primaries_per_step": n,
+                       "tally": "fp64 edep + edep^2, history-by-history", "l2": "flushed between steps (256 MiB write)",
+                       "parallelism": f"replicas x{ws}, disjoint history ranges"},
+            "matched_sigma": {"sigma_tle": sig_t, "sigma_analog": sig_a, "ms_per_step_tle": t_t,
+                              "ms_per_step_analog": t_a, "efficiency_gain": gain,
+                              "analog_equivalent_primaries_per_s": value * gain,
+                              "note": "efficiency = 1 / (sigma^2 T), sigma = mean relative uncertainty "
+                                      "over voxels > 10 % of max"},
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                         "traffic": None, "peak_kind": peak_kind, "kernel": "k_transport<float> (estimator)",
+                         "bytes_alg_per_step": bytes_alg,
+                         "units": {"woodcock_steps": counters["woodcock_steps"],
+                                   "tally_entries": counters["tally_entries"], "deposits": counters["deposits"]},
+                         "stage_ms_per_step": {"generate": stage[0], "transport": stage[1], "flush": stage[2]}},
+            "cpu_baseline": cpu,
+            "clocks": clk.summary(),
+            "gpu_launches": int(launches),
+        }
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
 def run_ours(args):
     ws, rank, local = dist_env()
     import torch
@@ -665,6 +818,8 @@ def run_ours(args):
         return run_ours_arf(args, ws, rank, local, dist, use_cuda)
     if args.workload == "batched":
         return run_ours_batched(args, ws, rank, local, dist, use_cuda)
+    if args.workload == "tle":
+        return run_ours_tle(args, ws, rank, local, dist, use_cuda)
     from opengate_gb300 import _capi as C
     from opengate_gb300 import workloads as W
     from opengate_gb300.engine import DoseEngine
@@ -781,9 +936,11 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="dose", choices=["dose", "spect", "spect_arf", "batched"],
+    ap.add_argument("--workload", default="dose", choices=["dose", "spect", "spect_arf", "batched", "tle"],
                     help="dose: CT phantom DoseActor (default); spect: Tc-99m SPECT acquisition, 60 positions; "
-                         "spect_arf: Lu-177 SPECT with ARF detectors vs plain tracking, 120 positions")
+                         "spect_arf: Lu-177 SPECT with ARF detectors vs plain tracking, 120 positions; "
+                         "batched: 48 uneven dose simulations in one launch sequence; "
+                         "tle: track-length estimator vs analog dose, 64^3 water, 1 MeV pencil")
     ap.add_argument("--primaries", type=int, default=PRIMARIES_PER_STEP)
     ap.add_argument("--arf-train-samples", type=int, default=ARF_TRAIN_SAMPLES)
     ap.add_argument("--arf-epochs", type=int, default=80)

@@ -26,6 +26,8 @@
  *                               (core/opengate_core/opengate_lib/GateSPSVoxelsPosDistribution.cpp:29-74)
  *   gg_add_dose_tally           GateDoseActor::InitializeCpp / BeginOfRunAction
  *                               (core/opengate_core/opengate_lib/GateDoseActor.cpp:100-137)
+ *   gg_set_tle                  GateTLEDoseActor (track-length estimator)
+ *                               (core/opengate_core/opengate_lib/GateTLEDoseActor.cpp:174-299)
  *   gg_run                      GateSourceManager::StartMasterThread -> /run/beamOn
  *                               (core/opengate_core/opengate_lib/GateSourceManager.cpp:198-244)
  *                               with GateDoseActor::SteppingAction / ScoreSquaredValue /
@@ -240,6 +242,26 @@ int gg_set_source(gg_ctx *ctx, const gg_source_desc *source);
 /* Enables the edep / edep-squared tally on the image grid and zeroes it. */
 int gg_add_dose_tally(gg_ctx *ctx, int32_t score_squared);
 int gg_reset_tally(gg_ctx *ctx);
+
+/* Track-length estimator of the dose tally (replaces the TLEDoseActor:
+   GateTLEDoseActor::SteppingAction / ScoreTLEDepositStep,
+   core/opengate_core/opengate_lib/GateTLEDoseActor.cpp:174-299, options of
+   opengate/actors/doseactors.py:722-776).  With enabled = 1 a photon inside
+   the image whose energy is at or below threshold_energy scores
+   E * mu_en(E, material) * length in every voxel its paths cross, and the
+   energy it gives to electrons at its interactions is not scored; photons
+   above the threshold score as without the estimator.  A scored photon at or
+   below energy_min deposits its energy in its voxel and stops.  mu_en comes
+   from `muen` ([n_comp][n_e], mm^-1 per g/cm3, the grid and compositions of
+   the uploaded tables).  Single (not batched) dose runs only; enabled = 0
+   switches it off. */
+typedef struct {
+  int32_t enabled;
+  double threshold_energy; /* MeV; +inf scores every photon (threshold type "None") */
+  double energy_min;       /* MeV */
+  const float *muen;       /* [n_comp][n_e] */
+} gg_tle_desc;
+int gg_set_tle(gg_ctx *ctx, const gg_tle_desc *tle);
 /* Simulates histories [first_history, first_history + n) with the given seed
    and adds them to the tally.  Histories are processed in batches (the
    context's batch size); the result does not depend on launch parameters. */

@@ -51,6 +51,13 @@ class TablesDesc(ctypes.Structure):
     ]
 
 
+class TleDesc(ctypes.Structure):
+    _fields_ = [
+        ("enabled", ctypes.c_int32), ("threshold_energy", ctypes.c_double), ("energy_min", ctypes.c_double),
+        ("muen", _f32p),
+    ]
+
+
 class VolumeDesc(ctypes.Structure):
     _fields_ = [
         ("dims", ctypes.c_int32 * 3), ("spacing", ctypes.c_double * 3),
@@ -167,6 +174,7 @@ PROTOTYPES = [
     ("gg_set_source", ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(SourceDesc)]),
     ("gg_add_dose_tally", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
     ("gg_reset_tally", ctypes.c_int, [ctypes.c_void_p]),
+    ("gg_set_tle", ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(TleDesc)]),
     ("gg_run", ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64]),
     ("gg_synchronize", ctypes.c_int, [ctypes.c_void_p]),
     ("gg_get_image", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, _f64p, ctypes.c_size_t]),

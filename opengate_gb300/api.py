@@ -411,6 +411,35 @@ class DoseActor(GateObject):
         return self.edep.number_of_samples
 
 
+class TLEDoseActor(DoseActor):
+    """Track-length estimator dose (TLEDoseActor, opengate/actors/doseactors.py:722-776;
+    GateTLEDoseActor, core/opengate_core/opengate_lib/GateTLEDoseActor.cpp): photons at or
+    below the threshold score E * mu_en * track length in every voxel they cross instead of
+    the energy their electrons deposit; photons at or below ``energy_min`` deposit their
+    energy where they are and stop.  mu_en from the EPDL or NIST element tables of the
+    reference (mass-fraction mixture, log-log interpolation)."""
+
+    type_name = "TLEDoseActor"
+    user_info_defaults = dict(DoseActor.user_info_defaults, energy_min=0.0, tle_threshold=np.inf,
+                              tle_threshold_type="None", database="EPDL")
+
+    def check(self, image_volume, image):
+        super().check(image_volume, image)
+        if self.tle_threshold_type not in ("None", "energy", "max range", "average range"):
+            raise ValueError("You did not define a correct threshold type")
+        if self.tle_threshold_type in ("max range", "average range"):
+            raise NotImplementedError(
+                f"tle_threshold_type '{self.tle_threshold_type}' needs electron CSDA ranges (G4EmCalculator), "
+                "which the GPU path does not have; use 'None' or 'energy'")
+        if self.database not in ("EPDL", "NIST"):
+            raise ValueError(f"database must be 'EPDL' or 'NIST', not {self.database!r}")
+
+    @property
+    def threshold_energy(self):
+        """Photon energy (MeV) at or below which the estimator scores (inf for type 'None')."""
+        return np.inf if self.tle_threshold_type == "None" else float(self.tle_threshold)
+
+
 class DigitizerProjectionActor(GateObject):
     """Projection of the singles of one SPECT head's crystal (GateDigitizerProjectionActor,
     core/opengate_core/opengate_lib/digitizer/GateDigitizerProjectionActor.cpp:127-223;
@@ -491,7 +520,8 @@ class Simulation:
     def add_actor(self, actor_type, name):
         if name in self.actors:
             raise ValueError(f"an actor named '{name}' already exists")
-        cls = {"DoseActor": DoseActor, "SimulationStatisticsActor": SimulationStatisticsActor,
+        cls = {"DoseActor": DoseActor, "TLEDoseActor": TLEDoseActor,
+               "SimulationStatisticsActor": SimulationStatisticsActor,
                "DigitizerProjectionActor": DigitizerProjectionActor}.get(actor_type)
         if cls is None:
             raise NotImplementedError(f"actor type '{actor_type}' is not supported by the GPU path")
@@ -666,8 +696,13 @@ class Simulation:
             raise NotImplementedError("one DoseActor with an uncertainty goal")
         if goals and (len(sources) > 1 or len(runs) > 1):
             raise NotImplementedError("the uncertainty goal needs one source and one run")
+        tles = [a for a in doses if isinstance(a, TLEDoseActor)]
+        if tles and len(doses) > 1:
+            raise NotImplementedError("a TLEDoseActor cannot share the run with another dose actor")
         eng = DoseEngine(scene, device=self.device, precision=self.precision, batch=self.batch)
         try:
+            if tles:
+                eng.set_tle(tles[0].threshold_energy, float(tles[0].energy_min), tles[0].database)
             first = 0
             for r in range(len(runs)):
                 for k, (src, spec) in enumerate(sources):

@@ -48,6 +48,10 @@ struct gg_ctx {
   int n_e = 0, n_comp = 0, n_ray = 0, n_mat = 0;
   float ln_emin = 0, inv_dln = 0, e_min = 0, e_max = 0;
   void *d_sig = nullptr, *d_cum = nullptr, *d_ray_amax = nullptr, *d_ray_cum = nullptr, *d_mat_rho = nullptr;
+  // track-length estimator (gg_set_tle)
+  void *d_muen = nullptr;
+  bool tle = false;
+  double tle_thr = 0.0, tle_emin = 0.0;
   void *d_ray_x2 = nullptr;
   int *d_mat_comp = nullptr;
   std::vector<int> h_mat_comp;
@@ -199,6 +203,7 @@ struct gg_ctx {
 
   void release() {
     dfree(d_sig); dfree(d_cum); dfree(d_ray_amax); dfree(d_ray_cum); dfree(d_mat_rho); dfree(d_mat_comp);
+    dfree(d_muen);
     dfree(d_ray_x2);
     dfree(d_labels); dfree(d_maj); dfree(d_spec_e); dfree(d_spec_cdf); dfree(d_acc_box);
     dfree(d_acc_e); dfree(d_acc_e2); dfree(d_edep); dfree(d_edep2);
@@ -253,8 +258,12 @@ struct gg_ctx {
       s.bmin[a] = (real)corner[a];
       s.bmax[a] = (real)(corner[a] + (double)dims[a] * spacing[a]);
       s.inv_sp[a] = (real)(1.0 / spacing[a]);
+      s.sp[a] = (real)spacing[a];
       s.whalf[a] = (real)world.half_size[a];
     }
+    s.muen = (tle && !have_spect && !have_batch) ? (const real *)d_muen : nullptr;
+    s.tle_thr = (real)tle_thr;
+    s.tle_emin = (real)tle_emin;
     s.labels = d_labels;
     s.sims = have_batch ? (const gg::SimDesc<real> *)d_sims : nullptr;
     s.sim_maj = have_batch ? (const real *)d_sim_maj : nullptr;
@@ -649,6 +658,7 @@ int gg_upload_tables(gg_ctx *c, const gg_tables_desc *t) {
                                             : gg::transport_smem_bytes<float>(t->n_comp, t->n_e, t->n_mat);
   if (need > 190 * 1024)
     return c->fail(GG_ERR_ARG, "gg_upload_tables: tables need %zu bytes of shared memory (max 190 KiB)", need);
+  if (c->tle && (t->n_e != c->n_e || t->n_comp != c->n_comp)) c->tle = false;  // its table no longer fits
   c->n_e = t->n_e;
   c->n_comp = t->n_comp;
   c->n_ray = t->n_ray;
@@ -798,6 +808,30 @@ int gg_add_dose_tally(gg_ctx *c, int32_t score_squared) {
   c->squared = score_squared != 0;
   c->have_tally = true;
   return gg_reset_tally(c);
+}
+
+int gg_set_tle(gg_ctx *c, const gg_tle_desc *d) {
+  if (!c || !d) return GG_ERR_ARG;
+  cudaSetDevice(c->device);
+  if (!d->enabled) {
+    c->tle = false;
+    return GG_OK;
+  }
+  if (!c->d_sig) return c->fail(GG_ERR_STATE, "gg_set_tle: upload the physics tables first");
+  if (c->have_batch) return c->fail(GG_ERR_STATE, "gg_set_tle: batched simulations do not support the estimator");
+  if (!d->muen) return c->fail(GG_ERR_ARG, "gg_set_tle: no mu_en table");
+  if (std::isnan(d->threshold_energy) || !(d->energy_min >= 0) || !std::isfinite(d->energy_min))
+    return c->fail(GG_ERR_ARG, "gg_set_tle: invalid threshold or kill energy");
+  const size_t nce = (size_t)c->n_comp * c->n_e;
+  for (size_t i = 0; i < nce; ++i)
+    if (!(d->muen[i] >= 0) || !std::isfinite(d->muen[i]))
+      return c->fail(GG_ERR_ARG, "gg_set_tle: mu_en table has a negative or non-finite entry");
+  int st;
+  if ((st = c->upload_real(c->d_muen, d->muen, nce))) return st;
+  c->tle = true;
+  c->tle_thr = d->threshold_energy;
+  c->tle_emin = d->energy_min;
+  return GG_OK;
 }
 
 int gg_reset_tally(gg_ctx *c) {

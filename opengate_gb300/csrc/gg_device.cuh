@@ -385,8 +385,12 @@ struct Scene {
   const int *mat_comp;
   // image
   int nx, ny, nz;
-  real bmin[3], bmax[3], inv_sp[3];
+  real bmin[3], bmax[3], inv_sp[3], sp[3];
   const uint16_t *labels;
+  // track-length estimator (muen = null: off): energy absorption per unit
+  // density [n_comp][n_e], scored-photon energy threshold, kill energy
+  const real *muen;
+  real tle_thr, tle_emin;
   // batched simulations (n_sims > 0: labels is the concatenation of their
   // images, sim_maj their majorants [n_sims][n_e])
   const SimDesc<real> *sims;

@@ -484,14 +484,133 @@ enum : int { kDone = 0, kRefill = 1, kFly = 2, kInteract = 3 };
 // photon died.
 // pscored: what the pending interaction scores - 0 nothing (world), 1 the dose
 // voxel pv, 2 the crystal of the current head, 3 nothing (collimator).
-// One Woodcock tentative step of a photon inside the image box.
+// Voxel of a point inside (or on the surface of) the image box.
 template <typename real>
+__device__ __forceinline__ uint32_t voxel_of(const Scene<real> &s, const real p[3]) {
+  int ix = (int)((p[0] - s.bmin[0]) * s.inv_sp[0]);
+  int iy = (int)((p[1] - s.bmin[1]) * s.inv_sp[1]);
+  int iz = (int)((p[2] - s.bmin[2]) * s.inv_sp[2]);
+  ix = ix < 0 ? 0 : (ix >= s.nx ? s.nx - 1 : ix);
+  iy = iy < 0 ? 0 : (iy >= s.ny ? s.ny - 1 : iy);
+  iz = iz < 0 ? 0 : (iz >= s.nz ? s.nz - 1 : iz);
+  return (uint32_t)ix + (uint32_t)s.nx * ((uint32_t)iy + (uint32_t)s.ny * (uint32_t)iz);
+}
+
+// Track-length estimator (GateTLEDoseActor::ScoreTLEDepositStep,
+// core/opengate_core/opengate_lib/GateTLEDoseActor.cpp:249-299): the straight
+// path [p, p + len d) of a photon of energy e (table index ei) scores
+// e * mu_en(E, material) * length in every voxel it crosses.  Voxel walk of
+// Amanatides & Woo: distance to the next boundary per axis, the nearest one
+// crossed first (ties: x, then y, then z).
+template <typename real>
+__device__ __forceinline__ void tle_path(const Scene<real> &s, const real p[3], const real d[3], real len, real e,
+                                         const EIdx<real> &ei, HistList<real> &l, const Tally<real> &t,
+                                         BlockCounters *bc, unsigned int &n_dep) {
+  const int n0 = s.nx, n1 = s.ny, n2 = s.nz;
+  int i0 = (int)((p[0] - s.bmin[0]) * s.inv_sp[0]);
+  int i1 = (int)((p[1] - s.bmin[1]) * s.inv_sp[1]);
+  int i2 = (int)((p[2] - s.bmin[2]) * s.inv_sp[2]);
+  i0 = i0 < 0 ? 0 : (i0 >= n0 ? n0 - 1 : i0);
+  i1 = i1 < 0 ? 0 : (i1 >= n1 ? n1 - 1 : i1);
+  i2 = i2 < 0 ? 0 : (i2 >= n2 ? n2 - 1 : i2);
+  const real inf = gg_inf(real(0));
+  real tn0 = inf, tn1 = inf, tn2 = inf, td0 = inf, td1 = inf, td2 = inf;
+  int s0 = 0, s1 = 0, s2 = 0;
+  // first boundary along one axis: (bmin + k sp - p) / d, k the next plane index
+  auto first = [&](int a, int i, real pa, real da, real &tn, real &td, int &st) {
+    if (da > R<real>(0)) {
+      real b = (real)(i + 1) * s.sp[a];
+      b = s.bmin[a] + b;
+      b = b - pa;
+      tn = b / da;
+      td = s.sp[a] / da;
+      st = 1;
+    } else if (da < R<real>(0)) {
+      real b = (real)i * s.sp[a];
+      b = s.bmin[a] + b;
+      b = b - pa;
+      tn = b / da;
+      td = -s.sp[a];
+      td = td / da;
+      st = -1;
+    }
+    if (tn < R<real>(0)) tn = R<real>(0);
+  };
+  first(0, i0, p[0], d[0], tn0, td0, s0);
+  first(1, i1, p[1], d[1], tn1, td1, s1);
+  first(2, i2, p[2], d[2], tn2, td2, s2);
+  real tc = R<real>(0);
+  const int cap = n0 + n1 + n2 + 3;
+  for (int k = 0; k < cap; ++k) {
+    int a;
+    real tb;
+    if (tn1 < tn0) {
+      if (tn2 < tn1) a = 2, tb = tn2;
+      else a = 1, tb = tn1;
+    } else {
+      if (tn2 < tn0) a = 2, tb = tn2;
+      else a = 0, tb = tn0;
+    }
+    const real te = tb < len ? tb : len;
+    const real seg = te - tc;
+    if (seg > R<real>(0)) {
+      const uint32_t v = (uint32_t)i0 + (uint32_t)n0 * ((uint32_t)i1 + (uint32_t)n1 * (uint32_t)i2);
+      const int m = __ldg(s.labels + v);
+      real mu = interp_row(s.muen + (size_t)s.mat_comp[m] * s.n_e, ei);
+      mu = s.mat_rho[m] * mu;
+      real ed = e * mu;
+      ed = ed * seg;
+      deposit(l, t, bc, v, ed, n_dep);
+    }
+    tc = te;
+    if (!(tc < len)) break;
+    if (a == 0) {
+      i0 += s0;
+      if (i0 < 0 || i0 >= n0) break;
+      tn0 = tn0 + td0;
+    } else if (a == 1) {
+      i1 += s1;
+      if (i1 < 0 || i1 >= n1) break;
+      tn1 = tn1 + td1;
+    } else {
+      i2 += s2;
+      if (i2 < 0 || i2 >= n2) break;
+      tn2 = tn2 + td2;
+    }
+  }
+}
+
+// Scoring state handed to the flights of the track-length estimator.
+template <typename real>
+struct TleScore {
+  HistList<real> *l;
+  const Tally<real> *t;
+  unsigned int *n_dep;
+};
+
+// One Woodcock tentative step of a photon inside the image box.  With TLE, a
+// photon at or below the estimator's threshold first stops (depositing its
+// energy in its voxel) when at or below the kill energy, else scores the
+// path of the step.
+template <typename real, bool TLE = false>
 __device__ __forceinline__ int image_flight(const Scene<real> &s, Photon<real> &ph, Rng &g, int &pmat, uint32_t &pv,
-                                            int &pscored, unsigned int &n_wood, unsigned int &n_real) {
+                                            int &pscored, unsigned int &n_wood, unsigned int &n_real,
+                                            BlockCounters *bc = nullptr, TleScore<real> sc = {nullptr, nullptr, nullptr}) {
   {
+    if constexpr (TLE) {
+      if (ph.e <= s.tle_thr && ph.e <= s.tle_emin) {
+        deposit(*sc.l, *sc.t, bc, voxel_of(s, ph.pos), ph.e, *sc.n_dep);
+        ph.alive = 0;
+        return kRefill;
+      }
+    }
     real u = u01_open0<real>(g);
     real sd = -gg_log(u);
     sd = sd * ph.inv_mumax;
+    if constexpr (TLE) {
+      if (ph.e <= s.tle_thr)
+        tle_path(s, ph.pos, ph.dir, sd < ph.t_exit ? sd : ph.t_exit, ph.e, ph.ei, *sc.l, *sc.t, bc, *sc.n_dep);
+    }
     if (sd >= ph.t_exit) {
 #pragma unroll
       for (int a = 0; a < 3; ++a) ph.pos[a] = ph.pos[a] + ph.t_exit * ph.dir[a];
@@ -504,13 +623,7 @@ __device__ __forceinline__ int image_flight(const Scene<real> &s, Photon<real> &
 #pragma unroll
     for (int a = 0; a < 3; ++a) ph.pos[a] = ph.pos[a] + sd * ph.dir[a];
     ++n_wood;
-    int ix = (int)((ph.pos[0] - s.bmin[0]) * s.inv_sp[0]);
-    int iy = (int)((ph.pos[1] - s.bmin[1]) * s.inv_sp[1]);
-    int iz = (int)((ph.pos[2] - s.bmin[2]) * s.inv_sp[2]);
-    ix = ix < 0 ? 0 : (ix >= s.nx ? s.nx - 1 : ix);
-    iy = iy < 0 ? 0 : (iy >= s.ny ? s.ny - 1 : iy);
-    iz = iz < 0 ? 0 : (iz >= s.nz ? s.nz - 1 : iz);
-    uint32_t v = (uint32_t)ix + (uint32_t)s.nx * ((uint32_t)iy + (uint32_t)s.ny * (uint32_t)iz);
+    const uint32_t v = voxel_of(s, ph.pos);
     int m = __ldg(s.labels + v);
     real mu = interp_row(s.sig + (size_t)s.mat_comp[m] * s.n_e, ph.ei);
     mu = s.mat_rho[m] * mu;
@@ -524,17 +637,18 @@ __device__ __forceinline__ int image_flight(const Scene<real> &s, Photon<real> &
   }
 }
 
-template <typename real, bool SPECT>
+template <typename real, bool SPECT, bool TLE = false>
 __device__ __forceinline__ int flight(const Scene<real> &s, Photon<real> &ph, Rng &g, BlockCounters *bc, int &pmat,
                                       uint32_t &pv, int &pscored, unsigned int &n_wood, unsigned int &n_real,
-                                      unsigned int &n_world, unsigned int &n_head) {
+                                      unsigned int &n_world, unsigned int &n_head,
+                                      TleScore<real> sc = {nullptr, nullptr, nullptr}) {
   if (++ph.steps > kStepCap) {
     atomicAdd(&bc->loop_capped, 1u);
     ph.alive = 0;
     return kRefill;
   }
   if (ph.in_image) {
-    const int r = image_flight(s, ph, g, pmat, pv, pscored, n_wood, n_real);
+    const int r = image_flight<real, TLE>(s, ph, g, pmat, pv, pscored, n_wood, n_real, bc, sc);
     if constexpr (SPECT) return r;
     if (r != kFly || ph.in_image) return r;
     // Left the image box: take the world step at once (the same flight
@@ -609,14 +723,20 @@ __device__ __forceinline__ void event_add(const Scene<real> &s, Event<real> &ev,
   }
 }
 
-template <typename real, bool SPECT>
+// With TLE, the energy a photon at or below the estimator's threshold gives
+// to electrons is not scored (GateTLEDoseActor.cpp:236-243: secondaries of a
+// track-length-scored photon deposit nothing); its path scores instead.
+template <typename real, bool SPECT, bool TLE = false>
 __device__ __forceinline__ int do_interaction(const Scene<real> &s, Photon<real> &ph, Rng &g, BlockCounters *bc,
                                               int pmat, uint32_t pv, int pscored, HistList<real> &l,
                                               const Tally<real> &t, Secondary<real> &sec, unsigned int &n_dep,
                                               Event<real> &ev) {
+  const real e_pre = ph.e;
   real ed = interact(s, ph, pmat, g, bc, sec);
   if (pscored == 1) {
-    if constexpr (!SPECT) deposit(l, t, bc, pv, ed, n_dep);
+    if constexpr (!SPECT) {
+      if (!TLE || e_pre > s.tle_thr) deposit(l, t, bc, pv, ed, n_dep);
+    }
     if (ph.alive && ph.in_image) ph.t_exit = exit_distance(ph.pos, ph.dir, s.bmin, s.bmax);
   } else if (pscored == 0) {
     ph.can_enter = 1;

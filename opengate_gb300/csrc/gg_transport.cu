@@ -140,7 +140,7 @@ __global__ void __launch_bounds__(256) k_generate(Scene<real> s, KernelArgs a) {
 // unchanged.
 // MINB = resident blocks per SM the register budget is sized for.
 // SPECT selects the head transport and projection scoring instead of the dose tally.
-template <typename real, int MINB, bool SPECT, bool MULTI>
+template <typename real, int MINB, bool SPECT, bool MULTI, bool TLE>
 __global__ void __launch_bounds__(256, MINB) k_transport(Scene<real> sg, KernelArgs args) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ BlockCounters bc;
@@ -296,7 +296,7 @@ __global__ void __launch_bounds__(256, MINB) k_transport(Scene<real> sg, KernelA
       }
     } else if (phase == kInteract) {
       if (state == kInteract) {
-        state = do_interaction<real, SPECT>(s, ph, g, &bc, pmat, pv, pscored, l, t, sec, n_dep, ev);
+        state = do_interaction<real, SPECT, TLE>(s, ph, g, &bc, pmat, pv, pscored, l, t, sec, n_dep, ev);
         if (state == kRefill && sec.has) {
           pop_secondary(s, ph, sec);
           state = kFly;
@@ -304,7 +304,8 @@ __global__ void __launch_bounds__(256, MINB) k_transport(Scene<real> sg, KernelA
       }
     } else {
       if (state == kFly) {
-        state = flight<real, SPECT>(s, ph, g, &bc, pmat, pv, pscored, n_wood, n_real, n_world, n_head);
+        state = flight<real, SPECT, TLE>(s, ph, g, &bc, pmat, pv, pscored, n_wood, n_real, n_world, n_head,
+                                         TleScore<real>{&l, &t, &n_dep});
         if (state == kRefill && sec.has) {
           pop_secondary(s, ph, sec);
           state = kFly;
@@ -381,17 +382,17 @@ cudaError_t launch_generate(const Scene<real> &s, const KernelArgs &a, cudaStrea
   return cudaGetLastError();
 }
 
-template <typename real, int MINB, bool MULTI>
+template <typename real, int MINB, bool MULTI, bool TLE = false>
 static cudaError_t launch_transport_v(const Scene<real> &s, const KernelArgs &a, int grid, int block, size_t smem,
                                       cudaStream_t st) {
   static bool configured = false;
   if (!configured) {
-    cudaError_t e = cudaFuncSetAttribute(k_transport<real, MINB, false, MULTI>,
+    cudaError_t e = cudaFuncSetAttribute(k_transport<real, MINB, false, MULTI, TLE>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     if (e != cudaSuccess) return e;
     configured = true;
   }
-  k_transport<real, MINB, false, MULTI><<<grid, block, smem, st>>>(s, a);
+  k_transport<real, MINB, false, MULTI, TLE><<<grid, block, smem, st>>>(s, a);
   return cudaGetLastError();
 }
 
@@ -400,6 +401,13 @@ cudaError_t launch_transport(const Scene<real> &s, const KernelArgs &a, int grid
                              int minb, cudaStream_t st) {
   // SPECT runs use the two-stage kernels of gg_spect.cu
   if (s.spect) return cudaErrorInvalidValue;
+  if (s.muen) {
+    // track-length estimator (single simulations only)
+    if (s.n_sims > 0) return cudaErrorInvalidValue;
+    if (minb <= 2) return launch_transport_v<real, 2, false, true>(s, a, grid, block, smem, st);
+    if (minb == 3) return launch_transport_v<real, 3, false, true>(s, a, grid, block, smem, st);
+    return launch_transport_v<real, 4, false, true>(s, a, grid, block, smem, st);
+  }
   if (s.n_sims > 0) {
     if (minb <= 2) return launch_transport_v<real, 2, true>(s, a, grid, block, smem, st);
     if (minb == 3) return launch_transport_v<real, 3, true>(s, a, grid, block, smem, st);
@@ -418,9 +426,9 @@ cudaError_t launch_flush(unsigned long long *acc_e, unsigned long long *acc_e2, 
 
 template <typename real>
 cudaError_t occupancy_blocks(int block, size_t smem, int minb, int *bps) {
-  if (minb <= 2) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(bps, k_transport<real, 2, false, false>, block, smem);
-  if (minb == 3) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(bps, k_transport<real, 3, false, false>, block, smem);
-  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(bps, k_transport<real, 4, false, false>, block, smem);
+  if (minb <= 2) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(bps, k_transport<real, 2, false, false, false>, block, smem);
+  if (minb == 3) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(bps, k_transport<real, 3, false, false, false>, block, smem);
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(bps, k_transport<real, 4, false, false, false>, block, smem);
 }
 
 template size_t record_bytes<float>(size_t);

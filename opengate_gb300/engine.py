@@ -48,6 +48,15 @@ class DoseEngine:
     def reset(self):
         self._call("gg_reset_tally")
 
+    def set_tle(self, threshold_energy=float("inf"), energy_min=0.0, database="EPDL", enabled=True):
+        """Track-length estimator of the dose tally (gg_set_tle); mu_en of the
+        scene's compositions from ``database`` ("EPDL" or "NIST")."""
+        if enabled:
+            self._tle = self.scene.tle_desc(threshold_energy, energy_min, database)
+        else:
+            self._tle = C.TleDesc(0, 0.0, 0.0, None)
+        self._call("gg_set_tle", ctypes.byref(self._tle))
+
     def run(self, n, seed, first=0):
         self._call("gg_run", ctypes.c_uint64(n), ctypes.c_uint64(seed), ctypes.c_uint64(first))
 

@@ -83,6 +83,12 @@ class Scene:
             raise ValueError(f"source energies [{lo}, {hi}] MeV outside the tables [{T.E_MIN}, {T.E_MAX}]")
         self._build_descs()
 
+    def tle_desc(self, threshold_energy=float("inf"), energy_min=0.0, database="EPDL"):
+        """Descriptor of the track-length estimator (gg_set_tle) for these tables;
+        the mu_en table is kept alive by the scene."""
+        self._muen = np.ascontiguousarray(self.pt.muen(database), dtype=np.float32)
+        return C.TleDesc(1, float(threshold_energy), float(energy_min), C.ptr(self._muen, C.ctypes.c_float))
+
     @property
     def dims_xyz(self):
         nz, ny, nx = self.labels.shape

@@ -115,6 +115,21 @@ class PhysicsTables:
     def n_comp(self):
         return len(self.comps)
 
+    def muen(self, database="EPDL"):
+        """Energy absorption per unit density, mm^-1 per g/cm3 ([n_comp, N_E] float32):
+        0.1 x mu_en/rho of each composition at the grid energies, from the
+        material tables of :mod:`opengate_gb300.mu_tables` (the track-length
+        estimator's data; linear in ln E between grid points like ``sig``)."""
+        from . import mu_tables
+
+        out = np.zeros((self.n_comp, N_E), dtype=np.float32)
+        grid = energy_grid()
+        for c, ct in enumerate(self.comps):
+            t = mu_tables.material_table(tuple(int(z) for z in ct.z_list), tuple(float(w) for w in ct.w_list),
+                                         database)
+            out[c] = (0.1 * t.mu_en_over_rho(grid)).astype(np.float32)
+        return out
+
     def mu_mm(self, material_index, energy):
         """Linear attenuation (1/mm) of a material at ``energy`` (float64, for checks)."""
         c = self.mat_comp[material_index]

@@ -388,9 +388,13 @@ typedef struct {
   int *mat_comp;
   /* image */
   int nx, ny, nz;
-  real bmin[3], bmax[3], inv_sp[3];
+  real bmin[3], bmax[3], inv_sp[3], sp[3];
   const uint16_t *labels;
   real *maj;
+  /* track-length estimator (GateTLEDoseActor): tle = 0 off */
+  int tle;
+  real tle_thr, tle_emin;
+  real *muen; /* [n_comp][n_e] */
   /* world */
   real whalf[3];
   int world_mat;
@@ -1274,6 +1278,98 @@ static void score_singles(const scene_t *s, const event_t *ev, tally_t *t) {
   }
 }
 
+static uint32_t voxel_of(const scene_t *s, const real p[3]) {
+  int ix = (int)((p[0] - s->bmin[0]) * s->inv_sp[0]);
+  int iy = (int)((p[1] - s->bmin[1]) * s->inv_sp[1]);
+  int iz = (int)((p[2] - s->bmin[2]) * s->inv_sp[2]);
+  ix = ix < 0 ? 0 : (ix >= s->nx ? s->nx - 1 : ix);
+  iy = iy < 0 ? 0 : (iy >= s->ny ? s->ny - 1 : iy);
+  iz = iz < 0 ? 0 : (iz >= s->nz ? s->nz - 1 : iz);
+  return (uint32_t)ix + (uint32_t)s->nx * ((uint32_t)iy + (uint32_t)s->ny * (uint32_t)iz);
+}
+
+/* first boundary of a voxel walk along one axis: (bmin + k sp - p) / d for the
+   next plane k in the direction of travel, and the distance between planes */
+static void tle_first(const scene_t *s, int a, int i, real pa, real da, real *tn, real *td, int *st) {
+  if (da > R(0)) {
+    real b = (real)(i + 1) * s->sp[a];
+    b = s->bmin[a] + b;
+    b = b - pa;
+    *tn = b / da;
+    *td = s->sp[a] / da;
+    *st = 1;
+  } else if (da < R(0)) {
+    real b = (real)i * s->sp[a];
+    b = s->bmin[a] + b;
+    b = b - pa;
+    *tn = b / da;
+    real q = -s->sp[a];
+    *td = q / da;
+    *st = -1;
+  }
+  if (*tn < R(0)) *tn = R(0);
+}
+
+/* Track-length estimator (GateTLEDoseActor::ScoreTLEDepositStep,
+   GateTLEDoseActor.cpp:249-299): the straight path [p, p + len d) of a photon
+   of energy e scores e * mu_en(E, material) * length in every voxel it
+   crosses (Amanatides-Woo voxel walk; ties: x, then y, then z). */
+static void tle_path(const scene_t *s, const real p[3], const real d[3], real len, real e, eidx_t ei,
+                     hlist_t *l, tally_t *t) {
+  const int n0 = s->nx, n1 = s->ny, n2 = s->nz;
+  int i0 = (int)((p[0] - s->bmin[0]) * s->inv_sp[0]);
+  int i1 = (int)((p[1] - s->bmin[1]) * s->inv_sp[1]);
+  int i2 = (int)((p[2] - s->bmin[2]) * s->inv_sp[2]);
+  i0 = i0 < 0 ? 0 : (i0 >= n0 ? n0 - 1 : i0);
+  i1 = i1 < 0 ? 0 : (i1 >= n1 ? n1 - 1 : i1);
+  i2 = i2 < 0 ? 0 : (i2 >= n2 ? n2 - 1 : i2);
+  real tn0 = R(INFINITY), tn1 = R(INFINITY), tn2 = R(INFINITY);
+  real td0 = R(INFINITY), td1 = R(INFINITY), td2 = R(INFINITY);
+  int s0 = 0, s1 = 0, s2 = 0;
+  tle_first(s, 0, i0, p[0], d[0], &tn0, &td0, &s0);
+  tle_first(s, 1, i1, p[1], d[1], &tn1, &td1, &s1);
+  tle_first(s, 2, i2, p[2], d[2], &tn2, &td2, &s2);
+  real tc = R(0);
+  const int cap = n0 + n1 + n2 + 3;
+  for (int k = 0; k < cap; ++k) {
+    int a;
+    real tb;
+    if (tn1 < tn0) {
+      if (tn2 < tn1) a = 2, tb = tn2;
+      else a = 1, tb = tn1;
+    } else {
+      if (tn2 < tn0) a = 2, tb = tn2;
+      else a = 0, tb = tn0;
+    }
+    const real te = tb < len ? tb : len;
+    const real seg = te - tc;
+    if (seg > R(0)) {
+      const uint32_t v = (uint32_t)i0 + (uint32_t)n0 * ((uint32_t)i1 + (uint32_t)n1 * (uint32_t)i2);
+      const int m = s->labels[v];
+      real mu = interp_row(s->muen + (size_t)s->mat_comp[m] * s->n_e, ei);
+      mu = s->mat_rho[m] * mu;
+      real ed = e * mu;
+      ed = ed * seg;
+      deposit(l, t, v, ed);
+    }
+    tc = te;
+    if (!(tc < len)) break;
+    if (a == 0) {
+      i0 += s0;
+      if (i0 < 0 || i0 >= n0) break;
+      tn0 = tn0 + td0;
+    } else if (a == 1) {
+      i1 += s1;
+      if (i1 < 0 || i1 >= n1) break;
+      tn1 = tn1 + td1;
+    } else {
+      i2 += s2;
+      if (i2 < 0 || i2 >= n2) break;
+      tn2 = tn2 + td2;
+    }
+  }
+}
+
 static void transport_photon(const scene_t *s, photon_t *ph, rng_t *g, tally_t *t, hlist_t *l,
                              photon_t *sec, int *has_sec, event_t *ev) {
   int steps = 0;
@@ -1285,9 +1381,17 @@ static void transport_photon(const scene_t *s, photon_t *ph, rng_t *g, tally_t *
       break;
     }
     if (ph->in_image) {
+      if (s->tle && ph->e <= s->tle_thr && ph->e <= s->tle_emin) {
+        /* a scored photon at or below the kill energy stops in its voxel */
+        deposit(l, t, voxel_of(s, ph->pos), ph->e);
+        ph->alive = 0;
+        break;
+      }
       real u = u01_open0(g);
       real sd = -ggo_log(u);
       sd = sd * ph->inv_mumax;
+      if (s->tle && ph->e <= s->tle_thr)
+        tle_path(s, ph->pos, ph->dir, sd < ph->t_exit ? sd : ph->t_exit, ph->e, ph->ei, l, t);
       if (sd >= ph->t_exit) {
         for (int a = 0; a < 3; ++a) ph->pos[a] = ph->pos[a] + ph->t_exit * ph->dir[a];
         ph->in_image = 0;
@@ -1311,8 +1415,10 @@ static void transport_photon(const scene_t *s, photon_t *ph, rng_t *g, tally_t *
       real u2 = u01(g);
       if (u2 * ph->mumax >= mu) continue;
       t->cnt[GG_CNT_REAL_INTERACTIONS]++;
+      const real e_pre = ph->e;
       real ed = interact(s, ph, m, g, t, sec, has_sec);
-      if (!s->spect) deposit(l, t, v, ed);
+      /* electrons of a track-length-scored photon deposit nothing (GateTLEDoseActor.cpp:236-243) */
+      if (!s->spect && !(s->tle && e_pre <= s->tle_thr)) deposit(l, t, v, ed);
       if (ph->alive && ph->in_image) ph->t_exit = exit_distance(ph->pos, ph->dir, s->bmin, s->bmax);
     } else if (ph->in_head) {
       head_step(s, ph, g, t, ev);
@@ -1388,7 +1494,7 @@ static real *conv_d(const double *src, size_t n) {
 static void scene_free(scene_t *s) {
   free(s->sig); free(s->cum); free(s->ray_amax); free(s->ray_x2); free(s->ray_cum); free(s->mat_rho);
   free(s->mat_comp); free(s->maj); free(s->s_spec_e); free(s->s_spec_cdf); free(s->acc_box);
-  free(s->cdf_z); free(s->cdf_y); free(s->cdf_x);
+  free(s->cdf_z); free(s->cdf_y); free(s->cdf_x); free(s->muen);
 }
 
 static int scene_init(scene_t *s, const gg_tables_desc *tb, const gg_volume_desc *vol,
@@ -1410,6 +1516,7 @@ static int scene_init(scene_t *s, const gg_tables_desc *tb, const gg_volume_desc
     s->bmin[a] = (real)vol->corner[a];
     s->bmax[a] = (real)(vol->corner[a] + (double)vol->dims[a] * vol->spacing[a]);
     s->inv_sp[a] = (real)(1.0 / vol->spacing[a]);
+    s->sp[a] = (real)vol->spacing[a];
     s->whalf[a] = (real)w->half_size[a];
   }
   s->labels = vol->labels;
@@ -1517,12 +1624,18 @@ static void *worker_main(void *arg) {
 /* Runs histories [first, first + n) in batches of `batch`, adding the fixed
    point batch sums into the float64 images edep / edep2 (either may be
    NULL for the squared image), and adding to counters[GG_N_COUNTERS]. */
-int GGO_PREFIX(run_dose)(const gg_tables_desc *tb, const gg_volume_desc *vol, const gg_world_desc *w,
-                         const gg_source_desc *src, uint64_t seed, uint64_t first, uint64_t n,
-                         uint64_t batch, int n_threads, double *edep, double *edep2,
+static int run_dose_impl(const gg_tables_desc *tb, const gg_volume_desc *vol, const gg_world_desc *w,
+                         const gg_source_desc *src, const gg_tle_desc *tle, uint64_t seed, uint64_t first,
+                         uint64_t n, uint64_t batch, int n_threads, double *edep, double *edep2,
                          uint64_t *counters) {
   scene_t s;
   scene_init(&s, tb, vol, w, src);
+  if (tle && tle->enabled) {
+    s.tle = 1;
+    s.tle_thr = (real)tle->threshold_energy;
+    s.tle_emin = (real)tle->energy_min;
+    s.muen = conv_f(tle->muen, (size_t)tb->n_comp * tb->n_e);
+  }
   size_t nv = (size_t)s.nx * s.ny * s.nz;
   uint64_t *acc_e = (uint64_t *)calloc(nv, sizeof(uint64_t));
   uint64_t *acc_e2 = edep2 ? (uint64_t *)calloc(2 * nv, sizeof(uint64_t)) : NULL;
@@ -1572,6 +1685,21 @@ int GGO_PREFIX(run_dose)(const gg_tables_desc *tb, const gg_volume_desc *vol, co
   free(acc_e2);
   scene_free(&s);
   return status;
+}
+
+int GGO_PREFIX(run_dose)(const gg_tables_desc *tb, const gg_volume_desc *vol, const gg_world_desc *w,
+                         const gg_source_desc *src, uint64_t seed, uint64_t first, uint64_t n,
+                         uint64_t batch, int n_threads, double *edep, double *edep2,
+                         uint64_t *counters) {
+  return run_dose_impl(tb, vol, w, src, NULL, seed, first, n, batch, n_threads, edep, edep2, counters);
+}
+
+/* run_dose with the track-length estimator of gg_set_tle. */
+int GGO_PREFIX(run_dose_tle)(const gg_tables_desc *tb, const gg_volume_desc *vol, const gg_world_desc *w,
+                             const gg_source_desc *src, const gg_tle_desc *tle, uint64_t seed, uint64_t first,
+                             uint64_t n, uint64_t batch, int n_threads, double *edep, double *edep2,
+                             uint64_t *counters) {
+  return run_dose_impl(tb, vol, w, src, tle, seed, first, n, batch, n_threads, edep, edep2, counters);
 }
 
 /* SPECT projections: for each run r (gantry position, head frames

@@ -34,6 +34,13 @@ def lib(precision=32):
                        ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int,
                        ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double),
                        ctypes.POINTER(ctypes.c_uint64)]
+        fn = getattr(L, pre + "run_dose_tle")
+        fn.restype = ctypes.c_int
+        fn.argtypes = [ctypes.POINTER(C.TablesDesc), ctypes.POINTER(C.VolumeDesc),
+                       ctypes.POINTER(C.WorldDesc), ctypes.POINTER(C.SourceDesc), ctypes.POINTER(C.TleDesc),
+                       ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int,
+                       ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double),
+                       ctypes.POINTER(ctypes.c_uint64)]
         for name in ("log", "exp"):
             f = getattr(L, pre + name)
             f.restype = ctypes.c_double
@@ -62,17 +69,22 @@ def lib(precision=32):
     return _libs[precision]
 
 
-def run_dose(scene, n, seed, first=0, batch=0, threads=1, precision=32, squared=True):
-    """Oracle run of histories [first, first + n): (edep, edep2 or None, counters dict)."""
+def run_dose(scene, n, seed, first=0, batch=0, threads=1, precision=32, squared=True, tle=None):
+    """Oracle run of histories [first, first + n): (edep, edep2 or None, counters dict).
+    ``tle``: a gg_tle_desc (Scene.tle_desc) for the track-length estimator."""
     L = lib(precision)
     nv = scene.n_voxels
     edep = np.zeros(nv, dtype=np.float64)
     edep2 = np.zeros(nv, dtype=np.float64) if squared else None
     cnt = np.zeros(C.GG_N_COUNTERS, dtype=np.uint64)
-    st = getattr(L, f"ggo{precision}_run_dose")(
-        ctypes.byref(scene.tables_desc), ctypes.byref(scene.volume_desc), ctypes.byref(scene.world_desc),
-        ctypes.byref(scene.source_desc), seed, first, n, batch, threads,
-        C.ptr(edep, ctypes.c_double), C.ptr(edep2, ctypes.c_double), C.ptr(cnt, ctypes.c_uint64))
+    descs = (ctypes.byref(scene.tables_desc), ctypes.byref(scene.volume_desc), ctypes.byref(scene.world_desc),
+             ctypes.byref(scene.source_desc))
+    outs = (C.ptr(edep, ctypes.c_double), C.ptr(edep2, ctypes.c_double), C.ptr(cnt, ctypes.c_uint64))
+    if tle is not None:
+        st = getattr(L, f"ggo{precision}_run_dose_tle")(*descs, ctypes.byref(tle), seed, first, n, batch, threads,
+                                                        *outs)
+    else:
+        st = getattr(L, f"ggo{precision}_run_dose")(*descs, seed, first, n, batch, threads, *outs)
     if st != 0:
         raise RuntimeError(f"oracle run failed with status {st}")
     shape = scene.labels.shape
