@@ -26,6 +26,8 @@
  *                               (core/opengate_core/opengate_lib/GateSPSVoxelsPosDistribution.cpp:29-74)
  *   gg_add_dose_tally           GateDoseActor::InitializeCpp / BeginOfRunAction
  *                               (core/opengate_core/opengate_lib/GateDoseActor.cpp:100-137)
+ *   gg_spect_set_blur           GateDigitizerBlurringActor / GateDigitizerSpatialBlurringActor
+ *                               (core/opengate_core/opengate_lib/digitizer/*BlurringActor.cpp)
  *   gg_set_tle                  GateTLEDoseActor (track-length estimator)
  *                               (core/opengate_core/opengate_lib/GateTLEDoseActor.cpp:174-299)
  *   gg_run                      GateSourceManager::StartMasterThread -> /run/beamOn
@@ -196,7 +198,11 @@ typedef struct {
   double spacing[2];           /* mm */
   int32_t n_heads;             /* 1 or 2 */
   int32_t n_runs;              /* gantry positions; projection slice = window + run * n_windows */
+  int32_t adder_policy;        /* GG_ADDER_WINNER (0) or GG_ADDER_CENTROID: position of a single */
 } gg_spect_desc;
+/* adder policies (GateDigiAdderInVolume, digitizer/GateDigiAdderInVolume.cpp:29-88) */
+#define GG_ADDER_WINNER 0   /* EnergyWinnerPosition: the largest deposit's point */
+#define GG_ADDER_CENTROID 1 /* EnergyWeightedCentroidPosition: sum(e x) / sum(e) */
 
 /* ARF training photons (replaces the source + plane of
    contrib/spect/ge_discovery_nm670.py:994-1027 add_source_for_arf_training_dataset /
@@ -293,6 +299,39 @@ int gg_last_kernel_ms(gg_ctx *ctx, double *generate_ms, double *transport_ms, do
    gg_get_projection returns the counts as float64,
    [head][run][window][size[1]][size[0]]. */
 int gg_spect_setup(gg_ctx *ctx, const gg_spect_desc *spect);
+
+/* Digitizer blurring of the singles, between the adder and the energy
+   windows (replaces DigitizerBlurringActor on TotalEnergyDeposit and
+   DigitizerSpatialBlurringActor on PostPosition:
+   digitizer/GateDigitizerBlurringActor.cpp:74-97,
+   digitizer/GateDigitizerSpatialBlurringActor.cpp:85-206,
+   opengate/actors/digitizers.py:428-580, 801-920).  Energy: E' = N(E, sigma)
+   with sigma = energy_sigma (GG_BLUR_GAUSSIAN), or FWHM/E =
+   resolution sqrt(reference) / sqrt(E) (GG_BLUR_INVERSE_SQUARE), or
+   slope (E - reference) + resolution (GG_BLUR_LINEAR), sigma = FWHM / 2.3548.
+   Position: the energy-winner point in the crystal plane (a1, a2) moves by
+   N(0, spatial_sigma); with keep_in_solid_limits points outside the crystal
+   (|a| > half_width) are put just inside the edge (1e-6 half_width; the
+   reference's 1 nm would round onto the edge in FP32); with truncated = 1 they
+   are redrawn with the reference's corrected sigma instead.  The draws come
+   from each history's own random stream; ARF training rows take the blurred
+   energy's window.  All-zero descriptor = no blurring. */
+#define GG_BLUR_NONE 0
+#define GG_BLUR_GAUSSIAN 1
+#define GG_BLUR_INVERSE_SQUARE 2
+#define GG_BLUR_LINEAR 3
+typedef struct {
+  int32_t energy_method;        /* GG_BLUR_* */
+  double energy_sigma;          /* MeV (Gaussian) */
+  double energy_resolution;     /* FWHM / E at the reference energy */
+  double energy_reference;      /* MeV */
+  double energy_slope;          /* 1 / MeV (linear law) */
+  int32_t spatial;              /* 0 off, 1 on */
+  double spatial_sigma[2];      /* mm along a1, a2 */
+  int32_t keep_in_solid_limits; /* clamp into the crystal */
+  int32_t truncated;            /* redraw outside the crystal (truncated Gaussian) */
+} gg_blur_desc;
+int gg_spect_set_blur(gg_ctx *ctx, const gg_blur_desc *blur);
 int gg_spect_set_heads(gg_ctx *ctx, int32_t run, const double *frames);
 int gg_spect_run(gg_ctx *ctx, uint64_t n_per_run, uint64_t seed, uint64_t first, const double *frames);
 int gg_get_projection(gg_ctx *ctx, double *out, size_t n);

@@ -51,6 +51,18 @@ class TablesDesc(ctypes.Structure):
     ]
 
 
+GG_BLUR_NONE, GG_BLUR_GAUSSIAN, GG_BLUR_INVERSE_SQUARE, GG_BLUR_LINEAR = 0, 1, 2, 3
+
+
+class BlurDesc(ctypes.Structure):
+    _fields_ = [
+        ("energy_method", ctypes.c_int32), ("energy_sigma", ctypes.c_double),
+        ("energy_resolution", ctypes.c_double), ("energy_reference", ctypes.c_double),
+        ("energy_slope", ctypes.c_double), ("spatial", ctypes.c_int32), ("spatial_sigma", ctypes.c_double * 2),
+        ("keep_in_solid_limits", ctypes.c_int32), ("truncated", ctypes.c_int32),
+    ]
+
+
 class TleDesc(ctypes.Structure):
     _fields_ = [
         ("enabled", ctypes.c_int32), ("threshold_energy", ctypes.c_double), ("energy_min", ctypes.c_double),
@@ -92,8 +104,12 @@ class SpectDesc(ctypes.Structure):
         ("collimator_material", ctypes.c_int32), ("crystal_material", ctypes.c_int32),
         ("n_windows", ctypes.c_int32), ("window_lo", ctypes.c_double * 8), ("window_hi", ctypes.c_double * 8),
         ("size", ctypes.c_int32 * 2), ("spacing", ctypes.c_double * 2), ("n_heads", ctypes.c_int32),
-        ("n_runs", ctypes.c_int32),
+        ("n_runs", ctypes.c_int32), ("adder_policy", ctypes.c_int32),
     ]
+
+
+GG_ADDER_WINNER, GG_ADDER_CENTROID = 0, 1
+ADDER_POLICIES = {"EnergyWinnerPosition": GG_ADDER_WINNER, "EnergyWeightedCentroidPosition": GG_ADDER_CENTROID}
 
 
 class ArfSampling(ctypes.Structure):
@@ -182,6 +198,7 @@ PROTOTYPES = [
     ("gg_last_kernel_ms", ctypes.c_int,
      [ctypes.c_void_p, _f64p, _f64p, _f64p, ctypes.POINTER(ctypes.c_int32)]),
     ("gg_spect_setup", ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(SpectDesc)]),
+    ("gg_spect_set_blur", ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(BlurDesc)]),
     ("gg_spect_set_heads", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, _f64p]),
     ("gg_spect_run", ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64, _f64p]),
     ("gg_get_projection", ctypes.c_int, [ctypes.c_void_p, _f64p, ctypes.c_size_t]),

@@ -459,6 +459,92 @@ class DigitizerProjectionActor(GateObject):
         object.__setattr__(self, "counts_squared", ActorOutput(self, "squared_counts", False))
 
 
+FWHM_TO_SIGMA = 1.0 / (2.0 * math.sqrt(2.0 * math.log(2.0)))
+
+
+class DigitizerAdderActor(GateObject):
+    """Singles of a head crystal from its hits (DigitizerAdderActor; GateDigiAdderInVolume,
+    digitizer/GateDigiAdderInVolume.cpp:29-88): energy sum per event, position of the
+    energy winner or the energy-weighted centroid (``policy``)."""
+
+    type_name = "DigitizerAdderActor"
+    user_info_defaults = {"attached_to": None, "input_digi_collection": "Hits", "policy": "EnergyWinnerPosition",
+                          "time_difference": False, "number_of_hits": False, "group_volume": None,
+                          "skip_attributes": [], "clear_every": 1e5, "output_filename": "auto", "priority": 100}
+
+    def adder_policy(self):
+        if self.policy not in C.ADDER_POLICIES:
+            raise ValueError(f"policy '{self.policy}'")
+        if self.group_volume is not None:
+            raise NotImplementedError("the GPU path adds the hits of the whole crystal (group_volume None)")
+        return self.policy
+
+
+class DigitizerBlurringActor(GateObject):
+    """Energy blurring of the singles of a head crystal (DigitizerBlurringActor,
+    opengate/actors/digitizers.py:428-580; GateDigitizerBlurringActor.cpp:74-97):
+    Gaussian (blur_sigma or blur_fwhm), InverseSquare (blur_resolution = FWHM/E at
+    blur_reference_value) or Linear (+ blur_slope)."""
+
+    type_name = "DigitizerBlurringActor"
+    user_info_defaults = {"attached_to": None, "input_digi_collection": "Hits", "blur_attribute": None,
+                          "skip_attributes": [], "clear_every": 1e5, "blur_method": "Gaussian", "blur_sigma": None,
+                          "blur_fwhm": None, "blur_reference_value": 0, "blur_resolution": 0, "blur_slope": 0,
+                          "output_filename": "auto", "priority": 100}
+
+    def energy_blur(self):
+        """Keyword arguments of SpectSpec.set_energy_blur (MeV), validated as the reference does."""
+        if self.blur_attribute != "TotalEnergyDeposit":
+            raise NotImplementedError("the GPU path blurs the singles' TotalEnergyDeposit only")
+        m = self.blur_method
+        if m == "Gaussian":
+            if self.blur_fwhm is not None and self.blur_sigma is not None:
+                raise ValueError("Error, use blur_sigma or blur_fwhm, not both")
+            sigma = self.blur_fwhm * FWHM_TO_SIGMA if self.blur_fwhm is not None else self.blur_sigma
+            if sigma is None:
+                raise ValueError("Error, use blur_sigma or blur_fwhm")
+            return dict(method="Gaussian", sigma=float(sigma) / u.MeV)
+        if m not in ("InverseSquare", "Linear"):
+            raise ValueError(f"blur_method '{m}'")
+        if self.blur_reference_value is None or self.blur_reference_value < 0:
+            raise ValueError("Error, use positive blur_reference_value")
+        if self.blur_resolution is None or self.blur_resolution < 0:
+            raise ValueError("Error, use positive blur_resolution")
+        slope = 0.0 if self.blur_slope is None else float(self.blur_slope)
+        if m == "Linear" and self.blur_slope is None:
+            raise ValueError("Error, use positive blur_slope")
+        return dict(method=m, resolution=float(self.blur_resolution),
+                    reference=float(self.blur_reference_value) / u.MeV, slope=slope * u.MeV)
+
+
+class DigitizerSpatialBlurringActor(GateObject):
+    """Spatial blurring of the singles' position in the crystal (DigitizerSpatialBlurringActor,
+    opengate/actors/digitizers.py:801-920; GateDigitizerSpatialBlurringActor.cpp:85-206)."""
+
+    type_name = "DigitizerSpatialBlurringActor"
+    user_info_defaults = {"attached_to": None, "attributes": [], "input_digi_collection": "Hits",
+                          "skip_attributes": [], "clear_every": int(1e5), "blur_attribute": None, "blur_fwhm": None,
+                          "blur_sigma": None, "keep_in_solid_limits": True, "use_truncated_Gaussian": True,
+                          "output_filename": "auto", "priority": 100}
+
+    def spatial_blur(self):
+        """Keyword arguments of SpectSpec.set_spatial_blur (mm)."""
+        if self.blur_attribute not in ("PostPosition", "PrePosition", "Position"):
+            raise NotImplementedError("the GPU path blurs the singles' position only")
+        if self.blur_fwhm is not None and self.blur_sigma is not None:
+            raise ValueError("Error, use blur_sigma or blur_fwhm, not both")
+        if self.blur_fwhm is not None:
+            v = self.blur_fwhm
+            sigma = [x * FWHM_TO_SIGMA for x in v] if hasattr(v, "__len__") else [v * FWHM_TO_SIGMA] * 3
+        elif self.blur_sigma is not None:
+            v = self.blur_sigma
+            sigma = list(v) if hasattr(v, "__len__") else [v] * 3
+        else:
+            raise ValueError("Error, use blur_sigma or blur_fwhm")
+        return dict(sigma=[float(x) / u.mm for x in sigma[:2]], keep_in_solid_limits=bool(self.keep_in_solid_limits),
+                    truncated=bool(self.use_truncated_Gaussian))
+
+
 class SimulationStatisticsActor(GateObject):
     type_name = "SimulationStatisticsActor"
     user_info_defaults = {"attached_to": "world", "track_types_flag": False, "output_filename": "auto"}
@@ -522,6 +608,9 @@ class Simulation:
             raise ValueError(f"an actor named '{name}' already exists")
         cls = {"DoseActor": DoseActor, "TLEDoseActor": TLEDoseActor,
                "SimulationStatisticsActor": SimulationStatisticsActor,
+               "DigitizerAdderActor": DigitizerAdderActor,
+               "DigitizerBlurringActor": DigitizerBlurringActor,
+               "DigitizerSpatialBlurringActor": DigitizerSpatialBlurringActor,
                "DigitizerProjectionActor": DigitizerProjectionActor}.get(actor_type)
         if cls is None:
             raise NotImplementedError(f"actor type '{actor_type}' is not supported by the GPU path")
@@ -619,6 +708,26 @@ class Simulation:
                          head_start_deg=[h.start_angle_deg for h in heads])
         if half_w:
             sp.half_width = half_w
+        # digitizer adder and blurring: one setting shared by every head's crystal
+        def set_policy(policy):
+            sp.adder_policy = policy
+
+        for kind, setter, getter in ((DigitizerAdderActor, set_policy, "adder_policy"),
+                                     (DigitizerBlurringActor, sp.set_energy_blur, "energy_blur"),
+                                     (DigitizerSpatialBlurringActor, sp.set_spatial_blur, "spatial_blur")):
+            mods = [a for a in self.actors.values() if isinstance(a, kind)]
+            if not mods:
+                continue
+            for a in mods:
+                if a.attached_to not in head_of:
+                    raise ValueError(f"'{a.name}' must be attached to a head crystal ({', '.join(head_of)})")
+            params = [getattr(a, getter)() for a in mods]
+            if len({a.attached_to for a in mods}) != len(mods) or any(p != params[0] for p in params[1:]):
+                raise NotImplementedError(f"one {kind.type_name} per head crystal, the same on every head")
+            if isinstance(params[0], dict):
+                setter(**params[0])
+            else:
+                setter(params[0])
         return scene, sp, sources, projs, head_of
 
     def _run_spect(self):

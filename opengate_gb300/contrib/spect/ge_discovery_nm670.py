@@ -5,8 +5,10 @@ A head is one SpectHead volume (collimator with hexagonal holes, gap, NaI
 crystal); its crystal is addressed as f"{name}_crystal" by add_digitizer.
 Collimators: lehr (1.5 mm holes, 35 mm, 0.2 mm septa), megp (3 mm, 58 mm,
 1.05 mm), hegp (4 mm, 66 mm, 1.8 mm); crystal 3/8" or 5/8".  The digitizer is
-adder (energy winner) -> energy windows -> projection; the reference's
-energy and spatial blurring modules are not part of this digitizer.
+adder (energy winner) -> energy blurring -> spatial blurring -> energy windows
+-> projection, with the reference's add_digitizer parameters (inverse-square
+energy blur of 6.3 % FWHM at 140.57 keV, 3 mm FWHM spatial blur kept inside
+the crystal; ge_discovery_nm670.py:1166-1230).
 """
 
 from ...units import g4_units as _u
@@ -49,21 +51,50 @@ def get_default_size_and_spacing():
 
 
 class Digitizer:
-    """The chain of one head: its projection actor is `projection` (find_module("projection"))."""
+    """The chain of one head: blurring modules and the projection actor (find_module)."""
 
-    def __init__(self, name, projection):
+    def __init__(self, name, projection, modules=()):
         self.name = name
         self.projection = projection
+        self.modules = list(modules)
 
     def find_module(self, kind):
-        if "projection" in kind.lower():
+        k = kind.lower()
+        if "projection" in k:
             return self.projection
+        for m in self.modules:
+            if k in m.name.lower() or k == m.type_name.lower():
+                return m
         raise KeyError(f"digitizer '{self.name}' has no module '{kind}'")
 
 
-def add_digitizer(sim, crystal_name, name=None, size=None, spacing=None, channels=None, filename=None):
+def add_digitizer(sim, crystal_name, name=None, size=None, spacing=None, channels=None, filename=None,
+                  policy="EnergyWinnerPosition", resolution=0.063, reference_energy=140.57 * _u.keV,
+                  spatial_fwhm=3 * _u.mm):
+    """The NM670 chain: adder, inverse-square energy blur (FWHM/E = resolution at
+    reference_energy), spatial blur (spatial_fwhm, kept in the crystal), windows, projection."""
     name = crystal_name if name is None else name
     d_size, d_spacing = get_default_size_and_spacing()
+    # singles
+    sc = sim.add_actor("DigitizerAdderActor", f"{name}_singles")
+    sc.attached_to = crystal_name
+    sc.group_volume = None
+    sc.policy = policy
+    # energy blurring
+    eb = sim.add_actor("DigitizerBlurringActor", f"{name}_eblur")
+    eb.attached_to = crystal_name
+    eb.blur_attribute = "TotalEnergyDeposit"
+    eb.blur_method = "InverseSquare"
+    eb.blur_resolution = resolution
+    eb.blur_reference_value = reference_energy
+    # spatial blurring
+    sb = sim.add_actor("DigitizerSpatialBlurringActor", f"{name}_sblur")
+    sb.attached_to = crystal_name
+    sb.blur_attribute = "PostPosition"
+    sb.blur_fwhm = spatial_fwhm
+    sb.keep_in_solid_limits = True
+    sb.use_truncated_Gaussian = False
+    # energy windows and projection
     proj = sim.add_actor("DigitizerProjectionActor", f"{name}_projection")
     proj.attached_to = crystal_name
     proj.channels = channels if channels is not None else get_default_energy_windows("tc99m")
@@ -72,4 +103,4 @@ def add_digitizer(sim, crystal_name, name=None, size=None, spacing=None, channel
     proj.spacing = spacing if spacing is not None else d_spacing
     if filename is not None:
         proj.output_filename = filename
-    return Digitizer(name, proj)
+    return Digitizer(name, proj, [sc, eb, sb])

@@ -48,6 +48,8 @@ struct gg_ctx {
   int n_e = 0, n_comp = 0, n_ray = 0, n_mat = 0;
   float ln_emin = 0, inv_dln = 0, e_min = 0, e_max = 0;
   void *d_sig = nullptr, *d_cum = nullptr, *d_ray_amax = nullptr, *d_ray_cum = nullptr, *d_mat_rho = nullptr;
+  // digitizer blurring (gg_spect_set_blur)
+  gg_blur_desc blur{};
   // track-length estimator (gg_set_tle)
   void *d_muen = nullptr;
   bool tle = false;
@@ -262,6 +264,15 @@ struct gg_ctx {
       s.whalf[a] = (real)world.half_size[a];
     }
     s.muen = (tle && !have_spect && !have_batch) ? (const real *)d_muen : nullptr;
+    s.eblur = blur.energy_method;
+    s.eb_sigma = (real)blur.energy_sigma;
+    s.eb_res = (real)blur.energy_resolution;
+    s.eb_ref = (real)blur.energy_reference;
+    s.eb_slope = (real)blur.energy_slope;
+    s.sblur = blur.spatial ? (blur.truncated ? 2 : 1) : 0;
+    s.sb_keep = blur.keep_in_solid_limits;
+    s.sb_sigma[0] = (real)blur.spatial_sigma[0];
+    s.sb_sigma[1] = (real)blur.spatial_sigma[1];
     s.tle_thr = (real)tle_thr;
     s.tle_emin = (real)tle_emin;
     s.labels = d_labels;
@@ -320,6 +331,7 @@ struct gg_ctx {
       s.run_len = run_len;
       s.run_base = run_base;
       s.half_w = (real)sp.half_width;
+      s.centroid = sp.adder_policy == GG_ADDER_CENTROID ? 1 : 0;
       s.zb[0] = (real)0;
       s.zb[1] = (real)sp.collimator_thickness;
       s.zb[2] = (real)(sp.collimator_thickness + sp.gap);
@@ -808,6 +820,23 @@ int gg_add_dose_tally(gg_ctx *c, int32_t score_squared) {
   c->squared = score_squared != 0;
   c->have_tally = true;
   return gg_reset_tally(c);
+}
+
+int gg_spect_set_blur(gg_ctx *c, const gg_blur_desc *b) {
+  if (!c || !b) return GG_ERR_ARG;
+  if (b->energy_method < GG_BLUR_NONE || b->energy_method > GG_BLUR_LINEAR)
+    return c->fail(GG_ERR_ARG, "gg_spect_set_blur: unknown energy blurring method %d", b->energy_method);
+  if (b->energy_method == GG_BLUR_GAUSSIAN && !(b->energy_sigma >= 0))
+    return c->fail(GG_ERR_ARG, "gg_spect_set_blur: energy sigma must be >= 0");
+  if ((b->energy_method == GG_BLUR_INVERSE_SQUARE || b->energy_method == GG_BLUR_LINEAR) &&
+      (!(b->energy_resolution >= 0) || !(b->energy_reference >= 0) || !std::isfinite(b->energy_slope)))
+    return c->fail(GG_ERR_ARG, "gg_spect_set_blur: resolution and reference must be >= 0");
+  if (b->spatial && (!(b->spatial_sigma[0] >= 0) || !(b->spatial_sigma[1] >= 0)))
+    return c->fail(GG_ERR_ARG, "gg_spect_set_blur: spatial sigma must be >= 0");
+  if (b->spatial && b->truncated && (!(b->spatial_sigma[0] > 0) || !(b->spatial_sigma[1] > 0)))
+    return c->fail(GG_ERR_ARG, "gg_spect_set_blur: the truncated Gaussian needs sigma > 0");
+  c->blur = *b;
+  return GG_OK;
 }
 
 int gg_set_tle(gg_ctx *c, const gg_tle_desc *d) {

@@ -109,9 +109,10 @@ __global__ void __launch_bounds__(256) k_arf_sample(Scene<real> s, ArfArgs p) {
     }
     atomicAdd(&n_head, steps);
     int label = 0;
-    const real ed = ev.esum[0];
+    real ed = ev.esum[0];
     if (ed > R<real>(0)) {
       atomicAdd(&n_singles, 1u);
+      if (s.eblur) ed = blur_energy(s, ed, g);  // the window the digitizer chain reports
 #pragma unroll
       for (int k = 0; k < 8; ++k)
         if (k < s.n_win && ed >= s.wlo[k] && ed < s.whi[k]) label = k + 1;

@@ -421,6 +421,13 @@ struct Scene {
   int mat_coll, mat_cr;
   real wlo[8], whi[8], pix_half[2], inv_psp[2];
   unsigned long long *proj;
+  // digitizer blurring of the singles (GateDigitizerBlurringActor on the energy:
+  // eblur 0 off, 1 Gaussian, 2 inverse square, 3 linear law; and
+  // GateDigitizerSpatialBlurringActor on the crystal position: sblur 0 off,
+  // 1 Gaussian (clamped into the crystal when sb_keep), 2 truncated Gaussian)
+  int eblur, sblur, sb_keep;
+  int centroid;  // adder policy: 0 EnergyWinnerPosition, 1 EnergyWeightedCentroidPosition
+  real eb_sigma, eb_res, eb_ref, eb_slope, sb_sigma[2];
 };
 
 template <typename real>

@@ -712,11 +712,16 @@ __device__ __forceinline__ int flight(const Scene<real> &s, Photon<real> &ph, Rn
   return kRefill;
 }
 
-// The interaction a lane recorded during its last flight.
+// A crystal hit of head H added to the event (GateDigiAdderInVolume::Update,
+// digitizer/GateDigiAdderInVolume.cpp:29-72): energy sum, and either the
+// energy-winner position or (s.centroid) the energy-weighted position sum.
 template <typename real, int H>
 __device__ __forceinline__ void event_add(const Scene<real> &s, Event<real> &ev, const Photon<real> &ph, real ed) {
   ev.esum[H] = ev.esum[H] + ed;
-  if (ed > ev.emax[H]) {
+  if (s.centroid) {
+    ev.wpos[H][0] = ev.wpos[H][0] + ed * ph.pos[0];
+    ev.wpos[H][1] = ev.wpos[H][1] + ed * ph.pos[1];
+  } else if (ed > ev.emax[H]) {
     ev.emax[H] = ed;
     ev.wpos[H][0] = ph.pos[0];
     ev.wpos[H][1] = ph.pos[1];

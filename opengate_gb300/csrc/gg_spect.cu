@@ -182,7 +182,7 @@ __global__ void __launch_bounds__(256, MINB) k_spect_phantom(Scene<real> sg, Ker
         real v[8];
         load_event(in, slot, v);
         event_from(v, ev);
-        n_singles += score_singles(s, ev, ph.run);
+        n_singles += score_singles(s, ev, ph.run, g);
       }
       if (need) in_hist = false;
       const unsigned n_need = __popc(m_ref);
@@ -337,7 +337,7 @@ __global__ void __launch_bounds__(256, MINB) k_spect_head(Scene<real> sg, Kernel
     if (phase == kRefill) {
       const bool need = state == kRefill;
       if (need && in_hist) {
-        n_singles += score_singles(s, ev, ph.run);
+        n_singles += score_singles(s, ev, ph.run, g);
         in_hist = false;
       }
       const unsigned n_need = __popc(m_ref);

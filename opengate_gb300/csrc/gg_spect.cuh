@@ -295,9 +295,171 @@ __device__ __forceinline__ int spect_world_flight(const Scene<real> &s, Photon<r
   return 0;
 }
 
-// Singles of one event: windows and projection pixel per head.
+// Two standard normal deviates from the history's stream (Box & Muller 1958):
+// sqrt(-2 ln u1) (cos, sin)(2 pi u2), u1 in (0, 1].
 template <typename real>
-__device__ __forceinline__ unsigned score_singles(const Scene<real> &s, const Event<real> &ev, int run) {
+__device__ __forceinline__ void normal_pair(Rng &g, real &z0, real &z1) {
+  const real u1 = u01_open0<real>(g);
+  const real u2 = u01<real>(g);
+  real r = gg_log(u1);
+  r = R<real>(-2) * r;
+  r = gg_sqrt(r);
+  real sn, cs;
+  gg_sincos_turn(u2, sn, cs);
+  z0 = r * cs;
+  z1 = r * sn;
+}
+
+// FWHM -> standard deviation, 1 / (2 sqrt(2 ln 2))
+constexpr double kFwhmToSigma = 0.42466090014400953;
+
+// Energy blurring of a single (GateDigitizerBlurringActor::GaussianBlur /
+// InverseSquare / Linear, digitizer/GateDigitizerBlurringActor.cpp:74-97):
+// sigma fixed, or FWHM/E = res sqrt(E_ref) / sqrt(E), or slope (E - E_ref) + res.
+template <typename real>
+__device__ __forceinline__ real blur_energy(const Scene<real> &s, real e, Rng &g) {
+  real sigma;
+  if (s.eblur == 1) {
+    sigma = s.eb_sigma;
+  } else {
+    real v;
+    if (s.eblur == 2) {
+      v = gg_sqrt(s.eb_ref);
+      const real q = gg_sqrt(e);
+      v = v / q;
+      v = s.eb_res * v;
+    } else {
+      v = e - s.eb_ref;
+      v = s.eb_slope * v;
+      v = v + s.eb_res;
+    }
+    sigma = v * e;
+    sigma = sigma * (real)kFwhmToSigma;
+  }
+  real z0, z1;
+  normal_pair(g, z0, z1);
+  const real d = sigma * z0;
+  return e + d;
+}
+
+// erf by Abramowitz & Stegun 7.1.26 (|error| < 1.5e-7), odd extension.
+template <typename real>
+__device__ __forceinline__ real erf_as(real x) {
+  const real ax = x < R<real>(0) ? -x : x;
+  real t = R<real>(0.3275911) * ax;
+  t = R<real>(1) + t;
+  t = R<real>(1) / t;
+  real p = R<real>(1.061405429) * t;
+  p = p + R<real>(-1.453152027);
+  p = p * t;
+  p = p + R<real>(1.421413741);
+  p = p * t;
+  p = p + R<real>(-0.284496736);
+  p = p * t;
+  p = p + R<real>(0.254829592);
+  p = p * t;
+  real x2 = ax * ax;
+  x2 = -x2;
+  real y = p * gg_exp(x2);
+  y = R<real>(1) - y;
+  return x < R<real>(0) ? -y : y;
+}
+
+// Standard deviation of the redraws of a truncated blur
+// (GateDigitizerSpatialBlurringActor::ComputeTruncatedGaussianSigma and
+// ComputeEdgeCorrectedSigma, GateDigitizerSpatialBlurringActor.cpp:158-206).
+template <typename real>
+__device__ __forceinline__ real trunc_sigma(real mu, real sigma, real lo, real hi) {
+  const real inv_sqrt_2pi = R<real>(0.39894228040143267794);
+  const real inv_sqrt2 = R<real>(0.70710678118654752440);
+  real a = lo - mu;
+  a = a / sigma;
+  real b = hi - mu;
+  b = b / sigma;
+  real pa = R<real>(-0.5) * a;
+  pa = pa * a;
+  pa = gg_exp(pa) * inv_sqrt_2pi;
+  real pb = R<real>(-0.5) * b;
+  pb = pb * b;
+  pb = gg_exp(pb) * inv_sqrt_2pi;
+  real fa = erf_as(a * inv_sqrt2);
+  fa = R<real>(1) + fa;
+  fa = R<real>(0.5) * fa;
+  real fb = erf_as(b * inv_sqrt2);
+  fb = R<real>(1) + fb;
+  fb = R<real>(0.5) * fb;
+  const real z = fb - fa;
+  real shift = pa - pb;
+  shift = shift / z;
+  real c = a * pa;
+  c = c - b * pb;
+  c = c / z;
+  real var = R<real>(1) - c;
+  var = var - shift * shift;
+  real s1 = sigma * gg_sqrt(var);
+  real delta = mu - lo;
+  const real dh = hi - mu;
+  delta = dh < delta ? dh : delta;
+  delta = delta > R<real>(0) ? delta : R<real>(0);
+  real dn = delta / s1;
+  dn = dn > R<real>(0.95) ? dn : R<real>(0.95);
+  if (dn < R<real>(4)) {
+    real corr = R<real>(-0.86538264) * dn;
+    corr = R<real>(3.61070188) * gg_exp(corr);
+    s1 = s1 * corr;
+  }
+  return s1;
+}
+
+// Truncated blur of one coordinate: while outside [lo, hi], redraw around mu
+// with the corrected sigma (at most kLoopCap draws, then clamped).
+template <typename real>
+__device__ __forceinline__ real trunc_redraw(real mu, real p, real sigma, real lo, real hi, Rng &g) {
+  if (!(p > hi || p < lo)) return p;
+  const real sg = trunc_sigma(mu, sigma, lo, hi);
+  for (int k = 0; k < kLoopCap; ++k) {
+    real z0, z1;
+    normal_pair(g, z0, z1);
+    p = sg * z0;
+    p = mu + p;
+    if (!(p > hi || p < lo)) return p;
+  }
+  return p < lo ? lo : hi;
+}
+
+// Spatial blurring of a single's crystal position (a1, a2) (GateDigitizerSpatialBlurringActor::
+// BlurCurrentThreeVectorValue, GateDigitizerSpatialBlurringActor.cpp:85-156): the crystal
+// spans |a| <= half_width; keep_in_solid_limits puts points outside just inside the edge.
+template <typename real>
+__device__ __forceinline__ void blur_position(const Scene<real> &s, real &a1, real &a2, Rng &g) {
+  real z0, z1;
+  normal_pair(g, z0, z1);
+  real p0 = s.sb_sigma[0] * z0;
+  p0 = a1 + p0;
+  real p1 = s.sb_sigma[1] * z1;
+  p1 = a2 + p1;
+  const real hi = s.half_w, lo = -s.half_w;
+  if (s.sblur == 2) {
+    p0 = trunc_redraw(a1, p0, s.sb_sigma[0], lo, hi, g);
+    p1 = trunc_redraw(a2, p1, s.sb_sigma[1], lo, hi, g);
+  } else if (s.sb_keep) {
+    // just inside the edge: 1e-6 of the half width (1 nm in the reference,
+    // which FP32 would round back onto the edge)
+    const real tiny = s.half_w * R<real>(1e-6);
+    if (p0 < lo) p0 = lo + tiny;
+    if (p1 < lo) p1 = lo + tiny;
+    if (p0 > hi) p0 = hi - tiny;
+    if (p1 > hi) p1 = hi - tiny;
+  }
+  a1 = p0;
+  a2 = p1;
+}
+
+// Singles of one event: (blurring,) windows and projection pixel per head.
+// Blurring draws come from the history's stream, head 0 before head 1,
+// energy before position.
+template <typename real>
+__device__ __forceinline__ unsigned score_singles(const Scene<real> &s, const Event<real> &ev, int run, Rng &g) {
   unsigned n_singles = 0;
 #pragma unroll
   for (int h = 0; h < 2; ++h) {
@@ -305,9 +467,16 @@ __device__ __forceinline__ unsigned score_singles(const Scene<real> &s, const Ev
     real e = ev.esum[h];
     if (!(e > R<real>(0))) continue;
     ++n_singles;
-    real fx = ev.wpos[h][0] + s.pix_half[0];
+    real a1 = ev.wpos[h][0], a2 = ev.wpos[h][1];
+    if (s.centroid) {  // GateDigiAdderInVolume::Terminate: position sum / energy sum
+      a1 = a1 / e;
+      a2 = a2 / e;
+    }
+    if (s.eblur) e = blur_energy(s, e, g);
+    if (s.sblur) blur_position(s, a1, a2, g);
+    real fx = a1 + s.pix_half[0];
     fx = fx * s.inv_psp[0];
-    real fy = ev.wpos[h][1] + s.pix_half[1];
+    real fy = a2 + s.pix_half[1];
     fy = fy * s.inv_psp[1];
     if (!(fx >= R<real>(0) && fx < (real)s.pnx && fy >= R<real>(0) && fy < (real)s.pny)) continue;
     int i = (int)fx, j = (int)fy;

@@ -210,7 +210,7 @@ __global__ void __launch_bounds__(256, MINB) k_transport(Scene<real> sg, KernelA
     if (phase == kRefill) {
       const bool need = state == kRefill;
       if (need && in_hist) {
-        if constexpr (SPECT) n_singles += score_singles(s, ev, ph.run);
+        if constexpr (SPECT) n_singles += score_singles(s, ev, ph.run, g);
         else hlist_flush(l, t, &bc);
         in_hist = false;
       }

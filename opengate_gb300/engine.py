@@ -121,9 +121,11 @@ class SpectEngine(DoseEngine):
         self._call("gg_set_source", ctypes.byref(s.source_desc))
         self._desc = self.spect.desc()
         self._call("gg_spect_setup", ctypes.byref(self._desc))
+        self._call("gg_spect_set_blur", ctypes.byref(self.spect.blur))
 
     def reset(self):
         self._call("gg_spect_setup", ctypes.byref(self._desc))
+        self._call("gg_spect_set_blur", ctypes.byref(self.spect.blur))
 
     def run(self, n_per_run, seed, first=0):
         """All gantry positions in one gg_spect_run call (one set of launches)."""

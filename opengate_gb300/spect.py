@@ -66,6 +66,31 @@ class SpectSpec:
         self.crystal_material = int(crystal_material)
         # start angle of each head (default: evenly spread from start_angle_deg)
         self.head_start = None if head_start_deg is None else [math.radians(a) for a in head_start_deg]
+        # digitizer: adder policy of the singles' position, blurring (off by default)
+        self.adder_policy = "EnergyWinnerPosition"
+        self.blur = C.BlurDesc()
+
+    def set_energy_blur(self, method, sigma=0.0, resolution=0.0, reference=0.0, slope=0.0):
+        """DigitizerBlurringActor on the singles' energy (MeV): method "Gaussian" (sigma),
+        "InverseSquare" (resolution = FWHM/E at reference) or "Linear" (+ slope per MeV)."""
+        kinds = {"Gaussian": C.GG_BLUR_GAUSSIAN, "InverseSquare": C.GG_BLUR_INVERSE_SQUARE,
+                 "Linear": C.GG_BLUR_LINEAR}
+        if method not in kinds:
+            raise ValueError(f"blur_method must be one of {tuple(kinds)}, not {method!r}")
+        self.blur.energy_method = kinds[method]
+        self.blur.energy_sigma = float(sigma)
+        self.blur.energy_resolution = float(resolution)
+        self.blur.energy_reference = float(reference)
+        self.blur.energy_slope = float(slope)
+
+    def set_spatial_blur(self, sigma, keep_in_solid_limits=True, truncated=False):
+        """DigitizerSpatialBlurringActor on the crystal position: sigma (mm) along the
+        projection axes (a scalar for both)."""
+        sg = [float(sigma)] * 2 if not hasattr(sigma, "__len__") else [float(v) for v in list(sigma)[:2]]
+        self.blur.spatial = 1
+        self.blur.spatial_sigma[0], self.blur.spatial_sigma[1] = sg
+        self.blur.keep_in_solid_limits = int(bool(keep_in_solid_limits))
+        self.blur.truncated = int(bool(truncated))
 
     @property
     def n_windows(self):
@@ -90,6 +115,9 @@ class SpectSpec:
         d.spacing[:] = self.spacing
         d.n_heads = self.n_heads
         d.n_runs = self.n_runs
+        if self.adder_policy not in C.ADDER_POLICIES:
+            raise NotImplementedError(f"adder policy '{self.adder_policy}'")
+        d.adder_policy = C.ADDER_POLICIES[self.adder_policy]
         return d
 
     def angle(self, run, head):

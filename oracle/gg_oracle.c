@@ -417,6 +417,11 @@ typedef struct {
   int mat_coll, mat_cr;
   real wlo[8], whi[8], pix_half[2], inv_psp[2];
   uint64_t *proj; /* [head][run][window][pny][pnx], shared, atomics */
+  /* digitizer blurring (gg_blur_desc): eblur 0 off / 1 Gaussian / 2 inverse
+     square / 3 linear; sblur 0 off / 1 Gaussian (+ clamp) / 2 truncated */
+  int eblur, sblur, sb_keep;
+  int centroid; /* adder policy EnergyWeightedCentroidPosition */
+  real eb_sigma, eb_res, eb_ref, eb_slope, sb_sigma[2];
   const struct arf_s *arf; /* ARF detector model, or NULL */
 } scene_t;
 
@@ -1086,7 +1091,10 @@ static void head_step(const scene_t *s, photon_t *ph, rng_t *g, tally_t *t, even
   if (ph->hreg == 2 && ed > R(0)) {
     int h = ph->head;
     ev->esum[h] = ev->esum[h] + ed;
-    if (ed > ev->emax[h]) {
+    if (s->centroid) { /* EnergyWeightedCentroidPosition */
+      ev->wpos[h][0] = ev->wpos[h][0] + ed * l[0];
+      ev->wpos[h][1] = ev->wpos[h][1] + ed * l[1];
+    } else if (ed > ev->emax[h]) {
       ev->emax[h] = ed;
       ev->wpos[h][0] = l[0];
       ev->wpos[h][1] = l[1];
@@ -1258,14 +1266,165 @@ static void spect_world_step(const scene_t *s, photon_t *ph, rng_t *g, tally_t *
 }
 
 /* Singles of one event: energy windows and projection pixel per head. */
-static void score_singles(const scene_t *s, const event_t *ev, tally_t *t) {
+/* two standard normal deviates (Box & Muller 1958): sqrt(-2 ln u1) (cos, sin)(2 pi u2) */
+static void normal_pair(rng_t *g, real *z0, real *z1) {
+  const real u1 = u01_open0(g);
+  const real u2 = u01(g);
+  real r = ggo_log(u1);
+  r = R(-2) * r;
+  r = ggo_sqrt(r);
+  real sn, cs;
+  ggo_sincos_turn(u2, &sn, &cs);
+  *z0 = r * cs;
+  *z1 = r * sn;
+}
+
+#define FWHM_TO_SIGMA 0.42466090014400953
+
+/* energy blurring of a single (GateDigitizerBlurringActor.cpp:74-97) */
+static real blur_energy(const scene_t *s, real e, rng_t *g) {
+  real sigma;
+  if (s->eblur == 1) {
+    sigma = s->eb_sigma;
+  } else {
+    real v;
+    if (s->eblur == 2) {
+      v = ggo_sqrt(s->eb_ref);
+      const real q = ggo_sqrt(e);
+      v = v / q;
+      v = s->eb_res * v;
+    } else {
+      v = e - s->eb_ref;
+      v = s->eb_slope * v;
+      v = v + s->eb_res;
+    }
+    sigma = v * e;
+    sigma = sigma * (real)FWHM_TO_SIGMA;
+  }
+  real z0, z1;
+  normal_pair(g, &z0, &z1);
+  const real d = sigma * z0;
+  return e + d;
+}
+
+/* erf by Abramowitz & Stegun 7.1.26, odd extension */
+static real erf_as(real x) {
+  const real ax = x < R(0) ? -x : x;
+  real t = R(0.3275911) * ax;
+  t = R(1) + t;
+  t = R(1) / t;
+  real p = R(1.061405429) * t;
+  p = p + R(-1.453152027);
+  p = p * t;
+  p = p + R(1.421413741);
+  p = p * t;
+  p = p + R(-0.284496736);
+  p = p * t;
+  p = p + R(0.254829592);
+  p = p * t;
+  real x2 = ax * ax;
+  x2 = -x2;
+  real y = p * ggo_exp(x2);
+  y = R(1) - y;
+  return x < R(0) ? -y : y;
+}
+
+/* redraw sigma of a truncated blur (GateDigitizerSpatialBlurringActor.cpp:158-206) */
+static real trunc_sigma(real mu, real sigma, real lo, real hi) {
+  const real inv_sqrt_2pi = R(0.39894228040143267794);
+  const real inv_sqrt2 = R(0.70710678118654752440);
+  real a = lo - mu;
+  a = a / sigma;
+  real b = hi - mu;
+  b = b / sigma;
+  real pa = R(-0.5) * a;
+  pa = pa * a;
+  pa = ggo_exp(pa) * inv_sqrt_2pi;
+  real pb = R(-0.5) * b;
+  pb = pb * b;
+  pb = ggo_exp(pb) * inv_sqrt_2pi;
+  real fa = erf_as(a * inv_sqrt2);
+  fa = R(1) + fa;
+  fa = R(0.5) * fa;
+  real fb = erf_as(b * inv_sqrt2);
+  fb = R(1) + fb;
+  fb = R(0.5) * fb;
+  const real z = fb - fa;
+  real shift = pa - pb;
+  shift = shift / z;
+  real c = a * pa;
+  c = c - b * pb;
+  c = c / z;
+  real var = R(1) - c;
+  var = var - shift * shift;
+  real s1 = sigma * ggo_sqrt(var);
+  real delta = mu - lo;
+  const real dh = hi - mu;
+  delta = dh < delta ? dh : delta;
+  delta = delta > R(0) ? delta : R(0);
+  real dn = delta / s1;
+  dn = dn > R(0.95) ? dn : R(0.95);
+  if (dn < R(4)) {
+    real corr = R(-0.86538264) * dn;
+    corr = R(3.61070188) * ggo_exp(corr);
+    s1 = s1 * corr;
+  }
+  return s1;
+}
+
+static real trunc_redraw(real mu, real p, real sigma, real lo, real hi, rng_t *g) {
+  if (!(p > hi || p < lo)) return p;
+  const real sg = trunc_sigma(mu, sigma, lo, hi);
+  for (int k = 0; k < LOOP_CAP; ++k) {
+    real z0, z1;
+    normal_pair(g, &z0, &z1);
+    p = sg * z0;
+    p = mu + p;
+    if (!(p > hi || p < lo)) return p;
+  }
+  return p < lo ? lo : hi;
+}
+
+/* spatial blurring of the crystal position (GateDigitizerSpatialBlurringActor.cpp:85-156) */
+static void blur_position(const scene_t *s, real *a1, real *a2, rng_t *g) {
+  real z0, z1;
+  normal_pair(g, &z0, &z1);
+  real p0 = s->sb_sigma[0] * z0;
+  p0 = *a1 + p0;
+  real p1 = s->sb_sigma[1] * z1;
+  p1 = *a2 + p1;
+  const real hi = s->half_w, lo = -s->half_w;
+  if (s->sblur == 2) {
+    p0 = trunc_redraw(*a1, p0, s->sb_sigma[0], lo, hi, g);
+    p1 = trunc_redraw(*a2, p1, s->sb_sigma[1], lo, hi, g);
+  } else if (s->sb_keep) {
+    const real tiny = s->half_w * R(1e-6); /* just inside (FP32 keeps it inside) */
+    if (p0 < lo) p0 = lo + tiny;
+    if (p1 < lo) p1 = lo + tiny;
+    if (p0 > hi) p0 = hi - tiny;
+    if (p1 > hi) p1 = hi - tiny;
+  }
+  *a1 = p0;
+  *a2 = p1;
+}
+
+/* singles of one event: (blurring: head 0 before head 1, energy before
+   position, from the history's stream,) windows and projection pixel */
+static void score_singles(const scene_t *s, const event_t *ev, tally_t *t, rng_t *g) {
   for (int h = 0; h < s->n_heads; ++h) {
     real e = ev->esum[h];
     if (!(e > R(0))) continue;
     t->cnt[GG_CNT_SINGLES]++;
-    real fx = ev->wpos[h][0] + s->pix_half[0];
+    real a1 = ev->wpos[h][0], a2 = ev->wpos[h][1];
+    if (s->centroid) {
+      a1 = a1 / e;
+      a2 = a2 / e;
+    }
+    if (s->eblur) e = blur_energy(s, e, g);
+    if (s->sblur) blur_position(s, &a1, &a2, g);
+    real fx = a1 + s->pix_half[0];
     fx = fx * s->inv_psp[0];
-    real fy = ev->wpos[h][1] + s->pix_half[1];
+    real fy = a2 + s->pix_half[1];
     fy = fy * s->inv_psp[1];
     if (!(fx >= R(0) && fx < (real)s->pnx && fy >= R(0) && fy < (real)s->pny)) continue;
     int i = (int)fx, j = (int)fy;
@@ -1471,7 +1630,7 @@ static int run_history(const scene_t *s, uint64_t seed, uint64_t h, tally_t *t) 
     has_sec = 0;
     start_photon(s, &ph);
   }
-  if (s->spect) score_singles(s, &ev, t);
+  if (s->spect) score_singles(s, &ev, t, &g);
   else hlist_flush(&l, t);
   return GG_OK;
 }
@@ -1559,8 +1718,56 @@ static int scene_init(scene_t *s, const gg_tables_desc *tb, const gg_volume_desc
   return GG_OK;
 }
 
+/* n blurred singles of one event (energy e, crystal point a1, a2) on a crystal
+   of half width half_w, sample i on the stream of history i (tests) */
+void GGO_PREFIX(sample_blur)(const gg_blur_desc *b, double half_w, double e, double a1, double a2, uint64_t n,
+                             uint64_t seed, double *out_e, double *out_a1, double *out_a2) {
+  scene_t s;
+  memset(&s, 0, sizeof(s));
+  s.half_w = (real)half_w;
+  s.eblur = b->energy_method;
+  s.eb_sigma = (real)b->energy_sigma;
+  s.eb_res = (real)b->energy_resolution;
+  s.eb_ref = (real)b->energy_reference;
+  s.eb_slope = (real)b->energy_slope;
+  s.sblur = b->spatial ? (b->truncated ? 2 : 1) : 0;
+  s.sb_keep = b->keep_in_solid_limits;
+  s.sb_sigma[0] = (real)b->spatial_sigma[0];
+  s.sb_sigma[1] = (real)b->spatial_sigma[1];
+  for (uint64_t i = 0; i < n; ++i) {
+    rng_t g;
+    rng_init(&g, seed, i, 0u);
+    real ee = (real)e, p = (real)a1, q = (real)a2;
+    if (s.eblur) ee = blur_energy(&s, ee, &g);
+    if (s.sblur) blur_position(&s, &p, &q, &g);
+    out_e[i] = (double)ee;
+    out_a1[i] = (double)p;
+    out_a2[i] = (double)q;
+  }
+}
+
+double GGO_PREFIX(erf)(double x) { return (double)erf_as((real)x); }
+
+/* digitizer blurring of the following SPECT runs (set_blur) */
+static gg_blur_desc g_blur;
+
+void GGO_PREFIX(set_blur)(const gg_blur_desc *b) {
+  if (b) g_blur = *b;
+  else memset(&g_blur, 0, sizeof(g_blur));
+}
+
 static void spect_init(scene_t *s, const gg_spect_desc *sp) {
   s->spect = 1;
+  s->centroid = sp->adder_policy == GG_ADDER_CENTROID;
+  s->eblur = g_blur.energy_method;
+  s->eb_sigma = (real)g_blur.energy_sigma;
+  s->eb_res = (real)g_blur.energy_resolution;
+  s->eb_ref = (real)g_blur.energy_reference;
+  s->eb_slope = (real)g_blur.energy_slope;
+  s->sblur = g_blur.spatial ? (g_blur.truncated ? 2 : 1) : 0;
+  s->sb_keep = g_blur.keep_in_solid_limits;
+  s->sb_sigma[0] = (real)g_blur.spatial_sigma[0];
+  s->sb_sigma[1] = (real)g_blur.spatial_sigma[1];
   s->n_heads = sp->n_heads;
   s->n_runs = sp->n_runs;
   s->n_win = sp->n_windows;
@@ -1813,6 +2020,7 @@ static int arf_sample(const scene_t *s, const gg_arf_sampling *a, uint64_t seed,
   real ed = ev.esum[0];
   if (ed > R(0)) {
     t->cnt[GG_CNT_SINGLES]++;
+    if (s->eblur) ed = blur_energy(s, ed, &g); /* the window the digitizer chain reports */
     for (int k = 0; k < s->n_win; ++k)
       if (ed >= s->wlo[k] && ed < s->whi[k]) label = k + 1;
   }

@@ -155,6 +155,35 @@ def first_flight(scene, n, seed=1, precision=32):
     return int(out[0]), int(out[1])
 
 
+def _with_blur(L, precision, spect, call):
+    """Runs call() with the SPECT set-up's digitizer blurring installed in the oracle."""
+    f = getattr(L, f"ggo{precision}_set_blur")
+    f.argtypes = [ctypes.POINTER(C.BlurDesc)]
+    f(ctypes.byref(getattr(spect, "blur", C.BlurDesc())))
+    try:
+        return call()
+    finally:
+        f(None)
+
+
+def sample_blur(blur, half_w, e, a1, a2, n, seed=1, precision=32):
+    """n blurred singles of one event: (energies, a1, a2) float64 arrays."""
+    L = lib(precision)
+    f = getattr(L, f"ggo{precision}_sample_blur")
+    f.argtypes = [ctypes.POINTER(C.BlurDesc), ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                  ctypes.c_uint64, ctypes.c_uint64] + [ctypes.POINTER(ctypes.c_double)] * 3
+    out = [np.empty(n) for _ in range(3)]
+    f(ctypes.byref(blur), half_w, e, a1, a2, n, seed, *(C.ptr(o, ctypes.c_double) for o in out))
+    return tuple(out)
+
+
+def erf(x, precision=32):
+    f = getattr(lib(precision), f"ggo{precision}_erf")
+    f.restype = ctypes.c_double
+    f.argtypes = [ctypes.c_double]
+    return f(float(x))
+
+
 def run_spect(scene, spect, n_per_run, seed, first=0, threads=1, precision=32):
     """Oracle SPECT run: (projection counts [head][run*window][y][x] float64, counters)."""
     L = lib(precision)
@@ -169,8 +198,9 @@ def run_spect(scene, spect, n_per_run, seed, first=0, threads=1, precision=32):
     cnt = np.zeros(C.GG_N_COUNTERS, dtype=np.uint64)
     desc = spect.desc()
     frames = spect.all_frames()
-    st = fn(*_descs(scene), ctypes.byref(desc), C.ptr(frames, ctypes.c_double), seed, first, n_per_run, threads,
-            C.ptr(proj, ctypes.c_uint64), C.ptr(cnt, ctypes.c_uint64))
+    st = _with_blur(L, precision, spect, lambda: fn(
+        *_descs(scene), ctypes.byref(desc), C.ptr(frames, ctypes.c_double), seed, first, n_per_run, threads,
+        C.ptr(proj, ctypes.c_uint64), C.ptr(cnt, ctypes.c_uint64)))
     if st != 0:
         raise RuntimeError(f"oracle SPECT run failed with status {st}")
     return proj.astype(np.float64).reshape(shape), {name: int(cnt[i]) for i, name in enumerate(C.COUNTER_NAMES)}
@@ -209,8 +239,9 @@ def arf_dataset(tables_desc, spect, sampling, n, seed, first=0, threads=8, preci
     m = ctypes.c_uint64()
     cnt = np.zeros(C.GG_N_COUNTERS, dtype=np.uint64)
     desc = spect.desc()
-    st = fn(ctypes.byref(tables_desc), ctypes.byref(desc), ctypes.byref(sampling), seed, first, n, threads,
-            C.ptr(rows, ctypes.c_float), ctypes.byref(m), C.ptr(cnt, ctypes.c_uint64))
+    st = _with_blur(L, precision, spect, lambda: fn(
+        ctypes.byref(tables_desc), ctypes.byref(desc), ctypes.byref(sampling), seed, first, n, threads,
+        C.ptr(rows, ctypes.c_float), ctypes.byref(m), C.ptr(cnt, ctypes.c_uint64)))
     if st != 0:
         raise RuntimeError(f"oracle ARF dataset failed with status {st}")
     return rows[: m.value].copy(), {name: int(cnt[i]) for i, name in enumerate(C.COUNTER_NAMES)}
@@ -235,9 +266,10 @@ def run_spect_arf(scene, spect, n_per_run, seed, model, params, first=0, threads
     desc = spect.desc()
     frames = spect.all_frames()
     params = np.ascontiguousarray(params, dtype=np.float32)
-    st = fn(*_descs(scene), ctypes.byref(desc), C.ptr(frames, ctypes.c_double), seed, first, n_per_run, threads,
-            C.ptr(proj, ctypes.c_uint64), C.ptr(cnt, ctypes.c_uint64), ctypes.byref(model),
-            C.ptr(params, ctypes.c_float), C.ptr(aproj, ctypes.c_uint64), C.ptr(aproj2, ctypes.c_uint64))
+    st = _with_blur(L, precision, spect, lambda: fn(
+        *_descs(scene), ctypes.byref(desc), C.ptr(frames, ctypes.c_double), seed, first, n_per_run, threads,
+        C.ptr(proj, ctypes.c_uint64), C.ptr(cnt, ctypes.c_uint64), ctypes.byref(model),
+        C.ptr(params, ctypes.c_float), C.ptr(aproj, ctypes.c_uint64), C.ptr(aproj2, ctypes.c_uint64)))
     if st != 0:
         raise RuntimeError(f"oracle SPECT ARF run failed with status {st}")
     arf = aproj.astype(np.float64) * 2.0 ** -32

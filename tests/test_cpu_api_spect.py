@@ -135,3 +135,47 @@ def test_spect_setup_from_the_helpers(tmp_path):
     np.testing.assert_allclose(spec.vox_corner, [-96.0, -96.0, -60.0])
     assert head_of == {"spect0_crystal": 0, "spect1_crystal": 1}
     assert len(scene.pt.mat_rho) >= 4 and sp.collimator_material != sp.crystal_material
+
+
+def test_digitizer_chain_sets_blur_and_adder(tmp_path):
+    from opengate_gb300 import _capi as C
+    from opengate_gb300.contrib.spect import siemens_intevo as intevo
+
+    sim, _ = spect_sim(tmp_path)
+    _, sp, _, _, _ = sim.build_spect()
+    # the NM670 chain: energy winner, 6.3 % FWHM at 140.57 keV, 3 mm FWHM kept in the crystal
+    assert sp.adder_policy == "EnergyWinnerPosition"
+    assert sp.blur.energy_method == C.GG_BLUR_INVERSE_SQUARE
+    assert sp.blur.energy_resolution == pytest.approx(0.063) and sp.blur.energy_reference == pytest.approx(0.14057)
+    assert sp.blur.spatial == 1 and sp.blur.keep_in_solid_limits == 1 and sp.blur.truncated == 0
+    assert sp.blur.spatial_sigma[0] == pytest.approx(3.0 / 2.3548200450309493)
+    # the Intevo chain: centroid adder, 9.9 % at 140.5 keV, 3.6 mm
+    sim2 = gate.Simulation()
+    sim2.output_dir = tmp_path
+    head, _, crystal = intevo.add_spect_head(sim2, "intevo", "melp")
+    intevo.add_digitizer(sim2, crystal.name)
+    actors = {a.type_name for a in sim2.actors.values()}
+    assert {"DigitizerAdderActor", "DigitizerBlurringActor", "DigitizerSpatialBlurringActor",
+            "DigitizerProjectionActor"} <= actors
+    adder = [a for a in sim2.actors.values() if a.type_name == "DigitizerAdderActor"][0]
+    assert adder.adder_policy() == "EnergyWeightedCentroidPosition"
+    eb = [a for a in sim2.actors.values() if a.type_name == "DigitizerBlurringActor"][0]
+    assert eb.energy_blur() == dict(method="InverseSquare", resolution=0.099, reference=pytest.approx(0.1405),
+                                    slope=0.0)
+    sb = [a for a in sim2.actors.values() if a.type_name == "DigitizerSpatialBlurringActor"][0]
+    assert sb.spatial_blur()["sigma"][0] == pytest.approx(3.6 / 2.3548200450309493)
+
+
+def test_blur_actor_validation():
+    b = gate.Simulation().add_actor("DigitizerBlurringActor", "eb")
+    b.blur_attribute = "TotalEnergyDeposit"
+    with pytest.raises(ValueError):
+        b.energy_blur()  # Gaussian without sigma or fwhm
+    b.blur_fwhm = 0.01
+    assert b.energy_blur()["sigma"] == pytest.approx(0.01 / 2.3548200450309493)
+    b.blur_sigma = 0.002
+    with pytest.raises(ValueError):
+        b.energy_blur()  # both
+    b.blur_attribute = "GlobalTime"
+    with pytest.raises(NotImplementedError):
+        b.energy_blur()

@@ -56,6 +56,19 @@ def test_training_rows_match_oracle():
     np.testing.assert_allclose(rows[:, 2], ref[:, 2], rtol=0, atol=2e-4)
 
 
+def test_training_rows_with_energy_blur_match_oracle():
+    """Rows take the window of the blurred crystal energy, as the digitizer chain reports it."""
+    scene, sp, a = _arf_case()
+    sp.set_energy_blur("InverseSquare", resolution=0.063, reference=0.14057)
+    eng, net = _engine(scene, sp)
+    with eng:
+        rows = net.dataset(a, 200_000, seed=9, first=0)
+    ref, _ = O.arf_dataset(scene.tables_desc, sp, a, 200_000, seed=9, first=0, threads=8)
+    assert rows.shape == ref.shape and len(rows) > 1000
+    np.testing.assert_array_equal(rows[:, 0], ref[:, 0])
+    np.testing.assert_array_equal(rows[:, 3], ref[:, 3])
+
+
 def _rows(n, n_classes, seed):
     rng = np.random.default_rng(seed)
     return np.stack([rng.uniform(0.05, 0.25, n), rng.uniform(0, 30, n), rng.uniform(-180, 180, n),
