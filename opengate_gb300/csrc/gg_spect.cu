@@ -31,8 +31,9 @@
 
 namespace gg {
 
-// Phantom-stage flight: Woodcock step in the image or one world step; a photon
-// whose world step ends at a head-box entry leaves the stage (kPush).
+// Phantom-stage flight: Woodcock step in the image (followed, when it leaves
+// the image box, by the world step) or one world step; a photon whose world
+// step ends at a head-box entry leaves the stage (kPush).
 template <typename real>
 __device__ __forceinline__ int phantom_flight(const Scene<real> &s, Photon<real> &ph, Rng &g, BlockCounters *bc,
                                               int &pmat, uint32_t &pv, int &pscored, unsigned int &n_wood,
@@ -42,7 +43,17 @@ __device__ __forceinline__ int phantom_flight(const Scene<real> &s, Photon<real>
     ph.alive = 0;
     return kRefill;
   }
-  if (ph.in_image) return image_flight(s, ph, g, pmat, pv, pscored, n_wood, n_real);
+  if (ph.in_image) {
+    const int r = image_flight(s, ph, g, pmat, pv, pscored, n_wood, n_real);
+    if (r != kFly || ph.in_image) return r;
+    // left the image box: the world step follows in the same iteration (same
+    // flight count and draws as a separate phase)
+    if (++ph.steps > kStepCap) {
+      atomicAdd(&bc->loop_capped, 1u);
+      ph.alive = 0;
+      return kRefill;
+    }
+  }
   ++n_world;
   if (spect_world_flight(s, ph, g)) {
     pmat = s.world_mat;
