@@ -106,12 +106,61 @@ struct Rng {
   }
 };
 
-template <typename real>
-__device__ __forceinline__ real u01(Rng &g) {
+// The same stream with the next block computed ahead (the source stage: both
+// first blocks of a history are generated while the warp is converged, so the
+// divergent sampling loops draw without calling the generator).  State saved
+// as (blk, idx, buf) is that of an Rng at the same point of the stream.
+struct RngAhead : Rng {
+  uint32_t nxt[4];
+  bool ahead;
+
+  // blocks 0 and 1 of the history: block 0 in buf, block 1 ahead
+  __device__ __forceinline__ void start(uint64_t seed, uint64_t history, uint32_t s) {
+    init(seed, history, s);
+    const uint4 b0 = philox_block(0u, stream, h0, h1, k0, k1);
+    const uint4 b1 = philox_block(1u, stream, h0, h1, k0, k1);
+    buf[0] = b0.x;
+    buf[1] = b0.y;
+    buf[2] = b0.z;
+    buf[3] = b0.w;
+    nxt[0] = b1.x;
+    nxt[1] = b1.y;
+    nxt[2] = b1.z;
+    nxt[3] = b1.w;
+    blk = 1u;
+    idx = 0;
+    ahead = true;
+  }
+  __device__ __forceinline__ uint32_t next() {
+    if (idx == 4) {
+      if (ahead) {
+        buf[0] = nxt[0];
+        buf[1] = nxt[1];
+        buf[2] = nxt[2];
+        buf[3] = nxt[3];
+        ahead = false;
+      } else {
+        const uint4 b = philox_block(blk, stream, h0, h1, k0, k1);
+        buf[0] = b.x;
+        buf[1] = b.y;
+        buf[2] = b.z;
+        buf[3] = b.w;
+      }
+      blk += 1u;
+      idx = 0;
+    }
+    uint32_t v = idx == 0 ? buf[0] : (idx == 1 ? buf[1] : (idx == 2 ? buf[2] : buf[3]));
+    ++idx;
+    return v;
+  }
+};
+
+template <typename real, typename G>
+__device__ __forceinline__ real u01(G &g) {
   return (real)(g.next() >> 8) * R<real>(5.9604644775390625e-08);
 }
-template <typename real>
-__device__ __forceinline__ real u01_open0(Rng &g) {
+template <typename real, typename G>
+__device__ __forceinline__ real u01_open0(G &g) {
   return (real)((g.next() >> 8) + 1u) * R<real>(5.9604644775390625e-08);
 }
 

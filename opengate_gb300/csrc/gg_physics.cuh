@@ -272,8 +272,8 @@ __device__ __forceinline__ void rot_apply(const real m[9], const real v[3], real
   }
 }
 
-template <typename real>
-__device__ __forceinline__ void sample_direction(const Scene<real> &s, const real p[3], Rng &g, real d[3]) {
+template <typename real, typename G>
+__device__ __forceinline__ void sample_direction(const Scene<real> &s, const real p[3], G &g, real d[3]) {
   if (s.dir_type == GG_DIR_ISO) {
     real u = u01<real>(g);
     real cost = s.s_cos_tmin - s.s_cos_tmax;
@@ -321,8 +321,8 @@ __device__ __forceinline__ bool accept_dir(const Scene<real> &s, const real p[3]
 // GateGenericSource::GeneratePrimaries order: position, direction (with the
 // acceptance loop of GateSingleParticleSource::GenerateDirectionWithAA),
 // energy.
-template <typename real>
-__device__ __forceinline__ int sample_primary(const Scene<real> &s, Rng &g, Photon<real> &ph, BlockCounters *bc) {
+template <typename real, typename G>
+__device__ __forceinline__ int sample_primary(const Scene<real> &s, G &g, Photon<real> &ph, BlockCounters *bc) {
   real loc[3] = {R<real>(0), R<real>(0), R<real>(0)};
   int pt = s.pos_type;
   if (pt == GG_POS_BOX) {

@@ -43,17 +43,14 @@ namespace gg {
 template <typename real, bool MULTI>
 __global__ void __launch_bounds__(256) k_generate(Scene<real> s, KernelArgs a) {
   __shared__ BlockCounters bc;
-  __shared__ unsigned int n_world;
-  if (threadIdx.x == 0) {
-    bc = BlockCounters{0, 0, 0, 0, 0, 0, 0, 0};
-    n_world = 0;
-  }
+  if (threadIdx.x == 0) bc = BlockCounters{0, 0, 0, 0, 0, 0, 0, 0};
   __syncthreads();
   const uint64_t n = a.h_end - a.h_begin;
   const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  bool sampled = false, world_step = false;  // counted per block below
   if (i < n) {
     Records<real> rec = Records<real>::carve(a.records, a.rec_cap);
-    Rng g;
+    RngAhead g;
     uint32_t sim = 0;
     if constexpr (MULTI) {
       const uint64_t h = a.h_begin + i;
@@ -61,9 +58,9 @@ __global__ void __launch_bounds__(256) k_generate(Scene<real> s, KernelArgs a) {
       const SimDesc<real> &d = s.sims[sim];
       bind_geometry(s, d, s.labels, s.sim_maj + (size_t)sim * s.n_e);
       bind_source(s, d);
-      g.init(d.seed, h - d.h_begin, 0u);
+      g.start(d.seed, h - d.h_begin, 0u);
     } else {
-      g.init(a.seed, a.h_begin + i, 0u);
+      g.start(a.seed, a.h_begin + i, 0u);
     }
     Photon<real> ph;
     uint32_t state = kRecDead, steps = 0;
@@ -71,7 +68,7 @@ __global__ void __launch_bounds__(256) k_generate(Scene<real> s, KernelArgs a) {
     if (st != GG_OK) {
       atomicOr(a.status, (unsigned int)st);
     } else {
-      atomicAdd(&bc.histories, 1u);
+      sampled = true;
       start_photon(s, ph);
       if (ph.in_image) {
         state = kRecInImage;
@@ -79,7 +76,7 @@ __global__ void __launch_bounds__(256) k_generate(Scene<real> s, KernelArgs a) {
         state = kRecWorld;  // the world step also targets the heads: left to the transport stage
       } else {
         steps = 1;
-        atomicAdd(&n_world, 1u);
+        world_step = true;
         real inf = gg_inf(real(0));
         real tin = ph.can_enter ? entry_distance(ph.pos, ph.dir, s.bmin, s.bmax) : inf;
         real wlo[3] = {-s.whalf[0], -s.whalf[1], -s.whalf[2]};
@@ -115,10 +112,11 @@ __global__ void __launch_bounds__(256) k_generate(Scene<real> s, KernelArgs a) {
     rec.rng_buf[i] = make_uint4(g.buf[0], g.buf[1], g.buf[2], g.buf[3]);
     rec.sim[i] = sim;
   }
-  __syncthreads();
+  const int n_hist = __syncthreads_count(sampled);
+  const int n_world = __syncthreads_count(world_step);
   if (threadIdx.x == 0) {
     unsigned long long *cnt = a.counters;
-    if (bc.histories) atomicAdd(&cnt[GG_CNT_HISTORIES], (unsigned long long)bc.histories);
+    if (n_hist) atomicAdd(&cnt[GG_CNT_HISTORIES], (unsigned long long)n_hist);
     if (bc.skipped) atomicAdd(&cnt[GG_CNT_SKIPPED], (unsigned long long)bc.skipped);
     if (bc.escaped) atomicAdd(&cnt[GG_CNT_ESCAPED], (unsigned long long)bc.escaped);
     if (bc.loop_capped) atomicAdd(&cnt[GG_CNT_LOOP_CAPPED], (unsigned long long)bc.loop_capped);
