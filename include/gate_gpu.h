@@ -26,6 +26,7 @@
  *                               (core/opengate_core/opengate_lib/GateSPSVoxelsPosDistribution.cpp:29-74)
  *   gg_add_dose_tally           GateDoseActor::InitializeCpp / BeginOfRunAction
  *                               (core/opengate_core/opengate_lib/GateDoseActor.cpp:100-137)
+ *   gg_spect_set_free_flight    GateGammaFreeFlightOptrActor (biasing/GateGammaFreeFlightOptn.cpp:34-83)
  *   gg_spect_set_blur           GateDigitizerBlurringActor / GateDigitizerSpatialBlurringActor
  *                               (core/opengate_core/opengate_lib/digitizer/*BlurringActor.cpp)
  *   gg_set_tle                  GateTLEDoseActor (track-length estimator)
@@ -332,6 +333,25 @@ typedef struct {
   int32_t truncated;            /* redraw outside the crystal (truncated Gaussian) */
 } gg_blur_desc;
 int gg_spect_set_blur(gg_ctx *ctx, const gg_blur_desc *blur);
+
+/* Free flight outside the heads (replaces GammaFreeFlightActor attached to the
+   world with the heads as exclude_volumes: biasing/GateGammaFreeFlightOptn.cpp:34-83,
+   GateGammaFreeFlightOptrActor.cpp, GateVBiasOptrActor.cpp:85-92,
+   opengate/actors/biasingactors.py:247-300; the primary simulation of
+   contrib/spect/spect_config.py:937-970).  Outside the heads photons do not
+   interact: each flies straight to the nearest head entry and its weight is
+   multiplied by exp(-optical depth) of the path (image voxels and world
+   material); photons whose line misses every head stop, and so do photons
+   at or below the energy or weight cutoff.  Inside the heads transport is
+   analog.  Singles add their weight (and its history-by-history square)
+   to the weighted projection read with gg_get_arf_projection; the counts of
+   gg_get_projection stay zero.  Not together with the ARF detector. */
+typedef struct {
+  int32_t enabled;
+  double weight_cutoff; /* photons with weight <= this stop (reference default -1) */
+  double energy_cutoff; /* MeV, photons with energy <= this stop (reference default 0) */
+} gg_ff_desc;
+int gg_spect_set_free_flight(gg_ctx *ctx, const gg_ff_desc *ff);
 int gg_spect_set_heads(gg_ctx *ctx, int32_t run, const double *frames);
 int gg_spect_run(gg_ctx *ctx, uint64_t n_per_run, uint64_t seed, uint64_t first, const double *frames);
 int gg_get_projection(gg_ctx *ctx, double *out, size_t n);

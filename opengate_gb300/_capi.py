@@ -63,6 +63,10 @@ class BlurDesc(ctypes.Structure):
     ]
 
 
+class FfDesc(ctypes.Structure):
+    _fields_ = [("enabled", ctypes.c_int32), ("weight_cutoff", ctypes.c_double), ("energy_cutoff", ctypes.c_double)]
+
+
 class TleDesc(ctypes.Structure):
     _fields_ = [
         ("enabled", ctypes.c_int32), ("threshold_energy", ctypes.c_double), ("energy_min", ctypes.c_double),
@@ -199,6 +203,7 @@ PROTOTYPES = [
      [ctypes.c_void_p, _f64p, _f64p, _f64p, ctypes.POINTER(ctypes.c_int32)]),
     ("gg_spect_setup", ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(SpectDesc)]),
     ("gg_spect_set_blur", ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(BlurDesc)]),
+    ("gg_spect_set_free_flight", ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(FfDesc)]),
     ("gg_spect_set_heads", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, _f64p]),
     ("gg_spect_run", ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64, _f64p]),
     ("gg_get_projection", ctypes.c_int, [ctypes.c_void_p, _f64p, ctypes.c_size_t]),

@@ -545,6 +545,28 @@ class DigitizerSpatialBlurringActor(GateObject):
                     truncated=bool(self.use_truncated_Gaussian))
 
 
+class GammaFreeFlightActor(GateObject):
+    """Free flight of gammas (GammaFreeFlightActor, opengate/actors/biasingactors.py:247-300;
+    GateGammaFreeFlightOptrActor / GateGammaFreeFlightOptn): attached to the world with the
+    SPECT heads as ``exclude_volumes``, photons do not interact outside the heads and carry
+    the probability of reaching them as their weight; the projections become weighted sums.
+    The primary (unscattered) component of the reference's free-flight SPECT recipe
+    (contrib/spect/spect_config.py:937-970)."""
+
+    type_name = "GammaFreeFlightActor"
+    user_info_defaults = {"attached_to": "world", "exclude_volumes": [], "weight_cutoff": -1.0,
+                          "energy_cutoff": 0.0, "bias_primary_only": True, "bias_only_once": False,
+                          "particles": ["gamma"], "priority": 100}
+
+    def check(self, head_volumes):
+        if self.attached_to != "world":
+            raise NotImplementedError("the GPU path applies free flight to the whole world (attached_to='world')")
+        excluded = set(self.exclude_volumes)
+        for h in head_volumes:
+            if not ({h.name, h.crystal_name, f"{h.name}_collimator"} & excluded):
+                raise NotImplementedError(f"free flight must exclude the SPECT head '{h.name}' (exclude_volumes)")
+
+
 class SimulationStatisticsActor(GateObject):
     type_name = "SimulationStatisticsActor"
     user_info_defaults = {"attached_to": "world", "track_types_flag": False, "output_filename": "auto"}
@@ -609,6 +631,7 @@ class Simulation:
         cls = {"DoseActor": DoseActor, "TLEDoseActor": TLEDoseActor,
                "SimulationStatisticsActor": SimulationStatisticsActor,
                "DigitizerAdderActor": DigitizerAdderActor,
+               "GammaFreeFlightActor": GammaFreeFlightActor,
                "DigitizerBlurringActor": DigitizerBlurringActor,
                "DigitizerSpatialBlurringActor": DigitizerSpatialBlurringActor,
                "DigitizerProjectionActor": DigitizerProjectionActor}.get(actor_type)
@@ -708,6 +731,12 @@ class Simulation:
                          head_start_deg=[h.start_angle_deg for h in heads])
         if half_w:
             sp.half_width = half_w
+        ffs = [a for a in self.actors.values() if isinstance(a, GammaFreeFlightActor)]
+        if len(ffs) > 1:
+            raise NotImplementedError("one GammaFreeFlightActor")
+        if ffs:
+            ffs[0].check(heads)
+            sp.set_free_flight(float(ffs[0].weight_cutoff), float(ffs[0].energy_cutoff) / u.MeV)
         # digitizer adder and blurring: one setting shared by every head's crystal
         def set_policy(policy):
             sp.adder_policy = policy
@@ -755,7 +784,12 @@ class Simulation:
                         eng._call("gg_run", C.ctypes.c_uint64(plan[k][r]), C.ctypes.c_uint64(seed),
                                   C.ctypes.c_uint64(first))
                     first += plan[k][r]
-            proj, cnt = eng.projection(), eng.counters()
+            if sp.free_flight.enabled:
+                proj, proj2 = eng.weighted_projection(squared=True)
+            else:
+                proj = eng.projection()
+                proj2 = proj
+            cnt = eng.counters()
         finally:
             eng.close()
         elapsed = time.perf_counter() - t0
@@ -766,7 +800,7 @@ class Simulation:
             img = image_io.Image(proj[h], [sx, sy, 1.0], origin)
             a.counts.image = img
             a.counts.number_of_samples = first
-            a.counts_squared.image = image_io.Image(proj[h].copy(), [sx, sy, 1.0], origin)
+            a.counts_squared.image = image_io.Image(proj2[h].copy(), [sx, sy, 1.0], origin)
             if a.write_to_disk:
                 out = a.output_filename
                 path = self.get_output_path(f"{a.name}_counts.mhd" if out in (None, "", "auto") else out)

@@ -106,6 +106,9 @@ struct gg_ctx {
   size_t q_cap = 0;
   // ARF stage in the SPECT acquisition
   bool arf_on = false;
+  // free flight outside the heads (gg_spect_set_free_flight)
+  bool ff_on = false;
+  double ff_wcut = -1.0, ff_ecut = 0.0;
   unsigned long long *d_arf_proj = nullptr, *d_arf_proj2 = nullptr;
   size_t arf_proj_n = 0;
   unsigned long long *d_qn = nullptr;
@@ -332,6 +335,11 @@ struct gg_ctx {
       s.run_base = run_base;
       s.half_w = (real)sp.half_width;
       s.centroid = sp.adder_policy == GG_ADDER_CENTROID ? 1 : 0;
+      s.ff = ff_on ? 1 : 0;
+      s.ff_wcut = (real)ff_wcut;
+      s.ff_ecut = (real)ff_ecut;
+      s.wproj = ff_on ? d_arf_proj : nullptr;
+      s.wproj2 = ff_on ? d_arf_proj2 : nullptr;
       s.zb[0] = (real)0;
       s.zb[1] = (real)sp.collimator_thickness;
       s.zb[2] = (real)(sp.collimator_thickness + sp.gap);
@@ -1216,7 +1224,7 @@ int gg_spect_setup(gg_ctx *c, const gg_spect_desc *sp) {
   }
   if ((st = c->cuda(cudaMemsetAsync(c->d_proj, 0, n * 8, c->stream), "memset projections"))) return st;
   if ((st = c->cuda(cudaMemsetAsync(c->d_counters, 0, GG_N_COUNTERS * 8, c->stream), "memset counters"))) return st;
-  if (c->arf_on && (st = arf_projection_alloc(c, n))) return st;
+  if ((c->arf_on || c->ff_on) && (st = arf_projection_alloc(c, n))) return st;
   c->spect = *sp;
   c->have_spect = true;
   c->spect_run = 0;
@@ -1506,16 +1514,37 @@ int gg_spect_use_arf(gg_ctx *c, int32_t enable) {
   if (c->arf.n_classes != c->spect.n_windows + 1)
     return c->fail(GG_ERR_ARG, "gg_spect_use_arf: the model has %d classes, the heads %d windows + 1", c->arf.n_classes,
                    c->spect.n_windows);
+  if (c->ff_on) return c->fail(GG_ERR_STATE, "gg_spect_use_arf: switch free flight off first");
   c->arf_on = true;
   int st = arf_projection_alloc(c, c->n_proj);
   if (st) return st;
   return c->cuda(cudaStreamSynchronize(c->stream), "ARF projection");
 }
 
+int gg_spect_set_free_flight(gg_ctx *c, const gg_ff_desc *f) {
+  if (!c || !f) return GG_ERR_ARG;
+  cudaSetDevice(c->device);
+  if (!f->enabled) {
+    c->ff_on = false;
+    return GG_OK;
+  }
+  if (!c->have_spect) return c->fail(GG_ERR_STATE, "gg_spect_set_free_flight: call gg_spect_setup first");
+  if (c->arf_on) return c->fail(GG_ERR_STATE, "gg_spect_set_free_flight: the ARF detector is on");
+  if (std::isnan(f->weight_cutoff) || std::isnan(f->energy_cutoff))
+    return c->fail(GG_ERR_ARG, "gg_spect_set_free_flight: invalid cutoff");
+  c->ff_on = true;
+  c->ff_wcut = f->weight_cutoff;
+  c->ff_ecut = f->energy_cutoff;
+  int st = arf_projection_alloc(c, c->n_proj);
+  if (st) return st;
+  return c->cuda(cudaStreamSynchronize(c->stream), "weighted projection");
+}
+
 int gg_get_arf_projection(gg_ctx *c, double *counts, double *squared, size_t n) {
   if (!c || !counts) return GG_ERR_ARG;
   cudaSetDevice(c->device);
-  if (!c->arf_on || !c->d_arf_proj) return c->fail(GG_ERR_STATE, "gg_get_arf_projection: the ARF stage is off");
+  if ((!c->arf_on && !c->ff_on) || !c->d_arf_proj)
+    return c->fail(GG_ERR_STATE, "gg_get_arf_projection: neither the ARF stage nor free flight is on");
   if (n != c->arf_proj_n) return c->fail(GG_ERR_ARG, "gg_get_arf_projection: buffer has %zu values, need %zu", n, c->arf_proj_n);
   std::vector<unsigned long long> tmp(n);
   int st = c->d2h(tmp.data(), c->d_arf_proj, n * 8, "download ARF projection");

@@ -85,6 +85,7 @@ __global__ void __launch_bounds__(256) k_arf_sample(Scene<real> s, ArfArgs p) {
     ph.left_hole = 0;
     ph.exclude = -1;
     ph.run = 0;
+    ph.w = R<real>(1);
     ph.steps = 0;
     Secondary<real> sec;
     sec.base = sec_store;

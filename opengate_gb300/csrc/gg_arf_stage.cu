@@ -52,8 +52,9 @@ __device__ __forceinline__ void queue_copy(const PQueue<real> &in, size_t k, con
   out.dy[j] = in.dy[k];
   out.dz[j] = in.dz[k];
   out.e[j] = in.e[k];
+  out.w[j] = in.w[k];
 #pragma unroll
-  for (int i = 0; i < 8; ++i) out.ev[i][j] = in.ev[i][k];
+  for (int i = 0; i < kEvSlots; ++i) out.ev[i][j] = in.ev[i][k];
   out.rng_pos[j] = in.rng_pos[k];
   out.meta[j] = in.meta[k];
 }

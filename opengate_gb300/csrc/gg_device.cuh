@@ -476,6 +476,12 @@ struct Scene {
   // 1 Gaussian (clamped into the crystal when sb_keep), 2 truncated Gaussian)
   int eblur, sblur, sb_keep;
   int centroid;  // adder policy: 0 EnergyWinnerPosition, 1 EnergyWeightedCentroidPosition
+  // free flight outside the heads (GateGammaFreeFlightOptn, heads excluded):
+  // ff = 1 on; weight / energy cutoffs; singles then add their weight (2^-32
+  // fixed point, with history-by-history squares) to wproj / wproj2
+  int ff;
+  real ff_wcut, ff_ecut;
+  unsigned long long *wproj, *wproj2;
   real eb_sigma, eb_res, eb_ref, eb_slope, sb_sigma[2];
 };
 
@@ -568,6 +574,7 @@ struct Photon {
   // 0 image, 1 + h head h); head-local state while in_head
   int in_head, head, hreg, left_hole, exclude;
   int run;  // SPECT gantry position of the history
+  real w;   // SPECT free flight: statistical weight (1 otherwise)
 };
 
 template <typename real>

@@ -496,16 +496,13 @@ __device__ __forceinline__ uint32_t voxel_of(const Scene<real> &s, const real p[
   return (uint32_t)ix + (uint32_t)s.nx * ((uint32_t)iy + (uint32_t)s.ny * (uint32_t)iz);
 }
 
-// Track-length estimator (GateTLEDoseActor::ScoreTLEDepositStep,
-// core/opengate_core/opengate_lib/GateTLEDoseActor.cpp:249-299): the straight
-// path [p, p + len d) of a photon of energy e (table index ei) scores
-// e * mu_en(E, material) * length in every voxel it crosses.  Voxel walk of
-// Amanatides & Woo: distance to the next boundary per axis, the nearest one
-// crossed first (ties: x, then y, then z).
-template <typename real>
-__device__ __forceinline__ void tle_path(const Scene<real> &s, const real p[3], const real d[3], real len, real e,
-                                         const EIdx<real> &ei, HistList<real> &l, const Tally<real> &t,
-                                         BlockCounters *bc, unsigned int &n_dep) {
+// Voxel walk (Amanatides & Woo) of the straight path [p, p + len d) inside the
+// image: visit(v, m, length) for every voxel v (material m) it crosses, in
+// order; distance to the next boundary per axis, the nearest crossed first
+// (ties: x, then y, then z).
+template <typename real, typename Visit>
+__device__ __forceinline__ void voxel_walk(const Scene<real> &s, const real p[3], const real d[3], real len,
+                                           Visit &&visit) {
   const int n0 = s.nx, n1 = s.ny, n2 = s.nz;
   int i0 = (int)((p[0] - s.bmin[0]) * s.inv_sp[0]);
   int i1 = (int)((p[1] - s.bmin[1]) * s.inv_sp[1]);
@@ -555,12 +552,7 @@ __device__ __forceinline__ void tle_path(const Scene<real> &s, const real p[3], 
     const real seg = te - tc;
     if (seg > R<real>(0)) {
       const uint32_t v = (uint32_t)i0 + (uint32_t)n0 * ((uint32_t)i1 + (uint32_t)n1 * (uint32_t)i2);
-      const int m = __ldg(s.labels + v);
-      real mu = interp_row(s.muen + (size_t)s.mat_comp[m] * s.n_e, ei);
-      mu = s.mat_rho[m] * mu;
-      real ed = e * mu;
-      ed = ed * seg;
-      deposit(l, t, bc, v, ed, n_dep);
+      visit(v, (int)__ldg(s.labels + v), seg);
     }
     tc = te;
     if (!(tc < len)) break;
@@ -578,6 +570,38 @@ __device__ __forceinline__ void tle_path(const Scene<real> &s, const real p[3], 
       tn2 = tn2 + td2;
     }
   }
+}
+
+// Track-length estimator (GateTLEDoseActor::ScoreTLEDepositStep,
+// core/opengate_core/opengate_lib/GateTLEDoseActor.cpp:249-299): the straight
+// path [p, p + len d) of a photon of energy e (table index ei) scores
+// e * mu_en(E, material) * length in every voxel it crosses.
+template <typename real>
+__device__ __forceinline__ void tle_path(const Scene<real> &s, const real p[3], const real d[3], real len, real e,
+                                         const EIdx<real> &ei, HistList<real> &l, const Tally<real> &t,
+                                         BlockCounters *bc, unsigned int &n_dep) {
+  voxel_walk(s, p, d, len, [&](uint32_t v, int m, real seg) {
+    real mu = interp_row(s.muen + (size_t)s.mat_comp[m] * s.n_e, ei);
+    mu = s.mat_rho[m] * mu;
+    real ed = e * mu;
+    ed = ed * seg;
+    deposit(l, t, bc, v, ed, n_dep);
+  });
+}
+
+// Optical depth of the straight path [p, p + len d) inside the image:
+// sum of mu(E, material) * length over the voxels it crosses.
+template <typename real>
+__device__ __forceinline__ real image_depth(const Scene<real> &s, const real p[3], const real d[3], real len,
+                                           const EIdx<real> &ei) {
+  real tau = R<real>(0);
+  voxel_walk(s, p, d, len, [&](uint32_t, int m, real seg) {
+    real mu = interp_row(s.sig + (size_t)s.mat_comp[m] * s.n_e, ei);
+    mu = s.mat_rho[m] * mu;
+    mu = mu * seg;
+    tau = tau + mu;
+  });
+  return tau;
 }
 
 // Scoring state handed to the flights of the track-length estimator.
@@ -721,10 +745,12 @@ __device__ __forceinline__ void event_add(const Scene<real> &s, Event<real> &ev,
   if (s.centroid) {
     ev.wpos[H][0] = ev.wpos[H][0] + ed * ph.pos[0];
     ev.wpos[H][1] = ev.wpos[H][1] + ed * ph.pos[1];
+    ev.w[H] = ph.w;  // the last hit's weight
   } else if (ed > ev.emax[H]) {
     ev.emax[H] = ed;
     ev.wpos[H][0] = ph.pos[0];
     ev.wpos[H][1] = ph.pos[1];
+    ev.w[H] = ph.w;  // the winner hit's weight
   }
 }
 

@@ -18,13 +18,15 @@ namespace gg {
 
 // Photons handed between the stages, SoA.  meta: bits 0-19 steps taken,
 // bit 20 head, bits 21-22 head region, bit 23 event present, bits 24-26
-// exclude + 1.  ev: esum[2], emax[2], wpos[2][2] of the history's event.
+// exclude + 1.  ev: esum[2], emax[2], wpos[2][2], w[2] of the history's
+// event; w: the photon's weight (free flight).
+constexpr int kEvSlots = 10;
 template <typename real>
 struct PQueue {
   uint4 *rng_buf;
   unsigned long long *hid;
-  real *px, *py, *pz, *dx, *dy, *dz, *e;
-  real *ev[8];
+  real *px, *py, *pz, *dx, *dy, *dz, *e, *w;
+  real *ev[kEvSlots];
   uint32_t *rng_pos, *meta;
 
   __device__ __forceinline__ static PQueue carve(void *base, size_t cap) {
@@ -34,12 +36,12 @@ struct PQueue {
     p += cap * sizeof(uint4);
     q.hid = reinterpret_cast<unsigned long long *>(p);
     p += cap * sizeof(unsigned long long);
-    real **f[7] = {&q.px, &q.py, &q.pz, &q.dx, &q.dy, &q.dz, &q.e};
-    for (int i = 0; i < 7; ++i) {
+    real **f[8] = {&q.px, &q.py, &q.pz, &q.dx, &q.dy, &q.dz, &q.e, &q.w};
+    for (int i = 0; i < 8; ++i) {
       *f[i] = reinterpret_cast<real *>(p);
       p += cap * sizeof(real);
     }
-    for (int i = 0; i < 8; ++i) {
+    for (int i = 0; i < kEvSlots; ++i) {
       q.ev[i] = reinterpret_cast<real *>(p);
       p += cap * sizeof(real);
     }
@@ -52,7 +54,7 @@ struct PQueue {
 
 template <typename real>
 size_t queue_bytes(size_t cap) {
-  return cap * (sizeof(uint4) + sizeof(unsigned long long) + 15 * sizeof(real) + 2 * sizeof(uint32_t));
+  return cap * (sizeof(uint4) + sizeof(unsigned long long) + (8 + kEvSlots) * sizeof(real) + 2 * sizeof(uint32_t));
 }
 
 constexpr uint32_t kMetaSteps = (1u << 20) - 1u;
@@ -102,10 +104,11 @@ __device__ __forceinline__ int run_of(const Scene<real> &s, uint64_t hid) {
   return s.run_base + (int)((hid - s.run_first) / s.run_len);
 }
 
-// Writes the lane's photon (and event) to slot k of the output queue.
-template <typename real>
+// Writes the lane's photon (and event) to slot k of the output queue; the
+// weight only with free flight (FF), where it can differ from 1.
+template <typename real, bool FF = true>
 __device__ __forceinline__ void queue_put(const PQueue<real> &q, size_t k, const Photon<real> &ph, const Rng &g,
-                                          uint64_t hid, const real ev[8], bool has_ev) {
+                                          uint64_t hid, const real ev[kEvSlots], bool has_ev) {
   q.rng_buf[k] = make_uint4(g.buf[0], g.buf[1], g.buf[2], g.buf[3]);
   q.rng_pos[k] = (g.blk << 3) | (uint32_t)g.idx;
   q.hid[k] = hid;
@@ -116,9 +119,10 @@ __device__ __forceinline__ void queue_put(const PQueue<real> &q, size_t k, const
   q.dy[k] = ph.dir[1];
   q.dz[k] = ph.dir[2];
   q.e[k] = ph.e;
+  if constexpr (FF) q.w[k] = ph.w;
   if (has_ev) {
 #pragma unroll
-    for (int i = 0; i < 8; ++i) q.ev[i][k] = ev[i];
+    for (int i = 0; i < kEvSlots; ++i) q.ev[i][k] = ev[i];
   }
   q.meta[k] = ((uint32_t)ph.steps & kMetaSteps) | ((uint32_t)ph.head << 20) | ((uint32_t)ph.hreg << 21) |
               ((has_ev ? 1u : 0u) << 23) | ((uint32_t)(ph.exclude + 1) << 24);
@@ -127,7 +131,7 @@ __device__ __forceinline__ void queue_put(const PQueue<real> &q, size_t k, const
 // Reads slot k of an input queue into the lane (photon state as it was when
 // it entered the queue: at a head-box entry in head-local coordinates, or at
 // an image-box entry in world coordinates).
-template <typename real>
+template <typename real, bool FF = true>
 __device__ __forceinline__ uint64_t queue_get(const Scene<real> &s, const PQueue<real> &q, size_t k, Photon<real> &ph,
                                               Rng &g, uint64_t seed, bool &has_ev) {
   const uint64_t hid = q.hid[k];
@@ -139,6 +143,8 @@ __device__ __forceinline__ uint64_t queue_get(const Scene<real> &s, const PQueue
   ph.dir[1] = q.dy[k];
   ph.dir[2] = q.dz[k];
   set_energy(s, ph, q.e[k]);
+  if constexpr (FF) ph.w = q.w[k];
+  else ph.w = R<real>(1);
   const uint32_t m = q.meta[k];
   ph.steps = (int)(m & kMetaSteps);
   ph.head = (int)((m >> 20) & 1u);
@@ -165,13 +171,13 @@ __device__ __forceinline__ size_t queue_claim(unsigned long long *count, bool pu
 }
 
 template <typename real>
-__device__ __forceinline__ void load_event(const PQueue<real> &q, size_t k, real ev[8]) {
+__device__ __forceinline__ void load_event(const PQueue<real> &q, size_t k, real ev[kEvSlots]) {
 #pragma unroll
-  for (int i = 0; i < 8; ++i) ev[i] = q.ev[i][k];
+  for (int i = 0; i < kEvSlots; ++i) ev[i] = q.ev[i][k];
 }
 
 template <typename real>
-__device__ __forceinline__ void event_from(const real v[8], Event<real> &ev) {
+__device__ __forceinline__ void event_from(const real v[kEvSlots], Event<real> &ev) {
   ev.esum[0] = v[0];
   ev.esum[1] = v[1];
   ev.emax[0] = v[2];
@@ -180,10 +186,12 @@ __device__ __forceinline__ void event_from(const real v[8], Event<real> &ev) {
   ev.wpos[0][1] = v[5];
   ev.wpos[1][0] = v[6];
   ev.wpos[1][1] = v[7];
+  ev.w[0] = v[8];
+  ev.w[1] = v[9];
 }
 
 template <typename real>
-__device__ __forceinline__ void event_to(const Event<real> &ev, real v[8]) {
+__device__ __forceinline__ void event_to(const Event<real> &ev, real v[kEvSlots]) {
   v[0] = ev.esum[0];
   v[1] = ev.esum[1];
   v[2] = ev.emax[0];
@@ -192,6 +200,8 @@ __device__ __forceinline__ void event_to(const Event<real> &ev, real v[8]) {
   v[5] = ev.wpos[0][1];
   v[6] = ev.wpos[1][0];
   v[7] = ev.wpos[1][1];
+  v[8] = ev.w[0];
+  v[9] = ev.w[1];
 }
 
 }  // namespace gg

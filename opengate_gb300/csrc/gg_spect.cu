@@ -34,13 +34,19 @@ namespace gg {
 // Phantom-stage flight: Woodcock step in the image (followed, when it leaves
 // the image box, by the world step) or one world step; a photon whose world
 // step ends at a head-box entry leaves the stage (kPush).
-template <typename real>
+template <typename real, bool FF>
 __device__ __forceinline__ int phantom_flight(const Scene<real> &s, Photon<real> &ph, Rng &g, BlockCounters *bc,
                                               int &pmat, uint32_t &pv, int &pscored, unsigned int &n_wood,
                                               unsigned int &n_real, unsigned int &n_world) {
   if (++ph.steps > kStepCap) {
     atomicAdd(&bc->loop_capped, 1u);
     ph.alive = 0;
+    return kRefill;
+  }
+  if constexpr (FF) {  // free flight to a head: no interaction outside the heads
+    ++n_world;
+    if (ff_flight(s, ph)) return kPush;
+    atomicAdd(&bc->escaped, 1u);
     return kRefill;
   }
   if (ph.in_image) {
@@ -69,7 +75,7 @@ __device__ __forceinline__ int phantom_flight(const Scene<real> &s, Photon<real>
 
 // Head-stage flight: one step in a head, or one world step; a photon whose
 // world step ends at the image-box entry leaves the stage (kPush).
-template <typename real>
+template <typename real, bool FF>
 __device__ __forceinline__ int head_stage_flight(const Scene<real> &s, Photon<real> &ph, Rng &g, BlockCounters *bc,
                                                  int &pmat, int &pscored, unsigned int &n_world,
                                                  unsigned int &n_head) {
@@ -89,6 +95,11 @@ __device__ __forceinline__ int head_stage_flight(const Scene<real> &s, Photon<re
     return kFly;
   }
   ++n_world;
+  if constexpr (FF) {  // free flight to another head (the image crossed on the way)
+    if (ff_flight(s, ph)) return kFly;
+    atomicAdd(&bc->escaped, 1u);
+    return kRefill;
+  }
   if (spect_world_flight(s, ph, g)) {
     pmat = s.world_mat;
     pscored = 0;
@@ -130,7 +141,7 @@ __device__ __forceinline__ void stage_counters(unsigned long long *cnt, const Bl
 // return queue; output: the head queue.  Persistent grid with the
 // phase-batched lane loop of the dose transport kernel (refill / fly /
 // interact, one phase per warp iteration).
-template <typename real, int MINB>
+template <typename real, int MINB, bool FF>
 __global__ void __launch_bounds__(256, MINB) k_spect_phantom(Scene<real> sg, KernelArgs args, StageArgs q) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ BlockCounters bc;
@@ -190,7 +201,7 @@ __global__ void __launch_bounds__(256, MINB) k_spect_phantom(Scene<real> sg, Ker
       if (need && in_hist && has_ev) {
         // a photon that came back from a head died here: score its event
         Event<real> ev;
-        real v[8];
+        real v[kEvSlots];
         load_event(in, slot, v);
         event_from(v, ev);
         n_singles += score_singles(s, ev, ph.run, g);
@@ -215,7 +226,7 @@ __global__ void __launch_bounds__(256, MINB) k_spect_phantom(Scene<real> sg, Ker
         if (h >= n_items) {
           state = kDone;
         } else if (from_queue) {
-          hid = queue_get(s, in, h, ph, g, args.seed, has_ev);
+          hid = queue_get<real, FF>(s, in, h, ph, g, args.seed, has_ev);
           slot = h;
           ph.in_head = 0;
           ph.in_image = 1;
@@ -238,6 +249,7 @@ __global__ void __launch_bounds__(256, MINB) k_spect_phantom(Scene<real> sg, Ker
             ph.can_enter = 1;
             ph.in_head = 0;
             ph.exclude = -1;
+            ph.w = R<real>(1);
             hid = args.h_begin + h;
             ph.run = run_of(s, hid);
             has_ev = false;
@@ -269,7 +281,7 @@ __global__ void __launch_bounds__(256, MINB) k_spect_phantom(Scene<real> sg, Ker
       }
     } else {
       if (state == kFly) {
-        state = phantom_flight(s, ph, g, &bc, pmat, pv, pscored, n_wood, n_real, n_world);
+        state = phantom_flight<real, FF>(s, ph, g, &bc, pmat, pv, pscored, n_wood, n_real, n_world);
         if (state == kRefill && sec.has) {
           pop_secondary(s, ph, sec);
           state = kFly;
@@ -279,9 +291,9 @@ __global__ void __launch_bounds__(256, MINB) k_spect_phantom(Scene<real> sg, Ker
       const size_t k = queue_claim(q.out_n, push, lane, lt_mask);
       if (push) {
         if (k < q.q_cap) {
-          real v[8];
+          real v[kEvSlots];
           if (has_ev) load_event(in, slot, v);
-          queue_put(out, k, ph, g, hid, v, has_ev);
+          queue_put<real, FF>(out, k, ph, g, hid, v, has_ev);
         } else {
           atomicOr(args.status, kStatusQueueOverflow);
         }
@@ -296,7 +308,7 @@ __global__ void __launch_bounds__(256, MINB) k_spect_phantom(Scene<real> sg, Ker
 // Head stage.  Input: the head queue; output: the return queue.  Each lane
 // carries its photon's event in registers and scores it when the photon
 // dies.
-template <typename real, int MINB>
+template <typename real, int MINB, bool FF>
 __global__ void __launch_bounds__(256, MINB) k_spect_head(Scene<real> sg, KernelArgs args, StageArgs q) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ BlockCounters bc;
@@ -371,9 +383,9 @@ __global__ void __launch_bounds__(256, MINB) k_spect_head(Scene<real> sg, Kernel
           state = kDone;
         } else {
           bool has_ev;
-          hid = queue_get(s, in, h, ph, g, args.seed, has_ev);
+          hid = queue_get<real, FF>(s, in, h, ph, g, args.seed, has_ev);
           if (has_ev) {
-            real v[8];
+            real v[kEvSlots];
             load_event(in, h, v);
             event_from(v, ev);
           } else {
@@ -395,7 +407,7 @@ __global__ void __launch_bounds__(256, MINB) k_spect_head(Scene<real> sg, Kernel
       }
     } else {
       if (state == kFly) {
-        state = head_stage_flight(s, ph, g, &bc, pmat, pscored, n_world, n_head);
+        state = head_stage_flight<real, FF>(s, ph, g, &bc, pmat, pscored, n_world, n_head);
         if (state == kRefill && sec.has) {
           pop_secondary(s, ph, sec);
           state = kFly;
@@ -405,9 +417,9 @@ __global__ void __launch_bounds__(256, MINB) k_spect_head(Scene<real> sg, Kernel
       const size_t k = queue_claim(q.out_n, push, lane, lt_mask);
       if (push) {
         if (k < q.q_cap) {
-          real v[8];
+          real v[kEvSlots];
           event_to(ev, v);
-          queue_put(out, k, ph, g, hid, v, true);
+          queue_put<real, FF>(out, k, ph, g, hid, v, true);
         } else {
           atomicOr(args.status, kStatusQueueOverflow);
         }
@@ -419,26 +431,29 @@ __global__ void __launch_bounds__(256, MINB) k_spect_head(Scene<real> sg, Kernel
   stage_counters(args.counters, bc, lane, 0u, 0u, n_world, n_head, n_singles);
 }
 
-template <typename real, int MINB>
+template <typename real, int MINB, bool FF = false>
 static cudaError_t launch_stage_v(int stage, const Scene<real> &s, const KernelArgs &a, const StageArgs &q, int grid,
                                   int block, size_t smem, cudaStream_t st) {
   static bool configured[2] = {false, false};
   if (!configured[stage]) {
-    cudaError_t e = stage == 0 ? cudaFuncSetAttribute(k_spect_phantom<real, MINB>,
+    cudaError_t e = stage == 0 ? cudaFuncSetAttribute(k_spect_phantom<real, MINB, FF>,
                                                       cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024)
-                               : cudaFuncSetAttribute(k_spect_head<real, MINB>,
+                               : cudaFuncSetAttribute(k_spect_head<real, MINB, FF>,
                                                       cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     if (e != cudaSuccess) return e;
     configured[stage] = true;
   }
-  if (stage == 0) k_spect_phantom<real, MINB><<<grid, block, smem, st>>>(s, a, q);
-  else k_spect_head<real, MINB><<<grid, block, smem, st>>>(s, a, q);
+  if (stage == 0) k_spect_phantom<real, MINB, FF><<<grid, block, smem, st>>>(s, a, q);
+  else k_spect_head<real, MINB, FF><<<grid, block, smem, st>>>(s, a, q);
   return cudaGetLastError();
 }
 
 template <typename real>
 cudaError_t launch_spect_stage(int stage, const Scene<real> &s, const KernelArgs &a, const StageArgs &q, int grid,
                                int block, size_t smem, int minb, cudaStream_t st) {
+  // free flight: one register budget (4 blocks of 256 threads per SM); a
+  // smaller grid computed for another budget is a valid launch of it
+  if (s.ff) return launch_stage_v<real, 4, true>(stage, s, a, q, grid, block, smem, st);
   if (minb <= 2) return launch_stage_v<real, 2>(stage, s, a, q, grid, block, smem, st);
   if (minb == 3) return launch_stage_v<real, 3>(stage, s, a, q, grid, block, smem, st);
   return launch_stage_v<real, 4>(stage, s, a, q, grid, block, smem, st);
@@ -446,8 +461,8 @@ cudaError_t launch_spect_stage(int stage, const Scene<real> &s, const KernelArgs
 
 template <typename real, int MINB>
 static cudaError_t stage_occupancy_v(int stage, int block, size_t smem, int *bps) {
-  return stage == 0 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(bps, k_spect_phantom<real, MINB>, block, smem)
-                    : cudaOccupancyMaxActiveBlocksPerMultiprocessor(bps, k_spect_head<real, MINB>, block, smem);
+  return stage == 0 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(bps, k_spect_phantom<real, MINB, false>, block, smem)
+                    : cudaOccupancyMaxActiveBlocksPerMultiprocessor(bps, k_spect_head<real, MINB, false>, block, smem);
 }
 
 template <typename real>

@@ -146,12 +146,14 @@ __device__ __forceinline__ void move3(real p[3], const real d[3], real t) {
 template <typename real>
 struct Event {
   real esum[2], emax[2], wpos[2][2];
+  real w[2];  // weight of each head's single (free flight; 1 otherwise)
   __device__ __forceinline__ void clear() {
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
       esum[h] = R<real>(0);
       emax[h] = R<real>(0);
       wpos[h][0] = wpos[h][1] = R<real>(0);
+      w[h] = R<real>(1);
     }
   }
 };
@@ -293,6 +295,82 @@ __device__ __forceinline__ int spect_world_flight(const Scene<real> &s, Photon<r
   }
   ph.alive = 0;
   return 0;
+}
+
+// Free flight outside the heads (GateGammaFreeFlightOptn /
+// GateGammaFreeFlightOptrActor with the heads as excluded volumes,
+// biasing/GateGammaFreeFlightOptn.cpp:34-83, GateVBiasOptrActor.cpp:85-92):
+// the photon does not interact in the world or the image; it flies straight
+// to the nearest head entry (the head it just left excluded) and its weight
+// is multiplied by the probability of getting there, exp(-optical depth)
+// (air over the whole path, the voxels' attenuation inside the image box).
+// Photons at or below the energy or weight cutoff, and photons whose line
+// misses every head, stop.  Returns 1 at a head entry (head-local state as
+// spect_world_flight sets it), 0 when the photon stopped.
+template <typename real>
+__device__ __forceinline__ int ff_flight(const Scene<real> &s, Photon<real> &ph) {
+  if (ph.e <= s.ff_ecut || ph.w <= s.ff_wcut) {
+    ph.alive = 0;
+    return 0;
+  }
+  real tb = gg_inf(real(0));
+  int box = 0;
+  real hlo[3] = {-s.half_w, -s.half_w, R<real>(0)};
+  real hhi[3] = {s.half_w, s.half_w, s.zb[3]};
+  for (int h = 0; h < s.n_heads; ++h) {
+    if (ph.exclude == 1 + h) continue;
+    real lp[3], ld[3];
+    to_local(head_frame(s, ph.run, h), ph.pos, ph.dir, lp, ld);
+    real th = entry_distance(lp, ld, hlo, hhi);
+    if (th < tb) {
+      tb = th;
+      box = 1 + h;
+    }
+  }
+  real wlo[3] = {-s.whalf[0], -s.whalf[1], -s.whalf[2]};
+  const real tout = exit_distance(ph.pos, ph.dir, wlo, s.whalf);
+  if (!(tb <= tout)) {
+    ph.alive = 0;
+    return 0;
+  }
+  const int wm = s.world_mat;
+  real mu_air = interp_row(s.sig + (size_t)s.mat_comp[wm] * s.n_e, ph.ei);
+  mu_air = s.mat_rho[wm] * mu_air;
+  real l_air = tb;
+  real tau = R<real>(0);
+  const real t0 = entry_distance(ph.pos, ph.dir, s.bmin, s.bmax);
+  if (t0 < tb) {
+    real p0[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) p0[a] = ph.pos[a] + t0 * ph.dir[a];
+    real lin = exit_distance(p0, ph.dir, s.bmin, s.bmax);
+    const real rest = tb - t0;
+    lin = lin < rest ? lin : rest;
+    tau = image_depth(s, p0, ph.dir, lin, ph.ei);
+    l_air = l_air - lin;
+  }
+  real ta = mu_air * l_air;
+  tau = tau + ta;
+  ph.w = ph.w * gg_exp(-tau);
+  if (ph.w <= s.ff_wcut) {
+    ph.alive = 0;
+    return 0;
+  }
+  move3(ph.pos, ph.dir, tb);
+  const int h = box - 1;
+  real lp[3], ld[3];
+  to_local(head_frame(s, ph.run, h), ph.pos, ph.dir, lp, ld);
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    ph.pos[a] = lp[a];
+    ph.dir[a] = ld[a];
+  }
+  ph.in_image = 0;
+  ph.in_head = 1;
+  ph.head = h;
+  ph.hreg = lp[2] < s.zb[1] ? 0 : (lp[2] < s.zb[2] ? 1 : 2);
+  ph.left_hole = 0;
+  return 1;
 }
 
 // Two standard normal deviates from the history's stream (Box & Muller 1958):
@@ -480,11 +558,26 @@ __device__ __forceinline__ unsigned score_singles(const Scene<real> &s, const Ev
     fy = fy * s.inv_psp[1];
     if (!(fx >= R<real>(0) && fx < (real)s.pnx && fy >= R<real>(0) && fy < (real)s.pny)) continue;
     int i = (int)fx, j = (int)fy;
+    // free flight: the single adds its weight in 2^-32 units, and the exact
+    // square of that for the history-by-history variance (low 32 bits, rest)
+    unsigned long long q = 0, lo = 0, rest = 0;
+    if (s.ff) {
+      q = (unsigned long long)to_fixed(ev.w[h]);
+      lo = q * q;
+      rest = (__umul64hi(q, q) << 32) | (lo >> 32);
+      lo &= 0xffffffffull;
+    }
 #pragma unroll
     for (int k = 0; k < 8; ++k) {
       if (k < s.n_win && e >= s.wlo[k] && e < s.whi[k]) {
         size_t idx = ((((size_t)h * s.n_runs + run) * s.n_win + k) * s.pny + j) * s.pnx + i;
-        atomicAdd(s.proj + idx, 1ull);
+        if (!s.ff) {
+          atomicAdd(s.proj + idx, 1ull);
+        } else if (q) {
+          atomicAdd(s.wproj + idx, q);
+          if (lo) atomicAdd(s.wproj2 + 2 * idx, lo);
+          if (rest) atomicAdd(s.wproj2 + 2 * idx + 1, rest);
+        }
       }
     }
   }

@@ -258,6 +258,7 @@ __global__ void __launch_bounds__(256, MINB) k_transport(Scene<real> sg, KernelA
             ph.can_enter = 1;
             ph.in_head = 0;
             ph.exclude = -1;
+            ph.w = R<real>(1);
             if constexpr (SPECT) {
               ev.clear();
               ph.run = s.run_base + (int)((hid - s.run_first) / s.run_len);

@@ -122,10 +122,16 @@ class SpectEngine(DoseEngine):
         self._desc = self.spect.desc()
         self._call("gg_spect_setup", ctypes.byref(self._desc))
         self._call("gg_spect_set_blur", ctypes.byref(self.spect.blur))
+        self._call("gg_spect_set_free_flight", ctypes.byref(self.spect.free_flight))
 
     def reset(self):
         self._call("gg_spect_setup", ctypes.byref(self._desc))
         self._call("gg_spect_set_blur", ctypes.byref(self.spect.blur))
+        self._call("gg_spect_set_free_flight", ctypes.byref(self.spect.free_flight))
+
+    def weighted_projection(self, squared=False):
+        """Free-flight projection: summed single weights (and their history-by-history squares)."""
+        return self.arf_projection(squared)
 
     def run(self, n_per_run, seed, first=0):
         """All gantry positions in one gg_spect_run call (one set of launches)."""

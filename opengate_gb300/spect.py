@@ -69,6 +69,8 @@ class SpectSpec:
         # digitizer: adder policy of the singles' position, blurring (off by default)
         self.adder_policy = "EnergyWinnerPosition"
         self.blur = C.BlurDesc()
+        # free flight outside the heads (set_free_flight); off by default
+        self.free_flight = C.FfDesc(0, -1.0, 0.0)
 
     def set_energy_blur(self, method, sigma=0.0, resolution=0.0, reference=0.0, slope=0.0):
         """DigitizerBlurringActor on the singles' energy (MeV): method "Gaussian" (sigma),
@@ -82,6 +84,11 @@ class SpectSpec:
         self.blur.energy_resolution = float(resolution)
         self.blur.energy_reference = float(reference)
         self.blur.energy_slope = float(slope)
+
+    def set_free_flight(self, weight_cutoff=-1.0, energy_cutoff=0.0, enabled=True):
+        """GammaFreeFlightActor on the world with the heads excluded: no interaction outside
+        the heads, weights exp(-optical depth), weighted projections (MeV for the cutoff)."""
+        self.free_flight = C.FfDesc(int(bool(enabled)), float(weight_cutoff), float(energy_cutoff))
 
     def set_spatial_blur(self, sigma, keep_in_solid_limits=True, truncated=False):
         """DigitizerSpatialBlurringActor on the crystal position: sigma (mm) along the

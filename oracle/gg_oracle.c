@@ -421,6 +421,10 @@ typedef struct {
      square / 3 linear; sblur 0 off / 1 Gaussian (+ clamp) / 2 truncated */
   int eblur, sblur, sb_keep;
   int centroid; /* adder policy EnergyWeightedCentroidPosition */
+  /* free flight outside the heads (gg_ff_desc) and its weighted projection */
+  int ff;
+  real ff_wcut, ff_ecut;
+  uint64_t *wproj, *wproj2;
   real eb_sigma, eb_res, eb_ref, eb_slope, sb_sigma[2];
   const struct arf_s *arf; /* ARF detector model, or NULL */
 } scene_t;
@@ -562,12 +566,14 @@ typedef struct {
      always stays with plain tracking); head_stage = it is being tracked with
      the heads since its last image entry (head-to-head flights skip the ARF) */
   int visited_head, head_stage;
+  real w; /* free flight: statistical weight */
 } photon_t;
 
 /* per-event crystal accumulation of each head (adder, EnergyWinnerPosition);
    wpos = head-local (a1, a2) of the energy winner */
 typedef struct {
   real esum[2], emax[2], wpos[2][2];
+  real w[2]; /* weight of each head's single (free flight) */
 } event_t;
 
 static void set_energy(const scene_t *s, photon_t *ph, real e) {
@@ -852,6 +858,7 @@ static int sample_primary(const scene_t *s, rng_t *g, photon_t *ph, tally_t *t) 
   ph->alive = 1;
   ph->can_enter = 1;
   ph->in_image = 0;
+  ph->w = R(1);
   set_energy(s, ph, e);
   return GG_OK;
 }
@@ -1094,10 +1101,12 @@ static void head_step(const scene_t *s, photon_t *ph, rng_t *g, tally_t *t, even
     if (s->centroid) { /* EnergyWeightedCentroidPosition */
       ev->wpos[h][0] = ev->wpos[h][0] + ed * l[0];
       ev->wpos[h][1] = ev->wpos[h][1] + ed * l[1];
+      ev->w[h] = ph->w; /* the last hit's weight */
     } else if (ed > ev->emax[h]) {
       ev->emax[h] = ed;
       ev->wpos[h][0] = l[0];
       ev->wpos[h][1] = l[1];
+      ev->w[h] = ph->w; /* the winner hit's weight */
     }
   }
 }
@@ -1428,10 +1437,24 @@ static void score_singles(const scene_t *s, const event_t *ev, tally_t *t, rng_t
     fy = fy * s->inv_psp[1];
     if (!(fx >= R(0) && fx < (real)s->pnx && fy >= R(0) && fy < (real)s->pny)) continue;
     int i = (int)fx, j = (int)fy;
+    /* free flight: the single's weight in 2^-32 units and its exact square */
+    uint64_t q = 0, lo = 0, hi = 0;
+    if (s->ff) {
+      q = to_fixed(ev->w[h]);
+      unsigned __int128 sq = (unsigned __int128)q * q;
+      lo = (uint64_t)sq & 0xffffffffu;
+      hi = (uint64_t)(sq >> 32);
+    }
     for (int k = 0; k < s->n_win; ++k) {
       if (e >= s->wlo[k] && e < s->whi[k]) {
         size_t idx = ((((size_t)h * s->n_runs + s->run) * s->n_win + k) * s->pny + j) * s->pnx + i;
-        __atomic_fetch_add(&s->proj[idx], 1ull, __ATOMIC_RELAXED);
+        if (!s->ff) {
+          __atomic_fetch_add(&s->proj[idx], 1ull, __ATOMIC_RELAXED);
+        } else if (q) {
+          __atomic_fetch_add(&s->wproj[idx], q, __ATOMIC_RELAXED);
+          if (lo) __atomic_fetch_add(&s->wproj2[2 * idx], lo, __ATOMIC_RELAXED);
+          if (hi) __atomic_fetch_add(&s->wproj2[2 * idx + 1], hi, __ATOMIC_RELAXED);
+        }
       }
     }
   }
@@ -1469,12 +1492,12 @@ static void tle_first(const scene_t *s, int a, int i, real pa, real da, real *tn
   if (*tn < R(0)) *tn = R(0);
 }
 
-/* Track-length estimator (GateTLEDoseActor::ScoreTLEDepositStep,
-   GateTLEDoseActor.cpp:249-299): the straight path [p, p + len d) of a photon
-   of energy e scores e * mu_en(E, material) * length in every voxel it
-   crosses (Amanatides-Woo voxel walk; ties: x, then y, then z). */
-static void tle_path(const scene_t *s, const real p[3], const real d[3], real len, real e, eidx_t ei,
-                     hlist_t *l, tally_t *t) {
+/* Voxel walk (Amanatides-Woo) of the straight path [p, p + len d) inside the
+   image: visit(ctx, v, m, length) for every voxel crossed, in order (ties:
+   x, then y, then z). */
+typedef void (*visit_fn)(void *ctx, uint32_t v, int m, real seg);
+
+static void voxel_walk(const scene_t *s, const real p[3], const real d[3], real len, visit_fn visit, void *ctx) {
   const int n0 = s->nx, n1 = s->ny, n2 = s->nz;
   int i0 = (int)((p[0] - s->bmin[0]) * s->inv_sp[0]);
   int i1 = (int)((p[1] - s->bmin[1]) * s->inv_sp[1]);
@@ -1504,12 +1527,7 @@ static void tle_path(const scene_t *s, const real p[3], const real d[3], real le
     const real seg = te - tc;
     if (seg > R(0)) {
       const uint32_t v = (uint32_t)i0 + (uint32_t)n0 * ((uint32_t)i1 + (uint32_t)n1 * (uint32_t)i2);
-      const int m = s->labels[v];
-      real mu = interp_row(s->muen + (size_t)s->mat_comp[m] * s->n_e, ei);
-      mu = s->mat_rho[m] * mu;
-      real ed = e * mu;
-      ed = ed * seg;
-      deposit(l, t, v, ed);
+      visit(ctx, v, (int)s->labels[v], seg);
     }
     tc = te;
     if (!(tc < len)) break;
@@ -1529,6 +1547,120 @@ static void tle_path(const scene_t *s, const real p[3], const real d[3], real le
   }
 }
 
+typedef struct {
+  const scene_t *s;
+  real e;
+  eidx_t ei;
+  hlist_t *l;
+  tally_t *t;
+  real tau;
+} walk_ctx_t;
+
+static void tle_visit(void *c, uint32_t v, int m, real seg) {
+  walk_ctx_t *w = (walk_ctx_t *)c;
+  real mu = interp_row(w->s->muen + (size_t)w->s->mat_comp[m] * w->s->n_e, w->ei);
+  mu = w->s->mat_rho[m] * mu;
+  real ed = w->e * mu;
+  ed = ed * seg;
+  deposit(w->l, w->t, v, ed);
+}
+
+static void depth_visit(void *c, uint32_t v, int m, real seg) {
+  (void)v;
+  walk_ctx_t *w = (walk_ctx_t *)c;
+  real mu = interp_row(w->s->sig + (size_t)w->s->mat_comp[m] * w->s->n_e, w->ei);
+  mu = w->s->mat_rho[m] * mu;
+  mu = mu * seg;
+  w->tau = w->tau + mu;
+}
+
+/* Track-length estimator (GateTLEDoseActor::ScoreTLEDepositStep,
+   GateTLEDoseActor.cpp:249-299): the straight path [p, p + len d) of a photon
+   of energy e scores e * mu_en(E, material) * length in every voxel it
+   crosses. */
+static void tle_path(const scene_t *s, const real p[3], const real d[3], real len, real e, eidx_t ei,
+                     hlist_t *l, tally_t *t) {
+  walk_ctx_t c = {s, e, ei, l, t, R(0)};
+  voxel_walk(s, p, d, len, tle_visit, &c);
+}
+
+/* optical depth of [p, p + len d) inside the image */
+static real image_depth(const scene_t *s, const real p[3], const real d[3], real len, eidx_t ei) {
+  walk_ctx_t c = {s, R(0), ei, NULL, NULL, R(0)};
+  voxel_walk(s, p, d, len, depth_visit, &c);
+  return c.tau;
+}
+
+/* Free flight outside the heads (GateGammaFreeFlightOptn, heads excluded): no
+   interaction; straight to the nearest head entry (the head just left
+   excluded) with the weight multiplied by exp(-optical depth); photons at or
+   below a cutoff, or missing every head, stop. */
+static void ff_step(const scene_t *s, photon_t *ph, tally_t *t) {
+  t->cnt[GG_CNT_WORLD_STEPS]++;
+  if (ph->e <= s->ff_ecut || ph->w <= s->ff_wcut) {
+    ph->alive = 0;
+    t->cnt[GG_CNT_ESCAPED]++;
+    return;
+  }
+  real tb = R(INFINITY);
+  int box = 0;
+  real hlo[3] = {-s->half_w, -s->half_w, R(0)};
+  real hhi[3] = {s->half_w, s->half_w, s->zb[3]};
+  for (int h = 0; h < s->n_heads; ++h) {
+    if (ph->exclude == 1 + h) continue;
+    real lp[3], ld[3];
+    to_local(s, h, ph->pos, ph->dir, lp, ld);
+    real th = entry_distance(lp, ld, hlo, hhi);
+    if (th < tb) {
+      tb = th;
+      box = 1 + h;
+    }
+  }
+  real wlo[3] = {-s->whalf[0], -s->whalf[1], -s->whalf[2]};
+  const real tout = exit_distance(ph->pos, ph->dir, wlo, s->whalf);
+  if (!(tb <= tout)) {
+    ph->alive = 0;
+    t->cnt[GG_CNT_ESCAPED]++;
+    return;
+  }
+  const int wm = s->world_mat;
+  real mu_air = interp_row(s->sig + (size_t)s->mat_comp[wm] * s->n_e, ph->ei);
+  mu_air = s->mat_rho[wm] * mu_air;
+  real l_air = tb;
+  real tau = R(0);
+  const real t0 = entry_distance(ph->pos, ph->dir, s->bmin, s->bmax);
+  if (t0 < tb) {
+    real p0[3];
+    for (int a = 0; a < 3; ++a) p0[a] = ph->pos[a] + t0 * ph->dir[a];
+    real lin = exit_distance(p0, ph->dir, s->bmin, s->bmax);
+    const real rest = tb - t0;
+    lin = lin < rest ? lin : rest;
+    tau = image_depth(s, p0, ph->dir, lin, ph->ei);
+    l_air = l_air - lin;
+  }
+  real ta = mu_air * l_air;
+  tau = tau + ta;
+  ph->w = ph->w * ggo_exp(-tau);
+  if (ph->w <= s->ff_wcut) {
+    ph->alive = 0;
+    t->cnt[GG_CNT_ESCAPED]++;
+    return;
+  }
+  move(ph->pos, ph->dir, tb);
+  const int h = box - 1;
+  real lp[3], ld[3];
+  to_local(s, h, ph->pos, ph->dir, lp, ld);
+  for (int a = 0; a < 3; ++a) {
+    ph->pos[a] = lp[a];
+    ph->dir[a] = ld[a];
+  }
+  ph->in_image = 0;
+  ph->in_head = 1;
+  ph->head = h;
+  ph->hreg = lp[2] < s->zb[1] ? 0 : (lp[2] < s->zb[2] ? 1 : 2);
+  ph->left_hole = 0;
+}
+
 static void transport_photon(const scene_t *s, photon_t *ph, rng_t *g, tally_t *t, hlist_t *l,
                              photon_t *sec, int *has_sec, event_t *ev) {
   int steps = 0;
@@ -1538,6 +1670,10 @@ static void transport_photon(const scene_t *s, photon_t *ph, rng_t *g, tally_t *
       t->cnt[GG_CNT_LOOP_CAPPED]++;
       ph->alive = 0;
       break;
+    }
+    if (s->ff && !ph->in_head) {
+      ff_step(s, ph, t);
+      continue;
     }
     if (ph->in_image) {
       if (s->tle && ph->e <= s->tle_thr && ph->e <= s->tle_emin) {
@@ -1916,12 +2052,20 @@ int GGO_PREFIX(run_dose_tle)(const gg_tables_desc *tb, const gg_volume_desc *vol
 static int run_spect_impl(const gg_tables_desc *tb, const gg_volume_desc *vol, const gg_world_desc *w,
                           const gg_source_desc *src, const gg_spect_desc *sp, const double *frames,
                           uint64_t seed, uint64_t first, uint64_t n_per_run, int n_threads, uint64_t *proj,
-                          uint64_t *counters, const arf_t *arf) {
+                          uint64_t *counters, const arf_t *arf, const gg_ff_desc *ff, uint64_t *wproj,
+                          uint64_t *wproj2) {
   scene_t s;
   scene_init(&s, tb, vol, w, src);
   spect_init(&s, sp);
   s.proj = proj;
   s.arf = arf;
+  if (ff && ff->enabled) {
+    s.ff = 1;
+    s.ff_wcut = (real)ff->weight_cutoff;
+    s.ff_ecut = (real)ff->energy_cutoff;
+    s.wproj = wproj;
+    s.wproj2 = wproj2;
+  }
   if (n_threads < 1) n_threads = 1;
   worker_t *ws = (worker_t *)calloc((size_t)n_threads, sizeof(worker_t));
   pthread_t *th = (pthread_t *)calloc((size_t)n_threads, sizeof(pthread_t));
@@ -2120,7 +2264,18 @@ int GGO_PREFIX(run_spect)(const gg_tables_desc *tb, const gg_volume_desc *vol, c
                           const gg_source_desc *src, const gg_spect_desc *sp, const double *frames,
                           uint64_t seed, uint64_t first, uint64_t n_per_run, int n_threads, uint64_t *proj,
                           uint64_t *counters) {
-  return run_spect_impl(tb, vol, w, src, sp, frames, seed, first, n_per_run, n_threads, proj, counters, NULL);
+  return run_spect_impl(tb, vol, w, src, sp, frames, seed, first, n_per_run, n_threads, proj, counters, NULL, NULL,
+                        NULL, NULL);
+}
+
+/* run_spect with free flight outside the heads: weighted projection
+   (2^-32 units) and its history-by-history squares (low 32 bits, rest). */
+int GGO_PREFIX(run_spect_ff)(const gg_tables_desc *tb, const gg_volume_desc *vol, const gg_world_desc *w,
+                             const gg_source_desc *src, const gg_spect_desc *sp, const double *frames,
+                             const gg_ff_desc *ff, uint64_t seed, uint64_t first, uint64_t n_per_run, int n_threads,
+                             uint64_t *wproj, uint64_t *wproj2, uint64_t *proj, uint64_t *counters) {
+  return run_spect_impl(tb, vol, w, src, sp, frames, seed, first, n_per_run, n_threads, proj, counters, NULL, ff,
+                        wproj, wproj2);
 }
 
 /* SPECT with ARF detectors (the GPU's gg_spect_use_arf): as run_spect, with
@@ -2165,7 +2320,8 @@ int GGO_PREFIX(run_spect_arf)(const gg_tables_desc *tb, const gg_volume_desc *vo
   a->dc = (real)m->distance_to_crystal;
   a->proj = arf_proj;
   a->proj2 = arf_proj2;
-  int st = run_spect_impl(tb, vol, w, src, sp, frames, seed, first, n_per_run, n_threads, proj, counters, a);
+  int st = run_spect_impl(tb, vol, w, src, sp, frames, seed, first, n_per_run, n_threads, proj, counters, a, NULL,
+                          NULL, NULL);
   free(a);
   return st;
 }

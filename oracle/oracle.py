@@ -206,6 +206,36 @@ def run_spect(scene, spect, n_per_run, seed, first=0, threads=1, precision=32):
     return proj.astype(np.float64).reshape(shape), {name: int(cnt[i]) for i, name in enumerate(C.COUNTER_NAMES)}
 
 
+def run_spect_ff(scene, spect, n_per_run, seed, first=0, threads=1, precision=32):
+    """Oracle SPECT run with free flight outside the heads (spect.free_flight):
+    (weighted projection, its history-by-history squares, counters), projection layout."""
+    L = lib(precision)
+    fn = getattr(L, f"ggo{precision}_run_spect_ff")
+    fn.restype = ctypes.c_int
+    fn.argtypes = [ctypes.POINTER(C.TablesDesc), ctypes.POINTER(C.VolumeDesc), ctypes.POINTER(C.WorldDesc),
+                   ctypes.POINTER(C.SourceDesc), ctypes.POINTER(C.SpectDesc), ctypes.POINTER(ctypes.c_double),
+                   ctypes.POINTER(C.FfDesc), ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int,
+                   ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64),
+                   ctypes.POINTER(ctypes.c_uint64)]
+    shape = spect.projection_shape()
+    n = int(np.prod(shape))
+    wproj = np.zeros(n, dtype=np.uint64)
+    wproj2 = np.zeros(2 * n, dtype=np.uint64)
+    proj = np.zeros(n, dtype=np.uint64)
+    cnt = np.zeros(C.GG_N_COUNTERS, dtype=np.uint64)
+    desc = spect.desc()
+    frames = spect.all_frames()
+    st = _with_blur(L, precision, spect, lambda: fn(
+        *_descs(scene), ctypes.byref(desc), C.ptr(frames, ctypes.c_double), ctypes.byref(spect.free_flight), seed,
+        first, n_per_run, threads, C.ptr(wproj, ctypes.c_uint64), C.ptr(wproj2, ctypes.c_uint64),
+        C.ptr(proj, ctypes.c_uint64), C.ptr(cnt, ctypes.c_uint64)))
+    if st != 0:
+        raise RuntimeError(f"oracle SPECT free-flight run failed with status {st}")
+    w = wproj.astype(np.float64) * 2.0 ** -32
+    w2 = wproj2[1::2].astype(np.float64) * 2.0 ** -32 + wproj2[0::2].astype(np.float64) * 2.0 ** -64
+    return w.reshape(shape), w2.reshape(shape), {name: int(cnt[i]) for i, name in enumerate(C.COUNTER_NAMES)}
+
+
 def find_hole(spect, a1, a2, precision=32):
     L = lib(precision)
     f = getattr(L, f"ggo{precision}_find_hole")

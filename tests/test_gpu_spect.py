@@ -128,3 +128,54 @@ def test_centroid_adder_bit_exact(precision):
     ref, rcnt = O.run_spect(scene, sp, n, seed=31, threads=8, precision=precision)
     np.testing.assert_array_equal(proj, ref)
     assert cnt == rcnt
+
+
+@pytest.mark.parametrize("precision", [32, 64])
+def test_free_flight_bit_exact(precision):
+    """Free flight outside the heads: weighted projections (2^-32 fixed point) and
+    their history-by-history squares identical to the oracle's."""
+    scene, sp, _ = _case("tc99m_lehr")
+    sp.set_free_flight(weight_cutoff=1e-4, energy_cutoff=0.01)
+    n = 400_000
+    from opengate_gb300.engine import SpectEngine
+
+    with SpectEngine(scene, sp, precision=precision) as eng:
+        eng.run(n, 41)
+        w, w2 = eng.weighted_projection(squared=True)
+        cnt = eng.counters()
+        assert eng.projection().sum() == 0  # counts are not scored in free flight
+    rw, rw2, rcnt = O.run_spect_ff(scene, sp, n, seed=41, threads=8, precision=precision)
+    np.testing.assert_array_equal(w, rw)
+    np.testing.assert_array_equal(w2, rw2)
+    assert cnt == rcnt
+    assert w.sum() > 0 and np.all(w2 <= w + 1e-12)  # weights <= 1
+
+
+def test_free_flight_equals_analog_without_attenuation():
+    """In vacuum nothing scatters outside the heads: the weighted free-flight projection
+    and the analog counts estimate the same image in every window (free flight leaves
+    out only what scatters outside the heads, which the reference simulates separately)."""
+    from opengate_gb300 import materials as M
+    from opengate_gb300 import tables as T
+    from opengate_gb300.engine import SpectEngine
+    from opengate_gb300.scene import Scene
+
+    scene, sp, _ = _case("tc99m_lehr", n_runs=1)
+    mats = list(scene.pt.materials)
+    mats[0] = M.MaterialDatabase().get("G4_Galactic")  # label 0 and the world: vacuum
+    vac = np.zeros_like(scene.labels)
+    scene_air = Scene(T.PhysicsTables(mats), vac, scene.spacing, scene.corner, scene.world_half, 0,
+                      scene.source)
+    n = 60_000_000
+    with SpectEngine(scene_air, sp) as eng:
+        eng.run(n, 51)
+        analog = eng.projection()
+    sp.set_free_flight()
+    with SpectEngine(scene_air, sp) as eng:
+        eng.run(n, 52)
+        ff, ff2 = eng.weighted_projection(squared=True)
+    for k in range(sp.n_windows):
+        a, f = analog[:, k].sum(), ff[:, k].sum()
+        sigma = np.sqrt(a + ff2[:, k].sum())
+        assert abs(a - f) < 4 * sigma + 1e-9, (k, a, f, sigma)
+    assert analog[:, 0].sum() > 2000
