@@ -440,7 +440,7 @@ static int arf_alloc(gg_ctx *c, int tiles) {
     if ((st = c->cuda(cudaMalloc(&c->d_adam_m, gg::kNParams * sizeof(float)), "cudaMalloc"))) return st;
     if ((st = c->cuda(cudaMalloc(&c->d_adam_v, gg::kNParams * sizeof(float)), "cudaMalloc"))) return st;
     if ((st = c->cuda(cudaMalloc(&c->d_grad, gg::kNParams * sizeof(float)), "cudaMalloc"))) return st;
-    if ((st = c->cuda(cudaMalloc(&c->d_wbf, gg::kNBf * sizeof(__nv_bfloat16)), "cudaMalloc"))) return st;
+    if ((st = c->cuda(cudaMalloc(&c->d_wbf, gg::kNBfAll * sizeof(__nv_bfloat16)), "cudaMalloc"))) return st;
     if ((st = c->cuda(cudaMalloc(&c->d_loss_acc, 1024 * sizeof(double)), "cudaMalloc"))) return st;
   }
   if (tiles > c->partial_tiles) {

@@ -70,8 +70,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spect_arf(Scene<real> s, ArfS
     n_net = 0;
     n_fb = 0;
   }
-  tc_net_load(sm, a.params, a.wbf);
-  tc_net_setup(sm);
+  const bool ready = tc_net_prepare(sm, a.params, a.wbf + kTcBf);
 
   const PQueue<real> in = PQueue<real>::carve(a.in_q, a.q_cap);
   const PQueue<real> out = PQueue<real>::carve(a.out_q, a.q_cap);
@@ -83,7 +82,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spect_arf(Scene<real> s, ArfS
   uint32_t phase = 0;
   unsigned int my_net = 0, my_fb = 0;
 
+  if (!ready && threadIdx.x == 0) atomicOr(a.status, kStatusWaitTimeout);
   for (;;) {
+    if (!ready) break;
     // ---- claim a tile of 128 queued photons for the group ----
     if (r == 0) sm.claim[g] = atomicAdd(a.claim, (unsigned long long)kTcRows);
     named_bar(bar, kTcRows);

@@ -199,19 +199,17 @@ __global__ void k_mlp_adam(MlpAdamArgs a) {
   const float mh = m * a.c1, vh = v * a.c2;
   const float w = a.params[p] - a.lr * mh / (sqrtf(vh) + a.eps);
   a.params[p] = w;
-  if (p >= kOffW2 && p < kOffB2) a.wbf[kBfW2 + (p - kOffW2)] = __float2bfloat16_rn(w);
-  else if (p >= kOffW3 && p < kOffB3) a.wbf[kBfW3 + (p - kOffW3)] = __float2bfloat16_rn(w);
-  else if (p >= kOffW4 && p < kOffB4) a.wbf[kBfW4 + (p - kOffW4)] = __float2bfloat16_rn(w);
+  bf16_store_weight(a.wbf, p, w);
 }
 
 // BF16 copies of W2 / W3 / W4 from the FP32 parameters.
 __global__ void k_mlp_to_bf16(const float *params, __nv_bfloat16 *wbf) {
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e < kHid * kHid) {
-    wbf[kBfW2 + e] = __float2bfloat16_rn(params[kOffW2 + e]);
-    wbf[kBfW3 + e] = __float2bfloat16_rn(params[kOffW3 + e]);
+    bf16_store_weight(wbf, kOffW2 + e, params[kOffW2 + e]);
+    bf16_store_weight(wbf, kOffW3 + e, params[kOffW3 + e]);
   }
-  if (e < kOutPad * kHid) wbf[kBfW4 + e] = __float2bfloat16_rn(params[kOffW4 + e]);
+  if (e < kOutPad * kHid) bf16_store_weight(wbf, kOffW4 + e, params[kOffW4 + e]);
 }
 
 // Class probabilities of n rows on the 5th-generation tensor cores
@@ -220,12 +218,13 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     k_mlp_predict(MlpTrainArgs a, float *out, uint64_t n, unsigned int *status) {
   extern __shared__ __align__(1024) unsigned char tc_smem_raw[];
   TcNetSmem &sm = *reinterpret_cast<TcNetSmem *>(tc_smem_raw);
-  tc_net_load(sm, a.params, a.wbf);
-  tc_net_setup(sm);
+  const bool ready = tc_net_prepare(sm, a.params, a.wbf + kTcBf);
   const int g = threadIdx.x >> 7, r = threadIdx.x & 127;
   uint32_t phase = 0;
   const uint64_t n_tiles = (n + kTcRows - 1) / kTcRows;
-  for (uint64_t t = (uint64_t)blockIdx.x * kTcGroups + g; t < n_tiles; t += (uint64_t)gridDim.x * kTcGroups) {
+  if (!ready && threadIdx.x == 0) atomicOr(status, kStatusWaitTimeout);
+  for (uint64_t t = (uint64_t)blockIdx.x * kTcGroups + g; ready && t < n_tiles;
+       t += (uint64_t)gridDim.x * kTcGroups) {
     const uint64_t row = t * kTcRows + r;
     const float4 v = row < n ? a.rows[row] : make_float4(0.f, 0.f, 0.f, 0.f);
     const float x0 = (v.y - a.mean[0]) * a.inv_std[0];

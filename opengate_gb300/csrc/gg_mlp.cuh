@@ -37,13 +37,37 @@ constexpr int kOffW4 = kOffB3 + kHid;            // [16][128] (rows >= n_classes
 constexpr int kOffB4 = kOffW4 + kOutPad * kHid;  // [16]
 constexpr int kNParams = kOffB4 + kOutPad;       // 35600
 
-// BF16 weight copies used by the tensor cores: W2, W3, W4 back to back
+// BF16 weight copies used by the tensor cores: W2, W3, W4 back to back,
+// row-major [out][in] (the training kernel's ldmatrix operands), then the same
+// three matrices again as 5th-generation tensor-core operands (K-major core
+// matrices, gg_tc.cuh) starting at element kTcBf, so that one bulk copy per
+// matrix stages them in shared memory
 constexpr int kBfW2 = 0;
 constexpr int kBfW3 = kHid * kHid;
 constexpr int kBfW4 = 2 * kHid * kHid;
 constexpr int kNBf = 2 * kHid * kHid + kOutPad * kHid;
+constexpr int kTcBf = kNBf;
+constexpr int kNBfAll = 2 * kNBf;
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// Element offset of W(n, k) (n < rows, k < kHid) in the tensor-core copy of a
+// matrix: the byte offset of the K-major core-matrix layout / 2.
+__host__ __device__ constexpr int tc_elem(int n, int k) {
+  return (n >> 3) * (kHid / 8) * 64 + (k >> 3) * 64 + (n & 7) * 8 + (k & 7);
+}
+
+// Stores parameter p (a weight of W2, W3 or W4, value w) as BF16 in both copies.
+__device__ __forceinline__ void bf16_store_weight(__nv_bfloat16 *wbf, int p, float w) {
+  const __nv_bfloat16 b = __float2bfloat16_rn(w);
+  int base, tc, q;
+  if (p >= kOffW2 && p < kOffB2) base = kBfW2, tc = kTcBf + kBfW2, q = p - kOffW2;
+  else if (p >= kOffW3 && p < kOffB3) base = kBfW3, tc = kTcBf + kBfW3, q = p - kOffW3;
+  else if (p >= kOffW4 && p < kOffB4) base = kBfW4, tc = kTcBf + kBfW4, q = p - kOffW4;
+  else return;
+  wbf[base + q] = b;
+  wbf[tc + tc_elem(q / kHid, q % kHid)] = b;
+}
 
 __device__ __forceinline__ void ldsm_x4(uint32_t (&r)[4], const void *p) {
   asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0, %1, %2, %3}, [%4];\n"

@@ -42,6 +42,7 @@ struct TcNetSmem {
   alignas(1024) uint8_t act[kTcGroups][kTcBytesHid]; // A operand of each group: [row][unit]
   float w1[kHid * 3], b1[kHid], b2[kHid], b3[kHid], b4[kOutPad];
   uint64_t mbar[kTcGroups];
+  uint64_t mbar_load;                                 // bulk copy of the weight operands
   unsigned long long claim[kTcGroups];
   uint32_t tmem_base;
 };
@@ -63,20 +64,25 @@ __device__ __forceinline__ bool named_bar_any(int id, int count, bool pred) {
   return out != 0u;
 }
 
-// Weights into shared memory: BF16 W2, W3, W4 as B operands (one 16-byte
-// chunk = 8 inputs of one output per store), layer 1 and the biases in FP32.
-// `wbf` is 16-byte aligned.
-__device__ __forceinline__ void tc_net_load(TcNetSmem &sm, const float *params, const __nv_bfloat16 *wbf) {
-  const uint4 *src = reinterpret_cast<const uint4 *>(wbf);
-  constexpr int kChunksRow = kHid / 8;
-  for (int c = threadIdx.x; c < kHid * kChunksRow; c += blockDim.x) {
-    const int n = c / kChunksRow, k = (c % kChunksRow) * 8;
-    *reinterpret_cast<uint4 *>(sm.w2 + tc_offset(n, k, kHid)) = src[kBfW2 / 8 + c];
-    *reinterpret_cast<uint4 *>(sm.w3 + tc_offset(n, k, kHid)) = src[kBfW3 / 8 + c];
+// Weights into shared memory and the CTA's tensor memory; every thread of the
+// CTA calls it.  W2, W3, W4 arrive as three bulk asynchronous copies of their
+// tensor-core copies (`wtc`, the K-major core-matrix layout, 16-byte aligned)
+// completing on one mbarrier; layer 1 and the biases are plain FP32 loads.
+// Warp 0 allocates kTcCols TMEM columns.  False (for every thread) when the
+// copies did not complete within the bounded wait.
+__device__ __forceinline__ bool tc_net_prepare(TcNetSmem &sm, const float *params, const __nv_bfloat16 *wtc) {
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int g = 0; g < kTcGroups; ++g) mbar_init(&sm.mbar[g], 1u);
+    mbar_init(&sm.mbar_load, 1u);
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
   }
-  for (int c = threadIdx.x; c < kOutPad * kChunksRow; c += blockDim.x) {
-    const int n = c / kChunksRow, k = (c % kChunksRow) * 8;
-    *reinterpret_cast<uint4 *>(sm.w4 + tc_offset(n, k, kHid)) = src[kBfW4 / 8 + c];
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    mbar_expect_tx(&sm.mbar_load, (uint32_t)(2 * kTcBytesHid + kTcBytesOut));
+    bulk_load(sm.w2, wtc + kBfW2, (uint32_t)kTcBytesHid, &sm.mbar_load);
+    bulk_load(sm.w3, wtc + kBfW3, (uint32_t)kTcBytesHid, &sm.mbar_load);
+    bulk_load(sm.w4, wtc + kBfW4, (uint32_t)kTcBytesOut, &sm.mbar_load);
   }
   for (int e = threadIdx.x; e < kHid * 3; e += blockDim.x) sm.w1[e] = params[kOffW1 + e];
   for (int e = threadIdx.x; e < kHid; e += blockDim.x) {
@@ -85,23 +91,16 @@ __device__ __forceinline__ void tc_net_load(TcNetSmem &sm, const float *params, 
     sm.b3[e] = params[kOffB3 + e];
   }
   for (int e = threadIdx.x; e < kOutPad; e += blockDim.x) sm.b4[e] = params[kOffB4 + e];
-}
-
-// mbarriers and the CTA's TMEM columns; every thread of the CTA calls it after tc_net_load.
-__device__ __forceinline__ void tc_net_setup(TcNetSmem &sm) {
-  if (threadIdx.x == 0) {
-#pragma unroll
-    for (int g = 0; g < kTcGroups; ++g) mbar_init(&sm.mbar[g], 1u);
-    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
-  }
   if (threadIdx.x < 32) {
     tmem_alloc(&sm.tmem_base, kTcCols);
     tmem_relinquish();
   }
-  fence_async_smem();
+  bool ok = mbar_wait(&sm.mbar_load, 0u, kTcWaitLimit);
+  if (!ok) mbar_wait(&sm.mbar_load, 0u, kTcWaitLimit);  // let the copies land before the CTA can leave
   tc_fence_before();
-  __syncthreads();
+  ok = __syncthreads_and(ok) != 0;
   tc_fence_after();
+  return ok;
 }
 
 // Frees the TMEM columns; every thread of the CTA calls it once its group is done.

@@ -97,6 +97,19 @@ __device__ __forceinline__ void tc_commit(uint64_t *mbar) {
                : "memory");
 }
 
+// ---- bulk asynchronous copy (TMA engine), global -> shared, completion on an mbarrier ----
+// Both addresses 16-byte aligned, size a multiple of 16 bytes.
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *mbar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(tc_smem(mbar)), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void bulk_load(void *dst_smem, const void *src_gmem, uint32_t bytes, uint64_t *mbar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
+                   tc_smem(dst_smem)),
+               "l"(src_gmem), "r"(bytes), "r"(tc_smem(mbar))
+               : "memory");
+}
+
 // ---- mbarrier ----
 __device__ __forceinline__ void mbar_init(uint64_t *mbar, uint32_t count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(tc_smem(mbar)), "r"(count) : "memory");
