@@ -391,7 +391,7 @@ typedef struct {
   uint64_t n_samples;   /* training photons (rows come from gg_arf_dataset of these samples) */
   uint64_t seed;        /* dataset seed (Philox stream 1) */
   uint64_t init_seed;   /* weight initialisation (He-uniform) */
-  int32_t batch;        /* rows per Adam step, a multiple of 64, <= 65536 */
+  int32_t batch;        /* rows per Adam step, a multiple of 128, <= 65536 */
   int32_t epochs;
   float lr, beta1, beta2, eps;
   float lr_final;       /* learning rate decays exponentially from lr to lr_final over the steps (0: constant) */
@@ -411,7 +411,7 @@ int gg_arf_get_params(gg_ctx *ctx, float *params, size_t n);
 /* Network outputs (softmax, before the class-0 re-weighting) of n rows
    (E, theta, phi, -) -> probs[n][n_classes]. */
 int gg_arf_predict(gg_ctx *ctx, const float *rows, uint64_t n, float *probs);
-/* Gradient of the mean cross-entropy of n rows (n a multiple of 64) at the
+/* Gradient of the mean cross-entropy of n rows (n a multiple of 128) at the
    current parameters, no update: grad[GG_ARF_N_PARAMS], *loss = mean loss. */
 int gg_arf_gradient(gg_ctx *ctx, const float *rows, uint64_t n, float *grad, double *loss);
 

@@ -500,6 +500,7 @@ static gg::MlpTrainArgs arf_args(const gg_ctx *c) {
     a.inv_std[k] = 1.0f / c->arf.x_std[k];
   }
   a.n_classes = c->arf.n_classes;
+  a.status = c->d_status;
   return a;
 }
 
@@ -1372,8 +1373,9 @@ int gg_arf_gradient(gg_ctx *c, const float *rows, uint64_t n, float *grad, doubl
   if (!c || !rows || !grad) return GG_ERR_ARG;
   cudaSetDevice(c->device);
   if (!c->have_arf) return c->fail(GG_ERR_STATE, "gg_arf_gradient: no ARF model");
-  if (n == 0 || n % gg::kTileM || n > 65536) return c->fail(GG_ERR_ARG, "gg_arf_gradient: n must be a multiple of 64, <= 65536");
-  const int tiles = (int)(n / gg::kTileM);
+  if (n == 0 || n % gg::kTrainRows || n > 65536)
+    return c->fail(GG_ERR_ARG, "gg_arf_gradient: n must be a multiple of 128, <= 65536");
+  const int tiles = (int)(n / gg::kTrainRows);
   int st;
   if ((st = arf_alloc(c, tiles)) || (st = io_alloc(c, (size_t)n))) return st;
   if ((st = c->h2d(c->d_io_rows, rows, n * sizeof(float4), "upload"))) return st;
@@ -1404,7 +1406,7 @@ int gg_arf_gradient(gg_ctx *c, const float *rows, uint64_t n, float *grad, doubl
     for (float v : lp) sum += v;
     *loss = sum / (double)n;
   }
-  return GG_OK;
+  return check_tc_status(c, "gg_arf_gradient");
 }
 
 int gg_arf_train(gg_ctx *c, const gg_arf_sampling *smp, const gg_arf_train_opts *o, gg_arf_model *model_out,
@@ -1413,9 +1415,9 @@ int gg_arf_train(gg_ctx *c, const gg_arf_sampling *smp, const gg_arf_train_opts 
   cudaSetDevice(c->device);
   if (!c->have_tables || !c->have_spect)
     return c->fail(GG_ERR_STATE, "gg_arf_train: upload the tables and call gg_spect_setup first");
-  if (o->batch < gg::kTileM || o->batch % gg::kTileM || o->batch > 65536 || o->epochs < 1 || o->epochs > 1024 ||
+  if (o->batch < gg::kTrainRows || o->batch % gg::kTrainRows || o->batch > 65536 || o->epochs < 1 || o->epochs > 1024 ||
       !(o->lr > 0.0f) || o->n_samples == 0)
-    return c->fail(GG_ERR_ARG, "gg_arf_train: batch a multiple of 64 (<= 65536), 1..1024 epochs, lr > 0, samples > 0");
+    return c->fail(GG_ERR_ARG, "gg_arf_train: batch a multiple of 128 (<= 65536), 1..1024 epochs, lr > 0, samples > 0");
   // training rows on the device
   uint64_t n_rows = 0;
   {
@@ -1447,7 +1449,7 @@ int gg_arf_train(gg_ctx *c, const gg_arf_sampling *smp, const gg_arf_train_opts 
   if ((st = arf_model_check(c, &m))) return st;
   std::vector<float> w0 = arf_init_params(o->init_seed, m.n_classes);
   if ((st = gg_arf_set_model(c, &m, w0.data()))) return st;
-  const int tiles = o->batch / gg::kTileM;
+  const int tiles = o->batch / gg::kTrainRows;
   if ((st = arf_alloc(c, tiles))) return st;
   if ((st = c->cuda(cudaMemsetAsync(c->d_adam_m, 0, gg::kNParams * sizeof(float), c->stream), "memset"))) return st;
   if ((st = c->cuda(cudaMemsetAsync(c->d_adam_v, 0, gg::kNParams * sizeof(float), c->stream), "memset"))) return st;
@@ -1489,6 +1491,7 @@ int gg_arf_train(gg_ctx *c, const gg_arf_sampling *smp, const gg_arf_train_opts 
                     "download")))
     return st;
   if ((st = c->cuda(cudaStreamSynchronize(c->stream), "ARF training"))) return st;
+  if ((st = check_tc_status(c, "gg_arf_train"))) return st;
   if (loss)
     for (int ep = 0; ep < o->epochs; ++ep) loss[ep] = lacc[ep] / ((double)steps_per_epoch * o->batch);
   if (model_out) *model_out = m;

@@ -58,7 +58,7 @@ struct ArfArgs {
 // One training step (or a prediction) of the ARF network (see gg_mlp.cu).
 struct MlpTrainArgs {
   const float4 *rows;            // (E, theta, phi, class) rows
-  uint64_t row0, n_rows;         // tile t reads rows (row0 + 64 t + r) % n_rows
+  uint64_t row0, n_rows;         // tile t reads rows (row0 + 128 t + r) % n_rows
   const float *params;           // FP32 parameters
   const __nv_bfloat16 *wbf;      // BF16 copies of W2, W3, W4
   float *partial;                // [tiles][kNParams] gradient of each tile
@@ -66,7 +66,10 @@ struct MlpTrainArgs {
   float mean[3], inv_std[3];     // standardisation of (theta, phi, E)
   int n_classes;
   float inv_batch;               // 1 / rows in the step
+  unsigned int *status;          // kStatusWaitTimeout when a tensor-core wait ran out
 };
+
+constexpr int kTrainRows = 128;  // rows per training tile (one CTA, MMA M)
 
 struct MlpAdamArgs {
   const float *partial;
@@ -103,7 +106,7 @@ struct ArfStageArgs {
   unsigned long long *claim;       // chunk claim counter, zero at launch
 };
 
-size_t mlp_smem_bytes();
+size_t mlp_train_smem_bytes();
 cudaError_t launch_mlp_train(const MlpTrainArgs &a, int n_tiles, cudaStream_t st);
 cudaError_t launch_mlp_adam(const MlpAdamArgs &a, cudaStream_t st);
 cudaError_t launch_mlp_to_bf16(const float *params, __nv_bfloat16 *wbf, cudaStream_t st);
