@@ -16,6 +16,7 @@ Geant4 stack cannot be installed here) on all host cores.
 """
 
 import argparse
+import copy
 import json
 import math
 import os
@@ -52,6 +53,12 @@ BATCH_WORKLOAD = "batched_48_slab_phantoms_32-128vox_1-3mm_mono_0.05-2MeV_1e5-1e
 # collimator, 120 gantry positions, 1e10 decays; the network is trained on
 # 2e8 photons of the plain collimator tracking, and the plain acquisition of
 # the same decays is run beside it for the matched-sigma comparison
+FF_METRIC = ("primaries/s (free-flight SPECT recipe: primary free-flight pass + scatter-splitting pass, "
+             "SPECT projections)")
+FF_DECAYS = 100_000_000
+FF_SPLIT = (50, 10, 10000, 10.0)  # Compton, Rayleigh factors, max Compton level, angle tolerance (deg)
+FF_CHUNKS = 8  # scatter pass in independent chunks: its variance (copies of a history are correlated)
+FF_WORKLOAD = SPECT_WORKLOAD + "_freeflight_primary+scattersplit_c50_r10_aa10deg"
 ARF_METRIC = "primaries/s at matched sigma (ARF GPU vs plain GPU collimator tracking, SPECT projections)"
 ARF_DECAYS = 10_000_000_000
 ARF_YIELD = 0.166
@@ -248,6 +255,16 @@ def reference_workload(args, threads):
                 (" (the reference's CPU method; the network is not part of its CPU path)"
                  if args.workload == "spect_arf" else ""))
         return meta + ("synthetic (seeded CT phantom + activity image)", run, note, 2000 * runs, int(4e8))
+    if args.workload == "spect_ff":
+        scene, sp_p, sp_s = spect_ff_specs()
+        runs = sp_p.n_runs
+
+        def run(n, seed):
+            O.run_spect_ff(scene, sp_p, max(n // runs, 1), seed, threads=threads)
+            O.run_spect_ff(scene, sp_s, max(n // runs, 1), seed + 1, threads=threads)
+
+        return (FF_METRIC, FF_WORKLOAD, int(FF_DECAYS * SPECT_YIELD), "synthetic (seeded CT phantom + activity image)",
+                run, f"primary free flight + scatter splitting over all {runs} positions", 200 * runs, int(4e8))
     if args.workload == "batched":
         _, sims = W.batched_phantoms(seed=args.seed)
         total = int(sum(k for _, k, _ in sims))
@@ -414,6 +431,193 @@ def run_ours_spect(args, ws, rank, local, dist, use_cuda):
         }
         print(json.dumps(line), flush=True)
     eng.close()
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+def spect_ff_specs():
+    """(scene, primary free-flight spec, scatter-splitting spec) of the SPECT workload."""
+    from opengate_gb300 import workloads as W
+
+    scene, sp_p, _ = W.spect_phantom()
+    sp_s = copy.deepcopy(sp_p)
+    sp_p.set_free_flight()
+    nc, nr, lvl, deg = FF_SPLIT
+    sp_s.set_scatter_splitting(nc, nr, lvl, angle_tolerance_max=math.radians(deg))
+    return scene, sp_p, sp_s
+
+
+def run_ours_ff(args, ws, rank, local, dist, use_cuda):
+    """The reference's free-flight SPECT recipe (contrib/spect/spect_config.py:937-1000): a
+    primary pass (GammaFreeFlightActor) and a scatter pass (ScatterSplittingFreeFlightActor),
+    whose weighted projections add up to the acquisition.  value: primaries/s of both passes
+    on the same primaries; sigma: efficiency (1 / sigma^2 T) against the analog SPECT path."""
+    import torch
+
+    from opengate_gb300.engine import SpectEngine
+
+    scene, sp_p, sp_s = spect_ff_specs()
+    runs = sp_p.n_runs
+    n_step = args.primaries if args.primaries != PRIMARIES_PER_STEP else int(FF_DECAYS * SPECT_YIELD)
+    n_per_run = n_step // runs // FF_CHUNKS * FF_CHUNKS
+    n = n_per_run * runs
+    m = n_per_run // FF_CHUNKS
+    eng_p = SpectEngine(scene, sp_p, device=local, precision=32, batch=args.batch)
+    eng_s = SpectEngine(scene, sp_s, device=local, precision=32, batch=args.batch)
+    l2_flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=f"cuda:{local}")
+
+    def first_of(step):
+        return ((rank * (args.warmup + args.steps + 4)) + step) * n
+
+    parts = {}
+
+    def step(first, keep=False):
+        """Both passes; device ms, launches, (primary w, w2, scatter chunk projections) if keep."""
+        ms, nl, chunks = 0.0, 0, []
+        eng_p.reset()
+        eng_s.reset()
+        eng_p.run(n_per_run, args.seed, first)
+        tg, tt, tf, k = eng_p.last_kernel_ms()
+        ms, nl = ms + tg + tt + tf, nl + k
+        parts["primary_pass"] = tg + tt + tf
+        parts["scatter_phantom_stage"] = parts["scatter_head_stage"] = parts["scatter_copies"] = 0.0
+        prev = 0.0
+        for c in range(FF_CHUNKS):
+            eng_s.run(m, args.seed + 1, first + c * m * runs)  # run r of a call: first + r * m
+            tg, tt, tf, k = eng_s.last_kernel_ms()
+            ms, nl = ms + tg + tt + tf, nl + k
+            ph, hd, cp = eng_s.last_stage_ms()
+            parts["scatter_phantom_stage"] += ph
+            parts["scatter_head_stage"] += hd
+            parts["scatter_copies"] += cp
+            if keep:
+                cur = eng_s.weighted_projection()
+                chunks.append(cur - prev)
+                prev = cur
+        return ms, nl, chunks
+
+    for w in range(args.warmup):
+        step(first_of(w))
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    dev_ms, launches = [], 0
+    t0 = time.perf_counter()
+    with ClockSampler(local) as clk:
+        for k in range(args.steps):
+            l2_flush.zero_()
+            torch.cuda.synchronize()
+            ms, nl, _ = step(first_of(args.warmup + k))
+            dev_ms.append(ms)
+            launches += nl
+        torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    if dist:
+        dist.barrier()
+    total_ms = dist_max(dist, float(np.sum(dev_ms)), use_cuda)
+    value = ws * n * args.steps / (total_ms / 1e3)
+    # statistics of one more step: primary pass (w2: one photon, one single) + scatter chunks
+    ms_s, _, chunks = step(first_of(args.warmup + args.steps), keep=True)
+    cnt_s = eng_s.counters()
+    ph_ms = parts["scatter_phantom_stage"]
+    wp, wp2 = eng_p.weighted_projection(squared=True)
+    nw = sp_p.n_windows
+    # per-projection window totals (head, position, window): a photon of the primary pass
+    # scores one single; the scatter pass's variance comes from its independent chunks
+    ch = np.array(chunks).sum(axis=(3, 4))
+    t_ff = wp.sum(axis=(2, 3)) + ch.sum(axis=0)
+    v_ff = wp2.sum(axis=(2, 3)) + FF_CHUNKS * ch.var(axis=0, ddof=1)
+    # analog SPECT path, same primaries (one count per single: variance = counts)
+    sp_a = copy.deepcopy(sp_p)
+    sp_a.set_free_flight(enabled=False)
+    with SpectEngine(scene, sp_a, device=local, precision=32, batch=args.batch) as eng_a:
+        eng_a.run(n_per_run, args.seed + 2, first_of(args.warmup + args.steps + 1))
+        tg, tt, tf, _ = eng_a.last_kernel_ms()
+        ms_a = tg + tt + tf
+        t_a = eng_a.projection().sum(axis=(2, 3))
+
+    def rel(t, v, w):
+        tw, vw = t[:, w::nw], v[:, w::nw]
+        sel = tw > 0
+        return float((np.sqrt(vw[sel]) / tw[sel]).mean())
+
+    sig = {}
+    for w in range(nw):
+        s_ff, s_a = rel(t_ff, v_ff, w), rel(t_a, t_a, w)
+        sig[f"window_{w}"] = {"free_flight": s_ff, "analog": s_a, "ratio_totals": float(t_ff[:, w::nw].sum() /
+                                                                                         t_a[:, w::nw].sum()),
+                              "efficiency_gain_vs_analog": (s_a ** 2 * ms_a) / (s_ff ** 2 * ms_s)}
+
+    # e2e through the C ABI with host buffers: uploads, both passes, weighted projections down
+    h2d = 2 * (scene.labels.nbytes + scene._sig.nbytes + scene._cum.nbytes + scene._ray_amax.nbytes +
+               scene._ray_cum.nbytes + scene.majorant.nbytes + scene.source_desc_bytes() + sp_p.all_frames().nbytes)
+    d2h = 2 * 3 * int(np.prod(sp_p.projection_shape())) * 8
+    torch.cuda.synchronize()
+    e2e_t = []
+    for k in range(max(1, min(args.steps, 2))):
+        t1 = time.perf_counter()
+        eng_p.upload()
+        eng_s.upload()
+        first = first_of(args.warmup + args.steps + 2 + k)
+        eng_p.run(n_per_run, args.seed, first)
+        eng_s.run(n_per_run, args.seed + 1, first)
+        eng_p.weighted_projection(squared=True)
+        eng_s.weighted_projection(squared=True)
+        e2e_t.append(time.perf_counter() - t1)
+    e2e_s = dist_max(dist, float(np.mean(e2e_t)), use_cuda)
+
+    peak_bw, peak_kind = measured_peaks()
+    bytes_alg = 32.0 * cnt_s["woodcock_steps"]
+    achieved = bytes_alg / (ph_ms / 1e3) / 1e9
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak_bw, "unit": "GB/s",
+                "frac": achieved / peak_bw, "traffic": args.traffic, "peak_kind": peak_kind,
+                "kernel": "k_spect_phantom<float, 2, scatter splitting> (scatter pass, phantom stage)",
+                "bytes_alg_per_step": bytes_alg,
+                "note": "label gathers of the analog Woodcock steps only; the copies' free flights "
+                        "(voxel walks of exp(-optical depth)) are latency-bound gathers not counted",
+                "units": dict(cnt_s), "ms_per_step": dict(parts)}
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        from oracle import oracle as O
+
+        threads = os.cpu_count() or 1
+
+        def run(nn, seed):
+            O.run_spect_ff(scene, sp_p, max(nn // runs, 1), seed, threads=threads)
+            O.run_spect_ff(scene, sp_s, max(nn // runs, 1), seed + 1, threads=threads)
+
+        r, ns, dt = grow_sample(run, args.cpu_seconds, 200 * runs, int(4e8))
+        cpu = {"value": r, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"{ns} primaries through both passes over the {runs} positions, {dt:.1f} s on "
+                         f"{threads} host threads"}
+    if rank == 0:
+        line = {
+            "metric": FF_METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded CT phantom + activity image)",
+            "config": {"workload": FF_WORKLOAD, "primaries_per_step": n, "decays_per_step": n / SPECT_YIELD,
+                       "split": {"compton": FF_SPLIT[0], "rayleigh": FF_SPLIT[1], "max_compton_level": FF_SPLIT[2],
+                                 "angle_tolerance_deg": FF_SPLIT[3]},
+                       "l2": "flushed between steps (256 MiB write)", "batch": args.batch,
+                       "parallelism": f"replicas x{ws}, disjoint history ranges"},
+            "sigma": {"mean_relative_uncertainty_of_projection_totals": sig, "analog_ms": ms_a,
+                      "free_flight_ms": ms_s, "primaries": n,
+                      "method": f"per (head, position) window totals; efficiency 1 / (sigma^2 T); primary "
+                                f"pass: history-by-history squares; scatter pass: variance of {FF_CHUNKS} "
+                                f"independent chunks; analog: Poisson"},
+            "e2e": {"value": ws * n / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h)},
+            "roofline": roofline,
+            "cpu_baseline": cpu,
+            "clocks": clk.summary(),
+            "gpu_launches": int(launches),
+            "wall_s": wall,
+        }
+        print(json.dumps(line), flush=True)
+    eng_p.close()
+    eng_s.close()
     if dist:
         dist.destroy_process_group()
     return 0
@@ -820,6 +1024,8 @@ def run_ours(args):
         return run_ours_batched(args, ws, rank, local, dist, use_cuda)
     if args.workload == "tle":
         return run_ours_tle(args, ws, rank, local, dist, use_cuda)
+    if args.workload == "spect_ff":
+        return run_ours_ff(args, ws, rank, local, dist, use_cuda)
     from opengate_gb300 import _capi as C
     from opengate_gb300 import workloads as W
     from opengate_gb300.engine import DoseEngine
@@ -936,11 +1142,12 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="dose", choices=["dose", "spect", "spect_arf", "batched", "tle"],
+    ap.add_argument("--workload", default="dose", choices=["dose", "spect", "spect_arf", "batched", "tle", "spect_ff"],
                     help="dose: CT phantom DoseActor (default); spect: Tc-99m SPECT acquisition, 60 positions; "
                          "spect_arf: Lu-177 SPECT with ARF detectors vs plain tracking, 120 positions; "
                          "batched: 48 uneven dose simulations in one launch sequence; "
-                         "tle: track-length estimator vs analog dose, 64^3 water, 1 MeV pencil")
+                         "tle: track-length estimator vs analog dose, 64^3 water, 1 MeV pencil; "
+                         "spect_ff: free-flight SPECT recipe (primary + scatter splitting) on the spect workload")
     ap.add_argument("--primaries", type=int, default=PRIMARIES_PER_STEP)
     ap.add_argument("--arf-train-samples", type=int, default=ARF_TRAIN_SAMPLES)
     ap.add_argument("--arf-epochs", type=int, default=80)

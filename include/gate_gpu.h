@@ -346,10 +346,34 @@ int gg_spect_set_blur(gg_ctx *ctx, const gg_blur_desc *blur);
    analog.  Singles add their weight (and its history-by-history square)
    to the weighted projection read with gg_get_arf_projection; the counts of
    gg_get_projection stay zero.  Not together with the ARF detector. */
+#define GG_FF_OFF 0
+#define GG_FF_PRIMARY 1 /* GammaFreeFlightActor: no interaction outside the heads */
+#define GG_FF_SCATTER 2 /* ScatterSplittingFreeFlightActor (below) */
+#define GG_MAX_SPLITTING 4096
 typedef struct {
-  int32_t enabled;
+  int32_t enabled;      /* GG_FF_OFF, GG_FF_PRIMARY or GG_FF_SCATTER */
   double weight_cutoff; /* photons with weight <= this stop (reference default -1) */
   double energy_cutoff; /* MeV, photons with energy <= this stop (reference default 0) */
+  /* GG_FF_SCATTER (ScatterSplittingFreeFlightOptrActor, biasing/
+     GateScatterSplittingFreeFlightOptrActor.cpp:200-420, GateScatterSplittingFreeFlightOptn.cpp:
+     ApplyFinalStateBiasing_V1_PostStepDoIt): photons are tracked analog
+     outside the heads and die when they enter one; each of their Compton
+     scatterings (up to max_compton_level of them; the one after that kills
+     the photon) and Rayleigh scatterings is re-sampled compton_splitting /
+     rayleigh_splitting times from the state before it, each copy with
+     1 / factor of the weight and its own random stream, and copies whose
+     line reaches a head fly freely to it (angular acceptance: the heads) and
+     are tracked there as in GG_FF_PRIMARY.  Factors are at most
+     GG_MAX_SPLITTING.  A phantom pass whose copies overflow the head queue
+     is repeated on fewer histories (results do not depend on the pass
+     sizes). */
+  int32_t compton_splitting;
+  int32_t rayleigh_splitting;
+  int32_t max_compton_level;
+  /* angular acceptance, angle check (biasingactors.py generic_source_default_aa
+     angle_tolerance_max): a copy that enters a head more than this many
+     radians off the head's axis is dropped; <= 0: no angle check */
+  double angle_tolerance_max;
 } gg_ff_desc;
 int gg_spect_set_free_flight(gg_ctx *ctx, const gg_ff_desc *ff);
 int gg_spect_set_heads(gg_ctx *ctx, int32_t run, const double *frames);
@@ -429,7 +453,8 @@ int gg_arf_gradient(gg_ctx *ctx, const float *rows, uint64_t n, float *grad, dou
    gg_spect_setup zeroes them. */
 int gg_spect_use_arf(gg_ctx *ctx, int32_t enable);
 /* Device time of the last gg_run / gg_spect_run per SPECT stage (sums of
-   CUDA-event intervals around the stage launches, ms). */
+   CUDA-event intervals around the stage launches, ms); arf_ms holds the ARF
+   stage, or with GG_FF_SCATTER the split and walk kernels of the copies. */
 int gg_last_stage_ms(gg_ctx *ctx, double *phantom_ms, double *head_ms, double *arf_ms);
 int gg_get_arf_projection(gg_ctx *ctx, double *counts, double *squared, size_t n);
 

@@ -63,8 +63,14 @@ class BlurDesc(ctypes.Structure):
     ]
 
 
+FF_OFF, FF_PRIMARY, FF_SCATTER = 0, 1, 2
+MAX_SPLITTING = 4096
+
+
 class FfDesc(ctypes.Structure):
-    _fields_ = [("enabled", ctypes.c_int32), ("weight_cutoff", ctypes.c_double), ("energy_cutoff", ctypes.c_double)]
+    _fields_ = [("enabled", ctypes.c_int32), ("weight_cutoff", ctypes.c_double), ("energy_cutoff", ctypes.c_double),
+                ("compton_splitting", ctypes.c_int32), ("rayleigh_splitting", ctypes.c_int32),
+                ("max_compton_level", ctypes.c_int32), ("angle_tolerance_max", ctypes.c_double)]
 
 
 class TleDesc(ctypes.Structure):

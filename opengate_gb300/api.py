@@ -567,6 +567,68 @@ class GammaFreeFlightActor(GateObject):
                 raise NotImplementedError(f"free flight must exclude the SPECT head '{h.name}' (exclude_volumes)")
 
 
+def _default_angular_acceptance():
+    """Angular-acceptance parameters (biasingactors.py:16-64 generic_source_default_aa)."""
+    return Box({"policy": None, "skip_policy": "SkipEvents", "max_rejection": 10000, "target_volumes": [],
+                "enable_intersection_check": False, "enable_angle_check": False,
+                "angle_check_reference_vector": [0, 0, 1], "angle_check_proximity_distance": 0.0,
+                "angle_tolerance_proximal": 90 * u.deg, "angle_tolerance_min": 0.0,
+                "angle_tolerance_max": 6 * u.deg})
+
+
+class ScatterSplittingFreeFlightActor(GateObject):
+    """Scatter splitting with free flight (ScatterSplittingFreeFlightActor,
+    opengate/actors/biasingactors.py:368-460; GateScatterSplittingFreeFlightOptrActor.cpp:200-420 and
+    GateScatterSplittingFreeFlightOptn.cpp:69-149): attached to the world with the SPECT heads as
+    ``exclude_volumes`` and ``kill_interacting_in_volumes``.  Photons are tracked analog outside the
+    heads and die when they enter one; each Compton (up to ``max_compton_level``, the next one kills
+    the photon) and each Rayleigh scattering is re-sampled ``compton_splitting_factor`` /
+    ``rayleigh_splitting_factor`` times into copies of 1 / factor of the weight that fly freely to
+    the heads.  The projections become weighted sums: the scattered component of the reference's
+    free-flight SPECT recipe (contrib/spect/spect_config.py:937-1000); GammaFreeFlightActor gives
+    the primary one.  Angular acceptance: the intersection check is always applied (a copy that
+    misses every head is dropped); the angle check measures the angle to the axis of the head
+    the copy enters (angle_tolerance_max; no proximity rule)."""
+
+    type_name = "ScatterSplittingFreeFlightActor"
+    user_info_defaults = {"attached_to": "world", "exclude_volumes": [], "kill_interacting_in_volumes": [],
+                          "splitting_factor": 1, "compton_splitting_factor": -1, "rayleigh_splitting_factor": -1,
+                          "max_compton_level": 10, "weight_cutoff": -1.0, "energy_cutoff": 0.0,
+                          "particles": ["gamma"], "priority": 100, "debug": False}
+
+    def __init__(self, name, simulation=None, **kw):
+        super().__init__(name, simulation, **kw)
+        object.__setattr__(self, "angular_acceptance", _default_angular_acceptance())
+
+    def check(self, head_volumes):
+        if self.attached_to != "world":
+            raise NotImplementedError("the GPU path applies scatter splitting to the whole world (attached_to='world')")
+        excluded, killed = set(self.exclude_volumes), set(self.kill_interacting_in_volumes)
+        for h in head_volumes:
+            names = {h.name, h.crystal_name, f"{h.name}_collimator"}
+            if not names & excluded:
+                raise NotImplementedError(f"scatter splitting must exclude the SPECT head '{h.name}' (exclude_volumes)")
+            if not names & killed:
+                raise NotImplementedError(
+                    f"the SPECT head '{h.name}' must be a kill volume (kill_interacting_in_volumes)")
+        aa = self.angular_acceptance
+        if aa.policy not in (None, False, "Rejection"):
+            raise NotImplementedError("angular acceptance: only the 'Rejection' policy (or none)")
+        if aa.policy == "Rejection" and aa.enable_angle_check and (
+                float(aa.angle_check_proximity_distance) != 0.0 or float(aa.angle_tolerance_min) != 0.0):
+            raise NotImplementedError("angular acceptance: angle_tolerance_max only (no proximity, no minimum)")
+
+    def factors(self):
+        """(Compton factor, Rayleigh factor, angle tolerance in radians or 0)."""
+        nc = int(self.compton_splitting_factor)
+        nr = int(self.rayleigh_splitting_factor)
+        nc = int(self.splitting_factor) if nc < 0 else nc
+        nr = int(self.splitting_factor) if nr < 0 else nr
+        aa = self.angular_acceptance
+        tol = float(aa.angle_tolerance_max) / u.rad if aa.policy == "Rejection" and aa.enable_angle_check else 0.0
+        return nc, nr, tol
+
+
 class SimulationStatisticsActor(GateObject):
     type_name = "SimulationStatisticsActor"
     user_info_defaults = {"attached_to": "world", "track_types_flag": False, "output_filename": "auto"}
@@ -632,6 +694,7 @@ class Simulation:
                "SimulationStatisticsActor": SimulationStatisticsActor,
                "DigitizerAdderActor": DigitizerAdderActor,
                "GammaFreeFlightActor": GammaFreeFlightActor,
+               "ScatterSplittingFreeFlightActor": ScatterSplittingFreeFlightActor,
                "DigitizerBlurringActor": DigitizerBlurringActor,
                "DigitizerSpatialBlurringActor": DigitizerSpatialBlurringActor,
                "DigitizerProjectionActor": DigitizerProjectionActor}.get(actor_type)
@@ -732,11 +795,18 @@ class Simulation:
         if half_w:
             sp.half_width = half_w
         ffs = [a for a in self.actors.values() if isinstance(a, GammaFreeFlightActor)]
-        if len(ffs) > 1:
-            raise NotImplementedError("one GammaFreeFlightActor")
+        sss = [a for a in self.actors.values() if isinstance(a, ScatterSplittingFreeFlightActor)]
+        if len(ffs) + len(sss) > 1:
+            raise NotImplementedError("one free-flight actor (GammaFreeFlightActor or ScatterSplittingFreeFlightActor)")
         if ffs:
             ffs[0].check(heads)
             sp.set_free_flight(float(ffs[0].weight_cutoff), float(ffs[0].energy_cutoff) / u.MeV)
+        if sss:
+            ss = sss[0]
+            ss.check(heads)
+            nc, nr, tol = ss.factors()
+            sp.set_scatter_splitting(nc, nr, int(ss.max_compton_level), float(ss.weight_cutoff),
+                                     float(ss.energy_cutoff) / u.MeV, tol)
         # digitizer adder and blurring: one setting shared by every head's crystal
         def set_policy(policy):
             sp.adder_policy = policy

@@ -106,9 +106,20 @@ struct gg_ctx {
   size_t q_cap = 0;
   // ARF stage in the SPECT acquisition
   bool arf_on = false;
-  // free flight outside the heads (gg_spect_set_free_flight)
+  // free flight outside the heads (gg_spect_set_free_flight): ff_mode
+  // GG_FF_PRIMARY or GG_FF_SCATTER (split copies in free flight)
   bool ff_on = false;
+  int ff_mode = GG_FF_OFF;
   double ff_wcut = -1.0, ff_ecut = 0.0;
+  int ss_nc = 0, ss_nr = 0, ss_max = 0;
+  double ss_cos = -2.0;
+  // scatter splitting: histories per phantom pass whose copies fit the head
+  // queue (lowered when a pass overflows), and the counters before a pass
+  uint64_t ss_span = 0;
+  unsigned long long *d_cnt_save = nullptr;
+  void *d_split = nullptr;  // split requests (phantom stage -> split kernel)
+  size_t split_cap = 0;
+  unsigned long long *d_split_n = nullptr;
   unsigned long long *d_arf_proj = nullptr, *d_arf_proj2 = nullptr;
   size_t arf_proj_n = 0;
   unsigned long long *d_qn = nullptr;
@@ -212,7 +223,8 @@ struct gg_ctx {
     dfree(d_ray_x2);
     dfree(d_labels); dfree(d_maj); dfree(d_spec_e); dfree(d_spec_cdf); dfree(d_acc_box);
     dfree(d_acc_e); dfree(d_acc_e2); dfree(d_edep); dfree(d_edep2);
-    dfree(d_counters); dfree(d_next); dfree(d_status); dfree(d_records);
+    dfree(d_counters); dfree(d_next); dfree(d_status); dfree(d_records); dfree(d_cnt_save);
+    dfree(d_split); dfree(d_split_n);
     dfree(d_queue[0]); dfree(d_queue[1]); dfree(d_queue[2]); dfree(d_qn);
     dfree(d_arf_proj); dfree(d_arf_proj2);
     arf_proj_n = 0;
@@ -335,9 +347,13 @@ struct gg_ctx {
       s.run_base = run_base;
       s.half_w = (real)sp.half_width;
       s.centroid = sp.adder_policy == GG_ADDER_CENTROID ? 1 : 0;
-      s.ff = ff_on ? 1 : 0;
+      s.ff = ff_on ? ff_mode : GG_FF_OFF;
       s.ff_wcut = (real)ff_wcut;
       s.ff_ecut = (real)ff_ecut;
+      s.ss_nc = ss_nc;
+      s.ss_nr = ss_nr;
+      s.ss_max = ss_max;
+      s.ss_cos = (real)ss_cos;
       s.wproj = ff_on ? d_arf_proj : nullptr;
       s.wproj2 = ff_on ? d_arf_proj2 : nullptr;
       s.zb[0] = (real)0;
@@ -921,6 +937,9 @@ static void stage_collect(gg_ctx *c) {
   c->stage_kind.clear();
 }
 
+// Longest head queue of scatter splitting (entries).
+static constexpr size_t kSsQueueMax = (size_t)1 << 26;
+
 // SPECT transport of one batch: phantom stage on the primary records, head
 // stage on the head queue, then phantom / head passes on the photons that
 // flew back into the image until the return queue stays empty.
@@ -936,7 +955,7 @@ static int spect_stages(gg_ctx *c, gg::KernelArgs a, size_t smem, int minb) {
   unsigned long long *nh = c->d_qn, *nr = c->d_qn + 1, *nf = c->d_qn + 2;
   auto stage_run = [&](int stage, void *in_q, const unsigned long long *in_n, void *out_q,
                        unsigned long long *out_n) -> int {
-    gg::StageArgs q{in_q, in_n, out_q, out_n, c->q_cap};
+    gg::StageArgs q{in_q, in_n, out_q, out_n, c->q_cap, c->d_split, c->d_split_n, c->split_cap};
     int st;
     if ((st = c->cuda(cudaMemsetAsync(out_n, 0, sizeof(unsigned long long), c->stream), "memset"))) return st;
     if ((st = c->cuda(cudaMemsetAsync(c->d_next, 0, 8, c->stream), "memset"))) return st;
@@ -998,6 +1017,79 @@ static int spect_stages(gg_ctx *c, gg::KernelArgs a, size_t smem, int minb) {
   };
   const int per_pass = c->arf_on ? 3 : 2;
   int st;
+  if (c->ff_on && c->ff_mode == GG_FF_SCATTER) {
+    // scatter splitting: analog photons never return from the heads; the
+    // phantom stage runs on spans of the batch whose copies fit the head
+    // queue.  A span that overflowed scored nothing yet (only the head stage
+    // scores), so it is repeated, shorter, after its counters are restored.
+    if (!c->d_cnt_save &&
+        (st = c->cuda(cudaMalloc(&c->d_cnt_save, GG_N_COUNTERS * sizeof(unsigned long long)), "cudaMalloc counters")))
+      return st;
+    // copies: split kernel (requests -> walk queue, the unused return queue),
+    // then their free flights (walk queue -> head queue)
+    auto split_run = [&]() -> int {
+      gg::StageArgs q{nullptr, nullptr, c->d_queue[1], nr, c->q_cap, c->d_split, c->d_split_n, c->split_cap};
+      int st2;
+      if ((st2 = c->cuda(cudaMemsetAsync(nr, 0, sizeof(unsigned long long), c->stream), "memset"))) return st2;
+      if ((st2 = stage_event(c, 2, true))) return st2;
+      cudaError_t e = c->precision == GG_PREC_F64
+                          ? gg::launch_spect_split<double>(c->scene<double>(), a, q, c->block, smem, c->n_sm, c->stream)
+                          : gg::launch_spect_split<float>(c->scene<float>(), a, q, c->block, smem, c->n_sm, c->stream);
+      if ((st2 = c->cuda(e, "split kernel launch"))) return st2;
+      gg::StageArgs w{c->d_queue[1], nr, c->d_queue[0], nh, c->q_cap, nullptr, nullptr, 0};
+      e = c->precision == GG_PREC_F64
+              ? gg::launch_spect_walk<double>(c->scene<double>(), a, w, c->block, smem, c->n_sm, c->stream)
+              : gg::launch_spect_walk<float>(c->scene<float>(), a, w, c->block, smem, c->n_sm, c->stream);
+      if ((st2 = c->cuda(e, "walk kernel launch"))) return st2;
+      return stage_event(c, 2, false);
+    };
+    const uint64_t h_end = a.h_end;
+    uint64_t lo = a.h_begin;
+    c->last_stage_launches = 0;
+    while (lo < h_end) {
+      if (c->ss_span == 0) c->ss_span = h_end - lo;
+      a.h_begin = lo;
+      a.h_end = lo + std::min<uint64_t>(c->ss_span, h_end - lo);
+      if ((st = c->cuda(cudaMemcpyAsync(c->d_cnt_save, c->d_counters, GG_N_COUNTERS * sizeof(unsigned long long),
+                                        cudaMemcpyDeviceToDevice, c->stream),
+                        "save counters")))
+        return st;
+      if ((st = c->cuda(cudaMemsetAsync(c->d_split_n, 0, 2 * sizeof(unsigned long long), c->stream), "memset")))
+        return st;
+      if ((st = stage_run(0, nullptr, nullptr, c->d_queue[0], nh))) return st;
+      if ((st = split_run())) return st;
+      unsigned long long len[3] = {0, 0, 0};
+      if ((st = c->cuda(cudaMemcpyAsync(len, c->d_split_n, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                                        c->stream),
+                        "split requests")) ||
+          (st = c->cuda(cudaMemcpyAsync(len + 2, nr, sizeof(unsigned long long), cudaMemcpyDeviceToHost, c->stream),
+                        "queue length")))
+        return st;
+      if ((st = c->cuda(cudaStreamSynchronize(c->stream), "SPECT phantom stage"))) return st;
+      stage_collect(c);
+      c->last_stage_launches += 3;
+      // the head queue holds a subset of the walk queue
+      const double fill = std::max((double)(len[0] + len[1]) / (double)c->split_cap, (double)len[2] / (double)c->q_cap);
+      if (fill > 1.0) {
+        const uint64_t span = a.h_end - a.h_begin;
+        if (span == 1)
+          return c->fail(GG_ERR_QUEUE_OVERFLOW, "SPECT stages: the split copies of one history overflow the queues");
+        if ((st = c->cuda(cudaMemcpyAsync(c->d_counters, c->d_cnt_save, GG_N_COUNTERS * sizeof(unsigned long long),
+                                          cudaMemcpyDeviceToDevice, c->stream),
+                          "restore counters")))
+          return st;
+        // requests / copies per history of this span, with a margin
+        c->ss_span = std::max<uint64_t>(1, std::min<uint64_t>(span / 2, (uint64_t)(0.85 * (double)span / fill)));
+        continue;
+      }
+      if ((st = stage_run(1, c->d_queue[0], nh, c->d_queue[1], nr))) return st;
+      ++c->last_stage_launches;
+      lo = a.h_end;
+    }
+    if ((st = c->cuda(cudaStreamSynchronize(c->stream), "SPECT head stage"))) return st;
+    stage_collect(c);
+    return GG_OK;
+  }
   if ((st = stage_run(0, nullptr, nullptr, c->d_queue[0], nh))) return st;
   if ((st = head_pass())) return st;
   c->last_stage_launches = per_pass;
@@ -1045,16 +1137,30 @@ static int run_impl(gg_ctx *c, uint64_t n, uint64_t seed, uint64_t first, bool c
     if (st) return st;
     c->rec_cap = cap;
   }
-  if (c->have_spect && (cap > c->q_cap || (c->arf_on && !c->d_queue[2]))) {
+  // scatter splitting pushes several copies per history: a longer head queue
+  // (the phantom passes adapt to it)
+  const size_t q_need = c->ff_on && c->ff_mode == GG_FF_SCATTER ? std::max(cap, std::min(cap * 16, kSsQueueMax)) : cap;
+  if (c->have_spect && (q_need > c->q_cap || (c->arf_on && !c->d_queue[2]))) {
     for (int k = 0; k < 3; ++k) dfree(c->d_queue[k]);
     c->q_cap = 0;
-    size_t qb = c->precision == GG_PREC_F64 ? gg::queue_bytes<double>(cap) : gg::queue_bytes<float>(cap);
+    size_t qb = c->precision == GG_PREC_F64 ? gg::queue_bytes<double>(q_need) : gg::queue_bytes<float>(q_need);
     int st = c->cuda(cudaMalloc(&c->d_queue[0], qb), "cudaMalloc head queue");
     if (!st) st = c->cuda(cudaMalloc(&c->d_queue[1], qb), "cudaMalloc return queue");
     if (!st && c->arf_on) st = c->cuda(cudaMalloc(&c->d_queue[2], qb), "cudaMalloc ARF fallback queue");
     if (!st && !c->d_qn) st = c->cuda(cudaMalloc(&c->d_qn, 3 * sizeof(unsigned long long)), "cudaMalloc queue lengths");
     if (st) return st;
-    c->q_cap = cap;
+    c->q_cap = q_need;
+  }
+  if (c->have_spect && c->ff_on && c->ff_mode == GG_FF_SCATTER && c->split_cap < q_need) {
+    // split requests: one per split interaction (a few per history)
+    dfree(c->d_split);
+    c->split_cap = 0;
+    size_t sb = c->precision == GG_PREC_F64 ? gg::split_bytes<double>(q_need) : gg::split_bytes<float>(q_need);
+    int st = c->cuda(cudaMalloc(&c->d_split, sb), "cudaMalloc split requests");
+    if (!st && !c->d_split_n)
+      st = c->cuda(cudaMalloc(&c->d_split_n, 2 * sizeof(unsigned long long)), "cudaMalloc split lengths");
+    if (st) return st;
+    c->split_cap = q_need;
   }
   while (c->ev.size() < 3 * nb + 1) {
     cudaEvent_t e;
@@ -1083,6 +1189,7 @@ static int run_impl(gg_ctx *c, uint64_t n, uint64_t seed, uint64_t first, bool c
   for (uint64_t b = 0; b < nb; ++b) {
     a.h_begin = first + b * (uint64_t)c->batch;
     a.h_end = std::min(first + n, a.h_begin + (uint64_t)c->batch);
+    a.rec_first = a.h_begin;
     if ((st = c->cuda(cudaMemsetAsync(c->d_next, 0, 8, c->stream), "memset"))) return st;
     if (!capturing && (st = c->cuda(cudaEventRecord(c->ev[3 * b], c->stream), "event"))) return st;
     cudaError_t e = c->precision == GG_PREC_F64 ? gg::launch_generate<double>(c->scene<double>(), a, c->stream)
@@ -1527,17 +1634,32 @@ int gg_spect_use_arf(gg_ctx *c, int32_t enable) {
 int gg_spect_set_free_flight(gg_ctx *c, const gg_ff_desc *f) {
   if (!c || !f) return GG_ERR_ARG;
   cudaSetDevice(c->device);
-  if (!f->enabled) {
+  if (f->enabled == GG_FF_OFF) {
     c->ff_on = false;
+    c->ff_mode = GG_FF_OFF;
     return GG_OK;
   }
+  if (f->enabled != GG_FF_PRIMARY && f->enabled != GG_FF_SCATTER)
+    return c->fail(GG_ERR_ARG, "gg_spect_set_free_flight: unknown mode %d", f->enabled);
   if (!c->have_spect) return c->fail(GG_ERR_STATE, "gg_spect_set_free_flight: call gg_spect_setup first");
   if (c->arf_on) return c->fail(GG_ERR_STATE, "gg_spect_set_free_flight: the ARF detector is on");
   if (std::isnan(f->weight_cutoff) || std::isnan(f->energy_cutoff))
     return c->fail(GG_ERR_ARG, "gg_spect_set_free_flight: invalid cutoff");
+  if (std::isnan(f->angle_tolerance_max)) return c->fail(GG_ERR_ARG, "gg_spect_set_free_flight: invalid angle");
+  if (f->enabled == GG_FF_SCATTER &&
+      (f->compton_splitting < 0 || f->rayleigh_splitting < 0 || f->max_compton_level < 0 ||
+       f->compton_splitting > GG_MAX_SPLITTING || f->rayleigh_splitting > GG_MAX_SPLITTING))
+    return c->fail(GG_ERR_ARG, "gg_spect_set_free_flight: splitting factors must be in [0, %d], the level >= 0",
+                   GG_MAX_SPLITTING);
   c->ff_on = true;
+  c->ff_mode = f->enabled;
   c->ff_wcut = f->weight_cutoff;
   c->ff_ecut = f->energy_cutoff;
+  c->ss_nc = f->enabled == GG_FF_SCATTER ? f->compton_splitting : 0;
+  c->ss_nr = f->enabled == GG_FF_SCATTER ? f->rayleigh_splitting : 0;
+  c->ss_max = f->enabled == GG_FF_SCATTER ? f->max_compton_level : 0;
+  c->ss_cos = f->enabled == GG_FF_SCATTER && f->angle_tolerance_max > 0.0 ? std::cos(f->angle_tolerance_max) : -2.0;
+  c->ss_span = 0;
   int st = arf_projection_alloc(c, c->n_proj);
   if (st) return st;
   return c->cuda(cudaStreamSynchronize(c->stream), "weighted projection");

@@ -56,6 +56,7 @@ __device__ __forceinline__ void queue_copy(const PQueue<real> &in, size_t k, con
 #pragma unroll
   for (int i = 0; i < kEvSlots; ++i) out.ev[i][j] = in.ev[i][k];
   out.rng_pos[j] = in.rng_pos[k];
+  out.stream[j] = in.stream[k];
   out.meta[j] = in.meta[k];
 }
 

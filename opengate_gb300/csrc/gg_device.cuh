@@ -479,8 +479,10 @@ struct Scene {
   // free flight outside the heads (GateGammaFreeFlightOptn, heads excluded):
   // ff = 1 on; weight / energy cutoffs; singles then add their weight (2^-32
   // fixed point, with history-by-history squares) to wproj / wproj2
-  int ff;
+  int ff;  // 0 off, 1 primary free flight, 2 scatter splitting (+ free flight of the copies)
   real ff_wcut, ff_ecut;
+  int ss_nc, ss_nr, ss_max;  // splitting factors (Compton, Rayleigh), max Compton level
+  real ss_cos;               // copies entering a head with a local dir z below this are dropped (-2: off)
   unsigned long long *wproj, *wproj2;
   real eb_sigma, eb_res, eb_ref, eb_slope, sb_sigma[2];
 };

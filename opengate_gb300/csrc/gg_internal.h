@@ -23,6 +23,7 @@ struct KernelArgs {
   int chunk;                        // histories claimed per warp refill
   void *records;                    // primary records of the batch (k_generate -> k_transport)
   size_t rec_cap;                   // records capacity (histories per batch)
+  uint64_t rec_first;               // history of record 0 (<= h_begin; a SPECT pass can start later)
   int refill_min;                   // lanes that must wait for a history before a refill phase
   int interact_min;                 // pending collisions that trigger an interaction phase
 };
@@ -41,6 +42,11 @@ struct StageArgs {
   void *out_q;                     // output queue
   unsigned long long *out_n;       // output queue length (appended to)
   size_t q_cap;                    // capacity of each queue (entries)
+  // scatter splitting: requests of the phantom stage for the split kernel
+  // (Compton from the front, Rayleigh from the back of one buffer)
+  void *split_q;
+  unsigned long long *split_n;     // [Compton requests, Rayleigh requests]
+  size_t split_cap;
 };
 
 // One launch of the ARF training-row generator (see gg_arf.cu).
@@ -130,6 +136,19 @@ cudaError_t launch_spect_stage(int stage, const Scene<real> &s, const KernelArgs
                                int block, size_t smem, int minb, cudaStream_t st);
 template <typename real>
 cudaError_t spect_stage_occupancy(int stage, int block, size_t smem, int minb, int *blocks_per_sm);
+// Copies of scatter splitting (gg_spect.cu): the split requests of q.split_q
+// into the walk queue (q.out_q / q.out_n); does nothing when the requests
+// overflowed the buffer.
+template <typename real>
+cudaError_t launch_spect_split(const Scene<real> &s, const KernelArgs &a, const StageArgs &q, int block, size_t smem,
+                               int n_sm, cudaStream_t st);
+template <typename real>
+size_t split_bytes(size_t cap);
+// Free flights of the copies the split kernel queued (q.in_q / q.in_n) into
+// the head queue (q.out_q / q.out_n).
+template <typename real>
+cudaError_t launch_spect_walk(const Scene<real> &s, const KernelArgs &a, const StageArgs &q, int block, size_t smem,
+                              int n_sm, cudaStream_t st);
 template <typename real>
 size_t record_bytes(size_t cap);
 template <typename real>

@@ -304,6 +304,7 @@ extern "C" int gg_dose_run_noalloc(int32_t device, void *stream, const gg_tables
     for (uint64_t h0 = first_history; h0 < first_history + n_histories && e == cudaSuccess;
          h0 += (uint64_t)GG_NOALLOC_BATCH) {
       a.h_begin = h0;
+      a.rec_first = h0;
       a.h_end = h0 + (uint64_t)GG_NOALLOC_BATCH < first_history + n_histories ? h0 + (uint64_t)GG_NOALLOC_BATCH
                                                                             : first_history + n_histories;
       e = cudaMemsetAsync(a.next, 0, 8, st);

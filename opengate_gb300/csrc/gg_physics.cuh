@@ -210,6 +210,9 @@ __device__ __forceinline__ void iso_dir(Rng &g, real d[3]) {
   d[2] = cost;
 }
 
+// interaction kinds (interact's `kind`)
+enum : int { kCompton = 1, kPhoto = 2, kRayleigh = 3, kPair = 4 };
+
 // One secondary slot per thread, in shared memory: after a pair conversion the
 // photon continues as one 511 keV photon and the other waits here.  511 keV
 // cannot convert again, so one slot always suffices.
@@ -225,22 +228,28 @@ struct Secondary {
 // locally (scored by the caller when inside the image).
 template <typename real>
 __device__ __forceinline__ real interact(const Scene<real> &s, Photon<real> &ph, int mat, Rng &g,
-                                         BlockCounters *bc, Secondary<real> &sec) {
+                                         BlockCounters *bc, Secondary<real> &sec, int *kind = nullptr) {
   int c = s.mat_comp[mat];
   const real *cu = s.cum + (size_t)c * 3 * s.n_e;
   real r = u01<real>(g);
   real fc = interp_row(cu, ph.ei);
-  if (r < fc) return compton(s, ph, g, bc);
+  if (r < fc) {
+    if (kind) *kind = kCompton;
+    return compton(s, ph, g, bc);
+  }
   real fp = interp_row(cu + s.n_e, ph.ei);
   if (r < fp) {
+    if (kind) *kind = kPhoto;
     ph.alive = 0;
     return ph.e;
   }
   real fr = interp_row(cu + 2 * s.n_e, ph.ei);
   if (r < fr) {
+    if (kind) *kind = kRayleigh;
     rayleigh(s, c, ph, g, bc);
     return R<real>(0);
   }
+  if (kind) *kind = kPair;
   real ekin = ph.e - R<real>(2.0 * kMC2);
   real d[3];
   iso_dir(g, d);
@@ -761,9 +770,9 @@ template <typename real, bool SPECT, bool TLE = false>
 __device__ __forceinline__ int do_interaction(const Scene<real> &s, Photon<real> &ph, Rng &g, BlockCounters *bc,
                                               int pmat, uint32_t pv, int pscored, HistList<real> &l,
                                               const Tally<real> &t, Secondary<real> &sec, unsigned int &n_dep,
-                                              Event<real> &ev) {
+                                              Event<real> &ev, int *kind = nullptr) {
   const real e_pre = ph.e;
-  real ed = interact(s, ph, pmat, g, bc, sec);
+  real ed = interact(s, ph, pmat, g, bc, sec, kind);
   if (pscored == 1) {
     if constexpr (!SPECT) {
       if (!TLE || e_pre > s.tle_thr) deposit(l, t, bc, pv, ed, n_dep);

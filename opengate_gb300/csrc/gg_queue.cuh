@@ -28,6 +28,7 @@ struct PQueue {
   real *px, *py, *pz, *dx, *dy, *dz, *e, *w;
   real *ev[kEvSlots];
   uint32_t *rng_pos, *meta;
+  uint32_t *stream;  // Philox stream of the photon (split copies; free flight only)
 
   __device__ __forceinline__ static PQueue carve(void *base, size_t cap) {
     PQueue q;
@@ -48,13 +49,48 @@ struct PQueue {
     q.rng_pos = reinterpret_cast<uint32_t *>(p);
     p += cap * sizeof(uint32_t);
     q.meta = reinterpret_cast<uint32_t *>(p);
+    p += cap * sizeof(uint32_t);
+    q.stream = reinterpret_cast<uint32_t *>(p);
     return q;
   }
 };
 
 template <typename real>
 size_t queue_bytes(size_t cap) {
-  return cap * (sizeof(uint4) + sizeof(unsigned long long) + (8 + kEvSlots) * sizeof(real) + 2 * sizeof(uint32_t));
+  return cap * (sizeof(uint4) + sizeof(unsigned long long) + (8 + kEvSlots) * sizeof(real) + 3 * sizeof(uint32_t));
+}
+
+// Split requests of scatter splitting (phantom stage -> split kernel), SoA:
+// the photon before the interaction (position, direction, energy, weight),
+// its history, the stream offset of its first copy and the composition of
+// the material (Rayleigh form factors).
+template <typename real>
+struct SplitQueue {
+  unsigned long long *hid;
+  real *px, *py, *pz, *dx, *dy, *dz, *e, *w;
+  uint32_t *base;
+  int32_t *comp;
+
+  __device__ __forceinline__ static SplitQueue carve(void *b, size_t cap) {
+    SplitQueue q;
+    unsigned char *p = reinterpret_cast<unsigned char *>(b);
+    q.hid = reinterpret_cast<unsigned long long *>(p);
+    p += cap * sizeof(unsigned long long);
+    real **f[8] = {&q.px, &q.py, &q.pz, &q.dx, &q.dy, &q.dz, &q.e, &q.w};
+    for (int i = 0; i < 8; ++i) {
+      *f[i] = reinterpret_cast<real *>(p);
+      p += cap * sizeof(real);
+    }
+    q.base = reinterpret_cast<uint32_t *>(p);
+    p += cap * sizeof(uint32_t);
+    q.comp = reinterpret_cast<int32_t *>(p);
+    return q;
+  }
+};
+
+template <typename real>
+size_t split_bytes(size_t cap) {
+  return cap * (sizeof(unsigned long long) + 8 * sizeof(real) + 2 * sizeof(uint32_t));
 }
 
 constexpr uint32_t kMetaSteps = (1u << 20) - 1u;
@@ -85,10 +121,11 @@ __device__ __forceinline__ void stage_tables(const Scene<real> &sg, Scene<real> 
   s.mat_comp = scomp;
 }
 
-__device__ __forceinline__ void rng_resume(Rng &g, uint64_t seed, uint64_t hid, uint32_t rp, uint4 b) {
+__device__ __forceinline__ void rng_resume(Rng &g, uint64_t seed, uint64_t hid, uint32_t rp, uint4 b,
+                                           uint32_t stream = 0u) {
   g.k0 = (uint32_t)seed;
   g.k1 = (uint32_t)(seed >> 32);
-  g.stream = 0u;
+  g.stream = stream;
   g.h0 = (uint32_t)hid;
   g.h1 = (uint32_t)(hid >> 32);
   g.blk = rp >> 3;
@@ -119,7 +156,10 @@ __device__ __forceinline__ void queue_put(const PQueue<real> &q, size_t k, const
   q.dy[k] = ph.dir[1];
   q.dz[k] = ph.dir[2];
   q.e[k] = ph.e;
-  if constexpr (FF) q.w[k] = ph.w;
+  if constexpr (FF) {
+    q.w[k] = ph.w;
+    q.stream[k] = g.stream;
+  }
   if (has_ev) {
 #pragma unroll
     for (int i = 0; i < kEvSlots; ++i) q.ev[i][k] = ev[i];
@@ -135,7 +175,7 @@ template <typename real, bool FF = true>
 __device__ __forceinline__ uint64_t queue_get(const Scene<real> &s, const PQueue<real> &q, size_t k, Photon<real> &ph,
                                               Rng &g, uint64_t seed, bool &has_ev) {
   const uint64_t hid = q.hid[k];
-  rng_resume(g, seed, hid, q.rng_pos[k], q.rng_buf[k]);
+  rng_resume(g, seed, hid, q.rng_pos[k], q.rng_buf[k], FF ? q.stream[k] : 0u);
   ph.pos[0] = q.px[k];
   ph.pos[1] = q.py[k];
   ph.pos[2] = q.pz[k];

@@ -31,10 +31,16 @@
 
 namespace gg {
 
+// Free-flight modes of the stages (Scene::ff).
+constexpr int kFfOff = 0, kFfPrimary = 1, kFfScatter = 2;
+
 // Phantom-stage flight: Woodcock step in the image (followed, when it leaves
 // the image box, by the world step) or one world step; a photon whose world
-// step ends at a head-box entry leaves the stage (kPush).
-template <typename real, bool FF>
+// step ends at a head-box entry leaves the stage (kPush).  Primary free
+// flight (FFM 1): one free flight to a head instead.  Scatter splitting
+// (FFM 2): analog flights, and an analog photon that reaches a head is killed
+// there (the heads are its kill volumes; only its split copies are detected).
+template <typename real, int FFM>
 __device__ __forceinline__ int phantom_flight(const Scene<real> &s, Photon<real> &ph, Rng &g, BlockCounters *bc,
                                               int &pmat, uint32_t &pv, int &pscored, unsigned int &n_wood,
                                               unsigned int &n_real, unsigned int &n_world) {
@@ -43,9 +49,9 @@ __device__ __forceinline__ int phantom_flight(const Scene<real> &s, Photon<real>
     ph.alive = 0;
     return kRefill;
   }
-  if constexpr (FF) {  // free flight to a head: no interaction outside the heads
+  if constexpr (FFM == kFfPrimary) {  // free flight to a head: no interaction outside the heads
     ++n_world;
-    if (ff_flight(s, ph)) return kPush;
+    if (ff_flight(s, ph, R<real>(-2))) return kPush;
     atomicAdd(&bc->escaped, 1u);
     return kRefill;
   }
@@ -69,6 +75,14 @@ __device__ __forceinline__ int phantom_flight(const Scene<real> &s, Photon<real>
   if (!ph.alive) {
     atomicAdd(&bc->escaped, 1u);
     return kRefill;
+  }
+  if constexpr (FFM == kFfScatter) {
+    if (ph.in_head) {
+      ph.alive = 0;
+      atomicAdd(&bc->escaped, 1u);
+      return kRefill;
+    }
+    return kFly;
   }
   return ph.in_head ? kPush : kFly;
 }
@@ -96,7 +110,7 @@ __device__ __forceinline__ int head_stage_flight(const Scene<real> &s, Photon<re
   }
   ++n_world;
   if constexpr (FF) {  // free flight to another head (the image crossed on the way)
-    if (ff_flight(s, ph)) return kFly;
+    if (ff_flight(s, ph, R<real>(-2))) return kFly;
     atomicAdd(&bc->escaped, 1u);
     return kRefill;
   }
@@ -137,11 +151,129 @@ __device__ __forceinline__ void stage_counters(unsigned long long *cnt, const Bl
   }
 }
 
+// Scatter splitting, the copies (GateScatterSplittingFreeFlightOptn.cpp:69-149):
+// one thread per copy.  Request r of the phantom stage holds the photon
+// before a Compton (or Rayleigh) interaction; its copy c re-samples that
+// interaction from there on Philox stream 2 + base + c of the history, with
+// 1 / n of the weight, and flies freely to a head: the intersection check of
+// the angular acceptance is the flight itself (a copy that misses every head
+// cannot be detected), the angle check comes before the optical depth.
+// A copy whose line enters a head (past the checks) goes to the walk queue
+// (q.out_q), where k_spect_walk computes its optical depth: the few copies
+// that pass then walk the voxels with full warps.  Compton requests fill the
+// buffer from the front and Rayleigh requests from the back; when together
+// they overflowed it, nothing is done (the host repeats the pass on fewer
+// histories).
+template <typename real>
+__global__ void __launch_bounds__(256) k_spect_split(Scene<real> sg, KernelArgs args, StageArgs q) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ BlockCounters bc;
+  Scene<real> s = sg;
+  stage_tables(sg, s, smem_raw, bc);
+  const uint64_t n_c = *q.split_n, n_r = q.split_n[1];
+  if (n_c + n_r > (uint64_t)q.split_cap) return;
+  const uint64_t per_c = (uint64_t)s.ss_nc, per_r = (uint64_t)s.ss_nr;
+  const uint64_t all_c = n_c * per_c, total = all_c + n_r * per_r;
+  const SplitQueue<real> sq = SplitQueue<real>::carve(q.split_q, q.split_cap);
+  const PQueue<real> out = PQueue<real>::carve(q.out_q, q.q_cap);
+  const unsigned lane = threadIdx.x & 31u;
+  const unsigned lt_mask = (1u << lane) - 1u;
+  unsigned int n_world = 0;
+  // the loop bound is the same for all threads of a block: queue claims stay warp-collective
+  for (uint64_t i0 = (uint64_t)blockIdx.x * blockDim.x; i0 < total; i0 += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t i = i0 + threadIdx.x;
+    Photon<real> cp;
+    Rng gc;
+    uint64_t hid = 0;
+    bool push = false;
+    if (i < total) {
+      uint64_t r;
+      uint32_t c, n;
+      if (i < all_c) {
+        r = i / per_c;
+        c = (uint32_t)(i - r * per_c);
+        n = (uint32_t)per_c;
+      } else {
+        const uint64_t j = i - all_c, rr = j / per_r;
+        c = (uint32_t)(j - rr * per_r);
+        r = (uint64_t)q.split_cap - 1 - rr;
+        n = (uint32_t)per_r;
+      }
+      hid = sq.hid[r];
+      cp.pos[0] = sq.px[r];
+      cp.pos[1] = sq.py[r];
+      cp.pos[2] = sq.pz[r];
+      cp.dir[0] = sq.dx[r];
+      cp.dir[1] = sq.dy[r];
+      cp.dir[2] = sq.dz[r];
+      set_energy(s, cp, sq.e[r]);
+      cp.w = sq.w[r] / (real)n;
+      cp.alive = 1;
+      cp.run = run_of(s, hid);
+      gc.init(args.seed, hid, 2u + sq.base[r] + c);
+      if (i < all_c) compton(s, cp, gc, &bc);
+      else rayleigh(s, sq.comp[r], cp, gc, &bc);
+      if (cp.alive) {
+        cp.exclude = -1;
+        cp.steps = 0;
+        cp.head = 0;
+        cp.hreg = 0;
+        ++n_world;
+        real tb;
+        push = ff_target(s, cp, s.ss_cos, tb) != 0;  // with the angle check of the angular acceptance
+        if (!push) atomicAdd(&bc.escaped, 1u);
+      }
+    }
+    const size_t k = queue_claim(q.out_n, push, lane, lt_mask);
+    if (push && k < q.q_cap) {
+      real v[kEvSlots];
+      queue_put<real, true>(out, k, cp, gc, hid, v, false);
+    }
+  }
+  stage_counters(args.counters, bc, lane, 0u, 0u, n_world, 0u, 0u);
+}
+
+// Scatter splitting, the free flights of the copies that passed the split
+// kernel's checks: the whole ff_flight (its first part again, bit for bit the
+// same, then the optical depth along the line), one copy per thread; copies
+// that reach their head go to the head queue.
+template <typename real>
+__global__ void __launch_bounds__(256) k_spect_walk(Scene<real> sg, KernelArgs args, StageArgs q) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ BlockCounters bc;
+  Scene<real> s = sg;
+  stage_tables(sg, s, smem_raw, bc);
+  const uint64_t n = min((uint64_t)*q.in_n, (uint64_t)q.q_cap);
+  const PQueue<real> in = PQueue<real>::carve(q.in_q, q.q_cap);
+  const PQueue<real> out = PQueue<real>::carve(q.out_q, q.q_cap);
+  const unsigned lane = threadIdx.x & 31u;
+  const unsigned lt_mask = (1u << lane) - 1u;
+  for (uint64_t i0 = (uint64_t)blockIdx.x * blockDim.x; i0 < n; i0 += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t i = i0 + threadIdx.x;
+    Photon<real> cp;
+    Rng g;
+    uint64_t hid = 0;
+    bool push = false;
+    if (i < n) {
+      bool has_ev;
+      hid = queue_get<real, true>(s, in, i, cp, g, args.seed, has_ev);
+      push = ff_flight(s, cp, s.ss_cos) != 0;
+      if (!push) atomicAdd(&bc.escaped, 1u);
+    }
+    const size_t k = queue_claim(q.out_n, push, lane, lt_mask);
+    if (push && k < q.q_cap) {
+      real v[kEvSlots];
+      queue_put<real, true>(out, k, cp, g, hid, v, false);
+    }
+  }
+  stage_counters(args.counters, bc, lane, 0u, 0u, 0u, 0u, 0u);
+}
+
 // Phantom stage.  Input: the batch's primary records (q.in_q == null) or the
 // return queue; output: the head queue.  Persistent grid with the
 // phase-batched lane loop of the dose transport kernel (refill / fly /
-// interact, one phase per warp iteration).
-template <typename real, int MINB, bool FF>
+// interact, one phase per warp iteration).  FFM: free-flight mode (kFf*).
+template <typename real, int MINB, int FFM>
 __global__ void __launch_bounds__(256, MINB) k_spect_phantom(Scene<real> sg, KernelArgs args, StageArgs q) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ BlockCounters bc;
@@ -181,6 +313,8 @@ __global__ void __launch_bounds__(256, MINB) k_spect_phantom(Scene<real> sg, Ker
   int pmat = 0, pscored = 0;
   uint32_t pv = 0;
   unsigned int n_wood = 0, n_real = 0, n_dep = 0, n_world = 0, n_singles = 0;
+  uint32_t nsplit = 0;  // split copies of the history so far
+  int ncompt = 0;       // Compton interactions of the analog track
 
   for (;;) {
     // phase chosen per block: all warps run the same code region at the same
@@ -226,7 +360,7 @@ __global__ void __launch_bounds__(256, MINB) k_spect_phantom(Scene<real> sg, Ker
         if (h >= n_items) {
           state = kDone;
         } else if (from_queue) {
-          hid = queue_get<real, FF>(s, in, h, ph, g, args.seed, has_ev);
+          hid = queue_get<real, FFM != kFfOff>(s, in, h, ph, g, args.seed, has_ev);
           slot = h;
           ph.in_head = 0;
           ph.in_image = 1;
@@ -234,16 +368,17 @@ __global__ void __launch_bounds__(256, MINB) k_spect_phantom(Scene<real> sg, Ker
           state = kFly;
           in_hist = true;
         } else {
-          const uint32_t f = rec.flags[h];
+          const uint64_t r = h + (args.h_begin - args.rec_first);  // record of the history
+          const uint32_t f = rec.flags[r];
           const uint32_t rs = f & 3u;
           if (rs != kRecDead) {
-            ph.pos[0] = rec.px[h];
-            ph.pos[1] = rec.py[h];
-            ph.pos[2] = rec.pz[h];
-            ph.dir[0] = rec.dx[h];
-            ph.dir[1] = rec.dy[h];
-            ph.dir[2] = rec.dz[h];
-            set_energy(s, ph, rec.e[h]);
+            ph.pos[0] = rec.px[r];
+            ph.pos[1] = rec.py[r];
+            ph.pos[2] = rec.pz[r];
+            ph.dir[0] = rec.dx[r];
+            ph.dir[1] = rec.dy[r];
+            ph.dir[2] = rec.dz[r];
+            set_energy(s, ph, rec.e[r]);
             ph.steps = (int)((f >> 2) & 1u);
             ph.alive = 1;
             ph.can_enter = 1;
@@ -253,7 +388,9 @@ __global__ void __launch_bounds__(256, MINB) k_spect_phantom(Scene<real> sg, Ker
             hid = args.h_begin + h;
             ph.run = run_of(s, hid);
             has_ev = false;
-            rng_resume(g, args.seed, hid, rec.rng_pos[h], rec.rng_buf[h]);
+            nsplit = 0;
+            ncompt = 0;
+            rng_resume(g, args.seed, hid, rec.rng_pos[r], rec.rng_buf[r]);
             if (rs == kRecInImage) {
               ph.in_image = 1;
               ph.t_exit = exit_distance(ph.pos, ph.dir, s.bmin, s.bmax);
@@ -272,7 +409,54 @@ __global__ void __launch_bounds__(256, MINB) k_spect_phantom(Scene<real> sg, Ker
         }
       }
     } else if (phase == kInteract) {
-      if (state == kInteract) {
+      if constexpr (FFM == kFfScatter) {
+        // GateScatterSplittingFreeFlightOptrActor.cpp:291-360: every Compton
+        // up to the maximum level and every Rayleigh is split; the analog
+        // photon goes on, and is killed after a Compton beyond the level
+        const Photon<real> pre = ph;
+        int kind = 0, n = 0;
+        if (state == kInteract) {
+          state = do_interaction<real, true>(s, ph, g, &bc, pmat, pv, pscored, l, t, sec, n_dep, ev_unused, &kind);
+          if (kind == kCompton && s.ss_nc > 0) {
+            if (++ncompt > s.ss_max) {
+              ph.alive = 0;
+              state = kRefill;
+            } else {
+              n = s.ss_nc;
+            }
+          } else if (kind == kRayleigh) {
+            n = s.ss_nr;
+          }
+        }
+        // the copies are made by the split kernel: one request per split interaction
+        const bool req_c = n > 0 && kind == kCompton, req_r = n > 0 && kind == kRayleigh;
+        const size_t kc = queue_claim(q.split_n, req_c, lane, lt_mask);
+        const size_t kr = queue_claim(q.split_n + 1, req_r, lane, lt_mask);
+        if (req_c || req_r) {
+          // past the capacity the split kernel skips the whole buffer and the pass is repeated
+          if (req_c ? kc < q.split_cap : kr < q.split_cap) {
+            const size_t k = req_c ? kc : q.split_cap - 1 - kr;
+            const SplitQueue<real> sq = SplitQueue<real>::carve(q.split_q, q.split_cap);
+            sq.hid[k] = hid;
+            sq.px[k] = pre.pos[0];
+            sq.py[k] = pre.pos[1];
+            sq.pz[k] = pre.pos[2];
+            sq.dx[k] = pre.dir[0];
+            sq.dy[k] = pre.dir[1];
+            sq.dz[k] = pre.dir[2];
+            sq.e[k] = pre.e;
+            sq.w[k] = pre.w;
+            sq.base[k] = nsplit;
+            sq.comp[k] = s.mat_comp[pmat];
+          }
+          nsplit += (uint32_t)n;
+        }
+        if (state == kRefill && sec.has) {
+          pop_secondary(s, ph, sec);
+          ncompt = 0;
+          state = kFly;
+        }
+      } else if (state == kInteract) {
         state = do_interaction<real, true>(s, ph, g, &bc, pmat, pv, pscored, l, t, sec, n_dep, ev_unused);
         if (state == kRefill && sec.has) {
           pop_secondary(s, ph, sec);
@@ -281,7 +465,7 @@ __global__ void __launch_bounds__(256, MINB) k_spect_phantom(Scene<real> sg, Ker
       }
     } else {
       if (state == kFly) {
-        state = phantom_flight<real, FF>(s, ph, g, &bc, pmat, pv, pscored, n_wood, n_real, n_world);
+        state = phantom_flight<real, FFM>(s, ph, g, &bc, pmat, pv, pscored, n_wood, n_real, n_world);
         if (state == kRefill && sec.has) {
           pop_secondary(s, ph, sec);
           state = kFly;
@@ -293,7 +477,7 @@ __global__ void __launch_bounds__(256, MINB) k_spect_phantom(Scene<real> sg, Ker
         if (k < q.q_cap) {
           real v[kEvSlots];
           if (has_ev) load_event(in, slot, v);
-          queue_put<real, FF>(out, k, ph, g, hid, v, has_ev);
+          queue_put<real, FFM != kFfOff>(out, k, ph, g, hid, v, has_ev);
         } else {
           atomicOr(args.status, kStatusQueueOverflow);
         }
@@ -431,20 +615,23 @@ __global__ void __launch_bounds__(256, MINB) k_spect_head(Scene<real> sg, Kernel
   stage_counters(args.counters, bc, lane, 0u, 0u, n_world, n_head, n_singles);
 }
 
-template <typename real, int MINB, bool FF = false>
+// MINB / HMINB: register budgets (resident 256-thread blocks per SM) of the
+// phantom and the head stage.
+template <typename real, int MINB, int FFM = kFfOff, int HMINB = MINB>
 static cudaError_t launch_stage_v(int stage, const Scene<real> &s, const KernelArgs &a, const StageArgs &q, int grid,
                                   int block, size_t smem, cudaStream_t st) {
+  constexpr bool FF = FFM != kFfOff;
   static bool configured[2] = {false, false};
   if (!configured[stage]) {
-    cudaError_t e = stage == 0 ? cudaFuncSetAttribute(k_spect_phantom<real, MINB, FF>,
+    cudaError_t e = stage == 0 ? cudaFuncSetAttribute(k_spect_phantom<real, MINB, FFM>,
                                                       cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024)
-                               : cudaFuncSetAttribute(k_spect_head<real, MINB, FF>,
+                               : cudaFuncSetAttribute(k_spect_head<real, HMINB, FF>,
                                                       cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     if (e != cudaSuccess) return e;
     configured[stage] = true;
   }
-  if (stage == 0) k_spect_phantom<real, MINB, FF><<<grid, block, smem, st>>>(s, a, q);
-  else k_spect_head<real, MINB, FF><<<grid, block, smem, st>>>(s, a, q);
+  if (stage == 0) k_spect_phantom<real, MINB, FFM><<<grid, block, smem, st>>>(s, a, q);
+  else k_spect_head<real, HMINB, FF><<<grid, block, smem, st>>>(s, a, q);
   return cudaGetLastError();
 }
 
@@ -453,7 +640,10 @@ cudaError_t launch_spect_stage(int stage, const Scene<real> &s, const KernelArgs
                                int block, size_t smem, int minb, cudaStream_t st) {
   // free flight: one register budget (4 blocks of 256 threads per SM); a
   // smaller grid computed for another budget is a valid launch of it
-  if (s.ff) return launch_stage_v<real, 4, true>(stage, s, a, q, grid, block, smem, st);
+  // the splitting loop keeps the photon before the interaction live: the
+  // scatter-splitting phantom stage gets the 2-block register budget
+  if (s.ff == kFfScatter) return launch_stage_v<real, 2, kFfScatter, 4>(stage, s, a, q, grid, block, smem, st);
+  if (s.ff) return launch_stage_v<real, 4, kFfPrimary>(stage, s, a, q, grid, block, smem, st);
   if (minb <= 2) return launch_stage_v<real, 2>(stage, s, a, q, grid, block, smem, st);
   if (minb == 3) return launch_stage_v<real, 3>(stage, s, a, q, grid, block, smem, st);
   return launch_stage_v<real, 4>(stage, s, a, q, grid, block, smem, st);
@@ -461,7 +651,7 @@ cudaError_t launch_spect_stage(int stage, const Scene<real> &s, const KernelArgs
 
 template <typename real, int MINB>
 static cudaError_t stage_occupancy_v(int stage, int block, size_t smem, int *bps) {
-  return stage == 0 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(bps, k_spect_phantom<real, MINB, false>, block, smem)
+  return stage == 0 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(bps, k_spect_phantom<real, MINB, kFfOff>, block, smem)
                     : cudaOccupancyMaxActiveBlocksPerMultiprocessor(bps, k_spect_head<real, MINB, false>, block, smem);
 }
 
@@ -472,6 +662,48 @@ cudaError_t spect_stage_occupancy(int stage, int block, size_t smem, int minb, i
   return stage_occupancy_v<real, 4>(stage, block, smem, blocks_per_sm);
 }
 
+template <typename real>
+cudaError_t launch_spect_split(const Scene<real> &s, const KernelArgs &a, const StageArgs &q, int block, size_t smem,
+                               int n_sm, cudaStream_t st) {
+  static bool configured = false;
+  static int bps = 1;
+  if (!configured) {
+    cudaError_t e = cudaFuncSetAttribute(k_spect_split<real>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_spect_split<real>, block, smem);
+    if (e != cudaSuccess) return e;
+    if (bps < 1) bps = 1;
+    configured = true;
+  }
+  k_spect_split<real><<<n_sm * bps, block, smem, st>>>(s, a, q);
+  return cudaGetLastError();
+}
+
+template <typename real>
+cudaError_t launch_spect_walk(const Scene<real> &s, const KernelArgs &a, const StageArgs &q, int block, size_t smem,
+                              int n_sm, cudaStream_t st) {
+  static bool configured = false;
+  static int bps = 1;
+  if (!configured) {
+    cudaError_t e = cudaFuncSetAttribute(k_spect_walk<real>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_spect_walk<real>, block, smem);
+    if (e != cudaSuccess) return e;
+    if (bps < 1) bps = 1;
+    configured = true;
+  }
+  k_spect_walk<real><<<n_sm * bps, block, smem, st>>>(s, a, q);
+  return cudaGetLastError();
+}
+
+template cudaError_t launch_spect_walk<float>(const Scene<float> &, const KernelArgs &, const StageArgs &, int,
+                                              size_t, int, cudaStream_t);
+template cudaError_t launch_spect_walk<double>(const Scene<double> &, const KernelArgs &, const StageArgs &, int,
+                                               size_t, int, cudaStream_t);
+template size_t split_bytes<float>(size_t);
+template size_t split_bytes<double>(size_t);
+template cudaError_t launch_spect_split<float>(const Scene<float> &, const KernelArgs &, const StageArgs &, int,
+                                               size_t, int, cudaStream_t);
+template cudaError_t launch_spect_split<double>(const Scene<double> &, const KernelArgs &, const StageArgs &, int,
+                                                size_t, int, cudaStream_t);
 template size_t queue_bytes<float>(size_t);
 template size_t queue_bytes<double>(size_t);
 template cudaError_t launch_spect_stage<float>(int, const Scene<float> &, const KernelArgs &, const StageArgs &, int,

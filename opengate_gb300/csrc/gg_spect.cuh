@@ -305,16 +305,37 @@ __device__ __forceinline__ int spect_world_flight(const Scene<real> &s, Photon<r
 // is multiplied by the probability of getting there, exp(-optical depth)
 // (air over the whole path, the voxels' attenuation inside the image box).
 // Photons at or below the energy or weight cutoff, and photons whose line
-// misses every head, stop.  Returns 1 at a head entry (head-local state as
-// spect_world_flight sets it), 0 when the photon stopped.
+// misses every head, stop; so do photons whose direction makes a cosine
+// below cos_min with the axis of the head they would enter (angle check of
+// the angular acceptance, before the optical depth is computed; -2: none).
+// Returns 1 at a head entry (head-local state as spect_world_flight sets it),
+// 0 when the photon stopped.  ff_target is its first part: the cutoffs, the
+// head the line enters (1 + head, at distance tb) and the checks on it; 0
+// when the photon stopped there.
 template <typename real>
-__device__ __forceinline__ int ff_flight(const Scene<real> &s, Photon<real> &ph) {
+__device__ __forceinline__ int ff_target(const Scene<real> &s, Photon<real> &ph, real cos_min, real &tb_out) {
   if (ph.e <= s.ff_ecut || ph.w <= s.ff_wcut) {
     ph.alive = 0;
     return 0;
   }
+  if (cos_min > R<real>(-1)) {
+    // angle check first: no head axis within the tolerance means the test
+    // below fails too (its cosine is the same dot product), without the
+    // box intersections
+    bool any = false;
+    for (int h = 0; h < s.n_heads; ++h) {
+      if (ph.exclude == 1 + h) continue;
+      const HeadFrame<real> f = head_frame(s, ph.run, h);
+      any = any || !(dot3(ph.dir, f.u) < cos_min);
+    }
+    if (!any) {
+      ph.alive = 0;
+      return 0;
+    }
+  }
   real tb = gg_inf(real(0));
   int box = 0;
+  real cos_box = R<real>(0);
   real hlo[3] = {-s.half_w, -s.half_w, R<real>(0)};
   real hhi[3] = {s.half_w, s.half_w, s.zb[3]};
   for (int h = 0; h < s.n_heads; ++h) {
@@ -325,14 +346,24 @@ __device__ __forceinline__ int ff_flight(const Scene<real> &s, Photon<real> &ph)
     if (th < tb) {
       tb = th;
       box = 1 + h;
+      cos_box = ld[2];
     }
   }
   real wlo[3] = {-s.whalf[0], -s.whalf[1], -s.whalf[2]};
   const real tout = exit_distance(ph.pos, ph.dir, wlo, s.whalf);
-  if (!(tb <= tout)) {
+  if (!(tb <= tout) || cos_box < cos_min) {
     ph.alive = 0;
     return 0;
   }
+  tb_out = tb;
+  return box;
+}
+
+template <typename real>
+__device__ __forceinline__ int ff_flight(const Scene<real> &s, Photon<real> &ph, real cos_min) {
+  real tb;
+  const int box = ff_target(s, ph, cos_min, tb);
+  if (!box) return 0;
   const int wm = s.world_mat;
   real mu_air = interp_row(s.sig + (size_t)s.mat_comp[wm] * s.n_e, ph.ei);
   mu_air = s.mat_rho[wm] * mu_air;

@@ -156,7 +156,7 @@ class SpectEngine(DoseEngine):
         return tuple(self.kernel_ms)
 
     def last_stage_ms(self):
-        """(phantom, head, ARF) stage device times of the last run, ms."""
+        """(phantom, head, ARF or scatter-splitting copies) stage device times of the last run, ms."""
         v = [ctypes.c_double() for _ in range(3)]
         self._call("gg_last_stage_ms", *(ctypes.byref(x) for x in v))
         return tuple(x.value for x in v)

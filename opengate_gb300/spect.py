@@ -70,7 +70,7 @@ class SpectSpec:
         self.adder_policy = "EnergyWinnerPosition"
         self.blur = C.BlurDesc()
         # free flight outside the heads (set_free_flight); off by default
-        self.free_flight = C.FfDesc(0, -1.0, 0.0)
+        self.free_flight = C.FfDesc(C.FF_OFF, -1.0, 0.0, 0, 0, 0, 0.0)
 
     def set_energy_blur(self, method, sigma=0.0, resolution=0.0, reference=0.0, slope=0.0):
         """DigitizerBlurringActor on the singles' energy (MeV): method "Gaussian" (sigma),
@@ -88,7 +88,24 @@ class SpectSpec:
     def set_free_flight(self, weight_cutoff=-1.0, energy_cutoff=0.0, enabled=True):
         """GammaFreeFlightActor on the world with the heads excluded: no interaction outside
         the heads, weights exp(-optical depth), weighted projections (MeV for the cutoff)."""
-        self.free_flight = C.FfDesc(int(bool(enabled)), float(weight_cutoff), float(energy_cutoff))
+        self.free_flight = C.FfDesc(C.FF_PRIMARY if enabled else C.FF_OFF, float(weight_cutoff),
+                                    float(energy_cutoff), 0, 0, 0, 0.0)
+
+    def set_scatter_splitting(self, compton_splitting, rayleigh_splitting, max_compton_level=10,
+                              weight_cutoff=-1.0, energy_cutoff=0.0, angle_tolerance_max=0.0):
+        """ScatterSplittingFreeFlightActor on the world, the heads excluded and kill volumes:
+        analog photons outside the heads, every Compton (up to max_compton_level) and Rayleigh
+        re-sampled into compton_splitting / rayleigh_splitting weighted copies that fly freely
+        to the heads; the analog photons die at the heads.  Projections are weighted (the
+        scattered component; the primary one comes from set_free_flight).  angle_tolerance_max
+        (radians, 0 = off): copies entering a head further off its axis are dropped."""
+        nc, nr, lvl = int(compton_splitting), int(rayleigh_splitting), int(max_compton_level)
+        if not (0 <= nc <= C.MAX_SPLITTING and 0 <= nr <= C.MAX_SPLITTING):
+            raise ValueError(f"splitting factors must be in [0, {C.MAX_SPLITTING}]")
+        if lvl < 0:
+            raise ValueError("max_compton_level must be >= 0")
+        self.free_flight = C.FfDesc(C.FF_SCATTER, float(weight_cutoff), float(energy_cutoff), nc, nr, lvl,
+                                    float(angle_tolerance_max))
 
     def set_spatial_blur(self, sigma, keep_in_solid_limits=True, truncated=False):
         """DigitizerSpatialBlurringActor on the crystal position: sigma (mm) along the

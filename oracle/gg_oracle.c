@@ -422,8 +422,10 @@ typedef struct {
   int eblur, sblur, sb_keep;
   int centroid; /* adder policy EnergyWeightedCentroidPosition */
   /* free flight outside the heads (gg_ff_desc) and its weighted projection */
-  int ff;
+  int ff; /* 0 off, 1 primary free flight, 2 scatter splitting */
   real ff_wcut, ff_ecut;
+  int ss_nc, ss_nr, ss_max;
+  real ss_cos; /* angle check: copies entering a head with local dir z below this are dropped */
   uint64_t *wproj, *wproj2;
   real eb_sigma, eb_res, eb_ref, eb_slope, sb_sigma[2];
   const struct arf_s *arf; /* ARF detector model, or NULL */
@@ -499,6 +501,7 @@ static real entry_distance(const real p[3], const real d[3], const real lo[3], c
 typedef struct {
   uint64_t *acc_e, *acc_e2; /* shared per batch, updated with atomics */
   uint64_t cnt[GG_N_COUNTERS];
+  uint32_t ss_next; /* scatter splitting: copies of the current history so far */
 } tally_t;
 
 typedef struct {
@@ -567,7 +570,11 @@ typedef struct {
      the heads since its last image entry (head-to-head flights skip the ARF) */
   int visited_head, head_stage;
   real w; /* free flight: statistical weight */
+  int kind;   /* last interaction (KIND_*), set by interact */
+  int ncompt; /* scatter splitting: Compton interactions of this track */
 } photon_t;
+
+enum { KIND_COMPTON = 1, KIND_PHOTO = 2, KIND_RAYLEIGH = 3, KIND_PAIR = 4 };
 
 /* per-event crystal accumulation of each head (adder, EnergyWinnerPosition);
    wpos = head-local (a1, a2) of the energy winner */
@@ -896,19 +903,23 @@ static real interact(const scene_t *s, photon_t *ph, int mat, rng_t *g, tally_t 
   real fc = interp_row(cu, ph->ei);
   if (r < fc) {
     real ed;
+    ph->kind = KIND_COMPTON;
     compton(s, ph, g, t, &ed);
     return ed;
   }
   real fp = interp_row(cu + s->n_e, ph->ei);
   if (r < fp) {
+    ph->kind = KIND_PHOTO;
     ph->alive = 0;
     return ph->e;
   }
   real fr = interp_row(cu + 2 * s->n_e, ph->ei);
   if (r < fr) {
+    ph->kind = KIND_RAYLEIGH;
     rayleigh(s, c, ph, g, t);
     return R(0);
   }
+  ph->kind = KIND_PAIR;
   /* pair: both leptons stopped at creation, positron annihilates at rest */
   real ekin = ph->e - R(2.0 * MC2);
   real d[3];
@@ -917,6 +928,7 @@ static real interact(const scene_t *s, photon_t *ph, int mat, rng_t *g, tally_t 
     t->cnt[GG_CNT_STACK_OVERFLOW]++;
   } else {
     *sec = *ph;
+    sec->ncompt = 0;
     sec->dir[0] = -d[0];
     sec->dir[1] = -d[1];
     sec->dir[2] = -d[2];
@@ -1215,6 +1227,8 @@ static void arf_at_head(const scene_t *s, photon_t *ph, tally_t *t) {
 }
 
 /* World step with the image box and the head boxes as possible targets. */
+static void ss_split(const scene_t *s, const photon_t *pre, photon_t *ph, int mat, const rng_t *g, tally_t *t);
+
 static void spect_world_step(const scene_t *s, photon_t *ph, rng_t *g, tally_t *t, photon_t *sec,
                              int *has_sec) {
   t->cnt[GG_CNT_WORLD_STEPS]++;
@@ -1242,8 +1256,10 @@ static void spect_world_step(const scene_t *s, photon_t *ph, rng_t *g, tally_t *
   sd = sd / mu;
   if (sd < tb && sd < tout) {
     move(ph->pos, ph->dir, sd);
+    const photon_t pre = *ph;
     interact(s, ph, wm, g, t, sec, has_sec);
     ph->exclude = -1;
+    if (s->ff == 2) ss_split(s, &pre, ph, wm, g, t);
   } else if (tb <= tout) {
     move(ph->pos, ph->dir, tb);
     if (box == 0) {
@@ -1594,16 +1610,30 @@ static real image_depth(const scene_t *s, const real p[3], const real d[3], real
 /* Free flight outside the heads (GateGammaFreeFlightOptn, heads excluded): no
    interaction; straight to the nearest head entry (the head just left
    excluded) with the weight multiplied by exp(-optical depth); photons at or
-   below a cutoff, or missing every head, stop. */
-static void ff_step(const scene_t *s, photon_t *ph, tally_t *t) {
+   below a cutoff, missing every head, or (angle check of the angular
+   acceptance, before the optical depth) entering it with a direction cosine
+   to its axis below cos_min (-2: no check), stop. */
+static void ff_step(const scene_t *s, photon_t *ph, tally_t *t, real cos_min) {
   t->cnt[GG_CNT_WORLD_STEPS]++;
   if (ph->e <= s->ff_ecut || ph->w <= s->ff_wcut) {
     ph->alive = 0;
     t->cnt[GG_CNT_ESCAPED]++;
     return;
   }
+  if (cos_min > R(-1)) {
+    /* no head axis within the angle tolerance: the check below fails too */
+    int any = 0;
+    for (int h = 0; h < s->n_heads; ++h)
+      if (ph->exclude != 1 + h && !(dot3(ph->dir, s->hu[h]) < cos_min)) any = 1;
+    if (!any) {
+      ph->alive = 0;
+      t->cnt[GG_CNT_ESCAPED]++;
+      return;
+    }
+  }
   real tb = R(INFINITY);
   int box = 0;
+  real cos_box = R(0);
   real hlo[3] = {-s->half_w, -s->half_w, R(0)};
   real hhi[3] = {s->half_w, s->half_w, s->zb[3]};
   for (int h = 0; h < s->n_heads; ++h) {
@@ -1614,11 +1644,12 @@ static void ff_step(const scene_t *s, photon_t *ph, tally_t *t) {
     if (th < tb) {
       tb = th;
       box = 1 + h;
+      cos_box = ld[2];
     }
   }
   real wlo[3] = {-s->whalf[0], -s->whalf[1], -s->whalf[2]};
   const real tout = exit_distance(ph->pos, ph->dir, wlo, s->whalf);
-  if (!(tb <= tout)) {
+  if (!(tb <= tout) || cos_box < cos_min) {
     ph->alive = 0;
     t->cnt[GG_CNT_ESCAPED]++;
     return;
@@ -1661,6 +1692,57 @@ static void ff_step(const scene_t *s, photon_t *ph, tally_t *t) {
   ph->left_hole = 0;
 }
 
+/* Scatter splitting (GateScatterSplittingFreeFlightOptrActor.cpp:291-360 and
+   GateScatterSplittingFreeFlightOptn.cpp:69-149), after an interaction of the
+   analog photon outside the heads: each Compton up to max_compton_level and
+   each Rayleigh is sampled again n times from the photon's state before it
+   (pre); copy c of the history draws from Philox stream 2 + c, weighs
+   pre->w / n, flies freely to a head (ff_step), is tracked there and scores
+   its own event.  The Compton after the last level kills the analog photon
+   (without copies). */
+static void ss_split(const scene_t *s, const photon_t *pre, photon_t *ph, int mat, const rng_t *g, tally_t *t) {
+  int n = 0;
+  if (ph->kind == KIND_COMPTON && s->ss_nc > 0) {
+    if (++ph->ncompt > s->ss_max) {
+      ph->alive = 0;
+      return;
+    }
+    n = s->ss_nc;
+  } else if (ph->kind == KIND_RAYLEIGH) {
+    n = s->ss_nr;
+  }
+  const uint64_t seed = (uint64_t)g->key[0] | ((uint64_t)g->key[1] << 32);
+  const uint64_t hid = (uint64_t)g->ctr[2] | ((uint64_t)g->ctr[3] << 32);
+  for (int c = 0; c < n; ++c) {
+    rng_t gc;
+    rng_init(&gc, seed, hid, 2u + t->ss_next++);
+    photon_t cp = *pre;
+    cp.w = pre->w / (real)n;
+    if (ph->kind == KIND_COMPTON) {
+      real ed;
+      compton(s, &cp, &gc, t, &ed);
+    } else {
+      rayleigh(s, s->mat_comp[mat], &cp, &gc, t);
+    }
+    if (!cp.alive) continue;
+    cp.exclude = -1;
+    ff_step(s, &cp, t, s->ss_cos); /* with the angle check of the angular acceptance */
+    event_t ev;
+    memset(&ev, 0, sizeof(ev));
+    int steps = 0;
+    while (cp.alive) {
+      if (++steps > STEP_CAP) {
+        t->cnt[GG_CNT_LOOP_CAPPED]++;
+        cp.alive = 0;
+        break;
+      }
+      if (cp.in_head) head_step(s, &cp, &gc, t, &ev);
+      else ff_step(s, &cp, t, R(-2));
+    }
+    score_singles(s, &ev, t, &gc);
+  }
+}
+
 static void transport_photon(const scene_t *s, photon_t *ph, rng_t *g, tally_t *t, hlist_t *l,
                              photon_t *sec, int *has_sec, event_t *ev) {
   int steps = 0;
@@ -1671,8 +1753,8 @@ static void transport_photon(const scene_t *s, photon_t *ph, rng_t *g, tally_t *
       ph->alive = 0;
       break;
     }
-    if (s->ff && !ph->in_head) {
-      ff_step(s, ph, t);
+    if (s->ff == 1 && !ph->in_head) {
+      ff_step(s, ph, t, R(-2));
       continue;
     }
     if (ph->in_image) {
@@ -1711,14 +1793,21 @@ static void transport_photon(const scene_t *s, photon_t *ph, rng_t *g, tally_t *
       if (u2 * ph->mumax >= mu) continue;
       t->cnt[GG_CNT_REAL_INTERACTIONS]++;
       const real e_pre = ph->e;
+      const photon_t pre = *ph;
       real ed = interact(s, ph, m, g, t, sec, has_sec);
       /* electrons of a track-length-scored photon deposit nothing (GateTLEDoseActor.cpp:236-243) */
       if (!s->spect && !(s->tle && e_pre <= s->tle_thr)) deposit(l, t, v, ed);
       if (ph->alive && ph->in_image) ph->t_exit = exit_distance(ph->pos, ph->dir, s->bmin, s->bmax);
+      if (s->ff == 2) ss_split(s, &pre, ph, m, g, t);
     } else if (ph->in_head) {
       head_step(s, ph, g, t, ev);
     } else if (s->spect) {
       spect_world_step(s, ph, g, t, sec, has_sec);
+      if (s->ff == 2 && ph->alive && ph->in_head) {
+        /* scatter splitting: the heads are kill volumes of the analog photon */
+        ph->alive = 0;
+        t->cnt[GG_CNT_ESCAPED]++;
+      }
     } else {
       t->cnt[GG_CNT_WORLD_STEPS]++;
       real tin = ph->can_enter ? entry_distance(ph->pos, ph->dir, s->bmin, s->bmax) : R(INFINITY);
@@ -1758,6 +1847,8 @@ static int run_history(const scene_t *s, uint64_t seed, uint64_t h, tally_t *t) 
   int st = sample_primary(s, &g, &ph, t);
   if (st != GG_OK) return st;
   t->cnt[GG_CNT_HISTORIES]++;
+  t->ss_next = 0;
+  ph.ncompt = 0;
   start_photon(s, &ph);
   for (;;) {
     transport_photon(s, &ph, &g, t, &l, &sec, &has_sec, &ev);
@@ -2060,9 +2151,15 @@ static int run_spect_impl(const gg_tables_desc *tb, const gg_volume_desc *vol, c
   s.proj = proj;
   s.arf = arf;
   if (ff && ff->enabled) {
-    s.ff = 1;
+    s.ff = ff->enabled == 2 ? 2 : 1;
     s.ff_wcut = (real)ff->weight_cutoff;
     s.ff_ecut = (real)ff->energy_cutoff;
+    if (s.ff == 2) {
+      s.ss_nc = ff->compton_splitting;
+      s.ss_nr = ff->rayleigh_splitting;
+      s.ss_max = ff->max_compton_level;
+      s.ss_cos = (real)(ff->angle_tolerance_max > 0.0 ? cos(ff->angle_tolerance_max) : -2.0);
+    }
     s.wproj = wproj;
     s.wproj2 = wproj2;
   }

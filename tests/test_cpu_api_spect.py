@@ -179,3 +179,54 @@ def test_blur_actor_validation():
     b.blur_attribute = "GlobalTime"
     with pytest.raises(NotImplementedError):
         b.energy_blur()
+
+
+def test_free_flight_actors_set_the_modes(tmp_path):
+    """GammaFreeFlightActor -> primary free flight; ScatterSplittingFreeFlightActor ->
+    scatter splitting with its factors (-1 = splitting_factor), level and angle check."""
+    from opengate_gb300 import _capi as C
+
+    sim, heads = spect_sim(tmp_path)
+    ff = sim.add_actor("GammaFreeFlightActor", "ff")
+    ff.exclude_volumes = [h.name for h, _ in heads]
+    _, sp, _, _, _ = sim.build_spect()
+    assert sp.free_flight.enabled == C.FF_PRIMARY
+    sim.actors.pop("ff")
+    ss = sim.add_actor("ScatterSplittingFreeFlightActor", "ss")
+    ss.exclude_volumes = [h.name for h, _ in heads]
+    with pytest.raises(NotImplementedError):
+        sim.build_spect()  # the heads must be kill volumes
+    ss.kill_interacting_in_volumes = [f"{h.name}_crystal" for h, _ in heads]
+    ss.splitting_factor = 7
+    ss.rayleigh_splitting_factor = 3
+    ss.max_compton_level = 4
+    ss.weight_cutoff = 1e-9
+    ss.angular_acceptance.policy = "Rejection"
+    ss.angular_acceptance.enable_intersection_check = True
+    ss.angular_acceptance.enable_angle_check = True
+    ss.angular_acceptance.angle_tolerance_max = 10 * u.deg
+    _, sp, _, _, _ = sim.build_spect()
+    f = sp.free_flight
+    assert (f.enabled, f.compton_splitting, f.rayleigh_splitting, f.max_compton_level) == (C.FF_SCATTER, 7, 3, 4)
+    assert f.weight_cutoff == 1e-9 and f.angle_tolerance_max == pytest.approx(math.radians(10))
+    ss.angular_acceptance.angle_tolerance_min = 1 * u.deg
+    with pytest.raises(NotImplementedError):
+        sim.build_spect()
+    ss.angular_acceptance.angle_tolerance_min = 0.0
+    sim.add_actor("GammaFreeFlightActor", "ff2").exclude_volumes = [h.name for h, _ in heads]
+    with pytest.raises(NotImplementedError):
+        sim.build_spect()  # one free-flight actor
+
+
+def test_scatter_splitting_arguments():
+    from opengate_gb300 import spect as S
+
+    sp = S.SpectSpec()
+    with pytest.raises(ValueError):
+        sp.set_scatter_splitting(-1, 2)
+    with pytest.raises(ValueError):
+        sp.set_scatter_splitting(5000, 2)
+    with pytest.raises(ValueError):
+        sp.set_scatter_splitting(5, 2, max_compton_level=-1)
+    sp.set_scatter_splitting(5, 2)
+    assert sp.free_flight.max_compton_level == 10

@@ -179,3 +179,93 @@ def test_free_flight_equals_analog_without_attenuation():
         sigma = np.sqrt(a + ff2[:, k].sum())
         assert abs(a - f) < 4 * sigma + 1e-9, (k, a, f, sigma)
     assert analog[:, 0].sum() > 2000
+
+
+@pytest.mark.parametrize("precision", [32, 64])
+def test_scatter_splitting_bit_exact(precision):
+    """Scatter splitting: analog photons outside the heads, each Compton / Rayleigh
+    re-sampled into weighted copies on their own random streams, copies in free flight
+    to the heads (angle check on).  Weighted projections, squares and counters identical
+    to the oracle's."""
+    scene, sp, _ = _case("tc99m_lehr")
+    sp.set_scatter_splitting(8, 4, 3, weight_cutoff=1e-7, energy_cutoff=0.01, angle_tolerance_max=0.6)
+    n = 60_000
+    from opengate_gb300.engine import SpectEngine
+
+    with SpectEngine(scene, sp, precision=precision) as eng:
+        eng.run(n, 71)
+        w, w2 = eng.weighted_projection(squared=True)
+        cnt = eng.counters()
+        assert eng.projection().sum() == 0
+    rw, rw2, rcnt = O.run_spect_ff(scene, sp, n, seed=71, threads=8, precision=precision)
+    np.testing.assert_array_equal(w, rw)
+    np.testing.assert_array_equal(w2, rw2)
+    assert cnt == rcnt
+    assert w.sum() > 0 and w.max() < 1.0
+
+
+def test_scatter_splitting_queue_overflow_repeats_the_pass():
+    """Many copies per history and short batches: the head queue overflows, the phantom
+    pass is repeated on fewer histories, and the result stays the oracle's, bit for bit
+    (counters included: the overflowed pass leaves none behind)."""
+    scene, sp, _ = _case("tc99m_lehr", n_runs=1)
+    sp.set_scatter_splitting(64, 16, 5)
+    n, batch = 24_000, 1024
+    from opengate_gb300.engine import SpectEngine
+
+    with SpectEngine(scene, sp, batch=batch) as eng:
+        eng.run(n, 73)
+        w, w2 = eng.weighted_projection(squared=True)
+        cnt = eng.counters()
+        launches = eng.last_kernel_ms()[3]
+    nb = (n + batch - 1) // batch
+    assert launches > 3 * nb  # generate + phantom + head per batch, plus the repeated / split passes
+    rw, rw2, rcnt = O.run_spect_ff(scene, sp, n, seed=73, threads=8)
+    np.testing.assert_array_equal(w, rw)
+    np.testing.assert_array_equal(w2, rw2)
+    assert cnt == rcnt
+
+
+def test_free_flight_plus_scatter_splitting_equal_analog():
+    """The reference's free-flight SPECT recipe: the primary (GammaFreeFlightActor) and
+    the scattered (ScatterSplittingFreeFlightActor) weighted projections add up to the
+    analog acquisition, window by window and head by head, within the statistics."""
+    scene, sp, _ = _case("tc99m_lehr", n_runs=1)
+    from opengate_gb300.engine import SpectEngine
+
+    n_a, n_f, n_s = 400_000_000, 60_000_000, 12_000_000
+    with SpectEngine(scene, sp) as eng:
+        eng.run(n_a, 81)
+        analog = eng.projection()
+    sp.set_free_flight()
+    with SpectEngine(scene, sp) as eng:
+        eng.run(n_f, 82)
+        ff, ff2 = eng.weighted_projection(squared=True)
+    # the copies of one history are correlated: the scattered part's variance comes
+    # from independent chunks of histories
+    sp.set_scatter_splitting(20, 5, 1000)
+    n_chunks = 12
+    m = n_s // n_chunks
+    shape = sp.projection_shape()
+    axes = tuple(range(2, len(shape)))
+    chunks = []
+    with SpectEngine(scene, sp) as eng:
+        prev = 0.0
+        for k in range(n_chunks):
+            eng.run(m, 83, first=k * m)
+            cur, _ = eng.weighted_projection(squared=True)
+            chunks.append((cur - prev).reshape(shape).sum(axis=axes))
+            prev = cur
+        ss = prev
+    chunks = np.array(chunks)
+    kf, ks = n_a / n_f, n_a / (m * n_chunks)
+    a_t = analog.reshape(shape).sum(axis=axes)
+    ss_t = ss.reshape(shape).sum(axis=axes) * ks
+    e_t = ff.reshape(shape).sum(axis=axes) * kf + ss_t
+    var_ss = ks * ks * n_chunks * chunks.var(axis=0, ddof=1)
+    v_t = a_t + (ff2.reshape(shape).sum(axis=axes) * kf * kf) + var_ss
+    z = (a_t - e_t) / np.sqrt(v_t)
+    print("analog", a_t.tolist(), "primary + scatter", e_t.tolist(), "z", z.tolist())
+    assert np.all(np.abs(z) < 4.5), (a_t, e_t, z)
+    assert a_t.min() > 3000
+    assert (ss * ks).reshape(shape).sum(axis=axes)[..., 1].min() > 0.3 * e_t[..., 1].min()
