@@ -367,12 +367,14 @@ class ActorOutput:
         return self.image
 
     def get_output_path(self):
+        """The actor's output_filename with the output's name inserted before the extension
+        (``projection_1.mhd`` -> ``projection_1_counts.mhd``; actoroutput.py:1053-1058)."""
         base = self.actor.output_filename
         if base in (None, "auto", ""):
             base = f"{self.actor.name}.mhd"
         base = pathlib.Path(base)
         sim = self.actor.simulation
-        return pathlib.Path(sim.output_dir) / f"{base.stem}_{self.suffix}.mhd"
+        return pathlib.Path(sim.output_dir) / base.parent / f"{base.stem}_{self.suffix}.mhd"
 
 
 class DoseActor(GateObject):
@@ -451,12 +453,16 @@ class DigitizerProjectionActor(GateObject):
     user_info_defaults = {"attached_to": None, "input_digi_collections": [], "channels": [],
                           "size": [128, 128], "spacing": [4.42 * u.mm, 4.42 * u.mm], "output_filename": "auto",
                           "write_to_disk": True, "detector_orientation_matrix": np.eye(3),
-                          "squared_counts": False, "priority": 100}
+                          "priority": 100}
 
     def __init__(self, name, simulation=None, **kw):
         super().__init__(name, simulation, **kw)
         object.__setattr__(self, "counts", ActorOutput(self, "counts", True))
-        object.__setattr__(self, "counts_squared", ActorOutput(self, "squared_counts", False))
+        # history-by-history squared counts (free flight: summed squared weights), written
+        # when ``squared_counts.active`` is set, as in the reference
+        sq = ActorOutput(self, "squared_counts", False)
+        object.__setattr__(self, "squared_counts", sq)
+        object.__setattr__(self, "counts_squared", sq)
 
 
 FWHM_TO_SIGMA = 1.0 / (2.0 * math.sqrt(2.0 * math.log(2.0)))
@@ -871,10 +877,13 @@ class Simulation:
             a.counts.image = img
             a.counts.number_of_samples = first
             a.counts_squared.image = image_io.Image(proj2[h].copy(), [sx, sy, 1.0], origin)
+            a.counts_squared.number_of_samples = first
             if a.write_to_disk:
-                out = a.output_filename
-                path = self.get_output_path(f"{a.name}_counts.mhd" if out in (None, "", "auto") else out)
+                path = a.counts.get_output_path()
+                path.parent.mkdir(parents=True, exist_ok=True)
                 image_io.write_mhd(path, img)
+                if a.squared_counts.active:
+                    image_io.write_mhd(a.squared_counts.get_output_path(), a.counts_squared.image)
         for a in self.actors.values():
             if isinstance(a, SimulationStatisticsActor):
                 a.counts.runs = len(runs)

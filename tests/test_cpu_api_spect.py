@@ -230,3 +230,45 @@ def test_scatter_splitting_arguments():
         sp.set_scatter_splitting(5, 2, max_compton_level=-1)
     sp.set_scatter_splitting(5, 2)
     assert sp.free_flight.max_compton_level == 10
+
+
+def test_projection_output_names_follow_the_reference(tmp_path):
+    """output_filename 'projection_1_ffa.mhd' -> projection_1_ffa_counts.mhd and, with
+    squared_counts.active, projection_1_ffa_squared_counts.mhd."""
+    sim, heads = spect_sim(tmp_path)
+    proj = heads[0][1].projection
+    proj.output_filename = "projection_1_ffa.mhd"
+    proj.squared_counts.active = True
+    assert proj.counts.get_output_path() == tmp_path / "projection_1_ffa_counts.mhd"
+    assert proj.squared_counts.get_output_path() == tmp_path / "projection_1_ffa_squared_counts.mhd"
+    assert proj.counts_squared is proj.squared_counts
+
+
+def test_merge_freeflight_uncertainty(tmp_path):
+    """Primary + scatter components merged as the reference's helper does: means add, the
+    variances of the means add; files written with the reference's names."""
+    from opengate_gb300 import image_io
+    from opengate_gb300.contrib.spect import spect_freeflight_helpers as ffh
+
+    rng = np.random.default_rng(3)
+    shape = (2, 4, 5)
+    comps = {"primary": 1000, "scatter": 400, "skipped": 1}
+    cs, c2s = {}, {}
+    for name, n in comps.items():
+        c = rng.uniform(0.0, 5.0, shape)
+        c2 = c * rng.uniform(0.05, 0.5, shape)
+        cs[name], c2s[name] = c, c2
+        for h in range(2):
+            image_io.write_mhd(tmp_path / name / f"projection_{h}_counts.mhd", image_io.Image(c * (h + 1), [2, 2, 1]))
+            image_io.write_mhd(tmp_path / name / f"projection_{h}_squared_counts.mhd",
+                               image_io.Image(c2 * (h + 1), [2, 2, 1]))
+    out = ffh.merge_freeflight_uncertainty_for_all_heads(tmp_path, 5000, list(comps), list(comps.values()), 2)
+    e = sum(cs[k] / n for k, n in comps.items() if n > 1)
+    v = sum(np.clip((c2s[k] / n - (cs[k] / n) ** 2) / (n - 1), 0, None) for k, n in comps.items() if n > 1)
+    np.testing.assert_allclose(out[0][0].array, e * 5000, rtol=1e-12)
+    np.testing.assert_allclose(out[0][1].array, np.sqrt(v) / e, rtol=1e-12)
+    h1 = image_io.read_mhd(tmp_path / "projection_1_counts.mhd").array
+    np.testing.assert_allclose(h1, 2 * e * 5000, rtol=1e-6)
+    assert (tmp_path / "relative_uncertainty_1_counts.mhd").exists()
+    with pytest.raises(ValueError):
+        ffh.merge_freeflight_uncertainty(tmp_path, 1, ["primary"], [1000, 2])

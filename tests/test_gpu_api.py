@@ -82,3 +82,42 @@ def test_spect_simulation_matches_oracle(tmp_path, built_lib):
         np.testing.assert_array_equal(proj, ref[head_of[digi.projection.attached_to]])
         assert digi.projection.counts.get_output_path().exists()
     assert ref.sum() > 0
+
+
+def test_free_flight_recipe_through_the_api(tmp_path, built_lib):
+    """The reference's free-flight recipe through the API: a primary simulation
+    (GammaFreeFlightActor) and a scatter simulation (ScatterSplittingFreeFlightActor) write
+    projection_<h>_counts / _squared_counts per component; spect_freeflight_helpers merges
+    them; each component equals its oracle run bit for bit."""
+    from oracle import oracle as O
+
+    from opengate_gb300 import image_io
+    from opengate_gb300.contrib.spect import spect_freeflight_helpers as ffh
+
+    from .test_cpu_api_spect import spect_sim
+
+    n = 200_000
+    for sub, kind in (("primary", "GammaFreeFlightActor"), ("scatter", "ScatterSplittingFreeFlightActor")):
+        sim, heads = spect_sim(tmp_path / sub, n_per_run=n, angles=2)
+        sim.random_seed = 99
+        for h, (head, digi) in enumerate(heads):
+            digi.projection.output_filename = f"projection_{h}.mhd"
+            digi.projection.squared_counts.active = True
+        ff = sim.add_actor(kind, "ff")
+        ff.exclude_volumes = [head.name for head, _ in heads]
+        if kind == "ScatterSplittingFreeFlightActor":
+            ff.kill_interacting_in_volumes = [head.name for head, _ in heads]
+            ff.compton_splitting_factor = 20
+            ff.rayleigh_splitting_factor = 5
+        sim.run()
+        scene, sp, _, _, head_of = sim.build_spect()
+        w, w2, _ = O.run_spect_ff(scene, sp, n, 99, threads=8)
+        for h, (head, digi) in enumerate(heads):
+            got = image_io.read_mhd(tmp_path / sub / f"projection_{h}_counts.mhd").array
+            got2 = image_io.read_mhd(tmp_path / sub / f"projection_{h}_squared_counts.mhd").array
+            k = head_of[digi.projection.attached_to]
+            np.testing.assert_array_equal(got, w[k].astype(got.dtype))
+            np.testing.assert_array_equal(got2, w2[k].astype(got2.dtype))
+    merged = ffh.merge_freeflight_uncertainty_for_all_heads(tmp_path, 2 * n, ["primary", "scatter"], [2 * n, 2 * n], 2)
+    for counts, unc in merged:
+        assert counts.array.sum() > 0 and np.all(unc.array >= 0)
