@@ -573,15 +573,6 @@ class GammaFreeFlightActor(GateObject):
                 raise NotImplementedError(f"free flight must exclude the SPECT head '{h.name}' (exclude_volumes)")
 
 
-def _default_angular_acceptance():
-    """Angular-acceptance parameters (biasingactors.py:16-64 generic_source_default_aa)."""
-    return Box({"policy": None, "skip_policy": "SkipEvents", "max_rejection": 10000, "target_volumes": [],
-                "enable_intersection_check": False, "enable_angle_check": False,
-                "angle_check_reference_vector": [0, 0, 1], "angle_check_proximity_distance": 0.0,
-                "angle_tolerance_proximal": 90 * u.deg, "angle_tolerance_min": 0.0,
-                "angle_tolerance_max": 6 * u.deg})
-
-
 class ScatterSplittingFreeFlightActor(GateObject):
     """Scatter splitting with free flight (ScatterSplittingFreeFlightActor,
     opengate/actors/biasingactors.py:368-460; GateScatterSplittingFreeFlightOptrActor.cpp:200-420 and

@@ -281,24 +281,32 @@ __device__ __forceinline__ void rot_apply(const real m[9], const real v[3], real
   }
 }
 
+// Isotropic direction between the source's theta and phi bounds from two
+// uniforms (GateSPSAngDistribution::GenerateIsotropicFlux).
+template <typename real>
+__device__ __forceinline__ void iso_direction(const Scene<real> &s, real u, real v, real d[3]) {
+  real cost = s.s_cos_tmin - s.s_cos_tmax;
+  cost = u * cost;
+  cost = s.s_cos_tmin - cost;
+  real st2 = cost * cost;
+  st2 = R<real>(1) - st2;
+  real sint = gg_sqrt(st2 > R<real>(0) ? st2 : R<real>(0));
+  real f = s.s_dphi_turn * v;
+  f = s.s_phi0_turn + f;
+  f = f - gg_floor(f);
+  real sp, cp;
+  gg_sincos_turn(f, sp, cp);
+  d[0] = -(sint * cp);
+  d[1] = -(sint * sp);
+  d[2] = -cost;
+}
+
 template <typename real, typename G>
 __device__ __forceinline__ void sample_direction(const Scene<real> &s, const real p[3], G &g, real d[3]) {
   if (s.dir_type == GG_DIR_ISO) {
-    real u = u01<real>(g);
-    real cost = s.s_cos_tmin - s.s_cos_tmax;
-    cost = u * cost;
-    cost = s.s_cos_tmin - cost;
-    real st2 = cost * cost;
-    st2 = R<real>(1) - st2;
-    real sint = gg_sqrt(st2 > R<real>(0) ? st2 : R<real>(0));
-    real f = s.s_dphi_turn * u01<real>(g);
-    f = s.s_phi0_turn + f;
-    f = f - gg_floor(f);
-    real sp, cp;
-    gg_sincos_turn(f, sp, cp);
-    d[0] = -(sint * cp);
-    d[1] = -(sint * sp);
-    d[2] = -cost;
+    const real u = u01<real>(g);
+    const real v = u01<real>(g);
+    iso_direction(s, u, v, d);
   } else if (s.dir_type == GG_DIR_MOMENTUM) {
     d[0] = s.s_mom[0];
     d[1] = s.s_mom[1];
@@ -327,11 +335,9 @@ __device__ __forceinline__ bool accept_dir(const Scene<real> &s, const real p[3]
   return false;
 }
 
-// GateGenericSource::GeneratePrimaries order: position, direction (with the
-// acceptance loop of GateSingleParticleSource::GenerateDirectionWithAA),
-// energy.
+// Source position (GateSPSPosDistribution: point, box, sphere, disc, voxels).
 template <typename real, typename G>
-__device__ __forceinline__ int sample_primary(const Scene<real> &s, G &g, Photon<real> &ph, BlockCounters *bc) {
+__device__ __forceinline__ void sample_position(const Scene<real> &s, G &g, Photon<real> &ph, BlockCounters *bc) {
   real loc[3] = {R<real>(0), R<real>(0), R<real>(0)};
   int pt = s.pos_type;
   if (pt == GG_POS_BOX) {
@@ -406,6 +412,12 @@ __device__ __forceinline__ int sample_primary(const Scene<real> &s, G &g, Photon
 #pragma unroll
     for (int a = 0; a < 3; ++a) ph.pos[a] = s.s_t[a] + off[a];
   }
+}
+
+// Direction with the acceptance loop, one history.
+template <typename real, typename G>
+__device__ __forceinline__ int sample_direction_accepted(const Scene<real> &s, G &g, Photon<real> &ph,
+                                                         BlockCounters *bc) {
   int tries = 0;
   for (;;) {
     sample_direction(s, ph.pos, g, ph.dir);
@@ -413,6 +425,125 @@ __device__ __forceinline__ int sample_primary(const Scene<real> &s, G &g, Photon
     atomicAdd(&bc->skipped, 1u);
     if (++tries > s.max_rejection) return GG_ERR_DOMAIN;
   }
+  return GG_OK;
+}
+
+__device__ __forceinline__ uint32_t block_word(const uint4 &b, uint32_t w) {
+  return w == 0 ? b.x : (w == 1 ? b.y : (w == 2 ? b.z : b.w));
+}
+
+// Words q and q + 1 (0-based counts of 32-bit draws) of a history's Philox
+// stream: one block, or two when the pair straddles a block boundary.
+__device__ __forceinline__ void stream_pair(const Rng &g, uint32_t q, uint32_t &x, uint32_t &y) {
+  const uint4 b = philox_block(q >> 2, g.stream, g.h0, g.h1, g.k0, g.k1);
+  x = block_word(b, q & 3u);
+  if ((q & 3u) != 3u) {
+    y = block_word(b, (q + 1u) & 3u);
+  } else {
+    const uint4 c = philox_block((q >> 2) + 1u, g.stream, g.h0, g.h1, g.k0, g.k1);
+    y = c.x;
+  }
+}
+
+// Isotropic directions with the acceptance loop for the histories of a warp
+// together (every lane calls it; `need`: the lane's history wants a
+// direction; its position is set and p0 words of its stream are drawn).
+// Trial k of a history draws words p0 + 2k and p0 + 2k + 1, so trials can be
+// evaluated out of order: each round deals the 32 lanes over the histories
+// still waiting (lane l evaluates trial next + l / np of waiting history
+// l % np) and every history takes its first accepted trial.  Results, draws
+// and the rejection count per history equal those of
+// sample_direction_accepted; the lanes stay converged instead of waiting for
+// the warp's longest loop.  On return g stands after the accepted trial.
+template <typename real>
+__device__ __forceinline__ int warp_iso_direction_accepted(const Scene<real> &s, RngAhead &g, Photon<real> &ph,
+                                                           bool need, BlockCounters *bc) {
+  const unsigned lane = threadIdx.x & 31u;
+  const uint32_t p0 = (g.blk - 1u) * 4u + (uint32_t)g.idx;  // words drawn so far (Rng / RngAhead state)
+  const uint32_t max_rej = (uint32_t)s.max_rejection;
+  bool pending = need;
+  uint32_t next = 0;  // first trial not yet evaluated
+  int status = GG_OK;
+  uint32_t k_acc = 0;
+  for (;;) {
+    const unsigned m = __ballot_sync(0xffffffffu, pending);
+    if (m == 0u) break;
+    const int np = __popc(m);
+    const int r = (int)lane % np;
+    const int owner = (int)__fns(m, 0u, r + 1);
+    const uint32_t o_p0 = __shfl_sync(0xffffffffu, p0, owner);
+    const uint32_t o_next = __shfl_sync(0xffffffffu, next, owner);
+    Rng o = g;  // the owner's stream: key and counter words
+    o.h0 = __shfl_sync(0xffffffffu, g.h0, owner);
+    o.h1 = __shfl_sync(0xffffffffu, g.h1, owner);
+    real op[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) op[a] = __shfl_sync(0xffffffffu, ph.pos[a], owner);
+    const uint32_t q = o_p0 + 2u * (o_next + (uint32_t)((int)lane / np));
+    uint32_t wu, wv;
+    stream_pair(o, q, wu, wv);
+    const real u = (real)(wu >> 8) * R<real>(5.9604644775390625e-08);
+    const real v = (real)(wv >> 8) * R<real>(5.9604644775390625e-08);
+    real d[3];
+    iso_direction(s, u, v, d);
+    const unsigned am = __ballot_sync(0xffffffffu, accept_dir(s, op, d));
+    int src = (int)lane;
+    bool won = false;
+    if (pending) {
+      const int rk = __popc(m & ((1u << lane) - 1u));  // this history's rank among the waiting ones
+      unsigned grp = 0u;
+      for (int l = rk; l < 32; l += np) grp |= 1u << l;
+      const unsigned hits = am & grp;
+      if (hits) {
+        const int w = __ffs(hits) - 1;
+        k_acc = next + (uint32_t)(w / np);
+        src = w;
+        won = true;
+        pending = false;
+        if (k_acc > max_rej) {
+          status = GG_ERR_DOMAIN;
+          k_acc = max_rej + 1u;
+        }
+      } else {
+        next += (uint32_t)__popc(grp);
+        if (next > max_rej) {
+          status = GG_ERR_DOMAIN;
+          k_acc = max_rej + 1u;
+          pending = false;
+        }
+      }
+    }
+    // the winning lane's direction to the history's lane
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      const real x = __shfl_sync(0xffffffffu, d[a], src);
+      if (won) ph.dir[a] = x;
+    }
+  }
+  if (!need) return GG_OK;
+  if (k_acc) atomicAdd(&bc->skipped, k_acc);
+  if (status != GG_OK) return status;
+  // the stream after the accepted trial
+  const uint32_t pe = p0 + 2u * (k_acc + 1u);
+  g.ahead = false;
+  if ((pe & 3u) == 0u) {
+    g.blk = pe >> 2;
+    g.idx = 4;
+    g.buf[0] = g.buf[1] = g.buf[2] = g.buf[3] = 0u;
+  } else {
+    const uint4 b = philox_block(pe >> 2, g.stream, g.h0, g.h1, g.k0, g.k1);
+    g.buf[0] = b.x;
+    g.buf[1] = b.y;
+    g.buf[2] = b.z;
+    g.buf[3] = b.w;
+    g.blk = (pe >> 2) + 1u;
+    g.idx = (int)(pe & 3u);
+  }
+  return GG_OK;
+}
+
+template <typename real, typename G>
+__device__ __forceinline__ void sample_energy(const Scene<real> &s, G &g, Photon<real> &ph) {
   real e;
   int et = s.ene_type;
   if (et == GG_ENE_MONO) {
@@ -446,6 +577,17 @@ __device__ __forceinline__ int sample_primary(const Scene<real> &s, G &g, Photon
   ph.can_enter = 1;
   ph.in_image = 0;
   set_energy(s, ph, e);
+}
+
+// GateGenericSource::GeneratePrimaries order: position, direction (with the
+// acceptance loop of GateSingleParticleSource::GenerateDirectionWithAA),
+// energy.
+template <typename real, typename G>
+__device__ __forceinline__ int sample_primary(const Scene<real> &s, G &g, Photon<real> &ph, BlockCounters *bc) {
+  sample_position(s, g, ph, bc);
+  const int st = sample_direction_accepted(s, g, ph, bc);
+  if (st != GG_OK) return st;
+  sample_energy(s, g, ph);
   return GG_OK;
 }
 

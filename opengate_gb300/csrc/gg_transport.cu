@@ -34,12 +34,70 @@
 
 namespace gg {
 
+// First step of a sampled primary in the source stage: a photon outside the
+// image takes its first world flight here (dose; SPECT leaves it to the
+// transport stage, whose world step also targets the heads).  Sets the
+// record state; true when a world step was taken.
+template <typename real>
+__device__ __forceinline__ bool first_flight(const Scene<real> &s, RngAhead &g, Photon<real> &ph, uint32_t &state,
+                                             uint32_t &steps, BlockCounters *bc) {
+  if (ph.in_image) {
+    state = kRecInImage;
+    return false;
+  }
+  if (s.spect) {
+    state = kRecWorld;
+    return false;
+  }
+  steps = 1;
+  real inf = gg_inf(real(0));
+  real tin = ph.can_enter ? entry_distance(ph.pos, ph.dir, s.bmin, s.bmax) : inf;
+  real wlo[3] = {-s.whalf[0], -s.whalf[1], -s.whalf[2]};
+  real tout = exit_distance(ph.pos, ph.dir, wlo, s.whalf);
+  int wm = s.world_mat;
+  real mu = interp_row(s.sig + (size_t)s.mat_comp[wm] * s.n_e, ph.ei);
+  mu = s.mat_rho[wm] * mu;
+  real u = u01_open0<real>(g);
+  real sd = -gg_log(u);
+  sd = sd / mu;
+  if (sd < tin && sd < tout) {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) ph.pos[k] = ph.pos[k] + sd * ph.dir[k];
+    state = kRecPendingWorld;
+  } else if (tin <= tout) {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) ph.pos[k] = ph.pos[k] + tin * ph.dir[k];
+    state = kRecInImage;
+  } else {
+    atomicAdd(&bc->escaped, 1u);
+  }
+  return true;
+}
+
+template <typename real>
+__device__ __forceinline__ void write_record(const Records<real> &rec, uint64_t i, const Photon<real> &ph,
+                                             const RngAhead &g, uint32_t state, uint32_t steps, uint32_t sim) {
+  rec.px[i] = ph.pos[0];
+  rec.py[i] = ph.pos[1];
+  rec.pz[i] = ph.pos[2];
+  rec.dx[i] = ph.dir[0];
+  rec.dy[i] = ph.dir[1];
+  rec.dz[i] = ph.dir[2];
+  rec.e[i] = ph.e;
+  rec.flags[i] = state | (steps << 2);
+  rec.rng_pos[i] = (g.blk << 3) | (uint32_t)g.idx;
+  rec.rng_buf[i] = make_uint4(g.buf[0], g.buf[1], g.buf[2], g.buf[3]);
+  rec.sim[i] = sim;
+}
+
 // Source stage: one thread per history.  Samples the primary
 // (GateGenericSource::GeneratePrimaries order), places it, and performs the
 // first transport iteration when the photon starts in the world (free flight
 // to the image, to an air interaction, or out of the world).
 // MULTI: batched simulations (Scene::sims): the thread's history picks its
-// simulation, whose geometry, source and Philox key it then uses.
+// simulation, whose geometry, source and Philox key it then uses.  Without
+// MULTI, isotropic directions with an acceptance loop are sampled by the
+// warp together (warp_iso_direction_accepted).
 template <typename real, bool MULTI>
 __global__ void __launch_bounds__(256) k_generate(Scene<real> s, KernelArgs a) {
   __shared__ BlockCounters bc;
@@ -48,7 +106,30 @@ __global__ void __launch_bounds__(256) k_generate(Scene<real> s, KernelArgs a) {
   const uint64_t n = a.h_end - a.h_begin;
   const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   bool sampled = false, world_step = false;  // counted per block below
-  if (i < n) {
+  // isotropic directions with an acceptance loop: the warp samples them together
+  const bool warp_dirs = !MULTI && s.dir_type == GG_DIR_ISO && s.n_accept > 0;
+  if (warp_dirs) {
+    Records<real> rec = Records<real>::carve(a.records, a.rec_cap);
+    RngAhead g;  // blocks made on demand: the warp's trials read the stream directly
+    g.init(a.seed, a.h_begin + i, 0u);
+    g.ahead = false;
+    Photon<real> ph;
+    const bool live = i < n;
+    if (live) sample_position(s, g, ph, &bc);
+    int st = warp_iso_direction_accepted(s, g, ph, live, &bc);
+    if (live) {
+      uint32_t state = kRecDead, steps = 0;
+      if (st != GG_OK) {
+        atomicOr(a.status, (unsigned int)st);
+      } else {
+        sample_energy(s, g, ph);
+        sampled = true;
+        start_photon(s, ph);
+        world_step = first_flight(s, g, ph, state, steps, &bc);
+      }
+      write_record(rec, i, ph, g, state, steps, 0u);
+    }
+  } else if (i < n) {
     Records<real> rec = Records<real>::carve(a.records, a.rec_cap);
     RngAhead g;
     uint32_t sim = 0;
@@ -70,47 +151,9 @@ __global__ void __launch_bounds__(256) k_generate(Scene<real> s, KernelArgs a) {
     } else {
       sampled = true;
       start_photon(s, ph);
-      if (ph.in_image) {
-        state = kRecInImage;
-      } else if (s.spect) {
-        state = kRecWorld;  // the world step also targets the heads: left to the transport stage
-      } else {
-        steps = 1;
-        world_step = true;
-        real inf = gg_inf(real(0));
-        real tin = ph.can_enter ? entry_distance(ph.pos, ph.dir, s.bmin, s.bmax) : inf;
-        real wlo[3] = {-s.whalf[0], -s.whalf[1], -s.whalf[2]};
-        real tout = exit_distance(ph.pos, ph.dir, wlo, s.whalf);
-        int wm = s.world_mat;
-        real mu = interp_row(s.sig + (size_t)s.mat_comp[wm] * s.n_e, ph.ei);
-        mu = s.mat_rho[wm] * mu;
-        real u = u01_open0<real>(g);
-        real sd = -gg_log(u);
-        sd = sd / mu;
-        if (sd < tin && sd < tout) {
-#pragma unroll
-          for (int k = 0; k < 3; ++k) ph.pos[k] = ph.pos[k] + sd * ph.dir[k];
-          state = kRecPendingWorld;
-        } else if (tin <= tout) {
-#pragma unroll
-          for (int k = 0; k < 3; ++k) ph.pos[k] = ph.pos[k] + tin * ph.dir[k];
-          state = kRecInImage;
-        } else {
-          atomicAdd(&bc.escaped, 1u);
-        }
-      }
+      world_step = first_flight(s, g, ph, state, steps, &bc);
     }
-    rec.px[i] = ph.pos[0];
-    rec.py[i] = ph.pos[1];
-    rec.pz[i] = ph.pos[2];
-    rec.dx[i] = ph.dir[0];
-    rec.dy[i] = ph.dir[1];
-    rec.dz[i] = ph.dir[2];
-    rec.e[i] = ph.e;
-    rec.flags[i] = state | (steps << 2);
-    rec.rng_pos[i] = (g.blk << 3) | (uint32_t)g.idx;
-    rec.rng_buf[i] = make_uint4(g.buf[0], g.buf[1], g.buf[2], g.buf[3]);
-    rec.sim[i] = sim;
+    write_record(rec, i, ph, g, state, steps, sim);
   }
   const int n_hist = __syncthreads_count(sampled);
   const int n_world = __syncthreads_count(world_step);

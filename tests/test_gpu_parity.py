@@ -118,3 +118,38 @@ def test_reproducible_for_fixed_seed(lib):
     _assert_same(a, b)
     c = _gpu(sc, 20000, 31338, batch=1 << 20)
     assert not np.array_equal(a[0], c[0])
+
+
+@pytest.mark.parametrize("precision", [32, 64])
+def test_narrow_acceptance_bit_exact(lib, precision):
+    """A field a tenth as wide: ~1 % of the directions are accepted, so the
+    warp-cooperative acceptance loop deals many lanes to few histories per round; doses,
+    rejection counts and everything else equal the oracle's sequential loop."""
+    sc = small_ct()
+    (lo, hi), = sc.source.accept_boxes
+    c = [(a + b) / 2 for a, b in zip(lo, hi)]
+    hx, hz = (hi[0] - lo[0]) / 20, (hi[2] - lo[2]) / 20  # a tenth of the field's half-width
+    sc.source.accept_boxes = [((c[0] - hx, lo[1], c[2] - hz), (c[0] + hx, hi[1], c[2] + hz))]
+    sc.set_source(sc.source)
+    n = 6000 if precision == 32 else 2000
+    g = _gpu(sc, n, 4242, precision=precision, batch=4096)
+    o = _oracle(sc, n, 4242, precision=precision, batch=4096)
+    _assert_same(g, o)
+    assert g[2]["skipped"] > 20 * n
+
+
+def test_acceptance_exhausted_fails_like_the_oracle(lib):
+    """max_rejection = 2 with a ~1 % acceptance: both the GPU and the oracle stop with the
+    domain error (GateSingleParticleSource gives up after max_rejection rejections)."""
+    sc = small_ct()
+    (lo, hi), = sc.source.accept_boxes
+    c = [(a + b) / 2 for a, b in zip(lo, hi)]
+    hx, hz = (hi[0] - lo[0]) / 20, (hi[2] - lo[2]) / 20  # a tenth of the field's half-width
+    sc.source.accept_boxes = [((c[0] - hx, lo[1], c[2] - hz), (c[0] + hx, hi[1], c[2] + hz))]
+    sc.set_source(sc.source)
+    sc.source.max_rejection = 2
+    sc.set_source(sc.source)
+    with pytest.raises(Exception):
+        _gpu(sc, 2000, 5, batch=4096)
+    with pytest.raises(Exception):
+        _oracle(sc, 2000, 5, batch=4096)
