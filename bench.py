@@ -1077,13 +1077,16 @@ def run_ours(args):
     h2d = scene.labels.nbytes + scene._sig.nbytes + scene._cum.nbytes + scene._ray_amax.nbytes + \
         scene._ray_cum.nbytes + scene.majorant.nbytes
     d2h = 2 * scene.n_voxels * 8
+    # the images land in page-locked host buffers reused every step (gg_host_alloc)
+    out_e = eng.pinned_empty(scene.labels.shape)
+    out_e2 = eng.pinned_empty(scene.labels.shape)
     torch.cuda.synchronize()
     e2e_t = []
     for k in range(max(1, min(args.steps, 3))):
         t1 = time.perf_counter()
         eng.upload()
         eng.run(n, args.seed, first_of(args.warmup + args.steps + k))
-        a, b = eng.edep(), eng.edep_squared()
+        eng.edep(out_e), eng.edep_squared(out_e2)
         e2e_t.append(time.perf_counter() - t1)
     e2e_s = dist_max(dist, float(np.mean(e2e_t)), use_cuda)
     e2e_value = ws * n / e2e_s

@@ -276,6 +276,14 @@ int gg_run(gg_ctx *ctx, uint64_t n_histories, uint64_t seed, uint64_t first_hist
 int gg_synchronize(gg_ctx *ctx);
 int gg_get_image(gg_ctx *ctx, int32_t which, double *out, size_t n);
 int gg_get_counters(gg_ctx *ctx, uint64_t *out, size_t n);
+/* Page-locked host memory (cudaMallocHost) for callers that download or
+   upload the same buffers repeatedly: copies from and to it run at the host
+   link's DMA rate instead of through the driver's staging of pageable
+   memory.  gg_host_alloc returns NULL on failure; gg_host_free(NULL) is a
+   no-op.  No reference counterpart (the reference's images live in host
+   memory). */
+void *gg_host_alloc(size_t bytes);
+int gg_host_free(void *ptr);
 /* Device time (CUDA events on the context's stream) of the last gg_run, ms:
    source stage, transport kernel and tally flush, summed over batches, and
    the number of kernel launches. */

@@ -205,6 +205,8 @@ PROTOTYPES = [
     ("gg_synchronize", ctypes.c_int, [ctypes.c_void_p]),
     ("gg_get_image", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, _f64p, ctypes.c_size_t]),
     ("gg_get_counters", ctypes.c_int, [ctypes.c_void_p, _u64p, ctypes.c_size_t]),
+    ("gg_host_alloc", ctypes.c_void_p, [ctypes.c_size_t]),
+    ("gg_host_free", ctypes.c_int, [ctypes.c_void_p]),
     ("gg_last_kernel_ms", ctypes.c_int,
      [ctypes.c_void_p, _f64p, _f64p, _f64p, ctypes.POINTER(ctypes.c_int32)]),
     ("gg_spect_setup", ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(SpectDesc)]),

@@ -1285,6 +1285,17 @@ int gg_get_image(gg_ctx *c, int32_t which, double *out, size_t n) {
   return c->cuda(cudaStreamSynchronize(c->stream), "download");
 }
 
+void *gg_host_alloc(size_t bytes) {
+  void *p = nullptr;
+  if (bytes == 0 || cudaMallocHost(&p, bytes) != cudaSuccess) return nullptr;
+  return p;
+}
+
+int gg_host_free(void *p) {
+  if (!p) return GG_OK;
+  return cudaFreeHost(p) == cudaSuccess ? GG_OK : GG_ERR_CUDA;
+}
+
 int gg_get_counters(gg_ctx *c, uint64_t *out, size_t n) {
   if (!c || !out) return GG_ERR_ARG;
   cudaSetDevice(c->device);

@@ -26,6 +26,7 @@ class DoseEngine:
         st = self.lib.gg_create(ctypes.byref(opts), ctypes.byref(ctx))
         C.check(self.lib, None, st)
         self.ctx = ctx
+        self._pinned = []
         self.score_squared = score_squared
         self.upload()
 
@@ -60,16 +61,33 @@ class DoseEngine:
     def run(self, n, seed, first=0):
         self._call("gg_run", ctypes.c_uint64(n), ctypes.c_uint64(seed), ctypes.c_uint64(first))
 
-    def image(self, which):
-        out = np.empty(self.scene.n_voxels, dtype=np.float64)
+    def image(self, which, out=None):
+        """Image `which` [nz][ny][nx] (float64); into `out` when given (e.g. a pinned_empty
+        buffer, reused between calls: the copy then runs at the link's DMA rate)."""
+        if out is None:
+            out = np.empty(self.scene.labels.shape, dtype=np.float64)
+        if out.dtype != np.float64 or out.size != self.scene.n_voxels or not out.flags.c_contiguous:
+            raise ValueError("out must be a C-contiguous float64 array of the image's size")
         self._call("gg_get_image", which, C.ptr(out, ctypes.c_double), out.size)
         return out.reshape(self.scene.labels.shape)
 
-    def edep(self):
-        return self.image(C.GG_IMG_EDEP)
+    def edep(self, out=None):
+        return self.image(C.GG_IMG_EDEP, out)
 
-    def edep_squared(self):
-        return self.image(C.GG_IMG_EDEP_SQUARED)
+    def edep_squared(self, out=None):
+        return self.image(C.GG_IMG_EDEP_SQUARED, out)
+
+    def pinned_empty(self, shape, dtype=np.float64):
+        """Uninitialised array in page-locked host memory (gg_host_alloc), freed with the
+        engine."""
+        dtype = np.dtype(dtype)
+        n = int(np.prod(shape)) * dtype.itemsize
+        ptr = self.lib.gg_host_alloc(n)
+        if not ptr:
+            raise MemoryError(f"gg_host_alloc({n}) failed")
+        self._pinned.append(ptr)
+        buf = (ctypes.c_char * n).from_address(ptr)
+        return np.frombuffer(buf, dtype=dtype).reshape(shape)
 
     def counters(self):
         out = np.zeros(C.GG_N_COUNTERS, dtype=np.uint64)
@@ -86,6 +104,9 @@ class DoseEngine:
         if self.ctx:
             self.lib.gg_destroy(self.ctx)
             self.ctx = None
+        for ptr in getattr(self, "_pinned", []):
+            self.lib.gg_host_free(ptr)
+        self._pinned = []
 
     def __del__(self):
         try:

@@ -20,7 +20,7 @@ HEADER = pathlib.Path(__file__).resolve().parents[1] / "include" / "gate_gpu.h"
 
 def declared_functions():
     text = HEADER.read_text()
-    return sorted(set(re.findall(r"^int\s+(gg_\w+)\s*\(", text, flags=re.M)))
+    return sorted(set(re.findall(r"^(?:int|void\s*\*)\s*(gg_\w+)\s*\(", text, flags=re.M)))
 
 
 def test_header_declares_the_api():
@@ -92,3 +92,11 @@ def test_majorant_bounds_every_material():
     present = np.unique(sc.labels)
     mu = sc.pt.sig[sc.pt.mat_comp[present]] * sc.pt.mat_rho[present, None]
     assert np.all(sc.majorant[None, :] >= mu)
+
+
+def test_host_alloc_symbols_need_no_gpu_to_load(built_lib):
+    """gg_host_alloc / gg_host_free are exported with their prototypes (calling them needs
+    the CUDA runtime and a device: covered by the GPU tests)."""
+    lib = C.load()
+    assert lib.gg_host_alloc.restype is ctypes.c_void_p
+    assert lib.gg_host_free(None) == 0  # NULL is a no-op

@@ -153,3 +153,18 @@ def test_acceptance_exhausted_fails_like_the_oracle(lib):
         _gpu(sc, 2000, 5, batch=4096)
     with pytest.raises(Exception):
         _oracle(sc, 2000, 5, batch=4096)
+
+
+def test_images_into_pinned_buffers(lib):
+    """edep / edep_squared into page-locked buffers (gg_host_alloc) equal the plain ones."""
+    from opengate_gb300.engine import DoseEngine
+
+    sc = W.water_pencil()
+    with DoseEngine(sc, batch=1 << 20) as eng:
+        eng.run(5000, 3)
+        a, b = eng.edep(), eng.edep_squared()
+        pa = eng.pinned_empty(sc.labels.shape)
+        pb = eng.pinned_empty(sc.labels.shape)
+        np.testing.assert_array_equal(eng.edep(pa), a)
+        np.testing.assert_array_equal(eng.edep_squared(pb), b)
+        assert pa.ctypes.data != a.ctypes.data
