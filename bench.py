@@ -830,12 +830,14 @@ def run_ours_batched(args, ws, rank, local, dist, use_cuda):
     # e2e through the C ABI: descriptors + labels upload, one run, all images download
     h2d = sum(s.labels.nbytes + s.majorant.nbytes for s, _, _ in sims) + sims[0][0]._sig.nbytes
     d2h = 2 * sum(s.n_voxels for s, _, _ in sims) * 8
+    # images into page-locked host buffers reused every step (gg_host_alloc)
+    outs = [(eng.pinned_empty(sc.labels.shape), eng.pinned_empty(sc.labels.shape)) for sc, _, _ in sims]
     t1 = time.perf_counter()
     eng.upload()
     eng.run()
     for k in range(len(sims)):
-        eng.image(k, C.GG_IMG_EDEP)
-        eng.image(k, C.GG_IMG_EDEP_SQUARED)
+        eng.image(k, C.GG_IMG_EDEP, outs[k][0])
+        eng.image(k, C.GG_IMG_EDEP_SQUARED, outs[k][1])
     e2e_s = dist_max(dist, time.perf_counter() - t1, use_cuda)
     peak_bw, peak_kind = measured_peaks()
     # counters of the last step (the tally and counters are reset before each replay)

@@ -285,6 +285,7 @@ class BatchEngine:
         ctx = ctypes.c_void_p()
         C.check(self.lib, None, self.lib.gg_create(ctypes.byref(opts), ctypes.byref(ctx)))
         self.ctx = ctx
+        self._pinned = []
         self.upload()
 
     def _call(self, name, *args):
@@ -324,11 +325,17 @@ class BatchEngine:
     def reset(self):
         self._call("gg_reset_tally")
 
-    def image(self, k, which):
+    def image(self, k, which, out=None):
+        """Image `which` of simulation k; into `out` when given (e.g. pinned_empty)."""
         scene = self.sims[k][0]
-        out = np.empty(scene.n_voxels, dtype=np.float64)
+        if out is None:
+            out = np.empty(scene.labels.shape, dtype=np.float64)
+        if out.dtype != np.float64 or out.size != scene.n_voxels or not out.flags.c_contiguous:
+            raise ValueError("out must be a C-contiguous float64 array of the image's size")
         self._call("gg_batch_get_image", k, which, C.ptr(out, ctypes.c_double), out.size)
         return out.reshape(scene.labels.shape)
+
+    pinned_empty = DoseEngine.pinned_empty
 
     def counters(self):
         out = np.zeros(C.GG_N_COUNTERS, dtype=np.uint64)
@@ -344,6 +351,9 @@ class BatchEngine:
         if self.ctx:
             self.lib.gg_destroy(self.ctx)
             self.ctx = None
+        for ptr in getattr(self, "_pinned", []):
+            self.lib.gg_host_free(ptr)
+        self._pinned = []
 
     def __del__(self):
         try:
