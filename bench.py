@@ -33,6 +33,7 @@ import numpy as np  # noqa: E402
 METRIC = "primaries/s at matched sigma (plain GPU transport, CT phantom dose)"
 UNIT = "primaries/s"
 PRIMARIES_PER_STEP = 100_000_000
+TRANSPORT_DRAM_PER_PRIMARY = (478.16e6 + 200.48e6) / 3e6  # bytes, ncu capture of the dose workload
 WORKLOAD = "ct_phantom_256x256x160_1.2mm_ssd100_field10x10_spectrum60_0.1-6MeV"
 
 # SPECT acquisition: CT phantom as attenuation map, Tc-99m activity image,
@@ -1097,8 +1098,14 @@ def run_ours(args):
     peak, peak_kind = measured_peaks()
     bytes_alg = 32.0 * counters["woodcock_steps"] + 64.0 * counters["tally_entries"]
     achieved = bytes_alg / (transport_ms / 1e3) / 1e9
+    # DRAM traffic of the transport kernel: an ncu capture of the same workload at 3e6
+    # primaries (one launch: dram__bytes_read.sum 478.16 MB + dram__bytes_write.sum
+    # 200.48 MB) scaled by primaries to this launch, unless measured and passed in
+    traffic = args.traffic if args.traffic is not None else TRANSPORT_DRAM_PER_PRIMARY * n
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak, "traffic": args.traffic,
+                "frac": achieved / peak, "traffic": traffic,
+                "traffic_note": None if args.traffic is not None else
+                "ncu dram bytes of a 3e6-primary launch of this workload, scaled by primaries",
                 "peak_kind": peak_kind, "kernel": "k_transport<float>",
                 "bytes_alg_per_step": bytes_alg,
                 "units": {"woodcock_steps": counters["woodcock_steps"], "tally_entries": counters["tally_entries"],
