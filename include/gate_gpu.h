@@ -231,7 +231,7 @@ typedef struct {
   int32_t block_size; /* 0 = default */
   int32_t blocks_per_sm; /* 0 = default */
   int32_t chunk;      /* histories a warp claims per queue fetch, 0 = default */
-  int64_t batch;      /* histories per tally batch, 0 = default */
+  int64_t batch;      /* histories per tally batch, 0 = default (2^26; buffers sized to min(batch, run)) */
   int32_t refill_min;   /* 1..32: lanes waiting for a history that trigger a refill phase, 0 = default */
   int32_t interact_min; /* 1..32: pending collisions that trigger an interaction phase, 0 = default */
 } gg_device_opts;
