@@ -195,9 +195,13 @@ class SpectEngine(DoseEngine):
         self._call("gg_get_arf_projection", C.ptr(out, ctypes.c_double), C.ptr(sq, ctypes.c_double), n)
         return (out.reshape(shape), sq.reshape(shape)) if squared else out.reshape(shape)
 
-    def projection(self):
+    def projection(self, out=None):
+        """Counts (head, run * window, y, x); into `out` when given (e.g. pinned_empty)."""
         shape = self.spect.projection_shape()
-        out = np.empty(int(np.prod(shape)), dtype=np.float64)
+        if out is None:
+            out = np.empty(shape, dtype=np.float64)
+        if out.dtype != np.float64 or out.size != int(np.prod(shape)) or not out.flags.c_contiguous:
+            raise ValueError("out must be a C-contiguous float64 array of the projection's size")
         self._call("gg_get_projection", C.ptr(out, ctypes.c_double), out.size)
         return out.reshape(shape)
 
