@@ -834,13 +834,17 @@ def run_ours_batched(args, ws, rank, local, dist, use_cuda):
     d2h = 2 * sum(s.n_voxels for s, _, _ in sims) * 8
     # images into page-locked host buffers reused every step (gg_host_alloc)
     outs = [(eng.pinned_empty(sc.labels.shape), eng.pinned_empty(sc.labels.shape)) for sc, _, _ in sims]
-    t1 = time.perf_counter()
-    eng.upload()
-    eng.run()
-    for k in range(len(sims)):
-        eng.image(k, C.GG_IMG_EDEP, outs[k][0])
-        eng.image(k, C.GG_IMG_EDEP_SQUARED, outs[k][1])
-    e2e_s = dist_max(dist, time.perf_counter() - t1, use_cuda)
+    e2e_t = []
+    for _ in range(3):
+        eng.reset()
+        t1 = time.perf_counter()
+        eng.upload()
+        eng.run()
+        for k in range(len(sims)):
+            eng.image(k, C.GG_IMG_EDEP, outs[k][0])
+            eng.image(k, C.GG_IMG_EDEP_SQUARED, outs[k][1])
+        e2e_t.append(time.perf_counter() - t1)
+    e2e_s = dist_max(dist, float(np.mean(e2e_t)), use_cuda)
     peak_bw, peak_kind = measured_peaks()
     # counters of the last step (the tally and counters are reset before each replay)
     bytes_alg = 32.0 * counters["woodcock_steps"] + 64.0 * counters["tally_entries"]
