@@ -17,6 +17,7 @@
 #include "../../include/gate_gpu.h"
 #include "gg_device.cuh"
 #include "gg_internal.h"
+#include "gg_validate.h"
 #include "gg_mlp.cuh"
 
 namespace {
@@ -679,20 +680,9 @@ int gg_last_error(const gg_ctx *ctx, char *buf, size_t len) {
 int gg_upload_tables(gg_ctx *c, const gg_tables_desc *t) {
   if (!c || !t) return GG_ERR_ARG;
   cudaSetDevice(c->device);
-  if (t->n_e < 2 || t->n_comp < 1 || t->n_ray < 2 || t->n_mat < 1 || !t->sig || !t->cum || !t->ray_amax ||
-      !t->ray_cum || !t->ray_x2 || !t->mat_comp || !t->mat_rho)
-    return c->fail(GG_ERR_ARG, "gg_upload_tables: incomplete table descriptor");
-  if (!(t->inv_dln > 0) || !(t->e_min > 0) || !(t->e_max > t->e_min))
-    return c->fail(GG_ERR_ARG, "gg_upload_tables: invalid energy grid");
-  for (int m = 0; m < t->n_mat; ++m) {
-    if (t->mat_comp[m] < 0 || t->mat_comp[m] >= t->n_comp)
-      return c->fail(GG_ERR_ARG, "gg_upload_tables: material %d refers to composition %d", m, t->mat_comp[m]);
-    if (!(t->mat_rho[m] > 0)) return c->fail(GG_ERR_ARG, "gg_upload_tables: material %d density <= 0", m);
-  }
+  char msg[160];
+  if (gg::check_tables(t, msg, sizeof(msg))) return c->fail(GG_ERR_ARG, "gg_upload_tables: %s", msg);
   size_t nce = (size_t)t->n_comp * t->n_e;
-  for (size_t i = 0; i < nce; ++i)
-    if (!(t->sig[i] >= 0) || !std::isfinite(t->sig[i]))
-      return c->fail(GG_ERR_ARG, "gg_upload_tables: attenuation table has a negative or non-finite entry");
   size_t need = c->precision == GG_PREC_F64 ? gg::transport_smem_bytes<double>(t->n_comp, t->n_e, t->n_mat)
                                             : gg::transport_smem_bytes<float>(t->n_comp, t->n_e, t->n_mat);
   if (need > 190 * 1024)
@@ -712,9 +702,6 @@ int gg_upload_tables(gg_ctx *c, const gg_tables_desc *t) {
   if ((st = c->upload_real(c->d_ray_amax, t->ray_amax, nce))) return st;
   if ((st = c->upload_real(c->d_ray_cum, t->ray_cum, (size_t)t->n_comp * t->n_ray))) return st;
   if ((st = c->upload_real(c->d_ray_x2, t->ray_x2, (size_t)t->n_ray))) return st;
-  for (int i = 1; i < t->n_ray; ++i)
-    if (!(t->ray_x2[i] > t->ray_x2[i - 1]))
-      return c->fail(GG_ERR_ARG, "gg_upload_tables: Rayleigh x^2 nodes must increase");
   if ((st = c->upload_real(c->d_mat_rho, t->mat_rho, (size_t)t->n_mat))) return st;
   dfree(c->d_mat_comp);
   if ((st = c->cuda(cudaMalloc(&c->d_mat_comp, sizeof(int) * t->n_mat), "cudaMalloc"))) return st;
@@ -735,20 +722,19 @@ int gg_upload_volume(gg_ctx *c, const gg_volume_desc *v) {
   if (!c || !v) return GG_ERR_ARG;
   cudaSetDevice(c->device);
   if (!c->have_tables) return c->fail(GG_ERR_STATE, "gg_upload_volume: upload the tables first");
-  for (int a = 0; a < 3; ++a) {
-    if (v->dims[a] <= 0) return c->fail(GG_ERR_ARG, "gg_upload_volume: dims must be > 0");
-    if (!(v->spacing[a] > 0)) return c->fail(GG_ERR_ARG, "gg_upload_volume: spacing must be > 0");
-  }
+  for (int a = 0; a < 3; ++a)
+    if (!(v->spacing[a] > 0) || !std::isfinite(v->spacing[a]))
+      return c->fail(GG_ERR_ARG, "gg_upload_volume: spacing must be finite and > 0");
   if (!v->labels || !v->majorant) return c->fail(GG_ERR_ARG, "gg_upload_volume: null labels or majorant");
-  size_t n = (size_t)v->dims[0] * v->dims[1] * v->dims[2];
-  if (n >= (size_t)UINT32_MAX) return c->fail(GG_ERR_ARG, "gg_upload_volume: more than 2^32-1 voxels");
+  char msg[160];
+  size_t n = 0;
+  if (gg::check_dims(v->dims, (size_t)UINT32_MAX - 1, &n, msg, sizeof(msg)))
+    return c->fail(GG_ERR_ARG, "gg_upload_volume: %s", msg);
   uint16_t lmax = 0;
   for (size_t i = 0; i < n; ++i) lmax = std::max(lmax, v->labels[i]);
   if ((int)lmax >= c->n_mat)
     return c->fail(GG_ERR_ARG, "gg_upload_volume: label %u outside the material table (%d)", lmax, c->n_mat);
-  for (int i = 0; i < c->n_e; ++i)
-    if (!(v->majorant[i] > 0) || !std::isfinite(v->majorant[i]))
-      return c->fail(GG_ERR_ARG, "gg_upload_volume: majorant must be finite and > 0");
+  if (gg::check_majorant(v->majorant, c->n_e, msg, sizeof(msg))) return c->fail(GG_ERR_ARG, "gg_upload_volume: %s", msg);
   int st;
   dfree(c->d_labels);
   if ((st = c->cuda(cudaMalloc(&c->d_labels, n * sizeof(uint16_t)), "cudaMalloc labels"))) return st;
@@ -791,16 +777,8 @@ int gg_set_source(gg_ctx *c, const gg_source_desc *s) {
   if (s->ene_type < GG_ENE_MONO || s->ene_type > GG_ENE_RANGE) return c->fail(GG_ERR_ARG, "gg_set_source: energy type");
   if (s->n_accept < 0 || (s->n_accept > 0 && !s->accept_boxes)) return c->fail(GG_ERR_ARG, "gg_set_source: acceptance boxes");
   double elo = 0, ehi = 0;
-  if (s->ene_type == GG_ENE_MONO) elo = ehi = s->mono;
-  else if (s->ene_type == GG_ENE_RANGE) { elo = s->e_lo; ehi = s->e_hi; }
-  else {
-    if (s->n_spec < 1 || !s->spec_e || !s->spec_cdf) return c->fail(GG_ERR_ARG, "gg_set_source: empty spectrum");
-    int ne = s->ene_type == GG_ENE_HISTOGRAM ? s->n_spec + 1 : s->n_spec;
-    elo = *std::min_element(s->spec_e, s->spec_e + ne);
-    ehi = *std::max_element(s->spec_e, s->spec_e + ne);
-    for (int i = 1; i < s->n_spec; ++i)
-      if (s->spec_cdf[i] < s->spec_cdf[i - 1]) return c->fail(GG_ERR_ARG, "gg_set_source: cumulative weights decrease");
-  }
+  char msg[160];
+  if (gg::check_source_energy(s, &elo, &ehi, msg, sizeof(msg))) return c->fail(GG_ERR_ARG, "gg_set_source: %s", msg);
   c->src_emax = ehi;
   if (!(elo >= c->e_min) || !(ehi <= c->e_max))
     return c->fail(GG_ERR_DOMAIN, "gg_set_source: energies [%g, %g] MeV outside the tables [%g, %g]", elo, ehi,

@@ -182,13 +182,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spect_arf(Scene<real> s, ArfS
 
 template <typename real>
 cudaError_t launch_spect_arf(const Scene<real> &s, const ArfStageArgs &a, int grid, cudaStream_t st) {
-  static bool configured = false;
-  if (!configured) {
-    cudaError_t e = cudaFuncSetAttribute(k_spect_arf<real>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)sizeof(TcNetSmem));
-    if (e != cudaSuccess) return e;
-    configured = true;
-  }
+  static unsigned long long configured = 0;
+  cudaError_t e = configure_smem(k_spect_arf<real>, (int)sizeof(TcNetSmem), configured);
+  if (e != cudaSuccess) return e;
   k_spect_arf<real><<<grid, kTcThreads, sizeof(TcNetSmem), st>>>(s, a);
   return cudaGetLastError();
 }

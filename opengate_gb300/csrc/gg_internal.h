@@ -8,6 +8,22 @@
 
 namespace gg {
 
+// cudaFuncSetAttribute applies to the current device only: `done` remembers,
+// one bit per device ordinal (< 64), on which devices a kernel's dynamic
+// shared-memory limit has been raised.
+template <typename K>
+inline cudaError_t configure_smem(K kernel, int bytes, unsigned long long &done) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  const unsigned long long bit = (dev >= 0 && dev < 64) ? (1ull << dev) : 0ull;
+  if (bit && (done & bit)) return cudaSuccess;
+  e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (e == cudaSuccess) done |= bit;
+  return e;
+}
+
+
 template <typename real>
 struct Scene;
 

@@ -102,13 +102,9 @@ size_t mlp_tc_smem_bytes() { return sizeof(TcNetSmem); }
 
 cudaError_t launch_mlp_predict(const MlpTrainArgs &a, float *out, uint64_t n, int grid, unsigned int *status,
                                cudaStream_t st) {
-  static bool configured = false;
-  if (!configured) {
-    cudaError_t e = cudaFuncSetAttribute(k_mlp_predict, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)sizeof(TcNetSmem));
-    if (e != cudaSuccess) return e;
-    configured = true;
-  }
+  static unsigned long long configured = 0;
+  cudaError_t e = configure_smem(k_mlp_predict, (int)sizeof(TcNetSmem), configured);
+  if (e != cudaSuccess) return e;
   k_mlp_predict<<<grid, kTcThreads, sizeof(TcNetSmem), st>>>(a, out, n, status);
   return cudaGetLastError();
 }

@@ -378,13 +378,9 @@ __global__ void __launch_bounds__(kTrThreads, 1) k_mlp_train(MlpTrainArgs a) {
 size_t mlp_train_smem_bytes() { return sizeof(TrainSmem); }
 
 cudaError_t launch_mlp_train(const MlpTrainArgs &a, int n_tiles, cudaStream_t st) {
-  static bool configured = false;
-  if (!configured) {
-    cudaError_t e =
-        cudaFuncSetAttribute(k_mlp_train, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(TrainSmem));
-    if (e != cudaSuccess) return e;
-    configured = true;
-  }
+  static unsigned long long configured = 0;
+  cudaError_t e = configure_smem(k_mlp_train, (int)sizeof(TrainSmem), configured);
+  if (e != cudaSuccess) return e;
   k_mlp_train<<<n_tiles, kTrThreads, sizeof(TrainSmem), st>>>(a);
   return cudaGetLastError();
 }

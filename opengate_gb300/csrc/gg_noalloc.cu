@@ -34,6 +34,7 @@
 #include "../../include/gate_gpu.h"
 #include "gg_device.cuh"
 #include "gg_internal.h"
+#include "gg_validate.h"
 
 namespace {
 
@@ -123,18 +124,18 @@ extern "C" int gg_dose_run_noalloc(int32_t device, void *stream, const gg_tables
                 "table sizes beyond the no-allocation limits (n_e <= %d, n_comp <= %d, n_ray <= %d, n_mat <= %d)",
                 GG_NOALLOC_MAX_ENERGIES, GG_NOALLOC_MAX_COMPOSITIONS, GG_NOALLOC_MAX_RAYLEIGH,
                 GG_NOALLOC_MAX_MATERIALS);
-  if (!t->sig || !t->cum || !t->ray_amax || !t->ray_x2 || !t->ray_cum || !t->mat_comp || !t->mat_rho ||
-      !v->labels || !v->majorant)
-    return fail(err, err_len, GG_ERR_ARG, "incomplete table or volume descriptor");
-  size_t n_vox = 1;
-  for (int a = 0; a < 3; ++a) {
-    if (v->dims[a] <= 0 || !(v->spacing[a] > 0) || !(w->half_size[a] > 0))
-      return fail(err, err_len, GG_ERR_ARG, "dims, spacing and world half sizes must be > 0");
-    n_vox *= (size_t)v->dims[a];
-  }
-  if (n_vox > GG_NOALLOC_MAX_VOXELS)
-    return fail(err, err_len, GG_ERR_ARG, "image has %zu voxels; the no-allocation run handles at most %u",
-                n_vox, (unsigned)GG_NOALLOC_MAX_VOXELS);
+  // the same checks as gg_upload_tables / gg_upload_volume / gg_set_source
+  char msg[160];
+  if (gg::check_tables(t, msg, sizeof(msg))) return fail(err, err_len, GG_ERR_ARG, "tables: %s", msg);
+  if (!v->labels || !v->majorant) return fail(err, err_len, GG_ERR_ARG, "incomplete volume descriptor");
+  for (int a = 0; a < 3; ++a)
+    if (!(v->spacing[a] > 0) || !std::isfinite(v->spacing[a]) || !(w->half_size[a] > 0))
+      return fail(err, err_len, GG_ERR_ARG, "spacing and world half sizes must be > 0");
+  size_t n_vox = 0;
+  if (gg::check_dims(v->dims, (size_t)GG_NOALLOC_MAX_VOXELS, &n_vox, msg, sizeof(msg)))
+    return fail(err, err_len, GG_ERR_ARG, "the no-allocation run handles at most %u voxels: %s",
+                (unsigned)GG_NOALLOC_MAX_VOXELS, msg);
+  if (gg::check_majorant(v->majorant, t->n_e, msg, sizeof(msg))) return fail(err, err_len, GG_ERR_ARG, "%s", msg);
   // voxel (activity image) sources need their CDF arrays on the device: gg_run only
   if (src->pos_type < GG_POS_POINT || src->pos_type > GG_POS_DISC)
     return fail(err, err_len, GG_ERR_ARG, "position type %d not handled by the no-allocation run", src->pos_type);
@@ -146,25 +147,14 @@ extern "C" int gg_dose_run_noalloc(int32_t device, void *stream, const gg_tables
   bool spectrum = src->ene_type == GG_ENE_LINES || src->ene_type == GG_ENE_HISTOGRAM;
   if (spectrum && (src->n_spec < 1 || src->n_spec > GG_NOALLOC_MAX_SPECTRUM || !src->spec_e || !src->spec_cdf))
     return fail(err, err_len, GG_ERR_ARG, "spectrum must have 1..%d entries", GG_NOALLOC_MAX_SPECTRUM);
+  double elo = 0, ehi = 0;
+  if (gg::check_source_energy(src, &elo, &ehi, msg, sizeof(msg)))
+    return fail(err, err_len, GG_ERR_ARG, "source: %s", msg);
   if (src->n_accept < 0 || src->n_accept > GG_NOALLOC_MAX_ACCEPT || (src->n_accept && !src->accept_boxes))
     return fail(err, err_len, GG_ERR_ARG, "at most %d acceptance boxes", GG_NOALLOC_MAX_ACCEPT);
   if (w->material < 0 || w->material >= t->n_mat) return fail(err, err_len, GG_ERR_ARG, "bad world material");
-  for (int m = 0; m < t->n_mat; ++m)
-    if (t->mat_comp[m] < 0 || t->mat_comp[m] >= t->n_comp || !(t->mat_rho[m] > 0))
-      return fail(err, err_len, GG_ERR_ARG, "material %d: bad composition or density", m);
   for (size_t i = 0; i < n_vox; ++i)
     if (v->labels[i] >= t->n_mat) return fail(err, err_len, GG_ERR_ARG, "label outside the material table");
-  double elo = src->mono, ehi = src->mono;
-  if (src->ene_type == GG_ENE_RANGE) {
-    elo = src->e_lo;
-    ehi = src->e_hi;
-  } else if (spectrum) {
-    elo = ehi = src->spec_e[0];
-    for (int i = 0; i < n_spec_e; ++i) {
-      elo = fmin(elo, src->spec_e[i]);
-      ehi = fmax(ehi, src->spec_e[i]);
-    }
-  }
   if (!(elo >= t->e_min) || !(ehi <= t->e_max))
     return fail(err, err_len, GG_ERR_DOMAIN, "source energies outside the tables");
   if (n_histories == 0) return GG_OK;
@@ -312,15 +302,17 @@ extern "C" int gg_dose_run_noalloc(int32_t device, void *stream, const gg_tables
       if (e == cudaSuccess) e = gg::launch_transport<float>(s, a, n_sm * (bps > 0 ? bps : 1), 256, smem, 3, st);
       if (e == cudaSuccess) e = gg::launch_flush(a.acc_e, a.acc_e2, d_edep, d_edep2, n_vox, n_sm * 8, st);
     }
-    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) {
       rc = fail(err, err_len, GG_ERR_CUDA, "transport: %s", cudaGetErrorString(e));
       break;
     }
+    // status and counters through the caller's stream (no device-wide wait)
     unsigned int status = 0;
     unsigned long long cnt[GG_N_COUNTERS];
-    e = cudaMemcpy(&status, b + L.status, 4, cudaMemcpyDeviceToHost);
-    if (e == cudaSuccess && counters) e = cudaMemcpy(cnt, b + L.counters, sizeof(cnt), cudaMemcpyDeviceToHost);
+    e = cudaMemcpyAsync(&status, b + L.status, 4, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess && counters)
+      e = cudaMemcpyAsync(cnt, b + L.counters, sizeof(cnt), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) {
       rc = fail(err, err_len, GG_ERR_CUDA, "reading status: %s", cudaGetErrorString(e));
       break;

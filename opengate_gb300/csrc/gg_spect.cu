@@ -621,15 +621,10 @@ template <typename real, int MINB, int FFM = kFfOff, int HMINB = MINB>
 static cudaError_t launch_stage_v(int stage, const Scene<real> &s, const KernelArgs &a, const StageArgs &q, int grid,
                                   int block, size_t smem, cudaStream_t st) {
   constexpr bool FF = FFM != kFfOff;
-  static bool configured[2] = {false, false};
-  if (!configured[stage]) {
-    cudaError_t e = stage == 0 ? cudaFuncSetAttribute(k_spect_phantom<real, MINB, FFM>,
-                                                      cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024)
-                               : cudaFuncSetAttribute(k_spect_head<real, HMINB, FF>,
-                                                      cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    if (e != cudaSuccess) return e;
-    configured[stage] = true;
-  }
+  static unsigned long long configured[2] = {0, 0};
+  cudaError_t e = stage == 0 ? configure_smem(k_spect_phantom<real, MINB, FFM>, 200 * 1024, configured[0])
+                             : configure_smem(k_spect_head<real, HMINB, FF>, 200 * 1024, configured[1]);
+  if (e != cudaSuccess) return e;
   if (stage == 0) k_spect_phantom<real, MINB, FFM><<<grid, block, smem, st>>>(s, a, q);
   else k_spect_head<real, HMINB, FF><<<grid, block, smem, st>>>(s, a, q);
   return cudaGetLastError();
@@ -665,15 +660,12 @@ cudaError_t spect_stage_occupancy(int stage, int block, size_t smem, int minb, i
 template <typename real>
 cudaError_t launch_spect_split(const Scene<real> &s, const KernelArgs &a, const StageArgs &q, int block, size_t smem,
                                int n_sm, cudaStream_t st) {
-  static bool configured = false;
-  static int bps = 1;
-  if (!configured) {
-    cudaError_t e = cudaFuncSetAttribute(k_spect_split<real>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_spect_split<real>, block, smem);
-    if (e != cudaSuccess) return e;
-    if (bps < 1) bps = 1;
-    configured = true;
-  }
+  static unsigned long long configured = 0;
+  cudaError_t e = configure_smem(k_spect_split<real>, 200 * 1024, configured);
+  int bps = 1;
+  if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_spect_split<real>, block, smem);
+  if (e != cudaSuccess) return e;
+  if (bps < 1) bps = 1;
   k_spect_split<real><<<n_sm * bps, block, smem, st>>>(s, a, q);
   return cudaGetLastError();
 }
@@ -681,15 +673,12 @@ cudaError_t launch_spect_split(const Scene<real> &s, const KernelArgs &a, const 
 template <typename real>
 cudaError_t launch_spect_walk(const Scene<real> &s, const KernelArgs &a, const StageArgs &q, int block, size_t smem,
                               int n_sm, cudaStream_t st) {
-  static bool configured = false;
-  static int bps = 1;
-  if (!configured) {
-    cudaError_t e = cudaFuncSetAttribute(k_spect_walk<real>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_spect_walk<real>, block, smem);
-    if (e != cudaSuccess) return e;
-    if (bps < 1) bps = 1;
-    configured = true;
-  }
+  static unsigned long long configured = 0;
+  cudaError_t e = configure_smem(k_spect_walk<real>, 200 * 1024, configured);
+  int bps = 1;
+  if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_spect_walk<real>, block, smem);
+  if (e != cudaSuccess) return e;
+  if (bps < 1) bps = 1;
   k_spect_walk<real><<<n_sm * bps, block, smem, st>>>(s, a, q);
   return cudaGetLastError();
 }

@@ -427,13 +427,9 @@ cudaError_t launch_generate(const Scene<real> &s, const KernelArgs &a, cudaStrea
 template <typename real, int MINB, bool MULTI, bool TLE = false>
 static cudaError_t launch_transport_v(const Scene<real> &s, const KernelArgs &a, int grid, int block, size_t smem,
                                       cudaStream_t st) {
-  static bool configured = false;
-  if (!configured) {
-    cudaError_t e = cudaFuncSetAttribute(k_transport<real, MINB, false, MULTI, TLE>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    if (e != cudaSuccess) return e;
-    configured = true;
-  }
+  static unsigned long long configured = 0;
+  cudaError_t e = configure_smem(k_transport<real, MINB, false, MULTI, TLE>, 200 * 1024, configured);
+  if (e != cudaSuccess) return e;
   k_transport<real, MINB, false, MULTI, TLE><<<grid, block, smem, st>>>(s, a);
   return cudaGetLastError();
 }
