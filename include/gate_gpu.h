@@ -437,6 +437,17 @@ typedef struct {
    context's ARF model. */
 int gg_arf_train(gg_ctx *ctx, const gg_arf_sampling *sampling, const gg_arf_train_opts *opts,
                  gg_arf_model *model_out, double *loss);
+/* Trains the network on caller-supplied rows instead of generating them: the
+   garf training step (garf_train on the ROOT file the reference's
+   ARFTrainingDatasetActor writes, GateARFTrainingDatasetActor.cpp:76-137)
+   with this library's kernels.  rows[n_rows][4] = (E MeV, theta deg, phi
+   deg, class), class 0 = no window (kept with probability 1 / rr), k =
+   window k.  `domain` gives the trained energy range, theta_max_deg and
+   russian_roulette (its other fields are ignored): the standardisation
+   follows from them as for gg_arf_train.  opts->n_samples and opts->seed are
+   not used. */
+int gg_arf_train_rows(gg_ctx *ctx, const float *rows, uint64_t n_rows, const gg_arf_model *domain,
+                      const gg_arf_train_opts *opts, gg_arf_model *model_out, double *loss);
 /* Sets / reads the context's ARF model (params: GG_ARF_N_PARAMS floats). */
 int gg_arf_set_model(gg_ctx *ctx, const gg_arf_model *model, const float *params);
 int gg_arf_get_params(gg_ctx *ctx, float *params, size_t n);

@@ -217,6 +217,9 @@ PROTOTYPES = [
     ("gg_get_projection", ctypes.c_int, [ctypes.c_void_p, _f64p, ctypes.c_size_t]),
     ("gg_arf_train", ctypes.c_int,
      [ctypes.c_void_p, ctypes.POINTER(ArfSampling), ctypes.POINTER(ArfTrainOpts), ctypes.POINTER(ArfModel), _f64p]),
+    ("gg_arf_train_rows", ctypes.c_int,
+     [ctypes.c_void_p, ctypes.POINTER(ctypes.c_float), ctypes.c_uint64, ctypes.POINTER(ArfModel),
+      ctypes.POINTER(ArfTrainOpts), ctypes.POINTER(ArfModel), _f64p]),
     ("gg_arf_set_model", ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ArfModel), ctypes.POINTER(ctypes.c_float)]),
     ("gg_arf_get_params", ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_float), ctypes.c_size_t]),
     ("gg_arf_predict", ctypes.c_int,

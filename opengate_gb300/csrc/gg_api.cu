@@ -1507,15 +1507,48 @@ int gg_arf_gradient(gg_ctx *c, const float *rows, uint64_t n, float *grad, doubl
   return check_tc_status(c, "gg_arf_gradient");
 }
 
+// The model of a training domain: classes = windows + 1, inputs standardised
+// by the mean and standard deviation of uniform theta in [0, theta_max] deg,
+// phi in [-180, 180) deg and E in [e_min, e_max].
+static gg_arf_model arf_domain_model(const gg_ctx *c, double e_min, double e_max, double theta_max_deg,
+                                     double russian_roulette) {
+  gg_arf_model m{};
+  m.n_classes = c->spect.n_windows + 1;
+  const double th = theta_max_deg;
+  m.x_mean[0] = (float)(0.5 * th);
+  m.x_std[0] = (float)(th / std::sqrt(12.0));
+  m.x_mean[1] = 0.0f;
+  m.x_std[1] = (float)(360.0 / std::sqrt(12.0));
+  m.x_mean[2] = (float)(0.5 * (e_min + e_max));
+  m.x_std[2] = (float)((e_max - e_min) / std::sqrt(12.0));
+  m.russian_roulette = russian_roulette;
+  m.e_min = e_min;
+  m.e_max = e_max;
+  m.theta_max_deg = th;
+  m.distance_to_crystal = c->spect.collimator_thickness + c->spect.gap + 0.5 * c->spect.crystal_thickness;
+  return m;
+}
+
+static int arf_check_opts(gg_ctx *c, const gg_arf_train_opts *o, const char *who) {
+  if (o->batch < gg::kTrainRows || o->batch % gg::kTrainRows || o->batch > 65536 || o->epochs < 1 || o->epochs > 1024 ||
+      !(o->lr > 0.0f))
+    return c->fail(GG_ERR_ARG, "%s: batch a multiple of 128 (<= 65536), 1..1024 epochs, lr > 0", who);
+  return GG_OK;
+}
+
+// Adam training of the network of model m on the n_rows rows in c->d_arf_rows.
+static int arf_train_impl(gg_ctx *c, uint64_t n_rows, const gg_arf_model &m, const gg_arf_train_opts *o,
+                          gg_arf_model *model_out, double *loss);
+
 int gg_arf_train(gg_ctx *c, const gg_arf_sampling *smp, const gg_arf_train_opts *o, gg_arf_model *model_out,
                  double *loss) {
   if (!c || !smp || !o) return GG_ERR_ARG;
   cudaSetDevice(c->device);
   if (!c->have_tables || !c->have_spect)
     return c->fail(GG_ERR_STATE, "gg_arf_train: upload the tables and call gg_spect_setup first");
-  if (o->batch < gg::kTrainRows || o->batch % gg::kTrainRows || o->batch > 65536 || o->epochs < 1 || o->epochs > 1024 ||
-      !(o->lr > 0.0f) || o->n_samples == 0)
-    return c->fail(GG_ERR_ARG, "gg_arf_train: batch a multiple of 128 (<= 65536), 1..1024 epochs, lr > 0, samples > 0");
+  int st;
+  if ((st = arf_check_opts(c, o, "gg_arf_train"))) return st;
+  if (o->n_samples == 0) return c->fail(GG_ERR_ARG, "gg_arf_train: samples > 0");
   // training rows on the device
   uint64_t n_rows = 0;
   {
@@ -1523,26 +1556,51 @@ int gg_arf_train(gg_ctx *c, const gg_arf_sampling *smp, const gg_arf_train_opts 
         !(smp->e_max < 2.0 * gg::kMC2) || !(smp->cos_theta_max >= 0.0 && smp->cos_theta_max < 1.0) ||
         !(smp->russian_roulette >= 1.0))
       return c->fail(GG_ERR_ARG, "gg_arf_train: invalid sampling");
-    int st = c->precision == GG_PREC_F64 ? arf_generate<double>(c, smp, o->n_samples, o->seed, 0, o->n_samples)
-                                         : arf_generate<float>(c, smp, o->n_samples, o->seed, 0, o->n_samples);
+    st = c->precision == GG_PREC_F64 ? arf_generate<double>(c, smp, o->n_samples, o->seed, 0, o->n_samples)
+                                     : arf_generate<float>(c, smp, o->n_samples, o->seed, 0, o->n_samples);
     if (st) return st;
     n_rows = c->arf_n_rows;
     if (n_rows < (uint64_t)o->batch) return c->fail(GG_ERR_DOMAIN, "gg_arf_train: fewer rows than one batch");
   }
-  gg_arf_model m{};
-  m.n_classes = c->spect.n_windows + 1;
-  const double th = std::acos(smp->cos_theta_max) * (180.0 / M_PI);
-  m.x_mean[0] = (float)(0.5 * th);
-  m.x_std[0] = (float)(th / std::sqrt(12.0));
-  m.x_mean[1] = 0.0f;
-  m.x_std[1] = (float)(360.0 / std::sqrt(12.0));
-  m.x_mean[2] = (float)(0.5 * (smp->e_min + smp->e_max));
-  m.x_std[2] = (float)((smp->e_max - smp->e_min) / std::sqrt(12.0));
-  m.russian_roulette = smp->russian_roulette;
-  m.e_min = smp->e_min;
-  m.e_max = smp->e_max;
-  m.theta_max_deg = th;
-  m.distance_to_crystal = c->spect.collimator_thickness + c->spect.gap + 0.5 * c->spect.crystal_thickness;
+  const gg_arf_model m = arf_domain_model(c, smp->e_min, smp->e_max, std::acos(smp->cos_theta_max) * (180.0 / M_PI),
+                                          smp->russian_roulette);
+  return arf_train_impl(c, n_rows, m, o, model_out, loss);
+}
+
+int gg_arf_train_rows(gg_ctx *c, const float *rows, uint64_t n_rows, const gg_arf_model *domain,
+                      const gg_arf_train_opts *o, gg_arf_model *model_out, double *loss) {
+  if (!c || !rows || !domain || !o) return GG_ERR_ARG;
+  cudaSetDevice(c->device);
+  if (!c->have_tables || !c->have_spect)
+    return c->fail(GG_ERR_STATE, "gg_arf_train_rows: upload the tables and call gg_spect_setup first");
+  int st;
+  if ((st = arf_check_opts(c, o, "gg_arf_train_rows"))) return st;
+  if (n_rows < (uint64_t)o->batch) return c->fail(GG_ERR_DOMAIN, "gg_arf_train_rows: fewer rows than one batch");
+  if (!(domain->e_min > 0) || !(domain->e_max > domain->e_min) || !(domain->theta_max_deg > 0) ||
+      !(domain->theta_max_deg <= 90.0) || !(domain->russian_roulette >= 1.0))
+    return c->fail(GG_ERR_ARG, "gg_arf_train_rows: domain needs 0 < e_min < e_max, 0 < theta_max <= 90, rr >= 1");
+  const int n_classes = c->spect.n_windows + 1;
+  for (uint64_t i = 0; i < n_rows; ++i) {
+    const float *r = rows + 4 * i;
+    if (!std::isfinite(r[0]) || !std::isfinite(r[1]) || !std::isfinite(r[2]) || !(r[3] >= 0.0f) ||
+        !(r[3] < (float)n_classes) || r[3] != std::floor(r[3]))
+      return c->fail(GG_ERR_ARG, "gg_arf_train_rows: row %llu: non-finite input or class outside [0, %d)",
+                     (unsigned long long)i, n_classes);
+  }
+  if (n_rows > c->arf_rows_cap) {
+    dfree(c->d_arf_rows);
+    c->arf_rows_cap = 0;
+    if ((st = c->cuda(cudaMalloc(&c->d_arf_rows, n_rows * sizeof(float4)), "cudaMalloc ARF rows"))) return st;
+    c->arf_rows_cap = n_rows;
+  }
+  if ((st = c->h2d(c->d_arf_rows, rows, n_rows * sizeof(float4), "upload ARF rows"))) return st;
+  const gg_arf_model m = arf_domain_model(c, domain->e_min, domain->e_max, domain->theta_max_deg,
+                                          domain->russian_roulette);
+  return arf_train_impl(c, n_rows, m, o, model_out, loss);
+}
+
+static int arf_train_impl(gg_ctx *c, uint64_t n_rows, const gg_arf_model &m, const gg_arf_train_opts *o,
+                          gg_arf_model *model_out, double *loss) {
   int st;
   if ((st = arf_model_check(c, &m))) return st;
   std::vector<float> w0 = arf_init_params(o->init_seed, m.n_classes);
@@ -1692,18 +1750,19 @@ int gg_batch_setup(gg_ctx *c, const gg_sim_desc *sims, int32_t n) {
   for (int k = 0; k < n; ++k) {
     const gg_volume_desc &v = sims[k].volume;
     const gg_source_desc &src = sims[k].source;
-    uint64_t m = 1;
+    size_t m = 0;
+    char msg[160];
+    if (gg::check_dims(v.dims, (size_t)UINT32_MAX - 1, &m, msg, sizeof(msg)))
+      return c->fail(GG_ERR_ARG, "sim %d: %s", k, msg);
     for (int a = 0; a < 3; ++a) {
-      if (v.dims[a] <= 0 || !(v.spacing[a] > 0)) return c->fail(GG_ERR_ARG, "sim %d: dims and spacing must be > 0", k);
+      if (!(v.spacing[a] > 0)) return c->fail(GG_ERR_ARG, "sim %d: spacing must be > 0", k);
       if (!(std::fabs(v.corner[a]) + v.dims[a] * v.spacing[a] <= 2.0 * c->world.half_size[a]))
         return c->fail(GG_ERR_ARG, "sim %d: the image is not inside the world", k);
-      m *= (uint64_t)v.dims[a];
     }
     if (!v.labels || !v.majorant) return c->fail(GG_ERR_ARG, "sim %d: labels and majorant needed", k);
     for (uint64_t i = 0; i < m; ++i)
       if (v.labels[i] >= c->n_mat) return c->fail(GG_ERR_ARG, "sim %d: label outside the material table", k);
-    for (int i = 0; i < c->n_e; ++i)
-      if (!(v.majorant[i] > 0) || !std::isfinite(v.majorant[i])) return c->fail(GG_ERR_ARG, "sim %d: bad majorant", k);
+    if (gg::check_majorant(v.majorant, c->n_e, msg, sizeof(msg))) return c->fail(GG_ERR_ARG, "sim %d: %s", k, msg);
     if (src.pos_type < GG_POS_POINT || src.pos_type > GG_POS_DISC || src.dir_type < GG_DIR_ISO ||
         src.dir_type > GG_DIR_FOCUSED || (src.ene_type != GG_ENE_MONO && src.ene_type != GG_ENE_RANGE) ||
         src.n_accept != 0)
