@@ -126,6 +126,21 @@ class SpectHead(GateObject):
         return f"{self.name}_crystal"
 
 
+class ArfDetectorPlane(SpectHead):
+    """Detection plane of an ARF detector or of an ARF training dataset
+    (contrib/spect/ge_discovery_nm670.py:957-991 add_detection_plane_for_arf).
+    On the GPU path the plane is the collimator face of a head of
+    `collimator_type`, placed like a SpectHead by rotate_gantry: photons that
+    reach it inside the network's domain are scored by the ARFActor's
+    network, the others are tracked through the collimator and crystal
+    behind it.  `size` (the plane's extent, default 576 x 446 mm) bounds the
+    face; the thickness (1 nm in the reference) is not used."""
+
+    type_name = "ArfDetectorPlane"
+    user_info_defaults = dict(SpectHead.user_info_defaults, size=[576 * u.mm, 446 * u.mm, 1 * u.nm],
+                              material="G4_Galactic", color=[1, 0, 0, 1])
+
+
 class VolumeManager:
     def __init__(self, simulation):
         self.simulation = simulation
@@ -137,7 +152,7 @@ class VolumeManager:
         if name in self.volumes:
             raise ValueError(f"a volume named '{name}' already exists")
         cls = {"Box": BoxVolume, "BoxVolume": BoxVolume, "Image": ImageVolume, "ImageVolume": ImageVolume,
-               "SpectHead": SpectHead}.get(volume_type)
+               "SpectHead": SpectHead, "ArfDetectorPlane": ArfDetectorPlane}.get(volume_type)
         if cls is None:
             raise NotImplementedError(f"volume type '{volume_type}' is not supported by the GPU path")
         v = cls(name, self.simulation)
@@ -465,6 +480,90 @@ class DigitizerProjectionActor(GateObject):
         object.__setattr__(self, "counts_squared", sq)
 
 
+class DigitizerEnergyWindowsActor(GateObject):
+    """Energy windows of a head's singles (GateDigitizerEnergyWindowsActor::ApplyThreshold,
+    core/opengate_core/opengate_lib/digitizer/GateDigitizerEnergyWindowsActor.cpp:116-132;
+    opengate/actors/digitizers.py): `channels` = [{"name", "min", "max"}], [min, max).  A
+    projection actor on the same crystal without channels of its own takes these."""
+
+    type_name = "DigitizerEnergyWindowsActor"
+    user_info_defaults = {"attached_to": None, "input_digi_collection": "Singles", "channels": [],
+                          "output_filename": "auto", "write_to_disk": False, "priority": 90}
+
+
+def check_channel_overlap(ch1, ch2):
+    """True when two energy windows overlap (opengate/actors/arfactors.py:19-30)."""
+    a0, a1, b0, b1 = float(ch1["min"]), float(ch1["max"]), float(ch2["min"]), float(ch2["max"])
+    return b0 < a0 < b1 or b0 < a1 < b1 or a0 < b0 < a1 or a0 < b1 < a1
+
+
+class ARFTrainingDatasetActor(GateObject):
+    """Training rows of an ARF network (GateARFTrainingDatasetActor,
+    core/opengate_core/opengate_lib/GateARFTrainingDatasetActor.cpp:76-137; arfactors.py:33-145):
+    for photons reaching the detection plane `attached_to`, (E, Theta, Phi) at the plane and
+    the energy window (1..n) their single ends in, 0 = none (kept with probability
+    1 / russian_roulette).  The GPU path starts the photons on the plane with the source's
+    energy range, directions uniform in theta up to `theta_max_deg` (default: the largest angle
+    between the source disc and the plane) and phi, and tracks them through the head and the
+    digitizer of the windows actor `energy_windows_actor`.  Rows go to `output_filename` (.npz,
+    opengate_gb300.arf format)."""
+
+    type_name = "ARFTrainingDatasetActor"
+    user_info_defaults = {"attached_to": None, "energy_windows_actor": None, "russian_roulette": 1,
+                          "plane_axis": [0, 1, 2], "attributes": [], "debug": False, "clear_every": 1e5,
+                          "keep_zero_edep": False, "output_filename": "arf_training_dataset.npz",
+                          "write_to_disk": True, "theta_max_deg": None, "priority": 100}
+
+    def __init__(self, name, simulation=None, **kw):
+        super().__init__(name, simulation, **kw)
+        object.__setattr__(self, "rows", None)
+        object.__setattr__(self, "number_of_samples", 0)
+        object.__setattr__(self, "sampling", None)  # gg_arf_sampling of the last run
+
+    def get_output_path(self):
+        return pathlib.Path(self.simulation.output_dir) / pathlib.Path(self.output_filename)
+
+
+class ARFActor(GateObject):
+    """ARF detector (GateARFActor, core/opengate_core/opengate_lib/GateARFActor.cpp:60-113;
+    opengate/actors/arfactors.py:147-453): photons reaching the plane `attached_to` are scored
+    with the window probabilities of the network in `pth_filename` at the pixel where their line
+    crosses the plane `distance_to_crystal` behind it.  Output `counts` (and `squared_counts`):
+    [run * n_windows + window][y][x] float32, spacing (image_spacing, 1), origin as the
+    projection actor's.  The network file is this library's (.npz from train_arf, not a garf .pth);
+    photons outside its trained domain, or entering the head through a side, are tracked through
+    the collimator and crystal instead and counted in the same image.  batch_size and
+    verbose_batch have no effect (every photon is scored on the GPU); flip_plane,
+    enable_hit_slice, plane_axis other than [0, 1, 2] and gpu_mode "cpu" raise."""
+
+    type_name = "ARFActor"
+    user_info_defaults = {"attached_to": None, "batch_size": 2e5, "pth_filename": None, "image_size": [128, 128],
+                          "image_spacing": [4.41806 * u.mm, 4.41806 * u.mm], "distance_to_crystal": None,
+                          "verbose_batch": False, "enable_hit_slice": False, "flip_plane": False,
+                          "plane_axis": [0, 1, 2], "gpu_mode": "auto", "output_filename": "auto",
+                          "write_to_disk": True, "priority": 100}
+
+    def __init__(self, name, simulation=None, **kw):
+        super().__init__(name, simulation, **kw)
+        object.__setattr__(self, "counts", ActorOutput(self, "counts", True))
+        sq = ActorOutput(self, "squared_counts", False)
+        object.__setattr__(self, "squared_counts", sq)
+        object.__setattr__(self, "counts_squared", sq)
+
+    def check(self):
+        if self.flip_plane:
+            raise NotImplementedError(f"ARFActor '{self.name}': flip_plane")
+        if self.enable_hit_slice:
+            raise NotImplementedError(f"ARFActor '{self.name}': enable_hit_slice")
+        if list(self.plane_axis) != [0, 1, 2]:
+            raise NotImplementedError(f"ARFActor '{self.name}': plane_axis other than [0, 1, 2]")
+        if self.gpu_mode not in ("auto", "gpu"):
+            raise NotImplementedError(f"ARFActor '{self.name}': gpu_mode '{self.gpu_mode}' (the network runs "
+                                      "on the GPU only)")
+        if not self.pth_filename:
+            raise ValueError(f"ARFActor '{self.name}': set pth_filename")
+
+
 FWHM_TO_SIGMA = 1.0 / (2.0 * math.sqrt(2.0 * math.log(2.0)))
 
 
@@ -694,7 +793,9 @@ class Simulation:
                "ScatterSplittingFreeFlightActor": ScatterSplittingFreeFlightActor,
                "DigitizerBlurringActor": DigitizerBlurringActor,
                "DigitizerSpatialBlurringActor": DigitizerSpatialBlurringActor,
-               "DigitizerProjectionActor": DigitizerProjectionActor}.get(actor_type)
+               "DigitizerProjectionActor": DigitizerProjectionActor,
+               "DigitizerEnergyWindowsActor": DigitizerEnergyWindowsActor,
+               "ARFActor": ARFActor, "ARFTrainingDatasetActor": ARFTrainingDatasetActor}.get(actor_type)
         if cls is None:
             raise NotImplementedError(f"actor type '{actor_type}' is not supported by the GPU path")
         a = cls(name, self)
@@ -764,33 +865,77 @@ class Simulation:
             raise ValueError(f"rotate_gantry gave {h0.nb_angle} positions for {len(runs)} runs")
         step = h0.step_angle_deg if h0.nb_angle > 1 else 0.0
         projs = [a for a in self.actors.values() if isinstance(a, DigitizerProjectionActor)]
-        if not projs:
-            raise ValueError("a SPECT simulation needs a DigitizerProjectionActor")
-        head_of = {h.crystal_name: i for i, h in enumerate(heads)}
-        for a in projs:
-            if a.attached_to not in head_of:
-                raise ValueError(f"projection actor '{a.name}' must be attached to a head crystal "
-                                 f"({', '.join(head_of)})")
-            if a.channels != projs[0].channels or list(a.size) != list(projs[0].size) or \
-                    not np.allclose(a.spacing, projs[0].spacing):
-                raise NotImplementedError("projection actors must share channels, size and spacing")
-        channels = projs[0].channels
-        windows = [(float(c["min"]) / u.MeV, float(c["max"]) / u.MeV) for c in channels]
+        arfs = [a for a in self.actors.values() if isinstance(a, ARFActor)]
+        if projs and arfs:
+            raise NotImplementedError("ARF detectors and projection actors in one simulation")
+        if not projs and not arfs:
+            raise ValueError("a SPECT simulation needs a DigitizerProjectionActor or an ARFActor")
+        arf = None
+        if arfs:
+            # ARF detectors: the windows, adder and blurring are those the network was trained with
+            from . import arf as ARF
+
+            head_of = {h.name: i for i, h in enumerate(heads)}
+            for a in arfs:
+                a.check()
+                if a.attached_to not in head_of:
+                    raise ValueError(f"ARFActor '{a.name}' must be attached to a detection plane or head "
+                                     f"({', '.join(head_of)})")
+                if str(a.pth_filename) != str(arfs[0].pth_filename) or list(a.image_size) != \
+                        list(arfs[0].image_size) or not np.allclose(a.image_spacing, arfs[0].image_spacing) or \
+                        a.distance_to_crystal != arfs[0].distance_to_crystal:
+                    raise NotImplementedError("ARF detectors must share the network, image size, spacing and "
+                                              "distance to the crystal")
+            model, params, meta = ARF.load_model(arfs[0].pth_filename)
+            if meta["collimator_type"].lower() != str(h0.collimator_type).lower() or \
+                    meta["crystal_size"] != str(h0.crystal_size):
+                raise ValueError(f"network '{arfs[0].pth_filename}' was trained for a {meta['collimator_type']} "
+                                 f"collimator and a {meta['crystal_size']} crystal, the heads have "
+                                 f"{h0.collimator_type} / {h0.crystal_size}")
+            if arfs[0].distance_to_crystal is not None:
+                model.distance_to_crystal = float(arfs[0].distance_to_crystal) / u.mm
+            arf = (model, params, meta)
+            windows = [(float(a), float(b)) for a, b in np.asarray(meta["windows"])]
+            size, spacing_in = arfs[0].image_size, arfs[0].image_spacing
+        else:
+            head_of = {h.crystal_name: i for i, h in enumerate(heads)}
+            ewas = {a.attached_to: a for a in self.actors.values() if isinstance(a, DigitizerEnergyWindowsActor)}
+            for a in projs:
+                if a.attached_to not in head_of:
+                    raise ValueError(f"projection actor '{a.name}' must be attached to a head crystal "
+                                     f"({', '.join(head_of)})")
+                if not a.channels and a.attached_to in ewas:
+                    a.channels = ewas[a.attached_to].channels
+                if a.channels != projs[0].channels or list(a.size) != list(projs[0].size) or \
+                        not np.allclose(a.spacing, projs[0].spacing):
+                    raise NotImplementedError("projection actors must share channels, size and spacing")
+            channels = projs[0].channels
+            windows = [(float(c["min"]) / u.MeV, float(c["max"]) / u.MeV) for c in channels]
+            size, spacing_in = projs[0].size, projs[0].spacing
         extra = [h0.collimator_material, h0.crystal_material]
         scene, vol, hu, names, sources = self.build_scene(extra_materials=extra)
         coll = S.COLLIMATORS.get(str(h0.collimator_type).lower())
         if coll is None:
             raise NotImplementedError(f"collimator '{h0.collimator_type}'")
-        spacing = [float(x) / u.mm for x in projs[0].spacing]
+        spacing = [float(x) / u.mm for x in spacing_in]
         half_w = h0.half_width / u.mm if h0.half_width else None
         sp = S.SpectSpec(collimator=coll, crystal_thickness=S.CRYSTALS[h0.crystal_size], gap=h0.gap / u.mm,
                          radius=h0.radius / u.mm, n_heads=len(heads), n_runs=len(runs), windows=windows,
-                         size=[int(x) for x in projs[0].size], spacing=spacing,
+                         size=[int(x) for x in size], spacing=spacing,
                          step_angle_deg=step, collimator_material=names.index(h0.collimator_material),
                          crystal_material=names.index(h0.crystal_material),
                          head_start_deg=[h.start_angle_deg for h in heads])
         if half_w:
             sp.half_width = half_w
+        sp.arf = arf
+        if arf is not None:
+            ARF.apply_head_meta(sp, arf[2])
+            mods = [a.name for a in self.actors.values()
+                    if isinstance(a, (DigitizerAdderActor, DigitizerBlurringActor, DigitizerSpatialBlurringActor,
+                                      GammaFreeFlightActor, ScatterSplittingFreeFlightActor))]
+            if mods:
+                raise NotImplementedError(f"with ARF detectors the digitizer is the network's own: remove {mods}")
+            return scene, sp, sources, arfs, head_of
         ffs = [a for a in self.actors.values() if isinstance(a, GammaFreeFlightActor)]
         sss = [a for a in self.actors.values() if isinstance(a, ScatterSplittingFreeFlightActor)]
         if len(ffs) + len(sss) > 1:
@@ -840,6 +985,11 @@ class Simulation:
         plan = [events_per_run(src, runs, rng) for src, _ in sources]
         eng = SpectEngine(scene, sp, device=self.device, precision=self.precision, batch=self.batch)
         try:
+            if sp.arf is not None:
+                from .engine import ArfNetwork
+
+                ArfNetwork(eng).set_model(sp.arf[0], sp.arf[1])
+                eng.use_arf(True)
             first = 0
             for r in range(len(runs)):
                 frames = np.ascontiguousarray(sp.frames(r), dtype=np.float64)
@@ -851,7 +1001,13 @@ class Simulation:
                         eng._call("gg_run", C.ctypes.c_uint64(plan[k][r]), C.ctypes.c_uint64(seed),
                                   C.ctypes.c_uint64(first))
                     first += plan[k][r]
-            if sp.free_flight.enabled:
+            if sp.arf is not None:
+                # ARF detectors: network window weights plus the counts of the photons tracked instead
+                counts = eng.projection()
+                w, w2 = eng.arf_projection(squared=True)
+                proj = (counts + w).astype(np.float32)
+                proj2 = (counts + w2).astype(np.float32)
+            elif sp.free_flight.enabled:
                 proj, proj2 = eng.weighted_projection(squared=True)
             else:
                 proj = eng.projection()
@@ -863,7 +1019,8 @@ class Simulation:
         for a in projs:
             h = head_of[a.attached_to]
             sx, sy = spacing
-            origin = [-a.size[0] * sx / 2 + sx / 2, -a.size[1] * sy / 2 + sy / 2, 0.0]
+            n0, n1 = (a.image_size if isinstance(a, ARFActor) else a.size)[:2]
+            origin = [-n0 * sx / 2 + sx / 2, -n1 * sy / 2 + sy / 2, 0.0]
             img = image_io.Image(proj[h], [sx, sy, 1.0], origin)
             a.counts.image = img
             a.counts.number_of_samples = first
@@ -886,9 +1043,118 @@ class Simulation:
                 a.counts.sps = int(a.counts.steps / elapsed) if elapsed > 0 else 0
         return cnt
 
+    def _arf_theta_max(self, actor, plane, source):
+        """Largest angle (degrees) between the plane normal and a line from the source's disc to
+        the plane: the angular domain of the training rows (capped to [1, 89] degrees)."""
+        if actor.theta_max_deg is not None:
+            return float(actor.theta_max_deg)
+        pos = source.position
+        if str(pos.type) not in ("disc", "point", "sphere"):
+            return 85.0
+        t = math.radians(plane.start_angle_deg)
+        normal = np.array([math.sin(t), -math.cos(t), 0.0])
+        centre = (plane.radius / u.mm) * normal
+        src = np.asarray(pos.translation, dtype=np.float64) / u.mm
+        depth = float(np.dot(src - centre, normal))
+        if not depth > 0.0:
+            return 85.0
+        r = float(pos.radius) / u.mm if str(pos.type) != "point" else 0.0
+        size = getattr(plane, "size", None)
+        half_diag = 0.5 * math.hypot(size[0] / u.mm, size[1] / u.mm) if size is not None else plane.half_width
+        lateral = float(np.linalg.norm((src - centre) - depth * normal))
+        th = math.degrees(math.atan((r + lateral + half_diag) / depth))
+        return float(min(max(th, 1.0), 89.0))
+
+    def _run_arf_dataset(self):
+        """ARF training rows (ARFTrainingDatasetActor): photons started on the detection plane,
+        tracked through the head and the digitizer chain, one row per photon (class 0 rows
+        Russian-rouletted), written to the actor's output file."""
+        from . import arf as ARF
+        from . import spect as S
+
+        t0 = time.perf_counter()
+        actors = [a for a in self.actors.values() if isinstance(a, ARFTrainingDatasetActor)]
+        if len(actors) != 1:
+            raise NotImplementedError("one ARFTrainingDatasetActor per simulation")
+        act = actors[0]
+        plane = self.volumes.get(act.attached_to)
+        if not isinstance(plane, SpectHead):
+            raise ValueError(f"ARFTrainingDatasetActor '{act.name}' must be attached to a detection plane "
+                             "(add_detection_plane_for_arf) or a SPECT head")
+        if list(act.plane_axis) != [0, 1, 2]:
+            raise NotImplementedError("plane_axis other than [0, 1, 2]")
+        ewa = self.actors.get(act.energy_windows_actor)
+        if not isinstance(ewa, DigitizerEnergyWindowsActor):
+            raise ValueError(f"The actor '{act.name}' has the user input energy_windows_actor="
+                             f"{act.energy_windows_actor}, but no DigitizerEnergyWindowsActor of this name exists")
+        chans = list(ewa.channels)
+        for i, c1 in enumerate(chans):
+            for j, c2 in enumerate(chans[i + 1:]):
+                if check_channel_overlap(c1, c2):
+                    raise ValueError(f"In the actor '{act.name}', the energy channels {i} and {i + 1 + j} overlap. "
+                                     "This is not possible for ARF.")
+        if not chans:
+            raise ValueError(f"energy windows actor '{ewa.name}' has no channels")
+        sources = list(self.sources.values())
+        if len(sources) != 1 or sources[0].energy.type != "range":
+            raise NotImplementedError("the ARF training dataset needs one GenericSource with energy.type 'range'")
+        src = sources[0]
+        e_min, e_max = float(src.energy.min_energy) / u.MeV, float(src.energy.max_energy) / u.MeV
+        seed = self._seed()
+        self.last_seed = seed
+        rng = np.random.default_rng(seed)
+        n = int(sum(events_per_run(src, self.run_timing_intervals, rng)))
+        # head and digitizer: the plane's collimator / crystal, the windows, adder and blurring on its crystal
+        sp = S.SpectSpec(collimator=S.COLLIMATORS[str(plane.collimator_type).lower()],
+                         crystal_thickness=S.CRYSTALS[plane.crystal_size], gap=plane.gap / u.mm, n_heads=1,
+                         n_runs=1, windows=[(float(c["min"]) / u.MeV, float(c["max"]) / u.MeV) for c in chans])
+        # the digitizer modules on the windows actor's crystal (the plane's own, or that of a head
+        # behind the plane as in the reference's set-up); the head geometry is the plane's
+        for a in self.actors.values():
+            if isinstance(a, (DigitizerAdderActor, DigitizerBlurringActor, DigitizerSpatialBlurringActor)):
+                if a.attached_to != ewa.attached_to:
+                    continue
+                if isinstance(a, DigitizerAdderActor):
+                    sp.adder_policy = a.adder_policy()
+                elif isinstance(a, DigitizerBlurringActor):
+                    sp.set_energy_blur(**a.energy_blur())
+                else:
+                    sp.set_spatial_blur(**a.spatial_blur())
+        meta = ARF.head_meta(sp, plane.collimator_type, plane.crystal_size)
+        theta_max = self._arf_theta_max(act, plane, src)
+        size = getattr(plane, "size", None)
+        half = [0.5 * float(size[0]) / u.mm, 0.5 * float(size[1]) / u.mm] if size is not None else [sp.half_width] * 2
+        half = [min(h, sp.half_width) for h in half]
+        from .engine import ArfNetwork
+
+        eng, _ = ARF.head_engine(meta, device=self.device, precision=self.precision,
+                                 collimator_material=plane.collimator_material,
+                                 crystal_material=plane.crystal_material)
+        with eng:
+            smp = ArfNetwork.sampling(e_min, e_max, theta_max, half, float(act.russian_roulette))
+            rows = ArfNetwork(eng).dataset(smp, n, seed)
+            cnt = eng.counters()
+        object.__setattr__(act, "rows", rows)
+        object.__setattr__(act, "number_of_samples", n)
+        object.__setattr__(act, "sampling", smp)
+        if act.write_to_disk:
+            ARF.save_dataset(act.get_output_path(), rows, meta, e_min, e_max, theta_max, act.russian_roulette)
+        elapsed = time.perf_counter() - t0
+        for a in self.actors.values():
+            if isinstance(a, SimulationStatisticsActor):
+                a.counts.runs = len(self.run_timing_intervals)
+                a.counts.events = n
+                a.counts.tracks = n
+                a.counts.steps = cnt["head_steps"]
+                a.counts.duration = elapsed * u.s
+                a.counts.pps = int(n / elapsed) if elapsed > 0 else 0
+        return cnt
+
     def run(self, start_new_process=False):
         from .engine import DoseEngine
 
+        if any(isinstance(a, ARFTrainingDatasetActor) for a in self.actors.values()):
+            return self._run_arf_dataset()
         if any(isinstance(v, SpectHead) for v in self.volumes.values()):
             return self._run_spect()
         t0 = time.perf_counter()

@@ -95,12 +95,106 @@ def add_digitizer(sim, crystal_name, name=None, size=None, spacing=None, channel
     sb.keep_in_solid_limits = True
     sb.use_truncated_Gaussian = False
     # energy windows and projection
+    cc = sim.add_actor("DigitizerEnergyWindowsActor", f"{name}_energy_window")
+    cc.attached_to = crystal_name
+    cc.channels = channels if channels is not None else get_default_energy_windows("tc99m")
     proj = sim.add_actor("DigitizerProjectionActor", f"{name}_projection")
     proj.attached_to = crystal_name
-    proj.channels = channels if channels is not None else get_default_energy_windows("tc99m")
+    proj.channels = cc.channels
     proj.input_digi_collections = [c["name"] for c in proj.channels]
     proj.size = size if size is not None else d_size
     proj.spacing = spacing if spacing is not None else d_spacing
     if filename is not None:
         proj.output_filename = filename
-    return Digitizer(name, proj, [sc, eb, sb])
+    return Digitizer(name, proj, [sc, eb, sb, cc])
+
+
+def add_digitizer_energy_windows(sim, crystal_volume_name, channels, policy="EnergyWinnerPosition"):
+    """Singles (adder) and energy windows of a head crystal, no blurring and no projection
+    (the chain of add_digitizer_energy_windows_OLD, ge_discovery_nm670.py:601-630); returns the
+    DigitizerEnergyWindowsActor, e.g. for an ARFTrainingDatasetActor."""
+    sc = sim.add_actor("DigitizerAdderActor", f"Singles_{crystal_volume_name}")
+    sc.attached_to = crystal_volume_name
+    sc.group_volume = None
+    sc.policy = policy
+    cc = sim.add_actor("DigitizerEnergyWindowsActor", f"EnergyWindows_{crystal_volume_name}")
+    cc.attached_to = crystal_volume_name
+    cc.input_digi_collection = sc.name
+    cc.channels = channels
+    return cc
+
+
+# ---------------------------------------------------------------------------------- ARF
+def add_detection_plane_for_arf(sim, det_name, colli_type, plane_size=None):
+    """The ARF detection plane (ge_discovery_nm670.py:957-991): on the GPU path, the collimator
+    face of a `colli_type` head placed by rotate_gantry like a SpectHead (the reference puts a
+    1 nm G4_Galactic box in front of the head).  plane_size: [576 mm, 446 mm] by default."""
+    mm = _u.mm
+    plane = sim.add_volume("ArfDetectorPlane", det_name)
+    plane.collimator_type = str(colli_type).lower()
+    if plane_size is None:
+        plane_size = [576 * mm, 446 * mm]
+    plane.size = [plane_size[0], plane_size[1], 1 * _u.nm]
+    rotate_gantry(plane, plane.radius, start_angle_deg=0)
+    return plane
+
+
+def add_source_for_arf_training_dataset(sim, source_name, activity, detector_plane, min_energy, max_energy):
+    """The training source of ge_discovery_nm670.py:994-1011: a 5 cm disc 20 cm in front of the
+    plane, isotropic directions accepted towards the plane, energies uniform in [min, max]."""
+    cm = _u.cm
+    source = sim.add_source("GenericSource", source_name)
+    source.particle = "gamma"
+    source.activity = activity
+    source.position.type = "disc"
+    source.position.radius = 5 * cm
+    source.position.translation = [0, -20 * cm, 0]
+    source.direction.type = "iso"
+    source.energy.type = "range"
+    source.energy.min_energy = min_energy
+    source.energy.max_energy = max_energy
+    source.direction.angular_acceptance.target_volumes = [detector_plane.name]
+    source.direction.angular_acceptance.enable_intersection_check = True
+    return source
+
+
+def add_actor_for_arf_training_dataset(sim, colli_type, ene_win_actor, rr):
+    """Detection plane + ARFTrainingDatasetActor (ge_discovery_nm670.py:1014-1026); the rows go
+    to arf_training_dataset.npz (this library's dataset format) in the output directory."""
+    detector_plane = add_detection_plane_for_arf(sim, "arf_plane", colli_type)
+    arf = sim.add_actor("ARFTrainingDatasetActor", "ARF (training)")
+    arf.energy_windows_actor = ene_win_actor.name
+    arf.attached_to = detector_plane.name
+    arf.output_filename = "arf_training_dataset.npz"
+    arf.russian_roulette = rr
+    arf.plane_axis = [0, 1, 2]
+    return detector_plane, arf
+
+
+def distance_to_crystal(colli_type, crystal_size="3/8", gap=0.0):
+    """Distance (mm units) from the collimator face to the middle of the crystal: the depth of
+    the ARF projection plane."""
+    from ... import spect as S
+
+    coll = S.COLLIMATORS[str(colli_type).lower()]
+    return (coll["collimator_thickness"] + gap + 0.5 * S.CRYSTALS[crystal_size]) * _u.mm
+
+
+def add_arf_detector(sim, name, colli_type, image_size, image_spacing, pth_filename):
+    """Detection plane + ARFActor (ge_discovery_nm670.py:1029-1053); `pth_filename` is a network
+    file of this library (train_arf), the projection depth the middle of the crystal."""
+    det_plane = add_detection_plane_for_arf(sim, det_name=name, colli_type=colli_type)
+    arf = sim.add_actor("ARFActor", f"{name}_arf")
+    arf.attached_to = det_plane.name
+    arf.output_filename = f"projection_{arf.name}.mhd"
+    arf.batch_size = 1e5
+    arf.image_size = image_size
+    arf.image_spacing = image_spacing
+    arf.verbose_batch = False
+    arf.distance_to_crystal = distance_to_crystal(colli_type, det_plane.crystal_size, det_plane.gap)
+    arf.pth_filename = pth_filename
+    arf.flip_plane = False
+    arf.plane_axis = [0, 1, 2]
+    arf.enable_hit_slice = False
+    arf.gpu_mode = "auto"
+    return det_plane, arf

@@ -250,6 +250,27 @@ class ArfNetwork:
         self.model = model
         return model, loss
 
+    def train_rows(self, rows, e_min, e_max, theta_max_deg, russian_roulette, epochs=4, batch=8192, lr=1e-3,
+                   init_seed=1, beta1=0.9, beta2=0.999, eps=1e-8, lr_final=None):
+        """Trains on given rows [n][4] = (E MeV, theta deg, phi deg, class) (gg_arf_train_rows):
+        the domain (energy range, largest theta, Russian roulette of class 0) sets the
+        standardisation and the range where the network replaces tracking."""
+        rows = np.ascontiguousarray(rows, dtype=np.float32).reshape(-1, 4)
+        o = C.ArfTrainOpts()
+        o.n_samples, o.seed, o.init_seed = len(rows), 0, int(init_seed)
+        o.batch, o.epochs = int(batch), int(epochs)
+        o.lr, o.beta1, o.beta2, o.eps = lr, beta1, beta2, eps
+        o.lr_final = lr / 100.0 if lr_final is None else lr_final
+        dom = C.ArfModel()
+        dom.e_min, dom.e_max = float(e_min), float(e_max)
+        dom.theta_max_deg, dom.russian_roulette = float(theta_max_deg), float(russian_roulette)
+        model = C.ArfModel()
+        loss = np.zeros(epochs, dtype=np.float64)
+        self.eng._call("gg_arf_train_rows", C.ptr(rows, ctypes.c_float), ctypes.c_uint64(len(rows)),
+                       ctypes.byref(dom), ctypes.byref(o), ctypes.byref(model), C.ptr(loss, ctypes.c_double))
+        self.model = model
+        return model, loss
+
     def set_model(self, model, params):
         params = np.ascontiguousarray(params, dtype=np.float32)
         if params.size != C.GG_ARF_N_PARAMS:
