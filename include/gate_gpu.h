@@ -236,6 +236,12 @@ typedef struct {
   int32_t interact_min; /* 1..32: pending collisions that trigger an interaction phase, 0 = default */
 } gg_device_opts;
 
+/* Dose transport kernel of gg_run for single simulations with analog scoring
+   (the track-length estimator and batched simulations always use the phase
+   kernel).  Both give identical results; they differ in speed only. */
+#define GG_KERNEL_WAVEFRONT 0 /* per-block wavefront compacted by event type */
+#define GG_KERNEL_PHASED 1    /* block-synchronous phases, one history per thread (default) */
+
 int gg_create(const gg_device_opts *opts, gg_ctx **out);
 int gg_destroy(gg_ctx *ctx);
 /* Copies the last error message of ctx (or of the last failed gg_create if
@@ -248,6 +254,9 @@ int gg_set_world(gg_ctx *ctx, const gg_world_desc *world);
 int gg_set_source(gg_ctx *ctx, const gg_source_desc *source);
 /* Enables the edep / edep-squared tally on the image grid and zeroes it. */
 int gg_add_dose_tally(gg_ctx *ctx, int32_t score_squared);
+/* Selects the dose transport kernel (GG_KERNEL_*); no counterpart in the
+   reference (Geant4 has one stepping loop). */
+int gg_set_transport_kernel(gg_ctx *ctx, int32_t kind);
 int gg_reset_tally(gg_ctx *ctx);
 
 /* Track-length estimator of the dose tally (replaces the TLEDoseActor:

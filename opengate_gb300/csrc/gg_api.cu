@@ -43,6 +43,10 @@ struct gg_ctx {
   int64_t batch = 1 << 26;
   int refill_min = 8;
   int interact_min = 16;
+  // dose transport kernel of single simulations: the block-synchronous phase kernel (default,
+  // also used for the track-length estimator and batches) or the compacted wavefront
+  int transport_kernel = GG_KERNEL_PHASED;
+  uint64_t last_batch = 0;  // histories per tally batch of the last run (after the overflow cap)
   int n_sm = 0;
   cudaStream_t stream = nullptr;
   std::string err;
@@ -1107,8 +1111,37 @@ static int run_impl(gg_ctx *c, uint64_t n, uint64_t seed, uint64_t first, bool c
     if (bps < 1) bps = 1;
   }
   int grid = c->n_sm * bps;
-  uint64_t nb = (n + (uint64_t)c->batch - 1) / (uint64_t)c->batch;
-  size_t cap = (size_t)std::min<uint64_t>(n, (uint64_t)c->batch);
+  // the compacted wavefront kernel: single dose simulations with analog scoring
+  const bool wave = !c->have_spect && !c->tle && !c->have_batch && c->transport_kernel == GG_KERNEL_WAVEFRONT;
+  size_t wsmem = 0;
+  int wgrid = 0, wminb = c->precision == GG_PREC_F64 ? 2 : 3;
+  if (wave) {
+    wsmem = c->precision == GG_PREC_F64 ? gg::wavefront_smem_bytes<double>(c->n_comp, c->n_e, c->n_mat)
+                                        : gg::wavefront_smem_bytes<float>(c->n_comp, c->n_e, c->n_mat);
+    if (wsmem > 220 * 1024)
+      return c->fail(GG_ERR_ARG, "gg_run: tables and photon slots need %zu bytes of shared memory (max 220 KiB); "
+                     "use the phase kernel (gg_set_transport_kernel)", wsmem);
+    int wbps = 0;
+    cudaError_t e = c->precision == GG_PREC_F64 ? gg::wavefront_occupancy<double>(wsmem, wminb, &wbps)
+                                                : gg::wavefront_occupancy<float>(wsmem, wminb, &wbps);
+    if (e != cudaSuccess) return c->cuda(e, "wavefront occupancy");
+    if (wbps < 1) return c->fail(GG_ERR_CUDA, "gg_run: the wavefront kernel does not fit an SM");
+    wgrid = c->n_sm * wbps;
+  }
+  // Histories per tally batch.  The fixed-point dose tallies cannot wrap within
+  // a batch: a history deposits at most E_max in total, so over n histories a
+  // voxel's edep^2 high word (units of 2^32 of (2^-32 MeV)^2) gains at most
+  // n E_max^2 2^32 and its edep word n E_max 2^32; n <= 2^32 / E_max^2 (and
+  // 2^32 / E_max) keeps both below 2^64.
+  uint64_t batch = (uint64_t)c->batch;
+  if (c->have_tally && !c->have_spect) {
+    const double em = std::max(c->src_emax, 1e-6) * 1.001;
+    const double lim = std::min(4294967296.0 / (em * em), 4294967296.0 / em);
+    if ((double)batch > lim) batch = std::max<uint64_t>(1, (uint64_t)lim);
+  }
+  c->last_batch = batch;
+  uint64_t nb = (n + batch - 1) / batch;
+  size_t cap = (size_t)std::min<uint64_t>(n, batch);
   if (cap > c->rec_cap) {
     dfree(c->d_records);
     c->rec_cap = 0;
@@ -1167,8 +1200,8 @@ static int run_impl(gg_ctx *c, uint64_t n, uint64_t seed, uint64_t first, bool c
   int st;
   // per batch: [ev 3b] generate [ev 3b+1] transport [ev 3b+2] flush [ev 3b+3]
   for (uint64_t b = 0; b < nb; ++b) {
-    a.h_begin = first + b * (uint64_t)c->batch;
-    a.h_end = std::min(first + n, a.h_begin + (uint64_t)c->batch);
+    a.h_begin = first + b * batch;
+    a.h_end = std::min(first + n, a.h_begin + batch);
     a.rec_first = a.h_begin;
     if ((st = c->cuda(cudaMemsetAsync(c->d_next, 0, 8, c->stream), "memset"))) return st;
     if (!capturing && (st = c->cuda(cudaEventRecord(c->ev[3 * b], c->stream), "event"))) return st;
@@ -1179,6 +1212,11 @@ static int run_impl(gg_ctx *c, uint64_t n, uint64_t seed, uint64_t first, bool c
     if (c->have_spect) {
       if ((st = spect_stages(c, a, smem, minb))) return st;
       c->run_stage_launches += c->last_stage_launches;
+    } else if (wave) {
+      e = c->precision == GG_PREC_F64
+              ? gg::launch_wavefront<double>(c->scene<double>(), a, wgrid, wsmem, wminb, c->stream)
+              : gg::launch_wavefront<float>(c->scene<float>(), a, wgrid, wsmem, wminb, c->stream);
+      if ((st = c->cuda(e, "wavefront transport launch"))) return st;
     } else {
       e = c->precision == GG_PREC_F64
               ? gg::launch_transport<double>(c->scene<double>(), a, grid, c->block, smem, minb, c->stream)
@@ -1217,7 +1255,8 @@ static int run_impl(gg_ctx *c, uint64_t n, uint64_t seed, uint64_t first, bool c
     if (status & gg::kStatusQueueOverflow)
       return c->fail(GG_ERR_QUEUE_OVERFLOW, "gg_run: a SPECT stage queue overflowed (photons were dropped)");
     if (status & gg::kStatusWaitTimeout)
-      return c->fail(GG_ERR_TIMEOUT, "gg_run: a tensor-core wait of the ARF stage ran out");
+      return c->fail(GG_ERR_TIMEOUT, "gg_run: a bounded wait ran out (ARF stage tensor cores, or the queues of "
+                                     "the wavefront transport); the batch is incomplete");
     return c->fail(GG_ERR_DOMAIN, "gg_run: source sampling failed (angular acceptance exhausted max_rejection)");
   }
   return GG_OK;
@@ -1244,6 +1283,14 @@ int gg_run(gg_ctx *c, uint64_t n, uint64_t seed, uint64_t first) {
     if (st) return st;
   }
   return run_impl(c, n, seed, first);
+}
+
+int gg_set_transport_kernel(gg_ctx *c, int32_t kind) {
+  if (!c) return GG_ERR_ARG;
+  if (kind != GG_KERNEL_WAVEFRONT && kind != GG_KERNEL_PHASED)
+    return c->fail(GG_ERR_ARG, "gg_set_transport_kernel: unknown kernel %d", kind);
+  c->transport_kernel = kind;
+  return GG_OK;
 }
 
 int gg_synchronize(gg_ctx *c) {

@@ -175,6 +175,15 @@ cudaError_t launch_transport(const Scene<real> &s, const KernelArgs &a, int grid
                              int minb, cudaStream_t st);
 template <typename real>
 cudaError_t occupancy_blocks(int block, size_t smem, int minb, int *blocks_per_sm);
+// Compacted wavefront dose transport (gg_wavefront.cu): 256-thread blocks,
+// dynamic shared memory = tables + photon slots.
+template <typename real>
+size_t wavefront_smem_bytes(int n_comp, int n_e, int n_mat);
+template <typename real>
+cudaError_t launch_wavefront(const Scene<real> &s, const KernelArgs &a, int grid, size_t smem, int minb,
+                             cudaStream_t st);
+template <typename real>
+cudaError_t wavefront_occupancy(size_t smem, int minb, int *blocks_per_sm);
 cudaError_t launch_flush(unsigned long long *acc_e, unsigned long long *acc_e2, double *edep, double *edep2,
                          size_t n, int grid, cudaStream_t st);
 

@@ -250,11 +250,14 @@ __global__ void __launch_bounds__(256, MINB) k_transport(Scene<real> sg, KernelA
 
     if (phase == kRefill) {
       const bool need = state == kRefill;
-      if (need && in_hist) {
-        if constexpr (SPECT) n_singles += score_singles(s, ev, ph.run, g);
-        else hlist_flush(l, t, &bc);
-        in_hist = false;
+      if constexpr (SPECT) {
+        if (need && in_hist) n_singles += score_singles(s, ev, ph.run, g);
+      } else {
+        // every lane of the warp is here: same-voxel entries of the ending histories are summed
+        // across the warp before their atomics
+        hlist_flush_warp(l, need && in_hist, t, &bc);
       }
+      if (need) in_hist = false;
       const unsigned n_need = __popc(m_ref);
       const unsigned rank = __popc(m_ref & lt_mask);
       const uint64_t avail = pool_end - pool_next;

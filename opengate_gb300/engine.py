@@ -49,6 +49,10 @@ class DoseEngine:
     def reset(self):
         self._call("gg_reset_tally")
 
+    def set_transport_kernel(self, kind):
+        """C.GG_KERNEL_PHASED (default) or C.GG_KERNEL_WAVEFRONT: same results, different speed."""
+        self._call("gg_set_transport_kernel", int(kind))
+
     def set_tle(self, threshold_energy=float("inf"), energy_min=0.0, database="EPDL", enabled=True):
         """Track-length estimator of the dose tally (gg_set_tle); mu_en of the
         scene's compositions from ``database`` ("EPDL" or "NIST")."""

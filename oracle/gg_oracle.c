@@ -2075,6 +2075,22 @@ static int run_dose_impl(const gg_tables_desc *tb, const gg_volume_desc *vol, co
   uint64_t *acc_e2 = edep2 ? (uint64_t *)calloc(2 * nv, sizeof(uint64_t)) : NULL;
   if (n_threads < 1) n_threads = 1;
   if (batch == 0) batch = n ? n : 1;
+  {
+    /* the library's cap on histories per batch (gg_api.cu run_impl): the
+       fixed-point tallies cannot wrap, n <= 2^32 / E_max^2 and 2^32 / E_max */
+    double em = src->mono;
+    if (src->ene_type == GG_ENE_RANGE) em = src->e_hi;
+    else if (src->ene_type == GG_ENE_LINES || src->ene_type == GG_ENE_HISTOGRAM) {
+      const int ne = src->ene_type == GG_ENE_HISTOGRAM ? src->n_spec + 1 : src->n_spec;
+      em = src->spec_e[0];
+      for (int i = 1; i < ne; ++i)
+        if (src->spec_e[i] > em) em = src->spec_e[i];
+    }
+    em = (em > 1e-6 ? em : 1e-6) * 1.001;
+    double lim = 4294967296.0 / (em * em);
+    if (4294967296.0 / em < lim) lim = 4294967296.0 / em;
+    if ((double)batch > lim) batch = lim >= 1.0 ? (uint64_t)lim : 1;
+  }
   worker_t *ws = (worker_t *)calloc((size_t)n_threads, sizeof(worker_t));
   pthread_t *th = (pthread_t *)calloc((size_t)n_threads, sizeof(pthread_t));
   int status = GG_OK;
