@@ -412,6 +412,9 @@ def run_ours_spect(args, ws, rank, local, dist, use_cuda):
         r, ns, dt = spect_cpu_sample(scene, sp, threads, target_s=args.cpu_seconds)
         cpu = {"value": r, "unit": UNIT, "cores": threads, "kind": "port",
                "sample": f"{ns} primaries over the 60 positions, {dt:.1f} s on {threads} host threads"}
+    fp64 = None
+    if rank == 0 and args.fp64_primaries > 0:
+        fp64 = spect_fp64_error(scene, sp, max(1, args.fp64_primaries // sp.n_runs), args.seed, local, args.batch)
     if rank == 0:
         line = {
             "metric": SPECT_METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
@@ -423,6 +426,7 @@ def run_ours_spect(args, ws, rank, local, dist, use_cuda):
                        "parallelism": f"replicas x{ws}, disjoint history ranges"},
             "sigma": {"mean_relative_uncertainty_peak_window_gt10pct_max": sigma, "primaries": n,
                       "counts_peak_window": float(peak.sum())},
+            "fp64_error": fp64,
             "e2e": {"value": ws * n / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h)},
             "roofline": roofline,
@@ -593,6 +597,12 @@ def run_ours_ff(args, ws, rank, local, dist, use_cuda):
         cpu = {"value": r, "unit": UNIT, "cores": threads, "kind": "port",
                "sample": f"{ns} primaries through both passes over the {runs} positions, {dt:.1f} s on "
                          f"{threads} host threads"}
+    fp64 = None
+    if rank == 0 and args.fp64_primaries > 0:
+        npr = max(1, min(args.fp64_primaries, 10_000_000) // runs)
+        fp64 = {"primary_pass": spect_fp64_error(scene, sp_p, npr, args.seed, local, args.batch, weighted=True),
+                "scatter_pass": spect_fp64_error(scene, sp_s, max(1, npr // 10), args.seed, local, args.batch,
+                                                 weighted=True)}
     if rank == 0:
         line = {
             "metric": FF_METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
@@ -609,6 +619,7 @@ def run_ours_ff(args, ws, rank, local, dist, use_cuda):
                       "method": f"per (head, position) window totals; efficiency 1 / (sigma^2 T); primary "
                                 f"pass: history-by-history squares; scatter pass: variance of {FF_CHUNKS} "
                                 f"independent chunks; analog: Poisson"},
+            "fp64_error": fp64,
             "e2e": {"value": ws * n / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h)},
             "roofline": roofline,
@@ -724,6 +735,10 @@ def run_ours_arf(args, ws, rank, local, dist, use_cuda):
         eng.arf_projection(squared=True)
         e2e_t.append(time.perf_counter() - t1)
     e2e_s = dist_max(dist, float(np.mean(e2e_t)), use_cuda)
+    fp64 = None
+    if rank == 0 and args.fp64_primaries > 0:
+        fp64 = spect_fp64_error(scene, sp, max(1, args.fp64_primaries // sp.n_runs), args.seed, local,
+                                min(args.batch, 1 << 26), arf=(model, params))
     # the network's arithmetic: forward FLOP per scored photon
     flop_photon = 2.0 * (3 * 128 + 2 * 128 * 128 + 128 * 16)
     peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
@@ -748,6 +763,7 @@ def run_ours_arf(args, ws, rank, local, dist, use_cuda):
                 "note": "efficiency = 1 / (sigma^2 T), contrib/spect/spect_helpers.py:480-488, 582-591"},
             "training": {"seconds": train_s, "loss_first_last": [float(loss[0]), float(loss[-1])],
                          "epochs": args.arf_epochs},
+            "fp64_error": fp64,
             "e2e": {"value": ws * n / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h)},
             "roofline": {"bound": "hbm", "kernel": "k_spect_phantom<float> (phantom stage, dominant)",
@@ -880,10 +896,11 @@ def run_ours_batched(args, ws, rank, local, dist, use_cuda):
     return 0
 
 
-def fp64_error(scene, n, seed, device, batch):
+def fp64_error(scene, n, seed, device, batch, tle=None):
     """Dose images of n histories in the FP32 and the FP64 build of the same
     kernels (same seed, same histories) and the error of the first against the
-    second (opengate_gb300.dose.precision_error), with both builds' rates."""
+    second (opengate_gb300.dose.precision_error), with both builds' rates.
+    tle: (threshold, kill energy, database) of the track-length estimator."""
     import torch
     from opengate_gb300.dose import precision_error
     from opengate_gb300.engine import DoseEngine
@@ -891,6 +908,8 @@ def fp64_error(scene, n, seed, device, batch):
     imgs, rate = {}, {}
     for prec in (32, 64):
         with DoseEngine(scene, device=device, precision=prec, batch=batch) as e:
+            if tle is not None:
+                e.set_tle(*tle)
             e.run(n, seed, 0)
             torch.cuda.synchronize()
             tg, tt, tf, _ = e.last_kernel_ms()
@@ -899,6 +918,45 @@ def fp64_error(scene, n, seed, device, batch):
     err = precision_error(imgs[32][0], imgs[32][1], imgs[64][0], imgs[64][1], n)
     err.update({"primaries": n, "seed": seed, "voxels_gt": "10 % of max",
                 "rate_f32": rate[32], "rate_f64": rate[64]})
+    return err
+
+
+def spect_fp64_error(scene, sp, n_per_run, seed, device, batch, arf=None, weighted=False):
+    """Projections of the same histories from the FP32 and the FP64 build of the SPECT
+    kernels (same seed) and the error of the first against the second
+    (opengate_gb300.dose.precision_error over pixels > 10 % of max, per-pixel sigma
+    from the history-by-history squares): analog counts (squares = counts), free
+    flight (weights and their squares) or ARF detectors (tracked counts + network
+    weights; `arf` = (model, params))."""
+    import torch
+
+    from opengate_gb300.dose import precision_error
+    from opengate_gb300.engine import ArfNetwork, SpectEngine
+
+    imgs, rate = {}, {}
+    n = n_per_run * sp.n_runs
+    for prec in (32, 64):
+        with SpectEngine(scene, sp, device=device, precision=prec, batch=batch) as e:
+            if arf is not None:
+                ArfNetwork(e).set_model(*arf)
+                e.use_arf(True)
+                e.reset()
+            e.run(n_per_run, seed)
+            torch.cuda.synchronize()
+            tg, tt, tf, _ = e.last_kernel_ms()
+            rate[prec] = n / ((tg + tt + tf) / 1e3)
+            if weighted:
+                imgs[prec] = e.weighted_projection(squared=True)
+            elif arf is not None:
+                c = e.projection()
+                w, w2 = e.arf_projection(squared=True)
+                imgs[prec] = (c + w, c + w2)
+            else:
+                c = e.projection()
+                imgs[prec] = (c, c)
+    err = precision_error(imgs[32][0], imgs[32][1], imgs[64][0], imgs[64][1], n)
+    err.update({"primaries": n, "seed": seed, "pixels_gt": "10 % of max", "rate_f32": rate[32],
+                "rate_f64": rate[64]})
     return err
 
 
@@ -964,6 +1022,9 @@ def run_ours_tle(args, ws, rank, local, dist, use_cuda):
     ams, _ = timed(ana, args.steps, args.warmup)
     sig_a = mean_relative_uncertainty(ana.edep(), ana.edep_squared(), n)
     ana.close()
+    fp64 = None
+    if rank == 0 and args.fp64_primaries > 0:
+        fp64 = fp64_error(scene, min(n, args.fp64_primaries), args.seed, local, args.batch, tle=(np.inf, 0.0, "EPDL"))
     t_t, t_a = float(np.sum(ms)) / args.steps, float(np.sum(ams)) / args.steps
     gain = (sig_a ** 2 * t_a) / (sig_t ** 2 * t_t)
     peak, peak_kind = measured_peaks()
@@ -998,6 +1059,7 @@ def run_ours_tle(args, ws, rank, local, dist, use_cuda):
                               "analog_equivalent_primaries_per_s": value * gain,
                               "note": "efficiency = 1 / (sigma^2 T), sigma = mean relative uncertainty "
                                       "over voxels > 10 % of max"},
+            "fp64_error": fp64,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": None, "peak_kind": peak_kind, "kernel": "k_transport<float> (estimator)",
