@@ -84,6 +84,8 @@ extern "C" {
 /* images returned by gg_get_image */
 #define GG_IMG_EDEP 0
 #define GG_IMG_EDEP_SQUARED 1
+#define GG_IMG_DOSE 2          /* dose grid with score_dose: sum of edep / rho (MeV cm3 / g) */
+#define GG_IMG_DOSE_SQUARED 3  /* its history-by-history squares */
 
 /* counters returned by gg_get_counters (uint64 slots) */
 #define GG_CNT_HISTORIES 0
@@ -254,6 +256,24 @@ int gg_set_world(gg_ctx *ctx, const gg_world_desc *world);
 int gg_set_source(gg_ctx *ctx, const gg_source_desc *source);
 /* Enables the edep / edep-squared tally on the image grid and zeroes it. */
 int gg_add_dose_tally(gg_ctx *ctx, int32_t score_squared);
+/* Dose tally on a grid of its own (replaces the DoseActor placement of
+   GateDoseActor::BeginOfRunActionMasterThread + AttachImageToVolume and
+   GetVoxelPosition, core/opengate_core/opengate_lib/GateDoseActor.cpp:88-178,
+   GateHelpersImage.txx:20-58): dims voxels of `spacing`, outer corner
+   `corner` (world, mm), axis-aligned with the image.  A deposit in the
+   image is scored in the grid voxel of the interaction point, or not at all
+   outside the grid; score_dose adds the dose tally sum(edep / rho) of the
+   material at the point (GG_IMG_DOSE, GG_IMG_DOSE_SQUARED).  gg_get_image then
+   returns grid-sized images.  NULL or dims[0] = 0: back to the image grid.
+   Not with the track-length estimator or batched simulations. */
+typedef struct {
+  int32_t dims[3];
+  double spacing[3]; /* mm */
+  double corner[3];  /* mm, world position of the outer corner of voxel (0, 0, 0) */
+  int32_t score_dose;
+} gg_dose_grid_desc;
+int gg_set_dose_grid(gg_ctx *ctx, const gg_dose_grid_desc *grid);
+
 /* Selects the dose transport kernel (GG_KERNEL_*); no counterpart in the
    reference (Geant4 has one stepping loop). */
 int gg_set_transport_kernel(gg_ctx *ctx, int32_t kind);

@@ -29,7 +29,7 @@ GG_KERNEL_WAVEFRONT, GG_KERNEL_PHASED = 0, 1
 GG_POS_POINT, GG_POS_BOX, GG_POS_SPHERE, GG_POS_DISC, GG_POS_VOXELS = 0, 1, 2, 3, 4
 GG_DIR_ISO, GG_DIR_MOMENTUM, GG_DIR_FOCUSED = 0, 1, 2
 GG_ENE_MONO, GG_ENE_LINES, GG_ENE_HISTOGRAM, GG_ENE_RANGE = 0, 1, 2, 3
-GG_IMG_EDEP, GG_IMG_EDEP_SQUARED = 0, 1
+GG_IMG_EDEP, GG_IMG_EDEP_SQUARED, GG_IMG_DOSE, GG_IMG_DOSE_SQUARED = 0, 1, 2, 3
 GG_N_COUNTERS = 16
 COUNTER_NAMES = ["histories", "woodcock_steps", "real_interactions", "deposits", "tally_entries",
                  "list_overflows", "world_steps", "escaped", "skipped", "loop_capped",
@@ -78,6 +78,13 @@ class TleDesc(ctypes.Structure):
     _fields_ = [
         ("enabled", ctypes.c_int32), ("threshold_energy", ctypes.c_double), ("energy_min", ctypes.c_double),
         ("muen", _f32p),
+    ]
+
+
+class DoseGridDesc(ctypes.Structure):
+    _fields_ = [
+        ("dims", ctypes.c_int32 * 3), ("spacing", ctypes.c_double * 3), ("corner", ctypes.c_double * 3),
+        ("score_dose", ctypes.c_int32),
     ]
 
 
@@ -205,6 +212,7 @@ PROTOTYPES = [
     ("gg_run", ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64]),
     ("gg_synchronize", ctypes.c_int, [ctypes.c_void_p]),
     ("gg_set_transport_kernel", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
+    ("gg_set_dose_grid", ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(DoseGridDesc)]),
     ("gg_get_image", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, _f64p, ctypes.c_size_t]),
     ("gg_get_counters", ctypes.c_int, [ctypes.c_void_p, _u64p, ctypes.c_size_t]),
     ("gg_host_alloc", ctypes.c_void_p, [ctypes.c_size_t]),

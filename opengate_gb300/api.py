@@ -418,10 +418,50 @@ class DoseActor(GateObject):
             raise NotImplementedError("score_in other than 'material' is not supported")
         if self.hit_type not in ("random", "pre", "post", "middle"):
             raise ValueError(f"hit_type '{self.hit_type}'")
-        same = list(self.size) == list(image.size) and np.allclose(self.spacing, image.spacing) and \
+        if self.output_coordinate_system not in ("local", "global", "attached_to_image", None):
+            raise ValueError(f"Illegal parameter 'output_coordinate_system': {self.output_coordinate_system}")
+        if len(self.size) != 3 or min(int(v) for v in self.size) < 1 or min(float(v) for v in self.spacing) <= 0:
+            raise ValueError(f"DoseActor '{self.name}': size must be 3 positive integers, spacing > 0")
+
+    def on_image_grid(self, image):
+        """True when the dose grid is the image's own voxel grid."""
+        return list(self.size) == list(image.size) and np.allclose(self.spacing, image.spacing) and \
             np.allclose(self.translation, 0.0)
-        if not same:
-            raise NotImplementedError("the dose grid must be the image grid (size and spacing of the image)")
+
+    def scoring_grid(self, volume):
+        """(dims, spacing, corner) in mm of the scoring grid: centred on the attached image volume
+        plus `translation`, axis-aligned with it (GateDoseActor::BeginOfRunActionMasterThread ->
+        AttachImageToVolume, GateHelpersImage.txx:20-58; the actor's `rotation` only orients the
+        output images, as in the reference).  Deposits are scored at the interaction point: with
+        electrons stopped at creation the step of a deposit has no length, so the hit types
+        "random", "pre", "post" and "middle" all give that point."""
+        size = np.array([int(v) for v in self.size], dtype=np.int64)
+        sp = np.array([float(v) for v in self.spacing]) / u.mm
+        centre = np.asarray(volume.translation, dtype=np.float64) / u.mm + np.asarray(self.translation) / u.mm
+        return [int(v) for v in size], sp.tolist(), (centre - size * sp / 2.0).tolist()
+
+    def output_geometry(self, volume, image):
+        """(spacing, origin, direction) of the output images
+        (VoxelDepositActor._update_output_coordinate_system, doseactors.py:170-232)."""
+        from scipy.spatial.transform import Rotation
+
+        size = np.array([int(v) for v in self.size], dtype=np.float64)
+        sp = np.array([float(v) for v in self.spacing]) / u.mm
+        origin = -size * sp / 2.0 + sp / 2.0
+        rot = np.asarray(self.rotation, dtype=np.float64)
+        origin_local = Rotation.from_matrix(rot).apply(origin) + np.asarray(self.translation) / u.mm
+        cs = self.output_coordinate_system
+        if cs is None:
+            return sp, origin, np.eye(3)
+        if cs == "local":
+            return sp, origin_local, rot
+        if cs == "attached_to_image":
+            n_rot = np.asarray(image.direction, dtype=np.float64)
+            n_size = np.array(image.size, dtype=np.float64)
+            n_tr = np.asarray(image.origin) + Rotation.from_matrix(n_rot).apply((n_size - 1.0) * image.spacing / 2.0)
+            return sp, Rotation.from_matrix(n_rot).apply(origin_local) + n_tr, n_rot @ rot
+        # global: the attached image volume is an unrotated daughter of the world
+        return sp, origin_local + np.asarray(volume.translation, dtype=np.float64) / u.mm, rot
 
     @property
     def number_of_samples(self):
@@ -1167,6 +1207,12 @@ class Simulation:
         doses = [a for a in self.actors.values() if isinstance(a, DoseActor)]
         for a in doses:
             a.check(vol, hu)
+        grids = {None if a.on_image_grid(hu) else tuple(map(tuple, a.scoring_grid(vol))) for a in doses}
+        if len(grids) > 1:
+            raise NotImplementedError("dose actors of one simulation must share their dose grid")
+        grid = grids.pop() if grids else None
+        if grid is not None and any(isinstance(a, TLEDoseActor) for a in doses):
+            raise NotImplementedError("the TLEDoseActor scores on the image grid (size, spacing of the image)")
         if vol.dump_label_image:
             image_io.write_mhd(self.get_output_path(vol.dump_label_image),
                                image_io.Image(scene.labels, hu.spacing, hu.origin))
@@ -1180,6 +1226,8 @@ class Simulation:
             raise NotImplementedError("a TLEDoseActor cannot share the run with another dose actor")
         eng = DoseEngine(scene, device=self.device, precision=self.precision, batch=self.batch)
         try:
+            if grid is not None:
+                eng.set_dose_grid(*grid, score_dose=True)
             if tles:
                 eng.set_tle(tles[0].threshold_energy, float(tles[0].energy_min), tles[0].database)
             first = 0
@@ -1212,22 +1260,28 @@ class Simulation:
                                                               g.uncertainty_overshoot_factor_N_events), first + 1)
                     object.__setattr__(g, "_uncertainty_reached", unc)
             edep, edep2, cnt = eng.edep(), eng.edep_squared(), eng.counters()
+            if grid is not None:
+                dsum, dsum2 = eng.dose_sum(), eng.dose_sum_squared()
         finally:
             eng.close()
         elapsed = time.perf_counter() - t0
         n_events = first
         rho = scene.voxel_density()
         for a in doses:
-            origin = hu.origin if a.output_coordinate_system == "attached_to_image" else None
-            dose = D.edep_to_dose(edep, rho, hu.spacing)
-            dose2 = D.edep_to_dose(edep2, rho, hu.spacing, squared=True)
+            spacing, origin, direction = a.output_geometry(vol, hu)
+            if grid is None:
+                dose = D.edep_to_dose(edep, rho, hu.spacing)
+                dose2 = D.edep_to_dose(edep2, rho, hu.spacing, squared=True)
+            else:
+                dose = D.dose_sum_to_gy(dsum, grid[1])
+                dose2 = D.dose_sum_to_gy(dsum2, grid[1], squared=True)
             data = {"edep": edep, "edep_squared": edep2,
                     "edep_uncertainty": D.variance_or_uncertainty(edep, edep2, n_events, "uncertainty"),
                     "dose": dose, "dose_squared": dose2,
                     "dose_uncertainty": D.variance_or_uncertainty(dose, dose2, n_events, "uncertainty")}
             for key, arr in data.items():
                 out = getattr(a, key)
-                out.image = image_io.Image(arr, hu.spacing, origin)
+                out.image = image_io.Image(arr, spacing, origin, direction)
                 out.number_of_samples = n_events
                 if out.active and out.write_to_disk:
                     image_io.write_mhd(out.get_output_path(), out.image)

@@ -102,6 +102,15 @@ struct gg_ctx {
   unsigned long long *d_acc_e = nullptr, *d_acc_e2 = nullptr;
   double *d_edep = nullptr, *d_edep2 = nullptr;
   bool have_tally = false, squared = false;
+  // dose tally on a grid of its own (gg_set_dose_grid): voxels of the tally images (the image
+  // grid's n_vox when off), and the dose tally sum(edep * rho_min / rho)
+  size_t n_tally = 0;
+  bool dgrid_on = false, ddose = false;
+  int ddims[3] = {0, 0, 0};
+  double dspacing[3] = {0, 0, 0}, dcorner[3] = {0, 0, 0};
+  float drho_min = 1.0f;
+  unsigned long long *d_acc_d = nullptr, *d_acc_d2 = nullptr;
+  double *d_dose = nullptr, *d_dose2 = nullptr;
 
   // run bookkeeping
   unsigned long long *d_counters = nullptr, *d_next = nullptr;
@@ -230,6 +239,7 @@ struct gg_ctx {
     dfree(d_ray_x2);
     dfree(d_labels); dfree(d_maj); dfree(d_spec_e); dfree(d_spec_cdf); dfree(d_acc_box);
     dfree(d_acc_e); dfree(d_acc_e2); dfree(d_edep); dfree(d_edep2);
+    dfree(d_acc_d); dfree(d_acc_d2); dfree(d_dose); dfree(d_dose2);
     dfree(d_counters); dfree(d_next); dfree(d_status); dfree(d_records); dfree(d_cnt_save);
     dfree(d_split); dfree(d_split_n);
     dfree(d_queue[0]); dfree(d_queue[1]); dfree(d_queue[2]); dfree(d_qn);
@@ -286,6 +296,18 @@ struct gg_ctx {
       s.whalf[a] = (real)world.half_size[a];
     }
     s.muen = (tle && !have_spect && !have_batch) ? (const real *)d_muen : nullptr;
+    if (dgrid_on && !have_spect && !have_batch) {
+      s.dgrid = 1;
+      s.dnx = ddims[0];
+      s.dny = ddims[1];
+      s.dnz = ddims[2];
+      for (int a = 0; a < 3; ++a) {
+        s.dcorner[a] = (real)dcorner[a];
+        s.dinv_sp[a] = (real)(1.0 / dspacing[a]);
+      }
+      s.ddose = ddose ? 1 : 0;
+      s.drho_min = (real)drho_min;
+    }
     s.eblur = blur.energy_method;
     s.eb_sigma = (real)blur.energy_sigma;
     s.eb_res = (real)blur.energy_resolution;
@@ -615,6 +637,39 @@ static void drop_graph(gg_ctx *c) {
   c->graph = nullptr;
 }
 
+// (Re)allocates the tally images for the current tally grid: the dose grid
+// when set, else the image grid (only once a volume is there); the dose
+// tally only with gg_set_dose_grid(score_dose).
+static int tally_alloc(gg_ctx *c) {
+  size_t n = 0;
+  if (c->dgrid_on) n = (size_t)c->ddims[0] * c->ddims[1] * c->ddims[2];
+  else if (c->have_volume) n = c->n_vox;
+  if (n != c->n_tally) {
+    dfree(c->d_acc_e); dfree(c->d_acc_e2); dfree(c->d_edep); dfree(c->d_edep2);
+    dfree(c->d_acc_d); dfree(c->d_acc_d2); dfree(c->d_dose); dfree(c->d_dose2);
+    c->n_tally = n;
+  }
+  if (!n) return GG_OK;
+  int st;
+  if (!c->d_acc_e) {
+    if ((st = c->cuda(cudaMalloc(&c->d_acc_e, n * 8), "cudaMalloc tally"))) return st;
+    if ((st = c->cuda(cudaMalloc(&c->d_edep, n * 8), "cudaMalloc edep"))) return st;
+  }
+  if (c->squared && !c->d_acc_e2) {
+    if ((st = c->cuda(cudaMalloc(&c->d_acc_e2, n * 16), "cudaMalloc tally2"))) return st;  // 128-bit per voxel
+    if ((st = c->cuda(cudaMalloc(&c->d_edep2, n * 8), "cudaMalloc edep2"))) return st;
+  }
+  if (c->dgrid_on && c->ddose && !c->d_acc_d) {
+    if ((st = c->cuda(cudaMalloc(&c->d_acc_d, n * 8), "cudaMalloc dose tally"))) return st;
+    if ((st = c->cuda(cudaMalloc(&c->d_dose, n * 8), "cudaMalloc dose"))) return st;
+  }
+  if (c->dgrid_on && c->ddose && c->squared && !c->d_acc_d2) {
+    if ((st = c->cuda(cudaMalloc(&c->d_acc_d2, n * 16), "cudaMalloc dose tally2"))) return st;
+    if ((st = c->cuda(cudaMalloc(&c->d_dose2, n * 8), "cudaMalloc dose2"))) return st;
+  }
+  return GG_OK;
+}
+
 extern "C" {
 
 int gg_create(const gg_device_opts *opts, gg_ctx **out) {
@@ -746,8 +801,9 @@ int gg_upload_volume(gg_ctx *c, const gg_volume_desc *v) {
                     "cudaMemcpy labels")))
     return st;
   if ((st = c->upload_real(c->d_maj, v->majorant, (size_t)c->n_e))) return st;
-  if (n != c->n_vox) {
+  if (n != c->n_vox && !c->dgrid_on) {
     dfree(c->d_acc_e); dfree(c->d_acc_e2); dfree(c->d_edep); dfree(c->d_edep2);
+    c->n_tally = 0;
     c->have_tally = false;
   }
   for (int a = 0; a < 3; ++a) {
@@ -816,19 +872,45 @@ int gg_add_dose_tally(gg_ctx *c, int32_t score_squared) {
   if (!c) return GG_ERR_ARG;
   cudaSetDevice(c->device);
   if (!c->have_volume) return c->fail(GG_ERR_STATE, "gg_add_dose_tally: upload the volume first");
-  int st;
-  size_t n = c->n_vox;
-  if (!c->d_acc_e) {
-    if ((st = c->cuda(cudaMalloc(&c->d_acc_e, n * 8), "cudaMalloc tally"))) return st;
-    if ((st = c->cuda(cudaMalloc(&c->d_edep, n * 8), "cudaMalloc edep"))) return st;
-  }
-  if (score_squared && !c->d_acc_e2) {
-    if ((st = c->cuda(cudaMalloc(&c->d_acc_e2, n * 16), "cudaMalloc tally2"))) return st;  // 128-bit per voxel
-    if ((st = c->cuda(cudaMalloc(&c->d_edep2, n * 8), "cudaMalloc edep2"))) return st;
-  }
   c->squared = score_squared != 0;
+  int st = tally_alloc(c);
+  if (st) return st;
   c->have_tally = true;
   return gg_reset_tally(c);
+}
+
+int gg_set_dose_grid(gg_ctx *c, const gg_dose_grid_desc *d) {
+  if (!c) return GG_ERR_ARG;
+  cudaSetDevice(c->device);
+  if (!c->have_tables) return c->fail(GG_ERR_STATE, "gg_set_dose_grid: upload the tables first");
+  if (c->have_batch || c->have_spect)
+    return c->fail(GG_ERR_STATE, "gg_set_dose_grid: dose grids are for single dose simulations");
+  if (!d || d->dims[0] == 0) {
+    c->dgrid_on = false;
+    c->ddose = false;
+  } else {
+    char msg[160];
+    size_t n = 0;
+    if (gg::check_dims(d->dims, (size_t)UINT32_MAX - 1, &n, msg, sizeof(msg)))
+      return c->fail(GG_ERR_ARG, "gg_set_dose_grid: %s", msg);
+    for (int a = 0; a < 3; ++a)
+      if (!(d->spacing[a] > 0) || !std::isfinite(d->spacing[a]) || !std::isfinite(d->corner[a]))
+        return c->fail(GG_ERR_ARG, "gg_set_dose_grid: spacing must be finite and > 0, corner finite");
+    c->dgrid_on = true;
+    c->ddose = d->score_dose != 0;
+    for (int a = 0; a < 3; ++a) {
+      c->ddims[a] = d->dims[a];
+      c->dspacing[a] = d->spacing[a];
+      c->dcorner[a] = d->corner[a];
+    }
+    float rmin = c->h_mat_rho.empty() ? 1.0f : c->h_mat_rho[0];
+    for (float r : c->h_mat_rho) rmin = std::min(rmin, r);
+    c->drho_min = rmin;
+  }
+  int st = tally_alloc(c);
+  if (st) return st;
+  c->have_tally = c->d_acc_e != nullptr;
+  return c->have_tally ? gg_reset_tally(c) : GG_OK;
 }
 
 int gg_spect_set_blur(gg_ctx *c, const gg_blur_desc *b) {
@@ -876,13 +958,21 @@ int gg_reset_tally(gg_ctx *c) {
   if (!c) return GG_ERR_ARG;
   if (!c->have_tally) return c->fail(GG_ERR_STATE, "gg_reset_tally: no tally");
   cudaSetDevice(c->device);
-  size_t n = c->n_vox;
+  size_t n = c->n_tally;
   int st;
   if ((st = c->cuda(cudaMemsetAsync(c->d_acc_e, 0, n * 8, c->stream), "memset"))) return st;
   if ((st = c->cuda(cudaMemsetAsync(c->d_edep, 0, n * 8, c->stream), "memset"))) return st;
   if (c->d_acc_e2) {
     if ((st = c->cuda(cudaMemsetAsync(c->d_acc_e2, 0, n * 16, c->stream), "memset"))) return st;
     if ((st = c->cuda(cudaMemsetAsync(c->d_edep2, 0, n * 8, c->stream), "memset"))) return st;
+  }
+  if (c->d_acc_d) {
+    if ((st = c->cuda(cudaMemsetAsync(c->d_acc_d, 0, n * 8, c->stream), "memset"))) return st;
+    if ((st = c->cuda(cudaMemsetAsync(c->d_dose, 0, n * 8, c->stream), "memset"))) return st;
+  }
+  if (c->d_acc_d2) {
+    if ((st = c->cuda(cudaMemsetAsync(c->d_acc_d2, 0, n * 16, c->stream), "memset"))) return st;
+    if ((st = c->cuda(cudaMemsetAsync(c->d_dose2, 0, n * 8, c->stream), "memset"))) return st;
   }
   if ((st = c->cuda(cudaMemsetAsync(c->d_counters, 0, GG_N_COUNTERS * 8, c->stream), "memset"))) return st;
   return c->cuda(cudaMemsetAsync(c->d_status, 0, sizeof(unsigned int), c->stream), "memset");
@@ -1112,7 +1202,10 @@ static int run_impl(gg_ctx *c, uint64_t n, uint64_t seed, uint64_t first, bool c
   }
   int grid = c->n_sm * bps;
   // the compacted wavefront kernel: single dose simulations with analog scoring
-  const bool wave = !c->have_spect && !c->tle && !c->have_batch && c->transport_kernel == GG_KERNEL_WAVEFRONT;
+  if (c->dgrid_on && c->tle && !c->have_spect && !c->have_batch)
+    return c->fail(GG_ERR_STATE, "gg_run: the track-length estimator scores on the image grid (no dose grid)");
+  const bool wave = !c->have_spect && !c->tle && !c->have_batch && !c->dgrid_on &&
+                    c->transport_kernel == GG_KERNEL_WAVEFRONT;
   size_t wsmem = 0;
   int wgrid = 0, wminb = c->precision == GG_PREC_F64 ? 2 : 3;
   if (wave) {
@@ -1186,6 +1279,9 @@ static int run_impl(gg_ctx *c, uint64_t n, uint64_t seed, uint64_t first, bool c
   a.next = c->d_next;
   a.acc_e = c->d_acc_e;
   a.acc_e2 = c->squared ? c->d_acc_e2 : nullptr;
+  const bool dg = c->dgrid_on && !c->have_spect && !c->have_batch;
+  a.acc_d = dg && c->ddose ? c->d_acc_d : nullptr;
+  a.acc_d2 = dg && c->ddose && c->squared ? c->d_acc_d2 : nullptr;
   a.counters = c->d_counters;
   a.status = c->d_status;
   a.chunk = c->chunk;
@@ -1226,8 +1322,13 @@ static int run_impl(gg_ctx *c, uint64_t n, uint64_t seed, uint64_t first, bool c
     if (!capturing && (st = c->cuda(cudaEventRecord(c->ev[3 * b + 2], c->stream), "event"))) return st;
     if (c->have_tally &&
         (st = c->cuda(gg::launch_flush(c->d_acc_e, a.acc_e2, c->d_edep, c->squared ? c->d_edep2 : nullptr,
-                                       c->n_vox, flush_grid, c->stream),
+                                       c->n_tally, flush_grid, c->stream),
                       "flush launch")))
+      return st;
+    if (a.acc_d &&
+        (st = c->cuda(gg::launch_flush(a.acc_d, a.acc_d2, c->d_dose, a.acc_d2 ? c->d_dose2 : nullptr, c->n_tally,
+                                       flush_grid, c->stream, 1.0 / (double)c->drho_min),
+                      "dose flush launch")))
       return st;
   }
   if (capturing) return GG_OK;
@@ -1302,10 +1403,13 @@ int gg_get_image(gg_ctx *c, int32_t which, double *out, size_t n) {
   if (!c || !out) return GG_ERR_ARG;
   cudaSetDevice(c->device);
   if (!c->have_tally) return c->fail(GG_ERR_STATE, "gg_get_image: no tally");
-  if (n != c->n_vox) return c->fail(GG_ERR_ARG, "gg_get_image: buffer has %zu voxels, image %zu", n, c->n_vox);
+  if (n != c->n_tally)
+    return c->fail(GG_ERR_ARG, "gg_get_image: buffer has %zu voxels, image %zu", n, c->n_tally);
   double *src = nullptr;
   if (which == GG_IMG_EDEP) src = c->d_edep;
   else if (which == GG_IMG_EDEP_SQUARED) src = c->squared ? c->d_edep2 : nullptr;
+  else if (which == GG_IMG_DOSE) src = c->dgrid_on && c->ddose ? c->d_dose : nullptr;
+  else if (which == GG_IMG_DOSE_SQUARED) src = c->dgrid_on && c->ddose && c->squared ? c->d_dose2 : nullptr;
   if (!src) return c->fail(GG_ERR_ARG, "gg_get_image: image %d not scored", which);
   int st = c->cuda(cudaMemcpyAsync(out, src, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream), "download");
   if (st) return st;
@@ -1791,6 +1895,7 @@ int gg_batch_setup(gg_ctx *c, const gg_sim_desc *sims, int32_t n) {
   if (!c->have_tables || !c->have_world)
     return c->fail(GG_ERR_STATE, "gg_batch_setup: upload the tables and set the world first");
   if (c->have_spect) return c->fail(GG_ERR_STATE, "gg_batch_setup: SPECT heads are set up on this context");
+  if (c->dgrid_on) return c->fail(GG_ERR_STATE, "gg_batch_setup: a dose grid is set on this context");
   std::vector<uint64_t> off(n), nv(n);
   uint64_t total = 0, hist = 0;
   double emax = 0;

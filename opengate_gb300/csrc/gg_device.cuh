@@ -440,6 +440,12 @@ struct Scene {
   // density [n_comp][n_e], scored-photon energy threshold, kill energy
   const real *muen;
   real tle_thr, tle_emin;
+  // dose tally on a grid of its own (dgrid 1; DoseActor size / spacing /
+  // translation other than the image's): axis-aligned with the image box,
+  // the voxel of a point p is floor((p - dcorner) * dinv_sp) when inside the
+  // grid; ddose 1: also the dose tally sum(edep * drho_min / rho)
+  int dgrid, dnx, dny, dnz, ddose;
+  real dcorner[3], dinv_sp[3], drho_min;
   // batched simulations (n_sims > 0: labels is the concatenation of their
   // images, sim_maj their majorants [n_sims][n_e])
   const SimDesc<real> *sims;

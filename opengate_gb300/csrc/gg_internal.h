@@ -42,6 +42,8 @@ struct KernelArgs {
   uint64_t rec_first;               // history of record 0 (<= h_begin; a SPECT pass can start later)
   int refill_min;                   // lanes that must wait for a history before a refill phase
   int interact_min;                 // pending collisions that trigger an interaction phase
+  unsigned long long *acc_d;        // dose grid: fixed-point sum(edep * rho_min / rho) (or null)
+  unsigned long long *acc_d2;       // its history-by-history squares (or null)
 };
 
 // Bit of the kernel status word set when a stage queue overflowed (the low
@@ -184,7 +186,8 @@ cudaError_t launch_wavefront(const Scene<real> &s, const KernelArgs &a, int grid
                              cudaStream_t st);
 template <typename real>
 cudaError_t wavefront_occupancy(size_t smem, int minb, int *blocks_per_sm);
+// image += fixed point * 2^-32 * scale (squares: * scale^2), then clears the fixed-point sums
 cudaError_t launch_flush(unsigned long long *acc_e, unsigned long long *acc_e2, double *edep, double *edep2,
-                         size_t n, int grid, cudaStream_t st);
+                         size_t n, int grid, cudaStream_t st, double scale = 1.0);
 
 }  // namespace gg

@@ -77,7 +77,7 @@ __device__ __forceinline__ void hlist_flush_warp(HistList<real> &l, bool has, co
     const uint32_t v = valid ? l.vox[k] : 0u;
     const unsigned long long q = valid ? (unsigned long long)to_fixed(l.acc[k]) : 0ull;
     const unsigned long long lo = q * q;
-    const unsigned long long hi = __umulhi(q, q);
+    const unsigned long long hi = __umul64hi(q, q);
     const unsigned long long e2lo = lo & 0xffffffffull, e2hi = (hi << 32) | (lo >> 32);
     // grouped by tally address (batched simulations bind different tallies per lane)
     const unsigned long long addr = valid ? (unsigned long long)(uintptr_t)(t.acc_e + v) : ~0ull;
@@ -993,6 +993,52 @@ __device__ __forceinline__ int do_interaction(const Scene<real> &s, Photon<real>
       if (ph.head == 0) event_add<real, 0>(s, ev, ph, ed);
       else event_add<real, 1>(s, ev, ph, ed);
     }
+  }
+  return ph.alive ? kFly : kRefill;
+}
+
+// Voxel of point p in the dose grid (Scene::dgrid); false outside the grid.
+template <typename real>
+__device__ __forceinline__ bool dose_voxel(const Scene<real> &s, const real p[3], uint32_t &v) {
+  real f[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    real d = p[a] - s.dcorner[a];
+    f[a] = d * s.dinv_sp[a];
+  }
+  if (!(f[0] >= R<real>(0)) || !(f[1] >= R<real>(0)) || !(f[2] >= R<real>(0))) return false;
+  if (!(f[0] < (real)s.dnx) || !(f[1] < (real)s.dny) || !(f[2] < (real)s.dnz)) return false;
+  int ix = (int)f[0], iy = (int)f[1], iz = (int)f[2];
+  if (ix >= s.dnx || iy >= s.dny || iz >= s.dnz) return false;
+  v = (uint32_t)ix + (uint32_t)s.dnx * ((uint32_t)iy + (uint32_t)s.dny * (uint32_t)iz);
+  return true;
+}
+
+// do_interaction of the dose path with the tally on its own grid
+// (GateDoseActor::SteppingAction, GateDoseActor.cpp:180-243: the deposit is
+// scored in the dose-grid voxel of the interaction point, when there is one;
+// DG 2: also edep * rho_min / rho of the material there in the dose list ld).
+template <typename real, int DG>
+__device__ __forceinline__ int do_interaction_grid(const Scene<real> &s, Photon<real> &ph, Rng &g, BlockCounters *bc,
+                                                   int pmat, int pscored, HistList<real> &l, HistList<real> &ld,
+                                                   const Tally<real> &t, const Tally<real> &td,
+                                                   Secondary<real> &sec, unsigned int &n_dep, BlockCounters *bcd) {
+  const real ed = interact(s, ph, pmat, g, bc, sec);
+  if (pscored == 1) {
+    uint32_t dv;
+    if (dose_voxel(s, ph.pos, dv)) {
+      deposit(l, t, bc, dv, ed, n_dep);
+      if constexpr (DG == 2) {
+        real dd = ed * s.drho_min;
+        dd = dd / s.mat_rho[pmat];
+        unsigned int nd = 0;
+        deposit(ld, td, bcd, dv, dd, nd);
+      }
+    }
+    if (ph.alive && ph.in_image) ph.t_exit = exit_distance(ph.pos, ph.dir, s.bmin, s.bmax);
+  } else if (pscored == 0) {
+    ph.can_enter = 1;
+    ph.exclude = -1;
   }
   return ph.alive ? kFly : kRefill;
 }

@@ -181,10 +181,12 @@ __global__ void __launch_bounds__(256) k_generate(Scene<real> s, KernelArgs a) {
 // unchanged.
 // MINB = resident blocks per SM the register budget is sized for.
 // SPECT selects the head transport and projection scoring instead of the dose tally.
-template <typename real, int MINB, bool SPECT, bool MULTI, bool TLE>
+// DG: dose tally on a grid of its own (1: edep, 2: edep and dose), Scene::dgrid.
+template <typename real, int MINB, bool SPECT, bool MULTI, bool TLE, int DG = 0>
 __global__ void __launch_bounds__(256, MINB) k_transport(Scene<real> sg, KernelArgs args) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ BlockCounters bc;
+  __shared__ BlockCounters bcd;  // counts of the dose list (DG 2), not reported
   __shared__ real sec_store[6 * 256];
   // ---- stage tables in shared memory --------------------------------------
   Scene<real> s = sg;
@@ -210,6 +212,10 @@ __global__ void __launch_bounds__(256, MINB) k_transport(Scene<real> sg, KernelA
   }
   const Records<real> rec = Records<real>::carve(args.records, args.rec_cap);
   Tally<real> t{args.acc_e, args.acc_e2};
+  const Tally<real> td{args.acc_d, args.acc_d2};
+  if constexpr (DG == 2) {
+    if (threadIdx.x == 0) bcd = BlockCounters{0, 0, 0, 0, 0, 0, 0, 0};
+  }
   const unsigned lane = threadIdx.x & 31u;
   const unsigned lt_mask = (1u << lane) - 1u;
   const uint64_t n_hist = args.h_end - args.h_begin;
@@ -225,6 +231,8 @@ __global__ void __launch_bounds__(256, MINB) k_transport(Scene<real> sg, KernelA
   sec.has = 0;
   HistList<real> l;
   l.n = 0;
+  HistList<real> ld;  // dose list of the history (DG 2): same voxels as l
+  ld.n = 0;
   Event<real> ev;
   ev.clear();
   Rng g;
@@ -256,6 +264,7 @@ __global__ void __launch_bounds__(256, MINB) k_transport(Scene<real> sg, KernelA
         // every lane of the warp is here: same-voxel entries of the ending histories are summed
         // across the warp before their atomics
         hlist_flush_warp(l, need && in_hist, t, &bc);
+        if constexpr (DG == 2) hlist_flush_warp(ld, need && in_hist, td, &bcd);
       }
       if (need) in_hist = false;
       const unsigned n_need = __popc(m_ref);
@@ -341,7 +350,10 @@ __global__ void __launch_bounds__(256, MINB) k_transport(Scene<real> sg, KernelA
       }
     } else if (phase == kInteract) {
       if (state == kInteract) {
-        state = do_interaction<real, SPECT, TLE>(s, ph, g, &bc, pmat, pv, pscored, l, t, sec, n_dep, ev);
+        if constexpr (DG > 0)
+          state = do_interaction_grid<real, DG>(s, ph, g, &bc, pmat, pscored, l, ld, t, td, sec, n_dep, &bcd);
+        else
+          state = do_interaction<real, SPECT, TLE>(s, ph, g, &bc, pmat, pv, pscored, l, t, sec, n_dep, ev);
         if (state == kRefill && sec.has) {
           pop_secondary(s, ph, sec);
           state = kFly;
@@ -384,13 +396,17 @@ __global__ void __launch_bounds__(256, MINB) k_transport(Scene<real> sg, KernelA
 }
 
 // Adds the per-batch fixed-point sums into the float64 images and clears them.
+// scale multiplies the sums (1 for edep; 1 / rho_min for the dose tally, whose
+// entries are edep * rho_min / rho), scale2 = scale^2 their squares.
 __global__ void k_flush(unsigned long long *acc_e, unsigned long long *acc_e2, double *edep, double *edep2,
-                        size_t n) {
+                        size_t n, double scale, double scale2) {
   size_t stride = (size_t)gridDim.x * blockDim.x;
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
     unsigned long long a = acc_e[i];
     if (a) {
-      edep[i] += (double)a * 2.3283064365386963e-10;
+      double v = (double)a * 2.3283064365386963e-10;
+      v = v * scale;
+      edep[i] += v;
       acc_e[i] = 0ull;
     }
     if (acc_e2) {
@@ -400,7 +416,9 @@ __global__ void k_flush(unsigned long long *acc_e, unsigned long long *acc_e2, d
         lo = lo * 5.421010862427522e-20;  // 2^-64
         double hi = (double)b.y;
         hi = hi * 2.3283064365386963e-10;  // 2^-32
-        edep2[i] += hi + lo;
+        double v = hi + lo;
+        v = v * scale2;
+        edep2[i] += v;
         reinterpret_cast<ulonglong2 *>(acc_e2)[i] = make_ulonglong2(0ull, 0ull);
       }
     }
@@ -427,13 +445,13 @@ cudaError_t launch_generate(const Scene<real> &s, const KernelArgs &a, cudaStrea
   return cudaGetLastError();
 }
 
-template <typename real, int MINB, bool MULTI, bool TLE = false>
+template <typename real, int MINB, bool MULTI, bool TLE = false, int DG = 0>
 static cudaError_t launch_transport_v(const Scene<real> &s, const KernelArgs &a, int grid, int block, size_t smem,
                                       cudaStream_t st) {
   static unsigned long long configured = 0;
-  cudaError_t e = configure_smem(k_transport<real, MINB, false, MULTI, TLE>, 200 * 1024, configured);
+  cudaError_t e = configure_smem(k_transport<real, MINB, false, MULTI, TLE, DG>, 200 * 1024, configured);
   if (e != cudaSuccess) return e;
-  k_transport<real, MINB, false, MULTI, TLE><<<grid, block, smem, st>>>(s, a);
+  k_transport<real, MINB, false, MULTI, TLE, DG><<<grid, block, smem, st>>>(s, a);
   return cudaGetLastError();
 }
 
@@ -442,6 +460,18 @@ cudaError_t launch_transport(const Scene<real> &s, const KernelArgs &a, int grid
                              int minb, cudaStream_t st) {
   // SPECT runs use the two-stage kernels of gg_spect.cu
   if (s.spect) return cudaErrorInvalidValue;
+  if (s.dgrid) {
+    // dose grid of its own (single simulations, analog scoring)
+    if (s.muen || s.n_sims > 0) return cudaErrorInvalidValue;
+    if (s.ddose) {
+      if (minb <= 2) return launch_transport_v<real, 2, false, false, 2>(s, a, grid, block, smem, st);
+      if (minb == 3) return launch_transport_v<real, 3, false, false, 2>(s, a, grid, block, smem, st);
+      return launch_transport_v<real, 4, false, false, 2>(s, a, grid, block, smem, st);
+    }
+    if (minb <= 2) return launch_transport_v<real, 2, false, false, 1>(s, a, grid, block, smem, st);
+    if (minb == 3) return launch_transport_v<real, 3, false, false, 1>(s, a, grid, block, smem, st);
+    return launch_transport_v<real, 4, false, false, 1>(s, a, grid, block, smem, st);
+  }
   if (s.muen) {
     // track-length estimator (single simulations only)
     if (s.n_sims > 0) return cudaErrorInvalidValue;
@@ -460,8 +490,8 @@ cudaError_t launch_transport(const Scene<real> &s, const KernelArgs &a, int grid
 }
 
 cudaError_t launch_flush(unsigned long long *acc_e, unsigned long long *acc_e2, double *edep, double *edep2,
-                         size_t n, int grid, cudaStream_t st) {
-  k_flush<<<grid, 256, 0, st>>>(acc_e, acc_e2, edep, edep2, n);
+                         size_t n, int grid, cudaStream_t st, double scale) {
+  k_flush<<<grid, 256, 0, st>>>(acc_e, acc_e2, edep, edep2, n, scale, scale * scale);
   return cudaGetLastError();
 }
 

@@ -57,6 +57,14 @@ def edep_to_dose(edep, density_g_cm3, spacing_mm, squared=False):
     return out
 
 
+def dose_sum_to_gy(dose_sum, spacing_mm, squared=False):
+    """Dose image in Gy from the dose tally sum(edep / rho) in MeV cm3 / g of a dose grid
+    (every deposit divided by the density where it happened, GateDoseActor.cpp:206-217),
+    divided by the voxel volume (doseactors.py:686-696; squared for the squared image)."""
+    scale = MEV_J / (spacing_mm[0] * spacing_mm[1] * spacing_mm[2] * 1e-6)
+    return np.asarray(dose_sum, dtype=np.float64) * (scale * scale if squared else scale)
+
+
 def mean_relative_uncertainty(edep, edep2, n, threshold=0.1):
     """Mean relative uncertainty over voxels with edep above threshold * max."""
     unc = variance_or_uncertainty(edep, edep2, n, "uncertainty")

@@ -65,15 +65,44 @@ class DoseEngine:
     def run(self, n, seed, first=0):
         self._call("gg_run", ctypes.c_uint64(n), ctypes.c_uint64(seed), ctypes.c_uint64(first))
 
+    def set_dose_grid(self, dims, spacing, corner, score_dose=True):
+        """Dose tally on a grid of its own (gg_set_dose_grid): dims (nx, ny, nz), spacing and
+        outer corner in mm (world); None: back to the image grid."""
+        if dims is None:
+            self._grid = None
+            self._call("gg_set_dose_grid", None)
+            return
+        d = C.DoseGridDesc()
+        d.dims[:] = [int(v) for v in dims]
+        d.spacing[:] = [float(v) for v in spacing]
+        d.corner[:] = [float(v) for v in corner]
+        d.score_dose = 1 if score_dose else 0
+        self._call("gg_set_dose_grid", ctypes.byref(d))
+        self._grid = (int(dims[2]), int(dims[1]), int(dims[0]))
+
+    def image_shape(self):
+        """[nz][ny][nx] of the tally images: the dose grid's when set, else the image's."""
+        return getattr(self, "_grid", None) or self.scene.labels.shape
+
     def image(self, which, out=None):
         """Image `which` [nz][ny][nx] (float64); into `out` when given (e.g. a pinned_empty
         buffer, reused between calls: the copy then runs at the link's DMA rate)."""
+        shape = self.image_shape()
+        n = int(np.prod(shape))
         if out is None:
-            out = np.empty(self.scene.labels.shape, dtype=np.float64)
-        if out.dtype != np.float64 or out.size != self.scene.n_voxels or not out.flags.c_contiguous:
+            out = np.empty(shape, dtype=np.float64)
+        if out.dtype != np.float64 or out.size != n or not out.flags.c_contiguous:
             raise ValueError("out must be a C-contiguous float64 array of the image's size")
         self._call("gg_get_image", which, C.ptr(out, ctypes.c_double), out.size)
-        return out.reshape(self.scene.labels.shape)
+        return out.reshape(shape)
+
+    def dose_sum(self):
+        """Dose grid: sum of edep / rho per voxel (MeV cm3 / g), the DoseActor's dose before the
+        division by the voxel volume."""
+        return self.image(C.GG_IMG_DOSE)
+
+    def dose_sum_squared(self):
+        return self.image(C.GG_IMG_DOSE_SQUARED)
 
     def edep(self, out=None):
         return self.image(C.GG_IMG_EDEP, out)

@@ -4,8 +4,8 @@ The reference reads CT images and writes actor outputs through ITK, whose
 default format for this path is MetaImage (opengate/image.py, actor outputs
 ``*_edep.mhd`` etc.).  Only what the path needs is supported: 3D scalar
 images, ElementType MET_SHORT / MET_USHORT / MET_UCHAR / MET_FLOAT /
-MET_DOUBLE / MET_INT, little endian, identity direction, raw data in a
-separate file (or LOCAL).  Arrays are returned in numpy [z][y][x] order as
+MET_DOUBLE / MET_INT, little endian, a direction matrix (TransformMatrix,
+the ITK direction cosines), raw data in a separate file (or LOCAL).  Arrays are returned in numpy [z][y][x] order as
 ITK's GetArrayFromImage does; ``origin`` is the centre of the first voxel.
 """
 
@@ -23,8 +23,9 @@ _NAMES = {np.dtype(v): k for k, v in _TYPES.items()}
 class Image:
     """A 3D image: ``array`` [z][y][x], ``spacing`` and ``origin`` in mm (x, y, z)."""
 
-    def __init__(self, array, spacing=(1.0, 1.0, 1.0), origin=None):
+    def __init__(self, array, spacing=(1.0, 1.0, 1.0), origin=None, direction=None):
         self.array = np.asarray(array)
+        self.direction = np.eye(3) if direction is None else np.asarray(direction, dtype=np.float64).reshape(3, 3)
         if self.array.ndim != 3:
             raise ValueError("only 3D images are supported")
         self.spacing = np.asarray(spacing, dtype=np.float64)
@@ -67,7 +68,10 @@ def read_mhd(path):
         data = np.fromfile(path.parent / df, dtype=dtype, count=n)
     if data.size != n:
         raise ValueError(f"{path}: expected {n} elements, found {data.size}")
-    return Image(data.reshape(dims[2], dims[1], dims[0]).copy(), spacing, origin)
+    tm = [float(x) for x in header.get("TransformMatrix", "1 0 0 0 1 0 0 0 1").split()]
+    # MetaImage stores the direction column by column (ITK's writer)
+    direction = np.array(tm, dtype=np.float64).reshape(3, 3).T
+    return Image(data.reshape(dims[2], dims[1], dims[0]).copy(), spacing, origin, direction)
 
 
 def write_mhd(path, image):
@@ -81,7 +85,8 @@ def write_mhd(path, image):
     nx, ny, nz = image.size
     lines = [
         "ObjectType = Image", "NDims = 3", "BinaryData = True", "BinaryDataByteOrderMSB = False",
-        "CompressedData = False", "TransformMatrix = 1 0 0 0 1 0 0 0 1",
+        "CompressedData = False",
+        "TransformMatrix = " + " ".join(repr(float(v)) for v in np.asarray(image.direction).T.ravel()),
         "Offset = " + " ".join(repr(float(v)) for v in image.origin), "CenterOfRotation = 0 0 0",
         "AnatomicalOrientation = RAI",
         "ElementSpacing = " + " ".join(repr(float(v)) for v in image.spacing),

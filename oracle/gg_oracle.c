@@ -391,6 +391,9 @@ typedef struct {
   real bmin[3], bmax[3], inv_sp[3], sp[3];
   const uint16_t *labels;
   real *maj;
+  /* dose tally on a grid of its own (gg_set_dose_grid): dgrid = 0 off */
+  int dgrid, dnx, dny, dnz, ddose;
+  real dcorner[3], dinv_sp[3], drho_min;
   /* track-length estimator (GateTLEDoseActor): tle = 0 off */
   int tle;
   real tle_thr, tle_emin;
@@ -499,16 +502,20 @@ static real entry_distance(const real p[3], const real d[3], const real lo[3], c
 /* History state and tally                                                   */
 /* ------------------------------------------------------------------------ */
 typedef struct {
-  uint64_t *acc_e, *acc_e2; /* shared per batch, updated with atomics */
-  uint64_t cnt[GG_N_COUNTERS];
-  uint32_t ss_next; /* scatter splitting: copies of the current history so far */
-} tally_t;
-
-typedef struct {
   uint32_t vox[HIST_LIST];
   real acc[HIST_LIST];
   int n;
 } hlist_t;
+
+typedef struct {
+  uint64_t *acc_e, *acc_e2; /* shared per batch, updated with atomics */
+  uint64_t cnt[GG_N_COUNTERS];
+  uint32_t ss_next; /* scatter splitting: copies of the current history so far */
+  /* dose grid with the dose tally: sum(edep rho_min / rho), its squares, and
+     the history's dose list (same voxels as its edep list) */
+  uint64_t *acc_d, *acc_d2;
+  hlist_t *ld;
+} tally_t;
 
 static uint64_t to_fixed(real v) {
   /* v * 2^32 is exact; round to nearest even */
@@ -535,6 +542,36 @@ static void hlist_flush(hlist_t *l, tally_t *t) {
   }
   t->cnt[GG_CNT_TALLY_ENTRIES] += (uint64_t)l->n;
   l->n = 0;
+}
+
+/* The dose list of a history: flushed and filled like the edep list, into
+   acc_d / acc_d2, without counting (the counters describe the edep list). */
+static void dose_flush(hlist_t *l, tally_t *t) {
+  for (int k = 0; k < l->n; ++k) {
+    uint64_t q = to_fixed(l->acc[k]);
+    size_t v = l->vox[k];
+    __atomic_fetch_add(&t->acc_d[v], q, __ATOMIC_RELAXED);
+    if (t->acc_d2) {
+      unsigned __int128 sq = (unsigned __int128)q * q;
+      __atomic_fetch_add(&t->acc_d2[2 * v], (uint64_t)sq & 0xffffffffu, __ATOMIC_RELAXED);
+      __atomic_fetch_add(&t->acc_d2[2 * v + 1], (uint64_t)(sq >> 32), __ATOMIC_RELAXED);
+    }
+  }
+  l->n = 0;
+}
+
+static void dose_deposit(hlist_t *l, tally_t *t, uint32_t v, real e) {
+  if (!(e > R(0))) return;
+  for (int k = 0; k < l->n; ++k) {
+    if (l->vox[k] == v) {
+      l->acc[k] = l->acc[k] + e;
+      return;
+    }
+  }
+  if (l->n == HIST_LIST) dose_flush(l, t);
+  l->vox[l->n] = v;
+  l->acc[l->n] = e;
+  l->n++;
 }
 
 static void deposit(hlist_t *l, tally_t *t, uint32_t v, real e) {
@@ -1743,6 +1780,21 @@ static void ss_split(const scene_t *s, const photon_t *pre, photon_t *ph, int ma
   }
 }
 
+/* Voxel of point p in the dose grid; 0 outside (the library's dose_voxel). */
+static int dose_voxel(const scene_t *s, const real p[3], uint32_t *v) {
+  real f[3];
+  for (int a = 0; a < 3; ++a) {
+    real d = p[a] - s->dcorner[a];
+    f[a] = d * s->dinv_sp[a];
+  }
+  if (!(f[0] >= R(0)) || !(f[1] >= R(0)) || !(f[2] >= R(0))) return 0;
+  if (!(f[0] < (real)s->dnx) || !(f[1] < (real)s->dny) || !(f[2] < (real)s->dnz)) return 0;
+  int ix = (int)f[0], iy = (int)f[1], iz = (int)f[2];
+  if (ix >= s->dnx || iy >= s->dny || iz >= s->dnz) return 0;
+  *v = (uint32_t)ix + (uint32_t)s->dnx * ((uint32_t)iy + (uint32_t)s->dny * (uint32_t)iz);
+  return 1;
+}
+
 static void transport_photon(const scene_t *s, photon_t *ph, rng_t *g, tally_t *t, hlist_t *l,
                              photon_t *sec, int *has_sec, event_t *ev) {
   int steps = 0;
@@ -1796,7 +1848,19 @@ static void transport_photon(const scene_t *s, photon_t *ph, rng_t *g, tally_t *
       const photon_t pre = *ph;
       real ed = interact(s, ph, m, g, t, sec, has_sec);
       /* electrons of a track-length-scored photon deposit nothing (GateTLEDoseActor.cpp:236-243) */
-      if (!s->spect && !(s->tle && e_pre <= s->tle_thr)) deposit(l, t, v, ed);
+      if (s->dgrid) {
+        uint32_t dv;
+        if (dose_voxel(s, ph->pos, &dv)) {
+          deposit(l, t, dv, ed);
+          if (s->ddose) {
+            real dd = ed * s->drho_min;
+            dd = dd / s->mat_rho[m];
+            dose_deposit(t->ld, t, dv, dd);
+          }
+        }
+      } else if (!s->spect && !(s->tle && e_pre <= s->tle_thr)) {
+        deposit(l, t, v, ed);
+      }
       if (ph->alive && ph->in_image) ph->t_exit = exit_distance(ph->pos, ph->dir, s->bmin, s->bmax);
       if (s->ff == 2) ss_split(s, &pre, ph, m, g, t);
     } else if (ph->in_head) {
@@ -1838,8 +1902,10 @@ static void transport_photon(const scene_t *s, photon_t *ph, rng_t *g, tally_t *
 static int run_history(const scene_t *s, uint64_t seed, uint64_t h, tally_t *t) {
   rng_t g;
   rng_init(&g, seed, h, 0u);
-  hlist_t l;
+  hlist_t l, ld;
   l.n = 0;
+  ld.n = 0;
+  t->ld = &ld;
   photon_t ph, sec;
   int has_sec = 0;
   event_t ev;
@@ -1857,8 +1923,13 @@ static int run_history(const scene_t *s, uint64_t seed, uint64_t h, tally_t *t) 
     has_sec = 0;
     start_photon(s, &ph);
   }
-  if (s->spect) score_singles(s, &ev, t, &g);
-  else hlist_flush(&l, t);
+  if (s->spect) {
+    score_singles(s, &ev, t, &g);
+  } else {
+    hlist_flush(&l, t);
+    if (s->dgrid && s->ddose) dose_flush(&ld, t);
+  }
+  t->ld = NULL;
   return GG_OK;
 }
 
@@ -2059,20 +2130,39 @@ static void *worker_main(void *arg) {
    point batch sums into the float64 images edep / edep2 (either may be
    NULL for the squared image), and adding to counters[GG_N_COUNTERS]. */
 static int run_dose_impl(const gg_tables_desc *tb, const gg_volume_desc *vol, const gg_world_desc *w,
-                         const gg_source_desc *src, const gg_tle_desc *tle, uint64_t seed, uint64_t first,
-                         uint64_t n, uint64_t batch, int n_threads, double *edep, double *edep2,
-                         uint64_t *counters) {
+                         const gg_source_desc *src, const gg_tle_desc *tle, const gg_dose_grid_desc *grid,
+                         uint64_t seed, uint64_t first, uint64_t n, uint64_t batch, int n_threads, double *edep,
+                         double *edep2, double *dose, double *dose2, uint64_t *counters) {
   scene_t s;
   scene_init(&s, tb, vol, w, src);
+  double dscale = 1.0;
+  if (grid && grid->dims[0] > 0) {
+    s.dgrid = 1;
+    s.dnx = grid->dims[0];
+    s.dny = grid->dims[1];
+    s.dnz = grid->dims[2];
+    for (int a = 0; a < 3; ++a) {
+      s.dcorner[a] = (real)grid->corner[a];
+      s.dinv_sp[a] = (real)(1.0 / grid->spacing[a]);
+    }
+    s.ddose = grid->score_dose != 0 && dose != NULL;
+    float rmin = tb->mat_rho[0];
+    for (int m = 1; m < tb->n_mat; ++m)
+      if (tb->mat_rho[m] < rmin) rmin = tb->mat_rho[m];
+    s.drho_min = (real)rmin;
+    dscale = 1.0 / (double)rmin;
+  }
   if (tle && tle->enabled) {
     s.tle = 1;
     s.tle_thr = (real)tle->threshold_energy;
     s.tle_emin = (real)tle->energy_min;
     s.muen = conv_f(tle->muen, (size_t)tb->n_comp * tb->n_e);
   }
-  size_t nv = (size_t)s.nx * s.ny * s.nz;
+  size_t nv = s.dgrid ? (size_t)s.dnx * s.dny * s.dnz : (size_t)s.nx * s.ny * s.nz;
   uint64_t *acc_e = (uint64_t *)calloc(nv, sizeof(uint64_t));
   uint64_t *acc_e2 = edep2 ? (uint64_t *)calloc(2 * nv, sizeof(uint64_t)) : NULL;
+  uint64_t *acc_d = s.ddose ? (uint64_t *)calloc(nv, sizeof(uint64_t)) : NULL;
+  uint64_t *acc_d2 = s.ddose && dose2 ? (uint64_t *)calloc(2 * nv, sizeof(uint64_t)) : NULL;
   if (n_threads < 1) n_threads = 1;
   if (batch == 0) batch = n ? n : 1;
   {
@@ -2104,6 +2194,8 @@ static int run_dose_impl(const gg_tables_desc *tb, const gg_volume_desc *vol, co
       ws[i].h1 = ws[i].h0 + per < b1 ? ws[i].h0 + per : b1;
       ws[i].t.acc_e = acc_e;
       ws[i].t.acc_e2 = acc_e2;
+      ws[i].t.acc_d = acc_d;
+      ws[i].t.acc_d2 = acc_d2;
       ws[i].status = GG_OK;
       if (n_threads > 1) pthread_create(&th[i], NULL, worker_main, &ws[i]);
       else worker_main(&ws[i]);
@@ -2125,6 +2217,23 @@ static int run_dose_impl(const gg_tables_desc *tb, const gg_volume_desc *vol, co
         edep2[v] += hi + lo;
         acc_e2[2 * v] = acc_e2[2 * v + 1] = 0;
       }
+      /* dose tally: the library's k_flush with scale 1 / rho_min */
+      if (acc_d && acc_d[v]) {
+        double x = (double)acc_d[v] * 2.3283064365386963e-10;
+        x = x * dscale;
+        dose[v] += x;
+        acc_d[v] = 0;
+      }
+      if (acc_d2 && (acc_d2[2 * v] | acc_d2[2 * v + 1])) {
+        double lo = (double)acc_d2[2 * v];
+        lo = lo * 5.421010862427522e-20;
+        double hi = (double)acc_d2[2 * v + 1];
+        hi = hi * 2.3283064365386963e-10;
+        double x = hi + lo;
+        x = x * (dscale * dscale);
+        dose2[v] += x;
+        acc_d2[2 * v] = acc_d2[2 * v + 1] = 0;
+      }
     }
   }
   for (int i = 0; i < n_threads; ++i)
@@ -2133,6 +2242,8 @@ static int run_dose_impl(const gg_tables_desc *tb, const gg_volume_desc *vol, co
   free(th);
   free(acc_e);
   free(acc_e2);
+  free(acc_d);
+  free(acc_d2);
   scene_free(&s);
   return status;
 }
@@ -2141,7 +2252,18 @@ int GGO_PREFIX(run_dose)(const gg_tables_desc *tb, const gg_volume_desc *vol, co
                          const gg_source_desc *src, uint64_t seed, uint64_t first, uint64_t n,
                          uint64_t batch, int n_threads, double *edep, double *edep2,
                          uint64_t *counters) {
-  return run_dose_impl(tb, vol, w, src, NULL, seed, first, n, batch, n_threads, edep, edep2, counters);
+  return run_dose_impl(tb, vol, w, src, NULL, NULL, seed, first, n, batch, n_threads, edep, edep2, NULL, NULL,
+                       counters);
+}
+
+/* run_dose with the tally on a grid of its own (gg_set_dose_grid): edep and,
+   with grid->score_dose, the dose sum(edep / rho) (either squares may be NULL). */
+int GGO_PREFIX(run_dose_grid)(const gg_tables_desc *tb, const gg_volume_desc *vol, const gg_world_desc *w,
+                              const gg_source_desc *src, const gg_dose_grid_desc *grid, uint64_t seed,
+                              uint64_t first, uint64_t n, uint64_t batch, int n_threads, double *edep,
+                              double *edep2, double *dose, double *dose2, uint64_t *counters) {
+  return run_dose_impl(tb, vol, w, src, NULL, grid, seed, first, n, batch, n_threads, edep, edep2, dose, dose2,
+                       counters);
 }
 
 /* run_dose with the track-length estimator of gg_set_tle. */
@@ -2149,7 +2271,8 @@ int GGO_PREFIX(run_dose_tle)(const gg_tables_desc *tb, const gg_volume_desc *vol
                              const gg_source_desc *src, const gg_tle_desc *tle, uint64_t seed, uint64_t first,
                              uint64_t n, uint64_t batch, int n_threads, double *edep, double *edep2,
                              uint64_t *counters) {
-  return run_dose_impl(tb, vol, w, src, tle, seed, first, n, batch, n_threads, edep, edep2, counters);
+  return run_dose_impl(tb, vol, w, src, tle, NULL, seed, first, n, batch, n_threads, edep, edep2, NULL, NULL,
+                       counters);
 }
 
 /* SPECT projections: for each run r (gantry position, head frames

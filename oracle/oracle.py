@@ -92,6 +92,33 @@ def run_dose(scene, n, seed, first=0, batch=0, threads=1, precision=32, squared=
     return edep.reshape(shape), (edep2.reshape(shape) if squared else None), counters
 
 
+def run_dose_grid(scene, grid, n, seed, first=0, batch=0, threads=1, precision=32, squared=True):
+    """Oracle run with the tally on its own grid (grid: a C.DoseGridDesc):
+    (edep, edep2 or None, dose sum or None, dose2 or None, counters), grid shape [nz][ny][nx]."""
+    L = lib(precision)
+    fn = getattr(L, f"ggo{precision}_run_dose_grid")
+    fn.restype = ctypes.c_int
+    fn.argtypes = [ctypes.POINTER(C.TablesDesc), ctypes.POINTER(C.VolumeDesc), ctypes.POINTER(C.WorldDesc),
+                   ctypes.POINTER(C.SourceDesc), ctypes.POINTER(C.DoseGridDesc), ctypes.c_uint64, ctypes.c_uint64,
+                   ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int] + [ctypes.POINTER(ctypes.c_double)] * 4 + \
+        [ctypes.POINTER(ctypes.c_uint64)]
+    shape = (grid.dims[2], grid.dims[1], grid.dims[0])
+    nv = int(np.prod(shape))
+    edep = np.zeros(nv)
+    edep2 = np.zeros(nv) if squared else None
+    dose = np.zeros(nv) if grid.score_dose else None
+    dose2 = np.zeros(nv) if grid.score_dose and squared else None
+    cnt = np.zeros(C.GG_N_COUNTERS, dtype=np.uint64)
+    descs = (ctypes.byref(scene.tables_desc), ctypes.byref(scene.volume_desc), ctypes.byref(scene.world_desc),
+             ctypes.byref(scene.source_desc))
+    st = fn(*descs, ctypes.byref(grid), seed, first, n, batch, threads,
+            *(C.ptr(a, ctypes.c_double) for a in (edep, edep2, dose, dose2)), C.ptr(cnt, ctypes.c_uint64))
+    if st != 0:
+        raise RuntimeError(f"oracle run failed with status {st}")
+    r = lambda a: None if a is None else a.reshape(shape)  # noqa: E731
+    return r(edep), r(edep2), r(dose), r(dose2), {name: int(cnt[i]) for i, name in enumerate(C.COUNTER_NAMES)}
+
+
 def philox(ctr, key, precision=32):
     L = lib(precision)
     c = (ctypes.c_uint32 * 4)(*ctr)

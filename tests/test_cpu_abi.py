@@ -54,7 +54,7 @@ def test_ctypes_struct_layout_matches_header(tmp_path):
                "gg_world_desc": C.WorldDesc, "gg_source_desc": C.SourceDesc, "gg_device_opts": C.DeviceOpts,
                "gg_arf_sampling": C.ArfSampling, "gg_sim_desc": C.SimDescC, "gg_arf_model": C.ArfModel,
                "gg_arf_train_opts": C.ArfTrainOpts, "gg_tle_desc": C.TleDesc,
-               "gg_ff_desc": C.FfDesc, "gg_blur_desc": C.BlurDesc}
+               "gg_ff_desc": C.FfDesc, "gg_blur_desc": C.BlurDesc, "gg_dose_grid_desc": C.DoseGridDesc}
     lines = ['#include <stdio.h>', '#include <stddef.h>', f'#include "{HEADER}"', "int main(void) {"]
     for cname, py in structs.items():
         lines.append(f'  printf("{cname} %zu\\n", sizeof({cname}));')

@@ -76,10 +76,53 @@ def test_unsupported_options_raise(tmp_path):
     with pytest.raises(NotImplementedError):
         sim.add_actor("LETActor", "let")
     sim = water_sim(tmp_path)
-    sim.actors["dose"].spacing = [4 * u.mm] * 3
+    sim.actors["dose"].score_in = "G4_WATER"
     scene, vol, hu, names, sources = sim.build_scene()
     with pytest.raises(NotImplementedError):
         sim.actors["dose"].check(vol, hu)
+    sim.actors["dose"].score_in = "material"
+    sim.actors["dose"].output_coordinate_system = "elsewhere"
+    with pytest.raises(ValueError):
+        sim.actors["dose"].check(vol, hu)
+
+
+def test_dose_grid_placement_and_output_coordinates(tmp_path):
+    """A dose grid of its own: centred on the image volume + translation, axis-aligned
+    (AttachImageToVolume); output origin / direction per output_coordinate_system as in
+    VoxelDepositActor._update_output_coordinate_system (doseactors.py:170-232)."""
+    from scipy.spatial.transform import Rotation
+
+    sim = water_sim(tmp_path)
+    vol = sim.volumes["phantom"]
+    vol.translation = [5 * u.mm, -3 * u.mm, 2 * u.mm]
+    d = sim.actors["dose"]
+    d.size = [10, 12, 14]
+    d.spacing = [4 * u.mm, 5 * u.mm, 6 * u.mm]
+    d.translation = [1 * u.mm, 2 * u.mm, 3 * u.mm]
+    rot = Rotation.from_euler("z", 30, degrees=True).as_matrix()
+    d.rotation = rot
+    scene, v, hu, names, sources = sim.build_scene()
+    d.check(v, hu)
+    assert not d.on_image_grid(hu)
+    dims, sp, corner = d.scoring_grid(v)
+    assert dims == [10, 12, 14] and sp == pytest.approx([4, 5, 6])
+    np.testing.assert_allclose(corner, np.array([6, -1, 5]) - np.array([40, 60, 84]) / 2.0)
+    size, spa = np.array([10, 12, 14.0]), np.array([4.0, 5.0, 6.0])
+    origin = -size * spa / 2 + spa / 2
+    local = Rotation.from_matrix(rot).apply(origin) + np.array([1.0, 2.0, 3.0])
+    for cs, o, r in ((None, origin, np.eye(3)), ("local", local, rot),
+                     ("global", local + np.array([5.0, -3.0, 2.0]), rot)):
+        d.output_coordinate_system = cs
+        s2, o2, r2 = d.output_geometry(v, hu)
+        np.testing.assert_allclose(o2, o, atol=1e-12)
+        np.testing.assert_allclose(r2, r, atol=1e-12)
+    d.output_coordinate_system = "attached_to_image"
+    _, o3, r3 = d.output_geometry(v, hu)
+    n_tr = np.asarray(hu.origin) + (np.array(hu.size) - 1.0) * hu.spacing / 2.0
+    np.testing.assert_allclose(o3, local + n_tr, atol=1e-12)
+    # the image grid itself is recognised
+    d.size, d.spacing, d.translation = list(hu.size), list(hu.spacing), [0, 0, 0]
+    assert d.on_image_grid(hu)
 
 
 def test_spectrum_and_acceptance_conversion(tmp_path):
