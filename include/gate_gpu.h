@@ -408,8 +408,14 @@ typedef struct {
   int32_t rayleigh_splitting;
   int32_t max_compton_level;
   /* angular acceptance, angle check (biasingactors.py generic_source_default_aa
-     angle_tolerance_max): a copy that enters a head more than this many
-     radians off the head's axis is dropped; <= 0: no angle check */
+     angle_tolerance_max): a photon (GG_FF_PRIMARY) or copy (GG_FF_SCATTER)
+     whose line enters a head more than this many radians off the head's axis
+     is dropped before its optical depth is computed, as the reference's
+     free-flight recipes skip such directions at the source
+     (contrib/spect/spect_config.py:937-970); <= 0: no angle check.  With the
+     ARF detectors on (gg_spect_use_arf) free flight and the network combine:
+     a photon reaching a head face is scored with its free-flight weight times
+     the network's window weights. */
   double angle_tolerance_max;
 } gg_ff_desc;
 int gg_spect_set_free_flight(gg_ctx *ctx, const gg_ff_desc *ff);

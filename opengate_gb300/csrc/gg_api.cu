@@ -1156,8 +1156,8 @@ static int spect_stages(gg_ctx *c, gg::KernelArgs a, size_t smem, int minb) {
         c->ss_span = std::max<uint64_t>(1, std::min<uint64_t>(span / 2, (uint64_t)(0.85 * (double)span / fill)));
         continue;
       }
-      if ((st = stage_run(1, c->d_queue[0], nh, c->d_queue[1], nr))) return st;
-      ++c->last_stage_launches;
+      if ((st = head_pass())) return st;
+      c->last_stage_launches += c->arf_on ? 2 : 1;
       lo = a.h_end;
     }
     if ((st = c->cuda(cudaStreamSynchronize(c->stream), "SPECT head stage"))) return st;
@@ -1824,7 +1824,6 @@ int gg_spect_use_arf(gg_ctx *c, int32_t enable) {
   if (c->arf.n_classes != c->spect.n_windows + 1)
     return c->fail(GG_ERR_ARG, "gg_spect_use_arf: the model has %d classes, the heads %d windows + 1", c->arf.n_classes,
                    c->spect.n_windows);
-  if (c->ff_on) return c->fail(GG_ERR_STATE, "gg_spect_use_arf: switch free flight off first");
   c->arf_on = true;
   int st = arf_projection_alloc(c, c->n_proj);
   if (st) return st;
@@ -1842,7 +1841,6 @@ int gg_spect_set_free_flight(gg_ctx *c, const gg_ff_desc *f) {
   if (f->enabled != GG_FF_PRIMARY && f->enabled != GG_FF_SCATTER)
     return c->fail(GG_ERR_ARG, "gg_spect_set_free_flight: unknown mode %d", f->enabled);
   if (!c->have_spect) return c->fail(GG_ERR_STATE, "gg_spect_set_free_flight: call gg_spect_setup first");
-  if (c->arf_on) return c->fail(GG_ERR_STATE, "gg_spect_set_free_flight: the ARF detector is on");
   if (std::isnan(f->weight_cutoff) || std::isnan(f->energy_cutoff))
     return c->fail(GG_ERR_ARG, "gg_spect_set_free_flight: invalid cutoff");
   if (std::isnan(f->angle_tolerance_max)) return c->fail(GG_ERR_ARG, "gg_spect_set_free_flight: invalid angle");
@@ -1858,7 +1856,7 @@ int gg_spect_set_free_flight(gg_ctx *c, const gg_ff_desc *f) {
   c->ss_nc = f->enabled == GG_FF_SCATTER ? f->compton_splitting : 0;
   c->ss_nr = f->enabled == GG_FF_SCATTER ? f->rayleigh_splitting : 0;
   c->ss_max = f->enabled == GG_FF_SCATTER ? f->max_compton_level : 0;
-  c->ss_cos = f->enabled == GG_FF_SCATTER && f->angle_tolerance_max > 0.0 ? std::cos(f->angle_tolerance_max) : -2.0;
+  c->ss_cos = f->angle_tolerance_max > 0.0 ? std::cos(f->angle_tolerance_max) : -2.0;
   c->ss_span = 0;
   int st = arf_projection_alloc(c, c->n_proj);
   if (st) return st;

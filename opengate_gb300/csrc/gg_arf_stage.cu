@@ -21,7 +21,9 @@
 // named-barrier synchronisation inside the group only, so the groups overlap
 // one another's MMAs and epilogues.  Window weights are w_k = p_k / (RR p_0 +
 // sum_k>0 p_k) (class 0 re-weighted by the Russian roulette of its training
-// rows) and go to fixed-point projection tallies (2^-32 units, with the exact
+// rows), times the photon's weight with free flight (the expected detection
+// of a photon that got there with probability w), and go to fixed-point
+// projection tallies (2^-32 units, with the exact
 // square for the history-by-history variance), so projections are
 // bit-reproducible.
 #include <cuda_bf16.h>
@@ -95,6 +97,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spect_arf(Scene<real> s, ArfS
     const uint64_t k = base + r;
     int mode = kArfNone;
     float x0 = 0.f, x1 = 0.f, x2 = 0.f;
+    float wph = 1.0f;  // the photon's free-flight weight (1 without free flight)
     long long p_off = -1;
     if (k < n_items) {
       const uint32_t meta = in.meta[k];
@@ -109,6 +112,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spect_arf(Scene<real> s, ArfS
       } else if (lz < (real)1e-3 && dz > (real)0 && e >= (real)a.e_min && e <= (real)a.e_max &&
                  dz >= (real)a.cos_theta_max) {
         mode = kArfNet;
+        if (s.ff) wph = (float)in.w[k];
         const real dx = in.dx[k], dy = in.dy[k];
         const float th = acosf((float)dz) * kArfRadToDeg;
         const float ph = atan2f((float)dy, (float)dx) * kArfRadToDeg;
@@ -160,7 +164,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spect_arf(Scene<real> s, ArfS
 #pragma unroll
       for (int c = 1; c < 16; ++c) {
         if (c >= a.n_classes) break;
-        const unsigned long long q = __float2ull_rn((p[c] * inv) * 4294967296.0f);
+        const unsigned long long q = __float2ull_rn(((p[c] * inv) * wph) * 4294967296.0f);
         if (!q) continue;
         const size_t idx = (size_t)p_off + (size_t)(c - 1) * plane;
         atomicAdd(a.proj + idx, q);

@@ -51,7 +51,7 @@ __device__ __forceinline__ int phantom_flight(const Scene<real> &s, Photon<real>
   }
   if constexpr (FFM == kFfPrimary) {  // free flight to a head: no interaction outside the heads
     ++n_world;
-    if (ff_flight(s, ph, R<real>(-2))) return kPush;
+    if (ff_flight(s, ph, s.ss_cos)) return kPush;
     atomicAdd(&bc->escaped, 1u);
     return kRefill;
   }

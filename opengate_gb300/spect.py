@@ -85,11 +85,13 @@ class SpectSpec:
         self.blur.energy_reference = float(reference)
         self.blur.energy_slope = float(slope)
 
-    def set_free_flight(self, weight_cutoff=-1.0, energy_cutoff=0.0, enabled=True):
+    def set_free_flight(self, weight_cutoff=-1.0, energy_cutoff=0.0, enabled=True, angle_tolerance_max=0.0):
         """GammaFreeFlightActor on the world with the heads excluded: no interaction outside
-        the heads, weights exp(-optical depth), weighted projections (MeV for the cutoff)."""
+        the heads, weights exp(-optical depth), weighted projections (MeV for the cutoff).
+        angle_tolerance_max (radians, 0 = off): the angle check of the source's angular
+        acceptance - photons whose line enters a head further off its axis are dropped."""
         self.free_flight = C.FfDesc(C.FF_PRIMARY if enabled else C.FF_OFF, float(weight_cutoff),
-                                    float(energy_cutoff), 0, 0, 0, 0.0)
+                                    float(energy_cutoff), 0, 0, 0, float(angle_tolerance_max))
 
     def set_scatter_splitting(self, compton_splitting, rayleigh_splitting, max_compton_level=10,
                               weight_cutoff=-1.0, energy_cutoff=0.0, angle_tolerance_max=0.0):

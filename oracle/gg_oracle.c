@@ -1253,6 +1253,7 @@ static void arf_at_head(const scene_t *s, photon_t *ph, tally_t *t) {
   size_t plane = (size_t)s->pny * s->pnx;
   for (int c = 1; c < a->nc; ++c) {
     double w = norm > 0 ? p[c] / norm : 0.0;
+    if (s->ff) w = w * (double)ph->w; /* free flight: the photon got here with probability w */
     uint64_t q = (uint64_t)llrint(w * 4294967296.0);
     if (!q) continue;
     size_t idx = ((((size_t)ph->head * s->n_runs + s->run) * s->n_win + (c - 1)) * plane) + (size_t)j * s->pnx + i;
@@ -1315,7 +1316,8 @@ static void spect_world_step(const scene_t *s, photon_t *ph, rng_t *g, tally_t *
       ph->head = h;
       ph->hreg = lp[2] < s->zb[1] ? 0 : (lp[2] < s->zb[2] ? 1 : 2);
       ph->left_hole = 0;
-      if (s->arf && !ph->head_stage) arf_at_head(s, ph, t);
+      /* (scatter splitting: the analog photon dies at the head, only its copies are scored) */
+      if (s->arf && !ph->head_stage && s->ff != 2) arf_at_head(s, ph, t);
       if (ph->alive) {
         ph->visited_head = 1;
         ph->head_stage = 1;
@@ -1727,6 +1729,10 @@ static void ff_step(const scene_t *s, photon_t *ph, tally_t *t, real cos_min) {
   ph->head = h;
   ph->hreg = lp[2] < s->zb[1] ? 0 : (lp[2] < s->zb[2] ? 1 : 2);
   ph->left_hole = 0;
+  /* ARF detectors: a photon that reaches a head from the phantom is scored
+     by the network with its weight, or tracked (the library's ARF stage) */
+  if (s->arf && !ph->visited_head) arf_at_head(s, ph, t);
+  if (ph->alive) ph->visited_head = 1;
 }
 
 /* Scatter splitting (GateScatterSplittingFreeFlightOptrActor.cpp:291-360 and
@@ -1806,7 +1812,7 @@ static void transport_photon(const scene_t *s, photon_t *ph, rng_t *g, tally_t *
       break;
     }
     if (s->ff == 1 && !ph->in_head) {
-      ff_step(s, ph, t, R(-2));
+      ff_step(s, ph, t, ph->visited_head ? R(-2) : s->ss_cos);
       continue;
     }
     if (ph->in_image) {
@@ -2297,8 +2303,10 @@ static int run_spect_impl(const gg_tables_desc *tb, const gg_volume_desc *vol, c
       s.ss_nc = ff->compton_splitting;
       s.ss_nr = ff->rayleigh_splitting;
       s.ss_max = ff->max_compton_level;
-      s.ss_cos = (real)(ff->angle_tolerance_max > 0.0 ? cos(ff->angle_tolerance_max) : -2.0);
     }
+    /* angle check: the copies of scatter splitting, and primary free flights
+       from the phantom (not the flights of photons leaving a head) */
+    s.ss_cos = (real)(ff->angle_tolerance_max > 0.0 ? cos(ff->angle_tolerance_max) : -2.0);
     s.wproj = wproj;
     s.wproj2 = wproj2;
   }
@@ -2519,11 +2527,8 @@ int GGO_PREFIX(run_spect_ff)(const gg_tables_desc *tb, const gg_volume_desc *vol
    photon reaches a head from the phantom side; window weights go to
    arf_proj / arf_proj2 (fixed point, 2^-32 and 2^-64 / 2^-32 units, zeroed by
    the caller). */
-int GGO_PREFIX(run_spect_arf)(const gg_tables_desc *tb, const gg_volume_desc *vol, const gg_world_desc *w,
-                              const gg_source_desc *src, const gg_spect_desc *sp, const double *frames,
-                              uint64_t seed, uint64_t first, uint64_t n_per_run, int n_threads, uint64_t *proj,
-                              uint64_t *counters, const gg_arf_model *m, const float *params, uint64_t *arf_proj,
-                              uint64_t *arf_proj2) {
+static arf_t *arf_make(const gg_spect_desc *sp, const gg_arf_model *m, const float *params, uint64_t *arf_proj,
+                       uint64_t *arf_proj2) {
   arf_t *a = (arf_t *)calloc(1, sizeof(arf_t));
   a->nc = m->n_classes;
   const float *pw = params;
@@ -2556,8 +2561,33 @@ int GGO_PREFIX(run_spect_arf)(const gg_tables_desc *tb, const gg_volume_desc *vo
   a->dc = (real)m->distance_to_crystal;
   a->proj = arf_proj;
   a->proj2 = arf_proj2;
+  return a;
+}
+
+int GGO_PREFIX(run_spect_arf)(const gg_tables_desc *tb, const gg_volume_desc *vol, const gg_world_desc *w,
+                              const gg_source_desc *src, const gg_spect_desc *sp, const double *frames,
+                              uint64_t seed, uint64_t first, uint64_t n_per_run, int n_threads, uint64_t *proj,
+                              uint64_t *counters, const gg_arf_model *m, const float *params, uint64_t *arf_proj,
+                              uint64_t *arf_proj2) {
+  arf_t *a = arf_make(sp, m, params, arf_proj, arf_proj2);
   int st = run_spect_impl(tb, vol, w, src, sp, frames, seed, first, n_per_run, n_threads, proj, counters, a, NULL,
                           NULL, NULL);
+  free(a);
+  return st;
+}
+
+/* ARF detectors with free flight (gg_spect_use_arf + gg_spect_set_free_flight):
+   network window weights times the free-flight weight and the weighted singles
+   of the photons tracked instead go to the same weighted projection
+   (arf_proj, arf_proj2), as in the library. */
+int GGO_PREFIX(run_spect_arf_ff)(const gg_tables_desc *tb, const gg_volume_desc *vol, const gg_world_desc *w,
+                                 const gg_source_desc *src, const gg_spect_desc *sp, const double *frames,
+                                 const gg_ff_desc *ff, uint64_t seed, uint64_t first, uint64_t n_per_run,
+                                 int n_threads, uint64_t *proj, uint64_t *counters, const gg_arf_model *m,
+                                 const float *params, uint64_t *arf_proj, uint64_t *arf_proj2) {
+  arf_t *a = arf_make(sp, m, params, arf_proj, arf_proj2);
+  int st = run_spect_impl(tb, vol, w, src, sp, frames, seed, first, n_per_run, n_threads, proj, counters, a, ff,
+                          arf_proj, arf_proj2);
   free(a);
   return st;
 }

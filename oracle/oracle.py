@@ -333,3 +333,36 @@ def run_spect_arf(scene, spect, n_per_run, seed, model, params, first=0, threads
     arf2 = aproj2[1::2].astype(np.float64) * 2.0 ** -32 + aproj2[0::2].astype(np.float64) * 2.0 ** -64
     return (proj.astype(np.float64).reshape(shape), arf.reshape(shape), arf2.reshape(shape),
             {name: int(cnt[i]) for i, name in enumerate(C.COUNTER_NAMES)})
+
+
+def run_spect_arf_ff(scene, spect, n_per_run, seed, model, params, first=0, threads=1, precision=32):
+    """Oracle SPECT run with ARF detectors and free flight (spect.free_flight): (tracked counts,
+    weighted projection of network weights x free-flight weights + weighted fallback singles,
+    its history-by-history squares, counters), projection layout."""
+    L = lib(precision)
+    fn = getattr(L, f"ggo{precision}_run_spect_arf_ff")
+    fn.restype = ctypes.c_int
+    fn.argtypes = [ctypes.POINTER(C.TablesDesc), ctypes.POINTER(C.VolumeDesc), ctypes.POINTER(C.WorldDesc),
+                   ctypes.POINTER(C.SourceDesc), ctypes.POINTER(C.SpectDesc), ctypes.POINTER(ctypes.c_double),
+                   ctypes.POINTER(C.FfDesc), ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int,
+                   ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(C.ArfModel),
+                   ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64)]
+    shape = spect.projection_shape()
+    n = int(np.prod(shape))
+    proj = np.zeros(n, dtype=np.uint64)
+    aproj = np.zeros(n, dtype=np.uint64)
+    aproj2 = np.zeros(2 * n, dtype=np.uint64)
+    cnt = np.zeros(C.GG_N_COUNTERS, dtype=np.uint64)
+    desc = spect.desc()
+    frames = spect.all_frames()
+    params = np.ascontiguousarray(params, dtype=np.float32)
+    st = _with_blur(L, precision, spect, lambda: fn(
+        *_descs(scene), ctypes.byref(desc), C.ptr(frames, ctypes.c_double), ctypes.byref(spect.free_flight), seed,
+        first, n_per_run, threads, C.ptr(proj, ctypes.c_uint64), C.ptr(cnt, ctypes.c_uint64), ctypes.byref(model),
+        C.ptr(params, ctypes.c_float), C.ptr(aproj, ctypes.c_uint64), C.ptr(aproj2, ctypes.c_uint64)))
+    if st != 0:
+        raise RuntimeError(f"oracle SPECT ARF + free-flight run failed with status {st}")
+    w = aproj.astype(np.float64) * 2.0 ** -32
+    w2 = aproj2[1::2].astype(np.float64) * 2.0 ** -32 + aproj2[0::2].astype(np.float64) * 2.0 ** -64
+    return (proj.astype(np.float64).reshape(shape), w.reshape(shape), w2.reshape(shape),
+            {name: int(cnt[i]) for i, name in enumerate(C.COUNTER_NAMES)})
