@@ -50,23 +50,33 @@ SPECT_WORKLOAD = ("spect_tc99m_lehr_2heads_60angles_r250mm_128x128x4.42mm_window
 BATCH_METRIC = "primaries/s at matched sigma (batched GPU: 48 uneven simulations in one launch sequence)"
 BATCH_WORKLOAD = "batched_48_slab_phantoms_32-128vox_1-3mm_mono_0.05-2MeV_1e5-1e7_primaries"
 
-# SPECT with ARF detectors: Lu-177 (113 keV 6.2 %, 208 keV 10.4 %), medium-energy
-# collimator, 120 gantry positions, 1e10 decays; the network is trained on
-# 2e8 photons of the plain collimator tracking, and the plain acquisition of
-# the same decays is run beside it for the matched-sigma comparison
 FF_METRIC = ("primaries/s (free-flight SPECT recipe: primary free-flight pass + scatter-splitting pass, "
              "SPECT projections)")
 FF_DECAYS = 100_000_000
 FF_SPLIT = (50, 10, 10000, 10.0)  # Compton, Rayleigh factors, max Compton level, angle tolerance (deg)
 FF_CHUNKS = 8  # scatter pass in independent chunks: its variance (copies of a history are correlated)
 FF_WORKLOAD = SPECT_WORKLOAD + "_freeflight_primary+scattersplit_c50_r10_aa10deg"
-ARF_METRIC = "primaries/s at matched sigma (ARF GPU vs plain GPU collimator tracking, SPECT projections)"
+
+# SPECT with ARF detectors: Lu-177 (113 keV 6.2 %, 208 keV 10.4 %), medium-energy
+# collimator, 120 gantry positions, 1e10 decays.  The ARF acquisition is the
+# reference's recipe: a primary pass in free flight (angle check at the source)
+# into the ARF detectors plus a scatter-splitting pass into the ARF detectors on
+# 1/8 of the primaries; the network is trained on 2e8 photons of the plain
+# collimator tracking, and the plain acquisition of as many decays is run beside
+# it for the matched-sigma comparison
+ARF_METRIC = ("primaries/s (ARF SPECT recipe: primary free-flight pass + scatter-splitting pass on 1/8 of the "
+              "primaries, both into ARF detectors; SPECT projections)")
 ARF_DECAYS = 10_000_000_000
 ARF_YIELD = 0.166
 ARF_WINDOWS = ((0.1872, 0.2288), (0.166, 0.187), (0.1017, 0.1243))
 ARF_TRAIN_SAMPLES = 200_000_000
+ARF_PRIMARY_DEG = 15.0  # primary pass: angle tolerance of the source's angular acceptance
+ARF_SPLIT = (10, 2, 10000, 15.0)  # scatter pass: Compton, Rayleigh factors, max Compton level, angle tolerance
+ARF_SCATTER_SHARE = 8  # the scatter pass runs 1 / 8 of the primaries
+ARF_CHUNKS = 16  # ... in independent chunks (its variance)
+ARF_SUMMARY_PRIMARIES = 240_000_000  # reduced comparison carried by the default (dose) line
 ARF_WORKLOAD = ("spect_lu177_melp_2heads_120angles_r250mm_128x128x4.42mm_windows187-229_166-187_101-125keV_"
-                "ct_phantom_256x256x160_1.2mm_arf_mlp3x128_bf16")
+                "ct_phantom_256x256x160_1.2mm_arf_mlp3x128_bf16_freeflight_aa15deg+scattersplit_c10_r2_aa15deg_1of8")
 
 
 def measured_peaks():
@@ -636,63 +646,218 @@ def run_ours_ff(args, ws, rank, local, dist, use_cuda):
     return 0
 
 
-def projection_sigma(tot, tot2, n, n_win):
-    """(per-pixel sigma of the peak window as for the plain bench, mean relative
-    uncertainty of the per-projection window totals)."""
-    from opengate_gb300 import spect as S
+class ArfRecipe:
+    """The ARF acquisition of the spect_arf workload, and the plain acquisition beside it.
 
-    pix = S.mean_relative_uncertainty(tot[:, 0::n_win], tot2[:, 0::n_win], n)
-    # per projection (head, position, window): totals and history-by-history squares
-    t = tot.sum(axis=(2, 3))
-    t2 = tot2.sum(axis=(2, 3))  # a history adds to one pixel of a projection at most
-    rel = S.compute_history_by_history_relative_uncertainty(t, t2, n)
-    return pix, float(rel[t > 0].mean())
+    ARF acquisition, as the reference's free-flight and ARF recipes compose it
+    (contrib/spect/spect_config.py:937-1000, actors/arfactors.py:349-453):
+      * primary pass: free flight from the source with the angle check of the
+        source's angular acceptance (biasing/GateGammaFreeFlightOptn.cpp:34-83);
+        a photon that reaches a head face adds exp(-optical depth) x the
+        network's window probabilities;
+      * scatter pass, on 1 / ARF_SCATTER_SHARE of the primaries: scatter
+        splitting (GateScatterSplittingFreeFlightOptrActor.cpp:291-420), the
+        copies reaching a head scored by the network with their weight; run in
+        ARF_CHUNKS independent chunks (the copies of a history are correlated,
+        so its variance comes from the chunks).
+    Plain acquisition: analog photons tracked through the collimator and
+    crystal (counts).  The network is trained on rows of the plain head
+    transport before either runs."""
+
+    def __init__(self, local, seed, batch, train_samples, epochs, n_runs=120, primary_deg=ARF_PRIMARY_DEG,
+                 split=ARF_SPLIT, share=ARF_SCATTER_SHARE):
+        from opengate_gb300 import spect as S
+        from opengate_gb300 import workloads as W
+        from opengate_gb300.engine import ArfNetwork, SpectEngine
+
+        self.scene, self.sp, _ = W.spect_phantom(nuclide=W.LU177, collimator=S.MELP, n_runs=n_runs,
+                                                 windows=ARF_WINDOWS)
+        batch = min(batch, 1 << 26)
+        self.plain = SpectEngine(self.scene, self.sp, device=local, precision=32, batch=batch)
+        net = ArfNetwork(self.plain)
+        # training rows: plain head transport of photons on the face, theta uniform to 85 degrees
+        smp = ArfNetwork.sampling(min(lo for lo, _ in ARF_WINDOWS), 0.21, 85.0, (200.0, 200.0), 40.0)
+        t0 = time.perf_counter()
+        self.model, self.loss = net.train(smp, train_samples, seed=seed + 7, epochs=epochs, batch=8192, lr=2e-3,
+                                          lr_final=1e-5)
+        self.train_s = time.perf_counter() - t0
+        self.params = net.params()
+        self.sp_p = copy.deepcopy(self.sp)
+        self.primary_deg, self.split, self.share = primary_deg, tuple(split), share
+        self.sp_p.set_free_flight(angle_tolerance_max=math.radians(primary_deg))
+        nc, nr, lvl, deg = self.split
+        self.sp_s = copy.deepcopy(self.sp)
+        self.sp_s.set_scatter_splitting(nc, nr, lvl, angle_tolerance_max=math.radians(deg))
+        self.prim = SpectEngine(self.scene, self.sp_p, device=local, precision=32, batch=batch)
+        self.scat = SpectEngine(self.scene, self.sp_s, device=local, precision=32, batch=batch)
+        for e in (self.prim, self.scat):
+            ArfNetwork(e).set_model(self.model, self.params)
+            e.use_arf(True)
+            e.reset()
+        self.nw = self.sp.n_windows
+
+    def scatter_per_run(self, n_per_run):
+        return max(1, n_per_run // self.share // ARF_CHUNKS)
+
+    def acquire(self, n_per_run, seed, first, keep=False):
+        """One ARF acquisition (histories first .. first + n_per_run x positions): device ms,
+        kernel launches, device ms per pass, and with keep the tallies for its statistics."""
+        runs = self.sp.n_runs
+        m = self.scatter_per_run(n_per_run)
+        self.prim.reset()
+        self.prim.run(n_per_run, seed, first)
+        tg, tt, tf, nl = self.prim.last_kernel_ms()
+        parts = {"primary_pass": tg + tt + tf}
+        ph, hd, arf = self.prim.last_stage_ms()
+        parts.update({"primary_phantom_stage": ph, "primary_head_stage": hd, "primary_arf_stage": arf})
+        ms = tg + tt + tf
+        st = None
+        if keep:
+            wp, wp2 = self.prim.weighted_projection(squared=True)
+            st = {"wp": wp, "wp2": wp2, "n_p": n_per_run * runs, "n_s": m * ARF_CHUNKS * runs,
+                  "counters_primary": self.prim.counters()}
+            prev, s2, tot = 0.0, 0.0, []
+        self.scat.reset()
+        sc = {"scatter_pass": 0.0, "scatter_phantom_stage": 0.0, "scatter_head_stage": 0.0,
+              "scatter_copies_and_arf": 0.0}
+        for c in range(ARF_CHUNKS):
+            self.scat.run(m, seed + 1, first + c * m * runs)  # run r of a call: first + r * m
+            tg, tt, tf, k = self.scat.last_kernel_ms()
+            ph, hd, cp = self.scat.last_stage_ms()
+            ms, nl = ms + tg + tt + tf, nl + k
+            sc["scatter_pass"] += tg + tt + tf
+            sc["scatter_phantom_stage"] += ph
+            sc["scatter_head_stage"] += hd
+            sc["scatter_copies_and_arf"] += cp
+            if keep:
+                cur = self.scat.weighted_projection()
+                d = cur - prev
+                s2 = s2 + d * d
+                tot.append(d.sum(axis=(2, 3)))
+                prev = cur
+        parts.update(sc)
+        if keep:
+            st.update({"ws": prev, "ws_c2": s2, "chunk_totals": np.array(tot), "counters_scatter": self.scat.counters()})
+        return ms, nl, parts, st
+
+    def estimate(self, st):
+        """Per-primary projection of the ARF acquisition and the variance of that mean,
+        per pixel and per projection total (head, position x window)."""
+        n_p, n_s, j = st["n_p"], st["n_s"], ARF_CHUNKS
+        mp = st["wp"] / n_p
+        vp = np.maximum((st["wp2"] / n_p - mp * mp) / (n_p - 1), 0.0)
+        # var(sum of j iid chunks) = j / (j - 1) * (sum c^2 - (sum c)^2 / j)
+        vs = np.maximum(j / (j - 1) * (st["ws_c2"] - st["ws"] ** 2 / j), 0.0) / n_s ** 2
+        m = mp + st["ws"] / n_s
+        tp = st["wp"].sum(axis=(2, 3)) / n_p
+        tvp = np.maximum((st["wp2"].sum(axis=(2, 3)) / n_p - tp * tp) / (n_p - 1), 0.0)
+        ch = st["chunk_totals"]
+        t = tp + ch.sum(axis=0) / n_s
+        tv = tvp + j * ch.var(axis=0, ddof=1) / n_s ** 2
+        return m, vp + vs, t, tv
+
+    def compare(self, n_per_run, seed, first_arf, first_plain, arf_ms=None):
+        """Matched-sigma comparison: one ARF acquisition and one plain acquisition of
+        n_per_run histories per position.  Efficiency 1 / (sigma^2 T) per pixel of the
+        peak window (mean relative sigma over pixels > 10 % of max) and per projection
+        total (mean over projections, per window); window totals ARF / plain with their
+        1-sigma statistical error."""
+        import torch
+
+        from opengate_gb300 import spect as S
+
+        ms_a, _, parts, st = self.acquire(n_per_run, seed, first_arf, keep=True)
+        if arf_ms is not None:
+            ms_a = arf_ms
+        self.plain.reset()
+        torch.cuda.synchronize()
+        self.plain.run(n_per_run, seed + 2, first_plain)
+        tg, tt, tf, _ = self.plain.last_kernel_ms()
+        ms_p = tg + tt + tf
+        cp = self.plain.projection()
+        n = n_per_run * self.sp.n_runs
+        nw = self.nw
+        m, v, t, tv = self.estimate(st)
+        pk = m[:, 0::nw]
+        sel = pk > 0.1 * pk.max()
+        sig_a_pix = float((np.sqrt(v[:, 0::nw][sel]) / pk[sel]).mean())
+        sig_p_pix = S.mean_relative_uncertainty(cp[:, 0::nw], cp[:, 0::nw], n)
+        tp = cp.sum(axis=(2, 3))
+        out = {"arf_ms": ms_a, "plain_ms": ms_p, "primaries": n, "scatter_pass_primaries": st["n_s"],
+               "arf_ms_per_pass": parts,
+               "pixel_peak_window": {"sigma_arf": sig_a_pix, "sigma_plain": sig_p_pix,
+                                     "efficiency_gain": (sig_p_pix ** 2 * ms_p) / (sig_a_pix ** 2 * ms_a)},
+               "projection_totals": {}, "window_totals_arf_over_plain": [], "window_ratio_sigma": []}
+        for w in range(nw):
+            ta, va, tpl = t[:, w::nw], tv[:, w::nw], tp[:, w::nw]
+            ok = (ta > 0) & (tpl > 0)
+            sa = float((np.sqrt(va[ok]) / ta[ok]).mean())
+            spl = float((1.0 / np.sqrt(tpl[ok])).mean())
+            out["projection_totals"][f"window_{w}"] = {
+                "sigma_arf": sa, "sigma_plain": spl, "efficiency_gain": (spl ** 2 * ms_p) / (sa ** 2 * ms_a)}
+            r = float(ta.sum() / (tpl.sum() / n))
+            out["window_totals_arf_over_plain"].append(r)
+            out["window_ratio_sigma"].append(r * math.sqrt(va.sum() / ta.sum() ** 2 + 1.0 / tpl.sum()))
+        cnt = {f"primary_{k}": st["counters_primary"][k] for k in ("world_steps", "arf_photons", "arf_fallback")}
+        cnt.update({f"scatter_{k}": st["counters_scatter"][k] for k in ("woodcock_steps", "arf_photons",
+                                                                        "arf_fallback")})
+        out["units"] = cnt
+        out["method"] = ("ARF: primary pass history-by-history squares + scatter pass variance of "
+                         f"{ARF_CHUNKS} independent chunks; plain: counts (Poisson); efficiency 1 / (sigma^2 T), "
+                         "contrib/spect/spect_helpers.py:480-488")
+        return out
+
+    def close(self):
+        for e in (self.prim, self.scat, self.plain):
+            e.close()
+
+
+def arf_options(args):
+    split = list(ARF_SPLIT)
+    split[3] = args.arf_scatter_deg
+    return {"primary_deg": args.arf_primary_deg, "split": split, "share": args.arf_scatter_share}
+
+
+def arf_summary(args, local):
+    """A reduced spect_arf comparison for the default bench line (rank 0, untimed)."""
+    r = ArfRecipe(local, args.seed, args.batch, args.arf_train_samples, args.arf_epochs, **arf_options(args))
+    try:
+        n_per_run = ARF_SUMMARY_PRIMARIES // r.sp.n_runs
+        r.acquire(n_per_run // 8, args.seed, 0)  # warm-up
+        out = r.compare(n_per_run, args.seed, 1 << 40, 1 << 41)
+        out["training_seconds"] = r.train_s
+        out["workload"] = ARF_WORKLOAD
+        out["options"] = arf_options(args)
+        return out
+    finally:
+        r.close()
 
 
 def run_ours_arf(args, ws, rank, local, dist, use_cuda):
     import torch
 
-    from opengate_gb300 import spect as S
-    from opengate_gb300 import workloads as W
-    from opengate_gb300.engine import ArfNetwork, SpectEngine
-
-    scene, sp, _ = W.spect_phantom(nuclide=W.LU177, collimator=S.MELP, n_runs=120, windows=ARF_WINDOWS)
+    rec = ArfRecipe(local, args.seed, args.batch, args.arf_train_samples, args.arf_epochs, **arf_options(args))
+    scene, sp = rec.scene, rec.sp
     n_step = args.primaries if args.primaries != PRIMARIES_PER_STEP else int(ARF_DECAYS * ARF_YIELD)
     n_per_run = n_step // sp.n_runs
     n = n_per_run * sp.n_runs
-    nw = sp.n_windows
-    eng = SpectEngine(scene, sp, device=local, precision=32, batch=min(args.batch, 1 << 26))
-    net = ArfNetwork(eng)
-    # training (not timed): rows from the plain head transport, theta uniform to 85 degrees
-    smp = ArfNetwork.sampling(min(lo for lo, _ in ARF_WINDOWS), 0.21, 85.0, (200.0, 200.0), 40.0)
-    t0 = time.perf_counter()
-    model, loss = net.train(smp, args.arf_train_samples, seed=args.seed + 7, epochs=args.arf_epochs, batch=8192,
-                            lr=2e-3, lr_final=1e-5)
-    train_s = time.perf_counter() - t0
     l2_flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=f"cuda:{local}")
 
     def first_of(step):
         return ((rank * (args.warmup + args.steps + 8)) + step) * n
 
-    def acquire(arf, step):
-        eng.use_arf(arf)
-        l2_flush.zero_()
-        torch.cuda.synchronize()
-        eng.reset()
-        eng.run(n_per_run, args.seed, first_of(step))
-        tg, tt, tf, nl = eng.last_kernel_ms()
-        return tg + tt + tf, nl
-
     for w in range(args.warmup):
-        acquire(True, w)
+        rec.acquire(n_per_run, args.seed, first_of(w))
     torch.cuda.synchronize()
     if dist:
         dist.barrier()
-    dev_ms, launches = [], 0
+    dev_ms, launches, parts = [], 0, None
     t0 = time.perf_counter()
     with ClockSampler(local) as clk:
         for k in range(args.steps):
-            ms, nl = acquire(True, args.warmup + k)
+            l2_flush.zero_()
+            torch.cuda.synchronize()
+            ms, nl, parts, _ = rec.acquire(n_per_run, args.seed, first_of(args.warmup + k))
             dev_ms.append(ms)
             launches += nl
         torch.cuda.synchronize()
@@ -701,48 +866,50 @@ def run_ours_arf(args, ws, rank, local, dist, use_cuda):
         dist.barrier()
     total_ms = dist_max(dist, float(np.sum(dev_ms)), use_cuda)
     value = ws * n * args.steps / (total_ms / 1e3)
-    counters = eng.counters()
-    ph_ms, hd_ms, arf_ms = eng.last_stage_ms()
-    a_counts, (a_w, a_w2) = eng.projection(), eng.arf_projection(squared=True)
-    tot_a, tot2_a = a_counts + a_w, a_counts + a_w2
-    stage_ms = dict(zip(("generate", "transport", "flush"), eng.last_kernel_ms()[:3]))
-    stage_ms.update({"phantom_stage": ph_ms, "head_stage": hd_ms, "arf_stage": arf_ms})
-    # the plain acquisition of the same histories (last timed step) for the matched-sigma comparison
-    plain_ms, _ = acquire(False, args.warmup + args.steps - 1)
-    tot_p = eng.projection()
-    sig_a = projection_sigma(tot_a, tot2_a, n, nw)
-    sig_p = projection_sigma(tot_p, tot_p, n, nw)
-    t_a = total_ms / args.steps
-    gain_pix = (sig_p[0] ** 2 * plain_ms) / (sig_a[0] ** 2 * t_a)
-    gain_proj = (sig_p[1] ** 2 * plain_ms) / (sig_a[1] ** 2 * t_a)
-    win_ratio = [float(tot_a[:, k::nw].sum() / max(tot_p[:, k::nw].sum(), 1e-30)) for k in range(nw)]
+    # statistics of one more acquisition (untimed: it reads the projections per chunk),
+    # charged the timed steps' mean duration, and the plain acquisition of as many primaries
+    cmp = rec.compare(n_per_run, args.seed, first_of(args.warmup + args.steps),
+                      first_of(args.warmup + args.steps + 1), arf_ms=total_ms / args.steps)
+    cnt_p = rec.prim.counters()
 
-    # e2e through the C ABI with host buffers: scene + heads + network upload, acquisition, projections download
-    params = net.params()
-    h2d = scene.labels.nbytes + scene._sig.nbytes + scene._cum.nbytes + scene._ray_amax.nbytes + \
-        scene._ray_cum.nbytes + scene.majorant.nbytes + scene.source_desc_bytes() + sp.all_frames().nbytes + \
-        params.nbytes
-    d2h = 3 * int(np.prod(sp.projection_shape())) * 8
+    # e2e through the C ABI with host buffers: scene + heads + network upload to both
+    # passes' contexts, the acquisition, weighted projections down
+    h2d = 2 * (scene.labels.nbytes + scene._sig.nbytes + scene._cum.nbytes + scene._ray_amax.nbytes +
+               scene._ray_cum.nbytes + scene.majorant.nbytes + scene.source_desc_bytes() + sp.all_frames().nbytes +
+               rec.params.nbytes)
+    d2h = 2 * 3 * int(np.prod(sp.projection_shape())) * 8
+    from opengate_gb300.engine import ArfNetwork
+
     torch.cuda.synchronize()
     e2e_t = []
     for k in range(max(1, min(args.steps, 2))):
         t1 = time.perf_counter()
-        eng.upload()
-        net.set_model(model, params)
-        eng.use_arf(True)
-        eng.run(n_per_run, args.seed, first_of(args.warmup + args.steps + 1 + k))
-        eng.projection()
-        eng.arf_projection(squared=True)
+        for e in (rec.prim, rec.scat):
+            e.upload()
+            ArfNetwork(e).set_model(rec.model, rec.params)
+            e.use_arf(True)
+        rec.acquire(n_per_run, args.seed, first_of(args.warmup + args.steps + 2 + k))
+        rec.prim.weighted_projection(squared=True)
+        rec.scat.weighted_projection(squared=True)
         e2e_t.append(time.perf_counter() - t1)
     e2e_s = dist_max(dist, float(np.mean(e2e_t)), use_cuda)
     fp64 = None
     if rank == 0 and args.fp64_primaries > 0:
-        fp64 = spect_fp64_error(scene, sp, max(1, args.fp64_primaries // sp.n_runs), args.seed, local,
-                                min(args.batch, 1 << 26), arf=(model, params))
+        npr = max(1, args.fp64_primaries // sp.n_runs)
+        fp64 = {"primary_pass": spect_fp64_error(scene, rec.sp_p, npr, args.seed, local, min(args.batch, 1 << 26),
+                                                 arf=(rec.model, rec.params), weighted=True),
+                "scatter_pass": spect_fp64_error(scene, rec.sp_s, max(1, npr // 10), args.seed, local,
+                                                 min(args.batch, 1 << 26), arf=(rec.model, rec.params),
+                                                 weighted=True)}
     # the network's arithmetic: forward FLOP per scored photon
     flop_photon = 2.0 * (3 * 128 + 2 * 128 * 128 + 128 * 16)
+    peak_bw, peak_kind = measured_peaks()
     peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
         os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
+    cnt_s = rec.scat.counters()
+    bytes_alg = 32.0 * cnt_s["woodcock_steps"]
+    ph_ms = parts["scatter_phantom_stage"]
+    net_tf = flop_photon * cnt_p["arf_photons"] / (parts["primary_arf_stage"] / 1e3) / 1e12
     if rank == 0:
         line = {
             "metric": ARF_METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
@@ -750,46 +917,39 @@ def run_ours_arf(args, ws, rank, local, dist, use_cuda):
             "scaling": "weak", "vs_baseline": None, "dtype": "f32 transport, bf16 network (f32 accumulate)",
             "data": "synthetic (seeded CT phantom + activity image)",
             "config": {"workload": ARF_WORKLOAD, "primaries_per_step": n, "decays_per_step": n / ARF_YIELD,
+                       "primary_pass_angle_tolerance_deg": rec.primary_deg,
+                       "scatter_pass": {"share_of_primaries": 1.0 / rec.share, "chunks": ARF_CHUNKS,
+                                        "compton": rec.split[0], "rayleigh": rec.split[1],
+                                        "max_compton_level": rec.split[2], "angle_tolerance_deg": rec.split[3]},
                        "l2": "flushed between steps (256 MiB write)", "training_samples": args.arf_train_samples,
                        "parallelism": f"replicas x{ws}, disjoint history ranges"},
-            "matched_sigma": {
-                "plain_primaries_per_s": n / (plain_ms / 1e3),
-                "plain_equivalent_primaries_per_s_pixel": value * sig_p[0] ** 2 / sig_a[0] ** 2,
-                "plain_equivalent_primaries_per_s_projection": value * sig_p[1] ** 2 / sig_a[1] ** 2,
-                "sigma_pixel": {"arf": sig_a[0], "plain": sig_p[0]},
-                "sigma_projection_total": {"arf": sig_a[1], "plain": sig_p[1]},
-                "efficiency_gain_pixel": gain_pix, "efficiency_gain_projection": gain_proj,
-                "window_counts_arf_over_plain": win_ratio,
-                "note": "efficiency = 1 / (sigma^2 T), contrib/spect/spect_helpers.py:480-488, 582-591"},
-            "training": {"seconds": train_s, "loss_first_last": [float(loss[0]), float(loss[-1])],
+            "matched_sigma": cmp,
+            "training": {"seconds": rec.train_s, "loss_first_last": [float(rec.loss[0]), float(rec.loss[-1])],
                          "epochs": args.arf_epochs},
             "fp64_error": fp64,
             "e2e": {"value": ws * n / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h)},
-            "roofline": {"bound": "hbm", "kernel": "k_spect_phantom<float> (phantom stage, dominant)",
-                         "achieved": 32.0 * counters["woodcock_steps"] / (ph_ms / 1e3) / 1e9,
-                         "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
-                         "frac": 32.0 * counters["woodcock_steps"] / (ph_ms / 1e3) / 1e9 / peaks.get("hbm_gbs", 1.0),
-                         "traffic": args.traffic, "bytes_alg_per_step": 32.0 * counters["woodcock_steps"]},
+            "roofline": {"bound": "hbm", "kernel": "k_spect_phantom<float, scatter splitting> (scatter pass)",
+                         "achieved": bytes_alg / (ph_ms / 1e3) / 1e9, "peak": peak_bw, "unit": "GB/s",
+                         "frac": bytes_alg / (ph_ms / 1e3) / 1e9 / peak_bw, "peak_kind": peak_kind,
+                         "traffic": args.traffic, "bytes_alg_per_step": bytes_alg,
+                         "note": "label gathers of the scatter pass's analog Woodcock steps"},
             "roofline_network": {"bound": "tensor", "kernel": "k_spect_arf<float> (ARF stage, network layers)",
                                  "flop_per_scored_photon": flop_photon,
-                                 "scored_photons_per_step": counters["arf_photons"],
-                                 "achieved": flop_photon * counters["arf_photons"] / (arf_ms / 1e3) / 1e12,
-                                 "peak": peaks.get("bf16_tflops"), "unit": "TFLOP/s",
-                                 "frac": flop_photon * counters["arf_photons"] / (arf_ms / 1e3) / 1e12 /
-                                 peaks.get("bf16_tflops", 1.0),
-                                 "note": "tcgen05.mma kind::f16 (M 128, N 128 / 16, K 16) BF16, FP32 accumulate "
-                                         "in TMEM; arf_stage_ms includes the "
-                                         "queue classification and the projection atomics"},
-            "units": {k: counters[k] for k in ("woodcock_steps", "head_steps", "arf_photons", "arf_fallback", "singles")},
-            "stage_ms_per_step": stage_ms,
+                                 "scored_photons_per_step": cnt_p["arf_photons"] + cnt_s["arf_photons"],
+                                 "achieved": net_tf, "peak": peaks.get("bf16_tflops"), "unit": "TFLOP/s",
+                                 "frac": net_tf / peaks.get("bf16_tflops", 1.0),
+                                 "note": "primary pass's ARF stage (network on its scored photons, the queue "
+                                         "classification and the projection atomics included); tcgen05.mma "
+                                         "kind::f16 (M 128, N 128 / 16, K 16) BF16, FP32 accumulate in TMEM"},
+            "stage_ms_per_step": parts,
             "cpu_baseline": None,
             "clocks": clk.summary(),
             "gpu_launches": int(launches),
             "wall_s": wall,
         }
         print(json.dumps(line), flush=True)
-    eng.close()
+    rec.close()
     if dist:
         dist.destroy_process_group()
     return 0
@@ -1060,6 +1220,7 @@ def run_ours_tle(args, ws, rank, local, dist, use_cuda):
                               "note": "efficiency = 1 / (sigma^2 T), sigma = mean relative uncertainty "
                                       "over voxels > 10 % of max"},
             "fp64_error": fp64,
+            "spect_arf_efficiency": arf,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": None, "peak_kind": peak_kind, "kernel": "k_transport<float> (estimator)",
@@ -1097,6 +1258,7 @@ def run_ours(args):
     if args.workload == "spect_ff":
         return run_ours_ff(args, ws, rank, local, dist, use_cuda)
     from opengate_gb300 import _capi as C
+    from opengate_gb300 import replicas as Rp
     from opengate_gb300 import workloads as W
     from opengate_gb300.engine import DoseEngine
 
@@ -1114,7 +1276,8 @@ def run_ours(args):
     torch.cuda.synchronize()
     if dist:
         dist.barrier()
-    dev_ms = []
+    dev_ms, merge_ms = [], []
+    n_merged = n
     launches = 0
     counters = None
     t0 = time.perf_counter()
@@ -1127,6 +1290,16 @@ def run_ours(args):
             tg, tt, tf, nl = eng.last_kernel_ms()
             dev_ms.append(tg + tt + tf)
             launches += nl
+            if ws > 1:
+                # the replicas' images summed on the devices (NCCL all_reduce of the FP64
+                # images in place), timed on torch's stream where the collective runs
+                ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                ev0.record()
+                n_merged = Rp.merge_tallies_device(eng, (C.GG_IMG_EDEP, C.GG_IMG_EDEP_SQUARED), n)
+                ev1.record()
+                torch.cuda.synchronize()
+                merge_ms.append(ev0.elapsed_time(ev1))
+                dev_ms[-1] += merge_ms[-1]
             if k == args.steps - 1:
                 counters = eng.counters()
                 transport_ms = tt
@@ -1139,9 +1312,10 @@ def run_ours(args):
     total_ms = dist_max(dist, float(np.sum(dev_ms)), use_cuda)
     value = ws * n * args.steps / (total_ms / 1e3)
 
-    # sigma reached by one step (mean relative uncertainty, voxels > 10 % max)
+    # sigma reached by one step (mean relative uncertainty, voxels > 10 % max); with
+    # replicas, of the merged images of all ranks' histories
     edep, edep2 = eng.edep(), eng.edep_squared()
-    sigma = mean_relative_uncertainty(edep, edep2, n)
+    sigma = mean_relative_uncertainty(edep, edep2, n_merged)
 
     # e2e through the C ABI with host buffers: scene upload (H2D), run, image download (D2H)
     h2d = scene.labels.nbytes + scene._sig.nbytes + scene._cum.nbytes + scene._ray_amax.nbytes + \
@@ -1184,6 +1358,12 @@ def run_ours(args):
     if rank == 0 and args.fp64_primaries > 0:
         fp64 = fp64_error(scene, args.fp64_primaries, args.seed, local, args.batch)
 
+    # the spect_arf matched-sigma comparison at reduced size (untimed, separate contexts)
+    arf = None
+    if rank == 0 and ws == 1 and not args.no_arf_summary:
+        eng.close()
+        arf = arf_summary(args, local)
+
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:
         threads = os.cpu_count() or 1
@@ -1199,8 +1379,12 @@ def run_ours(args):
             "config": {"workload": WORKLOAD, "primaries_per_step": n, "tally": "fp64 edep + edep^2, history-by-history",
                        "l2": "flushed between steps (256 MiB write)", "batch": args.batch,
                        "parallelism": f"replicas x{ws}, disjoint history ranges"},
-            "sigma": {"mean_relative_uncertainty_gt10pct_max": sigma, "primaries": n},
+            "sigma": {"mean_relative_uncertainty_gt10pct_max": sigma, "primaries": n_merged},
+            "replica_merge": {"ms_per_step": float(np.mean(merge_ms)) if merge_ms else None,
+                              "method": "NCCL all_reduce of the FP64 edep and edep^2 device images, in the "
+                                        "timed step (replicas.merge_tallies_device)"} if ws > 1 else None,
             "fp64_error": fp64,
+            "spect_arf_efficiency": arf,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
             "roofline": roofline,
             "cpu_baseline": cpu,
@@ -1230,9 +1414,17 @@ def main():
     ap.add_argument("--primaries", type=int, default=PRIMARIES_PER_STEP)
     ap.add_argument("--arf-train-samples", type=int, default=ARF_TRAIN_SAMPLES)
     ap.add_argument("--arf-epochs", type=int, default=80)
+    ap.add_argument("--arf-primary-deg", type=float, default=ARF_PRIMARY_DEG,
+                    help="spect_arf: angle tolerance of the primary free-flight pass (degrees)")
+    ap.add_argument("--arf-scatter-deg", type=float, default=ARF_SPLIT[3],
+                    help="spect_arf: angle tolerance of the scatter-splitting copies (degrees)")
+    ap.add_argument("--arf-scatter-share", type=int, default=ARF_SCATTER_SHARE,
+                    help="spect_arf: the scatter pass runs 1 / share of the primaries")
     ap.add_argument("--batch", type=int, default=1 << 27)
     ap.add_argument("--seed", type=int, default=20240611)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-arf-summary", action="store_true",
+                    help="dose workload: skip the reduced spect_arf comparison carried by its line")
     ap.add_argument("--fp64-primaries", type=int, default=10_000_000,
                     help="histories of the FP32-vs-FP64 comparison of the dose workload (0: skip)")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)

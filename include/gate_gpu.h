@@ -243,6 +243,7 @@ typedef struct {
    kernel).  Both give identical results; they differ in speed only. */
 #define GG_KERNEL_WAVEFRONT 0 /* per-block wavefront compacted by event type */
 #define GG_KERNEL_PHASED 1    /* block-synchronous phases, one history per thread (default) */
+#define GG_KERNEL_PHASED_WARP_FLUSH 2 /* the same, same-voxel tally entries of a warp summed before their atomics */
 
 int gg_create(const gg_device_opts *opts, gg_ctx **out);
 int gg_destroy(gg_ctx *ctx);
@@ -304,6 +305,13 @@ int gg_set_tle(gg_ctx *ctx, const gg_tle_desc *tle);
 int gg_run(gg_ctx *ctx, uint64_t n_histories, uint64_t seed, uint64_t first_history);
 int gg_synchronize(gg_ctx *ctx);
 int gg_get_image(gg_ctx *ctx, int32_t which, double *out, size_t n);
+/* The device copy of an image (GG_IMG_*): *ptr = its FP64 voxels on the
+   context's device, *n = their number; the context's stream is synchronised
+   first.  The pointer stays valid until the next gg_run, gg_reset_tally,
+   tally change or gg_destroy.  For merging replicas on the device (an
+   all-reduce over the ranks' images, opengate/engines.py's merge of the
+   processes' actor outputs) without a round trip through the host. */
+int gg_get_image_device(gg_ctx *ctx, int32_t which, void **ptr, size_t *n);
 int gg_get_counters(gg_ctx *ctx, uint64_t *out, size_t n);
 /* Page-locked host memory (cudaMallocHost) for callers that download or
    upload the same buffers repeatedly: copies from and to it run at the host

@@ -25,7 +25,7 @@ STATUS_NAMES = {0: "GG_OK", 1: "GG_ERR_ARG", 2: "GG_ERR_CUDA", 3: "GG_ERR_QUEUE_
 
 GG_PREC_F32 = 32
 GG_PREC_F64 = 64
-GG_KERNEL_WAVEFRONT, GG_KERNEL_PHASED = 0, 1
+GG_KERNEL_WAVEFRONT, GG_KERNEL_PHASED, GG_KERNEL_PHASED_WARP_FLUSH = 0, 1, 2
 GG_POS_POINT, GG_POS_BOX, GG_POS_SPHERE, GG_POS_DISC, GG_POS_VOXELS = 0, 1, 2, 3, 4
 GG_DIR_ISO, GG_DIR_MOMENTUM, GG_DIR_FOCUSED = 0, 1, 2
 GG_ENE_MONO, GG_ENE_LINES, GG_ENE_HISTOGRAM, GG_ENE_RANGE = 0, 1, 2, 3
@@ -214,6 +214,8 @@ PROTOTYPES = [
     ("gg_set_transport_kernel", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
     ("gg_set_dose_grid", ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(DoseGridDesc)]),
     ("gg_get_image", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, _f64p, ctypes.c_size_t]),
+    ("gg_get_image_device", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.POINTER(ctypes.c_void_p),
+                                           ctypes.POINTER(ctypes.c_size_t)]),
     ("gg_get_counters", ctypes.c_int, [ctypes.c_void_p, _u64p, ctypes.c_size_t]),
     ("gg_host_alloc", ctypes.c_void_p, [ctypes.c_size_t]),
     ("gg_host_free", ctypes.c_int, [ctypes.c_void_p]),

@@ -1164,9 +1164,27 @@ static int spect_stages(gg_ctx *c, gg::KernelArgs a, size_t smem, int minb) {
     stage_collect(c);
     return GG_OK;
   }
-  if ((st = stage_run(0, nullptr, nullptr, c->d_queue[0], nh))) return st;
+  // primary free flight: the phantom stage checks the flights and queues the
+  // photons that pass (third queue); their optical depths are walked by the
+  // walk kernel, one photon per thread, into the head queue
+  const bool ffp = c->ff_on && c->ff_mode == GG_FF_PRIMARY;
+  auto phantom_pass = [&](void *in_q, const unsigned long long *in_n) -> int {
+    if (!ffp) return stage_run(0, in_q, in_n, c->d_queue[0], nh);
+    int st2;
+    if ((st2 = stage_run(0, in_q, in_n, c->d_queue[2], nf))) return st2;
+    if ((st2 = c->cuda(cudaMemsetAsync(nh, 0, sizeof(unsigned long long), c->stream), "memset"))) return st2;
+    gg::StageArgs w{c->d_queue[2], nf, c->d_queue[0], nh, c->q_cap, nullptr, nullptr, 0};
+    if ((st2 = stage_event(c, 0, true))) return st2;
+    cudaError_t e = c->precision == GG_PREC_F64
+                        ? gg::launch_spect_walk<double>(c->scene<double>(), a, w, c->block, smem, c->n_sm, c->stream)
+                        : gg::launch_spect_walk<float>(c->scene<float>(), a, w, c->block, smem, c->n_sm, c->stream);
+    if ((st2 = c->cuda(e, "walk kernel launch"))) return st2;
+    return stage_event(c, 0, false);
+  };
+  const int per_phantom = ffp ? 2 : 1;
+  if ((st = phantom_pass(nullptr, nullptr))) return st;
   if ((st = head_pass())) return st;
-  c->last_stage_launches = per_pass;
+  c->last_stage_launches = per_pass + per_phantom - 1;
   for (int pass = 1;; ++pass) {
     unsigned long long back = 0;
     if ((st = c->cuda(cudaMemcpyAsync(&back, nr, sizeof(back), cudaMemcpyDeviceToHost, c->stream), "queue length")))
@@ -1177,9 +1195,9 @@ static int spect_stages(gg_ctx *c, gg::KernelArgs a, size_t smem, int minb) {
     // a photon re-enters the image at most once per phantom / head pass; the
     // per-photon step cap ends every history, so this loop ends too
     if (pass > 100000) return c->fail(GG_ERR_DOMAIN, "SPECT stages: photons keep returning to the image");
-    if ((st = stage_run(0, c->d_queue[1], nr, c->d_queue[0], nh))) return st;
+    if ((st = phantom_pass(c->d_queue[1], nr))) return st;
     if ((st = head_pass())) return st;
-    c->last_stage_launches += per_pass;
+    c->last_stage_launches += per_pass + per_phantom - 1;
   }
   return GG_OK;
 }
@@ -1246,13 +1264,15 @@ static int run_impl(gg_ctx *c, uint64_t n, uint64_t seed, uint64_t first, bool c
   // scatter splitting pushes several copies per history: a longer head queue
   // (the phantom passes adapt to it)
   const size_t q_need = c->ff_on && c->ff_mode == GG_FF_SCATTER ? std::max(cap, std::min(cap * 16, kSsQueueMax)) : cap;
-  if (c->have_spect && (q_need > c->q_cap || (c->arf_on && !c->d_queue[2]))) {
+  // the third queue: the ARF stage's fallback photons, and the walk queue of primary free flight
+  const bool q3 = c->arf_on || (c->ff_on && c->ff_mode == GG_FF_PRIMARY);
+  if (c->have_spect && (q_need > c->q_cap || (q3 && !c->d_queue[2]))) {
     for (int k = 0; k < 3; ++k) dfree(c->d_queue[k]);
     c->q_cap = 0;
     size_t qb = c->precision == GG_PREC_F64 ? gg::queue_bytes<double>(q_need) : gg::queue_bytes<float>(q_need);
     int st = c->cuda(cudaMalloc(&c->d_queue[0], qb), "cudaMalloc head queue");
     if (!st) st = c->cuda(cudaMalloc(&c->d_queue[1], qb), "cudaMalloc return queue");
-    if (!st && c->arf_on) st = c->cuda(cudaMalloc(&c->d_queue[2], qb), "cudaMalloc ARF fallback queue");
+    if (!st && q3) st = c->cuda(cudaMalloc(&c->d_queue[2], qb), "cudaMalloc ARF fallback / walk queue");
     if (!st && !c->d_qn) st = c->cuda(cudaMalloc(&c->d_qn, 3 * sizeof(unsigned long long)), "cudaMalloc queue lengths");
     if (st) return st;
     c->q_cap = q_need;
@@ -1274,7 +1294,7 @@ static int run_impl(gg_ctx *c, uint64_t n, uint64_t seed, uint64_t first, bool c
     if (st) return st;
     c->ev.push_back(e);
   }
-  gg::KernelArgs a;
+  gg::KernelArgs a{};
   a.seed = seed;
   a.next = c->d_next;
   a.acc_e = c->d_acc_e;
@@ -1289,6 +1309,7 @@ static int run_impl(gg_ctx *c, uint64_t n, uint64_t seed, uint64_t first, bool c
   a.rec_cap = c->rec_cap;
   a.refill_min = c->refill_min;
   a.interact_min = c->interact_min;
+  a.warp_flush = c->transport_kernel == GG_KERNEL_PHASED_WARP_FLUSH ? 1 : 0;
   int flush_grid = c->n_sm * 8;
   c->run_stage_launches = 0;
   c->stage_ms[0] = c->stage_ms[1] = c->stage_ms[2] = 0;
@@ -1388,7 +1409,7 @@ int gg_run(gg_ctx *c, uint64_t n, uint64_t seed, uint64_t first) {
 
 int gg_set_transport_kernel(gg_ctx *c, int32_t kind) {
   if (!c) return GG_ERR_ARG;
-  if (kind != GG_KERNEL_WAVEFRONT && kind != GG_KERNEL_PHASED)
+  if (kind != GG_KERNEL_WAVEFRONT && kind != GG_KERNEL_PHASED && kind != GG_KERNEL_PHASED_WARP_FLUSH)
     return c->fail(GG_ERR_ARG, "gg_set_transport_kernel: unknown kernel %d", kind);
   c->transport_kernel = kind;
   return GG_OK;
@@ -1414,6 +1435,23 @@ int gg_get_image(gg_ctx *c, int32_t which, double *out, size_t n) {
   int st = c->cuda(cudaMemcpyAsync(out, src, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream), "download");
   if (st) return st;
   return c->cuda(cudaStreamSynchronize(c->stream), "download");
+}
+
+int gg_get_image_device(gg_ctx *c, int32_t which, void **ptr, size_t *n) {
+  if (!c || !ptr || !n) return GG_ERR_ARG;
+  cudaSetDevice(c->device);
+  if (!c->have_tally) return c->fail(GG_ERR_STATE, "gg_get_image_device: no tally");
+  double *src = nullptr;
+  if (which == GG_IMG_EDEP) src = c->d_edep;
+  else if (which == GG_IMG_EDEP_SQUARED) src = c->squared ? c->d_edep2 : nullptr;
+  else if (which == GG_IMG_DOSE) src = c->dgrid_on && c->ddose ? c->d_dose : nullptr;
+  else if (which == GG_IMG_DOSE_SQUARED) src = c->dgrid_on && c->ddose && c->squared ? c->d_dose2 : nullptr;
+  if (!src) return c->fail(GG_ERR_ARG, "gg_get_image_device: image %d not scored", which);
+  int st = c->cuda(cudaStreamSynchronize(c->stream), "gg_get_image_device");
+  if (st) return st;
+  *ptr = src;
+  *n = c->n_tally;
+  return GG_OK;
 }
 
 void *gg_host_alloc(size_t bytes) {

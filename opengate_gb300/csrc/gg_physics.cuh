@@ -806,17 +806,125 @@ __device__ __forceinline__ void tle_path(const Scene<real> &s, const real p[3], 
 }
 
 // Optical depth of the straight path [p, p + len d) inside the image:
-// sum of mu(E, material) * length over the voxels it crosses.
-template <typename real>
+// sum of mu(E, material) * length over the voxels it crosses.  GROUP > 1:
+// the same walk (voxel_walk's arithmetic, step for step) in groups of GROUP
+// boundary crossings: the crossings of a group are computed first, then
+// their label gathers are issued together and the terms are added in walk
+// order, so up to GROUP loads are in flight per lane instead of one and the
+// sum is bit for bit voxel_walk's.
+template <typename real, int GROUP>
 __device__ __forceinline__ real image_depth(const Scene<real> &s, const real p[3], const real d[3], real len,
                                            const EIdx<real> &ei) {
   real tau = R<real>(0);
-  voxel_walk(s, p, d, len, [&](uint32_t, int m, real seg) {
-    real mu = interp_row(s.sig + (size_t)s.mat_comp[m] * s.n_e, ei);
-    mu = s.mat_rho[m] * mu;
-    mu = mu * seg;
-    tau = tau + mu;
-  });
+  if constexpr (GROUP == 1) {
+    voxel_walk(s, p, d, len, [&](uint32_t, int m, real seg) {
+      real mu = interp_row(s.sig + (size_t)s.mat_comp[m] * s.n_e, ei);
+      mu = s.mat_rho[m] * mu;
+      mu = mu * seg;
+      tau = tau + mu;
+    });
+  } else {
+    const int n0 = s.nx, n1 = s.ny, n2 = s.nz;
+    int i0 = (int)((p[0] - s.bmin[0]) * s.inv_sp[0]);
+    int i1 = (int)((p[1] - s.bmin[1]) * s.inv_sp[1]);
+    int i2 = (int)((p[2] - s.bmin[2]) * s.inv_sp[2]);
+    i0 = i0 < 0 ? 0 : (i0 >= n0 ? n0 - 1 : i0);
+    i1 = i1 < 0 ? 0 : (i1 >= n1 ? n1 - 1 : i1);
+    i2 = i2 < 0 ? 0 : (i2 >= n2 ? n2 - 1 : i2);
+    const real inf = gg_inf(real(0));
+    real tn[3] = {inf, inf, inf}, td[3] = {inf, inf, inf};
+    int st[3] = {0, 0, 0};
+    const int ii[3] = {i0, i1, i2};
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      const real da = d[a];
+      if (da > R<real>(0)) {
+        real b = (real)(ii[a] + 1) * s.sp[a];
+        b = s.bmin[a] + b;
+        b = b - p[a];
+        tn[a] = b / da;
+        td[a] = s.sp[a] / da;
+        st[a] = 1;
+      } else if (da < R<real>(0)) {
+        real b = (real)ii[a] * s.sp[a];
+        b = s.bmin[a] + b;
+        b = b - p[a];
+        tn[a] = b / da;
+        td[a] = -s.sp[a];
+        td[a] = td[a] / da;
+        st[a] = -1;
+      }
+      if (tn[a] < R<real>(0)) tn[a] = R<real>(0);
+    }
+    real tn0 = tn[0], tn1 = tn[1], tn2 = tn[2];
+    const real td0 = td[0], td1 = td[1], td2 = td[2];
+    const int s0 = st[0], s1 = st[1], s2 = st[2];
+    real tc = R<real>(0);
+    const int cap = n0 + n1 + n2 + 3;
+    int k = 0;
+    bool go = true;
+    while (go) {
+      uint32_t vv[GROUP];
+      real sg[GROUP];
+      bool ok[GROUP];
+#pragma unroll
+      for (int j = 0; j < GROUP; ++j) {
+        ok[j] = false;
+        vv[j] = 0u;
+        sg[j] = R<real>(0);
+        if (go && k < cap) {
+          int a;
+          real tb;
+          if (tn1 < tn0) {
+            if (tn2 < tn1) a = 2, tb = tn2;
+            else a = 1, tb = tn1;
+          } else {
+            if (tn2 < tn0) a = 2, tb = tn2;
+            else a = 0, tb = tn0;
+          }
+          const real te = tb < len ? tb : len;
+          const real seg = te - tc;
+          if (seg > R<real>(0)) {
+            vv[j] = (uint32_t)i0 + (uint32_t)n0 * ((uint32_t)i1 + (uint32_t)n1 * (uint32_t)i2);
+            sg[j] = seg;
+            ok[j] = true;
+          }
+          tc = te;
+          ++k;
+          if (!(tc < len)) {
+            go = false;
+          } else if (a == 0) {
+            i0 += s0;
+            if (i0 < 0 || i0 >= n0) go = false;
+            tn0 = tn0 + td0;
+          } else if (a == 1) {
+            i1 += s1;
+            if (i1 < 0 || i1 >= n1) go = false;
+            tn1 = tn1 + td1;
+          } else {
+            i2 += s2;
+            if (i2 < 0 || i2 >= n2) go = false;
+            tn2 = tn2 + td2;
+          }
+        } else {
+          go = false;
+        }
+      }
+      int lab[GROUP];
+#pragma unroll
+      for (int j = 0; j < GROUP; ++j) lab[j] = ok[j] ? (int)__ldg(s.labels + vv[j]) : 0;
+#pragma unroll
+      for (int j = 0; j < GROUP; ++j) {
+        if (ok[j]) {
+          const int m = lab[j];
+          real mu = interp_row(s.sig + (size_t)s.mat_comp[m] * s.n_e, ei);
+          mu = s.mat_rho[m] * mu;
+          mu = mu * sg[j];
+          tau = tau + mu;
+        }
+      }
+    }
+  }
   return tau;
 }
 

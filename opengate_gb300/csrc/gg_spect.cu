@@ -50,8 +50,11 @@ __device__ __forceinline__ int phantom_flight(const Scene<real> &s, Photon<real>
     return kRefill;
   }
   if constexpr (FFM == kFfPrimary) {  // free flight to a head: no interaction outside the heads
+    // the checks here (cutoffs, angle, the head the line enters); the optical
+    // depth of the photons that pass is walked by k_spect_walk, with full warps
     ++n_world;
-    if (ff_flight(s, ph, s.ss_cos)) return kPush;
+    real tb;
+    if (ff_target(s, ph, s.ss_cos, tb)) return kPush;
     atomicAdd(&bc->escaped, 1u);
     return kRefill;
   }
@@ -233,10 +236,15 @@ __global__ void __launch_bounds__(256) k_spect_split(Scene<real> sg, KernelArgs 
   stage_counters(args.counters, bc, lane, 0u, 0u, n_world, 0u, 0u);
 }
 
-// Scatter splitting, the free flights of the copies that passed the split
-// kernel's checks: the whole ff_flight (its first part again, bit for bit the
-// same, then the optical depth along the line), one copy per thread; copies
-// that reach their head go to the head queue.
+// Label gathers in flight per lane in the walk kernel's optical depths.
+constexpr int kWalkGroup = 8;
+
+// Free flights that passed their checks (the copies of scatter splitting
+// after the split kernel, the photons of primary free flight after the
+// phantom stage): the whole ff_flight (its first part again, bit for bit the
+// same, then the optical depth along the line), one photon per thread, so a
+// warp walks 32 lines at once instead of one line among lanes that have
+// finished; photons that reach their head go to the head queue.
 template <typename real>
 __global__ void __launch_bounds__(256) k_spect_walk(Scene<real> sg, KernelArgs args, StageArgs q) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -253,17 +261,21 @@ __global__ void __launch_bounds__(256) k_spect_walk(Scene<real> sg, KernelArgs a
     Photon<real> cp;
     Rng g;
     uint64_t hid = 0;
-    bool push = false;
+    bool push = false, has_ev = false;
     if (i < n) {
-      bool has_ev;
       hid = queue_get<real, true>(s, in, i, cp, g, args.seed, has_ev);
-      push = ff_flight(s, cp, s.ss_cos) != 0;
+      push = ff_flight<real, kWalkGroup>(s, cp, s.ss_cos) != 0;
       if (!push) atomicAdd(&bc.escaped, 1u);
     }
     const size_t k = queue_claim(q.out_n, push, lane, lt_mask);
-    if (push && k < q.q_cap) {
-      real v[kEvSlots];
-      queue_put<real, true>(out, k, cp, g, hid, v, false);
+    if (push) {
+      if (k < q.q_cap) {
+        real v[kEvSlots];
+        if (has_ev) load_event(in, i, v);
+        queue_put<real, true>(out, k, cp, g, hid, v, has_ev);
+      } else {
+        atomicOr(args.status, kStatusQueueOverflow);
+      }
     }
   }
   stage_counters(args.counters, bc, lane, 0u, 0u, 0u, 0u, 0u);

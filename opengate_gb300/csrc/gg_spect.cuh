@@ -359,7 +359,12 @@ __device__ __forceinline__ int ff_target(const Scene<real> &s, Photon<real> &ph,
   return box;
 }
 
-template <typename real>
+// Optical depth of a straight path through the image (gg_physics.cuh).
+template <typename real, int GROUP = 1>
+__device__ __forceinline__ real image_depth(const Scene<real> &s, const real p[3], const real d[3], real len,
+                                           const EIdx<real> &ei);
+
+template <typename real, int GROUP = 1>
 __device__ __forceinline__ int ff_flight(const Scene<real> &s, Photon<real> &ph, real cos_min) {
   real tb;
   const int box = ff_target(s, ph, cos_min, tb);
@@ -377,7 +382,7 @@ __device__ __forceinline__ int ff_flight(const Scene<real> &s, Photon<real> &ph,
     real lin = exit_distance(p0, ph.dir, s.bmin, s.bmax);
     const real rest = tb - t0;
     lin = lin < rest ? lin : rest;
-    tau = image_depth(s, p0, ph.dir, lin, ph.ei);
+    tau = image_depth<real, GROUP>(s, p0, ph.dir, lin, ph.ei);
     l_air = l_air - lin;
   }
   real ta = mu_air * l_air;

@@ -50,7 +50,8 @@ class DoseEngine:
         self._call("gg_reset_tally")
 
     def set_transport_kernel(self, kind):
-        """C.GG_KERNEL_PHASED (default) or C.GG_KERNEL_WAVEFRONT: same results, different speed."""
+        """C.GG_KERNEL_PHASED (default), C.GG_KERNEL_PHASED_WARP_FLUSH or C.GG_KERNEL_WAVEFRONT:
+        same results, different speed."""
         self._call("gg_set_transport_kernel", int(kind))
 
     def set_tle(self, threshold_energy=float("inf"), energy_min=0.0, database="EPDL", enabled=True):
@@ -109,6 +110,13 @@ class DoseEngine:
 
     def edep_squared(self, out=None):
         return self.image(C.GG_IMG_EDEP_SQUARED, out)
+
+    def image_device(self, which):
+        """(device pointer, voxels) of an FP64 image on the context's device
+        (gg_get_image_device): valid until the next run, reset or close."""
+        ptr, n = ctypes.c_void_p(), ctypes.c_size_t()
+        self._call("gg_get_image_device", int(which), ctypes.byref(ptr), ctypes.byref(n))
+        return ptr.value, n.value
 
     def pinned_empty(self, shape, dtype=np.float64):
         """Uninitialised array in page-locked host memory (gg_host_alloc), freed with the

@@ -73,3 +73,45 @@ def test_two_rank_gloo_merge_equals_single_run():
     assert total == n == c0["histories"] + c1["histories"]
     np.testing.assert_array_equal(m_edep, e0 + e1)
     np.testing.assert_array_equal(m_edep2, q0 + q1)
+
+
+def test_device_merge_without_process_group_is_identity():
+    """merge_tallies_device leaves the images alone and returns the rank's count when
+    no process group is up (a single replica)."""
+
+    class NoImages:
+        def image_device(self, which):
+            raise AssertionError("no device image may be touched")
+
+    assert Rp.merge_tallies_device(NoImages(), (0, 1), 1234) == 1234
+
+
+def _gloo_device_merge(rank, world, port, q):
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank), WORLD_SIZE=str(world))
+    import torch.distributed as dist
+
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        Rp.merge_tallies_device(object(), (0,), 10)
+        q.put((rank, "no error"))
+    except RuntimeError as e:
+        q.put((rank, str(e)))
+    dist.destroy_process_group()
+
+
+def test_device_merge_refuses_gloo():
+    """The device merge runs NCCL collectives on device buffers; under gloo it refuses
+    (the host merge, merge_tallies, is the one for CPU process groups)."""
+    import multiprocessing as mp
+
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_gloo_device_merge, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    got = dict(q.get(timeout=120) for _ in range(2))
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    assert all("nccl" in m for m in got.values()), got
