@@ -968,6 +968,7 @@ def run_ours_batched(args, ws, rank, local, dist, use_cuda):
     t0 = time.perf_counter()
     best = eng.autotune()
     tune_s = time.perf_counter() - t0
+    tune = eng.autotune_result()
     eng.capture()
     l2_flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=f"cuda:{local}")
 
@@ -1033,9 +1034,13 @@ def run_ours_batched(args, ws, rank, local, dist, use_cuda):
             "config": {"workload": BATCH_WORKLOAD, "simulations": len(sims), "primaries_per_step": n,
                        "voxels": int(sum(s.n_voxels for s, _, _ in sims)),
                        "l2": "flushed between steps (256 MiB write)",
-                       "launch": "CUDA graph replay of the batch (source, transport, flush per batch)",
+                       "launch": "CUDA graph replay; per batch one source launch, one persistent transport "
+                                 "launch taking the histories of all simulations from one device work counter "
+                                 "(in-kernel binding of each history's simulation), one flush launch",
                        "autotuned": {"blocks_per_sm": best.blocks_per_sm, "refill_min": best.refill_min,
-                                     "interact_min": best.interact_min, "seconds": tune_s},
+                                     "interact_min": best.interact_min, "claim_chunk": best.chunk,
+                                     "batch_length": int(best.batch), "block_size": best.block_size,
+                                     "search": tune, "seconds": tune_s},
                        "parallelism": f"replicas x{ws}, independent batches"},
             "sequential": {"primaries_per_s": n / (seq_ms / 1e3), "note": "gg_run per simulation, same context"},
             "e2e": {"value": ws * n / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),

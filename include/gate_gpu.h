@@ -202,6 +202,19 @@ typedef struct {
   int32_t n_heads;             /* 1 or 2 */
   int32_t n_runs;              /* gantry positions; projection slice = window + run * n_windows */
   int32_t adder_policy;        /* GG_ADDER_WINNER (0) or GG_ADDER_CENTROID: position of a single */
+  /* Head housing (replaces the shielding box of add_spect_box,
+     contrib/spect/ge_discovery_nm670.py:215-262): slabs across the head's
+     width, an entrance cover between the gap and the crystal and up to four
+     layers behind the crystal (reflector, back compartment, lead cover and
+     steel shielding backs), outwards from the crystal; interactions there
+     are tracked like the collimator's, deposits outside the crystal are not
+     scored.  No layers (all zero): collimator, gap and crystal only. */
+  int32_t n_cover;             /* 0 or 1 */
+  double cover_thickness;      /* mm */
+  int32_t cover_material;      /* material table index */
+  int32_t n_back;              /* 0..4 */
+  double back_thickness[4];    /* mm, from the crystal outwards */
+  int32_t back_material[4];
 } gg_spect_desc;
 /* adder policies (GateDigiAdderInVolume, digitizer/GateDigiAdderInVolume.cpp:29-88) */
 #define GG_ADDER_WINNER 0   /* EnergyWinnerPosition: the largest deposit's point */
@@ -243,7 +256,6 @@ typedef struct {
    kernel).  Both give identical results; they differ in speed only. */
 #define GG_KERNEL_WAVEFRONT 0 /* per-block wavefront compacted by event type */
 #define GG_KERNEL_PHASED 1    /* block-synchronous phases, one history per thread (default) */
-#define GG_KERNEL_PHASED_WARP_FLUSH 2 /* the same, same-voxel tally entries of a warp summed before their atomics */
 
 int gg_create(const gg_device_opts *opts, gg_ctx **out);
 int gg_destroy(gg_ctx *ctx);
@@ -535,9 +547,15 @@ int gg_get_arf_projection(gg_ctx *ctx, double *counts, double *squared, size_t n
    gg_batch_capture records the launch sequence of one gg_batch_run in a CUDA
    graph and gg_batch_replay replays it (the same histories again, images
    accumulate: call gg_reset_tally between replays to repeat a step).
-   gg_batch_autotune times gg_batch_run for a few launch configurations
-   (blocks per SM, refill / interaction thresholds) and keeps the fastest in
-   the context (*best, may be NULL); images are reset afterwards.
+   gg_batch_autotune searches the launch configuration of the one persistent
+   transport launch that takes the histories of all simulations from one
+   device work counter: first blocks per SM x refill / interaction thresholds,
+   then, at the best of those, the per-warp claim chunk x the batch length
+   (histories per generate / transport / flush sequence).  Every point is
+   timed as the median of three gg_batch_run calls; the fastest stays in the
+   context (*best, may be NULL) and gg_batch_autotune_result reports the
+   search (points timed, the winner's median / min / max); images are reset
+   afterwards.
    gg_batch_get_image returns simulation `sim`'s image (its n voxels). */
 typedef struct {
   gg_volume_desc volume;
@@ -551,6 +569,14 @@ int gg_batch_run(gg_ctx *ctx);
 int gg_batch_capture(gg_ctx *ctx);
 int gg_batch_replay(gg_ctx *ctx);
 int gg_batch_autotune(gg_ctx *ctx, gg_device_opts *best);
+typedef struct {
+  int32_t points;      /* configurations timed */
+  int32_t repeats;     /* timings per configuration (median taken) */
+  double median_ms;    /* the chosen configuration: median device time of gg_batch_run */
+  double min_ms, max_ms;
+  double default_median_ms; /* the configuration the context had before the search */
+} gg_autotune_result;
+int gg_batch_autotune_result(gg_ctx *ctx, gg_autotune_result *out);
 int gg_batch_get_image(gg_ctx *ctx, int32_t sim, int32_t which, double *out, size_t n);
 
 /* ---- dose run that allocates no device memory ------------------------------

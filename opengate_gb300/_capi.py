@@ -25,7 +25,7 @@ STATUS_NAMES = {0: "GG_OK", 1: "GG_ERR_ARG", 2: "GG_ERR_CUDA", 3: "GG_ERR_QUEUE_
 
 GG_PREC_F32 = 32
 GG_PREC_F64 = 64
-GG_KERNEL_WAVEFRONT, GG_KERNEL_PHASED, GG_KERNEL_PHASED_WARP_FLUSH = 0, 1, 2
+GG_KERNEL_WAVEFRONT, GG_KERNEL_PHASED = 0, 1
 GG_POS_POINT, GG_POS_BOX, GG_POS_SPHERE, GG_POS_DISC, GG_POS_VOXELS = 0, 1, 2, 3, 4
 GG_DIR_ISO, GG_DIR_MOMENTUM, GG_DIR_FOCUSED = 0, 1, 2
 GG_ENE_MONO, GG_ENE_LINES, GG_ENE_HISTOGRAM, GG_ENE_RANGE = 0, 1, 2, 3
@@ -123,6 +123,8 @@ class SpectDesc(ctypes.Structure):
         ("n_windows", ctypes.c_int32), ("window_lo", ctypes.c_double * 8), ("window_hi", ctypes.c_double * 8),
         ("size", ctypes.c_int32 * 2), ("spacing", ctypes.c_double * 2), ("n_heads", ctypes.c_int32),
         ("n_runs", ctypes.c_int32), ("adder_policy", ctypes.c_int32),
+        ("n_cover", ctypes.c_int32), ("cover_thickness", ctypes.c_double), ("cover_material", ctypes.c_int32),
+        ("n_back", ctypes.c_int32), ("back_thickness", ctypes.c_double * 4), ("back_material", ctypes.c_int32 * 4),
     ]
 
 
@@ -189,6 +191,11 @@ class DeviceOpts(ctypes.Structure):
     ]
 
 
+class AutotuneResult(ctypes.Structure):
+    _fields_ = [("points", ctypes.c_int32), ("repeats", ctypes.c_int32), ("median_ms", ctypes.c_double),
+                ("min_ms", ctypes.c_double), ("max_ms", ctypes.c_double), ("default_median_ms", ctypes.c_double)]
+
+
 def ptr(arr, ctype):
     """Pointer to a contiguous numpy array (the caller keeps ``arr`` alive)."""
     if arr is None:
@@ -243,6 +250,7 @@ PROTOTYPES = [
     ("gg_batch_capture", ctypes.c_int, [ctypes.c_void_p]),
     ("gg_batch_replay", ctypes.c_int, [ctypes.c_void_p]),
     ("gg_batch_autotune", ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(DeviceOpts)]),
+    ("gg_batch_autotune_result", ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(AutotuneResult)]),
     ("gg_batch_get_image", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, _f64p, ctypes.c_size_t]),
     ("gg_spect_use_arf", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32]),
     ("gg_last_stage_ms", ctypes.c_int, [ctypes.c_void_p, _f64p, _f64p, _f64p]),

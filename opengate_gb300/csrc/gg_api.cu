@@ -164,6 +164,7 @@ struct gg_ctx {
   int n_sims = 0;
   std::vector<uint64_t> sim_vox_off, sim_vox_n;
   uint64_t batch_total = 0;
+  gg_autotune_result tune{};  // last gg_batch_autotune search
   void *d_sims = nullptr, *d_sim_maj = nullptr;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t graph_exec = nullptr;
@@ -1309,7 +1310,6 @@ static int run_impl(gg_ctx *c, uint64_t n, uint64_t seed, uint64_t first, bool c
   a.rec_cap = c->rec_cap;
   a.refill_min = c->refill_min;
   a.interact_min = c->interact_min;
-  a.warp_flush = c->transport_kernel == GG_KERNEL_PHASED_WARP_FLUSH ? 1 : 0;
   int flush_grid = c->n_sm * 8;
   c->run_stage_launches = 0;
   c->stage_ms[0] = c->stage_ms[1] = c->stage_ms[2] = 0;
@@ -1409,7 +1409,7 @@ int gg_run(gg_ctx *c, uint64_t n, uint64_t seed, uint64_t first) {
 
 int gg_set_transport_kernel(gg_ctx *c, int32_t kind) {
   if (!c) return GG_ERR_ARG;
-  if (kind != GG_KERNEL_WAVEFRONT && kind != GG_KERNEL_PHASED && kind != GG_KERNEL_PHASED_WARP_FLUSH)
+  if (kind != GG_KERNEL_WAVEFRONT && kind != GG_KERNEL_PHASED)
     return c->fail(GG_ERR_ARG, "gg_set_transport_kernel: unknown kernel %d", kind);
   c->transport_kernel = kind;
   return GG_OK;
@@ -2061,20 +2061,43 @@ int gg_batch_autotune(gg_ctx *c, gg_device_opts *best) {
   if (!c) return GG_ERR_ARG;
   cudaSetDevice(c->device);
   if (!c->have_batch || !c->have_tally) return c->fail(GG_ERR_STATE, "gg_batch_autotune: call gg_batch_setup first");
+  constexpr int kRep = 3;
+  int st = GG_OK;
+  // median / min / max of kRep device timings of the current configuration
+  auto time_point = [&](double stats[3]) -> int {
+    double t[kRep];
+    for (int r = 0; r < kRep; ++r) {
+      int s2;
+      if ((s2 = gg_reset_tally(c)) || (s2 = gg_batch_run(c))) return s2;
+      t[r] = c->last_generate_ms + c->last_transport_ms + c->last_flush_ms;
+    }
+    std::sort(t, t + kRep);
+    stats[0] = t[kRep / 2];
+    stats[1] = t[0];
+    stats[2] = t[kRep - 1];
+    ++c->tune.points;
+    return GG_OK;
+  };
+  c->tune = gg_autotune_result{};
+  c->tune.repeats = kRep;
+  double cur[3];
+  if ((st = time_point(cur))) return st;
+  c->tune.default_median_ms = cur[0];
+  double bst[3] = {cur[0], cur[1], cur[2]};
+  int bm = c->blocks_per_sm, br = c->refill_min, bi = c->interact_min, bc = c->chunk;
+  int64_t bb = c->batch;
+  // stage 1: resident blocks per SM x phase thresholds
   const int minbs[3] = {2, 3, 4};
   const int thresholds[3][2] = {{8, 16}, {4, 8}, {12, 24}};
-  double best_ms = 1e300;
-  int bm = c->blocks_per_sm, br = c->refill_min, bi = c->interact_min;
-  int st;
   for (int a = 0; a < 3; ++a)
     for (int b = 0; b < 3; ++b) {
       c->blocks_per_sm = minbs[a];
       c->refill_min = thresholds[b][0];
       c->interact_min = thresholds[b][1];
-      if ((st = gg_reset_tally(c)) || (st = gg_batch_run(c))) return st;
-      const double ms = c->last_generate_ms + c->last_transport_ms + c->last_flush_ms;
-      if (ms < best_ms) {
-        best_ms = ms;
+      double t[3];
+      if ((st = time_point(t))) return st;
+      if (t[0] < bst[0]) {
+        std::copy(t, t + 3, bst);
         bm = minbs[a];
         br = thresholds[b][0];
         bi = thresholds[b][1];
@@ -2083,19 +2106,54 @@ int gg_batch_autotune(gg_ctx *c, gg_device_opts *best) {
   c->blocks_per_sm = bm;
   c->refill_min = br;
   c->interact_min = bi;
+  // stage 2: per-warp claim chunk x batch length (all histories in one
+  // generate / transport / flush sequence, or in 2 or 4)
+  const int chunks[3] = {64, 256, 1024};
+  const uint64_t tot = c->batch_total;
+  const int64_t batches[3] = {(int64_t)tot, (int64_t)((tot + 1) / 2), (int64_t)((tot + 3) / 4)};
+  const int64_t batch0 = c->batch;
+  const int chunk0 = c->chunk;
+  for (int a = 0; a < 3; ++a)
+    for (int b = 0; b < 3; ++b) {
+      c->chunk = chunks[a];
+      c->batch = std::max<int64_t>(1, batches[b]);
+      double t[3];
+      if ((st = time_point(t))) return st;
+      if (t[0] < bst[0]) {
+        std::copy(t, t + 3, bst);
+        bc = chunks[a];
+        bb = c->batch;
+      }
+    }
+  if (bst[0] >= c->tune.default_median_ms) {  // nothing beat the starting point
+    bc = chunk0;
+    bb = batch0;
+  }
+  c->chunk = bc;
+  c->batch = bb;
+  c->tune.median_ms = bst[0];
+  c->tune.min_ms = bst[1];
+  c->tune.max_ms = bst[2];
   drop_graph(c);
   if ((st = gg_reset_tally(c))) return st;
   if (best) {
     best->device = c->device;
     best->precision = c->precision;
     best->block_size = c->block;
-    best->blocks_per_sm = bm;
+    best->blocks_per_sm = c->blocks_per_sm;
     best->chunk = c->chunk;
     best->batch = (int64_t)c->batch;
-    best->refill_min = br;
-    best->interact_min = bi;
+    best->refill_min = c->refill_min;
+    best->interact_min = c->interact_min;
   }
   return c->cuda(cudaStreamSynchronize(c->stream), "autotune");
+}
+
+int gg_batch_autotune_result(gg_ctx *c, gg_autotune_result *out) {
+  if (!c || !out) return GG_ERR_ARG;
+  if (c->tune.points == 0) return c->fail(GG_ERR_STATE, "gg_batch_autotune_result: no search has run");
+  *out = c->tune;
+  return GG_OK;
 }
 
 int gg_batch_get_image(gg_ctx *c, int32_t sim, int32_t which, double *out, size_t n) {

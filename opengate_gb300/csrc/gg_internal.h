@@ -44,7 +44,6 @@ struct KernelArgs {
   int interact_min;                 // pending collisions that trigger an interaction phase
   unsigned long long *acc_d;        // dose grid: fixed-point sum(edep * rho_min / rho) (or null)
   unsigned long long *acc_d2;       // its history-by-history squares (or null)
-  int warp_flush;                   // phase kernel: warp-aggregated tally flush (hlist_flush_warp)
 };
 
 // Bit of the kernel status word set when a stage queue overflowed (the low

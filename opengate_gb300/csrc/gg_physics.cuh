@@ -61,56 +61,6 @@ __device__ __forceinline__ void hlist_flush(HistList<real> &l, const Tally<real>
   l.n = 0;
 }
 
-// hlist_flush for a whole warp (all 32 lanes call it, converged; `has`: the
-// lane holds a list): entries of the same tally voxel in the warp are summed
-// by their group's first lane, which then issues the three atomics once.  The
-// sums are exact integer sums of the same per-entry terms, so the tallies are
-// identical to hlist_flush's.
-template <typename real>
-__device__ __forceinline__ void hlist_flush_warp(HistList<real> &l, bool has, const Tally<real> &t,
-                                                 BlockCounters *bc) {
-  const unsigned lane = threadIdx.x & 31u;
-#pragma unroll
-  for (int k = 0; k < kHistList; ++k) {
-    const bool valid = has && k < l.n;
-    if (!__any_sync(0xffffffffu, valid)) break;  // lists fill from entry 0
-    const uint32_t v = valid ? l.vox[k] : 0u;
-    const unsigned long long q = valid ? (unsigned long long)to_fixed(l.acc[k]) : 0ull;
-    const unsigned long long lo = q * q;
-    const unsigned long long hi = __umul64hi(q, q);
-    const unsigned long long e2lo = lo & 0xffffffffull, e2hi = (hi << 32) | (lo >> 32);
-    // grouped by tally address (batched simulations bind different tallies per lane)
-    const unsigned long long addr = valid ? (unsigned long long)(uintptr_t)(t.acc_e + v) : ~0ull;
-    const unsigned grp = __match_any_sync(0xffffffffu, addr);
-    const int leader = __ffs(grp) - 1;
-    const int gmax = (int)__reduce_max_sync(0xffffffffu, valid ? (unsigned)__popc(grp) : 0u);
-    unsigned long long sq = q, slo = e2lo, shi = e2hi;
-    unsigned rest = grp & ~(1u << lane);
-    for (int j = 1; j < gmax; ++j) {
-      const bool take = (int)lane == leader && rest != 0u;
-      const int src = take ? __ffs(rest) - 1 : (int)lane;
-      const unsigned long long a = __shfl_sync(0xffffffffu, q, src);
-      const unsigned long long b = __shfl_sync(0xffffffffu, e2lo, src);
-      const unsigned long long c = __shfl_sync(0xffffffffu, e2hi, src);
-      if (take) {
-        sq += a;
-        slo += b;
-        shi += c;
-        rest &= rest - 1u;
-      }
-    }
-    if (valid && (int)lane == leader) {
-      atomicAdd(&t.acc_e[v], sq);
-      if (t.acc_e2) {
-        atomicAdd(&t.acc_e2[2 * (size_t)v], slo);
-        atomicAdd(&t.acc_e2[2 * (size_t)v + 1], shi);
-      }
-    }
-  }
-  if (has && l.n) atomicAdd(&bc->tally_entries, (unsigned int)l.n);
-  if (has) l.n = 0;
-}
-
 template <typename real>
 __device__ __forceinline__ void deposit(HistList<real> &l, const Tally<real> &t, BlockCounters *bc,
                                         uint32_t v, real e, unsigned int &n_dep) {

@@ -261,13 +261,10 @@ __global__ void __launch_bounds__(256, MINB) k_transport(Scene<real> sg, KernelA
       if constexpr (SPECT) {
         if (need && in_hist) n_singles += score_singles(s, ev, ph.run, g);
       } else {
-        // every lane of the warp is here.  Per-lane atomics by default; the warp-aggregated
-        // flush (same-voxel entries summed across the warp first) is selectable: with rare
-        // same-voxel collisions its match / shuffle rounds cost more than the atomics saved
-        if (args.warp_flush) {
-          hlist_flush_warp(l, need && in_hist, t, &bc);
-          if constexpr (DG == 2) hlist_flush_warp(ld, need && in_hist, td, &bcd);
-        } else if (need && in_hist) {
+        // per-lane atomics: a warp-aggregated flush (same-voxel entries of the warp summed
+        // first, __match_any_sync + shuffles) issued as many atomic instructions here and
+        // made the transport 28 % slower, so it is not used
+        if (need && in_hist) {
           hlist_flush(l, t, &bc);
           if constexpr (DG == 2) hlist_flush(ld, td, &bcd);
         }

@@ -50,8 +50,7 @@ class DoseEngine:
         self._call("gg_reset_tally")
 
     def set_transport_kernel(self, kind):
-        """C.GG_KERNEL_PHASED (default), C.GG_KERNEL_PHASED_WARP_FLUSH or C.GG_KERNEL_WAVEFRONT:
-        same results, different speed."""
+        """C.GG_KERNEL_PHASED (default) or C.GG_KERNEL_WAVEFRONT: same results, different speed."""
         self._call("gg_set_transport_kernel", int(kind))
 
     def set_tle(self, threshold_energy=float("inf"), energy_min=0.0, database="EPDL", enabled=True):
@@ -384,9 +383,17 @@ class BatchEngine:
         self._call("gg_batch_replay")
 
     def autotune(self):
+        """Searches the launch configuration (gg_batch_autotune); returns the chosen options."""
         best = C.DeviceOpts()
         self._call("gg_batch_autotune", ctypes.byref(best))
         return best
+
+    def autotune_result(self):
+        """The last search: points timed, repeats per point, the winner's median / min / max
+        device ms and the starting configuration's median."""
+        r = C.AutotuneResult()
+        self._call("gg_batch_autotune_result", ctypes.byref(r))
+        return {k: getattr(r, k) for k, _ in r._fields_}
 
     def reset(self):
         self._call("gg_reset_tally")

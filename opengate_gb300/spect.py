@@ -71,6 +71,9 @@ class SpectSpec:
         self.blur = C.BlurDesc()
         # free flight outside the heads (set_free_flight); off by default
         self.free_flight = C.FfDesc(C.FF_OFF, -1.0, 0.0, 0, 0, 0, 0.0)
+        # housing slabs (set_housing); none by default
+        self.cover = None
+        self.back = []
 
     def set_energy_blur(self, method, sigma=0.0, resolution=0.0, reference=0.0, slope=0.0):
         """DigitizerBlurringActor on the singles' energy (MeV): method "Gaussian" (sigma),
@@ -144,7 +147,32 @@ class SpectSpec:
         if self.adder_policy not in C.ADDER_POLICIES:
             raise NotImplementedError(f"adder policy '{self.adder_policy}'")
         d.adder_policy = C.ADDER_POLICIES[self.adder_policy]
+        if self.cover is not None:
+            d.n_cover = 1
+            d.cover_thickness, d.cover_material = float(self.cover[0]), int(self.cover[1])
+        d.n_back = len(self.back)
+        for k, (t, m) in enumerate(self.back):
+            d.back_thickness[k], d.back_material[k] = float(t), int(m)
         return d
+
+    def set_housing(self, cover=None, back=()):
+        """Head housing slabs (ge_discovery_nm670.py:215-262): ``cover`` = (thickness mm,
+        material index) between the gap and the crystal, ``back`` = up to four (thickness mm,
+        material index) layers behind the crystal, outwards.  Indices into the scene's
+        material table."""
+        back = [(float(t), int(m)) for t, m in back]
+        if len(back) > 4:
+            raise ValueError("at most four layers behind the crystal")
+        for t, _ in ([cover] if cover is not None else []) + back:
+            if not t > 0:
+                raise ValueError("housing layers need a positive thickness")
+        self.cover = None if cover is None else (float(cover[0]), int(cover[1]))
+        self.back = back
+
+    def housing_depth(self):
+        """Depth of the head box behind the collimator front face (mm)."""
+        return (self.collimator_thickness + self.gap + (self.cover[0] if self.cover else 0.0) +
+                self.crystal_thickness + sum(t for t, _ in self.back))
 
     def angle(self, run, head):
         if self.head_start is not None:

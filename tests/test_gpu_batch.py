@@ -71,7 +71,11 @@ def test_graph_replay_and_autotune_keep_results():
         b.replay()  # replays accumulate
         np.testing.assert_array_equal(_images(b, 0)[0], 2 * ref[0][0])
         best = b.autotune()
-        assert best.blocks_per_sm in (2, 3, 4)
+        assert best.blocks_per_sm in (2, 3, 4) and best.chunk in (64, 256, 1024)
+        res = b.autotune_result()
+        assert res["points"] == 19 and res["repeats"] == 3
+        assert res["min_ms"] <= res["median_ms"] <= res["max_ms"]
+        assert res["median_ms"] <= res["default_median_ms"]
         b.run()
         for k in range(len(sims)):
             np.testing.assert_array_equal(_images(b, k)[0], ref[k][0])

@@ -172,22 +172,20 @@ def test_images_into_pinned_buffers(lib):
 
 @pytest.mark.parametrize("precision", [32, 64])
 def test_wavefront_and_phase_kernels_agree(lib, precision):
-    """The block-phase kernel (default), the same with the warp-aggregated tally flush, and
-    the compacted wavefront kernel run the same histories to the same edep, edep^2 and
-    counters, on the CT phantom with its field source (acceptance loop, air gaps, pair
-    production above 1.022 MeV)."""
+    """The block-phase kernel (default) and the compacted wavefront kernel run the same
+    histories to the same edep, edep^2 and counters, on the CT phantom with its field
+    source (acceptance loop, air gaps, pair production above 1.022 MeV)."""
     from opengate_gb300.engine import DoseEngine
 
     sc = small_ct()
     n = 40000 if precision == 32 else 8000
     out = []
-    for kernel in (C.GG_KERNEL_PHASED, C.GG_KERNEL_PHASED_WARP_FLUSH, C.GG_KERNEL_WAVEFRONT):
+    for kernel in (C.GG_KERNEL_PHASED, C.GG_KERNEL_WAVEFRONT):
         with DoseEngine(sc, precision=precision, batch=15000) as eng:
             eng.set_transport_kernel(kernel)
             eng.run(n, 2468, 17)
             out.append((eng.edep(), eng.edep_squared(), eng.counters()))
     _assert_same(out[0], out[1])
-    _assert_same(out[0], out[2])
     assert out[0][2]["secondaries"] > 0 and out[0][2]["real_interactions"] > n
 
 
