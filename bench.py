@@ -41,7 +41,8 @@ WORKLOAD = "ct_phantom_256x256x160_1.2mm_ssd100_field10x10_spectrum60_0.1-6MeV"
 SPECT_METRIC = "primaries/s at matched sigma (plain GPU collimator tracking, SPECT projections)"
 SPECT_DECAYS = 1_000_000_000
 SPECT_YIELD = 0.89
-SPECT_WORKLOAD = ("spect_tc99m_lehr_2heads_60angles_r250mm_128x128x4.42mm_windows126-154_108-126keV_"
+SPECT_HOUSING = "nm670"  # the NM670 shielding box: cover, reflector, back compartment, lead / steel, shielded sides
+SPECT_WORKLOAD = ("spect_tc99m_lehr_nm670housing_2heads_60angles_r250mm_128x128x4.42mm_windows126-154_108-126keV_"
                   "ct_phantom_256x256x160_1.2mm")
 
 # Batched uneven simulations: 48 seeded slab phantoms (32-128 voxels, 1-3 mm),
@@ -75,7 +76,7 @@ ARF_SPLIT = (10, 2, 10000, 15.0)  # scatter pass: Compton, Rayleigh factors, max
 ARF_SCATTER_SHARE = 8  # the scatter pass runs 1 / 8 of the primaries
 ARF_CHUNKS = 16  # ... in independent chunks (its variance)
 ARF_SUMMARY_PRIMARIES = 240_000_000  # reduced comparison carried by the default (dose) line
-ARF_WORKLOAD = ("spect_lu177_melp_2heads_120angles_r250mm_128x128x4.42mm_windows187-229_166-187_101-125keV_"
+ARF_WORKLOAD = ("spect_lu177_melp_nm670housing_2heads_120angles_r250mm_128x128x4.42mm_windows187-229_166-187_101-125keV_"
                 "ct_phantom_256x256x160_1.2mm_arf_mlp3x128_bf16_freeflight_aa15deg+scattersplit_c10_r2_aa15deg_1of8")
 
 
@@ -252,10 +253,11 @@ def reference_workload(args, threads):
         from opengate_gb300 import spect as S
 
         if args.workload == "spect":
-            scene, sp, _ = W.spect_phantom()
+            scene, sp, _ = W.spect_phantom(housing=SPECT_HOUSING)
             meta = (SPECT_METRIC, SPECT_WORKLOAD, int(SPECT_DECAYS * SPECT_YIELD))
         else:
-            scene, sp, _ = W.spect_phantom(nuclide=W.LU177, collimator=S.MELP, n_runs=120, windows=ARF_WINDOWS)
+            scene, sp, _ = W.spect_phantom(nuclide=W.LU177, collimator=S.MELP, n_runs=120, windows=ARF_WINDOWS,
+                                           housing=SPECT_HOUSING)
             meta = (ARF_METRIC, ARF_WORKLOAD, int(ARF_DECAYS * ARF_YIELD))
         runs = sp.n_runs
 
@@ -346,7 +348,7 @@ def run_ours_spect(args, ws, rank, local, dist, use_cuda):
     from opengate_gb300 import workloads as W
     from opengate_gb300.engine import SpectEngine
 
-    scene, sp, _ = W.spect_phantom()
+    scene, sp, _ = W.spect_phantom(housing=SPECT_HOUSING)
     n_step = args.primaries if args.primaries != PRIMARIES_PER_STEP else int(SPECT_DECAYS * SPECT_YIELD)
     n_per_run = n_step // sp.n_runs
     n = n_per_run * sp.n_runs
@@ -456,7 +458,7 @@ def spect_ff_specs():
     """(scene, primary free-flight spec, scatter-splitting spec) of the SPECT workload."""
     from opengate_gb300 import workloads as W
 
-    scene, sp_p, _ = W.spect_phantom()
+    scene, sp_p, _ = W.spect_phantom(housing=SPECT_HOUSING)
     sp_s = copy.deepcopy(sp_p)
     sp_p.set_free_flight()
     nc, nr, lvl, deg = FF_SPLIT
@@ -671,7 +673,7 @@ class ArfRecipe:
         from opengate_gb300.engine import ArfNetwork, SpectEngine
 
         self.scene, self.sp, _ = W.spect_phantom(nuclide=W.LU177, collimator=S.MELP, n_runs=n_runs,
-                                                 windows=ARF_WINDOWS)
+                                                 windows=ARF_WINDOWS, housing=SPECT_HOUSING)
         batch = min(batch, 1 << 26)
         self.plain = SpectEngine(self.scene, self.sp, device=local, precision=32, batch=batch)
         net = ArfNetwork(self.plain)

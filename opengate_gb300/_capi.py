@@ -125,6 +125,7 @@ class SpectDesc(ctypes.Structure):
         ("n_runs", ctypes.c_int32), ("adder_policy", ctypes.c_int32),
         ("n_cover", ctypes.c_int32), ("cover_thickness", ctypes.c_double), ("cover_material", ctypes.c_int32),
         ("n_back", ctypes.c_int32), ("back_thickness", ctypes.c_double * 4), ("back_material", ctypes.c_int32 * 4),
+        ("shielded_sides", ctypes.c_int32),
     ]
 
 

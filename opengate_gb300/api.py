@@ -119,7 +119,7 @@ class SpectHead(GateObject):
     user_info_defaults = {"mother": "world", "collimator_type": "lehr", "crystal_size": "3/8",
                           "radius": 25 * u.cm, "start_angle_deg": 0.0, "step_angle_deg": 1.0, "nb_angle": 1,
                           "gap": 0.0, "half_width": None, "collimator_material": "G4_Pb",
-                          "crystal_material": "G4_SODIUM_IODIDE"}
+                          "crystal_material": "G4_SODIUM_IODIDE", "housing": "none"}
 
     @property
     def crystal_name(self):
@@ -952,7 +952,13 @@ class Simulation:
             channels = projs[0].channels
             windows = [(float(c["min"]) / u.MeV, float(c["max"]) / u.MeV) for c in channels]
             size, spacing_in = projs[0].size, projs[0].spacing
-        extra = [h0.collimator_material, h0.crystal_material]
+        housing = str(h0.housing)
+        if any(str(h.housing) != housing for h in heads):
+            raise NotImplementedError("heads with different housings")
+        if arf is not None and str(arf[2].get("housing", "none")) != housing:
+            raise ValueError(f"network '{arfs[0].pth_filename}' was trained for the housing "
+                             f"'{arf[2].get('housing', 'none')}', the heads have '{housing}'")
+        extra = [h0.collimator_material, h0.crystal_material] + list(S.HOUSING_MATERIALS.get(housing, ()))
         scene, vol, hu, names, sources = self.build_scene(extra_materials=extra)
         coll = S.COLLIMATORS.get(str(h0.collimator_type).lower())
         if coll is None:
@@ -967,6 +973,7 @@ class Simulation:
                          head_start_deg=[h.start_angle_deg for h in heads])
         if half_w:
             sp.half_width = half_w
+        sp.apply_housing(housing, names.index)
         sp.arf = arf
         if arf is not None:
             ARF.apply_head_meta(sp, arf[2])
@@ -1148,6 +1155,7 @@ class Simulation:
         sp = S.SpectSpec(collimator=S.COLLIMATORS[str(plane.collimator_type).lower()],
                          crystal_thickness=S.CRYSTALS[plane.crystal_size], gap=plane.gap / u.mm, n_heads=1,
                          n_runs=1, windows=[(float(c["min"]) / u.MeV, float(c["max"]) / u.MeV) for c in chans])
+        sp.housing = str(plane.housing)  # recorded with the dataset; head_engine builds it
         # the digitizer modules on the windows actor's crystal (the plane's own, or that of a head
         # behind the plane as in the reference's set-up); the head geometry is the plane's
         for a in self.actors.values():

@@ -56,6 +56,7 @@ def head_meta(sp, collimator_type, crystal_size):
     """Description of the head and digitizer of a SpectSpec, stored with datasets and models."""
     b = sp.blur
     return {"collimator_type": str(collimator_type), "crystal_size": str(crystal_size), "gap": float(sp.gap),
+            "housing": str(getattr(sp, "housing", "none")),
             "windows": np.asarray(sp.windows, dtype=np.float64).reshape(-1, 2),
             "adder_policy": str(sp.adder_policy),
             "blur": np.array([float(getattr(b, f)) for f in _BLUR_FIELDS] +
@@ -76,13 +77,15 @@ def apply_head_meta(sp, meta):
 
 def _meta_arrays(meta):
     return {"collimator_type": np.array(meta["collimator_type"]), "crystal_size": np.array(meta["crystal_size"]),
-            "gap": np.float64(meta["gap"]), "windows": np.asarray(meta["windows"], dtype=np.float64),
+            "gap": np.float64(meta["gap"]), "housing": np.array(meta.get("housing", "none")),
+            "windows": np.asarray(meta["windows"], dtype=np.float64),
             "adder_policy": np.array(meta["adder_policy"]), "blur": np.asarray(meta["blur"], dtype=np.float64)}
 
 
 def _meta_from(z):
     return {"collimator_type": str(z["collimator_type"]), "crystal_size": str(z["crystal_size"]),
-            "gap": float(z["gap"]), "windows": np.asarray(z["windows"]), "adder_policy": str(z["adder_policy"]),
+            "gap": float(z["gap"]), "housing": str(z["housing"]) if "housing" in z else "none",
+            "windows": np.asarray(z["windows"]), "adder_policy": str(z["adder_policy"]),
             "blur": np.asarray(z["blur"])}
 
 
@@ -143,8 +146,10 @@ def load_model(path):
         return m, params, _meta_from(z)
 
 
-def head_spec(meta, n_runs=1, size=(128, 128), spacing=(4.42, 4.42), collimator_material=0, crystal_material=0):
-    """A one-head SpectSpec of the stored head description."""
+def head_spec(meta, n_runs=1, size=(128, 128), spacing=(4.42, 4.42), collimator_material=0, crystal_material=0,
+              housing_index=None):
+    """A one-head SpectSpec of the stored head description (housing_index(name) -> material
+    index of the housing's materials, when it has one)."""
     from . import spect as S
 
     coll = S.COLLIMATORS.get(str(meta["collimator_type"]).lower())
@@ -154,6 +159,9 @@ def head_spec(meta, n_runs=1, size=(128, 128), spacing=(4.42, 4.42), collimator_
                      n_heads=1, n_runs=n_runs, size=size, spacing=spacing, collimator_material=collimator_material,
                      crystal_material=crystal_material, windows=[tuple(w) for w in np.asarray(meta["windows"])])
     apply_head_meta(sp, meta)
+    kind = str(meta.get("housing", "none"))
+    if kind != "none":
+        sp.apply_housing(kind, housing_index)
     return sp
 
 
@@ -166,10 +174,13 @@ def head_engine(meta, device=0, precision=32, world_material="G4_AIR", collimato
     from .engine import SpectEngine
     from .scene import Scene, SourceSpec
 
+    from . import spect as S
+
     db = M.MaterialDatabase()
-    names = [world_material, collimator_material, crystal_material]
+    hmats = list(S.HOUSING_MATERIALS.get(str(meta.get("housing", "none")), ()))
+    names = [world_material, collimator_material, crystal_material] + hmats
     pt = T.PhysicsTables([db.get(n) for n in names])
-    sp = head_spec(meta, collimator_material=1, crystal_material=2)
+    sp = head_spec(meta, collimator_material=1, crystal_material=2, housing_index=lambda m: 3 + hmats.index(m))
     src = SourceSpec()
     src.mono = 0.1
     scene = Scene(pt, np.zeros((1, 1, 1), np.uint16), [1.0] * 3, [-0.5] * 3, [2000.0] * 3, 0, src)

@@ -24,6 +24,7 @@ def add_spect_head(sim, name="spect", collimator_type="lehr", rotation_deg=0, de
     head = sim.add_volume("SpectHead", name)
     head.collimator_type = str(collimator_type).lower()
     head.crystal_size = crystal_size
+    head.housing = "nm670"  # the shielding box of add_spect_box (ge_discovery_nm670.py:215-262)
     crystal = Box({"name": head.crystal_name, "head": name})
     return head, Box({"name": f"{name}_collimator", "head": name}), crystal
 
@@ -132,6 +133,7 @@ def add_detection_plane_for_arf(sim, det_name, colli_type, plane_size=None):
     mm = _u.mm
     plane = sim.add_volume("ArfDetectorPlane", det_name)
     plane.collimator_type = str(colli_type).lower()
+    plane.housing = "nm670"  # the NM670 head behind the plane
     if plane_size is None:
         plane_size = [576 * mm, 446 * mm]
     plane.size = [plane_size[0], plane_size[1], 1 * _u.nm]
@@ -171,13 +173,15 @@ def add_actor_for_arf_training_dataset(sim, colli_type, ene_win_actor, rr):
     return detector_plane, arf
 
 
-def distance_to_crystal(colli_type, crystal_size="3/8", gap=0.0):
-    """Distance (mm units) from the collimator face to the middle of the crystal: the depth of
-    the ARF projection plane."""
+def distance_to_crystal(colli_type, crystal_size="3/8", gap=0.0, housing="nm670"):
+    """Distance (mm units) from the collimator face to the middle of the crystal (behind the
+    housing's entrance cover): the depth of the ARF projection plane."""
     from ... import spect as S
 
     coll = S.COLLIMATORS[str(colli_type).lower()]
-    return (coll["collimator_thickness"] + gap + 0.5 * S.CRYSTALS[crystal_size]) * _u.mm
+    cover, _ = S.housing_layers(housing, S.CRYSTALS[crystal_size])
+    c = cover[0] if cover else 0.0
+    return (coll["collimator_thickness"] + gap + c + 0.5 * S.CRYSTALS[crystal_size]) * _u.mm
 
 
 def add_arf_detector(sim, name, colli_type, image_size, image_spacing, pth_filename):
@@ -191,7 +195,8 @@ def add_arf_detector(sim, name, colli_type, image_size, image_spacing, pth_filen
     arf.image_size = image_size
     arf.image_spacing = image_spacing
     arf.verbose_batch = False
-    arf.distance_to_crystal = distance_to_crystal(colli_type, det_plane.crystal_size, det_plane.gap)
+    arf.distance_to_crystal = distance_to_crystal(colli_type, det_plane.crystal_size, det_plane.gap,
+                                                  det_plane.housing)
     arf.pth_filename = pth_filename
     arf.flip_plane = False
     arf.plane_axis = [0, 1, 2]

@@ -386,10 +386,30 @@ struct gg_ctx {
       s.ss_cos = (real)ss_cos;
       s.wproj = ff_on ? d_arf_proj : nullptr;
       s.wproj2 = ff_on ? d_arf_proj2 : nullptr;
-      s.zb[0] = (real)0;
-      s.zb[1] = (real)sp.collimator_thickness;
-      s.zb[2] = (real)(sp.collimator_thickness + sp.gap);
-      s.zb[3] = (real)(sp.collimator_thickness + sp.gap + sp.crystal_thickness);
+      {
+        // slab boundaries: running sums in double, each rounded once
+        double z = 0.0;
+        int k = 0;
+        s.zb[0] = (real)0;
+        auto slab = [&](double t, int m) {
+          z = z + t;
+          s.hmat[k] = m;
+          s.zb[++k] = (real)z;
+        };
+        slab(sp.collimator_thickness, sp.collimator_material);
+        slab(sp.gap, -1);
+        if (sp.n_cover > 0) slab(sp.cover_thickness, sp.cover_material);
+        s.hreg_cr = k;
+        slab(sp.crystal_thickness, sp.crystal_material);
+        for (int b = 0; b < sp.n_back; ++b) slab(sp.back_thickness[b], sp.back_material[b]);
+        s.n_hreg = k;
+        s.zend = s.zb[k];
+        for (int j = k; j < gg::kHeadRegions; ++j) {
+          s.hmat[j] = -1;
+          s.zb[j + 1] = s.zend;
+        }
+        s.side_black = sp.shielded_sides ? 1 : 0;
+      }
       s.apo = (real)sp.hole_apothem;
       s.px = (real)sp.pitch_x;
       s.py = (real)sp.pitch_y;
@@ -1501,6 +1521,13 @@ int gg_spect_setup(gg_ctx *c, const gg_spect_desc *sp) {
   if (sp->collimator_material < 0 || sp->collimator_material >= c->n_mat || sp->crystal_material < 0 ||
       sp->crystal_material >= c->n_mat)
     return c->fail(GG_ERR_ARG, "gg_spect_setup: head materials outside the material table");
+  if (sp->n_cover < 0 || sp->n_cover > 1 || sp->n_back < 0 || sp->n_back > 4)
+    return c->fail(GG_ERR_ARG, "gg_spect_setup: housing: at most one cover and four back layers");
+  if (sp->n_cover && (!(sp->cover_thickness > 0) || sp->cover_material < 0 || sp->cover_material >= c->n_mat))
+    return c->fail(GG_ERR_ARG, "gg_spect_setup: housing cover needs a thickness > 0 and a table material");
+  for (int b = 0; b < sp->n_back; ++b)
+    if (!(sp->back_thickness[b] > 0) || sp->back_material[b] < 0 || sp->back_material[b] >= c->n_mat)
+      return c->fail(GG_ERR_ARG, "gg_spect_setup: housing back layer %d needs a thickness > 0 and a table material", b);
   for (int k = 0; k < sp->n_windows; ++k)
     if (!(sp->window_hi[k] > sp->window_lo[k])) return c->fail(GG_ERR_ARG, "gg_spect_setup: empty window");
   size_t n = (size_t)sp->n_heads * sp->n_runs * sp->n_windows * sp->size[0] * sp->size[1];

@@ -106,7 +106,7 @@ __global__ void __launch_bounds__(256) k_arf_sample(Scene<real> s, ArfArgs p) {
       ++steps;
       int mat;
       if (head_flight(s, ph, g, mat))
-        do_interaction<real, true>(s, ph, g, &bc, mat, 0u, ph.hreg == 2 ? 2 : 3, l, t, sec, n_dep, ev);
+        do_interaction<real, true>(s, ph, g, &bc, mat, 0u, ph.hreg == s.hreg_cr ? 2 : 3, l, t, sec, n_dep, ev);
     }
     atomicAdd(&n_head, steps);
     int label = 0;

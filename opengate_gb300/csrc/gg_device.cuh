@@ -26,6 +26,7 @@ namespace gg {
 constexpr int kHistList = 8;      // per-history voxel list (registers)
 constexpr int kLoopCap = 1000;    // sampling-loop iteration cap
 constexpr int kStepCap = 1000000; // per-photon step cap (termination guard)
+constexpr int kHeadRegions = 8;   // SPECT head slabs: collimator, gap, cover, crystal, 4 back layers
 constexpr double kMC2 = 0.51099895;
 constexpr double kHcMevAngstrom = 12.398419843320026e-3;
 
@@ -472,8 +473,13 @@ struct Scene {
   const real *frames;
   uint64_t run_first, run_len;
   int run_base;
-  real half_w, zb[4], apo, px, py, hpx, hpy, inv_px, inv_py;
-  int mat_coll, mat_cr;
+  // head slabs along the local w axis: region k = [zb[k], zb[k + 1]) of
+  // material hmat[k] (-1 vacuum): 0 collimator (with the holes), 1 gap, the
+  // optional entrance cover, the crystal (region hreg_cr, the only scored
+  // one), the layers behind it; zend = zb[n_hreg] (the head box's depth);
+  // side_black: the box's side faces absorb
+  real half_w, zb[kHeadRegions + 1], zend, apo, px, py, hpx, hpy, inv_px, inv_py;
+  int mat_coll, mat_cr, hmat[kHeadRegions], n_hreg, hreg_cr, side_black;
   real wlo[8], whi[8], pix_half[2], inv_psp[2];
   unsigned long long *proj;
   // digitizer blurring of the singles (GateDigitizerBlurringActor on the energy:
@@ -539,6 +545,27 @@ __device__ __forceinline__ real exit_distance(const real p[3], const real d[3], 
   return t;
 }
 
+// exit_distance and the axis of the face it leaves through (the first axis
+// reaching the minimum; -1 when no axis bounds the path)
+template <typename real>
+__device__ __forceinline__ real exit_distance_face(const real p[3], const real d[3], const real lo[3],
+                                                   const real hi[3], int &face) {
+  real t = gg_inf(real(0));
+  face = -1;
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    if (d[a] > R<real>(0)) {
+      real ta = (hi[a] - p[a]) / d[a];
+      if (ta < t) t = ta, face = a;
+    } else if (d[a] < R<real>(0)) {
+      real ta = (lo[a] - p[a]) / d[a];
+      if (ta < t) t = ta, face = a;
+    }
+  }
+  if (t < R<real>(0)) t = R<real>(0);
+  return t;
+}
+
 template <typename real>
 __device__ __forceinline__ real entry_distance(const real p[3], const real d[3], const real lo[3],
                                                const real hi[3]) {
@@ -557,6 +584,34 @@ __device__ __forceinline__ real entry_distance(const real p[3], const real d[3],
         t2 = tmp;
       }
       if (t1 > tnear) tnear = t1;
+      if (t2 < tfar) tfar = t2;
+    }
+  }
+  if (tnear > tfar || tfar < R<real>(0)) return inf;
+  return tnear > R<real>(0) ? tnear : R<real>(0);
+}
+
+// entry_distance and the axis of the face it enters through (the first axis
+// reaching the largest near distance; -1 from inside or parallel to all)
+template <typename real>
+__device__ __forceinline__ real entry_distance_face(const real p[3], const real d[3], const real lo[3],
+                                                    const real hi[3], int &face) {
+  real inf = gg_inf(real(0));
+  real tnear = -inf, tfar = inf;
+  face = -1;
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    if (d[a] == R<real>(0)) {
+      if (p[a] < lo[a] || p[a] > hi[a]) return inf;
+    } else {
+      real t1 = (lo[a] - p[a]) / d[a];
+      real t2 = (hi[a] - p[a]) / d[a];
+      if (t1 > t2) {
+        real tmp = t1;
+        t1 = t2;
+        t2 = tmp;
+      }
+      if (t1 > tnear) tnear = t1, face = a;
       if (t2 < tfar) tfar = t2;
     }
   }

@@ -963,10 +963,10 @@ __device__ __forceinline__ int flight(const Scene<real> &s, Photon<real> &ph, Rn
       int mat;
       if (head_flight(s, ph, g, mat)) {
         pmat = mat;
-        pscored = ph.hreg == 2 ? 2 : 3;
+        pscored = ph.hreg == s.hreg_cr ? 2 : 3;
         return kInteract;
       }
-      return kFly;
+      return ph.alive ? kFly : kRefill;  // (stopped by a shielded side)
     }
     ++n_world;
     if (spect_world_flight(s, ph, g)) {

@@ -106,10 +106,10 @@ __device__ __forceinline__ int head_stage_flight(const Scene<real> &s, Photon<re
     int mat;
     if (head_flight(s, ph, g, mat)) {
       pmat = mat;
-      pscored = ph.hreg == 2 ? 2 : 3;
+      pscored = ph.hreg == s.hreg_cr ? 2 : 3;
       return kInteract;
     }
-    return kFly;
+    return ph.alive ? kFly : kRefill;  // (stopped by a shielded side)
   }
   ++n_world;
   if constexpr (FF) {  // free flight to another head (the image crossed on the way)

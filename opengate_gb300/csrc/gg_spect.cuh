@@ -158,6 +158,34 @@ struct Event {
   }
 };
 
+// Slab bound zb[k] and slab material hmat[k] for a k held in a register:
+// selected over the constant indices (an indexed access would move the
+// scene to local memory).
+template <typename real>
+__device__ __forceinline__ real head_zb(const Scene<real> &s, int k) {
+  real z = s.zb[0];
+#pragma unroll
+  for (int j = 1; j <= kHeadRegions; ++j) z = k == j ? s.zb[j] : z;
+  return z;
+}
+
+template <typename real>
+__device__ __forceinline__ int head_mat(const Scene<real> &s, int k) {
+  int m = s.hmat[0];
+#pragma unroll
+  for (int j = 1; j < kHeadRegions; ++j) m = k == j ? s.hmat[j] : m;
+  return m;
+}
+
+// Slab of a head-local depth w: the number of inner bounds at or below w.
+template <typename real>
+__device__ __forceinline__ int head_region(const Scene<real> &s, real w) {
+  int k = 0;
+#pragma unroll
+  for (int j = 1; j < kHeadRegions; ++j) k += (j < s.n_hreg && !(w < s.zb[j])) ? 1 : 0;
+  return k;
+}
+
 template <typename real>
 __device__ __forceinline__ void head_cross(const Scene<real> &s, Photon<real> &ph, bool leave) {
   if (leave) {
@@ -184,13 +212,11 @@ template <typename real>
 __device__ __forceinline__ int head_flight(const Scene<real> &s, Photon<real> &ph, Rng &g, int &mat) {
   real *l = ph.pos, *d = ph.dir;
   real lo[3] = {-s.half_w, -s.half_w, R<real>(0)};
-  real hi[3] = {s.half_w, s.half_w, s.zb[3]};
-  real tbox = exit_distance(l, d, lo, hi);
+  real hi[3] = {s.half_w, s.half_w, s.zend};
+  int face;
+  real tbox = exit_distance_face(l, d, lo, hi, face);
   real treg = gg_inf(real(0));
-  // region bounds zb[hreg] (below) and zb[hreg + 1] (above), selected without
-  // indexing the scene (an indexed access would move it to local memory)
-  const real zlo = ph.hreg == 0 ? s.zb[0] : (ph.hreg == 1 ? s.zb[1] : s.zb[2]);
-  const real zhi = ph.hreg == 0 ? s.zb[1] : (ph.hreg == 1 ? s.zb[2] : s.zb[3]);
+  const real zlo = head_zb(s, ph.hreg), zhi = head_zb(s, ph.hreg + 1);
   if (d[2] > R<real>(0)) {
     treg = zhi - l[2];
     treg = treg / d[2];
@@ -201,6 +227,8 @@ __device__ __forceinline__ int head_flight(const Scene<real> &s, Photon<real> &p
   if (treg < R<real>(0)) treg = R<real>(0);
   bool leave = tbox <= treg;
   real tlim = leave ? tbox : treg;
+  // shielded sides: a photon that reaches a side face of the box stops there
+  const bool absorb = leave && s.side_black && face != 2;
   if (ph.hreg == 0 && !ph.left_hole) {
     real cx, cy;
     if (find_hole(s, l[0], l[1], cx, cy)) {
@@ -211,17 +239,20 @@ __device__ __forceinline__ int head_flight(const Scene<real> &s, Photon<real> &p
         return 0;
       }
       move3(l, d, tlim);
-      head_cross(s, ph, leave);
+      if (absorb) ph.alive = 0;
+      else head_cross(s, ph, leave);
       return 0;
     }
   }
   ph.left_hole = 0;
-  if (ph.hreg == 1) {
+  const int rm = head_mat(s, ph.hreg);
+  if (rm < 0) {  // vacuum slab (the gap)
     move3(l, d, tlim);
-    head_cross(s, ph, leave);
+    if (absorb) ph.alive = 0;
+    else head_cross(s, ph, leave);
     return 0;
   }
-  mat = ph.hreg == 0 ? s.mat_coll : s.mat_cr;
+  mat = rm;
   real mu = interp_row(s.sig + (size_t)s.mat_comp[mat] * s.n_e, ph.ei);
   mu = s.mat_rho[mat] * mu;
   real u = u01_open0<real>(g);
@@ -229,7 +260,8 @@ __device__ __forceinline__ int head_flight(const Scene<real> &s, Photon<real> &p
   sd = sd / mu;
   if (sd >= tlim) {
     move3(l, d, tlim);
-    head_cross(s, ph, leave);
+    if (absorb) ph.alive = 0;
+    else head_cross(s, ph, leave);
     return 0;
   }
   move3(l, d, sd);
@@ -247,17 +279,19 @@ template <typename real>
 __device__ __forceinline__ int spect_world_flight(const Scene<real> &s, Photon<real> &ph, Rng &g) {
   real inf = gg_inf(real(0));
   real tb = ph.exclude != 0 ? entry_distance(ph.pos, ph.dir, s.bmin, s.bmax) : inf;
-  int box = 0;
+  int box = 0, bface = 2;
   real hlo[3] = {-s.half_w, -s.half_w, R<real>(0)};
-  real hhi[3] = {s.half_w, s.half_w, s.zb[3]};
+  real hhi[3] = {s.half_w, s.half_w, s.zend};
   for (int h = 0; h < s.n_heads; ++h) {
     if (ph.exclude == 1 + h) continue;
     real lp[3], ld[3];
     to_local(head_frame(s, ph.run, h), ph.pos, ph.dir, lp, ld);
-    real th = entry_distance(lp, ld, hlo, hhi);
+    int f;
+    real th = entry_distance_face(lp, ld, hlo, hhi, f);
     if (th < tb) {
       tb = th;
       box = 1 + h;
+      bface = f;
     }
   }
   real wlo[3] = {-s.whalf[0], -s.whalf[1], -s.whalf[2]};
@@ -277,6 +311,8 @@ __device__ __forceinline__ int spect_world_flight(const Scene<real> &s, Photon<r
     if (box == 0) {
       ph.in_image = 1;
       ph.t_exit = exit_distance(ph.pos, ph.dir, s.bmin, s.bmax);
+    } else if (s.side_black && bface != 2) {
+      ph.alive = 0;  // stopped by the head's side shielding
     } else {
       int h = box - 1;
       real lp[3], ld[3];
@@ -288,7 +324,7 @@ __device__ __forceinline__ int spect_world_flight(const Scene<real> &s, Photon<r
       }
       ph.in_head = 1;
       ph.head = h;
-      ph.hreg = lp[2] < s.zb[1] ? 0 : (lp[2] < s.zb[2] ? 1 : 2);
+      ph.hreg = head_region(s, lp[2]);
       ph.left_hole = 0;
     }
     return 0;
@@ -334,24 +370,27 @@ __device__ __forceinline__ int ff_target(const Scene<real> &s, Photon<real> &ph,
     }
   }
   real tb = gg_inf(real(0));
-  int box = 0;
+  int box = 0, bface = 2;
   real cos_box = R<real>(0);
   real hlo[3] = {-s.half_w, -s.half_w, R<real>(0)};
-  real hhi[3] = {s.half_w, s.half_w, s.zb[3]};
+  real hhi[3] = {s.half_w, s.half_w, s.zend};
   for (int h = 0; h < s.n_heads; ++h) {
     if (ph.exclude == 1 + h) continue;
     real lp[3], ld[3];
     to_local(head_frame(s, ph.run, h), ph.pos, ph.dir, lp, ld);
-    real th = entry_distance(lp, ld, hlo, hhi);
+    int f;
+    real th = entry_distance_face(lp, ld, hlo, hhi, f);
     if (th < tb) {
       tb = th;
       box = 1 + h;
       cos_box = ld[2];
+      bface = f;
     }
   }
   real wlo[3] = {-s.whalf[0], -s.whalf[1], -s.whalf[2]};
   const real tout = exit_distance(ph.pos, ph.dir, wlo, s.whalf);
-  if (!(tb <= tout) || cos_box < cos_min) {
+  // (a line into a shielded side face cannot be detected)
+  if (!(tb <= tout) || cos_box < cos_min || (s.side_black && bface != 2)) {
     ph.alive = 0;
     return 0;
   }
@@ -404,7 +443,7 @@ __device__ __forceinline__ int ff_flight(const Scene<real> &s, Photon<real> &ph,
   ph.in_image = 0;
   ph.in_head = 1;
   ph.head = h;
-  ph.hreg = lp[2] < s.zb[1] ? 0 : (lp[2] < s.zb[2] ? 1 : 2);
+  ph.hreg = head_region(s, lp[2]);
   ph.left_hole = 0;
   return 1;
 }

@@ -87,6 +87,18 @@ _NIST = {
 }
 
 
+# Materials of the SPECT head housing as the reference's GateMaterials.db
+# defines them (opengate/contrib/GateMaterials.db: Aluminium, TiO2, Pyrex66,
+# Lead, Steel): density g/cm3, element mass fractions.
+_GATE_DB = {
+    "Aluminium": (2.6989, ["Al"], [1.0]),
+    "TiO2": (4.23, ["Ti", "O"], [0.5993, 0.4007]),
+    "Pyrex66": (1.478, ["O", "Si", "Na", "P", "B", "Al"], [0.5386, 0.3768, 0.0297, 0.0042, 0.0401, 0.0106]),
+    "Lead": (11.4, ["Pb"], [1.0]),
+    "Steel": (7.86, ["C", "Mn", "Fe"], [0.002, 0.005, 0.993]),
+}
+
+
 class MaterialDatabase:
     """Named materials: NIST built-ins plus user materials added by weights."""
 
@@ -98,13 +110,16 @@ class MaterialDatabase:
         self._user[name] = Material(name, density, symbols, weights)
 
     def __contains__(self, name):
-        return name in self._user or name in _NIST
+        return name in self._user or name in _NIST or name in _GATE_DB
 
     def get(self, name):
         if name in self._user:
             return self._user[name]
         if name in _NIST:
             d, s, f = _NIST[name]
+            return Material(name, d, s, f)
+        if name in _GATE_DB:
+            d, s, f = _GATE_DB[name]
             return Material(name, d, s, f)
         raise KeyError(f"unknown material '{name}'")
 

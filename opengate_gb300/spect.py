@@ -35,6 +35,24 @@ HEGP = dict(hole_apothem=2.0, collimator_thickness=66.0, hole_pitch=5.8)  # 4 mm
 COLLIMATORS = {"lehr": LEHR, "melp": MELP, "megp": MEGP, "hegp": HEGP, "he": HEGP}
 CRYSTALS = {"3/8": 9.525, "5/8": 15.875}  # NaI thickness, mm
 
+# Housing of the NM670 head (ge_discovery_nm670.py:215-262 add_spect_box): the
+# aluminium cover in front of the crystal, then behind it the TiO2 reflector,
+# the Pyrex back compartment, what is left of the lead cover's 101.375 mm and
+# the steel shielding's 10 mm behind the lead cover; the side rims shield.
+HOUSING_MATERIALS = {"nm670": ("Aluminium", "TiO2", "Pyrex66", "Lead", "Steel")}
+
+
+def housing_layers(kind, crystal_thickness):
+    """(cover, back) of a housing kind ("none" or "nm670") as (thickness mm, material name)."""
+    if kind in (None, "none"):
+        return None, []
+    if kind != "nm670":
+        raise NotImplementedError(f"head housing '{kind}'")
+    alu, reflector, backside, lead_cover, shielding = 1.3, 1.2, 80.0, 101.375, 111.375
+    lead_back = lead_cover - (alu + crystal_thickness + reflector) - backside
+    return (alu, "Aluminium"), [(reflector, "TiO2"), (backside, "Pyrex66"), (lead_back, "Lead"),
+                                (shielding - lead_cover, "Steel")]
+
 
 class SpectSpec:
     def __init__(self, collimator=LEHR, crystal_thickness=9.525, gap=0.0, radius=250.0, n_heads=2,
@@ -71,9 +89,11 @@ class SpectSpec:
         self.blur = C.BlurDesc()
         # free flight outside the heads (set_free_flight); off by default
         self.free_flight = C.FfDesc(C.FF_OFF, -1.0, 0.0, 0, 0, 0, 0.0)
-        # housing slabs (set_housing); none by default
+        # housing slabs and side shielding (set_housing); none by default
         self.cover = None
         self.back = []
+        self.shielded_sides = False
+        self.housing = "none"
 
     def set_energy_blur(self, method, sigma=0.0, resolution=0.0, reference=0.0, slope=0.0):
         """DigitizerBlurringActor on the singles' energy (MeV): method "Gaussian" (sigma),
@@ -153,13 +173,15 @@ class SpectSpec:
         d.n_back = len(self.back)
         for k, (t, m) in enumerate(self.back):
             d.back_thickness[k], d.back_material[k] = float(t), int(m)
+        d.shielded_sides = 1 if self.shielded_sides else 0
         return d
 
-    def set_housing(self, cover=None, back=()):
-        """Head housing slabs (ge_discovery_nm670.py:215-262): ``cover`` = (thickness mm,
-        material index) between the gap and the crystal, ``back`` = up to four (thickness mm,
-        material index) layers behind the crystal, outwards.  Indices into the scene's
-        material table."""
+    def set_housing(self, cover=None, back=(), shielded_sides=True):
+        """Head housing (ge_discovery_nm670.py:215-262): ``cover`` = (thickness mm, material
+        index) between the gap and the crystal, ``back`` = up to four (thickness mm, material
+        index) layers behind the crystal, outwards; ``shielded_sides``: the head's side faces
+        absorb (the shielding box's lead / steel rims).  Indices into the scene's material
+        table."""
         back = [(float(t), int(m)) for t, m in back]
         if len(back) > 4:
             raise ValueError("at most four layers behind the crystal")
@@ -168,6 +190,17 @@ class SpectSpec:
                 raise ValueError("housing layers need a positive thickness")
         self.cover = None if cover is None else (float(cover[0]), int(cover[1]))
         self.back = back
+        self.shielded_sides = bool(shielded_sides)
+
+    def apply_housing(self, kind, index_of):
+        """set_housing for a housing kind ("none" or "nm670"); index_of(name) -> material index."""
+        cover, back = housing_layers(kind, self.crystal_thickness)
+        if cover is None and not back:
+            self.set_housing(None, (), shielded_sides=False)
+            self.housing = "none"
+            return
+        self.set_housing((cover[0], index_of(cover[1])), [(t, index_of(m)) for t, m in back], shielded_sides=True)
+        self.housing = kind
 
     def housing_depth(self):
         """Depth of the head box behind the collimator front face (mm)."""

@@ -172,11 +172,14 @@ LU177 = ([0.1129, 0.2084], [0.062, 0.104])
 
 
 def spect_phantom(shape=(160, 256, 256), spacing=1.2, nuclide=TC99M, collimator=None, n_runs=60,
-                  windows=((0.126, 0.154), (0.108, 0.126)), density_tolerance=0.05, seed=20240611):
+                  windows=((0.126, 0.154), (0.108, 0.126)), density_tolerance=0.05, seed=20240611,
+                  housing="none"):
     """SPECT workload: CT phantom as attenuation map, body + sphere activity, two heads.
 
     Returns (scene, spect_spec, activity).  Materials: the CT labels, then
-    G4_Pb (collimator) and G4_SODIUM_IODIDE (crystal).
+    G4_Pb (collimator) and G4_SODIUM_IODIDE (crystal), then the housing's
+    (housing="nm670": the NM670 shielding box's cover, reflector, back
+    compartment, lead and steel, and shielded sides).
     """
     from . import spect as S
 
@@ -184,7 +187,9 @@ def spect_phantom(shape=(160, 256, 256), spacing=1.2, nuclide=TC99M, collimator=
     vm, lut, mats = ct_materials(density_tolerance)
     labels = M.create_label_image(hu, "G4_AIR", vm, lut)
     db = M.MaterialDatabase()
-    mats = mats + [db.get("G4_Pb"), db.get("G4_SODIUM_IODIDE")]
+    n_ct = len(mats)
+    hmats = list(S.HOUSING_MATERIALS.get(housing, ())) if housing not in (None, "none") else []
+    mats = mats + [db.get("G4_Pb"), db.get("G4_SODIUM_IODIDE")] + [db.get(m) for m in hmats]
     pt = T.PhysicsTables(mats)
     nz, ny, nx = shape
     corner = [-nx * spacing / 2, -ny * spacing / 2, -nz * spacing / 2]
@@ -198,8 +203,9 @@ def spect_phantom(shape=(160, 256, 256), spacing=1.2, nuclide=TC99M, collimator=
     src.spec_cdf = np.cumsum(w) / np.sum(w)
     scene = Scene(pt, labels, [spacing] * 3, corner, [1500.0] * 3, 0, src)
     sp = S.SpectSpec(collimator=collimator or S.LEHR, n_runs=n_runs, windows=windows,
-                     step_angle_deg=360.0 / n_runs, collimator_material=len(mats) - 2,
-                     crystal_material=len(mats) - 1)
+                     step_angle_deg=360.0 / n_runs, collimator_material=n_ct, crystal_material=n_ct + 1)
+    if hmats:
+        sp.apply_housing(housing, lambda name: n_ct + 2 + hmats.index(name))
     return scene, sp, act
 
 

@@ -416,8 +416,12 @@ typedef struct {
   /* SPECT heads and projection digitizer */
   int spect, n_heads, n_win, pnx, pny, n_runs, run;
   real hc[2][3], hu[2][3], he1[2][3], he2[2][3];
-  real half_w, zb[4], apo, px, py, hpx, hpy, inv_px, inv_py;
-  int mat_coll, mat_cr;
+  /* head slabs along w: region k = [zb[k], zb[k + 1]) of material hmat[k]
+     (-1 vacuum): collimator (holes), gap, optional cover, crystal (hreg_cr,
+     the scored one), back layers; zend = zb[n_hreg]; side_black: the box's
+     side faces absorb (gg_spect_desc.shielded_sides) */
+  real half_w, zb[9], zend, apo, px, py, hpx, hpy, inv_px, inv_py;
+  int mat_coll, mat_cr, hmat[8], n_hreg, hreg_cr, side_black;
   real wlo[8], whi[8], pix_half[2], inv_psp[2];
   uint64_t *proj; /* [head][run][window][pny][pnx], shared, atomics */
   /* digitizer blurring (gg_blur_desc): eblur 0 off / 1 Gaussian / 2 inverse
@@ -474,6 +478,55 @@ static real exit_distance(const real p[3], const real d[3], const real lo[3], co
   }
   if (t < R(0)) t = R(0);
   return t;
+}
+
+/* exit_distance and the axis of the face it leaves through (first axis
+   reaching the minimum, -1 if none) */
+static real exit_distance_face(const real p[3], const real d[3], const real lo[3], const real hi[3], int *face) {
+  real t = R(INFINITY);
+  *face = -1;
+  for (int a = 0; a < 3; ++a) {
+    real ta;
+    if (d[a] > R(0)) {
+      ta = (hi[a] - p[a]) / d[a];
+      if (ta < t) t = ta, *face = a;
+    } else if (d[a] < R(0)) {
+      ta = (lo[a] - p[a]) / d[a];
+      if (ta < t) t = ta, *face = a;
+    }
+  }
+  if (t < R(0)) t = R(0);
+  return t;
+}
+
+/* entry_distance and the axis of the face it enters through */
+static real entry_distance_face(const real p[3], const real d[3], const real lo[3], const real hi[3], int *face) {
+  real tnear = -R(INFINITY), tfar = R(INFINITY);
+  *face = -1;
+  for (int a = 0; a < 3; ++a) {
+    if (d[a] == R(0)) {
+      if (p[a] < lo[a] || p[a] > hi[a]) return R(INFINITY);
+    } else {
+      real t1 = (lo[a] - p[a]) / d[a];
+      real t2 = (hi[a] - p[a]) / d[a];
+      if (t1 > t2) {
+        real tmp = t1;
+        t1 = t2;
+        t2 = tmp;
+      }
+      if (t1 > tnear) tnear = t1, *face = a;
+      if (t2 < tfar) tfar = t2;
+    }
+  }
+  if (tnear > tfar || tfar < R(0)) return R(INFINITY);
+  return tnear > R(0) ? tnear : R(0);
+}
+
+/* slab of head depth w: the inner bounds at or below it */
+static int head_region(const scene_t *s, real w) {
+  int k = 0;
+  for (int j = 1; j < s->n_hreg; ++j) k += !(w < s->zb[j]);
+  return k;
 }
 
 /* distance to enter box [lo, hi] from p along d; INFINITY if missed */
@@ -1094,8 +1147,9 @@ static void head_step(const scene_t *s, photon_t *ph, rng_t *g, tally_t *t, even
   t->cnt[GG_CNT_HEAD_STEPS]++;
   real *l = ph->pos, *d = ph->dir;
   real lo[3] = {-s->half_w, -s->half_w, R(0)};
-  real hi[3] = {s->half_w, s->half_w, s->zb[3]};
-  real tbox = exit_distance(l, d, lo, hi);
+  real hi[3] = {s->half_w, s->half_w, s->zend};
+  int face;
+  real tbox = exit_distance_face(l, d, lo, hi, &face);
   real treg = R(INFINITY);
   if (d[2] > R(0)) {
     treg = s->zb[ph->hreg + 1] - l[2];
@@ -1107,6 +1161,8 @@ static void head_step(const scene_t *s, photon_t *ph, rng_t *g, tally_t *t, even
   if (treg < R(0)) treg = R(0);
   int leave = tbox <= treg;
   real tlim = leave ? tbox : treg;
+  /* shielded sides: a photon that reaches a side face stops there */
+  const int absorb = leave && s->side_black && face != 2;
   if (ph->hreg == 0 && !ph->left_hole) {
     real cx, cy;
     if (find_hole(s, l[0], l[1], &cx, &cy)) {
@@ -1117,17 +1173,19 @@ static void head_step(const scene_t *s, photon_t *ph, rng_t *g, tally_t *t, even
         return;
       }
       move(l, d, tlim);
-      head_cross(s, ph, leave);
+      if (absorb) ph->alive = 0;
+      else head_cross(s, ph, leave);
       return;
     }
   }
   ph->left_hole = 0;
-  if (ph->hreg == 1) {
+  if (s->hmat[ph->hreg] < 0) { /* vacuum slab (the gap) */
     move(l, d, tlim);
-    head_cross(s, ph, leave);
+    if (absorb) ph->alive = 0;
+    else head_cross(s, ph, leave);
     return;
   }
-  int mat = ph->hreg == 0 ? s->mat_coll : s->mat_cr;
+  int mat = s->hmat[ph->hreg];
   real mu = interp_row(s->sig + (size_t)s->mat_comp[mat] * s->n_e, ph->ei);
   mu = s->mat_rho[mat] * mu;
   real u = u01_open0(g);
@@ -1135,7 +1193,8 @@ static void head_step(const scene_t *s, photon_t *ph, rng_t *g, tally_t *t, even
   sd = sd / mu;
   if (sd >= tlim) {
     move(l, d, tlim);
-    head_cross(s, ph, leave);
+    if (absorb) ph->alive = 0;
+    else head_cross(s, ph, leave);
     return;
   }
   move(l, d, sd);
@@ -1144,7 +1203,7 @@ static void head_step(const scene_t *s, photon_t *ph, rng_t *g, tally_t *t, even
     if (find_hole(s, l[0], l[1], &cx, &cy)) return; /* null collision inside a hole */
   }
   real ed = interact(s, ph, mat, g, t, NULL, NULL);
-  if (ph->hreg == 2 && ed > R(0)) {
+  if (ph->hreg == s->hreg_cr && ed > R(0)) {
     int h = ph->head;
     ev->esum[h] = ev->esum[h] + ed;
     if (s->centroid) { /* EnergyWeightedCentroidPosition */
@@ -1271,17 +1330,19 @@ static void spect_world_step(const scene_t *s, photon_t *ph, rng_t *g, tally_t *
                              int *has_sec) {
   t->cnt[GG_CNT_WORLD_STEPS]++;
   real tb = ph->exclude != 0 ? entry_distance(ph->pos, ph->dir, s->bmin, s->bmax) : R(INFINITY);
-  int box = 0;
+  int box = 0, bface = 2;
   real hlo[3] = {-s->half_w, -s->half_w, R(0)};
-  real hhi[3] = {s->half_w, s->half_w, s->zb[3]};
+  real hhi[3] = {s->half_w, s->half_w, s->zend};
   for (int h = 0; h < s->n_heads; ++h) {
     if (ph->exclude == 1 + h) continue;
     real lp[3], ld[3];
     to_local(s, h, ph->pos, ph->dir, lp, ld);
-    real th = entry_distance(lp, ld, hlo, hhi);
+    int f;
+    real th = entry_distance_face(lp, ld, hlo, hhi, &f);
     if (th < tb) {
       tb = th;
       box = 1 + h;
+      bface = f;
     }
   }
   real wlo[3] = {-s->whalf[0], -s->whalf[1], -s->whalf[2]};
@@ -1304,6 +1365,9 @@ static void spect_world_step(const scene_t *s, photon_t *ph, rng_t *g, tally_t *
       ph->in_image = 1;
       ph->t_exit = exit_distance(ph->pos, ph->dir, s->bmin, s->bmax);
       ph->head_stage = 0;
+    } else if (s->side_black && bface != 2) {
+      ph->alive = 0; /* stopped by the head's side shielding */
+      t->cnt[GG_CNT_ESCAPED]++;
     } else {
       int h = box - 1;
       real lp[3], ld[3];
@@ -1314,7 +1378,7 @@ static void spect_world_step(const scene_t *s, photon_t *ph, rng_t *g, tally_t *
       }
       ph->in_head = 1;
       ph->head = h;
-      ph->hreg = lp[2] < s->zb[1] ? 0 : (lp[2] < s->zb[2] ? 1 : 2);
+      ph->hreg = head_region(s, lp[2]);
       ph->left_hole = 0;
       /* (scatter splitting: the analog photon dies at the head, only its copies are scored) */
       if (s->arf && !ph->head_stage && s->ff != 2) arf_at_head(s, ph, t);
@@ -1671,24 +1735,27 @@ static void ff_step(const scene_t *s, photon_t *ph, tally_t *t, real cos_min) {
     }
   }
   real tb = R(INFINITY);
-  int box = 0;
+  int box = 0, bface = 2;
   real cos_box = R(0);
   real hlo[3] = {-s->half_w, -s->half_w, R(0)};
-  real hhi[3] = {s->half_w, s->half_w, s->zb[3]};
+  real hhi[3] = {s->half_w, s->half_w, s->zend};
   for (int h = 0; h < s->n_heads; ++h) {
     if (ph->exclude == 1 + h) continue;
     real lp[3], ld[3];
     to_local(s, h, ph->pos, ph->dir, lp, ld);
-    real th = entry_distance(lp, ld, hlo, hhi);
+    int f;
+    real th = entry_distance_face(lp, ld, hlo, hhi, &f);
     if (th < tb) {
       tb = th;
       box = 1 + h;
       cos_box = ld[2];
+      bface = f;
     }
   }
   real wlo[3] = {-s->whalf[0], -s->whalf[1], -s->whalf[2]};
   const real tout = exit_distance(ph->pos, ph->dir, wlo, s->whalf);
-  if (!(tb <= tout) || cos_box < cos_min) {
+  /* (a line into a shielded side face cannot be detected) */
+  if (!(tb <= tout) || cos_box < cos_min || (s->side_black && bface != 2)) {
     ph->alive = 0;
     t->cnt[GG_CNT_ESCAPED]++;
     return;
@@ -1727,7 +1794,7 @@ static void ff_step(const scene_t *s, photon_t *ph, tally_t *t, real cos_min) {
   ph->in_image = 0;
   ph->in_head = 1;
   ph->head = h;
-  ph->hreg = lp[2] < s->zb[1] ? 0 : (lp[2] < s->zb[2] ? 1 : 2);
+  ph->hreg = head_region(s, lp[2]);
   ph->left_hole = 0;
   /* ARF detectors: a photon that reaches a head from the phantom is scored
      by the network with its weight, or tracked (the library's ARF stage) */
@@ -2078,10 +2145,27 @@ static void spect_init(scene_t *s, const gg_spect_desc *sp) {
   s->pnx = sp->size[0];
   s->pny = sp->size[1];
   s->half_w = (real)sp->half_width;
-  s->zb[0] = R(0);
-  s->zb[1] = (real)sp->collimator_thickness;
-  s->zb[2] = (real)(sp->collimator_thickness + sp->gap);
-  s->zb[3] = (real)(sp->collimator_thickness + sp->gap + sp->crystal_thickness);
+  {
+    /* slab boundaries: running sums in double, each rounded once */
+    double z = 0.0;
+    int k = 0;
+    s->zb[0] = R(0);
+#define GGO_SLAB(t, m) (z = z + (t), s->hmat[k] = (m), s->zb[++k] = (real)z)
+    GGO_SLAB(sp->collimator_thickness, sp->collimator_material);
+    GGO_SLAB(sp->gap, -1);
+    if (sp->n_cover > 0) GGO_SLAB(sp->cover_thickness, sp->cover_material);
+    s->hreg_cr = k;
+    GGO_SLAB(sp->crystal_thickness, sp->crystal_material);
+    for (int b = 0; b < sp->n_back; ++b) GGO_SLAB(sp->back_thickness[b], sp->back_material[b]);
+#undef GGO_SLAB
+    s->n_hreg = k;
+    s->zend = s->zb[k];
+    for (int j = k; j < 8; ++j) {
+      s->hmat[j] = -1;
+      s->zb[j + 1] = s->zend;
+    }
+    s->side_black = sp->shielded_sides ? 1 : 0;
+  }
   s->apo = (real)sp->hole_apothem;
   s->px = (real)sp->pitch_x;
   s->py = (real)sp->pitch_y;

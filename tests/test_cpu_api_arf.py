@@ -29,6 +29,7 @@ def _meta(coll="melp", blur=True):
     if blur:
         sp.set_energy_blur("InverseSquare", resolution=0.1, reference=0.208)
         sp.set_spatial_blur(1.5, keep_in_solid_limits=True)
+    sp.housing = "nm670"  # a network of the NM670 head (the contrib helpers build its housing)
     return ARF.head_meta(sp, coll, "3/8")
 
 
@@ -108,8 +109,9 @@ def test_arf_acquisition_takes_windows_and_digitizer_from_the_network(tmp_path):
     assert sp.blur.energy_method == C.GG_BLUR_INVERSE_SQUARE and sp.blur.spatial == 1
     assert sp.collimator_thickness == pytest.approx(40.6)
     model, params, meta = sp.arf
-    # add_arf_detector's depth: collimator + half the crystal
-    assert model.distance_to_crystal == pytest.approx(40.6 + 9.525 / 2)
+    # add_arf_detector's depth: collimator + the housing's aluminium cover + half the crystal
+    assert model.distance_to_crystal == pytest.approx(40.6 + 1.3 + 9.525 / 2)
+    assert sp.housing == "nm670" and sp.desc().n_back == 4 and sp.desc().shielded_sides == 1
     assert head_of == {"arf0": 0, "arf1": 1} and [a.name for a in arfs] == ["arf0_arf", "arf1_arf"]
 
 
