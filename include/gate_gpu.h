@@ -493,7 +493,7 @@ typedef struct {
 /* Generates the training rows of `sampling` on the device and trains the
    network with Adam (cross-entropy, mean over the batch); model_out gets the
    standardisation and domain (theta from sampling, energies from sampling),
-   distance_to_crystal = collimator + gap + half the crystal.  loss (epochs
+   distance_to_crystal = collimator + gap + cover + half the crystal.  loss (epochs
    values, or NULL) = mean loss of each epoch.  The trained model becomes the
    context's ARF model. */
 int gg_arf_train(gg_ctx *ctx, const gg_arf_sampling *sampling, const gg_arf_train_opts *opts,

@@ -1741,7 +1741,8 @@ static gg_arf_model arf_domain_model(const gg_ctx *c, double e_min, double e_max
   m.e_min = e_min;
   m.e_max = e_max;
   m.theta_max_deg = th;
-  m.distance_to_crystal = c->spect.collimator_thickness + c->spect.gap + 0.5 * c->spect.crystal_thickness;
+  m.distance_to_crystal = c->spect.collimator_thickness + c->spect.gap +
+                          (c->spect.n_cover > 0 ? c->spect.cover_thickness : 0.0) + 0.5 * c->spect.crystal_thickness;
   return m;
 }
 

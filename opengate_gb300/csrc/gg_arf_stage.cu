@@ -101,7 +101,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spect_arf(Scene<real> s, ArfS
     long long p_off = -1;
     if (k < n_items) {
       const uint32_t meta = in.meta[k];
-      const bool has_ev = ((meta >> 23) & 1u) != 0u;
+      const bool has_ev = ((meta >> kMetaEv) & 1u) != 0u;
       const real e = in.e[k];
       const real lz = in.pz[k];
       const real dz = in.dz[k];
@@ -129,7 +129,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_spect_arf(Scene<real> s, ArfS
         fy = fy * s.inv_psp[1];
         if (fx >= (real)0 && fx < (real)s.pnx && fy >= (real)0 && fy < (real)s.pny) {
           const int i = (int)fx, j = (int)fy;
-          const int head = (int)((meta >> 20) & 1u);
+          const int head = (int)((meta >> kMetaHead) & 1u);
           const int run = run_of(s, in.hid[k]);
           p_off = (long long)((((size_t)head * s.n_runs + run) * s.n_win) * plane + (size_t)j * s.pnx + i);
         }

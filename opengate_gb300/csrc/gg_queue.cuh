@@ -94,6 +94,11 @@ size_t split_bytes(size_t cap) {
 }
 
 constexpr uint32_t kMetaSteps = (1u << 20) - 1u;
+// meta word above the step count: head (bit 20), head slab (3 bits from 21:
+// up to kHeadRegions slabs), event flag (bit 24), exclude + 1 (from bit 25)
+constexpr int kMetaHead = 20, kMetaReg = 21, kMetaEv = 24, kMetaExcl = 25;
+static_assert(kHeadRegions <= 8, "the head slab index has 3 bits in the queue meta word");
+static_assert(kStepCap <= (int)kMetaSteps, "the step count has 20 bits in the queue meta word");
 constexpr int kPush = 4;  // lane state: photon leaves this stage through the output queue
 
 // Tables of the block in shared memory (majorant, attenuation rows, label ->
@@ -164,8 +169,9 @@ __device__ __forceinline__ void queue_put(const PQueue<real> &q, size_t k, const
 #pragma unroll
     for (int i = 0; i < kEvSlots; ++i) q.ev[i][k] = ev[i];
   }
-  q.meta[k] = ((uint32_t)ph.steps & kMetaSteps) | ((uint32_t)ph.head << 20) | ((uint32_t)ph.hreg << 21) |
-              ((has_ev ? 1u : 0u) << 23) | ((uint32_t)(ph.exclude + 1) << 24);
+  q.meta[k] = ((uint32_t)ph.steps & kMetaSteps) | ((uint32_t)ph.head << kMetaHead) |
+              ((uint32_t)ph.hreg << kMetaReg) | ((has_ev ? 1u : 0u) << kMetaEv) |
+              ((uint32_t)(ph.exclude + 1) << kMetaExcl);
 }
 
 // Reads slot k of an input queue into the lane (photon state as it was when
@@ -187,10 +193,10 @@ __device__ __forceinline__ uint64_t queue_get(const Scene<real> &s, const PQueue
   else ph.w = R<real>(1);
   const uint32_t m = q.meta[k];
   ph.steps = (int)(m & kMetaSteps);
-  ph.head = (int)((m >> 20) & 1u);
-  ph.hreg = (int)((m >> 21) & 3u);
-  has_ev = ((m >> 23) & 1u) != 0u;
-  ph.exclude = (int)((m >> 24) & 7u) - 1;
+  ph.head = (int)((m >> kMetaHead) & 1u);
+  ph.hreg = (int)((m >> kMetaReg) & 7u);
+  has_ev = ((m >> kMetaEv) & 1u) != 0u;
+  ph.exclude = (int)((m >> kMetaExcl) & 7u) - 1;
   ph.alive = 1;
   ph.can_enter = 1;
   ph.left_hole = 0;
