@@ -755,8 +755,9 @@ class ArfRecipe:
         tvp = np.maximum((st["wp2"].sum(axis=(2, 3)) / n_p - tp * tp) / (n_p - 1), 0.0)
         ch = st["chunk_totals"]
         t = tp + ch.sum(axis=0) / n_s
-        tv = tvp + j * ch.var(axis=0, ddof=1) / n_s ** 2
-        return m, vp + vs, t, tv
+        tvs = j * ch.var(axis=0, ddof=1) / n_s ** 2
+        self.parts_var = (vp, vs, tvp, tvs)  # per-pass variances (allocation report)
+        return m, vp + vs, t, tvp + tvs
 
     def compare(self, n_per_run, seed, first_arf, first_plain, arf_ms=None):
         """Matched-sigma comparison: one ARF acquisition and one plain acquisition of
@@ -800,6 +801,25 @@ class ArfRecipe:
             r = float(ta.sum() / (tpl.sum() / n))
             out["window_totals_arf_over_plain"].append(r)
             out["window_ratio_sigma"].append(r * math.sqrt(va.sum() / ta.sum() ** 2 + 1.0 / tpl.sum()))
+        # allocation between the passes: each pass's share of the relative variance (peak-window
+        # pixels; projection totals of window 0) and the efficiency of the best split of the
+        # time between them, (sqrt(A t_p) + sqrt(B t_s))^-2 for variance shares A, B and pass
+        # times t_p, t_s (variance of a pass ~ 1 / its primaries, time ~ its primaries)
+        vp, vs, tvp, tvs = self.parts_var
+        t_p, t_s = parts["primary_pass"], parts["scatter_pass"]
+        alloc = {"primary_ms": t_p, "scatter_ms": t_s, "scatter_share": 1.0 / self.share}
+        for key, (a_, b_, mm, sel_) in {"pixel_peak_window": (vp[:, 0::nw], vs[:, 0::nw], pk, sel),
+                                         "projection_window_0": (tvp[:, 0::nw], tvs[:, 0::nw], t[:, 0::nw],
+                                                                 t[:, 0::nw] > 0)}.items():
+            a = float((a_[sel_] / mm[sel_] ** 2).mean())
+            b = float((b_[sel_] / mm[sel_] ** 2).mean())
+            best = (math.sqrt(a * t_p) + math.sqrt(b * t_s)) ** 2
+            plain = (sig_p_pix ** 2 * ms_p) if key.startswith("pixel") else \
+                out["projection_totals"]["window_0"]["sigma_plain"] ** 2 * ms_p
+            alloc[key] = {"rel_var_primary": a, "rel_var_scatter": b,
+                          "best_scatter_share": 1.0 / self.share * math.sqrt(b * t_p / max(a * t_s, 1e-300)),
+                          "efficiency_gain_at_best_split": plain / best}
+        out["allocation"] = alloc
         cnt = {f"primary_{k}": st["counters_primary"][k] for k in ("world_steps", "arf_photons", "arf_fallback")}
         cnt.update({f"scatter_{k}": st["counters_scatter"][k] for k in ("woodcock_steps", "arf_photons",
                                                                         "arf_fallback")})
@@ -1272,6 +1292,8 @@ def run_ours(args):
     scene, _ = W.ct_phantom()
     n = args.primaries
     eng = DoseEngine(scene, device=local, precision=32, batch=args.batch)
+    kernel = {"phased": C.GG_KERNEL_PHASED, "wavefront": C.GG_KERNEL_WAVEFRONT}[args.transport_kernel]
+    eng.set_transport_kernel(kernel)
     l2_flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=f"cuda:{local}")
     # history ranges are disjoint across ranks and steps
     def first_of(step):
@@ -1354,7 +1376,8 @@ def run_ours(args):
                 "frac": achieved / peak, "traffic": traffic,
                 "traffic_note": None if args.traffic is not None else
                 "ncu dram bytes of a 3e6-primary launch of this workload, scaled by primaries",
-                "peak_kind": peak_kind, "kernel": "k_transport<float>",
+                "peak_kind": peak_kind,
+                "kernel": "k_transport<float>" if args.transport_kernel == "phased" else "k_wavefront<float>",
                 "bytes_alg_per_step": bytes_alg,
                 "units": {"woodcock_steps": counters["woodcock_steps"], "tally_entries": counters["tally_entries"],
                           "transport_launches_per_step": transport_launches},
@@ -1384,6 +1407,7 @@ def run_ours(args):
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded CT phantom)",
             "config": {"workload": WORKLOAD, "primaries_per_step": n, "tally": "fp64 edep + edep^2, history-by-history",
+                       "transport_kernel": args.transport_kernel,
                        "l2": "flushed between steps (256 MiB write)", "batch": args.batch,
                        "parallelism": f"replicas x{ws}, disjoint history ranges"},
             "sigma": {"mean_relative_uncertainty_gt10pct_max": sigma, "primaries": n_merged},
@@ -1430,6 +1454,8 @@ def main():
     ap.add_argument("--batch", type=int, default=1 << 27)
     ap.add_argument("--seed", type=int, default=20240611)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--transport-kernel", default="phased", choices=["phased", "wavefront"],
+                    help="dose workload: the phase kernel (default) or the compacted wavefront kernel")
     ap.add_argument("--no-arf-summary", action="store_true",
                     help="dose workload: skip the reduced spect_arf comparison carried by its line")
     ap.add_argument("--fp64-primaries", type=int, default=10_000_000,
