@@ -71,13 +71,13 @@ ARF_DECAYS = 10_000_000_000
 ARF_YIELD = 0.166
 ARF_WINDOWS = ((0.1872, 0.2288), (0.166, 0.187), (0.1017, 0.1243))
 ARF_TRAIN_SAMPLES = 200_000_000
-ARF_PRIMARY_DEG = 15.0  # primary pass: angle tolerance of the source's angular acceptance
-ARF_SPLIT = (10, 2, 10000, 15.0)  # scatter pass: Compton, Rayleigh factors, max Compton level, angle tolerance
+ARF_PRIMARY_DEG = 10.0  # primary pass: angle tolerance of the source's angular acceptance
+ARF_SPLIT = (10, 2, 10000, 10.0)  # scatter pass: Compton, Rayleigh factors, max Compton level, angle tolerance
 ARF_SCATTER_SHARE = 8  # the scatter pass runs 1 / 8 of the primaries
 ARF_CHUNKS = 16  # ... in independent chunks (its variance)
 ARF_SUMMARY_PRIMARIES = 240_000_000  # reduced comparison carried by the default (dose) line
 ARF_WORKLOAD = ("spect_lu177_melp_nm670housing_2heads_120angles_r250mm_128x128x4.42mm_windows187-229_166-187_101-125keV_"
-                "ct_phantom_256x256x160_1.2mm_arf_mlp3x128_bf16_freeflight_aa15deg+scattersplit_c10_r2_aa15deg_1of8")
+                "ct_phantom_256x256x160_1.2mm_arf_mlp3x128_bf16_freeflight_aa10deg+scattersplit_c10_r2_aa10deg_1of8")
 
 
 def measured_peaks():
@@ -786,10 +786,24 @@ class ArfRecipe:
         sig_a_pix = float((np.sqrt(v[:, 0::nw][sel]) / pk[sel]).mean())
         sig_p_pix = S.mean_relative_uncertainty(cp[:, 0::nw], cp[:, 0::nw], n)
         tp = cp.sum(axis=(2, 3))
+        # the same pixels for both arms (peak-window pixels above 10 % of the primary pass's
+        # maximum: its mean image is the least noisy), relative variances against the ARF mean
+        # image; plain: Poisson variance of the counts
+        mpk = st["wp"][:, 0::nw] / st["n_p"]
+        mask = (mpk > 0.1 * mpk.max()) & (pk > 0)
+        rv_a = float((v[:, 0::nw][mask] / pk[mask] ** 2).mean())
+        rv_p = float((cp[:, 0::nw][mask] / float(n) ** 2 / pk[mask] ** 2).mean())
         out = {"arf_ms": ms_a, "plain_ms": ms_p, "primaries": n, "scatter_pass_primaries": st["n_s"],
                "arf_ms_per_pass": parts,
                "pixel_peak_window": {"sigma_arf": sig_a_pix, "sigma_plain": sig_p_pix,
-                                     "efficiency_gain": (sig_p_pix ** 2 * ms_p) / (sig_a_pix ** 2 * ms_a)},
+                                     "efficiency_gain": (sig_p_pix ** 2 * ms_p) / (sig_a_pix ** 2 * ms_a),
+                                     "method": "mean relative sigma over each arm's pixels > 10 % of its max "
+                                               "(the reference's per-pixel figure)"},
+               "pixel_peak_window_common_mask": {
+                   "pixels": int(mask.sum()), "rel_var_arf": rv_a, "rel_var_plain": rv_p,
+                   "efficiency_gain": (rv_p * ms_p) / (rv_a * ms_a),
+                   "method": "mean relative variance over the same pixels (> 10 % of the primary pass's "
+                             "max), both against the ARF mean image"},
                "projection_totals": {}, "window_totals_arf_over_plain": [], "window_ratio_sigma": []}
         for w in range(nw):
             ta, va, tpl = t[:, w::nw], tv[:, w::nw], tp[:, w::nw]
@@ -1048,6 +1062,24 @@ def run_ours_batched(args, ws, rank, local, dist, use_cuda):
     # counters of the last step (the tally and counters are reset before each replay)
     bytes_alg = 32.0 * counters["woodcock_steps"] + 64.0 * counters["tally_entries"]
     achieved = bytes_alg / (total_ms / args.steps / 1e3) / 1e9
+    # FP32 against the FP64 build on the same histories (untimed), per simulation
+    fp64 = None
+    if rank == 0 and args.fp64_primaries > 0:
+        from opengate_gb300.dose import precision_error
+
+        imgs = {}
+        rate = {}
+        for prec in (32, 64):
+            with BatchEngine(sims, device=local, precision=prec) as e:
+                e.run()
+                g, t, f, _ = e.last_kernel_ms()
+                rate[prec] = n / ((g + t + f) / 1e3)
+                imgs[prec] = [(e.image(k, C.GG_IMG_EDEP), e.image(k, C.GG_IMG_EDEP_SQUARED)) for k in range(len(sims))]
+        errs = [precision_error(a[0], a[1], b[0], b[1], k) for a, b, (_, k, _) in zip(imgs[32], imgs[64], sims)]
+        fp64 = {"simulations": len(errs), "primaries": n,
+                "integral_rel_max": max(e["integral_rel"] for e in errs),
+                "within_2sigma_min": min(e.get("within_2sigma", 1.0) for e in errs),
+                "rate_f32": rate[32], "rate_f64": rate[64], "voxels_gt": "10 % of max, per simulation"}
     if rank == 0:
         line = {
             "metric": BATCH_METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
@@ -1065,6 +1097,7 @@ def run_ours_batched(args, ws, rank, local, dist, use_cuda):
                                      "search": tune, "seconds": tune_s},
                        "parallelism": f"replicas x{ws}, independent batches"},
             "sequential": {"primaries_per_s": n / (seq_ms / 1e3), "note": "gg_run per simulation, same context"},
+            "fp64_error": fp64,
             "e2e": {"value": ws * n / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h)},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak_bw, "unit": "GB/s",
@@ -1073,7 +1106,7 @@ def run_ours_batched(args, ws, rank, local, dist, use_cuda):
                          "bytes_alg_per_step": bytes_alg, "note": "graph replay time includes source and flush"},
             "cpu_baseline": None,
             "clocks": clk.summary(),
-            "gpu_launches": int(len(dev_ms) * 3 * max(1, -(-n // (1 << 24)))),
+            "gpu_launches": int(len(dev_ms) * 3 * max(1, -(-n // max(1, int(best.batch))))),
             "wall_s": wall,
         }
         print(json.dumps(line), flush=True)
