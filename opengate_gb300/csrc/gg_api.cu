@@ -2112,7 +2112,9 @@ int gg_batch_autotune(gg_ctx *c, gg_device_opts *best) {
   if ((st = time_point(cur))) return st;
   c->tune.default_median_ms = cur[0];
   double bst[3] = {cur[0], cur[1], cur[2]};
-  int bm = c->blocks_per_sm, br = c->refill_min, bi = c->interact_min, bc = c->chunk;
+  // the starting configuration as run_impl resolves it (0 blocks per SM = its default)
+  int bm = c->blocks_per_sm > 0 ? std::min(c->blocks_per_sm, 4) : (c->precision == GG_PREC_F64 || c->have_batch ? 2 : 4);
+  int br = c->refill_min, bi = c->interact_min, bc = c->chunk;
   int64_t bb = c->batch;
   // stage 1: resident blocks per SM x phase thresholds
   const int minbs[3] = {2, 3, 4};
