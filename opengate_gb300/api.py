@@ -225,8 +225,12 @@ class GenericSource(GateObject):
                        "spectrum_energy_bin_edges": [], "spectrum_histogram_interpolation": None}),
     }
 
-    def to_spec(self, volumes):
-        """SourceSpec (mm, rad, MeV) of this source; raises on unsupported options."""
+    def to_spec(self, volumes, free_flight=False):
+        """SourceSpec (mm, rad, MeV) of this source; raises on unsupported options.  With
+        ``free_flight`` (a GammaFreeFlightActor on the world, the SPECT heads excluded) the
+        angular acceptance (intersection + angle check against the heads, as the reference's
+        free-flight recipe sets it, contrib/spect/spect_config.py:937-970) is applied by the
+        free flight itself: its tolerance is returned in ``spec.ff_angle_tolerance`` (rad)."""
         if self.particle != "gamma":
             raise NotImplementedError(f"source '{self.name}': only gamma primaries are transported")
         if self.attached_to != "world":
@@ -252,7 +256,17 @@ class GenericSource(GateObject):
         s.momentum = [float(x) for x in d.momentum]
         s.focus = [float(x) for x in d.focus_point]
         aa = d.angular_acceptance
-        if aa.policy:
+        s.ff_angle_tolerance = 0.0
+        if aa.policy and free_flight:
+            if aa.policy != "Rejection" or aa.skip_policy != "SkipEvents":
+                raise NotImplementedError("angular acceptance with free flight: policy 'Rejection', 'SkipEvents'")
+            if aa.enable_angle_check:
+                if float(aa.angle_check_proximity_distance) != 0.0 or float(aa.angle_tolerance_min) != 0.0:
+                    raise NotImplementedError("angular acceptance: angle_tolerance_max only (no proximity, "
+                                              "no minimum)")
+                s.ff_angle_tolerance = float(aa.angle_tolerance_max) / u.rad
+            # the intersection check is the flight's own: a line that misses every head stops
+        elif aa.policy:
             if aa.policy != "Rejection" or aa.skip_policy != "SkipEvents" or aa.enable_angle_check or \
                     not aa.enable_intersection_check:
                 raise NotImplementedError("angular acceptance: only policy 'Rejection' with 'SkipEvents' and "
@@ -298,11 +312,11 @@ class VoxelSource(GenericSource):
     type_name = "VoxelSource"
     user_info_defaults = dict(GenericSource.user_info_defaults, image=None)
 
-    def to_spec(self, volumes):
+    def to_spec(self, volumes, free_flight=False):
         p = self.position
         if p.type not in ("point", None) or p.confine:
             raise NotImplementedError("VoxelSource: position.type / confine are set by the image")
-        s = GenericSource.to_spec(self, volumes)
+        s = GenericSource.to_spec(self, volumes, free_flight=free_flight)
         img = self.image
         if isinstance(img, (str, pathlib.Path)):
             img = image_io.read_mhd(img)
@@ -851,7 +865,7 @@ class Simulation:
             return int.from_bytes(os.urandom(8), "little")
         return int(self.random_seed) & 0xFFFFFFFFFFFFFFFF
 
-    def build_scene(self, extra_materials=()):
+    def build_scene(self, extra_materials=(), free_flight=False):
         """(scene, image volume, HU image, material names by label, sources) for this configuration."""
         images = [v for v in self.volumes.values() if isinstance(v, ImageVolume)]
         if len(images) != 1:
@@ -881,7 +895,7 @@ class Simulation:
         sources = [s for s in self.sources.values()]
         if not sources:
             raise ValueError("no source")
-        specs = [s.to_spec(self.volumes) for s in sources]
+        specs = [s.to_spec(self.volumes, free_flight=free_flight) for s in sources]
         emax = max(sp.energy_bounds()[1] for sp in specs)
         self.physics_manager.check_supported(emax)
         half = [float(x) / 2.0 for x in self.world.size]
@@ -959,7 +973,11 @@ class Simulation:
             raise ValueError(f"network '{arfs[0].pth_filename}' was trained for the housing "
                              f"'{arf[2].get('housing', 'none')}', the heads have '{housing}'")
         extra = [h0.collimator_material, h0.crystal_material] + list(S.HOUSING_MATERIALS.get(housing, ()))
-        scene, vol, hu, names, sources = self.build_scene(extra_materials=extra)
+        ffs = [a for a in self.actors.values() if isinstance(a, GammaFreeFlightActor)]
+        sss = [a for a in self.actors.values() if isinstance(a, ScatterSplittingFreeFlightActor)]
+        if len(ffs) + len(sss) > 1:
+            raise NotImplementedError("one free-flight actor (GammaFreeFlightActor or ScatterSplittingFreeFlightActor)")
+        scene, vol, hu, names, sources = self.build_scene(extra_materials=extra, free_flight=bool(ffs))
         coll = S.COLLIMATORS.get(str(h0.collimator_type).lower())
         if coll is None:
             raise NotImplementedError(f"collimator '{h0.collimator_type}'")
@@ -975,27 +993,27 @@ class Simulation:
             sp.half_width = half_w
         sp.apply_housing(housing, names.index)
         sp.arf = arf
-        if arf is not None:
-            ARF.apply_head_meta(sp, arf[2])
-            mods = [a.name for a in self.actors.values()
-                    if isinstance(a, (DigitizerAdderActor, DigitizerBlurringActor, DigitizerSpatialBlurringActor,
-                                      GammaFreeFlightActor, ScatterSplittingFreeFlightActor))]
-            if mods:
-                raise NotImplementedError(f"with ARF detectors the digitizer is the network's own: remove {mods}")
-            return scene, sp, sources, arfs, head_of
-        ffs = [a for a in self.actors.values() if isinstance(a, GammaFreeFlightActor)]
-        sss = [a for a in self.actors.values() if isinstance(a, ScatterSplittingFreeFlightActor)]
-        if len(ffs) + len(sss) > 1:
-            raise NotImplementedError("one free-flight actor (GammaFreeFlightActor or ScatterSplittingFreeFlightActor)")
+        # free flight (with ARF detectors too: the reference's recipes with ARF detectors)
         if ffs:
             ffs[0].check(heads)
-            sp.set_free_flight(float(ffs[0].weight_cutoff), float(ffs[0].energy_cutoff) / u.MeV)
+            tols = {spec.ff_angle_tolerance for _, spec in sources}
+            if len(tols) > 1:
+                raise NotImplementedError("sources with different angle checks")
+            sp.set_free_flight(float(ffs[0].weight_cutoff), float(ffs[0].energy_cutoff) / u.MeV,
+                               angle_tolerance_max=tols.pop())
         if sss:
             ss = sss[0]
             ss.check(heads)
             nc, nr, tol = ss.factors()
             sp.set_scatter_splitting(nc, nr, int(ss.max_compton_level), float(ss.weight_cutoff),
                                      float(ss.energy_cutoff) / u.MeV, tol)
+        if arf is not None:
+            ARF.apply_head_meta(sp, arf[2])
+            mods = [a.name for a in self.actors.values()
+                    if isinstance(a, (DigitizerAdderActor, DigitizerBlurringActor, DigitizerSpatialBlurringActor))]
+            if mods:
+                raise NotImplementedError(f"with ARF detectors the digitizer is the network's own: remove {mods}")
+            return scene, sp, sources, arfs, head_of
         # digitizer adder and blurring: one setting shared by every head's crystal
         def set_policy(policy):
             sp.adder_policy = policy

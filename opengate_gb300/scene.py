@@ -29,6 +29,7 @@ class SourceSpec:
         self.momentum = [0.0, 0.0, 1.0]
         self.focus = [0.0, 0.0, 0.0]
         self.accept_boxes = []  # list of (min xyz, max xyz)
+        self.ff_angle_tolerance = 0.0  # angle check applied by a free flight (rad, 0 = none)
         self.max_rejection = 10000
         self.ene_type = C.GG_ENE_MONO
         self.mono = 1.0

@@ -176,3 +176,47 @@ def test_digitizer_has_an_energy_windows_module(tmp_path):
     d = nm670.add_digitizer(sim, crystal.name)
     ew = d.find_module("energy_window")
     assert ew.type_name == "DigitizerEnergyWindowsActor" and ew.channels == d.projection.channels
+
+
+def _ff_arf_sim(tmp_path, model_path, deg=10.0, n=1000):
+    """The reference's primary free-flight recipe (spect_config.py:937-970) with ARF detectors:
+    GammaFreeFlightActor on the world with the detection planes excluded, the source's angular
+    acceptance with the intersection and angle checks against the planes."""
+    sim, dets = _arf_sim(tmp_path, model_path, n=n)
+    ff = sim.add_actor("GammaFreeFlightActor", "ff")
+    ff.attached_to = "world"
+    ff.exclude_volumes = [p.name for p, _ in dets]
+    aa = sim.sources["s"].direction.angular_acceptance
+    aa.policy = "Rejection"
+    aa.skip_policy = "SkipEvents"
+    aa.target_volumes = [p.name for p, _ in dets]
+    aa.enable_intersection_check = True
+    aa.enable_angle_check = True
+    aa.angle_tolerance_max = deg * u.deg
+    return sim, dets
+
+
+def test_free_flight_with_arf_detectors_maps_to_the_engine(tmp_path):
+    _model_file(tmp_path / "net.npz")
+    sim, dets = _ff_arf_sim(tmp_path, tmp_path / "net.npz", deg=12.0)
+    scene, sp, sources, arfs, head_of = sim.build_spect()
+    assert sp.arf is not None and sp.free_flight.enabled == C.FF_PRIMARY
+    assert sp.free_flight.angle_tolerance_max == pytest.approx(np.radians(12.0))
+    assert sources[0][1].accept_boxes == []  # the acceptance is the free flight's own
+    # scatter splitting with ARF detectors
+    sim2, dets2 = _arf_sim(tmp_path / "b", tmp_path / "net.npz")
+    ss = sim2.add_actor("ScatterSplittingFreeFlightActor", "ss")
+    ss.exclude_volumes = ss.kill_interacting_in_volumes = [p.name for p, _ in dets2]
+    ss.compton_splitting_factor, ss.rayleigh_splitting_factor = 8, 2
+    ss.angular_acceptance.policy = "Rejection"
+    ss.angular_acceptance.enable_angle_check = True
+    ss.angular_acceptance.angle_tolerance_max = 20 * u.deg
+    _, sp2, *_ = sim2.build_spect()
+    assert sp2.arf is not None and sp2.free_flight.enabled == C.FF_SCATTER
+    assert (sp2.free_flight.compton_splitting, sp2.free_flight.rayleigh_splitting) == (8, 2)
+    # an angle check without free flight is still refused
+    sim3, _ = _arf_sim(tmp_path / "c", tmp_path / "net.npz")
+    aa = sim3.sources["s"].direction.angular_acceptance
+    aa.policy, aa.enable_intersection_check, aa.enable_angle_check = "Rejection", True, True
+    with pytest.raises(NotImplementedError):
+        sim3.build_spect()

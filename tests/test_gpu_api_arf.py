@@ -82,3 +82,45 @@ def test_arf_train_save_load_acquire(tmp_path, built_lib):
         np.testing.assert_array_equal(got, (counts[h] + w[h]).astype(np.float32))
         np.testing.assert_array_equal(got2, (counts[h] + w2[h]).astype(np.float32))
     assert len(LU177) == sp.n_windows
+
+
+def test_free_flight_recipe_with_arf_detectors_through_the_api(tmp_path, built_lib):
+    """GammaFreeFlightActor + the source's angular acceptance (angle check 12 degrees) + ARF
+    detectors through Simulation.run(): the written images equal the weighted projection of the
+    same histories run directly (free flight + gg_spect_use_arf)."""
+    import ctypes
+
+    from opengate_gb300 import _capi as C
+    from opengate_gb300 import image_io
+    from opengate_gb300.engine import ArfNetwork, SpectEngine
+
+    from .test_cpu_api_arf import _ff_arf_sim, _model_file
+
+    _model_file(tmp_path / "net.npz")
+    n = 300_000
+    sim, dets = _ff_arf_sim(tmp_path / "acq", tmp_path / "net.npz", deg=12.0, n=n)
+    for _, a in dets:
+        a.squared_counts.active = True
+    sim.random_seed = 4242
+    sim.run()
+    scene, sp, sources, arfs, head_of = sim.build_spect()
+    assert sp.free_flight.enabled == C.FF_PRIMARY
+    with SpectEngine(scene, sp) as e:
+        ArfNetwork(e).set_model(sp.arf[0], sp.arf[1])
+        e.use_arf(True)
+        first = 0
+        for r in range(sp.n_runs):
+            frames = np.ascontiguousarray(sp.frames(r), dtype=np.float64)
+            e._call("gg_spect_set_heads", r, C.ptr(frames, ctypes.c_double))
+            e._call("gg_run", ctypes.c_uint64(n), ctypes.c_uint64(4242), ctypes.c_uint64(first))
+            first += n
+        counts = e.projection()
+        w, w2 = e.arf_projection(squared=True)
+        cnt = e.counters()
+    assert counts.sum() == 0 and cnt["arf_photons"] > 100 and w.sum() > 0
+    for _, a in dets:
+        h = head_of[a.attached_to]
+        got = image_io.read_mhd(a.counts.get_output_path()).array
+        got2 = image_io.read_mhd(a.squared_counts.get_output_path()).array
+        np.testing.assert_array_equal(got, w[h].astype(np.float32))
+        np.testing.assert_array_equal(got2, w2[h].astype(np.float32))
