@@ -34,6 +34,10 @@ METRIC = "primaries/s at matched sigma (plain GPU transport, CT phantom dose)"
 UNIT = "primaries/s"
 PRIMARIES_PER_STEP = 100_000_000
 TRANSPORT_DRAM_PER_PRIMARY = (478.16e6 + 200.48e6) / 3e6  # bytes, ncu capture of the dose workload
+# warp instructions per primary of the dose transport kernels and their active lanes per warp
+# instruction (ncu captures of the same workload, 3e6 primaries: smsp__inst_executed.sum and
+# smsp__thread_inst_executed_per_inst_executed.ratio; phase kernel, compacted wavefront kernel)
+TRANSPORT_ISSUE = {"phased": (1.185021951e9 / 3e6, 9.05), "wavefront": (1.045618891e9 / 3e6, 14.12)}
 WORKLOAD = "ct_phantom_256x256x160_1.2mm_ssd100_field10x10_spectrum60_0.1-6MeV"
 
 # SPECT acquisition: CT phantom as attenuation map, Tc-99m activity image,
@@ -75,7 +79,7 @@ ARF_PRIMARY_DEG = 10.0  # primary pass: angle tolerance of the source's angular 
 ARF_SPLIT = (10, 2, 10000, 10.0)  # scatter pass: Compton, Rayleigh factors, max Compton level, angle tolerance
 ARF_SCATTER_SHARE = 8  # the scatter pass runs 1 / 8 of the primaries
 ARF_CHUNKS = 16  # ... in independent chunks (its variance)
-ARF_SUMMARY_PRIMARIES = 240_000_000  # reduced comparison carried by the default (dose) line
+ARF_SUMMARY_PRIMARIES = 600_000_000  # reduced comparison carried by the default (dose) line
 ARF_WORKLOAD = ("spect_lu177_melp_nm670housing_2heads_120angles_r250mm_128x128x4.42mm_windows187-229_166-187_101-125keV_"
                 "ct_phantom_256x256x160_1.2mm_arf_mlp3x128_bf16_freeflight_aa10deg+scattersplit_c10_r2_aa10deg_1of8")
 
@@ -1280,7 +1284,6 @@ def run_ours_tle(args, ws, rank, local, dist, use_cuda):
                               "note": "efficiency = 1 / (sigma^2 T), sigma = mean relative uncertainty "
                                       "over voxels > 10 % of max"},
             "fp64_error": fp64,
-            "spect_arf_efficiency": arf,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": None, "peak_kind": peak_kind, "kernel": "k_transport<float> (estimator)",
@@ -1416,6 +1419,20 @@ def run_ours(args):
                           "transport_launches_per_step": transport_launches},
                 "stage_ms_per_step": stage_ms}
 
+    # issue roofline of the transport kernel: warp instructions per second against the SMs'
+    # issue peak (4 schedulers per SM, one warp instruction per cycle each, at the sampled clock)
+    clk_summary = clk.summary()
+    mhz = (clk_summary or {}).get("sm_mhz") or (clk_summary or {}).get("sm_max_mhz") or 2070.0
+    n_sm = torch.cuda.get_device_properties(local).multi_processor_count
+    issue_peak = n_sm * 4 * mhz * 1e6
+    inst_pp, lanes = TRANSPORT_ISSUE[args.transport_kernel]
+    issue_ach = inst_pp * n / (transport_ms / 1e3)
+    roofline_issue = {"bound": "issue", "achieved": issue_ach, "peak": issue_peak, "unit": "warp instructions/s",
+                      "frac": issue_ach / issue_peak, "active_lanes_per_instruction": lanes,
+                      "lane_weighted_frac": issue_ach / issue_peak * lanes / 32.0,
+                      "note": "warp instructions per primary from an ncu capture of this kernel on this "
+                              "workload (3e6 primaries) x primaries / CUDA-event transport time; peak = SMs x 4 "
+                              "schedulers x the median sampled SM clock"}
     # error of the FP32 transport against the FP64 build on the same random stream (untimed)
     fp64 = None
     if rank == 0 and args.fp64_primaries > 0:
@@ -1451,8 +1468,9 @@ def run_ours(args):
             "spect_arf_efficiency": arf,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
             "roofline": roofline,
+            "roofline_issue": roofline_issue,
             "cpu_baseline": cpu,
-            "clocks": clk.summary(),
+            "clocks": clk_summary,
             "gpu_launches": int(launches),
             "wall_s": wall,
         }
