@@ -738,15 +738,22 @@ __device__ __forceinline__ void voxel_walk(const Scene<real> &s, const real p[3]
   }
 }
 
+// Label gathers in flight per lane in the track-length estimator's walks.
+constexpr int kTleGroup = 4;
+
+template <typename real, int GROUP, typename Visit>
+__device__ __forceinline__ void voxel_walk_grouped(const Scene<real> &s, const real p[3], const real d[3], real len,
+                                                   Visit &&visit);
+
 // Track-length estimator (GateTLEDoseActor::ScoreTLEDepositStep,
 // core/opengate_core/opengate_lib/GateTLEDoseActor.cpp:249-299): the straight
 // path [p, p + len d) of a photon of energy e (table index ei) scores
 // e * mu_en(E, material) * length in every voxel it crosses.
-template <typename real>
+template <typename real, int GROUP = kTleGroup>
 __device__ __forceinline__ void tle_path(const Scene<real> &s, const real p[3], const real d[3], real len, real e,
                                          const EIdx<real> &ei, HistList<real> &l, const Tally<real> &t,
                                          BlockCounters *bc, unsigned int &n_dep) {
-  voxel_walk(s, p, d, len, [&](uint32_t v, int m, real seg) {
+  voxel_walk_grouped<real, GROUP>(s, p, d, len, [&](uint32_t v, int m, real seg) {
     real mu = interp_row(s.muen + (size_t)s.mat_comp[m] * s.n_e, ei);
     mu = s.mat_rho[m] * mu;
     real ed = e * mu;
@@ -755,24 +762,16 @@ __device__ __forceinline__ void tle_path(const Scene<real> &s, const real p[3], 
   });
 }
 
-// Optical depth of the straight path [p, p + len d) inside the image:
-// sum of mu(E, material) * length over the voxels it crosses.  GROUP > 1:
-// the same walk (voxel_walk's arithmetic, step for step) in groups of GROUP
-// boundary crossings: the crossings of a group are computed first, then
-// their label gathers are issued together and the terms are added in walk
-// order, so up to GROUP loads are in flight per lane instead of one and the
-// sum is bit for bit voxel_walk's.
-template <typename real, int GROUP>
-__device__ __forceinline__ real image_depth(const Scene<real> &s, const real p[3], const real d[3], real len,
-                                           const EIdx<real> &ei) {
-  real tau = R<real>(0);
+// voxel_walk in groups of GROUP boundary crossings: the crossings of a group
+// are computed first (voxel_walk's arithmetic, step for step), then their
+// label gathers are issued together and visit() runs for each in walk order,
+// so up to GROUP loads are in flight per lane instead of one and every
+// visitor sees exactly voxel_walk's sequence.
+template <typename real, int GROUP, typename Visit>
+__device__ __forceinline__ void voxel_walk_grouped(const Scene<real> &s, const real p[3], const real d[3], real len,
+                                                   Visit &&visit) {
   if constexpr (GROUP == 1) {
-    voxel_walk(s, p, d, len, [&](uint32_t, int m, real seg) {
-      real mu = interp_row(s.sig + (size_t)s.mat_comp[m] * s.n_e, ei);
-      mu = s.mat_rho[m] * mu;
-      mu = mu * seg;
-      tau = tau + mu;
-    });
+    voxel_walk(s, p, d, len, visit);
   } else {
     const int n0 = s.nx, n1 = s.ny, n2 = s.nz;
     int i0 = (int)((p[0] - s.bmin[0]) * s.inv_sp[0]);
@@ -864,17 +863,25 @@ __device__ __forceinline__ real image_depth(const Scene<real> &s, const real p[3
 #pragma unroll
       for (int j = 0; j < GROUP; ++j) lab[j] = ok[j] ? (int)__ldg(s.labels + vv[j]) : 0;
 #pragma unroll
-      for (int j = 0; j < GROUP; ++j) {
-        if (ok[j]) {
-          const int m = lab[j];
-          real mu = interp_row(s.sig + (size_t)s.mat_comp[m] * s.n_e, ei);
-          mu = s.mat_rho[m] * mu;
-          mu = mu * sg[j];
-          tau = tau + mu;
-        }
-      }
+      for (int j = 0; j < GROUP; ++j)
+        if (ok[j]) visit(vv[j], lab[j], sg[j]);
     }
   }
+}
+
+// Optical depth of the straight path [p, p + len d) inside the image:
+// sum of mu(E, material) * length over the voxels it crosses (GROUP: label
+// gathers in flight per lane, voxel_walk_grouped).
+template <typename real, int GROUP>
+__device__ __forceinline__ real image_depth(const Scene<real> &s, const real p[3], const real d[3], real len,
+                                           const EIdx<real> &ei) {
+  real tau = R<real>(0);
+  voxel_walk_grouped<real, GROUP>(s, p, d, len, [&](uint32_t, int m, real seg) {
+    real mu = interp_row(s.sig + (size_t)s.mat_comp[m] * s.n_e, ei);
+    mu = s.mat_rho[m] * mu;
+    mu = mu * seg;
+    tau = tau + mu;
+  });
   return tau;
 }
 
