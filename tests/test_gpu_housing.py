@@ -88,3 +88,24 @@ def test_housing_changes_the_acquisition_as_expected():
     r113 = tot["nm670"][2] / tot["sides"][2]
     r208 = tot["nm670"][0] / tot["sides"][0]
     assert r113 < 0.97 and r208 < 1.01 and r113 < r208
+
+
+def test_housing_and_dose_grid_arguments_are_checked():
+    """gg_spect_setup refuses housing layers it cannot build (five back layers, a zero
+    thickness, a material outside the table) and the context stays usable."""
+    from opengate_gb300 import _capi as C
+    from opengate_gb300.engine import SpectEngine
+
+    scene, sp, _ = _case(n_runs=1)
+    with SpectEngine(scene, sp) as eng:
+        good = sp.desc()
+        for mutate in (lambda d: setattr(d, "n_back", 5), lambda d: d.back_thickness.__setitem__(1, 0.0),
+                       lambda d: d.back_material.__setitem__(0, 999), lambda d: setattr(d, "n_cover", 2)):
+            d = sp.desc()
+            mutate(d)
+            with pytest.raises(C.GGError) as e:
+                eng._call("gg_spect_setup", C.ctypes.byref(d))
+            assert e.value.status == C.GG_ERR_ARG
+        eng._call("gg_spect_setup", C.ctypes.byref(good))
+        eng.run(1000, 3)
+        assert eng.counters()["histories"] == 1000
