@@ -1051,6 +1051,8 @@ def run_ours_batched(args, ws, rank, local, dist, use_cuda):
     d2h = 2 * sum(s.n_voxels for s, _, _ in sims) * 8
     # images into page-locked host buffers reused every step (gg_host_alloc)
     outs = [(eng.pinned_empty(sc.labels.shape), eng.pinned_empty(sc.labels.shape)) for sc, _, _ in sims]
+    # the label images from page-locked buffers as well
+    eng.sims = [(eng.pinned_scene(sc), k, sd) for sc, k, sd in sims]
     e2e_t = []
     for _ in range(3):
         eng.reset()
@@ -1386,9 +1388,11 @@ def run_ours(args):
     h2d = scene.labels.nbytes + scene._sig.nbytes + scene._cum.nbytes + scene._ray_amax.nbytes + \
         scene._ray_cum.nbytes + scene.majorant.nbytes
     d2h = 2 * scene.n_voxels * 8
-    # the images land in page-locked host buffers reused every step (gg_host_alloc)
+    # the label image comes from and the images land in page-locked host buffers reused every
+    # step (gg_host_alloc), as a production caller keeps them
     out_e = eng.pinned_empty(scene.labels.shape)
     out_e2 = eng.pinned_empty(scene.labels.shape)
+    eng.scene = eng.pinned_scene(scene)
     torch.cuda.synchronize()
     e2e_t = []
     for k in range(max(1, min(args.steps, 3))):
@@ -1397,6 +1401,7 @@ def run_ours(args):
         eng.run(n, args.seed, first_of(args.warmup + args.steps + k))
         eng.edep(out_e), eng.edep_squared(out_e2)
         e2e_t.append(time.perf_counter() - t1)
+    eng.scene = scene
     e2e_s = dist_max(dist, float(np.mean(e2e_t)), use_cuda)
     e2e_value = ws * n / e2e_s
 

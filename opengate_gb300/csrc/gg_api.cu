@@ -71,6 +71,7 @@ struct gg_ctx {
   int dims[3] = {0, 0, 0};
   double spacing[3] = {0, 0, 0}, corner[3] = {0, 0, 0};
   uint16_t *d_labels = nullptr;
+  size_t labels_cap = 0;  // voxels d_labels holds (kept across uploads of the same size or smaller)
   void *d_maj = nullptr;
   size_t n_vox = 0;
   bool have_volume = false;
@@ -794,6 +795,17 @@ int gg_upload_tables(gg_ctx *c, const gg_tables_desc *t) {
   return GG_OK;
 }
 
+// Device label image of n voxels: the allocation is kept when it is large
+// enough (a re-upload of the same scene allocates nothing).
+static int labels_alloc(gg_ctx *c, size_t n) {
+  if (c->d_labels && c->labels_cap >= n) return GG_OK;
+  dfree(c->d_labels);
+  c->labels_cap = 0;
+  int st = c->cuda(cudaMalloc(&c->d_labels, n * sizeof(uint16_t)), "cudaMalloc labels");
+  if (!st) c->labels_cap = n;
+  return st;
+}
+
 int gg_upload_volume(gg_ctx *c, const gg_volume_desc *v) {
   if (c) {
     c->have_batch = false;  // a single image replaces the batched simulations
@@ -816,8 +828,7 @@ int gg_upload_volume(gg_ctx *c, const gg_volume_desc *v) {
     return c->fail(GG_ERR_ARG, "gg_upload_volume: label %u outside the material table (%d)", lmax, c->n_mat);
   if (gg::check_majorant(v->majorant, c->n_e, msg, sizeof(msg))) return c->fail(GG_ERR_ARG, "gg_upload_volume: %s", msg);
   int st;
-  dfree(c->d_labels);
-  if ((st = c->cuda(cudaMalloc(&c->d_labels, n * sizeof(uint16_t)), "cudaMalloc labels"))) return st;
+  if ((st = labels_alloc(c, n))) return st;
   if ((st = c->cuda(cudaMemcpyAsync(c->d_labels, v->labels, n * sizeof(uint16_t), cudaMemcpyHostToDevice, c->stream),
                     "cudaMemcpy labels")))
     return st;
@@ -1976,8 +1987,9 @@ int gg_batch_setup(gg_ctx *c, const gg_sim_desc *sims, int32_t n) {
         return c->fail(GG_ERR_ARG, "sim %d: the image is not inside the world", k);
     }
     if (!v.labels || !v.majorant) return c->fail(GG_ERR_ARG, "sim %d: labels and majorant needed", k);
-    for (uint64_t i = 0; i < m; ++i)
-      if (v.labels[i] >= c->n_mat) return c->fail(GG_ERR_ARG, "sim %d: label outside the material table", k);
+    uint16_t lmax = 0;  // (a branch-free reduction: the compiler vectorises it)
+    for (uint64_t i = 0; i < m; ++i) lmax = std::max(lmax, v.labels[i]);
+    if ((int)lmax >= c->n_mat) return c->fail(GG_ERR_ARG, "sim %d: label outside the material table", k);
     if (gg::check_majorant(v.majorant, c->n_e, msg, sizeof(msg))) return c->fail(GG_ERR_ARG, "sim %d: %s", k, msg);
     if (src.pos_type < GG_POS_POINT || src.pos_type > GG_POS_DISC || src.dir_type < GG_DIR_ISO ||
         src.dir_type > GG_DIR_FOCUSED || (src.ene_type != GG_ENE_MONO && src.ene_type != GG_ENE_RANGE) ||
@@ -1993,21 +2005,23 @@ int gg_batch_setup(gg_ctx *c, const gg_sim_desc *sims, int32_t n) {
     hist += sims[k].n_primaries;
   }
   drop_graph(c);
-  // concatenated labels and majorants (each simulation keeps its own); the
-  // element-wise maximum serves as the context's majorant
-  std::vector<uint16_t> labels(total);
+  // labels concatenated on the device (one copy per simulation, straight
+  // from the caller's buffers), majorants per simulation; the element-wise
+  // maximum serves as the context's majorant
   std::vector<float> maj(c->n_e, 0.0f), all_maj((size_t)n * c->n_e);
-  for (int k = 0; k < n; ++k) {
-    memcpy(labels.data() + off[k], sims[k].volume.labels, nv[k] * sizeof(uint16_t));
+  for (int k = 0; k < n; ++k)
     for (int i = 0; i < c->n_e; ++i) {
       maj[i] = std::max(maj[i], sims[k].volume.majorant[i]);
       all_maj[(size_t)k * c->n_e + i] = sims[k].volume.majorant[i];
     }
-  }
   int st;
-  dfree(c->d_labels);
-  if ((st = c->cuda(cudaMalloc(&c->d_labels, total * sizeof(uint16_t)), "cudaMalloc labels"))) return st;
-  if ((st = c->h2d(c->d_labels, labels.data(), total * sizeof(uint16_t), "upload labels"))) return st;
+  if ((st = labels_alloc(c, total))) return st;
+  for (int k = 0; k < n; ++k)
+    if ((st = c->cuda(cudaMemcpyAsync(c->d_labels + off[k], sims[k].volume.labels, nv[k] * sizeof(uint16_t),
+                                      cudaMemcpyHostToDevice, c->stream),
+                      "upload labels")))
+      return st;
+  if ((st = c->cuda(cudaStreamSynchronize(c->stream), "upload labels"))) return st;
   if ((st = c->upload_real(c->d_maj, maj.data(), (size_t)c->n_e))) return st;
   if ((st = c->upload_real(c->d_sim_maj, all_maj.data(), all_maj.size()))) return st;
   if (total != c->n_vox) {

@@ -117,6 +117,18 @@ class DoseEngine:
         self._call("gg_get_image_device", int(which), ctypes.byref(ptr), ctypes.byref(n))
         return ptr.value, n.value
 
+    def pinned_scene(self, scene):
+        """A copy of `scene` whose label image lives in page-locked host memory owned by this
+        engine (freed with it): uploads of it run at the host link's DMA rate."""
+        import copy
+
+        labels = self.pinned_empty(scene.labels.shape, np.uint16)
+        labels[...] = scene.labels
+        s = copy.copy(scene)
+        s.labels = labels
+        s._build_descs()
+        return s
+
     def pinned_empty(self, shape, dtype=np.float64):
         """Uninitialised array in page-locked host memory (gg_host_alloc), freed with the
         engine."""
@@ -409,6 +421,7 @@ class BatchEngine:
         return out.reshape(scene.labels.shape)
 
     pinned_empty = DoseEngine.pinned_empty
+    pinned_scene = DoseEngine.pinned_scene
 
     def counters(self):
         out = np.zeros(C.GG_N_COUNTERS, dtype=np.uint64)
