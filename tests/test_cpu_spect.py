@@ -181,3 +181,63 @@ def test_projection_metrics_match_reference():
     z = S.compute_zscore(g["counts"], g["test"], (u_ref * g["counts"]) ** 2, (g["u_test"] * g["test"]) ** 2)
     np.testing.assert_array_equal(z, g["zscore"])
     np.testing.assert_array_equal(S.compute_speedup(u_ref, g["u_test"], 12.5, 0.8), g["speedup"])
+
+
+def test_nm670_housing_layers_and_validation():
+    """The NM670 shielding box as slabs (ge_discovery_nm670.py:215-262): aluminium cover,
+    TiO2 reflector, 80 mm Pyrex back compartment, the rest of the 101.375 mm lead cover and
+    the 10 mm steel back; GateMaterials.db compositions; bad layers refused."""
+    cover, back = S.housing_layers("nm670", S.CRYSTALS["3/8"])
+    assert cover == (1.3, "Aluminium")
+    assert [m for _, m in back] == ["TiO2", "Pyrex66", "Lead", "Steel"]
+    assert sum(t for t, _ in back[:3]) + 1.3 + 9.525 == pytest.approx(101.375)
+    assert back[3][0] == pytest.approx(10.0)
+    _, back58 = S.housing_layers("nm670", S.CRYSTALS["5/8"])
+    assert back58[2][0] == pytest.approx(101.375 - 1.3 - 15.875 - 1.2 - 80.0)
+    assert S.housing_layers("none", 9.525) == (None, [])
+    with pytest.raises(NotImplementedError):
+        S.housing_layers("intevo", 9.525)
+    db = M.MaterialDatabase()
+    for name in S.HOUSING_MATERIALS["nm670"]:
+        m = db.get(name)
+        assert m.density > 1.0 and abs(m.fractions.sum() - 1.0) < 1e-12
+    assert db.get("Steel").z == [6, 25, 26] and db.get("Lead").density == pytest.approx(11.4)
+    sp = S.SpectSpec()
+    sp.apply_housing("nm670", {n: 10 + k for k, n in enumerate(S.HOUSING_MATERIALS["nm670"])}.get)
+    d = sp.desc()
+    assert (d.n_cover, d.cover_material, d.n_back, d.shielded_sides) == (1, 10, 4, 1)
+    assert list(d.back_material) == [11, 12, 13, 14]
+    assert sp.housing_depth() == pytest.approx(35.0 + 1.3 + 9.525 + 1.2 + 80.0 + 9.35 + 10.0)
+    with pytest.raises(ValueError):
+        sp.set_housing(None, [(1.0, 1)] * 5)
+    with pytest.raises(ValueError):
+        sp.set_housing((0.0, 1), ())
+    sp.apply_housing("none", None)
+    d = sp.desc()
+    assert (d.n_cover, d.n_back, d.shielded_sides, sp.housing) == (0, 0, 0, "none")
+
+
+def test_shielded_sides_stop_side_entries_in_the_oracle():
+    """A beam aimed at the side face of a head: with open sides photons reach the crystal
+    through it and are counted; with shielded sides none is."""
+    db = M.MaterialDatabase()
+    pt = T.PhysicsTables([db.get("G4_AIR"), db.get("G4_Pb"), db.get("G4_SODIUM_IODIDE")])
+    sp = S.SpectSpec(n_heads=1, n_runs=1, collimator_material=1, crystal_material=2,
+                     windows=((0.126, 0.154),))
+    fr = sp.frames(0)[0]
+    u, e1 = fr[3:6], fr[6:9]
+    # a point beside the head at the crystal's depth, aimed along e1 at the side face
+    depth = sp.collimator_thickness + sp.gap + 0.5 * sp.crystal_thickness
+    p = fr[:3] + depth * u - (sp.half_width + 20.0) * e1
+    src = SourceSpec()
+    src.translation = list(p)
+    src.dir_type = C.GG_DIR_MOMENTUM
+    src.momentum = list(e1)
+    src.ene_type = C.GG_ENE_MONO
+    src.mono = 0.1405
+    scene = Scene(pt, np.zeros((2, 2, 2), np.uint16), [5.0] * 3, [-5.0] * 3, [1500.0] * 3, 0, src)
+    open_proj, _ = O.run_spect(scene, sp, 20000, seed=3, threads=4)
+    sp.set_housing(None, (), shielded_sides=True)
+    shut_proj, cnt = O.run_spect(scene, sp, 20000, seed=3, threads=4)
+    assert open_proj.sum() > 1000 and shut_proj.sum() == 0
+    assert cnt["head_steps"] == 0 and cnt["escaped"] == 20000
