@@ -78,6 +78,7 @@ ARF_TRAIN_SAMPLES = 200_000_000
 ARF_PRIMARY_DEG = 10.0  # primary pass: angle tolerance of the source's angular acceptance
 ARF_SPLIT = (10, 2, 10000, 10.0)  # scatter pass: Compton, Rayleigh factors, max Compton level, angle tolerance
 ARF_SCATTER_SHARE = 8  # the scatter pass runs 1 / 8 of the primaries
+ARF_FORCED = 0.0  # primary pass with ForceDirection on this fraction of the decays per head (0: rejection)
 ARF_CHUNKS = 16  # ... in independent chunks (its variance)
 ARF_SUMMARY_PRIMARIES = 600_000_000  # reduced comparison carried by the default (dose) line
 ARF_WORKLOAD = ("spect_lu177_melp_nm670housing_2heads_120angles_r250mm_128x128x4.42mm_windows187-229_166-187_101-125keV_"
@@ -671,7 +672,7 @@ class ArfRecipe:
     transport before either runs."""
 
     def __init__(self, local, seed, batch, train_samples, epochs, n_runs=120, primary_deg=ARF_PRIMARY_DEG,
-                 split=ARF_SPLIT, share=ARF_SCATTER_SHARE):
+                 split=ARF_SPLIT, share=ARF_SCATTER_SHARE, forced=0.0):
         from opengate_gb300 import spect as S
         from opengate_gb300 import workloads as W
         from opengate_gb300.engine import ArfNetwork, SpectEngine
@@ -689,12 +690,25 @@ class ArfRecipe:
         self.train_s = time.perf_counter() - t0
         self.params = net.params()
         self.sp_p = copy.deepcopy(self.sp)
-        self.primary_deg, self.split, self.share = primary_deg, tuple(split), share
+        self.primary_deg, self.split, self.share, self.forced = primary_deg, tuple(split), share, float(forced)
         self.sp_p.set_free_flight(angle_tolerance_max=math.radians(primary_deg))
+        scene_p = self.scene
+        if self.forced > 0:
+            # ForceDirection toward the heads (the reference's setup_force_direction): each
+            # primary-pass history aims at one head within the cone, weight (1 - cos) / 2; the
+            # pass simulates `forced` of the decays per head
+            from opengate_gb300 import _capi as C
+
+            scene_p = copy.copy(self.scene)
+            src = copy.copy(self.scene.source)
+            src.dir_type = C.GG_DIR_FORCED
+            src.fd_angle_min, src.fd_angle_max = 0.0, math.radians(primary_deg)
+            scene_p.set_source(src)
         nc, nr, lvl, deg = self.split
         self.sp_s = copy.deepcopy(self.sp)
         self.sp_s.set_scatter_splitting(nc, nr, lvl, angle_tolerance_max=math.radians(deg))
-        self.prim = SpectEngine(self.scene, self.sp_p, device=local, precision=32, batch=batch)
+        self.scene_p = scene_p
+        self.prim = SpectEngine(scene_p, self.sp_p, device=local, precision=32, batch=batch)
         self.scat = SpectEngine(self.scene, self.sp_s, device=local, precision=32, batch=batch)
         for e in (self.prim, self.scat):
             ArfNetwork(e).set_model(self.model, self.params)
@@ -710,8 +724,11 @@ class ArfRecipe:
         kernel launches, device ms per pass, and with keep the tallies for its statistics."""
         runs = self.sp.n_runs
         m = self.scatter_per_run(n_per_run)
+        heads = self.sp.n_heads
+        # primary-pass histories per run, and the decays they stand for per head
+        np_run = max(heads, int(round(n_per_run * self.forced)) * heads) if self.forced > 0 else n_per_run
         self.prim.reset()
-        self.prim.run(n_per_run, seed, first)
+        self.prim.run(np_run, seed, first)
         tg, tt, tf, nl = self.prim.last_kernel_ms()
         parts = {"primary_pass": tg + tt + tf}
         ph, hd, arf = self.prim.last_stage_ms()
@@ -720,7 +737,8 @@ class ArfRecipe:
         st = None
         if keep:
             wp, wp2 = self.prim.weighted_projection(squared=True)
-            st = {"wp": wp, "wp2": wp2, "n_p": n_per_run * runs, "n_s": m * ARF_CHUNKS * runs,
+            st = {"wp": wp, "wp2": wp2, "n_p": (np_run // heads if self.forced > 0 else np_run) * runs,
+                  "n_s": m * ARF_CHUNKS * runs,
                   "counters_primary": self.prim.counters()}
             prev, s2, tot = 0.0, 0.0, []
         self.scat.reset()
@@ -855,7 +873,8 @@ class ArfRecipe:
 def arf_options(args):
     split = list(ARF_SPLIT)
     split[3] = args.arf_scatter_deg
-    return {"primary_deg": args.arf_primary_deg, "split": split, "share": args.arf_scatter_share}
+    return {"primary_deg": args.arf_primary_deg, "split": split, "share": args.arf_scatter_share,
+            "forced": args.arf_forced}
 
 
 def arf_summary(args, local):
@@ -936,7 +955,7 @@ def run_ours_arf(args, ws, rank, local, dist, use_cuda):
     fp64 = None
     if rank == 0 and args.fp64_primaries > 0:
         npr = max(1, args.fp64_primaries // sp.n_runs)
-        fp64 = {"primary_pass": spect_fp64_error(scene, rec.sp_p, npr, args.seed, local, min(args.batch, 1 << 26),
+        fp64 = {"primary_pass": spect_fp64_error(rec.scene_p, rec.sp_p, npr, args.seed, local, min(args.batch, 1 << 26),
                                                  arf=(rec.model, rec.params), weighted=True),
                 "scatter_pass": spect_fp64_error(scene, rec.sp_s, max(1, npr // 10), args.seed, local,
                                                  min(args.batch, 1 << 26), arf=(rec.model, rec.params),
@@ -958,6 +977,7 @@ def run_ours_arf(args, ws, rank, local, dist, use_cuda):
             "data": "synthetic (seeded CT phantom + activity image)",
             "config": {"workload": ARF_WORKLOAD, "primaries_per_step": n, "decays_per_step": n / ARF_YIELD,
                        "primary_pass_angle_tolerance_deg": rec.primary_deg,
+                       "primary_pass_forced_direction_share": rec.forced or None,
                        "scatter_pass": {"share_of_primaries": 1.0 / rec.share, "chunks": ARF_CHUNKS,
                                         "compton": rec.split[0], "rayleigh": rec.split[1],
                                         "max_compton_level": rec.split[2], "angle_tolerance_deg": rec.split[3]},
@@ -1505,6 +1525,9 @@ def main():
                     help="spect_arf: angle tolerance of the primary free-flight pass (degrees)")
     ap.add_argument("--arf-scatter-deg", type=float, default=ARF_SPLIT[3],
                     help="spect_arf: angle tolerance of the scatter-splitting copies (degrees)")
+    ap.add_argument("--arf-forced", type=float, default=ARF_FORCED,
+                    help="spect_arf: primary pass with ForceDirection toward the heads on this fraction of "
+                         "the decays per head (0: angle check by rejection on all decays)")
     ap.add_argument("--arf-scatter-share", type=int, default=ARF_SCATTER_SHARE,
                     help="spect_arf: the scatter pass runs 1 / share of the primaries")
     ap.add_argument("--batch", type=int, default=1 << 27)

@@ -74,6 +74,14 @@ extern "C" {
 #define GG_DIR_ISO 0
 #define GG_DIR_MOMENTUM 1
 #define GG_DIR_FOCUSED 2
+/* ForceDirection policy of the angular acceptance toward the SPECT heads
+   (GateForcedDirectionManager.cpp, contrib/spect/spect_config.py:986-1006
+   setup_force_direction: one source copy per head): the photon of history h
+   is aimed at head h mod n_heads, cos(theta) uniform in [fd_cos_max,
+   fd_cos_min] about the head's axis at the history's run, phi uniform, and
+   starts with weight (fd_cos_min - fd_cos_max) / 2.  With primary free
+   flight only (the weight needs the weighted tallies). */
+#define GG_DIR_FORCED 3
 
 /* energy types (GenericSource energy.type) */
 #define GG_ENE_MONO 0
@@ -174,6 +182,8 @@ typedef struct {
   const float *cdf_z;       /* [nz] */
   const float *cdf_y;       /* [nz][ny] */
   const float *cdf_x;       /* [nz][ny][nx] */
+  /* GG_DIR_FORCED: cosines of angle_tolerance_min and angle_tolerance_max */
+  double fd_cos_min, fd_cos_max;
 } gg_source_desc;
 
 /* SPECT heads: parallel-hole collimator + crystal, and the projection digitizer

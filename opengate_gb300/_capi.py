@@ -27,7 +27,7 @@ GG_PREC_F32 = 32
 GG_PREC_F64 = 64
 GG_KERNEL_WAVEFRONT, GG_KERNEL_PHASED = 0, 1
 GG_POS_POINT, GG_POS_BOX, GG_POS_SPHERE, GG_POS_DISC, GG_POS_VOXELS = 0, 1, 2, 3, 4
-GG_DIR_ISO, GG_DIR_MOMENTUM, GG_DIR_FOCUSED = 0, 1, 2
+GG_DIR_ISO, GG_DIR_MOMENTUM, GG_DIR_FOCUSED, GG_DIR_FORCED = 0, 1, 2, 3
 GG_ENE_MONO, GG_ENE_LINES, GG_ENE_HISTOGRAM, GG_ENE_RANGE = 0, 1, 2, 3
 GG_IMG_EDEP, GG_IMG_EDEP_SQUARED, GG_IMG_DOSE, GG_IMG_DOSE_SQUARED = 0, 1, 2, 3
 GG_N_COUNTERS = 16
@@ -111,6 +111,7 @@ class SourceDesc(ctypes.Structure):
         ("e_lo", ctypes.c_double), ("e_hi", ctypes.c_double),
         ("vox_dims", ctypes.c_int32 * 3), ("vox_spacing", ctypes.c_double * 3),
         ("vox_corner", ctypes.c_double * 3), ("cdf_z", _f32p), ("cdf_y", _f32p), ("cdf_x", _f32p),
+        ("fd_cos_min", ctypes.c_double), ("fd_cos_max", ctypes.c_double),
     ]
 
 

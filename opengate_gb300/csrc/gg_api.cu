@@ -343,6 +343,9 @@ struct gg_ctx {
     s.s_cos_tmax = (real)cos(src.theta[1]);
     s.s_phi0_turn = (real)(src.phi[0] / (2.0 * M_PI));
     s.s_dphi_turn = (real)((src.phi[1] - src.phi[0]) / (2.0 * M_PI));
+    s.s_fd_cmin = (real)src.fd_cos_min;
+    s.s_fd_cmax = (real)src.fd_cos_max;
+    s.s_fd_w = src.dir_type == GG_DIR_FORCED ? (real)((src.fd_cos_min - src.fd_cos_max) / 2.0) : (real)1;
     double mn = sqrt(src.momentum[0] * src.momentum[0] + src.momentum[1] * src.momentum[1] +
                      src.momentum[2] * src.momentum[2]);
     for (int a = 0; a < 3; ++a) s.s_mom[a] = (real)(mn > 0 ? src.momentum[a] / mn : 0.0);
@@ -865,7 +868,10 @@ int gg_set_source(gg_ctx *c, const gg_source_desc *s) {
   cudaSetDevice(c->device);
   if (!c->have_tables) return c->fail(GG_ERR_STATE, "gg_set_source: upload the tables first");
   if (s->pos_type < GG_POS_POINT || s->pos_type > GG_POS_VOXELS) return c->fail(GG_ERR_ARG, "gg_set_source: position type");
-  if (s->dir_type < GG_DIR_ISO || s->dir_type > GG_DIR_FOCUSED) return c->fail(GG_ERR_ARG, "gg_set_source: direction type");
+  if (s->dir_type < GG_DIR_ISO || s->dir_type > GG_DIR_FORCED) return c->fail(GG_ERR_ARG, "gg_set_source: direction type");
+  if (s->dir_type == GG_DIR_FORCED &&
+      !(s->fd_cos_min <= 1.0 && s->fd_cos_max >= -1.0 && s->fd_cos_max < s->fd_cos_min))
+    return c->fail(GG_ERR_ARG, "gg_set_source: forced direction needs -1 <= cos(max angle) < cos(min angle) <= 1");
   if (s->ene_type < GG_ENE_MONO || s->ene_type > GG_ENE_RANGE) return c->fail(GG_ERR_ARG, "gg_set_source: energy type");
   if (s->n_accept < 0 || (s->n_accept > 0 && !s->accept_boxes)) return c->fail(GG_ERR_ARG, "gg_set_source: acceptance boxes");
   double elo = 0, ehi = 0;
@@ -1254,6 +1260,9 @@ static int run_impl(gg_ctx *c, uint64_t n, uint64_t seed, uint64_t first, bool c
   // the compacted wavefront kernel: single dose simulations with analog scoring
   if (c->dgrid_on && c->tle && !c->have_spect && !c->have_batch)
     return c->fail(GG_ERR_STATE, "gg_run: the track-length estimator scores on the image grid (no dose grid)");
+  if (!c->have_batch && c->src.dir_type == GG_DIR_FORCED &&
+      !(c->have_spect && c->ff_on && c->ff_mode == GG_FF_PRIMARY))
+    return c->fail(GG_ERR_STATE, "gg_run: a forced-direction source needs SPECT heads and primary free flight");
   const bool wave = !c->have_spect && !c->tle && !c->have_batch && !c->dgrid_on &&
                     c->transport_kernel == GG_KERNEL_WAVEFRONT;
   size_t wsmem = 0;

@@ -461,6 +461,7 @@ struct Scene {
   real s_cos_tmin, s_cos_tmax, s_phi0_turn, s_dphi_turn;
   real s_mom[3], s_focus[3];
   real s_mono, s_elo, s_ehi;
+  real s_fd_cmin, s_fd_cmax, s_fd_w;  // forced direction: cone cosines, initial weight (1 otherwise)
   const real *spec_e, *spec_cdf, *acc_box;
   // voxel source
   int vnx, vny, vnz;

@@ -316,9 +316,67 @@ __device__ __forceinline__ void iso_direction(const Scene<real> &s, real u, real
   d[2] = -cost;
 }
 
+// Forced direction (GateForcedDirectionManager::SampleDirectionWithinCone):
+// about the axis a of the history's head, u1 from the larger of |a_x|, |a_y|
+// and u2 = a x u1 (both normalised); phi uniform (first draw), cos(theta)
+// uniform in [cos max, cos min] (second draw).
 template <typename real, typename G>
-__device__ __forceinline__ void sample_direction(const Scene<real> &s, const real p[3], G &g, real d[3]) {
-  if (s.dir_type == GG_DIR_ISO) {
+__device__ __forceinline__ void forced_direction(const Scene<real> &s, int run, int head, G &g, real d[3]) {
+  const HeadFrame<real> f = head_frame(s, run, head);
+  const real *a = f.u;
+  real u1[3], u2[3];
+  const real ax = a[0] < R<real>(0) ? -a[0] : a[0];
+  const real ay = a[1] < R<real>(0) ? -a[1] : a[1];
+  if (ax > ay) {
+    u1[0] = a[2];
+    u1[1] = R<real>(0);
+    u1[2] = -a[0];
+  } else {
+    u1[0] = R<real>(0);
+    u1[1] = -a[2];
+    u1[2] = a[1];
+  }
+  real n = u1[0] * u1[0];
+  n = n + u1[1] * u1[1];
+  n = n + u1[2] * u1[2];
+  n = R<real>(1) / gg_sqrt(n);
+#pragma unroll
+  for (int k = 0; k < 3; ++k) u1[k] = u1[k] * n;
+  u2[0] = a[1] * u1[2] - a[2] * u1[1];
+  u2[1] = a[2] * u1[0] - a[0] * u1[2];
+  u2[2] = a[0] * u1[1] - a[1] * u1[0];
+  n = u2[0] * u2[0];
+  n = n + u2[1] * u2[1];
+  n = n + u2[2] * u2[2];
+  n = R<real>(1) / gg_sqrt(n);
+#pragma unroll
+  for (int k = 0; k < 3; ++k) u2[k] = u2[k] * n;
+  const real v = u01<real>(g);
+  real sp, cp;
+  gg_sincos_turn(v, sp, cp);
+  real c = s.s_fd_cmin - s.s_fd_cmax;
+  c = u01<real>(g) * c;
+  c = s.s_fd_cmax + c;
+  real st = c * c;
+  st = R<real>(1) - st;
+  st = gg_sqrt(st > R<real>(0) ? st : R<real>(0));
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    real t = cp * u1[k];
+    const real t2 = sp * u2[k];
+    t = t + t2;
+    t = st * t;
+    d[k] = a[k] * c;
+    d[k] = d[k] + t;
+  }
+}
+
+template <typename real, typename G>
+__device__ __forceinline__ void sample_direction(const Scene<real> &s, const real p[3], G &g, real d[3], int run = 0,
+                                                 int head = 0) {
+  if (s.dir_type == GG_DIR_FORCED) {
+    forced_direction(s, run, head, g, d);
+  } else if (s.dir_type == GG_DIR_ISO) {
     const real u = u01<real>(g);
     const real v = u01<real>(g);
     iso_direction(s, u, v, d);
@@ -435,7 +493,7 @@ __device__ __forceinline__ int sample_direction_accepted(const Scene<real> &s, G
                                                          BlockCounters *bc) {
   int tries = 0;
   for (;;) {
-    sample_direction(s, ph.pos, g, ph.dir);
+    sample_direction(s, ph.pos, g, ph.dir, ph.run, ph.head);
     if (s.n_accept == 0 || accept_dir(s, ph.pos, ph.dir)) break;
     atomicAdd(&bc->skipped, 1u);
     if (++tries > s.max_rejection) return GG_ERR_DOMAIN;

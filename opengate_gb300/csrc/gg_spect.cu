@@ -396,7 +396,7 @@ __global__ void __launch_bounds__(256, MINB) k_spect_phantom(Scene<real> sg, Ker
             ph.can_enter = 1;
             ph.in_head = 0;
             ph.exclude = -1;
-            ph.w = R<real>(1);
+            ph.w = s.s_fd_w;  // 1, or the forced direction's cone weight
             hid = args.h_begin + h;
             ph.run = run_of(s, hid);
             has_ev = false;

@@ -144,6 +144,11 @@ __global__ void __launch_bounds__(256) k_generate(Scene<real> s, KernelArgs a) {
       g.start(a.seed, a.h_begin + i, 0u);
     }
     Photon<real> ph;
+    if (s.dir_type == GG_DIR_FORCED) {  // the head (and run) the history's photon is aimed at
+      const uint64_t h = a.h_begin + i;
+      ph.run = s.run_base + (int)((h - s.run_first) / s.run_len);
+      ph.head = (int)(h % (uint64_t)s.n_heads);
+    }
     uint32_t state = kRecDead, steps = 0;
     int st = sample_primary(s, g, ph, &bc);
     if (st != GG_OK) {
@@ -316,7 +321,7 @@ __global__ void __launch_bounds__(256, MINB) k_transport(Scene<real> sg, KernelA
             ph.can_enter = 1;
             ph.in_head = 0;
             ph.exclude = -1;
-            ph.w = R<real>(1);
+            ph.w = s.s_fd_w;  // 1, or the forced direction's cone weight
             if constexpr (SPECT) {
               ev.clear();
               ph.run = s.run_base + (int)((hid - s.run_first) / s.run_len);

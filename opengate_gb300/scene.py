@@ -30,6 +30,9 @@ class SourceSpec:
         self.focus = [0.0, 0.0, 0.0]
         self.accept_boxes = []  # list of (min xyz, max xyz)
         self.ff_angle_tolerance = 0.0  # angle check applied by a free flight (rad, 0 = none)
+        # GG_DIR_FORCED (ForceDirection toward the SPECT heads): cone angles (rad)
+        self.fd_angle_min = 0.0
+        self.fd_angle_max = 0.0
         self.max_rejection = 10000
         self.ene_type = C.GG_ENE_MONO
         self.mono = 1.0
@@ -169,6 +172,8 @@ class Scene:
         self._cdfs = [np.ascontiguousarray(c if c is not None else np.ones(1), dtype=np.float32)
                       for c in (s.cdf_z, s.cdf_y, s.cdf_x)]
         d.cdf_z, d.cdf_y, d.cdf_x = (C.ptr(c, C.ctypes.c_float) for c in self._cdfs)
+        d.fd_cos_min = math.cos(float(s.fd_angle_min))
+        d.fd_cos_max = math.cos(float(s.fd_angle_max))
         self.source_desc = d
 
     def set_source(self, source):

@@ -405,6 +405,7 @@ typedef struct {
   gg_source_desc src;
   real s_t[3], s_rot[9], s_half[3], s_radius;
   real s_cos_tmin, s_cos_tmax, s_phi0_turn, s_dphi_turn;
+  real s_fd_cmin, s_fd_cmax, s_fd_w; /* forced direction: cone cosines, initial weight (1 otherwise) */
   real s_mom[3], s_focus[3];
   real s_mono, s_elo, s_ehi;
   real *s_spec_e, *s_spec_cdf;
@@ -821,8 +822,61 @@ static int accept_dir(const scene_t *s, const real p[3], const real d[3]) {
   return 0;
 }
 
-static void sample_direction(const scene_t *s, const real p[3], rng_t *g, real d[3]) {
-  if (s->src.dir_type == GG_DIR_ISO) {
+/* ForceDirection of the angular acceptance (GateForcedDirectionManager.cpp
+   SampleDirectionWithinCone): history h aims at head h mod n_heads, about its
+   axis a: u1 from the larger of |a_x|, |a_y|, u2 = a x u1 (normalised); phi
+   uniform (first draw), cos(theta) uniform in [cos max, cos min]. */
+static void forced_direction(const scene_t *s, uint64_t hid, rng_t *g, real d[3]) {
+  const int head = (int)(hid % (uint64_t)s->n_heads);
+  const real *a = s->hu[head];
+  real u1[3], u2[3];
+  const real ax = a[0] < R(0) ? -a[0] : a[0];
+  const real ay = a[1] < R(0) ? -a[1] : a[1];
+  if (ax > ay) {
+    u1[0] = a[2];
+    u1[1] = R(0);
+    u1[2] = -a[0];
+  } else {
+    u1[0] = R(0);
+    u1[1] = -a[2];
+    u1[2] = a[1];
+  }
+  real n = u1[0] * u1[0];
+  n = n + u1[1] * u1[1];
+  n = n + u1[2] * u1[2];
+  n = R(1) / ggo_sqrt(n);
+  for (int k = 0; k < 3; ++k) u1[k] = u1[k] * n;
+  u2[0] = a[1] * u1[2] - a[2] * u1[1];
+  u2[1] = a[2] * u1[0] - a[0] * u1[2];
+  u2[2] = a[0] * u1[1] - a[1] * u1[0];
+  n = u2[0] * u2[0];
+  n = n + u2[1] * u2[1];
+  n = n + u2[2] * u2[2];
+  n = R(1) / ggo_sqrt(n);
+  for (int k = 0; k < 3; ++k) u2[k] = u2[k] * n;
+  const real v = u01(g);
+  real sp, cp;
+  ggo_sincos_turn(v, &sp, &cp);
+  real c = s->s_fd_cmin - s->s_fd_cmax;
+  c = u01(g) * c;
+  c = s->s_fd_cmax + c;
+  real st = c * c;
+  st = R(1) - st;
+  st = ggo_sqrt(st > R(0) ? st : R(0));
+  for (int k = 0; k < 3; ++k) {
+    real t = cp * u1[k];
+    const real t2 = sp * u2[k];
+    t = t + t2;
+    t = st * t;
+    d[k] = a[k] * c;
+    d[k] = d[k] + t;
+  }
+}
+
+static void sample_direction(const scene_t *s, const real p[3], rng_t *g, real d[3], uint64_t hid) {
+  if (s->src.dir_type == GG_DIR_FORCED) {
+    forced_direction(s, hid, g, d);
+  } else if (s->src.dir_type == GG_DIR_ISO) {
     real u = u01(g);
     real cost = s->s_cos_tmin - s->s_cos_tmax;
     cost = u * cost;
@@ -853,7 +907,7 @@ static void sample_direction(const scene_t *s, const real p[3], rng_t *g, real d
   }
 }
 
-static int sample_primary(const scene_t *s, rng_t *g, photon_t *ph, tally_t *t) {
+static int sample_primary(const scene_t *s, rng_t *g, photon_t *ph, tally_t *t, uint64_t hid) {
   real loc[3] = {R(0), R(0), R(0)};
   int pt = s->src.pos_type;
   if (pt == GG_POS_BOX) {
@@ -925,7 +979,7 @@ static int sample_primary(const scene_t *s, rng_t *g, photon_t *ph, tally_t *t) 
   /* direction, with the acceptance loop of GateSingleParticleSource */
   int tries = 0;
   for (;;) {
-    sample_direction(s, ph->pos, g, ph->dir);
+    sample_direction(s, ph->pos, g, ph->dir, hid);
     if (s->src.n_accept == 0 || accept_dir(s, ph->pos, ph->dir)) break;
     t->cnt[GG_CNT_SKIPPED]++;
     if (++tries > s->src.max_rejection) return GG_ERR_DOMAIN;
@@ -955,7 +1009,7 @@ static int sample_primary(const scene_t *s, rng_t *g, photon_t *ph, tally_t *t) 
   ph->alive = 1;
   ph->can_enter = 1;
   ph->in_image = 0;
-  ph->w = R(1);
+  ph->w = s->s_fd_w; /* 1, or the forced direction's cone weight */
   set_energy(s, ph, e);
   return GG_OK;
 }
@@ -1983,7 +2037,7 @@ static int run_history(const scene_t *s, uint64_t seed, uint64_t h, tally_t *t) 
   int has_sec = 0;
   event_t ev;
   memset(&ev, 0, sizeof(ev));
-  int st = sample_primary(s, &g, &ph, t);
+  int st = sample_primary(s, &g, &ph, t, h);
   if (st != GG_OK) return st;
   t->cnt[GG_CNT_HISTORIES]++;
   t->ss_next = 0;
@@ -2064,6 +2118,9 @@ static int scene_init(scene_t *s, const gg_tables_desc *tb, const gg_volume_desc
   s->s_cos_tmax = (real)cos(src->theta[1]);
   s->s_phi0_turn = (real)(src->phi[0] / (2.0 * M_PI));
   s->s_dphi_turn = (real)((src->phi[1] - src->phi[0]) / (2.0 * M_PI));
+  s->s_fd_cmin = (real)src->fd_cos_min;
+  s->s_fd_cmax = (real)src->fd_cos_max;
+  s->s_fd_w = src->dir_type == GG_DIR_FORCED ? (real)((src->fd_cos_min - src->fd_cos_max) / 2.0) : R(1);
   double mn = sqrt(src->momentum[0] * src->momentum[0] + src->momentum[1] * src->momentum[1] +
                    src->momentum[2] * src->momentum[2]);
   for (int a = 0; a < 3; ++a) s->s_mom[a] = (real)(mn > 0 ? src->momentum[a] / mn : 0.0);
@@ -2728,7 +2785,7 @@ int GGO_PREFIX(sample_source)(const gg_tables_desc *tb, const gg_volume_desc *vo
     rng_t g;
     rng_init(&g, seed, (uint64_t)i, 0u);
     photon_t ph;
-    st = sample_primary(&s, &g, &ph, &t);
+    st = sample_primary(&s, &g, &ph, &t, (uint64_t)i);
     for (int a = 0; a < 3; ++a) {
       pos[3 * i + a] = (double)ph.pos[a];
       dir[3 * i + a] = (double)ph.dir[a];
@@ -2781,7 +2838,7 @@ int GGO_PREFIX(first_flight)(const gg_tables_desc *tb, const gg_volume_desc *vol
     rng_t g;
     rng_init(&g, seed, (uint64_t)i, 0u);
     photon_t ph;
-    if (sample_primary(&s, &g, &ph, &t) != GG_OK) { scene_free(&s); return GG_ERR_DOMAIN; }
+    if (sample_primary(&s, &g, &ph, &t, (uint64_t)i) != GG_OK) { scene_free(&s); return GG_ERR_DOMAIN; }
     start_photon(&s, &ph);
     if (!ph.in_image) {
       real tin = entry_distance(ph.pos, ph.dir, s.bmin, s.bmax);

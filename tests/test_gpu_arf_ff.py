@@ -76,3 +76,22 @@ def test_scatter_splitting_with_arf():
     ref = O.run_spect_arf_ff(scene, sp, 30_000, 23, model, params, threads=8)
     _compare(got, ref, sp.n_windows)
     assert got[3]["arf_photons"] > 100
+
+
+def test_forced_direction_with_arf():
+    """ForceDirection + primary free flight + ARF detectors: each history's photon, aimed at
+    its head within the cone, adds its cone weight x exp(-optical depth) x the window weights."""
+    import math
+
+    from opengate_gb300 import _capi as C
+
+    scene, sp, model, params = _setup()
+    sp.set_free_flight(angle_tolerance_max=math.radians(10.0))
+    src = scene.source
+    src.dir_type = C.GG_DIR_FORCED
+    src.fd_angle_min, src.fd_angle_max = 0.0, math.radians(10.0)
+    scene.set_source(src)
+    got = _run(scene, sp, model, params, 40_000, 31)
+    ref = O.run_spect_arf_ff(scene, sp, 40_000, 31, model, params, threads=8)
+    _compare(got, ref, sp.n_windows)
+    assert got[3]["arf_photons"] > 10_000

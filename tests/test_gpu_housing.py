@@ -109,3 +109,47 @@ def test_housing_and_dose_grid_arguments_are_checked():
         eng._call("gg_spect_setup", C.ctypes.byref(good))
         eng.run(1000, 3)
         assert eng.counters()["histories"] == 1000
+
+
+@pytest.mark.parametrize("precision", [32, 64])
+def test_forced_direction_free_flight_bit_exact(precision):
+    """ForceDirection toward the heads (GateForcedDirectionManager.cpp) with primary free flight:
+    history h aims at head h mod 2 within a 10 degree cone, weight (1 - cos 10 deg) / 2.
+    Weighted projections, squares and counters equal the oracle's."""
+    import math
+
+    from opengate_gb300 import _capi as C
+    from opengate_gb300.engine import SpectEngine
+
+    scene, sp, _ = _case()
+    sp.set_free_flight(angle_tolerance_max=math.radians(10.0))
+    src = scene.source
+    src.dir_type = C.GG_DIR_FORCED
+    src.fd_angle_min, src.fd_angle_max = 0.0, math.radians(10.0)
+    scene.set_source(src)
+    n = 100_000
+    with SpectEngine(scene, sp, precision=precision) as eng:
+        eng.run(n, 29)
+        w, w2 = eng.weighted_projection(squared=True)
+        cnt = eng.counters()
+    rw, rw2, rcnt = O.run_spect_ff(scene, sp, n, seed=29, threads=8, precision=precision)
+    np.testing.assert_array_equal(w, rw)
+    np.testing.assert_array_equal(w2, rw2)
+    assert cnt == rcnt and w.sum() > 0
+
+
+def test_forced_direction_needs_primary_free_flight():
+    import math
+
+    from opengate_gb300 import _capi as C
+    from opengate_gb300.engine import SpectEngine
+
+    scene, sp, _ = _case(n_runs=1)
+    src = scene.source
+    src.dir_type = C.GG_DIR_FORCED
+    src.fd_angle_min, src.fd_angle_max = 0.0, math.radians(10.0)
+    scene.set_source(src)
+    with SpectEngine(scene, sp) as eng:
+        with pytest.raises(C.GGError) as e:
+            eng.run(1000, 3)
+        assert e.value.status == C.GG_ERR_STATE
