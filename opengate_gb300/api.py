@@ -257,7 +257,18 @@ class GenericSource(GateObject):
         s.focus = [float(x) for x in d.focus_point]
         aa = d.angular_acceptance
         s.ff_angle_tolerance = 0.0
-        if aa.policy and free_flight:
+        if aa.policy == "ForceDirection" and free_flight:
+            # GateForcedDirectionManager: the direction is drawn in the cone about the target
+            # head's axis with the cone's weight; here one source aims history h at head
+            # h mod n_heads (the reference's one source copy per head, spect_config.py:986-1006)
+            if s.dir_type != C.GG_DIR_ISO:
+                raise ValueError("'ForceDirection' replaces an 'iso' direction")
+            if not (0.0 <= float(aa.angle_tolerance_min) < float(aa.angle_tolerance_max)):
+                raise ValueError("'ForceDirection' needs 0 <= angle_tolerance_min < angle_tolerance_max")
+            s.dir_type = C.GG_DIR_FORCED
+            s.fd_angle_min = float(aa.angle_tolerance_min) / u.rad
+            s.fd_angle_max = float(aa.angle_tolerance_max) / u.rad
+        elif aa.policy and free_flight:
             if aa.policy != "Rejection" or aa.skip_policy != "SkipEvents":
                 raise NotImplementedError("angular acceptance with free flight: policy 'Rejection', 'SkipEvents'")
             if aa.enable_angle_check:
@@ -1048,6 +1059,9 @@ class Simulation:
         self.last_seed = seed
         rng = np.random.default_rng(seed)
         plan = [events_per_run(src, runs, rng) for src, _ in sources]
+        # a forced-direction source stands for one source copy per head: n_heads histories per event
+        plan = [[k * sp.n_heads for k in p] if spec.dir_type == C.GG_DIR_FORCED else p
+                for p, (_, spec) in zip(plan, sources)]
         eng = SpectEngine(scene, sp, device=self.device, precision=self.precision, batch=self.batch)
         try:
             if sp.arf is not None:

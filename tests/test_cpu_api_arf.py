@@ -220,3 +220,24 @@ def test_free_flight_with_arf_detectors_maps_to_the_engine(tmp_path):
     aa.policy, aa.enable_intersection_check, aa.enable_angle_check = "Rejection", True, True
     with pytest.raises(NotImplementedError):
         sim3.build_spect()
+
+
+def test_force_direction_policy_maps_to_forced_sources(tmp_path):
+    """angular_acceptance.policy = "ForceDirection" with a GammaFreeFlightActor (the reference's
+    setup_force_direction): the source aims each history at a head within the cone."""
+    _model_file(tmp_path / "net.npz")
+    sim, dets = _ff_arf_sim(tmp_path, tmp_path / "net.npz")
+    aa = sim.sources["s"].direction.angular_acceptance
+    aa.policy = "ForceDirection"
+    aa.angle_tolerance_max = 8 * u.deg
+    scene, sp, sources, arfs, head_of = sim.build_spect()
+    spec = sources[0][1]
+    assert spec.dir_type == C.GG_DIR_FORCED
+    assert spec.fd_angle_min == 0.0 and spec.fd_angle_max == pytest.approx(np.radians(8.0))
+    assert sp.free_flight.enabled == C.FF_PRIMARY and sp.free_flight.angle_tolerance_max == 0.0
+    d = spec_desc = scene.source_desc
+    assert d.dir_type == C.GG_DIR_FORCED and d.fd_cos_max == pytest.approx(np.cos(np.radians(8.0)))
+    assert spec_desc.fd_cos_min == pytest.approx(1.0)
+    aa.angle_tolerance_min, aa.angle_tolerance_max = 9 * u.deg, 8 * u.deg
+    with pytest.raises(ValueError):
+        sim.build_spect()

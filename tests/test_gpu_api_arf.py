@@ -84,10 +84,12 @@ def test_arf_train_save_load_acquire(tmp_path, built_lib):
     assert len(LU177) == sp.n_windows
 
 
-def test_free_flight_recipe_with_arf_detectors_through_the_api(tmp_path, built_lib):
-    """GammaFreeFlightActor + the source's angular acceptance (angle check 12 degrees) + ARF
-    detectors through Simulation.run(): the written images equal the weighted projection of the
-    same histories run directly (free flight + gg_spect_use_arf)."""
+@pytest.mark.parametrize("policy", ["Rejection", "ForceDirection"])
+def test_free_flight_recipe_with_arf_detectors_through_the_api(tmp_path, built_lib, policy):
+    """GammaFreeFlightActor + the source's angular acceptance (angle check 12 degrees, or the
+    direction forced into the 12 degree cone of each head) + ARF detectors through
+    Simulation.run(): the written images equal the weighted projection of the same histories
+    run directly (free flight + gg_spect_use_arf)."""
     import ctypes
 
     from opengate_gb300 import _capi as C
@@ -99,12 +101,14 @@ def test_free_flight_recipe_with_arf_detectors_through_the_api(tmp_path, built_l
     _model_file(tmp_path / "net.npz")
     n = 300_000
     sim, dets = _ff_arf_sim(tmp_path / "acq", tmp_path / "net.npz", deg=12.0, n=n)
+    sim.sources["s"].direction.angular_acceptance.policy = policy
     for _, a in dets:
         a.squared_counts.active = True
     sim.random_seed = 4242
     sim.run()
     scene, sp, sources, arfs, head_of = sim.build_spect()
     assert sp.free_flight.enabled == C.FF_PRIMARY
+    per_run = n * (sp.n_heads if policy == "ForceDirection" else 1)
     with SpectEngine(scene, sp) as e:
         ArfNetwork(e).set_model(sp.arf[0], sp.arf[1])
         e.use_arf(True)
@@ -112,8 +116,8 @@ def test_free_flight_recipe_with_arf_detectors_through_the_api(tmp_path, built_l
         for r in range(sp.n_runs):
             frames = np.ascontiguousarray(sp.frames(r), dtype=np.float64)
             e._call("gg_spect_set_heads", r, C.ptr(frames, ctypes.c_double))
-            e._call("gg_run", ctypes.c_uint64(n), ctypes.c_uint64(4242), ctypes.c_uint64(first))
-            first += n
+            e._call("gg_run", ctypes.c_uint64(per_run), ctypes.c_uint64(4242), ctypes.c_uint64(first))
+            first += per_run
         counts = e.projection()
         w, w2 = e.arf_projection(squared=True)
         cnt = e.counters()
