@@ -64,13 +64,14 @@ FF_WORKLOAD = SPECT_WORKLOAD + "_freeflight_primary+scattersplit_c50_r10_aa10deg
 
 # SPECT with ARF detectors: Lu-177 (113 keV 6.2 %, 208 keV 10.4 %), medium-energy
 # collimator, 120 gantry positions, 1e10 decays.  The ARF acquisition is the
-# reference's recipe: a primary pass in free flight (angle check at the source)
-# into the ARF detectors plus a scatter-splitting pass into the ARF detectors on
-# 1/8 of the primaries; the network is trained on 2e8 photons of the plain
-# collimator tracking, and the plain acquisition of as many decays is run beside
-# it for the matched-sigma comparison
-ARF_METRIC = ("primaries/s (ARF SPECT recipe: primary free-flight pass + scatter-splitting pass on 1/8 of the "
-              "primaries, both into ARF detectors; SPECT projections)")
+# reference's recipe: a primary pass in free flight with the source's
+# ForceDirection toward the heads (10 degree cones, on 1/32 of the decays per
+# head) into the ARF detectors plus a scatter-splitting pass into the ARF
+# detectors on 1/8 of the primaries; the network is trained on 2e8 photons of
+# the plain collimator tracking, and the plain acquisition of as many decays is
+# run beside it for the matched-sigma comparison
+ARF_METRIC = ("primaries/s (ARF SPECT recipe: primary free-flight pass with forced directions toward the heads + "
+              "scatter-splitting pass on 1/8 of the primaries, both into ARF detectors; SPECT projections)")
 ARF_DECAYS = 10_000_000_000
 ARF_YIELD = 0.166
 ARF_WINDOWS = ((0.1872, 0.2288), (0.166, 0.187), (0.1017, 0.1243))
@@ -78,11 +79,11 @@ ARF_TRAIN_SAMPLES = 200_000_000
 ARF_PRIMARY_DEG = 10.0  # primary pass: angle tolerance of the source's angular acceptance
 ARF_SPLIT = (10, 2, 10000, 10.0)  # scatter pass: Compton, Rayleigh factors, max Compton level, angle tolerance
 ARF_SCATTER_SHARE = 8  # the scatter pass runs 1 / 8 of the primaries
-ARF_FORCED = 0.0  # primary pass with ForceDirection on this fraction of the decays per head (0: rejection)
+ARF_FORCED = 1.0 / 32  # primary pass with ForceDirection on this fraction of the decays per head (0: rejection)
 ARF_CHUNKS = 16  # ... in independent chunks (its variance)
 ARF_SUMMARY_PRIMARIES = 600_000_000  # reduced comparison carried by the default (dose) line
 ARF_WORKLOAD = ("spect_lu177_melp_nm670housing_2heads_120angles_r250mm_128x128x4.42mm_windows187-229_166-187_101-125keV_"
-                "ct_phantom_256x256x160_1.2mm_arf_mlp3x128_bf16_freeflight_aa10deg+scattersplit_c10_r2_aa10deg_1of8")
+                "ct_phantom_256x256x160_1.2mm_arf_mlp3x128_bf16_freeflight_forced10deg_1of32+scattersplit_c10_r2_aa10deg_1of8")
 
 
 def measured_peaks():
