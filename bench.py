@@ -55,12 +55,14 @@ SPECT_WORKLOAD = ("spect_tc99m_lehr_nm670housing_2heads_60angles_r250mm_128x128x
 BATCH_METRIC = "primaries/s at matched sigma (batched GPU: 48 uneven simulations in one launch sequence)"
 BATCH_WORKLOAD = "batched_48_slab_phantoms_32-128vox_1-3mm_mono_0.05-2MeV_1e5-1e7_primaries"
 
-FF_METRIC = ("primaries/s (free-flight SPECT recipe: primary free-flight pass + scatter-splitting pass, "
-             "SPECT projections)")
+FF_METRIC = ("primaries/s (free-flight SPECT recipe: primary free-flight pass with forced directions + "
+             "scatter-splitting pass on 1/4 of the primaries, SPECT projections)")
 FF_DECAYS = 100_000_000
 FF_SPLIT = (50, 10, 10000, 10.0)  # Compton, Rayleigh factors, max Compton level, angle tolerance (deg)
 FF_CHUNKS = 8  # scatter pass in independent chunks: its variance (copies of a history are correlated)
-FF_WORKLOAD = SPECT_WORKLOAD + "_freeflight_primary+scattersplit_c50_r10_aa10deg"
+FF_FORCED = (1.0 / 8, 20.0)  # primary pass: ForceDirection on this fraction of the decays per head, cone (deg)
+FF_SCATTER_SHARE = 4  # the scatter pass runs 1 / 4 of the primaries
+FF_WORKLOAD = SPECT_WORKLOAD + "_freeflight_forced20deg_1of8+scattersplit_c50_r10_aa10deg_1of4"
 
 # SPECT with ARF detectors: Lu-177 (113 keV 6.2 %, 208 keV 10.4 %), medium-energy
 # collimator, 120 gantry positions, 1e10 decays.  The ARF acquisition is the
@@ -275,15 +277,19 @@ def reference_workload(args, threads):
                  if args.workload == "spect_arf" else ""))
         return meta + ("synthetic (seeded CT phantom + activity image)", run, note, 2000 * runs, int(4e8))
     if args.workload == "spect_ff":
-        scene, sp_p, sp_s = spect_ff_specs()
-        runs = sp_p.n_runs
+        forced = (args.ff_forced, FF_FORCED[1])
+        scene, scene_p, sp_p, sp_s = spect_ff_specs(forced)
+        runs, heads = sp_p.n_runs, sp_p.n_heads
 
-        def run(n, seed):
-            O.run_spect_ff(scene, sp_p, max(n // runs, 1), seed, threads=threads)
-            O.run_spect_ff(scene, sp_s, max(n // runs, 1), seed + 1, threads=threads)
+        def run(n, seed):  # the GPU step's composition for n primaries
+            per = max(n // runs, 1)
+            pr = max(heads, int(round(per * forced[0])) * heads) if forced[0] > 0 else per
+            O.run_spect_ff(scene_p, sp_p, pr, seed, threads=threads)
+            O.run_spect_ff(scene, sp_s, max(1, per // args.ff_scatter_share), seed + 1, threads=threads)
 
         return (FF_METRIC, FF_WORKLOAD, int(FF_DECAYS * SPECT_YIELD), "synthetic (seeded CT phantom + activity image)",
-                run, f"primary free flight + scatter splitting over all {runs} positions", 200 * runs, int(4e8))
+                run, f"primary free flight (forced directions) + scatter splitting over all {runs} positions",
+                200 * runs, int(4e8))
     if args.workload == "batched":
         _, sims = W.batched_phantoms(seed=args.seed)
         total = int(sum(k for _, k, _ in sims))
@@ -460,8 +466,12 @@ def run_ours_spect(args, ws, rank, local, dist, use_cuda):
     return 0
 
 
-def spect_ff_specs():
-    """(scene, primary free-flight spec, scatter-splitting spec) of the SPECT workload."""
+def spect_ff_specs(forced=FF_FORCED):
+    """(scene, primary-pass scene, primary free-flight spec, scatter-splitting spec) of the
+    SPECT workload; the primary-pass scene's source has ForceDirection toward the heads (the
+    reference's setup_force_direction, test085_free_flight_spect_2b_fd: 20 degree cones) when
+    `forced` is given."""
+    from opengate_gb300 import _capi as C
     from opengate_gb300 import workloads as W
 
     scene, sp_p, _ = W.spect_phantom(housing=SPECT_HOUSING)
@@ -469,7 +479,14 @@ def spect_ff_specs():
     sp_p.set_free_flight()
     nc, nr, lvl, deg = FF_SPLIT
     sp_s.set_scatter_splitting(nc, nr, lvl, angle_tolerance_max=math.radians(deg))
-    return scene, sp_p, sp_s
+    scene_p = scene
+    if forced and forced[0] > 0:
+        scene_p = copy.copy(scene)
+        src = copy.copy(scene.source)
+        src.dir_type = C.GG_DIR_FORCED
+        src.fd_angle_min, src.fd_angle_max = 0.0, math.radians(forced[1])
+        scene_p.set_source(src)
+    return scene, scene_p, sp_p, sp_s
 
 
 def run_ours_ff(args, ws, rank, local, dist, use_cuda):
@@ -481,13 +498,20 @@ def run_ours_ff(args, ws, rank, local, dist, use_cuda):
 
     from opengate_gb300.engine import SpectEngine
 
-    scene, sp_p, sp_s = spect_ff_specs()
+    forced = (args.ff_forced, FF_FORCED[1])
+    scene, scene_p, sp_p, sp_s = spect_ff_specs(forced)
     runs = sp_p.n_runs
+    heads = sp_p.n_heads
     n_step = args.primaries if args.primaries != PRIMARIES_PER_STEP else int(FF_DECAYS * SPECT_YIELD)
     n_per_run = n_step // runs // FF_CHUNKS * FF_CHUNKS
     n = n_per_run * runs
-    m = n_per_run // FF_CHUNKS
-    eng_p = SpectEngine(scene, sp_p, device=local, precision=32, batch=args.batch)
+    # scatter pass on 1 / share of the primaries, in FF_CHUNKS chunks
+    m = max(1, n_per_run // args.ff_scatter_share // FF_CHUNKS)
+    n_s = m * FF_CHUNKS * runs
+    # primary pass: all primaries, or (ForceDirection) `forced` of them per head
+    np_run = max(heads, int(round(n_per_run * forced[0])) * heads) if forced[0] > 0 else n_per_run
+    n_pe = (np_run // heads if forced[0] > 0 else np_run) * runs  # decays per head it stands for
+    eng_p = SpectEngine(scene_p, sp_p, device=local, precision=32, batch=args.batch)
     eng_s = SpectEngine(scene, sp_s, device=local, precision=32, batch=args.batch)
     l2_flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=f"cuda:{local}")
 
@@ -501,7 +525,7 @@ def run_ours_ff(args, ws, rank, local, dist, use_cuda):
         ms, nl, chunks = 0.0, 0, []
         eng_p.reset()
         eng_s.reset()
-        eng_p.run(n_per_run, args.seed, first)
+        eng_p.run(np_run, args.seed, first)
         tg, tt, tf, k = eng_p.last_kernel_ms()
         ms, nl = ms + tg + tt + tf, nl + k
         parts["primary_pass"] = tg + tt + tf
@@ -549,9 +573,11 @@ def run_ours_ff(args, ws, rank, local, dist, use_cuda):
     nw = sp_p.n_windows
     # per-projection window totals (head, position, window): a photon of the primary pass
     # scores one single; the scatter pass's variance comes from its independent chunks
+    # both passes scaled to the n primaries of the analog acquisition
+    sc_p, sc_s = n / n_pe, n / n_s
     ch = np.array(chunks).sum(axis=(3, 4))
-    t_ff = wp.sum(axis=(2, 3)) + ch.sum(axis=0)
-    v_ff = wp2.sum(axis=(2, 3)) + FF_CHUNKS * ch.var(axis=0, ddof=1)
+    t_ff = wp.sum(axis=(2, 3)) * sc_p + ch.sum(axis=0) * sc_s
+    v_ff = wp2.sum(axis=(2, 3)) * sc_p ** 2 + FF_CHUNKS * ch.var(axis=0, ddof=1) * sc_s ** 2
     # analog SPECT path, same primaries (one count per single: variance = counts)
     sp_a = copy.deepcopy(sp_p)
     sp_a.set_free_flight(enabled=False)
@@ -584,8 +610,8 @@ def run_ours_ff(args, ws, rank, local, dist, use_cuda):
         eng_p.upload()
         eng_s.upload()
         first = first_of(args.warmup + args.steps + 2 + k)
-        eng_p.run(n_per_run, args.seed, first)
-        eng_s.run(n_per_run, args.seed + 1, first)
+        eng_p.run(np_run, args.seed, first)
+        eng_s.run(m * FF_CHUNKS, args.seed + 1, first)
         eng_p.weighted_projection(squared=True)
         eng_s.weighted_projection(squared=True)
         e2e_t.append(time.perf_counter() - t1)
@@ -607,9 +633,11 @@ def run_ours_ff(args, ws, rank, local, dist, use_cuda):
 
         threads = os.cpu_count() or 1
 
-        def run(nn, seed):
-            O.run_spect_ff(scene, sp_p, max(nn // runs, 1), seed, threads=threads)
-            O.run_spect_ff(scene, sp_s, max(nn // runs, 1), seed + 1, threads=threads)
+        def run(nn, seed):  # the step's composition for nn primaries
+            per = max(nn // runs, 1)
+            pr = max(heads, int(round(per * forced[0])) * heads) if forced[0] > 0 else per
+            O.run_spect_ff(scene_p, sp_p, pr, seed, threads=threads)
+            O.run_spect_ff(scene, sp_s, max(1, per // args.ff_scatter_share), seed + 1, threads=threads)
 
         r, ns, dt = grow_sample(run, args.cpu_seconds, 200 * runs, int(4e8))
         cpu = {"value": r, "unit": UNIT, "cores": threads, "kind": "port",
@@ -618,7 +646,7 @@ def run_ours_ff(args, ws, rank, local, dist, use_cuda):
     fp64 = None
     if rank == 0 and args.fp64_primaries > 0:
         npr = max(1, min(args.fp64_primaries, 10_000_000) // runs)
-        fp64 = {"primary_pass": spect_fp64_error(scene, sp_p, npr, args.seed, local, args.batch, weighted=True),
+        fp64 = {"primary_pass": spect_fp64_error(scene_p, sp_p, npr, args.seed, local, args.batch, weighted=True),
                 "scatter_pass": spect_fp64_error(scene, sp_s, max(1, npr // 10), args.seed, local, args.batch,
                                                  weighted=True)}
     if rank == 0:
@@ -630,6 +658,10 @@ def run_ours_ff(args, ws, rank, local, dist, use_cuda):
             "config": {"workload": FF_WORKLOAD, "primaries_per_step": n, "decays_per_step": n / SPECT_YIELD,
                        "split": {"compton": FF_SPLIT[0], "rayleigh": FF_SPLIT[1], "max_compton_level": FF_SPLIT[2],
                                  "angle_tolerance_deg": FF_SPLIT[3]},
+                       "primary_pass": {"forced_direction_share_per_head": forced[0] or None,
+                                        "cone_deg": forced[1] if forced[0] > 0 else None,
+                                        "histories": int(np_run * runs)},
+                       "scatter_pass": {"share_of_primaries": 1.0 / args.ff_scatter_share, "histories": int(n_s)},
                        "l2": "flushed between steps (256 MiB write)", "batch": args.batch,
                        "parallelism": f"replicas x{ws}, disjoint history ranges"},
             "sigma": {"mean_relative_uncertainty_of_projection_totals": sig, "analog_ms": ms_a,
@@ -1526,6 +1558,11 @@ def main():
                     help="spect_arf: angle tolerance of the primary free-flight pass (degrees)")
     ap.add_argument("--arf-scatter-deg", type=float, default=ARF_SPLIT[3],
                     help="spect_arf: angle tolerance of the scatter-splitting copies (degrees)")
+    ap.add_argument("--ff-forced", type=float, default=FF_FORCED[0],
+                    help="spect_ff: primary pass with ForceDirection on this fraction of the decays per head "
+                         "(0: all decays, no angle check)")
+    ap.add_argument("--ff-scatter-share", type=int, default=FF_SCATTER_SHARE,
+                    help="spect_ff: the scatter pass runs 1 / share of the primaries")
     ap.add_argument("--arf-forced", type=float, default=ARF_FORCED,
                     help="spect_arf: primary pass with ForceDirection toward the heads on this fraction of "
                          "the decays per head (0: angle check by rejection on all decays)")
