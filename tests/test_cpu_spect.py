@@ -241,3 +241,32 @@ def test_shielded_sides_stop_side_entries_in_the_oracle():
     shut_proj, cnt = O.run_spect(scene, sp, 20000, seed=3, threads=4)
     assert open_proj.sum() > 1000 and shut_proj.sum() == 0
     assert cnt["head_steps"] == 0 and cnt["escaped"] == 20000
+
+
+def test_forced_direction_equals_angle_check_in_expectation():
+    """ForceDirection (history h aimed at head h mod 2 within the cone, weight (1 - cos)/2) and
+    the angle check by rejection on the same cone give the same expected weighted projection
+    totals per head and window (oracle, primary free flight, Lu-177 / MELP / NM670 housing)."""
+    from opengate_gb300 import workloads as W
+
+    sc, sp, _ = W.spect_phantom(shape=(40, 64, 64), spacing=4.8, n_runs=1, nuclide=W.LU177, collimator=S.MELP,
+                                windows=((0.1872, 0.2288), (0.1017, 0.1243)), housing="nm670")
+    tol = math.radians(10.0)
+    sp.set_free_flight(angle_tolerance_max=tol)
+    n = 600_000
+    w, w2, _ = O.run_spect_ff(sc, sp, n, seed=5, threads=8)
+    src = sc.source
+    src.dir_type = C.GG_DIR_FORCED
+    src.fd_angle_min, src.fd_angle_max = 0.0, tol
+    sc.set_source(src)
+    m = 60_000  # per head
+    wf, wf2, cnt = O.run_spect_ff(sc, sp, 2 * m, seed=6, threads=8)
+    assert cnt["histories"] == 2 * m and cnt["skipped"] == 0
+    for h in range(2):
+        for k in range(2):
+            a, va = w[h, k::2].sum() / n, w2[h, k::2].sum() / n ** 2
+            b, vb = wf[h, k::2].sum() / m, wf2[h, k::2].sum() / m ** 2
+            assert a > 0 and b > 0
+            assert abs(a - b) < 4.0 * math.sqrt(va + vb), (h, k, a, b)
+    # the forced estimate is far less noisy per history
+    assert wf2[0, 0::2].sum() / wf[0, 0::2].sum() ** 2 * m < w2[0, 0::2].sum() / w[0, 0::2].sum() ** 2 * n
