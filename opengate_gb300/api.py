@@ -17,8 +17,8 @@ uses, with the same names, units and semantics:
 * ``GenericSource`` (opengate/sources/generic.py:333) with ``n``,
   ``position``, ``direction`` (incl. ``angular_acceptance``), ``energy``;
 * ``DoseActor`` (opengate/actors/doseactors.py:317): edep / edep_squared /
-  edep_uncertainty / dose / dose_squared / dose_uncertainty outputs,
-  ``number_of_samples``; ``SimulationStatisticsActor`` (miscactors.py:30).
+  edep_uncertainty / dose / dose_squared / dose_uncertainty / density
+  outputs (``counts`` raises), ``number_of_samples``; ``SimulationStatisticsActor`` (miscactors.py:30).
 
 Options the GPU path does not implement raise errors at ``run()`` instead of
 being ignored; electron transport is not modelled, so the simulation must
@@ -431,7 +431,8 @@ class DoseActor(GateObject):
     def __init__(self, name, simulation=None, **kw):
         super().__init__(name, simulation, **kw)
         for suffix, active in (("edep", True), ("edep_squared", False), ("edep_uncertainty", False),
-                               ("dose", False), ("dose_squared", False), ("dose_uncertainty", False)):
+                               ("dose", False), ("dose_squared", False), ("dose_uncertainty", False),
+                               ("density", False), ("counts", False)):
             object.__setattr__(self, suffix, ActorOutput(self, suffix, active))
 
     def check(self, image_volume, image):
@@ -447,6 +448,23 @@ class DoseActor(GateObject):
             raise ValueError(f"Illegal parameter 'output_coordinate_system': {self.output_coordinate_system}")
         if len(self.size) != 3 or min(int(v) for v in self.size) < 1 or min(float(v) for v in self.spacing) <= 0:
             raise ValueError(f"DoseActor '{self.name}': size must be 3 positive integers, spacing > 0")
+        if self.counts.active:
+            raise NotImplementedError("the DoseActor 'counts' output (steps per voxel) is not scored")
+
+    def density_image(self, volume, image, material_db, spacing, origin, direction):
+        """The 'density' output (DoseActor.create_density_image_from_image_volume,
+        doseactors.py:530-542): the image volume's density map in g/cm3 (create_density_img,
+        materials.py:294-324), resampled linearly onto the output image's grid by physical position
+        with 0 outside when the two grids differ in size, spacing or origin (images_have_same_domain,
+        image.py:506-520)."""
+        rho = D.density_image(image.array, volume.voxel_materials, material_db)
+        same = list(self.size) == list(image.size) and \
+            all(math.isclose(a, b, rel_tol=1e-5) for a, b in zip(spacing, image.spacing)) and \
+            all(math.isclose(a, b, rel_tol=1e-5) for a, b in zip(origin, image.origin))
+        if same:
+            return rho
+        return D.resample_linear(rho, image.spacing, image.origin, self.size, spacing, origin,
+                                 direction).astype(np.float32)
 
     def on_image_grid(self, image):
         """True when the dose grid is the image's own voxel grid."""
@@ -1319,6 +1337,9 @@ class Simulation:
                     "edep_uncertainty": D.variance_or_uncertainty(edep, edep2, n_events, "uncertainty"),
                     "dose": dose, "dose_squared": dose2,
                     "dose_uncertainty": D.variance_or_uncertainty(dose, dose2, n_events, "uncertainty")}
+            if a.density.active:
+                data["density"] = a.density_image(vol, hu, self.volume_manager.material_database,
+                                                  spacing, origin, direction)
             for key, arr in data.items():
                 out = getattr(a, key)
                 out.image = image_io.Image(arr, spacing, origin, direction)

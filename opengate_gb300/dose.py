@@ -146,3 +146,54 @@ def precision_error(edep_a, edep2_a, edep_b, edep2_b, n, threshold=0.1):
         "median_rel": float(np.median(rel)),
         "equal": float(np.mean(d == 0)),
     }
+
+
+def density_image(hu, voxel_materials, material_db):
+    """Density (g/cm3) of each voxel from its HU interval (opengate/geometry/materials.py:294-324
+    create_density_img): voxels in [hu0, hu1) get the density of that interval's material, voxels
+    in no interval 0; float32."""
+    hu = np.asarray(hu)
+    rho = np.zeros(hu.shape, dtype=np.float32)
+    for hu0, hu1, name in voxel_materials:
+        rho[(hu >= hu0) & (hu < hu1)] = np.float32(material_db.get(name).density)
+    return rho
+
+
+def resample_linear(img, src_spacing, src_origin, dst_dims, dst_spacing, dst_origin, dst_direction=None,
+                    default=0.0):
+    """Linear resampling of an axis-aligned image onto another image's grid by physical position
+    (resample_itk_image_like, opengate/image.py:532-557: ITK ResampleImageFilter with the identity
+    transform and LinearInterpolateImageFunction).  The output voxel (i, j, k) sits at
+    p = dst_origin + dst_direction @ ((i, j, k) * dst_spacing); its continuous index in the source
+    is c = (p - src_origin) / src_spacing.  A point with c outside [-0.5, n - 0.5) on any axis gets
+    `default`; inside, trilinear weights over the eight neighbours, their indices clamped to the
+    image.  img [z][y][x]; spacings, origins and dims in x, y, z order; returns [z][y][x] float64."""
+    img = np.asarray(img, dtype=np.float64)
+    n = np.array(img.shape[::-1], dtype=np.int64)
+    dims = [int(v) for v in dst_dims]
+    sp_s, o_s = np.asarray(src_spacing, np.float64), np.asarray(src_origin, np.float64)
+    sp_d, o_d = np.asarray(dst_spacing, np.float64), np.asarray(dst_origin, np.float64)
+    rot = np.eye(3) if dst_direction is None else np.asarray(dst_direction, np.float64).reshape(3, 3)
+    flat = img.ravel()
+    out = np.empty((dims[2], dims[1], dims[0]), dtype=np.float64)
+    jj, ii = np.meshgrid(np.arange(dims[1]), np.arange(dims[0]), indexing="ij")
+    for k in range(dims[2]):  # one output slice at a time keeps the work arrays small
+        idx = np.stack([ii, jj, np.full_like(ii, k)], axis=-1) * sp_d
+        c = (o_d + idx @ rot.T - o_s) / sp_s  # [y][x][3]
+        ok = np.all((c >= -0.5) & (c < n - 0.5), axis=-1)
+        i0 = np.floor(c).astype(np.int64)
+        f = c - i0
+        lo, hi = np.clip(i0, 0, n - 1), np.clip(i0 + 1, 0, n - 1)
+        acc = np.zeros(ok.shape, dtype=np.float64)
+        for bz in (0, 1):
+            for by in (0, 1):
+                for bx in (0, 1):
+                    w = np.ones(ok.shape)
+                    at = []
+                    for a, b in ((0, bx), (1, by), (2, bz)):
+                        w = w * (f[..., a] if b else 1.0 - f[..., a])
+                        at.append(hi[..., a] if b else lo[..., a])
+                    acc += w * flat[(at[2] * n[1] + at[1]) * n[0] + at[0]]
+        acc[~ok] = default
+        out[k] = acc
+    return out

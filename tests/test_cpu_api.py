@@ -176,3 +176,79 @@ def test_units_follow_clhep():
     assert u.g_cm3 == pytest.approx(6.241509074460763e18, rel=1e-12)
     assert u.Gy == pytest.approx(1e-12, rel=1e-12)
     assert u.deg == pytest.approx(np.pi / 180)
+
+
+def test_dose_density_output_on_image_grid(tmp_path):
+    """density output = the HU-interval density map in g/cm3, 0 outside every interval
+    (create_density_img, materials.py:294-324); no resampling when the output grid is the image's."""
+    sim = water_sim(tmp_path)
+    vol = sim.volumes["phantom"]
+    arr = np.full((64, 64, 64), -2000, np.int16)
+    arr[10:20] = 0
+    arr[20:30] = 1500
+    vol.image = gate.Image(arr, spacing=(2.0, 2.0, 2.0))
+    vol.voxel_materials = [[-1000, 1000, "G4_WATER"], [1000, 3000, "G4_BONE_CORTICAL_ICRP"]]
+    d = sim.actors["dose"]
+    d.output_coordinate_system = "attached_to_image"
+    d.density.active = True
+    scene, v, hu, names, sources = sim.build_scene()
+    d.check(v, hu)
+    db = sim.volume_manager.material_database
+    spacing, origin, direction = d.output_geometry(v, hu)
+    rho = d.density_image(v, hu, db, spacing, origin, direction)
+    assert rho.dtype == np.float32 and rho.shape == arr.shape
+    assert np.all(rho[:10] == 0) and np.all(rho[30:] == 0)
+    assert np.all(rho[10:20] == np.float32(db.get("G4_WATER").density))
+    assert np.all(rho[20:30] == np.float32(db.get("G4_BONE_CORTICAL_ICRP").density))
+    d.counts.active = True
+    with pytest.raises(NotImplementedError):
+        d.check(v, hu)
+
+
+def test_dose_density_output_resampled_like_itk(tmp_path):
+    """A dose grid of its own: the density map is resampled linearly by physical position with 0
+    outside (resample_itk_image_like, image.py:532-557), checked against scipy's trilinear
+    map_coordinates on the continuous indices, and for a rotated output grid point by point."""
+    from scipy.ndimage import map_coordinates
+    from scipy.spatial.transform import Rotation
+
+    from opengate_gb300 import dose as D
+
+    rng = np.random.default_rng(7)
+    sim = water_sim(tmp_path)
+    vol = sim.volumes["phantom"]
+    arr = rng.integers(-1500, 2500, size=(20, 24, 28)).astype(np.int16)
+    vol.image = gate.Image(arr, spacing=(2.0, 2.5, 3.0), origin=(-20.0, 7.0, 3.0))
+    vol.voxel_materials = [[-1000, 0, "G4_ADIPOSE_TISSUE_ICRP"], [0, 1000, "G4_WATER"],
+                           [1000, 3000, "G4_BONE_CORTICAL_ICRP"]]
+    d = sim.actors["dose"]
+    d.size, d.spacing, d.translation = [11, 9, 13], [5.0, 6.0, 4.5], [3.0, -2.0, 1.0]
+    scene, v, hu, names, sources = sim.build_scene()
+    db = sim.volume_manager.material_database
+    rho_ct = D.density_image(hu.array, v.voxel_materials, db).astype(np.float64)
+    for cs in ("attached_to_image", None):
+        d.output_coordinate_system = cs
+        spacing, origin, direction = d.output_geometry(v, hu)
+        rho = d.density_image(v, hu, db, spacing, origin, direction)
+        assert rho.shape == (13, 9, 11) and rho.dtype == np.float32
+        grid = np.stack(np.meshgrid(*[np.arange(n) for n in (11, 9, 13)], indexing="ij"), -1)
+        p = np.asarray(origin) + (grid * np.asarray(spacing)) @ np.asarray(direction).T
+        c = (p - hu.origin) / hu.spacing  # [x][y][z][3], x-fastest axis first
+        n = np.array(hu.size)
+        inside = np.all((c >= -0.5) & (c < n - 0.5), axis=-1)
+        # trilinear with clamped neighbours = map_coordinates order 1, mode "nearest"
+        ref = map_coordinates(rho_ct, [c[..., 2], c[..., 1], c[..., 0]], order=1, mode="nearest")
+        ref[~inside] = 0.0
+        np.testing.assert_allclose(rho, ref.transpose(2, 1, 0).astype(np.float32), rtol=1e-6, atol=1e-7)
+        assert inside.any() and (~inside).any()
+    # rotated output grid
+    rot = Rotation.from_euler("zy", [25, -10], degrees=True).as_matrix()
+    out = D.resample_linear(rho_ct, hu.spacing, hu.origin, [7, 8, 9], [3.0, 3.0, 3.0], [-5.0, 10.0, 20.0], rot)
+    for (i, j, k) in [(0, 0, 0), (3, 4, 5), (6, 7, 8), (2, 0, 7)]:
+        p = np.array([-5.0, 10.0, 20.0]) + rot @ (np.array([i, j, k]) * 3.0)
+        c = (p - hu.origin) / hu.spacing
+        if np.all((c >= -0.5) & (c < np.array(hu.size) - 0.5)):
+            want = map_coordinates(rho_ct, [[c[2]], [c[1]], [c[0]]], order=1, mode="nearest")[0]
+        else:
+            want = 0.0
+        assert out[k, j, i] == pytest.approx(want, rel=1e-12, abs=1e-12)
