@@ -767,10 +767,13 @@ int gg_upload_tables(gg_ctx *c, const gg_tables_desc *t) {
   char msg[160];
   if (gg::check_tables(t, msg, sizeof(msg))) return c->fail(GG_ERR_ARG, "gg_upload_tables: %s", msg);
   size_t nce = (size_t)t->n_comp * t->n_e;
-  size_t need = c->precision == GG_PREC_F64 ? gg::transport_smem_bytes<double>(t->n_comp, t->n_e, t->n_mat)
-                                            : gg::transport_smem_bytes<float>(t->n_comp, t->n_e, t->n_mat);
-  if (need > 190 * 1024)
-    return c->fail(GG_ERR_ARG, "gg_upload_tables: tables need %zu bytes of shared memory (max 190 KiB)", need);
+  // tables plus the transport block's two per-history voxel lists
+  size_t need = c->precision == GG_PREC_F64
+                    ? gg::transport_smem_bytes<double>(t->n_comp, t->n_e, t->n_mat) + gg::hist_list_bytes<double>(2)
+                    : gg::transport_smem_bytes<float>(t->n_comp, t->n_e, t->n_mat) + gg::hist_list_bytes<float>(2);
+  if (need > (size_t)gg::kTransportSmemMax)
+    return c->fail(GG_ERR_ARG, "gg_upload_tables: tables and voxel lists need %zu bytes of shared memory (max %d)",
+                   need, gg::kTransportSmemMax);
   if (c->tle && (t->n_e != c->n_e || t->n_comp != c->n_comp)) c->tle = false;  // its table no longer fits
   c->n_e = t->n_e;
   c->n_comp = t->n_comp;

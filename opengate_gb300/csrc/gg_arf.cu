@@ -92,8 +92,7 @@ __global__ void __launch_bounds__(256) k_arf_sample(Scene<real> s, ArfArgs p) {
     sec.stride = blockDim.x;
     sec.tid = threadIdx.x;
     sec.has = 0;
-    HistList<real> l;
-    l.n = 0;
+    HistList<real> l{nullptr, nullptr, 0, 0};  // never scored here
     Tally<real> t{nullptr, nullptr};
     Event<real> ev;
     ev.clear();

@@ -23,7 +23,6 @@
 
 namespace gg {
 
-constexpr int kHistList = 8;      // per-history voxel list (registers)
 constexpr int kLoopCap = 1000;    // sampling-loop iteration cap
 constexpr int kStepCap = 1000000; // per-photon step cap (termination guard)
 constexpr int kHeadRegions = 8;   // SPECT head slabs: collimator, gap, cover, crystal, 4 back layers

@@ -140,8 +140,24 @@ cudaError_t launch_mlp_predict(const MlpTrainArgs &a, float *out, uint64_t n, in
 template <typename real>
 cudaError_t launch_spect_arf(const Scene<real> &s, const ArfStageArgs &a, int grid, cudaStream_t st);
 
+constexpr int kHistList = 8;     // entries of a history's voxel list
+constexpr int kBlock = 256;      // most threads per block of the transport kernels
+constexpr int kTransportSmemMax = 200 * 1024;  // dynamic shared memory of a transport block
+
+// Shared memory of the transport kernels' tables: sigma rows, majorant, density
+// and composition index per material, 16-byte aligned.
 template <typename real>
-size_t transport_smem_bytes(int n_comp, int n_e, int n_mat);
+__host__ __device__ inline size_t transport_smem_bytes(int n_comp, int n_e, int n_mat) {
+  size_t b = sizeof(real) * ((size_t)n_comp * n_e + n_e + n_mat) + sizeof(int) * (size_t)n_mat;
+  return (b + 15) & ~(size_t)15;
+}
+
+// Shared memory of `lists` per-history voxel lists of a block of `threads`
+// (one column per thread).
+template <typename real>
+__host__ __device__ constexpr size_t hist_list_bytes(int lists, int threads = kBlock) {
+  return (size_t)lists * kHistList * (size_t)threads * (sizeof(uint32_t) + sizeof(real));
+}
 // Rows of p.n samples appended to rows[*total ...] (capacity rows); *total advances on the device.
 template <typename real>
 cudaError_t launch_arf_dataset(const Scene<real> &s, const ArfArgs &p, float4 *rows, uint64_t capacity,

@@ -15,10 +15,15 @@
 
 namespace gg {
 
+// One history's voxel list: entry k at vox[k * stride], acc[k * stride] in
+// shared memory (a column per thread of the block), so the list takes no
+// registers across the transport loop.  Kernels that never score pass null
+// arrays with n = 0.
 template <typename real>
 struct HistList {
-  uint32_t vox[kHistList];
-  real acc[kHistList];
+  uint32_t *vox;
+  real *acc;
+  int stride;
   int n;
 };
 
@@ -43,18 +48,15 @@ struct Tally {
 // has edep^2 == edep * edep exactly in these units.
 template <typename real>
 __device__ __forceinline__ void hlist_flush(HistList<real> &l, const Tally<real> &t, BlockCounters *bc) {
-#pragma unroll
-  for (int k = 0; k < kHistList; ++k) {
-    if (k < l.n) {
-      const unsigned long long q = (unsigned long long)to_fixed(l.acc[k]);
-      const uint32_t v = l.vox[k];
-      atomicAdd(&t.acc_e[v], q);
-      if (t.acc_e2) {
-        const unsigned long long lo = q * q;
-        const unsigned long long hi = __umul64hi(q, q);
-        atomicAdd(&t.acc_e2[2 * (size_t)v], lo & 0xffffffffull);
-        atomicAdd(&t.acc_e2[2 * (size_t)v + 1], (hi << 32) | (lo >> 32));
-      }
+  for (int k = 0; k < l.n; ++k) {
+    const unsigned long long q = (unsigned long long)to_fixed(l.acc[k * l.stride]);
+    const uint32_t v = l.vox[k * l.stride];
+    atomicAdd(&t.acc_e[v], q);
+    if (t.acc_e2) {
+      const unsigned long long lo = q * q;
+      const unsigned long long hi = __umul64hi(q, q);
+      atomicAdd(&t.acc_e2[2 * (size_t)v], lo & 0xffffffffull);
+      atomicAdd(&t.acc_e2[2 * (size_t)v + 1], (hi << 32) | (lo >> 32));
     }
   }
   if (l.n) atomicAdd(&bc->tally_entries, (unsigned int)l.n);
@@ -66,26 +68,19 @@ __device__ __forceinline__ void deposit(HistList<real> &l, const Tally<real> &t,
                                         uint32_t v, real e, unsigned int &n_dep) {
   if (!(e > R<real>(0))) return;
   ++n_dep;
-  bool found = false;
-#pragma unroll
-  for (int k = 0; k < kHistList; ++k) {
-    if (!found && k < l.n && l.vox[k] == v) {
-      l.acc[k] = l.acc[k] + e;
-      found = true;
+  for (int k = 0; k < l.n; ++k) {
+    if (l.vox[k * l.stride] == v) {
+      real &a = l.acc[k * l.stride];
+      a = a + e;
+      return;
     }
   }
-  if (found) return;
   if (l.n == kHistList) {
     atomicAdd(&bc->list_overflows, 1u);
     hlist_flush(l, t, bc);
   }
-#pragma unroll
-  for (int k = 0; k < kHistList; ++k) {
-    if (k == l.n) {
-      l.vox[k] = v;
-      l.acc[k] = e;
-    }
-  }
+  l.vox[l.n * l.stride] = v;
+  l.acc[l.n * l.stride] = e;
   l.n++;
 }
 

@@ -314,8 +314,7 @@ __global__ void __launch_bounds__(256, MINB) k_spect_phantom(Scene<real> sg, Ker
   sec.stride = blockDim.x;
   sec.tid = threadIdx.x;
   sec.has = 0;
-  HistList<real> l;
-  l.n = 0;
+  HistList<real> l{nullptr, nullptr, 0, 0};  // never scored here
   Tally<real> t{nullptr, nullptr};
   Event<real> ev_unused;
   Rng g;
@@ -526,8 +525,7 @@ __global__ void __launch_bounds__(256, MINB) k_spect_head(Scene<real> sg, Kernel
   sec.stride = blockDim.x;
   sec.tid = threadIdx.x;
   sec.has = 0;
-  HistList<real> l;
-  l.n = 0;
+  HistList<real> l{nullptr, nullptr, 0, 0};  // never scored here
   Tally<real> t{nullptr, nullptr};
   Event<real> ev;
   ev.clear();

@@ -234,10 +234,22 @@ __global__ void __launch_bounds__(256, MINB) k_transport(Scene<real> sg, KernelA
   sec.stride = blockDim.x;
   sec.tid = threadIdx.x;
   sec.has = 0;
-  HistList<real> l;
-  l.n = 0;
-  HistList<real> ld;  // dose list of the history (DG 2): same voxels as l
-  ld.n = 0;
+  // history lists after the tables: [list][vox | acc][kHistList][blockDim.x]
+  HistList<real> l, ld;  // ld: dose list of the history (DG 2), same voxels as l
+  {
+    const int nt = (int)blockDim.x;
+    unsigned char *lists = smem_raw + transport_smem_bytes<real>(sg.n_comp, sg.n_e, sg.n_mat);
+    l.vox = reinterpret_cast<uint32_t *>(lists) + threadIdx.x;
+    l.acc = reinterpret_cast<real *>(lists + (size_t)kHistList * nt * sizeof(uint32_t)) + threadIdx.x;
+    l.stride = nt;
+    l.n = 0;
+    ld = l;
+    if constexpr (DG == 2) {
+      lists += hist_list_bytes<real>(1, nt);
+      ld.vox = reinterpret_cast<uint32_t *>(lists) + threadIdx.x;
+      ld.acc = reinterpret_cast<real *>(lists + (size_t)kHistList * nt * sizeof(uint32_t)) + threadIdx.x;
+    }
+  }
   Event<real> ev;
   ev.clear();
   Rng g;
@@ -433,11 +445,6 @@ __global__ void k_flush(unsigned long long *acc_e, unsigned long long *acc_e2, d
   }
 }
 
-template <typename real>
-size_t transport_smem_bytes(int n_comp, int n_e, int n_mat) {
-  size_t b = sizeof(real) * ((size_t)n_comp * n_e + n_e + n_mat) + sizeof(int) * (size_t)n_mat;
-  return (b + 15) & ~(size_t)15;
-}
 
 template <typename real>
 size_t record_bytes(size_t cap) {
@@ -457,8 +464,11 @@ template <typename real, int MINB, bool MULTI, bool TLE = false, int DG = 0>
 static cudaError_t launch_transport_v(const Scene<real> &s, const KernelArgs &a, int grid, int block, size_t smem,
                                       cudaStream_t st) {
   static unsigned long long configured = 0;
-  cudaError_t e = configure_smem(k_transport<real, MINB, false, MULTI, TLE, DG>, 200 * 1024, configured);
+  if (block <= 0 || block > kBlock) return cudaErrorInvalidValue;
+  cudaError_t e = configure_smem(k_transport<real, MINB, false, MULTI, TLE, DG>, kTransportSmemMax, configured);
   if (e != cudaSuccess) return e;
+  smem += hist_list_bytes<real>(DG == 2 ? 2 : 1, block);
+  if (smem > (size_t)kTransportSmemMax) return cudaErrorInvalidValue;
   k_transport<real, MINB, false, MULTI, TLE, DG><<<grid, block, smem, st>>>(s, a);
   return cudaGetLastError();
 }
@@ -505,6 +515,7 @@ cudaError_t launch_flush(unsigned long long *acc_e, unsigned long long *acc_e2, 
 
 template <typename real>
 cudaError_t occupancy_blocks(int block, size_t smem, int minb, int *bps) {
+  smem += hist_list_bytes<real>(1, block);
   if (minb <= 2) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(bps, k_transport<real, 2, false, false, false>, block, smem);
   if (minb == 3) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(bps, k_transport<real, 3, false, false, false>, block, smem);
   return cudaOccupancyMaxActiveBlocksPerMultiprocessor(bps, k_transport<real, 4, false, false, false>, block, smem);
@@ -514,8 +525,6 @@ template size_t record_bytes<float>(size_t);
 template size_t record_bytes<double>(size_t);
 template cudaError_t launch_generate<float>(const Scene<float> &, const KernelArgs &, cudaStream_t);
 template cudaError_t launch_generate<double>(const Scene<double> &, const KernelArgs &, cudaStream_t);
-template size_t transport_smem_bytes<float>(int, int, int);
-template size_t transport_smem_bytes<double>(int, int, int);
 template cudaError_t launch_transport<float>(const Scene<float> &, const KernelArgs &, int, int, size_t, int,
                                              cudaStream_t);
 template cudaError_t launch_transport<double>(const Scene<double> &, const KernelArgs &, int, int, size_t, int,

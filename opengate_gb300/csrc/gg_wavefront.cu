@@ -137,26 +137,18 @@ __device__ __forceinline__ void store_rng(const Slots<real> &S, int k, const Rng
   for (int j = 0; j < 4; ++j) S.rb[j * kWSlots + k] = g.buf[j];
 }
 
+// The voxel list of slot k, in place in the slot arrays.
 template <typename real>
 __device__ __forceinline__ void load_hist(const Slots<real> &S, int k, HistList<real> &l) {
+  l.vox = S.hvox + k;
+  l.acc = S.hacc + k;
+  l.stride = kWSlots;
   l.n = (int)S.hn[k];
-#pragma unroll
-  for (int j = 0; j < kHistList; ++j) {
-    l.vox[j] = S.hvox[j * kWSlots + k];
-    l.acc[j] = S.hacc[j * kWSlots + k];
-  }
 }
 
 template <typename real>
 __device__ __forceinline__ void store_hist(const Slots<real> &S, int k, const HistList<real> &l) {
   S.hn[k] = (uint32_t)l.n;
-#pragma unroll
-  for (int j = 0; j < kHistList; ++j) {
-    if (j < l.n) {
-      S.hvox[j * kWSlots + k] = l.vox[j];
-      S.hacc[j * kWSlots + k] = l.acc[j];
-    }
-  }
 }
 
 // pending interaction word: material | scored << 16 | kind << 24
