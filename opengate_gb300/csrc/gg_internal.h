@@ -10,7 +10,8 @@ namespace gg {
 
 // cudaFuncSetAttribute applies to the current device only: `done` remembers,
 // one bit per device ordinal (< 64), on which devices a kernel's dynamic
-// shared-memory limit has been raised.
+// shared-memory limit has been raised: to `bytes`, or to what the block's
+// opt-in limit leaves beside the kernel's static shared memory if less.
 template <typename K>
 inline cudaError_t configure_smem(K kernel, int bytes, unsigned long long &done) {
   int dev = 0;
@@ -18,6 +19,12 @@ inline cudaError_t configure_smem(K kernel, int bytes, unsigned long long &done)
   if (e != cudaSuccess) return e;
   const unsigned long long bit = (dev >= 0 && dev < 64) ? (1ull << dev) : 0ull;
   if (bit && (done & bit)) return cudaSuccess;
+  int optin = 0;
+  cudaFuncAttributes fa;
+  if ((e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev)) != cudaSuccess) return e;
+  if ((e = cudaFuncGetAttributes(&fa, kernel)) != cudaSuccess) return e;
+  const int room = optin - (int)fa.sharedSizeBytes;
+  if (room < bytes) bytes = room;
   e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
   if (e == cudaSuccess) done |= bit;
   return e;

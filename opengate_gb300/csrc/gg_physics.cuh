@@ -63,6 +63,39 @@ __device__ __forceinline__ void hlist_flush(HistList<real> &l, const Tally<real>
   l.n = 0;
 }
 
+// Histories a warp has claimed from the launch's work counter and not yet
+// handed out, [p[0], p[1]), kept in shared memory (one pair per warp) because
+// only refills use them.  Every lane of the warp calls this with the ballot of
+// the lanes that need a history; those get the next histories in lane order
+// (the others a value they ignore), `chunk` more being claimed when the pool
+// runs short.
+__device__ __forceinline__ uint64_t warp_pool_claim(uint64_t *p, unsigned m_need, unsigned lane, unsigned lt_mask,
+                                                    unsigned long long *next, int chunk) {
+  const unsigned n_need = __popc(m_need);
+  const unsigned rank = __popc(m_need & lt_mask);
+  uint64_t pn = p[0];
+  const uint64_t avail = p[1] - pn;
+  uint64_t h;
+  if (avail >= n_need) {
+    h = pn + rank;
+    pn += n_need;
+    __syncwarp();
+    if (lane == 0) p[0] = pn;
+  } else {
+    unsigned long long base = 0;
+    if (lane == 0) base = atomicAdd(next, (unsigned long long)chunk);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    h = rank < avail ? pn + rank : base + (rank - avail);
+    __syncwarp();
+    if (lane == 0) {
+      p[0] = base + (n_need - avail);
+      p[1] = base + (uint64_t)chunk;
+    }
+  }
+  __syncwarp();
+  return h;
+}
+
 template <typename real>
 __device__ __forceinline__ void deposit(HistList<real> &l, const Tally<real> &t, BlockCounters *bc,
                                         uint32_t v, real e, unsigned int &n_dep) {

@@ -302,7 +302,10 @@ __global__ void __launch_bounds__(256, MINB) k_spect_phantom(Scene<real> sg, Ker
   const uint64_t n_items = from_queue ? min((uint64_t)*q.in_n, (uint64_t)q.q_cap) : args.h_end - args.h_begin;
   const unsigned lane = threadIdx.x & 31u;
   const unsigned lt_mask = (1u << lane) - 1u;
-  uint64_t pool_next = 0, pool_end = 0;
+  __shared__ uint64_t wpool[kBlock / 32][2];  // per warp: claimed histories not yet handed out
+  uint64_t *pool = wpool[threadIdx.x >> 5];
+  if (lane == 0) pool[0] = pool[1] = 0;
+  __syncwarp();
 
   Photon<real> ph;
   ph.alive = 0;
@@ -319,8 +322,14 @@ __global__ void __launch_bounds__(256, MINB) k_spect_phantom(Scene<real> sg, Ker
   Event<real> ev_unused;
   Rng g;
   int state = kRefill;
-  bool in_hist = false, has_ev = false;
-  uint64_t hid = 0, slot = 0;
+  bool in_hist = false;
+  // the history id is the Rng's counter words (rng_resume sets both from it)
+  auto hid_of = [&]() { return ((uint64_t)g.h1 << 32) | (uint64_t)g.h0; };
+  // input-queue slot of the lane's photon | kHasEv when it carries an event
+  // (read when the photon dies or leaves)
+  __shared__ uint64_t sslot[kBlock];
+  constexpr uint64_t kHasEv = 1ull << 63;
+  sslot[threadIdx.x] = 0;
   int pmat = 0, pscored = 0;
   uint32_t pv = 0;
   unsigned int n_wood = 0, n_real = 0, n_dep = 0, n_world = 0, n_singles = 0;
@@ -343,36 +352,23 @@ __global__ void __launch_bounds__(256, MINB) k_spect_phantom(Scene<real> sg, Ker
 
     if (phase == kRefill) {
       const bool need = state == kRefill;
-      if (need && in_hist && has_ev) {
+      if (need && in_hist && (sslot[threadIdx.x] & kHasEv)) {
         // a photon that came back from a head died here: score its event
         Event<real> ev;
         real v[kEvSlots];
-        load_event(in, slot, v);
+        load_event(in, sslot[threadIdx.x] & ~kHasEv, v);
         event_from(v, ev);
         n_singles += score_singles(s, ev, ph.run, g);
       }
       if (need) in_hist = false;
-      const unsigned n_need = __popc(m_ref);
-      const unsigned rank = __popc(m_ref & lt_mask);
-      const uint64_t avail = pool_end - pool_next;
-      uint64_t h;
-      if (avail >= n_need) {
-        h = pool_next + rank;
-        pool_next += n_need;
-      } else {
-        unsigned long long base = 0;
-        if (lane == 0) base = atomicAdd(args.next, (unsigned long long)args.chunk);
-        base = __shfl_sync(0xffffffffu, base, 0);
-        h = rank < avail ? pool_next + rank : base + (rank - avail);
-        pool_next = base + (n_need - avail);
-        pool_end = base + (uint64_t)args.chunk;
-      }
+      const uint64_t h = warp_pool_claim(pool, m_ref, lane, lt_mask, args.next, args.chunk);
       if (need) {
         if (h >= n_items) {
           state = kDone;
         } else if (from_queue) {
-          hid = queue_get<real, FFM != kFfOff>(s, in, h, ph, g, args.seed, has_ev);
-          slot = h;
+          bool has_ev;
+          queue_get<real, FFM != kFfOff>(s, in, h, ph, g, args.seed, has_ev);
+          sslot[threadIdx.x] = h | (has_ev ? kHasEv : 0ull);
           ph.in_head = 0;
           ph.in_image = 1;
           ph.t_exit = exit_distance(ph.pos, ph.dir, s.bmin, s.bmax);
@@ -396,9 +392,9 @@ __global__ void __launch_bounds__(256, MINB) k_spect_phantom(Scene<real> sg, Ker
             ph.in_head = 0;
             ph.exclude = -1;
             ph.w = s.s_fd_w;  // 1, or the forced direction's cone weight
-            hid = args.h_begin + h;
+            const uint64_t hid = args.h_begin + h;
             ph.run = run_of(s, hid);
-            has_ev = false;
+            sslot[threadIdx.x] = 0;
             nsplit = 0;
             ncompt = 0;
             rng_resume(g, args.seed, hid, rec.rng_pos[r], rec.rng_buf[r]);
@@ -448,7 +444,7 @@ __global__ void __launch_bounds__(256, MINB) k_spect_phantom(Scene<real> sg, Ker
           if (req_c ? kc < q.split_cap : kr < q.split_cap) {
             const size_t k = req_c ? kc : q.split_cap - 1 - kr;
             const SplitQueue<real> sq = SplitQueue<real>::carve(q.split_q, q.split_cap);
-            sq.hid[k] = hid;
+            sq.hid[k] = hid_of();
             sq.px[k] = pre.pos[0];
             sq.py[k] = pre.pos[1];
             sq.pz[k] = pre.pos[2];
@@ -487,8 +483,10 @@ __global__ void __launch_bounds__(256, MINB) k_spect_phantom(Scene<real> sg, Ker
       if (push) {
         if (k < q.q_cap) {
           real v[kEvSlots];
-          if (has_ev) load_event(in, slot, v);
-          queue_put<real, FFM != kFfOff>(out, k, ph, g, hid, v, has_ev);
+          const uint64_t sl = sslot[threadIdx.x];
+          const bool has_ev = (sl & kHasEv) != 0;
+          if (has_ev) load_event(in, sl & ~kHasEv, v);
+          queue_put<real, FFM != kFfOff>(out, k, ph, g, hid_of(), v, has_ev);
         } else {
           atomicOr(args.status, kStatusQueueOverflow);
         }
@@ -515,7 +513,10 @@ __global__ void __launch_bounds__(256, MINB) k_spect_head(Scene<real> sg, Kernel
   const uint64_t n_items = min((uint64_t)*q.in_n, (uint64_t)q.q_cap);
   const unsigned lane = threadIdx.x & 31u;
   const unsigned lt_mask = (1u << lane) - 1u;
-  uint64_t pool_next = 0, pool_end = 0;
+  __shared__ uint64_t wpool[kBlock / 32][2];  // per warp: claimed histories not yet handed out
+  uint64_t *pool = wpool[threadIdx.x >> 5];
+  if (lane == 0) pool[0] = pool[1] = 0;
+  __syncwarp();
 
   Photon<real> ph;
   ph.alive = 0;
@@ -532,7 +533,6 @@ __global__ void __launch_bounds__(256, MINB) k_spect_head(Scene<real> sg, Kernel
   Rng g;
   int state = kRefill;
   bool in_hist = false;
-  uint64_t hid = 0;
   int pmat = 0, pscored = 0;
   uint32_t pv = 0;
   unsigned int n_dep = 0, n_world = 0, n_head = 0, n_singles = 0;
@@ -557,27 +557,13 @@ __global__ void __launch_bounds__(256, MINB) k_spect_head(Scene<real> sg, Kernel
         n_singles += score_singles(s, ev, ph.run, g);
         in_hist = false;
       }
-      const unsigned n_need = __popc(m_ref);
-      const unsigned rank = __popc(m_ref & lt_mask);
-      const uint64_t avail = pool_end - pool_next;
-      uint64_t h;
-      if (avail >= n_need) {
-        h = pool_next + rank;
-        pool_next += n_need;
-      } else {
-        unsigned long long base = 0;
-        if (lane == 0) base = atomicAdd(args.next, (unsigned long long)args.chunk);
-        base = __shfl_sync(0xffffffffu, base, 0);
-        h = rank < avail ? pool_next + rank : base + (rank - avail);
-        pool_next = base + (n_need - avail);
-        pool_end = base + (uint64_t)args.chunk;
-      }
+      const uint64_t h = warp_pool_claim(pool, m_ref, lane, lt_mask, args.next, args.chunk);
       if (need) {
         if (h >= n_items) {
           state = kDone;
         } else {
           bool has_ev;
-          hid = queue_get<real, FF>(s, in, h, ph, g, args.seed, has_ev);
+          queue_get<real, FF>(s, in, h, ph, g, args.seed, has_ev);
           if (has_ev) {
             real v[kEvSlots];
             load_event(in, h, v);
@@ -613,7 +599,7 @@ __global__ void __launch_bounds__(256, MINB) k_spect_head(Scene<real> sg, Kernel
         if (k < q.q_cap) {
           real v[kEvSlots];
           event_to(ev, v);
-          queue_put<real, FF>(out, k, ph, g, hid, v, true);
+          queue_put<real, FF>(out, k, ph, g, ((uint64_t)g.h1 << 32) | (uint64_t)g.h0, v, true);
         } else {
           atomicOr(args.status, kStatusQueueOverflow);
         }

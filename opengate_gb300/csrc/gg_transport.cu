@@ -224,8 +224,10 @@ __global__ void __launch_bounds__(256, MINB) k_transport(Scene<real> sg, KernelA
   const unsigned lane = threadIdx.x & 31u;
   const unsigned lt_mask = (1u << lane) - 1u;
   const uint64_t n_hist = args.h_end - args.h_begin;
-  // warp-uniform pool of claimed history offsets [pool_next, pool_end)
-  uint64_t pool_next = 0, pool_end = 0;
+  __shared__ uint64_t wpool[kBlock / 32][2];  // per warp: claimed histories not yet handed out
+  uint64_t *pool = wpool[threadIdx.x >> 5];
+  if (lane == 0) pool[0] = pool[1] = 0;
+  __syncwarp();
 
   Photon<real> ph;
   ph.alive = 0;
@@ -287,21 +289,7 @@ __global__ void __launch_bounds__(256, MINB) k_transport(Scene<real> sg, KernelA
         }
       }
       if (need) in_hist = false;
-      const unsigned n_need = __popc(m_ref);
-      const unsigned rank = __popc(m_ref & lt_mask);
-      const uint64_t avail = pool_end - pool_next;
-      uint64_t h;
-      if (avail >= n_need) {
-        h = pool_next + rank;
-        pool_next += n_need;
-      } else {
-        unsigned long long base = 0;
-        if (lane == 0) base = atomicAdd(args.next, (unsigned long long)args.chunk);
-        base = __shfl_sync(0xffffffffu, base, 0);
-        h = rank < avail ? pool_next + rank : base + (rank - avail);
-        pool_next = base + (n_need - avail);
-        pool_end = base + (uint64_t)args.chunk;
-      }
+      const uint64_t h = warp_pool_claim(pool, m_ref, lane, lt_mask, args.next, args.chunk);
       if (need) {
         if (h >= n_hist) {
           state = kDone;
