@@ -141,6 +141,9 @@ __device__ __forceinline__ void rng_resume(Rng &g, uint64_t seed, uint64_t hid, 
   g.buf[3] = b.w;
 }
 
+// The history of a resumed stream: its counter words (rng_resume sets both from it).
+__device__ __forceinline__ uint64_t rng_history(const Rng &g) { return ((uint64_t)g.h1 << 32) | (uint64_t)g.h0; }
+
 template <typename real>
 __device__ __forceinline__ int run_of(const Scene<real> &s, uint64_t hid) {
   return s.run_base + (int)((hid - s.run_first) / s.run_len);

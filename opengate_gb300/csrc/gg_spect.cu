@@ -323,8 +323,6 @@ __global__ void __launch_bounds__(256, MINB) k_spect_phantom(Scene<real> sg, Ker
   Rng g;
   int state = kRefill;
   bool in_hist = false;
-  // the history id is the Rng's counter words (rng_resume sets both from it)
-  auto hid_of = [&]() { return ((uint64_t)g.h1 << 32) | (uint64_t)g.h0; };
   // input-queue slot of the lane's photon | kHasEv when it carries an event
   // (read when the photon dies or leaves)
   __shared__ uint64_t sslot[kBlock];
@@ -444,7 +442,7 @@ __global__ void __launch_bounds__(256, MINB) k_spect_phantom(Scene<real> sg, Ker
           if (req_c ? kc < q.split_cap : kr < q.split_cap) {
             const size_t k = req_c ? kc : q.split_cap - 1 - kr;
             const SplitQueue<real> sq = SplitQueue<real>::carve(q.split_q, q.split_cap);
-            sq.hid[k] = hid_of();
+            sq.hid[k] = rng_history(g);
             sq.px[k] = pre.pos[0];
             sq.py[k] = pre.pos[1];
             sq.pz[k] = pre.pos[2];
@@ -486,7 +484,7 @@ __global__ void __launch_bounds__(256, MINB) k_spect_phantom(Scene<real> sg, Ker
           const uint64_t sl = sslot[threadIdx.x];
           const bool has_ev = (sl & kHasEv) != 0;
           if (has_ev) load_event(in, sl & ~kHasEv, v);
-          queue_put<real, FFM != kFfOff>(out, k, ph, g, hid_of(), v, has_ev);
+          queue_put<real, FFM != kFfOff>(out, k, ph, g, rng_history(g), v, has_ev);
         } else {
           atomicOr(args.status, kStatusQueueOverflow);
         }
@@ -599,7 +597,7 @@ __global__ void __launch_bounds__(256, MINB) k_spect_head(Scene<real> sg, Kernel
         if (k < q.q_cap) {
           real v[kEvSlots];
           event_to(ev, v);
-          queue_put<real, FF>(out, k, ph, g, ((uint64_t)g.h1 << 32) | (uint64_t)g.h0, v, true);
+          queue_put<real, FF>(out, k, ph, g, rng_history(g), v, true);
         } else {
           atomicOr(args.status, kStatusQueueOverflow);
         }
