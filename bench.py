@@ -33,11 +33,12 @@ import numpy as np  # noqa: E402
 METRIC = "primaries/s at matched sigma (plain GPU transport, CT phantom dose)"
 UNIT = "primaries/s"
 PRIMARIES_PER_STEP = 100_000_000
-TRANSPORT_DRAM_PER_PRIMARY = (478.16e6 + 200.48e6) / 3e6  # bytes, ncu capture of the dose workload
+TRANSPORT_DRAM_PER_PRIMARY = (407.04e6 + 110.38e6) / 3e6  # bytes, ncu capture of the dose workload
 # warp instructions per primary of the dose transport kernels and their active lanes per warp
 # instruction (ncu captures of the same workload, 3e6 primaries: smsp__inst_executed.sum and
-# smsp__thread_inst_executed_per_inst_executed.ratio; phase kernel, compacted wavefront kernel)
-TRANSPORT_ISSUE = {"phased": (1.185021951e9 / 3e6, 9.05), "wavefront": (1.045618891e9 / 3e6, 14.12)}
+# smsp__thread_inst_executed_per_inst_executed.ratio; phase kernel, compacted wavefront kernel
+# (the latter captured before the history lists moved to shared memory))
+TRANSPORT_ISSUE = {"phased": (1.136376062e9 / 3e6, 8.60), "wavefront": (1.045618891e9 / 3e6, 14.12)}
 WORKLOAD = "ct_phantom_256x256x160_1.2mm_ssd100_field10x10_spectrum60_0.1-6MeV"
 
 # SPECT acquisition: CT phantom as attenuation map, Tc-99m activity image,
