@@ -1249,9 +1249,12 @@ static int run_impl(gg_ctx *c, uint64_t n, uint64_t seed, uint64_t first, bool c
   size_t smem = c->precision == GG_PREC_F64 ? gg::transport_smem_bytes<double>(c->n_comp, c->n_e, c->n_mat)
                                             : gg::transport_smem_bytes<float>(c->n_comp, c->n_e, c->n_mat);
   // kernel variant: register budget for `minb` resident 256-thread blocks
-  // batched simulations bind their geometry per history: more live registers, default 2 blocks / SM
+  // batched simulations bind their geometry per history: more live registers, default 2 blocks / SM;
+  // the track-length estimator's voxel walks: 3 (80 registers: 34.3 ms per 1e7 pencil primaries
+  // against 36.5 at 4 blocks / SM)
+  const bool tle_run = c->tle && !c->have_spect && !c->have_batch;
   int minb = c->blocks_per_sm > 0 ? std::min(c->blocks_per_sm, 4)
-                                  : ((c->precision == GG_PREC_F64 || c->have_batch) ? 2 : 4);
+                                  : ((c->precision == GG_PREC_F64 || c->have_batch) ? 2 : (tle_run ? 3 : 4));
   int bps = 0;
   {
     cudaError_t e = c->precision == GG_PREC_F64 ? gg::occupancy_blocks<double>(c->block, smem, minb, &bps)

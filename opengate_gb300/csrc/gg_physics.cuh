@@ -825,7 +825,7 @@ __device__ __forceinline__ void voxel_walk(const Scene<real> &s, const real p[3]
 }
 
 // Label gathers in flight per lane in the track-length estimator's walks.
-constexpr int kTleGroup = 4;
+constexpr int kTleGroup = 2;
 
 template <typename real, int GROUP, typename Visit>
 __device__ __forceinline__ void voxel_walk_grouped(const Scene<real> &s, const real p[3], const real d[3], real len,
