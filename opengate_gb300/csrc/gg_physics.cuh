@@ -118,9 +118,11 @@ __device__ __forceinline__ void deposit(HistList<real> &l, const Tally<real> &t,
 }
 
 // Klein-Nishina (G4KleinNishinaCompton sampling of the Physics Reference Manual)
+// The rejection loop of the Klein-Nishina sampling: eps = E'/E, 1 - cos(theta)
+// and sin^2(theta) of the scattering (3 draws per trial).
 template <typename real>
-__device__ __forceinline__ real compton(const Scene<real> &s, Photon<real> &ph, Rng &g, BlockCounters *bc) {
-  real e = ph.e;
+__device__ __forceinline__ void compton_kn(real e, Rng &g, BlockCounters *bc, real &eps, real &onecost,
+                                           real &sint2) {
   real k = e * R<real>(1.0 / kMC2);
   real twok = R<real>(2) * k;
   real eps0 = R<real>(1) / (R<real>(1) + twok);
@@ -129,7 +131,7 @@ __device__ __forceinline__ real compton(const Scene<real> &s, Photon<real> &ph, 
   real alpha2 = R<real>(1) - eps0sq;
   alpha2 = R<real>(0.5) * alpha2;
   alpha2 = alpha1 + alpha2;
-  real eps, epssq, onecost, sint2;
+  real epssq;
   int it = 0;
   for (;;) {
     real r0 = u01<real>(g);
@@ -156,6 +158,14 @@ __device__ __forceinline__ real compton(const Scene<real> &s, Photon<real> &ph, 
       break;
     }
   }
+}
+
+// The rest of a Compton scattering sampled by compton_kn: azimuth (one draw),
+// new direction and energy; returns the energy given to the electron.
+template <typename real>
+__device__ __forceinline__ real compton_finish(const Scene<real> &s, Photon<real> &ph, Rng &g, real eps, real onecost,
+                                               real sint2) {
+  const real e = ph.e;
   real e1 = eps * e;
   real edep = e - e1;
   real cost = R<real>(1) - onecost;
@@ -173,8 +183,17 @@ __device__ __forceinline__ real compton(const Scene<real> &s, Photon<real> &ph, 
 }
 
 template <typename real>
-__device__ __forceinline__ void rayleigh(const Scene<real> &s, int comp, Photon<real> &ph, Rng &g,
-                                         BlockCounters *bc) {
+__device__ __forceinline__ real compton(const Scene<real> &s, Photon<real> &ph, Rng &g, BlockCounters *bc) {
+  real eps, onecost, sint2;
+  compton_kn(ph.e, g, bc, eps, onecost, sint2);
+  return compton_finish(s, ph, g, eps, onecost, sint2);
+}
+
+// The rejection loop of the Rayleigh sampling (form-factor inversion, then
+// the 1 + cos^2 acceptance): cos(theta) of the scattering.
+template <typename real>
+__device__ __forceinline__ real rayleigh_cost(const Scene<real> &s, int comp, const Photon<real> &ph, Rng &g,
+                                              BlockCounters *bc) {
   real k = ph.e * R<real>(1.0 / kHcMevAngstrom);
   real x2max = k * k;
   real amax = interp_row(s.ray_amax + (size_t)comp * s.n_e, ph.ei);
@@ -216,12 +235,29 @@ __device__ __forceinline__ void rayleigh(const Scene<real> &s, int comp, Photon<
     rhs = R<real>(1) + rhs;
     if (lhs <= rhs) break;
   }
+  return cost;
+}
+
+template <typename real>
+__device__ __forceinline__ real rayleigh_sint2(real cost) {
   real st2 = cost * cost;
-  st2 = R<real>(1) - st2;
+  return R<real>(1) - st2;
+}
+
+// The rest of a Rayleigh scattering of cosine cost: azimuth (one draw) and new direction.
+template <typename real>
+__device__ __forceinline__ void rayleigh_finish(Photon<real> &ph, Rng &g, real cost) {
+  const real st2 = rayleigh_sint2(cost);
   real sint = gg_sqrt(st2 > R<real>(0) ? st2 : R<real>(0));
   real sp, cp;
   gg_sincos_turn(u01<real>(g), sp, cp);
   rotate_dir(ph.dir[0], ph.dir[1], ph.dir[2], cost, sint, cp, sp);
+}
+
+template <typename real>
+__device__ __forceinline__ void rayleigh(const Scene<real> &s, int comp, Photon<real> &ph, Rng &g,
+                                         BlockCounters *bc) {
+  rayleigh_finish(ph, g, rayleigh_cost(s, comp, ph, g, bc));
 }
 
 template <typename real>

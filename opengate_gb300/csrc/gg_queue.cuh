@@ -62,14 +62,15 @@ size_t queue_bytes(size_t cap) {
 
 // Split requests of scatter splitting (phantom stage -> split kernel), SoA:
 // the photon before the interaction (position, direction, energy, weight),
-// its history, the stream offset of its first copy and the composition of
-// the material (Rayleigh form factors).
+// its history, the stream offset of its first copy, the composition of the
+// material (Rayleigh form factors) and the history's gantry position.
 template <typename real>
 struct SplitQueue {
   unsigned long long *hid;
   real *px, *py, *pz, *dx, *dy, *dz, *e, *w;
   uint32_t *base;
   int32_t *comp;
+  int32_t *run;  // gantry position of the history
 
   __device__ __forceinline__ static SplitQueue carve(void *b, size_t cap) {
     SplitQueue q;
@@ -84,13 +85,15 @@ struct SplitQueue {
     q.base = reinterpret_cast<uint32_t *>(p);
     p += cap * sizeof(uint32_t);
     q.comp = reinterpret_cast<int32_t *>(p);
+    p += cap * sizeof(int32_t);
+    q.run = reinterpret_cast<int32_t *>(p);
     return q;
   }
 };
 
 template <typename real>
 size_t split_bytes(size_t cap) {
-  return cap * (sizeof(unsigned long long) + 8 * sizeof(real) + 2 * sizeof(uint32_t));
+  return cap * (sizeof(unsigned long long) + 8 * sizeof(real) + 3 * sizeof(uint32_t));
 }
 
 constexpr uint32_t kMetaSteps = (1u << 20) - 1u;

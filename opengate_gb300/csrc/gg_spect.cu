@@ -154,6 +154,42 @@ __device__ __forceinline__ void stage_counters(unsigned long long *cnt, const Bl
   }
 }
 
+// Whether a photon of direction d scattered by theta (cos, sin^2) can pass the
+// angle check of some head (ff_target): over the azimuth, the largest cosine
+// between the new direction and a head axis u is cos(theta - theta_u) =
+// cos(theta) (d.u) + sin(theta) sqrt(1 - (d.u)^2).  A margin of 1e-4 on the
+// cosine keeps every direction the full check would accept (rounding is far
+// below it), so dropping the others changes no result.
+template <typename real>
+__device__ __forceinline__ bool cone_reachable(const Scene<real> &s, int run, const real d[3], real cost, real sint2,
+                                               real cos_min) {
+  const real sint = gg_sqrt(sint2 > R<real>(0) ? sint2 : R<real>(0));
+  const real lim = cos_min - R<real>(1e-4);
+  for (int h = 0; h < s.n_heads; ++h) {
+    const HeadFrame<real> f = head_frame(s, run, h);
+    const real c0 = dot3(d, f.u);
+    real s0 = R<real>(1) - c0 * c0;
+    s0 = gg_sqrt(s0 > R<real>(0) ? s0 : R<real>(0));
+    real m = cost * c0;
+    m = m + sint * s0;
+    if (!(m < lim)) return true;
+  }
+  return false;
+}
+
+// Copies of one warp that passed the scattering-angle test and wait for the
+// rest of their scattering and the head checks, kSplitPend at most: the copy
+// index, the sampled (eps, 1 - cos, sin^2) of a Compton or (cos, -, -) of a
+// Rayleigh scattering, and the copy's stream after its rejection loop.
+constexpr int kSplitPend = 64;
+template <typename real>
+struct SplitPending {
+  uint4 rb[kSplitPend];
+  uint64_t i[kSplitPend];
+  real a[kSplitPend], b[kSplitPend], c[kSplitPend];
+  uint32_t rpos[kSplitPend];
+};
+
 // Scatter splitting, the copies (GateScatterSplittingFreeFlightOptn.cpp:69-149):
 // one thread per copy.  Request r of the phantom stage holds the photon
 // before a Compton (or Rayleigh) interaction; its copy c re-samples that
@@ -167,10 +203,17 @@ __device__ __forceinline__ void stage_counters(unsigned long long *cnt, const Bl
 // buffer from the front and Rayleigh requests from the back; when together
 // they overflowed it, nothing is done (the host repeats the pass on fewer
 // histories).
+// Most copies scatter away from every head: right after the rejection loop
+// the scattering angle alone decides that (cone_reachable), and only the
+// others draw their azimuth and meet the full check.  Those wait in a
+// per-warp buffer until 32 of them fill the warp's lanes, so the azimuth,
+// the rotation and the head checks run on full warps; each copy's arithmetic
+// and draws are those of the plain sequence.
 template <typename real>
 __global__ void __launch_bounds__(256) k_spect_split(Scene<real> sg, KernelArgs args, StageArgs q) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ BlockCounters bc;
+  __shared__ SplitPending<real> pend_all[kBlock / 32];
   Scene<real> s = sg;
   stage_tables(sg, s, smem_raw, bc);
   const uint64_t n_c = *q.split_n, n_r = q.split_n[1];
@@ -181,41 +224,58 @@ __global__ void __launch_bounds__(256) k_spect_split(Scene<real> sg, KernelArgs 
   const PQueue<real> out = PQueue<real>::carve(q.out_q, q.q_cap);
   const unsigned lane = threadIdx.x & 31u;
   const unsigned lt_mask = (1u << lane) - 1u;
+  SplitPending<real> &P = pend_all[threadIdx.x >> 5];
+  int np = 0;  // copies waiting in P (the same in every lane of the warp)
   unsigned int n_world = 0;
-  // the loop bound is the same for all threads of a block: queue claims stay warp-collective
-  for (uint64_t i0 = (uint64_t)blockIdx.x * blockDim.x; i0 < total; i0 += (uint64_t)gridDim.x * blockDim.x) {
-    const uint64_t i = i0 + threadIdx.x;
+  // copy i: its request, the photon before the interaction, its stream
+  auto load_copy = [&](uint64_t i, Photon<real> &cp, Rng &gc, uint64_t &hid) {
+    uint64_t r;
+    uint32_t c, n;
+    if (i < all_c) {
+      r = i / per_c;
+      c = (uint32_t)(i - r * per_c);
+      n = (uint32_t)per_c;
+    } else {
+      const uint64_t j = i - all_c, rr = j / per_r;
+      c = (uint32_t)(j - rr * per_r);
+      r = (uint64_t)q.split_cap - 1 - rr;
+      n = (uint32_t)per_r;
+    }
+    hid = sq.hid[r];
+    cp.pos[0] = sq.px[r];
+    cp.pos[1] = sq.py[r];
+    cp.pos[2] = sq.pz[r];
+    cp.dir[0] = sq.dx[r];
+    cp.dir[1] = sq.dy[r];
+    cp.dir[2] = sq.dz[r];
+    cp.e = sq.e[r];  // the energy-grid state only where a sampling uses it (set_energy)
+    cp.w = sq.w[r] / (real)n;
+    cp.alive = 1;
+    cp.run = sq.run[r];
+    gc.init(args.seed, hid, 2u + sq.base[r] + c);
+    return r;
+  };
+  // the waiting copies P[k0 + lane] (lane < cnt): the rest of the scattering,
+  // the head checks, and the walk queue (every lane of the warp calls it)
+  auto finish = [&](int k0, int cnt) {
     Photon<real> cp;
     Rng gc;
     uint64_t hid = 0;
     bool push = false;
-    if (i < total) {
-      uint64_t r;
-      uint32_t c, n;
-      if (i < all_c) {
-        r = i / per_c;
-        c = (uint32_t)(i - r * per_c);
-        n = (uint32_t)per_c;
-      } else {
-        const uint64_t j = i - all_c, rr = j / per_r;
-        c = (uint32_t)(j - rr * per_r);
-        r = (uint64_t)q.split_cap - 1 - rr;
-        n = (uint32_t)per_r;
-      }
-      hid = sq.hid[r];
-      cp.pos[0] = sq.px[r];
-      cp.pos[1] = sq.py[r];
-      cp.pos[2] = sq.pz[r];
-      cp.dir[0] = sq.dx[r];
-      cp.dir[1] = sq.dy[r];
-      cp.dir[2] = sq.dz[r];
-      set_energy(s, cp, sq.e[r]);
-      cp.w = sq.w[r] / (real)n;
-      cp.alive = 1;
-      cp.run = run_of(s, hid);
-      gc.init(args.seed, hid, 2u + sq.base[r] + c);
-      if (i < all_c) compton(s, cp, gc, &bc);
-      else rayleigh(s, sq.comp[r], cp, gc, &bc);
+    if ((int)lane < cnt) {
+      const int k = k0 + (int)lane;
+      const uint64_t i = P.i[k];
+      load_copy(i, cp, gc, hid);
+      const uint32_t rp = P.rpos[k];
+      const uint4 b = P.rb[k];
+      gc.blk = rp >> 3;
+      gc.idx = (int)(rp & 7u);
+      gc.buf[0] = b.x;
+      gc.buf[1] = b.y;
+      gc.buf[2] = b.z;
+      gc.buf[3] = b.w;
+      if (i < all_c) compton_finish(s, cp, gc, P.a[k], P.b[k], P.c[k]);
+      else rayleigh_finish(cp, gc, P.a[k]);
       if (cp.alive) {
         cp.exclude = -1;
         cp.steps = 0;
@@ -227,12 +287,58 @@ __global__ void __launch_bounds__(256) k_spect_split(Scene<real> sg, KernelArgs 
         if (!push) atomicAdd(&bc.escaped, 1u);
       }
     }
-    const size_t k = queue_claim(q.out_n, push, lane, lt_mask);
-    if (push && k < q.q_cap) {
+    const size_t kq = queue_claim(q.out_n, push, lane, lt_mask);
+    if (push && kq < q.q_cap) {
       real v[kEvSlots];
-      queue_put<real, true>(out, k, cp, gc, hid, v, false);
+      queue_put<real, true>(out, kq, cp, gc, hid, v, false);
+    }
+  };
+  // the loop bound is the same for all threads of a block: queue claims stay warp-collective
+  for (uint64_t i0 = (uint64_t)blockIdx.x * blockDim.x; i0 < total; i0 += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t i = i0 + threadIdx.x;
+    bool wait = false;
+    real a = R<real>(0), b = R<real>(0), c = R<real>(0);
+    Rng gc;
+    if (i < total) {
+      Photon<real> cp;
+      uint64_t hid;
+      const uint64_t r = load_copy(i, cp, gc, hid);
+      bool dead = false, out_of_cone;
+      if (i < all_c) {
+        compton_kn(cp.e, gc, &bc, a, b, c);
+        // (below the energy cut the copy dies in compton_finish)
+        dead = a * cp.e < s.e_min;
+        out_of_cone = !dead && s.ss_cos > R<real>(-1) && !cone_reachable(s, cp.run, cp.dir, R<real>(1) - b, c, s.ss_cos);
+      } else {
+        set_energy(s, cp, cp.e);
+        a = rayleigh_cost(s, sq.comp[r], cp, gc, &bc);
+        out_of_cone = s.ss_cos > R<real>(-1) && !cone_reachable(s, cp.run, cp.dir, a, rayleigh_sint2(a), s.ss_cos);
+      }
+      if (out_of_cone) {  // a live copy that fails the head checks, as counted there
+        ++n_world;
+        atomicAdd(&bc.escaped, 1u);
+      }
+      wait = !dead && !out_of_cone;
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, wait);
+    if (wait) {
+      const int k = np + __popc(m & lt_mask);
+      P.i[k] = i;
+      P.a[k] = a;
+      P.b[k] = b;
+      P.c[k] = c;
+      P.rpos[k] = (gc.blk << 3) | (uint32_t)gc.idx;
+      P.rb[k] = make_uint4(gc.buf[0], gc.buf[1], gc.buf[2], gc.buf[3]);
+    }
+    np += __popc(m);
+    __syncwarp();
+    if (np >= 32) {
+      finish(np - 32, 32);
+      np -= 32;
+      __syncwarp();
     }
   }
+  if (np > 0) finish(0, np);
   stage_counters(args.counters, bc, lane, 0u, 0u, n_world, 0u, 0u);
 }
 
@@ -453,6 +559,7 @@ __global__ void __launch_bounds__(256, MINB) k_spect_phantom(Scene<real> sg, Ker
             sq.w[k] = pre.w;
             sq.base[k] = nsplit;
             sq.comp[k] = s.mat_comp[pmat];
+            sq.run[k] = ph.run;
           }
           nsplit += (uint32_t)n;
         }
