@@ -180,14 +180,13 @@ __device__ __forceinline__ bool cone_reachable(const Scene<real> &s, int run, co
 // Copies of one warp that passed the scattering-angle test and wait for the
 // rest of their scattering and the head checks, kSplitPend at most: the copy
 // index, the sampled (eps, 1 - cos, sin^2) of a Compton or (cos, -, -) of a
-// Rayleigh scattering, and the copy's stream after its rejection loop.
+// Rayleigh scattering, and the words of the copy's stream drawn so far.
 constexpr int kSplitPend = 64;
 template <typename real>
 struct SplitPending {
-  uint4 rb[kSplitPend];
   uint64_t i[kSplitPend];
   real a[kSplitPend], b[kSplitPend], c[kSplitPend];
-  uint32_t rpos[kSplitPend];
+  uint32_t words[kSplitPend];
 };
 
 // Scatter splitting, the copies (GateScatterSplittingFreeFlightOptn.cpp:69-149):
@@ -266,14 +265,20 @@ __global__ void __launch_bounds__(256) k_spect_split(Scene<real> sg, KernelArgs 
       const int k = k0 + (int)lane;
       const uint64_t i = P.i[k];
       load_copy(i, cp, gc, hid);
-      const uint32_t rp = P.rpos[k];
-      const uint4 b = P.rb[k];
-      gc.blk = rp >> 3;
-      gc.idx = (int)(rp & 7u);
-      gc.buf[0] = b.x;
-      gc.buf[1] = b.y;
-      gc.buf[2] = b.z;
-      gc.buf[3] = b.w;
+      // the stream after its first `w` words: the state an Rng reaches by drawing them
+      const uint32_t w = P.words[k];
+      if ((w & 3u) == 0u) {
+        gc.blk = w >> 2;
+        gc.idx = 4;
+      } else {
+        const uint4 b = philox_block(w >> 2, gc.stream, gc.h0, gc.h1, gc.k0, gc.k1);
+        gc.buf[0] = b.x;
+        gc.buf[1] = b.y;
+        gc.buf[2] = b.z;
+        gc.buf[3] = b.w;
+        gc.blk = (w >> 2) + 1u;
+        gc.idx = (int)(w & 3u);
+      }
       if (i < all_c) compton_finish(s, cp, gc, P.a[k], P.b[k], P.c[k]);
       else rayleigh_finish(cp, gc, P.a[k]);
       if (cp.alive) {
@@ -327,8 +332,7 @@ __global__ void __launch_bounds__(256) k_spect_split(Scene<real> sg, KernelArgs 
       P.a[k] = a;
       P.b[k] = b;
       P.c[k] = c;
-      P.rpos[k] = (gc.blk << 3) | (uint32_t)gc.idx;
-      P.rb[k] = make_uint4(gc.buf[0], gc.buf[1], gc.buf[2], gc.buf[3]);
+      P.words[k] = (gc.blk - 1u) * 4u + (uint32_t)gc.idx;  // (the loops drew at least one word)
     }
     np += __popc(m);
     __syncwarp();
