@@ -79,6 +79,7 @@ ARF_DECAYS = 10_000_000_000
 ARF_YIELD = 0.166
 ARF_WINDOWS = ((0.1872, 0.2288), (0.166, 0.187), (0.1017, 0.1243))
 ARF_TRAIN_SAMPLES = 200_000_000
+ARF_TRAIN_THETA_DEG = 85.0  # training photons on the detector face: incidence angle uniform up to this
 ARF_PRIMARY_DEG = 10.0  # primary pass: angle tolerance of the source's angular acceptance
 ARF_SPLIT = (10, 2, 10000, 10.0)  # scatter pass: Compton, Rayleigh factors, max Compton level, angle tolerance
 ARF_SCATTER_SHARE = 8  # the scatter pass runs 1 / 8 of the primaries
@@ -716,8 +717,8 @@ class ArfRecipe:
         batch = min(batch, 1 << 26)
         self.plain = SpectEngine(self.scene, self.sp, device=local, precision=32, batch=batch)
         net = ArfNetwork(self.plain)
-        # training rows: plain head transport of photons on the face, theta uniform to 85 degrees
-        smp = ArfNetwork.sampling(min(lo for lo, _ in ARF_WINDOWS), 0.21, 85.0, (200.0, 200.0), 40.0)
+        # training rows: plain head transport of photons on the face, theta uniform to ARF_TRAIN_THETA_DEG
+        smp = ArfNetwork.sampling(min(lo for lo, _ in ARF_WINDOWS), 0.21, ARF_TRAIN_THETA_DEG, (200.0, 200.0), 40.0)
         t0 = time.perf_counter()
         self.model, self.loss = net.train(smp, train_samples, seed=seed + 7, epochs=epochs, batch=8192, lr=2e-3,
                                           lr_final=1e-5)
