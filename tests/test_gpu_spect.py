@@ -204,6 +204,31 @@ def test_scatter_splitting_bit_exact(precision):
     assert w.sum() > 0 and w.max() < 1.0
 
 
+@pytest.mark.parametrize("angle", [0.35, 0.0])
+def test_scatter_splitting_one_head_bit_exact(angle):
+    """One head, more Compton copies per request than a warp has lanes: the copies'
+    scattering-angle test and head checks run over a single head axis, and the copies that
+    can still reach it wait and are finished on full warps; with the angle check (0.35 rad)
+    and without it (every live copy goes through the full check), weighted projections,
+    squares and counters equal the oracle's."""
+    scene, sp, _ = _case("tc99m_lehr", n_runs=2)
+    sp.n_heads = 1
+    sp.set_scatter_splitting(40, 6, 3, angle_tolerance_max=angle)
+    n = 40_000
+    from opengate_gb300.engine import SpectEngine
+
+    with SpectEngine(scene, sp, precision=32) as eng:
+        eng.run(n, 29)
+        w, w2 = eng.weighted_projection(squared=True)
+        cnt = eng.counters()
+    assert w.shape[0] == 1
+    rw, rw2, rcnt = O.run_spect_ff(scene, sp, n, seed=29, threads=8, precision=32)
+    np.testing.assert_array_equal(w, rw)
+    np.testing.assert_array_equal(w2, rw2)
+    assert cnt == rcnt
+    assert w.sum() > 0
+
+
 def test_scatter_splitting_queue_overflow_repeats_the_pass():
     """Many copies per history and short batches: the head queue overflows, the phantom
     pass is repeated on fewer histories, and the result stays the oracle's, bit for bit
