@@ -279,6 +279,10 @@ int gg_destroy(gg_ctx *ctx);
    ctx is NULL) into buf, always NUL-terminated. */
 int gg_last_error(const gg_ctx *ctx, char *buf, size_t len);
 
+/* The tables stay in each transport block's shared memory beside its two
+   per-history voxel lists: sizeof(real) * (n_comp * n_e + n_e + n_mat) +
+   4 * n_mat bytes (16-byte aligned) plus 2 * 8 * 256 * (4 + sizeof(real))
+   must not exceed 200 KiB (GG_ERR_ARG otherwise). */
 int gg_upload_tables(gg_ctx *ctx, const gg_tables_desc *tables);
 int gg_upload_volume(gg_ctx *ctx, const gg_volume_desc *volume);
 int gg_set_world(gg_ctx *ctx, const gg_world_desc *world);
