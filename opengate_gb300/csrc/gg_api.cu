@@ -1257,8 +1257,13 @@ static int run_impl(gg_ctx *c, uint64_t n, uint64_t seed, uint64_t first, bool c
                                   : ((c->precision == GG_PREC_F64 || c->have_batch) ? 2 : (tle_run ? 3 : 4));
   int bps = 0;
   {
-    cudaError_t e = c->precision == GG_PREC_F64 ? gg::occupancy_blocks<double>(c->block, smem, minb, &bps)
-                                                : gg::occupancy_blocks<float>(c->block, smem, minb, &bps);
+    // (occupancy_blocks counts one voxel list per thread; a dose grid scoring dose keeps two)
+    const bool two_lists = c->dgrid_on && c->ddose && !c->have_spect && !c->have_batch;
+    const size_t smem_occ = smem + (two_lists ? (c->precision == GG_PREC_F64 ? gg::hist_list_bytes<double>(1, c->block)
+                                                                             : gg::hist_list_bytes<float>(1, c->block))
+                                              : 0);
+    cudaError_t e = c->precision == GG_PREC_F64 ? gg::occupancy_blocks<double>(c->block, smem_occ, minb, &bps)
+                                                : gg::occupancy_blocks<float>(c->block, smem_occ, minb, &bps);
     if (e != cudaSuccess) return c->cuda(e, "occupancy");
     if (bps < 1) bps = 1;
   }
