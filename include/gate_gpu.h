@@ -463,6 +463,32 @@ int gg_spect_set_heads(gg_ctx *ctx, int32_t run, const double *frames);
 int gg_spect_run(gg_ctx *ctx, uint64_t n_per_run, uint64_t seed, uint64_t first, const double *frames);
 int gg_get_projection(gg_ctx *ctx, double *out, size_t n);
 
+/* Singles list (replaces the "Singles" digi collection of DigitizerAdderActor
+   and its ROOT ntuple: GateDigiCollection::FillToRoot,
+   core/opengate_core/opengate_lib/digitizer/GateDigiCollection.cpp:114-128,
+   written by GateDigiCollectionsRootManager; opengate/actors/digitizers.py:
+   300-420).  gg_spect_record_singles(ctx, capacity) keeps, from the next
+   gg_spect_run on, one gg_single per head single of the tracked heads (after
+   the adder and the blurring, before the windows and the projection pixel
+   test; network-scored ARF photons make no singles, as in the reference),
+   in a device list of `capacity` records (0: off, the default).  Records are
+   appended in completion order, not history order.  gg_spect_get_singles
+   copies min(recorded, capacity, out_capacity) records to `out`, sets
+   *n_recorded to all singles recorded since the list was last read or set
+   (more than the list's capacity when it overflowed: those beyond were
+   dropped) and empties the list.  Positions are the crystal-plane
+   coordinates (a1, a2) of the head frame of gg_spect_set_heads, mm. */
+typedef struct {
+  uint64_t event_id; /* history index (the copies of scatter splitting keep their history's) */
+  int32_t head;
+  int32_t run;       /* gantry position */
+  double energy;     /* MeV, after energy blurring */
+  double a1, a2;     /* mm, along the head frame's e1 / e2, after spatial blurring */
+  double weight;     /* free-flight weight (1 without free flight) */
+} gg_single;
+int gg_spect_record_singles(gg_ctx *ctx, uint64_t capacity);
+int gg_spect_get_singles(gg_ctx *ctx, gg_single *out, uint64_t out_capacity, uint64_t *n_recorded);
+
 /* ---- ARF surrogate ---------------------------------------------------------
    gg_arf_dataset replaces the ARF training-dataset simulation
    (GateARFTrainingDatasetActor, core/opengate_core/opengate_lib/

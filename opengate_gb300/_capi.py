@@ -206,6 +206,12 @@ def ptr(arr, ctype):
     return arr.ctypes.data_as(ctypes.POINTER(ctype))
 
 
+# gg_single (include/gate_gpu.h): one record of the singles list
+SINGLE_DTYPE = np.dtype([("event_id", np.uint64), ("head", np.int32), ("run", np.int32), ("energy", np.float64),
+                         ("a1", np.float64), ("a2", np.float64), ("weight", np.float64)], align=True)
+assert SINGLE_DTYPE.itemsize == 48
+
+
 # Exported symbols and their prototypes: (name, restype, argtypes)
 PROTOTYPES = [
     ("gg_create", ctypes.c_int, [ctypes.POINTER(DeviceOpts), ctypes.POINTER(ctypes.c_void_p)]),
@@ -236,6 +242,9 @@ PROTOTYPES = [
     ("gg_spect_set_heads", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, _f64p]),
     ("gg_spect_run", ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64, _f64p]),
     ("gg_get_projection", ctypes.c_int, [ctypes.c_void_p, _f64p, ctypes.c_size_t]),
+    ("gg_spect_record_singles", ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64]),
+    ("gg_spect_get_singles", ctypes.c_int,
+     [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint64)]),
     ("gg_arf_train", ctypes.c_int,
      [ctypes.c_void_p, ctypes.POINTER(ArfSampling), ctypes.POINTER(ArfTrainOpts), ctypes.POINTER(ArfModel), _f64p]),
     ("gg_arf_train_rows", ctypes.c_int,

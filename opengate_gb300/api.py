@@ -649,6 +649,9 @@ class ARFActor(GateObject):
 
 FWHM_TO_SIGMA = 1.0 / (2.0 * math.sqrt(2.0 * math.log(2.0)))
 
+# singles kept on the device between two reads when a digitizer module writes its singles (48 B each)
+SINGLES_LIST_CAPACITY = 1 << 22
+
 
 class DigitizerAdderActor(GateObject):
     """Singles of a head crystal from its hits (DigitizerAdderActor; GateDigiAdderInVolume,
@@ -658,7 +661,8 @@ class DigitizerAdderActor(GateObject):
     type_name = "DigitizerAdderActor"
     user_info_defaults = {"attached_to": None, "input_digi_collection": "Hits", "policy": "EnergyWinnerPosition",
                           "time_difference": False, "number_of_hits": False, "group_volume": None,
-                          "skip_attributes": [], "clear_every": 1e5, "output_filename": "auto", "priority": 100}
+                          "skip_attributes": [], "clear_every": 1e5, "output_filename": "auto", "priority": 100,
+                          "write_to_disk": True}
 
     def adder_policy(self):
         if self.policy not in C.ADDER_POLICIES:
@@ -678,7 +682,7 @@ class DigitizerBlurringActor(GateObject):
     user_info_defaults = {"attached_to": None, "input_digi_collection": "Hits", "blur_attribute": None,
                           "skip_attributes": [], "clear_every": 1e5, "blur_method": "Gaussian", "blur_sigma": None,
                           "blur_fwhm": None, "blur_reference_value": 0, "blur_resolution": 0, "blur_slope": 0,
-                          "output_filename": "auto", "priority": 100}
+                          "output_filename": "auto", "priority": 100, "write_to_disk": True}
 
     def energy_blur(self):
         """Keyword arguments of SpectSpec.set_energy_blur (MeV), validated as the reference does."""
@@ -713,7 +717,7 @@ class DigitizerSpatialBlurringActor(GateObject):
     user_info_defaults = {"attached_to": None, "attributes": [], "input_digi_collection": "Hits",
                           "skip_attributes": [], "clear_every": int(1e5), "blur_attribute": None, "blur_fwhm": None,
                           "blur_sigma": None, "keep_in_solid_limits": True, "use_truncated_Gaussian": True,
-                          "output_filename": "auto", "priority": 100}
+                          "output_filename": "auto", "priority": 100, "write_to_disk": True}
 
     def spatial_blur(self):
         """Keyword arguments of SpectSpec.set_spatial_blur (mm)."""
@@ -1080,8 +1084,12 @@ class Simulation:
         # a forced-direction source stands for one source copy per head: n_heads histories per event
         plan = [[k * sp.n_heads for k in p] if spec.dir_type == C.GG_DIR_FORCED else p
                 for p, (_, spec) in zip(plan, sources)]
+        writers = self._singles_writers(head_of) if sp.arf is None else {}
         eng = SpectEngine(scene, sp, device=self.device, precision=self.precision, batch=self.batch)
+        singles = []
         try:
+            if writers:
+                eng.record_singles(SINGLES_LIST_CAPACITY)
             if sp.arf is not None:
                 from .engine import ArfNetwork
 
@@ -1094,9 +1102,15 @@ class Simulation:
                 for k, (src, spec) in enumerate(sources):
                     if len(sources) > 1 or k:
                         eng.set_source(spec)
-                    if plan[k][r]:
-                        eng._call("gg_run", C.ctypes.c_uint64(plan[k][r]), C.ctypes.c_uint64(seed),
-                                  C.ctypes.c_uint64(first))
+                    # with a singles list, runs of at most capacity / n_heads histories (one single per
+                    # head and history, scatter-split copies aside), each list read after its run
+                    step = max(1, SINGLES_LIST_CAPACITY // sp.n_heads) if writers else max(plan[k][r], 1)
+                    for a in range(0, plan[k][r], step):
+                        m = min(step, plan[k][r] - a)
+                        eng._call("gg_run", C.ctypes.c_uint64(m), C.ctypes.c_uint64(seed),
+                                  C.ctypes.c_uint64(first + a))
+                        if writers:
+                            singles.append(eng.singles())
                     first += plan[k][r]
             if sp.arf is not None:
                 # ARF detectors: network window weights plus the counts of the photons tracked instead
@@ -1113,6 +1127,18 @@ class Simulation:
         finally:
             eng.close()
         elapsed = time.perf_counter() - t0
+        if writers:
+            from . import root_io
+
+            rec = np.concatenate(singles) if singles else np.zeros(0, dtype=C.SINGLE_DTYPE)
+            # completion order is not reproducible: sort by history, head, then the values
+            rec = rec[np.lexsort((rec["weight"], rec["a2"], rec["a1"], rec["energy"], rec["head"], rec["event_id"]))]
+            for h, a in writers.items():
+                path = pathlib.Path(self.output_dir) / (a.output_filename if a.output_filename not in
+                                                        (None, "", "auto") else f"{a.name}.root")
+                path.parent.mkdir(parents=True, exist_ok=True)
+                root_io.write_tree(path, a.name, sp.singles_columns(rec[rec["head"] == h]))
+                object.__setattr__(a, "singles", rec[rec["head"] == h])
         for a in projs:
             h = head_of[a.attached_to]
             sx, sy = spacing
@@ -1139,6 +1165,17 @@ class Simulation:
                 a.counts.pps = int(first / elapsed) if elapsed > 0 else 0
                 a.counts.sps = int(a.counts.steps / elapsed) if elapsed > 0 else 0
         return cnt
+
+    def _singles_writers(self, head_of):
+        """{head index: actor} of the digitizer module whose singles collection goes to disk: the
+        last of the chain adder -> energy blurring -> spatial blurring on each head crystal, as
+        the GPU path applies them (the intermediate collections are not kept)."""
+        last = {}
+        for kind in (DigitizerAdderActor, DigitizerBlurringActor, DigitizerSpatialBlurringActor):
+            for a in self.actors.values():
+                if isinstance(a, kind) and a.attached_to in head_of:
+                    last[head_of[a.attached_to]] = a
+        return {h: a for h, a in last.items() if a.write_to_disk}
 
     def _arf_theta_max(self, actor, plane, source):
         """Largest angle (degrees) between the plane normal and a line from the source's disc to

@@ -9,6 +9,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdarg>
+#include <cstddef>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -116,6 +117,10 @@ struct gg_ctx {
   // run bookkeeping
   unsigned long long *d_counters = nullptr, *d_next = nullptr;
   unsigned int *d_status = nullptr;
+  // singles list (gg_spect_record_singles): records and their count (0 capacity: off)
+  gg::SingleRec *d_singles = nullptr;
+  unsigned long long *d_n_singles = nullptr;
+  uint64_t singles_cap = 0;
   void *d_records = nullptr;
   size_t rec_cap = 0;
   // SPECT stage queues (head queue, return queue) and their lengths
@@ -253,6 +258,8 @@ struct gg_ctx {
     dfree(d_params); dfree(d_adam_m); dfree(d_adam_v); dfree(d_grad); dfree(d_partial); dfree(d_loss_part);
     dfree(d_loss_acc); dfree(d_wbf); dfree(d_io_rows); dfree(d_io_out);
     dfree(d_sims); dfree(d_sim_maj);
+    dfree(d_singles); dfree(d_n_singles);
+    singles_cap = 0;
     if (graph_exec) cudaGraphExecDestroy(graph_exec);
     if (graph) cudaGraphDestroy(graph);
     graph_exec = nullptr;
@@ -432,6 +439,11 @@ struct gg_ctx {
         s.inv_psp[a] = (real)(1.0 / sp.spacing[a]);
       }
       s.proj = d_proj;
+      if (singles_cap) {
+        s.singles = d_singles;
+        s.n_singles_rec = d_n_singles;
+        s.singles_cap = singles_cap;
+      }
     }
     return s;
   }
@@ -1628,6 +1640,43 @@ int gg_spect_run(gg_ctx *c, uint64_t n_per_run, uint64_t seed, uint64_t first, c
   int st = upload_frames(c);
   if (st) return st;
   return run_impl(c, n, seed, first);
+}
+
+static_assert(sizeof(gg_single) == sizeof(gg::SingleRec) && offsetof(gg_single, energy) == offsetof(gg::SingleRec, energy) &&
+                  offsetof(gg_single, weight) == offsetof(gg::SingleRec, weight),
+              "gg_single and the device record must share their layout");
+
+int gg_spect_record_singles(gg_ctx *c, uint64_t capacity) {
+  if (!c) return GG_ERR_ARG;
+  cudaSetDevice(c->device);
+  if (capacity > (1ull << 40) / sizeof(gg_single))
+    return c->fail(GG_ERR_ARG, "gg_spect_record_singles: capacity above 2^40 bytes of records");
+  int st;
+  if (capacity != c->singles_cap) {
+    dfree(c->d_singles);
+    c->singles_cap = 0;
+    if (capacity &&
+        (st = c->cuda(cudaMalloc(&c->d_singles, capacity * sizeof(gg_single)), "cudaMalloc singles list")))
+      return st;
+  }
+  if (!c->d_n_singles && (st = c->cuda(cudaMalloc(&c->d_n_singles, 8), "cudaMalloc singles count"))) return st;
+  if ((st = c->cuda(cudaMemsetAsync(c->d_n_singles, 0, 8, c->stream), "clear singles count"))) return st;
+  c->singles_cap = capacity;
+  return c->cuda(cudaStreamSynchronize(c->stream), "singles list");
+}
+
+int gg_spect_get_singles(gg_ctx *c, gg_single *out, uint64_t out_capacity, uint64_t *n_recorded) {
+  if (!c || !n_recorded || (out_capacity && !out)) return GG_ERR_ARG;
+  cudaSetDevice(c->device);
+  if (!c->singles_cap) return c->fail(GG_ERR_STATE, "gg_spect_get_singles: no singles list (gg_spect_record_singles)");
+  unsigned long long n = 0;
+  int st;
+  if ((st = c->d2h(&n, c->d_n_singles, 8, "singles count"))) return st;
+  *n_recorded = n;
+  const uint64_t m = std::min<uint64_t>(std::min<uint64_t>(n, c->singles_cap), out_capacity);
+  if (m && (st = c->d2h(out, c->d_singles, m * sizeof(gg_single), "download singles"))) return st;
+  if ((st = c->cuda(cudaMemsetAsync(c->d_n_singles, 0, 8, c->stream), "clear singles count"))) return st;
+  return c->cuda(cudaStreamSynchronize(c->stream), "singles list");
 }
 
 int gg_arf_dataset(gg_ctx *c, const gg_arf_sampling *a, uint64_t n, uint64_t seed, uint64_t first, float *rows,

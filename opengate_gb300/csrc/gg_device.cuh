@@ -425,6 +425,13 @@ struct SimDesc {
 };
 
 // ---------------------------------------------------------------------------
+// One single of the singles list (the C ABI's gg_single, same layout)
+struct SingleRec {
+  uint64_t event_id;
+  int32_t head, run;
+  double energy, a1, a2, weight;
+};
+
 template <typename real>
 struct Scene {
   // tables
@@ -497,6 +504,10 @@ struct Scene {
   real ss_cos;               // copies entering a head with a local dir z below this are dropped (-2: off)
   unsigned long long *wproj, *wproj2;
   real eb_sigma, eb_res, eb_ref, eb_slope, sb_sigma[2];
+  // singles list (null: off): records appended at slot atomicAdd(n_singles_rec),
+  // kept while the slot is below singles_cap
+  SingleRec *singles;
+  unsigned long long *n_singles_rec, singles_cap;
 };
 
 template <typename real>

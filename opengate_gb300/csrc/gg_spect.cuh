@@ -627,6 +627,20 @@ __device__ __forceinline__ unsigned score_singles(const Scene<real> &s, const Ev
     }
     if (s.eblur) e = blur_energy(s, e, g);
     if (s.sblur) blur_position(s, a1, a2, g);
+    if (s.singles) {
+      const unsigned long long slot = atomicAdd(s.n_singles_rec, 1ull);
+      if (slot < s.singles_cap) {
+        SingleRec r;
+        r.event_id = (uint64_t)g.h0 | ((uint64_t)g.h1 << 32);
+        r.head = h;
+        r.run = run;
+        r.energy = (double)e;
+        r.a1 = (double)a1;
+        r.a2 = (double)a2;
+        r.weight = s.ff ? (double)ev.w[h] : 1.0;
+        s.singles[slot] = r;
+      }
+    }
     real fx = a1 + s.pix_half[0];
     fx = fx * s.inv_psp[0];
     real fy = a2 + s.pix_half[1];

@@ -247,6 +247,25 @@ class SpectEngine(DoseEngine):
         self._call("gg_get_arf_projection", C.ptr(out, ctypes.c_double), C.ptr(sq, ctypes.c_double), n)
         return (out.reshape(shape), sq.reshape(shape)) if squared else out.reshape(shape)
 
+    def record_singles(self, capacity):
+        """Keep the singles of the following runs in a device list of `capacity` records
+        (0: off); see singles()."""
+        self._call("gg_spect_record_singles", ctypes.c_uint64(int(capacity)))
+        self._singles_cap = int(capacity)
+
+    def singles(self):
+        """The singles recorded since the last call (C.SINGLE_DTYPE records, completion order),
+        then an empty list.  Raises if the list overflowed: its records would be a biased subset."""
+        cap = getattr(self, "_singles_cap", 0)
+        out = np.zeros(cap, dtype=C.SINGLE_DTYPE)
+        n = ctypes.c_uint64()
+        self._call("gg_spect_get_singles", out.ctypes.data_as(ctypes.c_void_p), ctypes.c_uint64(cap),
+                   ctypes.byref(n))
+        if n.value > cap:
+            raise RuntimeError(f"singles list overflow: {n.value} singles, capacity {cap} "
+                               "(record_singles with a larger capacity)")
+        return out[:n.value]
+
     def projection(self, out=None):
         """Counts (head, run * window, y, x); into `out` when given (e.g. pinned_empty)."""
         shape = self.spect.projection_shape()

@@ -222,6 +222,25 @@ class SpectSpec:
             out[h] = np.concatenate([self.radius * u, u, e1, [0.0, 0.0, 1.0]])
         return out
 
+    def crystal_depth(self):
+        """Depth of the crystal's mid-plane behind the collimator front face (mm)."""
+        return (self.collimator_thickness + self.gap + (self.cover[0] if self.cover else 0.0) +
+                0.5 * self.crystal_thickness)
+
+    def singles_columns(self, singles):
+        """Columns of a singles list (C.SINGLE_DTYPE records) under the reference's digi
+        attribute names (one column per value; PostPosition split into _X/_Y/_Z, mm, world
+        frame, on the crystal's mid-plane of the record's head and gantry position)."""
+        frames = self.all_frames()  # [run][head][12]
+        f = frames[singles["run"], singles["head"]] if len(singles) else np.zeros((0, 12))
+        pos = (f[:, 0:3] + self.crystal_depth() * f[:, 3:6] + singles["a1"][:, None] * f[:, 6:9]
+               + singles["a2"][:, None] * f[:, 9:12])
+        return {"EventID": singles["event_id"].astype(np.int64), "RunID": singles["run"].astype(np.int32),
+                "HeadID": singles["head"].astype(np.int32),
+                "TotalEnergyDeposit": singles["energy"].astype(np.float64),
+                "PostPosition_X": pos[:, 0].copy(), "PostPosition_Y": pos[:, 1].copy(),
+                "PostPosition_Z": pos[:, 2].copy(), "Weight": singles["weight"].astype(np.float64)}
+
     def all_frames(self):
         return np.ascontiguousarray(np.stack([self.frames(r) for r in range(self.n_runs)]))
 

@@ -1590,6 +1590,20 @@ static void blur_position(const scene_t *s, real *a1, real *a2, rng_t *g) {
   *a2 = p1;
 }
 
+/* singles list of the following SPECT runs (set_singles; the C ABI's
+   gg_spect_record_singles): one gg_single per single at slot
+   fetch_add(g_singles_n), kept below g_singles_cap */
+static gg_single *g_singles;
+static uint64_t g_singles_cap, g_singles_n;
+
+void GGO_PREFIX(set_singles)(gg_single *buf, uint64_t cap) {
+  g_singles = buf;
+  g_singles_cap = buf ? cap : 0;
+  g_singles_n = 0;
+}
+
+uint64_t GGO_PREFIX(singles_count)(void) { return g_singles_n; }
+
 /* singles of one event: (blurring: head 0 before head 1, energy before
    position, from the history's stream,) windows and projection pixel */
 static void score_singles(const scene_t *s, const event_t *ev, tally_t *t, rng_t *g) {
@@ -1604,6 +1618,19 @@ static void score_singles(const scene_t *s, const event_t *ev, tally_t *t, rng_t
     }
     if (s->eblur) e = blur_energy(s, e, g);
     if (s->sblur) blur_position(s, &a1, &a2, g);
+    if (g_singles) {
+      const uint64_t slot = __atomic_fetch_add(&g_singles_n, 1, __ATOMIC_RELAXED);
+      if (slot < g_singles_cap) {
+        gg_single *r = &g_singles[slot];
+        r->event_id = (uint64_t)g->ctr[2] | ((uint64_t)g->ctr[3] << 32);
+        r->head = h;
+        r->run = s->run;
+        r->energy = (double)e;
+        r->a1 = (double)a1;
+        r->a2 = (double)a2;
+        r->weight = s->ff ? (double)ev->w[h] : 1.0;
+      }
+    }
     real fx = a1 + s->pix_half[0];
     fx = fx * s->inv_psp[0];
     real fy = a2 + s->pix_half[1];

@@ -193,6 +193,26 @@ def _with_blur(L, precision, spect, call):
         f(None)
 
 
+def with_singles(precision, capacity, call):
+    """Runs call() with a singles list of `capacity` records installed in the oracle:
+    (call's result, C.SINGLE_DTYPE records in completion order).  Raises on overflow."""
+    L = lib(precision)
+    f = getattr(L, f"ggo{precision}_set_singles")
+    f.argtypes = [ctypes.c_void_p, ctypes.c_uint64]
+    count = getattr(L, f"ggo{precision}_singles_count")
+    count.restype = ctypes.c_uint64
+    buf = np.zeros(int(capacity), dtype=C.SINGLE_DTYPE)
+    f(buf.ctypes.data_as(ctypes.c_void_p), int(capacity))
+    try:
+        res = call()
+        n = int(count())
+    finally:
+        f(None, 0)
+    if n > capacity:
+        raise RuntimeError(f"oracle singles list overflow: {n} > {capacity}")
+    return res, buf[:n]
+
+
 def sample_blur(blur, half_w, e, a1, a2, n, seed=1, precision=32):
     """n blurred singles of one event: (energies, a1, a2) float64 arrays."""
     L = lib(precision)
