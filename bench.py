@@ -368,6 +368,9 @@ def run_ours_spect(args, ws, rank, local, dist, use_cuda):
     n = n_per_run * sp.n_runs
     eng = SpectEngine(scene, sp, device=local, precision=32, batch=args.batch)
     l2_flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=f"cuda:{local}")
+    if args.record_singles:  # the digitizer's singles list, read back after every step
+        eng.record_singles(args.record_singles)
+    n_singles = []
 
     def first_of(step):
         return ((rank * (args.warmup + args.steps + 4)) + step) * n
@@ -375,6 +378,8 @@ def run_ours_spect(args, ws, rank, local, dist, use_cuda):
     for w in range(args.warmup):
         eng.reset()
         eng.run(n_per_run, args.seed, first_of(w))
+        if args.record_singles:
+            eng.singles()
     torch.cuda.synchronize()
     if dist:
         dist.barrier()
@@ -389,6 +394,8 @@ def run_ours_spect(args, ws, rank, local, dist, use_cuda):
             tg, tt, tf, nl = eng.last_kernel_ms()
             dev_ms.append(tg + tt + tf)
             launches += nl
+            if args.record_singles:
+                n_singles.append(len(eng.singles()))
             if k == args.steps - 1:
                 counters = eng.counters()
                 transport_ms = tt
@@ -430,7 +437,8 @@ def run_ours_spect(args, ws, rank, local, dist, use_cuda):
                 "kernel": "k_spect_phantom<float> (phantom stage)",
                 "bytes_alg_per_step": bytes_alg,
                 "units": {"woodcock_steps": counters["woodcock_steps"], "head_steps": counters["head_steps"],
-                          "singles": counters["singles"], "launches_per_step": launches_last},
+                          "singles": counters["singles"], "launches_per_step": launches_last,
+                          "singles_listed": n_singles[-1] if n_singles else None},
                 "stage_ms_per_step": stage_ms}
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:
@@ -1571,6 +1579,8 @@ def main():
     ap.add_argument("--arf-scatter-share", type=int, default=ARF_SCATTER_SHARE,
                     help="spect_arf: the scatter pass runs 1 / share of the primaries")
     ap.add_argument("--batch", type=int, default=1 << 27)
+    ap.add_argument("--record-singles", type=int, default=0,
+                    help="spect: keep the singles in a device list of this many records, read every step")
     ap.add_argument("--seed", type=int, default=20240611)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--transport-kernel", default="phased", choices=["phased", "wavefront"],
